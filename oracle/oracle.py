@@ -1,0 +1,319 @@
+"""Python driver for the CPU oracle (test infrastructure only).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` leg of
+``bench.py`` import this module.  It loads ``oracle/_build/libmcxoracle.so``
+(the plain-C restatement, ``mcx_oracle.c``) and, when it was built here from
+the reference sources, ``oracle/_ref/libmcxref.so`` (the reference kernel
+itself compiled on the host).
+
+``cfg`` dictionaries use the ``pmcxcl.run()`` keys of the reference Python
+module (src/pmcxcl.cpp:428-1110); unspecified keys take the defaults of
+``mcx_initcfg`` (src/mcx_utils.c:203-366).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmcxoracle.so")
+REF_PATH = os.environ.get("MCXO_REF_PATH", os.path.join(HERE, "_ref", "libmcxref.so"))
+
+MATH_LIBM, MATH_PMATH = 0, 1
+VARIANT_OPENCL, VARIANT_NVCC = 0, 1
+FIELD_FLOAT_SPILL, FIELD_DOUBLE = 0, 1
+
+SRCTYPES = ["pencil", "isotropic", "cone", "gaussian", "planar", "pattern", "fourier", "arcsine", "disk",
+            "fourierx", "fourierx2d", "zgaussian", "line", "slit", "pencilarray", "pattern3d", "hyperboloid",
+            "ring"]
+OUTPUTTYPES = {"flux": 0, "fluence": 1, "energy": 2, "length": 7}
+SAVEFLAGS = "DSPMXVWI"
+
+
+class MCXOInput(ctypes.Structure):
+    _fields_ = [
+        ("dimx", ctypes.c_uint), ("dimy", ctypes.c_uint), ("dimz", ctypes.c_uint),
+        ("vol", ctypes.c_void_p), ("mediabyte", ctypes.c_int), ("prop", ctypes.c_void_p),
+        ("medianum", ctypes.c_uint), ("unitinmm", ctypes.c_float),
+        ("srctype", ctypes.c_int), ("srcpos", ctypes.c_float * 4), ("srcdir", ctypes.c_float * 4),
+        ("srcparam1", ctypes.c_float * 4), ("srcparam2", ctypes.c_float * 4),
+        ("srcpattern", ctypes.c_void_p), ("srcnum", ctypes.c_uint), ("extrasrclen", ctypes.c_uint),
+        ("srcdata", ctypes.c_void_p), ("srcid", ctypes.c_int),
+        ("detpos", ctypes.c_void_p), ("detnum", ctypes.c_uint), ("maxdetphoton", ctypes.c_uint),
+        ("issavedet", ctypes.c_int), ("savedetflag", ctypes.c_uint), ("issaveseed", ctypes.c_int),
+        ("issaveref", ctypes.c_int), ("issaveexit", ctypes.c_int), ("ismomentum", ctypes.c_int),
+        ("tstart", ctypes.c_float), ("tstep", ctypes.c_float), ("tend", ctypes.c_float),
+        ("isreflect", ctypes.c_int), ("bc", ctypes.c_char * 12), ("minenergy", ctypes.c_float),
+        ("gscatter", ctypes.c_uint), ("voidtime", ctypes.c_int), ("isspecular", ctypes.c_int),
+        ("maxvoidstep", ctypes.c_int), ("outputtype", ctypes.c_int), ("isnormalized", ctypes.c_int),
+        ("issrcfrom0", ctypes.c_int), ("invcdf", ctypes.c_void_p), ("nphase", ctypes.c_uint),
+        ("angleinvcdf", ctypes.c_void_p), ("nangle", ctypes.c_uint),
+        ("nphoton", ctypes.c_double), ("nthread", ctypes.c_uint), ("core", ctypes.c_uint),
+        ("seed", ctypes.c_int), ("debugrng", ctypes.c_int),
+        ("mathmode", ctypes.c_int), ("variant", ctypes.c_int), ("fieldmode", ctypes.c_int),
+        ("nworkers", ctypes.c_int),
+    ]
+
+
+class MCXOStats(ctypes.Structure):
+    _fields_ = [
+        ("energytot", ctypes.c_double), ("energyesc", ctypes.c_double), ("energyabs", ctypes.c_double),
+        ("normalizer", ctypes.c_double), ("detected", ctypes.c_uint), ("saved", ctypes.c_uint),
+        ("threadphoton", ctypes.c_uint), ("oddphoton", ctypes.c_int), ("reclen", ctypes.c_uint),
+        ("fieldlen", ctypes.c_uint), ("maxgate", ctypes.c_uint),
+        ("nstep", ctypes.c_uint64), ("nscatter", ctypes.c_uint64), ("nlaunch", ctypes.c_uint64),
+        ("nreflect", ctypes.c_uint64), ("nfailed", ctypes.c_uint64),
+    ]
+
+
+_lib = None
+_ref = None
+
+
+def build(ref=None):
+    """Compile the oracle (and, when the reference sources exist, the reference harness)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    refdir = ref or os.environ.get("MCX_REFERENCE", "/root/reference")
+    if os.path.isfile(os.path.join(refdir, "src", "mcx_core.cl")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + refdir], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.mcxo_run.restype = ctypes.c_int
+        _lib.mcxo_reclen.restype = ctypes.c_uint
+        _lib.mcxo_fieldlen.restype = ctypes.c_uint
+        _lib.mcxo_pm_logf.restype = ctypes.c_float
+        _lib.mcxo_pm_logf.argtypes = [ctypes.c_float]
+        _lib.mcxo_pm_expf.restype = ctypes.c_float
+        _lib.mcxo_pm_expf.argtypes = [ctypes.c_float]
+        _lib.mcxo_pm_acosf.restype = ctypes.c_float
+        _lib.mcxo_pm_acosf.argtypes = [ctypes.c_float]
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(REF_PATH)
+
+
+def reflib():
+    global _ref
+    if _ref is None:
+        _ref = ctypes.CDLL(REF_PATH)
+        _ref.mcxref_run.restype = ctypes.c_int
+    return _ref
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _rows(v, ncol=4):
+    a = np.asarray(v, dtype=np.float32)
+    if a.ndim == 1:
+        a = a.reshape(1, -1)
+    out = np.zeros((a.shape[0], ncol), dtype=np.float32)
+    out[:, :a.shape[1]] = a
+    return out
+
+
+def _flags(s, letters):
+    if isinstance(s, (int, np.integer)):
+        return int(s)
+    v = 0
+    for ch in str(s).upper():
+        if ch in letters:
+            v |= 1 << letters.index(ch)
+    return v
+
+
+def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL,
+               fieldmode=FIELD_DOUBLE, nworkers=0):
+    """Translate a pmcxcl-style dict into the oracle's input struct.
+
+    Returns (struct, keepalive) -- keepalive holds the numpy buffers."""
+    keep = {}
+    inp = MCXOInput()
+    vol = np.asarray(cfg["vol"])
+    if vol.dtype == np.float32 and vol.ndim == 4 and vol.shape[0] == 1:
+        words = np.asfortranarray(vol[0]).view(np.uint32)
+        inp.mediabyte = 101
+        dims = vol.shape[1:]
+    else:
+        words = np.asfortranarray(vol).astype(np.uint32)
+        inp.mediabyte = {1: 1, 2: 2, 4: 4}.get(np.dtype(vol.dtype).itemsize, 4)
+        dims = vol.shape
+    words = np.ascontiguousarray(words.reshape(-1, order="F"))
+    keep["vol"] = words
+    inp.dimx, inp.dimy, inp.dimz = [int(d) for d in dims]
+    inp.vol = _ptr(words)
+    prop = np.ascontiguousarray(_rows(cfg["prop"]))
+    keep["prop"] = prop
+    inp.prop = _ptr(prop)
+    inp.medianum = prop.shape[0]
+    inp.unitinmm = float(cfg.get("unitinmm", 1.0))
+
+    st = cfg.get("srctype", "pencil")
+    inp.srctype = SRCTYPES.index(st) if isinstance(st, str) else int(st)
+    srcpos = _rows(cfg.get("srcpos", [0, 0, 0]))
+    if srcpos.shape[0] == 1 and np.asarray(cfg.get("srcpos", [0, 0, 0])).size == 3:
+        srcpos[0, 3] = 1.0
+    srcdir = _rows(cfg.get("srcdir", [0, 0, 1]))
+    p1 = _rows(cfg.get("srcparam1", [0, 0, 0, 0]))
+    p2 = _rows(cfg.get("srcparam2", [0, 0, 0, 0]))
+    n_src = max(srcpos.shape[0], srcdir.shape[0], p1.shape[0], p2.shape[0])
+
+    def row(a, i):
+        return a[i] if i < a.shape[0] else np.zeros(4, np.float32)
+    for k, a in (("srcpos", srcpos), ("srcdir", srcdir), ("srcparam1", p1), ("srcparam2", p2)):
+        getattr(inp, k)[:] = [float(x) for x in a[0]]
+    inp.extrasrclen = n_src - 1
+    if n_src > 1:
+        sd = np.zeros((n_src - 1, 16), np.float32)
+        for i in range(1, n_src):
+            if srcpos.shape[0] > i and np.asarray(cfg["srcpos"]).shape[1] == 3:
+                srcpos[i, 3] = 1.0
+            sd[i - 1] = np.concatenate([row(srcpos, i), row(srcdir, i), row(p1, i), row(p2, i)])
+        keep["srcdata"] = sd
+        inp.srcdata = _ptr(sd)
+    inp.srcid = int(cfg.get("srcid", 0))
+    if "srcpattern" in cfg:
+        pat = np.ascontiguousarray(np.asarray(cfg["srcpattern"], np.float32).reshape(-1, order="F"))
+        keep["srcpattern"] = pat
+        inp.srcpattern = _ptr(pat)
+    inp.srcnum = int(cfg.get("srcnum", 1))
+
+    if "detpos" in cfg and np.asarray(cfg["detpos"]).size:
+        det = np.ascontiguousarray(_rows(cfg["detpos"]))
+        keep["det"] = det
+        inp.detpos = _ptr(det)
+        inp.detnum = det.shape[0]
+    inp.maxdetphoton = int(cfg.get("maxdetphoton", 1000000))
+    inp.issavedet = int(cfg.get("issavedet", 1))
+    inp.savedetflag = _flags(cfg.get("savedetflag", 0x5), SAVEFLAGS)
+    inp.issaveseed = int(bool(cfg.get("issaveseed", 0)))
+    inp.issaveref = int(cfg.get("issaveref", 0))
+    inp.issaveexit = int(bool(cfg.get("issaveexit", 0)))
+    inp.ismomentum = int(bool(cfg.get("ismomentum", 0)))
+    inp.tstart = float(cfg.get("tstart", 0.0))
+    inp.tend = float(cfg.get("tend", 5e-9))
+    inp.tstep = float(cfg.get("tstep", 5e-9))
+    inp.isreflect = int(cfg.get("isreflect", 1))
+    bc = str(cfg.get("bc", "")).encode()[:12]
+    inp.bc = bc + b"\0" * (12 - len(bc))
+    inp.minenergy = float(cfg.get("minenergy", 0.0))
+    inp.gscatter = int(cfg.get("gscatter", 1000000000))
+    inp.voidtime = int(cfg.get("voidtime", 1))
+    inp.isspecular = int(bool(cfg.get("isspecular", 0)))
+    inp.maxvoidstep = int(cfg.get("maxvoidstep", 1000))
+    ot = cfg.get("outputtype", "flux")
+    inp.outputtype = OUTPUTTYPES[ot] if isinstance(ot, str) else int(ot)
+    inp.isnormalized = int(cfg.get("isnormalized", 1))
+    inp.issrcfrom0 = int(cfg.get("issrcfrom0", 0))
+    if "invcdf" in cfg:
+        cdf = np.ascontiguousarray(np.asarray(cfg["invcdf"], np.float32).ravel())
+        keep["invcdf"] = cdf
+        inp.invcdf = _ptr(cdf)
+        inp.nphase = cdf.size
+    if "angleinvcdf" in cfg:
+        acdf = np.ascontiguousarray(np.asarray(cfg["angleinvcdf"], np.float32).ravel())
+        keep["angleinvcdf"] = acdf
+        inp.angleinvcdf = _ptr(acdf)
+        inp.nangle = acdf.size
+    inp.nphoton = float(cfg["nphoton"])
+    inp.nthread = int(nthread)
+    inp.core = int(core if core is not None else nthread)
+    inp.seed = int(cfg.get("seed", 0x623F9A9E))
+    inp.debugrng = int("R" in str(cfg.get("debuglevel", "")).upper())
+    inp.mathmode = mathmode
+    inp.variant = variant
+    inp.fieldmode = fieldmode
+    inp.nworkers = nworkers
+    return inp, keep
+
+
+def run(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL, fieldmode=FIELD_DOUBLE,
+        nworkers=0):
+    """Run the oracle.  Returns a dict with the merged raw field (float64,
+    Fortran-ordered [x, y, z, gate]), the normalised field, per-thread energies,
+    detected-photon records, seeds, stats and event counters."""
+    inp, keep = make_input(cfg, nthread, core, mathmode, variant, fieldmode, nworkers)
+    L = lib()
+    fieldlen = L.mcxo_fieldlen(ctypes.byref(inp))
+    reclen = L.mcxo_reclen(ctypes.byref(inp))
+    field = np.zeros(fieldlen, np.float64)
+    fnorm = np.zeros(fieldlen, np.float32)
+    energy = np.zeros(2 * inp.nthread, np.float32)
+    maxdet = inp.maxdetphoton
+    detp = np.zeros(max(1, maxdet * max(reclen, 1)), np.float32)
+    seeds = np.zeros(max(2, maxdet * 2), np.uint64)
+    masked = np.zeros(inp.dimx * inp.dimy * inp.dimz, np.uint32)
+    st = MCXOStats()
+    rc = L.mcxo_run(ctypes.byref(inp), _ptr(field), _ptr(fnorm), _ptr(energy), _ptr(detp), _ptr(seeds),
+                    _ptr(masked), ctypes.byref(st))
+    if rc:
+        raise RuntimeError("oracle failed with code %d" % rc)
+    gates = st.maxgate
+    shape = (inp.dimx, inp.dimy, inp.dimz, -1)
+    nsaved = st.saved
+    out = {
+        "field_raw": field.reshape(shape, order="F"),
+        "flux": fnorm.reshape(shape, order="F"),
+        "energy": energy.reshape(-1, 2),
+        "detp": detp[:nsaved * reclen].reshape(nsaved, reclen).T if reclen else np.zeros((0, 0), np.float32),
+        "seeds": seeds[:2 * nsaved].reshape(nsaved, 2) if inp.issaveseed else None,
+        "masked": masked.reshape(inp.dimx, inp.dimy, inp.dimz, order="F"),
+        "stat": {k: getattr(st, k) for k, _ in MCXOStats._fields_},
+        "gates": gates,
+    }
+    return out
+
+
+def run_reference(cfg, nthread=4096, core=None, nblocksize=64, nworkers=1):
+    """Run the reference kernel compiled on the host (serial when nworkers == 1).
+    Returns the merged raw float field, per-thread energies, records, seeds."""
+    inp, keep = make_input(cfg, nthread, core, MATH_LIBM, VARIANT_NVCC, FIELD_FLOAT_SPILL, 1)
+    L = lib()
+    R = reflib()
+    fieldlen = L.mcxo_fieldlen(ctypes.byref(inp))
+    reclen = L.mcxo_reclen(ctypes.byref(inp))
+    field = np.zeros(fieldlen, np.float32)
+    energy = np.zeros(2 * inp.nthread, np.float32)
+    maxdet = inp.maxdetphoton
+    detp = np.zeros(max(1, maxdet * max(reclen, 1)), np.float32)
+    seeds = np.zeros(max(2, maxdet * 2), np.uint64)
+    cnt = ctypes.c_uint(0)
+    rc = R.mcxref_run(ctypes.byref(inp), ctypes.c_uint(nblocksize), ctypes.c_int(nworkers), _ptr(field),
+                      _ptr(energy), _ptr(detp), _ptr(seeds), ctypes.byref(cnt))
+    if rc:
+        raise RuntimeError("reference harness failed with code %d" % rc)
+    nsaved = min(cnt.value, maxdet)
+    shape = (inp.dimx, inp.dimy, inp.dimz, -1)
+    return {
+        "field_raw": field.reshape(shape, order="F"),
+        "energy": energy.reshape(-1, 2),
+        "detp": detp[:nsaved * reclen].reshape(nsaved, reclen).T if reclen else np.zeros((0, 0), np.float32),
+        "seeds": seeds[:2 * nsaved].reshape(nsaved, 2) if inp.issaveseed else None,
+        "detected": cnt.value,
+    }
+
+
+def cube60(**kw):
+    """The reference's cube60 benchmark input (src/mcx_bench.h:33-85, pmcxcl/bench.py)."""
+    cfg = {
+        "nphoton": 1000000,
+        "vol": np.ones((60, 60, 60), dtype=np.uint8),
+        "tstart": 0, "tend": 5e-9, "tstep": 5e-9,
+        "srcpos": [29, 29, 0], "srcdir": [0, 0, 1],
+        "prop": [[0, 0, 1, 1], [0.005, 1, 0.01, 1.37], [0.002, 5, 0.9, 1]],
+        "isreflect": 0, "seed": 1648335518,
+        "detpos": [[29, 19, 0, 1], [29, 39, 0, 1], [19, 29, 0, 1], [39, 29, 0, 1]],
+        "issrcfrom0": 1,
+    }
+    cfg.update(kw)
+    return cfg

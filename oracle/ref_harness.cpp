@@ -1,0 +1,166 @@
+/*
+ * ref_harness.cpp -- runs the reference photon-transport kernel
+ * (src/mcx_core.cl, compiled in place as host C++ through ref_shim.hpp) on
+ * the CPU with the same prepared inputs as the oracle.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Built by oracle/Makefile into oracle/_ref/ only
+ * when the reference sources are present; never committed, never shipped.
+ *
+ * Threads are run block by block, thread by thread, in global-index order,
+ * exactly one reference thread at a time, so the deposits happen in the same
+ * order as the oracle's serial mode and the outputs compare bit for bit.
+ */
+#include "ref_shim.hpp"
+#include "mcx_core.cl"
+
+#include "mcx_oracle.h"
+
+#include <vector>
+
+template <int ispencil, int isreflect>
+static void run_blocks(const mcxo_refprep& R, unsigned int nblock, unsigned int bsize, unsigned int* media,
+                       float* field, float* genergy, unsigned int* seeds, float* detp, unsigned int* detcount,
+                       float* gprop, float* gdet, RandType* gseed, float* srcpattern, const float* invcdf,
+                       unsigned int nphase, const float* angleinvcdf, unsigned int nangle, int nworkers) {
+    (void)nworkers;
+    for (long b = 0; b < (long)nblock; b++) {
+        unsigned int progress = 0;
+        blockIdx = make_uint3((unsigned int)b, 0, 0);
+        blockDim = make_uint3(bsize, 1, 1);
+        gridDim = make_uint3(nblock, 1, 1);
+        /* the kernel's table preload (mcx_core.cl:2354-2383) splits the copy
+           across the block's threads and synchronises; run one thread at a
+           time, the block's tables are filled up front instead */
+        if (invcdf) {
+            std::memcpy(sharedmem_raw, invcdf, sizeof(float) * nphase);
+        }
+        if (angleinvcdf) {
+            std::memcpy(sharedmem_raw + sizeof(float) * (nphase + (nphase & 1)), angleinvcdf, sizeof(float) * nangle);
+        }
+        for (unsigned int t = 0; t < bsize; t++) {
+            threadIdx = make_uint3(t, 0, 0);
+            mcx_main_loop<ispencil, isreflect, 1, 0, 0>(
+                media, field, genergy, seeds, detp, (const float4*)gprop, srcpattern, (const float4*)gdet,
+                &progress, detcount, nullptr, nullptr, nullptr, gseed, nullptr, nullptr, (float*)invcdf, (float*)angleinvcdf,
+                (RandType*)sharedmem_raw, nullptr);
+        }
+    }
+}
+
+extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nworkers, float* field_out,
+                          float* energy_out, float* detp_out, uint64_t* seeds_out, unsigned int* detcount_out) {
+    mcxo_refprep R;
+    int rc = mcxo_prepare_ref(in, &R);
+    if (rc) {
+        return rc;
+    }
+    if (in->nthread % nblocksize) {
+        mcxo_free_ref(&R);
+        return -10;
+    }
+    if (in->mediabyte > 4) {
+        mcxo_free_ref(&R);
+        return -11;      /* the __NVCC__ launch path garbles prop.y/z for MEDIA_MUA_FLOAT (mcx_core.cl:2214-2231) */
+    }
+    MCXParam& P = gcfg_const[0];
+    std::memset(&P, 0, sizeof(P));
+    std::memcpy(&P.src.pos, R.srcpos, 16);
+    std::memcpy(&P.src.dir, R.srcdir, 16);
+    std::memcpy(&P.src.param1, R.srcparam1, 16);
+    std::memcpy(&P.src.param2, R.srcparam2, 16);
+    P.extrasrclen = R.extrasrclen;
+    P.srcid = R.srcid;
+    std::memcpy(&P.maxidx, R.maxidx, 16);
+    std::memcpy(&P.dimlen, R.dimlen, 16);
+    P.minstep = 1.f;
+    P.twin0 = R.twin0;
+    P.twin1 = R.twin1;
+    P.tmax = in->tend;
+    P.oneoverc0 = R.oneoverc0;
+    P.save2pt = R.save2pt;
+    P.doreflect = R.doreflect;
+    P.savedet = R.savedet;
+    P.Rtstep = R.Rtstep;
+    P.minenergy = R.minenergy;
+    P.minaccumtime = R.minaccumtime;
+    P.maxdetphoton = R.maxdetphoton;
+    P.maxmedia = R.maxmedia;
+    P.detnum = R.detnum;
+    P.voidtime = (int)R.voidtime;
+    P.srctype = (int)R.srctype;
+    P.maxvoidstep = R.maxvoidstep;
+    P.issaveseed = R.issaveseed;
+    P.issaveref = R.issaveref;
+    P.isspecular = R.isspecular;
+    P.maxgate = R.maxgate;
+    P.seed = in->seed;
+    P.outputtype = R.outputtype;
+    P.threadphoton = R.threadphoton;
+    P.oddphoton = R.oddphoton;
+    P.savedetflag = R.savedetflag;
+    P.reclen = R.reclen;
+    P.partialdata = R.partialdata;
+    P.w0offset = R.w0offset;
+    P.mediaformat = R.mediaformat;
+    P.gscatter = R.gscatter;
+    P.is2d = R.is2d;
+    P.srcnum = R.srcnum;
+    P.nphase = R.nphase;
+    P.nphaselen = R.nphase + (R.nphase & 1);
+    P.nangle = R.nangle;
+    P.nanglelen = R.nangle + (R.nangle & 1);
+    std::memcpy(P.bc, R.bc, 12);
+
+    unsigned int nblock = in->nthread / nblocksize;
+    /* the __NVCC__ launch path reads media[idx + nvox] (updateproperty_asgn),
+       so the volume is padded with a zero second half */
+    std::vector<unsigned int> media(2 * (size_t)R.nvox, 0u);
+    std::memcpy(media.data(), R.media, sizeof(unsigned int) * R.nvox);
+    std::vector<float> field(2 * (size_t)R.fieldlen, 0.f);
+    std::vector<float> genergy(2 * (size_t)in->nthread, 0.f);
+    std::vector<unsigned int> seeds(R.seedwords, R.seedwords + 4 * (size_t)in->nthread);
+    size_t reclen = R.reclen ? R.reclen : 1;
+    std::vector<float> detp((size_t)R.maxdetphoton * reclen + 1, 0.f);
+    std::vector<RandType> gseed((size_t)R.maxdetphoton * 2 + 2, 0);
+    unsigned int detcount = 0;
+    std::vector<float> gprop(R.gprop, R.gprop + 4 * (size_t)R.nprop);
+    std::vector<float> gdet(4 * (size_t)(R.detnum + 1), 0.f);
+    if (R.detnum) {
+        std::memcpy(gdet.data(), R.gdet, sizeof(float) * 4 * R.detnum);
+    }
+
+    int ispencil = (in->srctype == MCX_SRC_PENCIL);
+    int isreflect = R.dorefl_compiled;
+#define RUN(a, b) run_blocks<a, b>(R, nblock, nblocksize, media.data(), field.data(), genergy.data(), seeds.data(), \
+                                   detp.data(), &detcount, gprop.data(), gdet.data(), gseed.data(), (float*)in->srcpattern, \
+                                   in->invcdf, in->nphase, in->angleinvcdf, in->nangle, nworkers)
+    if (ispencil && isreflect) {
+        RUN(1, 1);
+    } else if (ispencil) {
+        RUN(1, 0);
+    } else if (isreflect) {
+        RUN(0, 1);
+    } else {
+        RUN(0, 0);
+    }
+#undef RUN
+
+    for (size_t i = 0; i < R.fieldlen; i++) {
+        field_out[i] = field[i] + field[i + R.fieldlen];
+    }
+    if (energy_out) {
+        std::memcpy(energy_out, genergy.data(), sizeof(float) * 2 * in->nthread);
+    }
+    unsigned int saved = detcount < R.maxdetphoton ? detcount : R.maxdetphoton;
+    if (detp_out && R.reclen) {
+        std::memcpy(detp_out, detp.data(), sizeof(float) * saved * R.reclen);
+    }
+    if (seeds_out && R.issaveseed) {
+        std::memcpy(seeds_out, gseed.data(), sizeof(uint64_t) * 2 * saved);
+    }
+    if (detcount_out) {
+        *detcount_out = detcount;
+    }
+    mcxo_free_ref(&R);
+    return 0;
+}

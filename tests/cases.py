@@ -1,0 +1,132 @@
+"""Named simulation inputs shared by the tests and the golden-fixture script.
+
+Every case is a ``pmcxcl.run()``-style dict (the reference Python module's
+keys, src/pmcxcl.cpp:428-1110).  Volumes are built procedurally so fixtures
+only need to store results, not inputs.
+"""
+import numpy as np
+
+
+def cube60(**kw):
+    """The reference's built-in cube60 benchmark (src/mcx_bench.h:33-85)."""
+    cfg = {
+        "nphoton": 1000000,
+        "vol": np.ones((60, 60, 60), dtype=np.uint8),
+        "tstart": 0, "tend": 5e-9, "tstep": 5e-9,
+        "srcpos": [29, 29, 0], "srcdir": [0, 0, 1],
+        "prop": [[0, 0, 1, 1], [0.005, 1, 0.01, 1.37], [0.002, 5, 0.9, 1]],
+        "isreflect": 0, "seed": 1648335518,
+        "detpos": [[29, 19, 0, 1], [29, 39, 0, 1], [19, 29, 0, 1], [39, 29, 0, 1]],
+        "issrcfrom0": 1,
+    }
+    cfg.update(kw)
+    return cfg
+
+
+def sphere_volume(n=60, center=(30, 30, 30), radius=15, inner=2, outer=1):
+    """A cube of label `outer` with a sphere of label `inner`; a voxel is inside
+    when its centre is (the rule of mcx_raster_sphere, src/mcx_shapes.c:234-293)."""
+    idx = np.arange(n, dtype=np.float64) + 0.5
+    x, y, z = np.meshgrid(idx, idx, idx, indexing="ij")
+    d2 = (x - center[0]) ** 2 + (y - center[1]) ** 2 + (z - center[2]) ** 2
+    vol = np.full((n, n, n), outer, dtype=np.uint8)
+    vol[d2 < radius * radius] = inner
+    return vol
+
+
+def cubesph60(**kw):
+    """60^3 cube with a radius-15 sphere of label 2, Fresnel on, 50 gates of
+    0.1 ns and four disk detectors on the z=0 face: the two-medium benchmark
+    (BASELINE config 2; src/mcx_bench.h:200-252 is the 1-gate original)."""
+    cfg = cube60(
+        vol=sphere_volume(),
+        prop=[[0, 0, 1, 1], [0.005, 1.0, 0.01, 1.37], [0.002, 5.0, 0.9, 1.0]],
+        isreflect=1, tstep=1e-10, nphoton=100000000,
+        detpos=[[30, 20, 0, 1], [30, 40, 0, 1], [20, 30, 0, 1], [40, 30, 0, 1]],
+        savedetflag="dsp", issaveseed=1,
+    )
+    cfg.update(kw)
+    return cfg
+
+
+def small_two_media(**kw):
+    """40^3 cube with a 20^3 inner block of a second medium; the workhorse of
+    the bit-exact pins."""
+    vol = np.ones((40, 40, 40), np.uint8)
+    vol[10:30, 10:30, 10:30] = 2
+    cfg = dict(nphoton=2000, vol=vol, prop=[[0, 0, 1, 1], [0.01, 1, 0.5, 1.37], [0.02, 5, 0.9, 1.45]],
+               srcpos=[20, 20, 0], srcdir=[0, 0, 1], issrcfrom0=1, seed=12345, tstart=0, tend=5e-9,
+               tstep=2.5e-10, isreflect=1, detpos=[[20, 10, 0, 2], [10, 20, 0, 2]], savedetflag="dspmxvw",
+               issaveseed=1)
+    cfg.update(kw)
+    return cfg
+
+
+def _pattern(n, seed):
+    return np.random.RandomState(seed).rand(*n).astype(np.float32)
+
+
+# Variants of small_two_media covering each source type and boundary feature.
+VARIANTS = {
+    "pencil_gates": {},
+    "isotropic": dict(srctype="isotropic", srcpos=[20, 20, 20]),
+    "cone": dict(srctype="cone", srcparam1=[0.5, 0, 0, 0]),
+    "gaussian": dict(srctype="gaussian", srcparam1=[3, 0, 0, 0]),
+    "planar": dict(srctype="planar", srcpos=[5, 5, -5], srcparam1=[30, 0, 0, 0], srcparam2=[0, 30, 0, 0]),
+    "fourier": dict(srctype="fourier", srcpos=[5, 5, 0], srcparam1=[30, 0, 0, 2], srcparam2=[0, 30, 0, 1]),
+    "arcsine": dict(srctype="arcsine", srcpos=[20, 20, 20]),
+    "disk": dict(srctype="disk", srcparam1=[5, 0, 0, 0]),
+    "fourierx": dict(srctype="fourierx", srcpos=[5, 5, 0], srcparam1=[30, 0, 0, 30], srcparam2=[1, 2, 0.5, 0.5]),
+    "fourierx2d": dict(srctype="fourierx2d", srcpos=[5, 5, 0], srcparam1=[30, 0, 0, 30],
+                       srcparam2=[1, 2, 0.5, 0.5]),
+    "zgaussian": dict(srctype="zgaussian", srcparam1=[0.3, 0, 0, 0]),
+    "line": dict(srctype="line", srcpos=[10, 20, 20], srcparam1=[20, 0, 0, 0]),
+    "slit": dict(srctype="slit", srcpos=[10, 20, 0], srcparam1=[20, 0, 0, 0]),
+    "pencilarray": dict(srctype="pencilarray", srcpos=[5, 5, 0], srcparam1=[30, 0, 0, 4],
+                        srcparam2=[0, 30, 0, 3]),
+    "hyperboloid": dict(srctype="hyperboloid", srcparam1=[2, 10, 5, 0]),
+    "ring": dict(srctype="ring", srcparam1=[5, 2, 0, 0]),
+    "pattern": dict(srctype="pattern", srcpos=[5, 5, 0], srcparam1=[30, 0, 0, 4], srcparam2=[0, 30, 0, 4],
+                    srcpattern=_pattern((4, 4), 1)),
+    "pattern3d": dict(srctype="pattern3d", srcpos=[5, 5, 5], srcparam1=[4, 4, 4, 0],
+                      srcpattern=_pattern((4, 4, 4), 2)),
+    "focus": dict(srcdir=[0, 0, 1, 10]),
+    "lambert": dict(srcdir=[0, 0, 1, -np.inf]),
+    "noreflect": dict(isreflect=0),
+    "cyclic": dict(bc="ccrrcc", isreflect=0),
+    "facedet": dict(bc="aaaaaa001000", isreflect=0),
+    "roulette": dict(minenergy=0.01),
+    "unitinmm": dict(unitinmm=0.5),
+    "gscatter": dict(gscatter=3),
+    "outside_src_specular": dict(srcpos=[20, 20, -5], isspecular=1),
+    "multisrc": dict(srcpos=[[20, 20, 0, 1], [10, 10, 0, 1]], srcdir=[[0, 0, 1, 0], [0, 0, 1, 0]]),
+    "multisrc_id": dict(srcpos=[[20, 20, 0, 1], [10, 10, 0, 1]], srcdir=[[0, 0, 1, 0], [0, 0, 1, 0]], srcid=-1),
+    "energy_out": dict(outputtype="energy"),
+    "fluence_out": dict(outputtype="fluence"),
+    "invcdf": dict(invcdf=(np.sign(np.linspace(-1, 1, 101)) *
+                           np.abs(np.linspace(-1, 1, 101)) ** 0.7).astype(np.float32)),
+    "angleinvcdf": dict(angleinvcdf=np.linspace(0, 0.3, 21).astype(np.float32)),
+}
+
+
+def variant(name, **kw):
+    cfg = small_two_media(**VARIANTS[name])
+    cfg.update(kw)
+    return cfg
+
+
+def twod(**kw):
+    cfg = small_two_media(vol=np.ones((1, 40, 40), np.uint8), srcpos=[0, 20, 0], detpos=[[0, 20, 0, 3]])
+    cfg.update(kw)
+    return cfg
+
+
+def pin_cases():
+    """(name, cfg, nthread) triples pinned against the reference kernel."""
+    out = [("cube60", cube60(nphoton=3000), 256),
+           ("cube60b", cube60(nphoton=3000, isreflect=1), 256),
+           ("cube60b_dspmxvw", cube60(nphoton=3000, isreflect=1, savedetflag="dspmxvw", issaveseed=1), 256),
+           ("twod", twod(), 128)]
+    for k in VARIANTS:
+        out.append((k, variant(k), 128))
+    return out

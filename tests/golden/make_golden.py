@@ -1,0 +1,68 @@
+"""Generate tests/golden/ref_pins.json from the reference kernel itself.
+
+Builds oracle/_ref/libmcxref.so from the reference sources (src/mcx_core.cl
+compiled as host C++ in place, see oracle/Makefile), runs every case of
+tests/cases.py:pin_cases() one reference thread at a time, and records
+SHA-256 digests of the raw output bits (per-thread energies, merged fluence
+field, detected-photon records, saved seeds) plus a few readable values.
+tests/test_oracle_pins.py recomputes the same digests with the oracle.
+
+Run here, where the reference sources are present:
+    python tests/golden/make_golden.py [--reference /path/to/mcxcl]
+"""
+import argparse
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import oracle  # noqa: E402
+import cases  # noqa: E402
+
+
+def digest(a):
+    if a is None:
+        return None
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def summarize(res):
+    e = np.asarray(res["energy"], np.float32)
+    field = np.asarray(res["field_raw"], np.float32)
+    return {
+        "energy_sha": digest(e.view(np.uint32)),
+        "field_sha": digest(np.asfortranarray(field).ravel(order="F").view(np.uint32)),
+        "detp_sha": digest(np.asarray(res["detp"], np.float32).view(np.uint32)),
+        "seeds_sha": digest(res["seeds"]),
+        "energy_tot": float(e[:, 1].astype(np.float64).sum()),
+        "energy_esc": float(e[:, 0].astype(np.float64).sum()),
+        "field_sum": float(field.astype(np.float64).sum()),
+        "ndet": int(np.asarray(res["detp"]).shape[1]) if np.asarray(res["detp"]).ndim == 2 else 0,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("MCX_REFERENCE", "/root/reference"))
+    args = ap.parse_args()
+    oracle.build(args.reference)
+    if not oracle.ref_available():
+        sys.exit("reference harness could not be built from " + args.reference)
+    out = {}
+    for name, cfg, nthread in cases.pin_cases():
+        r = oracle.run_reference(cfg, nthread=nthread, core=nthread)
+        out[name] = dict(summarize(r), nthread=nthread)
+        print(name, out[name]["ndet"], out[name]["energy_tot"])
+    with open(os.path.join(HERE, "ref_pins.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,117 @@
+"""The oracle against the reference: bit-exact pins and known answers.
+
+* ref_pins.json holds digests of the reference kernel's own outputs
+  (src/mcx_core.cl compiled on the host, tests/golden/make_golden.py).  The
+  oracle, run with the same math library and the __NVCC__-branch hitgrid,
+  must reproduce every output bit: per-thread energies, the fluence field,
+  detected-photon records and their RNG seeds.
+* The reference's own test script (test/testmcx.sh) and benchmark checks
+  (mcxlabcl/examples/mcx_gpu_benchmarks.m) quote absorbed fractions; the
+  oracle in the OpenCL-branch semantics must land in the same bands.
+"""
+import hashlib
+import json
+import os
+import platform
+
+import numpy as np
+import pytest
+
+import cases
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PINS = json.load(open(os.path.join(HERE, "golden", "ref_pins.json")))
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.skipif(platform.machine() not in ("x86_64", "AMD64"),
+                    reason="libm-mode digests were recorded with x86-64 glibc")
+@pytest.mark.parametrize("name,cfg,nthread", cases.pin_cases(), ids=[c[0] for c in cases.pin_cases()])
+def test_oracle_matches_reference_bits(oracle_mod, name, cfg, nthread):
+    O = oracle_mod
+    pin = PINS[name]
+    r = O.run(cfg, nthread=nthread, core=nthread, mathmode=O.MATH_LIBM, variant=O.VARIANT_NVCC,
+              fieldmode=O.FIELD_FLOAT_SPILL)
+    e = np.asarray(r["energy"], np.float32)
+    assert _sha(e.view(np.uint32)) == pin["energy_sha"]
+    field = np.asarray(r["field_raw"], np.float32)
+    assert _sha(np.asfortranarray(field).ravel(order="F").view(np.uint32)) == pin["field_sha"]
+    assert r["detp"].shape[1] == pin["ndet"]
+    assert _sha(np.asarray(r["detp"], np.float32).view(np.uint32)) == pin["detp_sha"]
+    if pin["seeds_sha"] is not None:
+        assert _sha(r["seeds"]) == pin["seeds_sha"]
+
+
+def _absorbed(r):
+    s = r["stat"]
+    return (s["energytot"] - s["energyesc"]) / s["energytot"]
+
+
+# (name, cfg, band) -- bands quoted by test/testmcx.sh and mcx_gpu_benchmarks.m
+KNOWN = [
+    ("cube60 17.x%", cases.cube60(nphoton=200000), (0.17, 0.18)),
+    ("cube60b 27.x%", cases.cube60(nphoton=200000, isreflect=1), (0.27, 0.28)),
+    ("cube60 bc aarraa 27.x%", cases.cube60(nphoton=200000, isreflect=0, bc="aarraa"), (0.27, 0.28)),
+    ("cube60 cyclic 99.x%", cases.cube60(nphoton=1000, bc="cccccc", issavedet=0), (0.99, 1.0)),
+    ("isotropic 88.x%", cases.cube60(nphoton=100000, srctype="isotropic", srcpos=[29, 29, 29],
+                                      issavedet=0), (0.88, 0.89)),
+    ("cone 6.x%", cases.cube60(nphoton=100000, srctype="cone", srcparam1=[0.5, 0, 0, 0],
+                               prop=[[0, 0, 1, 1], [0.001, 0.001, 0, 1]], issavedet=0), (0.06, 0.07)),
+    ("planar 25.x%", cases.cube60(nphoton=200000, srctype="planar", srcpos=[10, 10, -10], isreflect=1,
+                                  srcparam1=[40, 0, 0, 0], srcparam2=[0, 40, 0, 0], issavedet=0), (0.25, 0.26)),
+]
+
+
+@pytest.mark.parametrize("name,cfg,band", KNOWN, ids=[k[0] for k in KNOWN])
+def test_oracle_known_absorbed_fraction(oracle_mod, name, cfg, band):
+    O = oracle_mod
+    r = O.run(cfg, nthread=16384, core=16384, mathmode=O.MATH_PMATH, variant=O.VARIANT_OPENCL,
+              fieldmode=O.FIELD_DOUBLE)
+    a = _absorbed(r)
+    assert band[0] <= a < band[1], (name, a)
+
+
+def test_oracle_cube60b_detects_4x_photons(oracle_mod):
+    """testmcx.sh:81 -- cube60b at 1e6 photons detects "4[0-9]+ photons"
+    (4000-4999); at 1e5 photons that band is 400-499."""
+    O = oracle_mod
+    r = O.run(cases.cube60(nphoton=100000, isreflect=1), nthread=16384, core=16384, mathmode=O.MATH_PMATH)
+    assert 400 <= r["stat"]["detected"] <= 499
+
+
+def test_oracle_rng_stream_matches_xorshift(oracle_mod):
+    """-D R fills the field with each thread's stream (mcx_core.cl:2408-2414);
+    check it against an independent numpy xorshift128+ of glibc-seeded words."""
+    import ctypes
+    O = oracle_mod
+    cfg = cases.cube60(nphoton=64, vol=np.ones((8, 8, 8), np.uint8), debuglevel="R", issavedet=0)
+    r = O.run(cfg, nthread=64, core=64, fieldmode=O.FIELD_FLOAT_SPILL)
+    libc = ctypes.CDLL(None)
+    libc.srand(ctypes.c_uint(cfg["seed"]))
+    words = np.array([libc.rand() for _ in range(64 * 4)], np.uint64).reshape(64, 4)
+    mask = (1 << 64) - 1
+    field = np.asarray(r["flux"]).ravel(order="F")
+    for tid in (0, 1, 37, 63):
+        t0 = int(words[tid, 0]) << 32 | int(words[tid, 1])
+        t1 = int(words[tid, 2]) << 32 | int(words[tid, 3])
+        for j in range(tid, field.size, 64):
+            s1, s0 = t0, t1
+            t0 = s0
+            s1 = (s1 ^ (s1 << 23)) & mask
+            t1 = s1 ^ s0 ^ (s1 >> 18) ^ (s0 >> 5)
+            lo = ((t1 + s0) & mask) & 0xFFFFFFFF
+            val = np.uint32(0x3F800000 | (lo >> 9)).view(np.float32) - np.float32(1.0)
+            assert field[j] == val
+
+
+def test_oracle_double_field_close_to_float(oracle_mod):
+    """The FP64 accumulator and the reference's float+spill accumulator agree to float precision."""
+    O = oracle_mod
+    cfg = cases.variant("pencil_gates")
+    a = O.run(cfg, nthread=128, core=128, fieldmode=O.FIELD_FLOAT_SPILL)
+    b = O.run(cfg, nthread=128, core=128, fieldmode=O.FIELD_DOUBLE)
+    np.testing.assert_allclose(a["field_raw"], b["field_raw"], rtol=2e-5, atol=1e-4)
+    np.testing.assert_array_equal(a["energy"], b["energy"])
