@@ -1,0 +1,288 @@
+/*
+ * mcx_gb300.h -- C ABI of the GB300 photon-transport path.
+ *
+ * Two layers, both plain C (no CUDA or torch types in any signature):
+ *
+ *  1. The drop-in host interface of the reference's simulation driver.
+ *     `Config` keeps the field names, types and meanings of the reference's
+ *     MCXConfig (src/mcx_utils.h:165-281) for every field the transport path
+ *     reads or writes; fields that only serve subsystems outside this path
+ *     (MATLAB/NIfTI/JNIfTI writers, shapes parser, polarisation, trajectory
+ *     debug, adjoint post-processing) are not carried.  Callers fill a
+ *     Config the way they fill the reference's, call mcx_validatecfg() and
+ *     mcx_run_simulation(), and read the same output fields.
+ *
+ *  2. The thin device layer (mcxg_*) that the C host driver calls: a session
+ *     owning device memory on one GPU, uploads, a kernel launch, FP64
+ *     reductions and readback.  Every call returns an int status
+ *     (MCXG_OK == 0); mcxg_error_string() names it.  It replaces the OpenCL
+ *     launch and readback code in mcx_run_simulation
+ *     (src/mcx_host.cpp:739-1345).
+ *
+ * One GPU per call.  Not re-entrant across threads that share a Config.
+ */
+#ifndef MCX_GB300_H
+#define MCX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCX_GB300_VERSION   "v2025.10-gb300"
+#define MAX_SESSION_LENGTH  64
+#define MAX_PATH_LENGTH     1024
+#define MAX_DEVICE          256
+
+/* ---- constants (src/mcx_const.h) ---------------------------------------- */
+#define MCX_SRC_PENCIL       0
+#define MCX_SRC_ISOTROPIC    1
+#define MCX_SRC_CONE         2
+#define MCX_SRC_GAUSSIAN     3
+#define MCX_SRC_PLANAR       4
+#define MCX_SRC_PATTERN      5
+#define MCX_SRC_FOURIER      6
+#define MCX_SRC_ARCSINE      7
+#define MCX_SRC_DISK         8
+#define MCX_SRC_FOURIERX     9
+#define MCX_SRC_FOURIERX2D   10
+#define MCX_SRC_ZGAUSSIAN    11
+#define MCX_SRC_LINE         12
+#define MCX_SRC_SLIT         13
+#define MCX_SRC_PENCILARRAY  14
+#define MCX_SRC_PATTERN3D    15
+#define MCX_SRC_HYPERBOLOID_GAUSSIAN 16
+#define MCX_SRC_RING         17
+
+#define MEDIA_MUA_FLOAT      101
+#define SEED_FROM_FILE       -999
+#define FILL_MAXDETPHOTON    3
+
+enum TOutputType {otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL};
+enum TBoundary {bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic};
+enum TMCXParent {mpStandalone, mpMATLAB, mpPython};
+
+/* savedetflag bits: D S P M X V W (src/mcx_const.h:93-100) */
+#define SAVE_DETID(a)  ((a) & 0x1)
+#define SAVE_NSCAT(a)  ((a) >> 1 & 0x1)
+#define SAVE_PPATH(a)  ((a) >> 2 & 0x1)
+#define SAVE_MOM(a)    ((a) >> 3 & 0x1)
+#define SAVE_PEXIT(a)  ((a) >> 4 & 0x1)
+#define SAVE_VEXIT(a)  ((a) >> 5 & 0x1)
+#define SAVE_W0(a)     ((a) >> 6 & 0x1)
+
+typedef struct { float x, y, z, w; } mcx_float4;
+typedef struct { unsigned int x, y, z, w; } mcx_uint4;
+
+/* src/mcx_utils.h:77-82 */
+typedef struct MCXMedium {
+    float mua, mus, g, n;
+} Medium;
+
+/* src/mcx_utils.h:100-105: one additional source */
+typedef struct MCXExtraSource {
+    mcx_float4 srcpos, srcdir, srcparam1, srcparam2;
+} ExtraSrc;
+
+/* src/mcx_utils.h:113-130: the .mch header, filled for detected photons */
+typedef struct MCXHistoryHeader {
+    char magic[4];
+    unsigned int version, maxmedia, detnum, colcount, totalphoton, detected, savedphoton;
+    float unitinmm;
+    unsigned int seedbyte;
+    float normalizer;
+    int respin;
+    unsigned int srcnum, savedetflag, totalsource;
+    int reserved[1];
+} History;
+
+/* src/mcx_utils.h:143-163 */
+typedef struct MCXGPUInfo {
+    char name[MAX_SESSION_LENGTH];
+    int id, devcount, platformid, major, minor;
+    size_t globalmem, constmem, sharedmem;
+    int regcount, clock, sm, core;
+    size_t autoblock, autothread;
+    unsigned int maxgate;
+    int maxmpthread, iscpu;
+    int vendor;
+} GPUInfo;
+
+/* The simulation configuration.  Names and meanings as src/mcx_utils.h:165-281. */
+typedef struct MCXConfig {
+    size_t nphoton;
+    unsigned int nblocksize;
+    unsigned int nthread;
+    int seed;
+    mcx_float4 srcpos, srcdir;
+    float tstart, tstep, tend;
+    mcx_float4 steps;
+    mcx_uint4 dim;
+    unsigned int medianum;
+    unsigned int detnum;
+    unsigned int maxdetphoton;
+    Medium* prop;
+    mcx_float4* detpos;
+    unsigned int maxgate;
+    int respin;
+    int gpuid;
+    unsigned int* vol;            /* one word per voxel, x fastest; labels, or float mua bits (MEDIA_MUA_FLOAT) */
+    char session[MAX_SESSION_LENGTH];
+    char isrowmajor, isreflect, isrefint, isnormalized, issavedet, issave2pt, isgpuinfo, isspecular;
+    char issrcfrom0, ismomentum, internalsrc, issaveseed, issaveexit, isatomic, issaveref;
+    char srctype, autopilot, outputtype;
+    float minenergy;
+    float unitinmm;
+    FILE* flog;
+    History his;
+    double energytot, energyabs, energyesc;
+    int maxvoidstep, voidtime;
+    mcx_float4 srcparam1, srcparam2;
+    unsigned int srcnum;
+    float* srcpattern;
+    char deviceid[MAX_DEVICE];
+    float workload[MAX_DEVICE];
+    float* exportfield;           /* [Nx,Ny,Nz,gates(,sources)] x fastest */
+    float* exportdetected;        /* [reclen x detected] */
+    unsigned int debuglevel;
+    float normalizer;
+    void* seeddata;               /* detected-photon RNG seeds, 16 bytes each */
+    unsigned int gscatter;
+    unsigned int savedetflag;
+    unsigned int detectedcount;
+    unsigned int runtime;         /* kernel time, ms */
+    int parentid;
+    unsigned int mediabyte;
+    char bc[13];
+    unsigned int nphase;
+    float* invcdf;
+    unsigned int nangle;
+    float* angleinvcdf;
+    int srcid;
+    unsigned int extrasrclen;
+    ExtraSrc* srcdata;
+    /* GB300 additions */
+    int exactmath;                /* 1: run the IEEE-only kernel (bit-identical to the CPU oracle) */
+    float kernelms;               /* kernel time from CUDA events, ms */
+    uint64_t eventcount[5];       /* exact kernel only: steps, scatterings, launches, Fresnel tests, failed launches */
+    unsigned int failedlaunch;    /* reference threads whose first launch found no entry point */
+    unsigned int threadused;      /* reference threads (RNG streams) of the last run */
+    float* exportenergy;          /* when savethreadenergy: 2 x threadused {escaped, launched} floats */
+    int savethreadenergy;
+    int errorcode;                /* last error in library mode */
+    char errormsg[256];
+} Config;
+
+/* ---- drop-in host interface ------------------------------------------------ */
+
+/* Defaults of mcx_initcfg (src/mcx_utils.c:203-366). */
+void mcx_initcfg(Config* cfg);
+/* Frees every buffer the Config owns (src/mcx_utils.c:368-476). */
+void mcx_clearcfg(Config* cfg);
+/* Checks inputs, converts to 0-based positions, scales by unitinmm, builds the
+   detector mask and launch voxel (src/mcx_utils.c:1822-1964, 1521-1809).
+   detps/dimdetps/seedbyte are accepted for signature compatibility; photon
+   replay is not part of this build and must be NULL/0. */
+void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte);
+/* Lists CUDA devices into *info (caller frees with mcx_cleargpuinfo); replaces
+   mcx_list_gpu(Config*, unsigned*, cl_device_id*, GPUInfo**)
+   (src/mcx_host.cpp:252).  Returns the number of active devices. */
+int  mcx_list_gpu(Config* cfg, unsigned int* activedev, GPUInfo** info);
+void mcx_cleargpuinfo(GPUInfo** info);
+/* Runs the simulation (src/mcx_host.h:168); fluence and totalenergy are unused,
+   as in the reference.  Outputs go to cfg: exportfield, exportdetected,
+   seeddata, detectedcount, energytot/energyesc/energyabs, normalizer, runtime. */
+void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy);
+/* Scales field[i*srcnum+pidx] by scale (src/mcx_utils.c:1208-1218). */
+void mcx_normalize(float field[], float scale, int fieldlen, int option, int pidx, int srcnum);
+/* Error reporting.  Standalone: print and exit(id).  Library mode
+   (cfg->parentid != mpStandalone): the failing public call returns with
+   cfg->errorcode/errormsg set; read them with mcx_last_error(). */
+void mcx_error(const int id, const char* msg, const char* file, const int linenum);
+int  mcx_last_error(const Config* cfg, const char** msg);
+/* Number of floats in one detected-photon record for this Config. */
+unsigned int mcx_detreclen(const Config* cfg);
+const char* mcx_version(void);
+/* sizeof(Config) and the byte offset of a named field ((size_t)-1 if
+   unknown), for checking foreign-function mirrors of the struct. */
+size_t mcx_config_sizeof(void);
+size_t mcx_config_offsetof(const char* name);
+/* Releases the device sessions cached per GPU by mcx_run_simulation. */
+void mcx_release_sessions(void);
+
+/* ---- thin device layer ------------------------------------------------------ */
+
+#define MCXG_OK              0
+#define MCXG_ERR_CUDA        1
+#define MCXG_ERR_ARG         2
+#define MCXG_ERR_NOMEM       3
+#define MCXG_ERR_LIMIT       4
+#define MCXG_ERR_STATE       5
+#define MCXG_ERR_NODEVICE    6
+
+/* mcxg_simulate flags */
+#define MCXG_EXACT    1u   /* IEEE-only kernel with event counters */
+#define MCXG_NOAGG    2u   /* disable warp aggregation of deposits */
+#define MCXG_RNGDUMP  4u   /* write each thread's RNG stream into the field (-D R) */
+#define MCXG_KEEP     8u   /* keep accumulating into the field (respin); energies, records and counters restart */
+
+typedef struct mcxg_devinfo {
+    char name[64];
+    int major, minor, sm, clock_khz;
+    size_t globalmem, sharedmem_per_block, constmem;
+    int regs_per_block, max_threads_per_sm;
+} mcxg_devinfo;
+
+typedef struct mcxg_session mcxg_session;
+
+int  mcxg_device_count(int* n);
+int  mcxg_device_info(int device, mcxg_devinfo* info);
+const char* mcxg_error_string(int code);
+
+int  mcxg_create(int device, mcxg_session** s);
+int  mcxg_destroy(mcxg_session* s);
+
+/*
+ * Upload one problem.  kparams points to an mcxg_kparams (csrc/mcx_kparams.h),
+ * passed opaquely with its size for ABI checking.  media holds nvox voxels of
+ * mediaword bytes each (1: label | detector bit << 7; 4: the reference's
+ * 32-bit word).  prop: medianum x 4 floats; detpos: detnum x 4; srcextra:
+ * extrasrclen x 16; tables may be NULL when their length is 0.
+ */
+int  mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, const void* media,
+                      uint32_t mediaword, const float* prop, const float* detpos, const float* srcextra,
+                      const float* invcdf, const float* angleinvcdf, const float* srcpattern, size_t npattern);
+/* Replace the parameter block of the current problem (same buffer shapes:
+   photon split, time window, flags); the next launch re-uploads it. */
+int  mcxg_set_params(mcxg_session* s, const void* kparams, size_t kparams_size);
+/* 4 seed words per reference thread, as the reference draws them with rand(). */
+int  mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread);
+/* Launch shape of the persistent grid (0 = automatic). */
+int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
+/* Run all photons once; kernel time (CUDA events) into *kernel_ms. */
+int  mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms);
+/* FP64 sums over threads of escaped and launched weight. */
+int  mcxg_get_energy(mcxg_session* s, double* escaped, double* launched);
+/* Per-thread {escaped, launched} floats, 2 x nthread. */
+int  mcxg_get_thread_energy(mcxg_session* s, float* out);
+/* Field: (hi + lo) in FP64, times scale, rounded to float; fieldlen values. */
+int  mcxg_get_field(mcxg_session* s, float* out, double scale);
+/* Field: (hi + lo) in FP64, unscaled. */
+int  mcxg_get_field_f64(mcxg_session* s, double* out);
+/* Detected photons: up to maxdetphoton records (reclen floats) and seeds
+   (2 x uint64 each, when enabled); *detected = all detections, including
+   those beyond the buffer. */
+int  mcxg_get_detected(mcxg_session* s, float* detp, uint64_t* seeds, uint32_t* detected);
+/* Event counters (exact kernel) and status words. */
+int  mcxg_get_counters(mcxg_session* s, uint64_t counters[5], uint32_t status[2]);
+/* The persistent grid actually used by the last launch. */
+int  mcxg_get_launch(mcxg_session* s, int* grid, int* block, int* regs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,637 @@
+/*
+ * mcx_device.cu -- the thin device layer (mcxg_* in include/mcx_gb300.h).
+ *
+ * Replaces the OpenCL buffer creation, launch and readback of the reference's
+ * mcx_run_simulation (src/mcx_host.cpp:739-1345).  A session owns one CUDA
+ * stream and the device buffers of one problem; buffers grow on demand and
+ * are reused across calls, so repeated runs (respin, autotuning, bench
+ * steps) allocate nothing after the first.
+ *
+ * The FP64 work of the path lives here: the per-thread escaped/launched
+ * weights are summed in double on the GPU (the reference sums them in double
+ * on the host, mcx_host.cpp:1303-1306) and the two-plane field is merged and
+ * normalised in double before rounding to float (the reference merges and
+ * scales in float, mcx_host.cpp:1252-1257, mcx_utils.c:1208-1218).
+ */
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/mcx_gb300.h"
+#include "mcx_kparams.h"
+#include "mcx_launch.h"
+
+using mcxg::KArgs;
+
+struct mcxg_session {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    mcxg_devinfo info{};
+    mcxg_kparams kp{};
+    bool has_problem = false;
+    bool has_seeds = false;
+    bool up_fast = false, up_exact = false;
+
+    void* d_media = nullptr;
+    size_t media_cap = 0;
+    float4* d_prop = nullptr;
+    size_t prop_cap = 0;
+    float* d_tables = nullptr;       /* invcdf then angleinvcdf */
+    size_t tables_cap = 0;
+    float* d_pattern = nullptr;
+    size_t pattern_cap = 0;
+    uint4* d_seeds = nullptr;
+    size_t seeds_cap = 0;
+    float* d_field = nullptr;        /* 2 x fieldlen */
+    size_t field_cap = 0;
+    float2* d_energy = nullptr;
+    size_t energy_cap = 0;
+    float* d_detp = nullptr;
+    size_t detp_cap = 0;             /* floats */
+    unsigned long long* d_detseed = nullptr;
+    size_t detseed_cap = 0;
+    unsigned int* d_words = nullptr; /* detcount, vtcounter, status[2] */
+    unsigned long long* d_events = nullptr;
+    double* d_red = nullptr;         /* reduction partials + result */
+    void* d_out = nullptr;           /* merged field, float or double */
+    size_t out_cap = 0;
+
+    std::vector<float> h_det, h_srcx;
+    int block_req = 0, bpsm_req = 0;
+    int grid = 0, block = 0, regs = 0;
+};
+
+namespace {
+
+constexpr int kRedBlocks = 256;
+constexpr int kRedThreads = 256;
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) {
+        return MCXG_OK;
+    }
+    if (e == cudaErrorMemoryAllocation) {
+        return MCXG_ERR_NOMEM;
+    }
+    return MCXG_ERR_CUDA;
+}
+
+#define MCXG_TRY(x)                       \
+    do {                                  \
+        int _rc = cuda_status((x));       \
+        if (_rc) {                        \
+            return _rc;                   \
+        }                                 \
+    } while (0)
+
+template <typename T>
+int ensure(T** ptr, size_t* cap, size_t count) {
+    if (count <= *cap && *ptr) {
+        return MCXG_OK;
+    }
+    if (*ptr) {
+        cudaFree(*ptr);
+        *ptr = nullptr;
+        *cap = 0;
+    }
+    if (count == 0) {
+        return MCXG_OK;
+    }
+    MCXG_TRY(cudaMalloc((void**)ptr, count * sizeof(T)));
+    *cap = count;
+    return MCXG_OK;
+}
+
+/* per-block partial FP64 sums of {escaped, launched} */
+__global__ void energy_partials(const float2* __restrict__ e, unsigned int n, double* __restrict__ part) {
+    double se = 0.0, sl = 0.0;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float2 v = e[i];
+        se += (double)v.x;
+        sl += (double)v.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        se += __shfl_down_sync(0xffffffffu, se, o);
+        sl += __shfl_down_sync(0xffffffffu, sl, o);
+    }
+    __shared__ double wse[32], wsl[32];
+    if ((threadIdx.x & 31) == 0) {
+        wse[threadIdx.x >> 5] = se;
+        wsl[threadIdx.x >> 5] = sl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (unsigned int w = 0; w < (blockDim.x + 31) / 32; w++) {
+            a += wse[w];
+            b += wsl[w];
+        }
+        part[blockIdx.x * 2] = a;
+        part[blockIdx.x * 2 + 1] = b;
+    }
+}
+
+/* fixed-order final sum, so the result is the same bits on every run */
+__global__ void energy_final(double* part, int nblocks) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < nblocks; i++) {
+            a += part[i * 2];
+            b += part[i * 2 + 1];
+        }
+        part[nblocks * 2] = a;
+        part[nblocks * 2 + 1] = b;
+    }
+}
+
+__global__ void field_merge_f32(const float* __restrict__ f, size_t n, double scale, float* __restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        out[i] = (float)(((double)f[i] + (double)f[i + n]) * scale);
+    }
+}
+
+__global__ void field_merge_f64(const float* __restrict__ f, size_t n, double* __restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        out[i] = (double)f[i] + (double)f[i + n];
+    }
+}
+
+int grid_for(const mcxg_session* s, size_t n) {
+    size_t g = (n + 255) / 256;
+    size_t cap = (size_t)s->info.sm * 8;
+    if (g > cap) {
+        g = cap;
+    }
+    return g < 1 ? 1 : (int)g;
+}
+
+size_t shared_bytes(const mcxg_kparams& kp, int block) {
+    size_t det = (kp.savedet ? kp.partialdata : 0);
+    return (size_t)kp.medianum * 16 + (size_t)(kp.nphase + kp.nangle) * 4 + det * (size_t)block * 4;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mcxg_error_string(int code) {
+    switch (code) {
+        case MCXG_OK: return "ok";
+        case MCXG_ERR_CUDA: return "CUDA runtime error";
+        case MCXG_ERR_ARG: return "invalid argument";
+        case MCXG_ERR_NOMEM: return "out of device memory";
+        case MCXG_ERR_LIMIT: return "input exceeds a compiled limit";
+        case MCXG_ERR_STATE: return "call out of order";
+        case MCXG_ERR_NODEVICE: return "no CUDA device";
+        default: return "unknown error";
+    }
+}
+
+int mcxg_device_count(int* n) {
+    if (!n) {
+        return MCXG_ERR_ARG;
+    }
+    *n = 0;
+    cudaError_t e = cudaGetDeviceCount(n);
+    if (e != cudaSuccess) {
+        *n = 0;
+        cudaGetLastError();
+        return MCXG_ERR_NODEVICE;
+    }
+    return MCXG_OK;
+}
+
+int mcxg_device_info(int device, mcxg_devinfo* info) {
+    if (!info) {
+        return MCXG_ERR_ARG;
+    }
+    cudaDeviceProp p;
+    MCXG_TRY(cudaGetDeviceProperties(&p, device));
+    memset(info, 0, sizeof(*info));
+    strncpy(info->name, p.name, sizeof(info->name) - 1);
+    info->major = p.major;
+    info->minor = p.minor;
+    info->sm = p.multiProcessorCount;
+    int clk = 0;
+    cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, device);
+    info->clock_khz = clk;
+    info->globalmem = p.totalGlobalMem;
+    info->sharedmem_per_block = p.sharedMemPerBlockOptin;
+    info->constmem = p.totalConstMem;
+    info->regs_per_block = p.regsPerBlock;
+    info->max_threads_per_sm = p.maxThreadsPerMultiProcessor;
+    return MCXG_OK;
+}
+
+int mcxg_create(int device, mcxg_session** out) {
+    if (!out) {
+        return MCXG_ERR_ARG;
+    }
+    *out = nullptr;
+    int n = 0;
+    if (mcxg_device_count(&n) || device < 0 || device >= n) {
+        return MCXG_ERR_NODEVICE;
+    }
+    mcxg_session* s = new (std::nothrow) mcxg_session();
+    if (!s) {
+        return MCXG_ERR_NOMEM;
+    }
+    s->device = device;
+    int rc = cuda_status(cudaSetDevice(device));
+    if (!rc) {
+        rc = mcxg_device_info(device, &s->info);
+    }
+    if (!rc) {
+        rc = cuda_status(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+    }
+    if (!rc) {
+        rc = cuda_status(cudaEventCreate(&s->e0));
+    }
+    if (!rc) {
+        rc = cuda_status(cudaEventCreate(&s->e1));
+    }
+    if (!rc) {
+        rc = cuda_status(cudaMalloc((void**)&s->d_words, 8 * sizeof(unsigned int)));
+    }
+    if (!rc) {
+        rc = cuda_status(cudaMalloc((void**)&s->d_events, 8 * sizeof(unsigned long long)));
+    }
+    if (!rc) {
+        rc = cuda_status(cudaMalloc((void**)&s->d_red, (2 * kRedBlocks + 2) * sizeof(double)));
+    }
+    if (rc) {
+        mcxg_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return MCXG_OK;
+}
+
+int mcxg_destroy(mcxg_session* s) {
+    if (!s) {
+        return MCXG_OK;
+    }
+    cudaSetDevice(s->device);
+    if (s->st) {
+        cudaStreamSynchronize(s->st);
+    }
+    void* bufs[] = {s->d_media, s->d_prop, s->d_tables, s->d_pattern, s->d_seeds, s->d_field, s->d_energy,
+                    s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out};
+    for (void* b : bufs) {
+        if (b) {
+            cudaFree(b);
+        }
+    }
+    if (s->e0) {
+        cudaEventDestroy(s->e0);
+    }
+    if (s->e1) {
+        cudaEventDestroy(s->e1);
+    }
+    if (s->st) {
+        cudaStreamDestroy(s->st);
+    }
+    delete s;
+    return MCXG_OK;
+}
+
+int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, const void* media,
+                     uint32_t mediaword, const float* prop, const float* detpos, const float* srcextra,
+                     const float* invcdf, const float* angleinvcdf, const float* srcpattern, size_t npattern) {
+    if (!s || !kparams || kparams_size != sizeof(mcxg_kparams) || !media || !prop) {
+        return MCXG_ERR_ARG;
+    }
+    const mcxg_kparams& kp = *(const mcxg_kparams*)kparams;
+    if (mediaword != 1 && mediaword != 4) {
+        return MCXG_ERR_ARG;
+    }
+    if (kp.medianum < 2 && kp.mediaformat <= 4) {
+        return MCXG_ERR_ARG;
+    }
+    if (kp.medianum > MCXG_MAX_MEDIA || kp.detnum > MCXG_MAX_DET || kp.extrasrclen > MCXG_MAX_EXTRASRC) {
+        return MCXG_ERR_LIMIT;
+    }
+    if ((kp.detnum && !detpos) || (kp.extrasrclen && !srcextra) || (kp.nphase && !invcdf) ||
+            (kp.nangle && !angleinvcdf) || ((kp.srctype == MCX_SRC_PATTERN || kp.srctype == MCX_SRC_PATTERN3D) && !srcpattern)) {
+        return MCXG_ERR_ARG;
+    }
+    if (kp.nvox == 0 || kp.fieldlen == 0 || kp.nthread == 0) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    s->kp = kp;
+    s->kp.mediaword = mediaword;
+    s->kp.npattern = (uint32_t)(npattern ? npattern : 1);
+    size_t mbytes = (size_t)kp.nvox * mediaword;
+    int rc = ensure((uint8_t**)&s->d_media, &s->media_cap, mbytes);
+    if (!rc) {
+        rc = ensure(&s->d_prop, &s->prop_cap, kp.medianum);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_tables, &s->tables_cap, (size_t)kp.nphase + kp.nangle + 1);
+    }
+    if (!rc && npattern) {
+        rc = ensure(&s->d_pattern, &s->pattern_cap, npattern);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_field, &s->field_cap, 2 * (size_t)kp.fieldlen);
+    }
+    if (!rc && kp.savedet) {
+        size_t recs = kp.maxdetphoton;
+        rc = ensure(&s->d_detp, &s->detp_cap, recs * (kp.reclen ? kp.reclen : 1));
+        if (!rc && kp.issaveseed) {
+            rc = ensure(&s->d_detseed, &s->detseed_cap, recs * 2 + 2);
+        }
+    }
+    if (rc) {
+        return rc;
+    }
+    MCXG_TRY(cudaMemcpyAsync(s->d_media, media, mbytes, cudaMemcpyHostToDevice, s->st));
+    MCXG_TRY(cudaMemcpyAsync(s->d_prop, prop, sizeof(float) * 4 * kp.medianum, cudaMemcpyHostToDevice, s->st));
+    if (kp.nphase) {
+        MCXG_TRY(cudaMemcpyAsync(s->d_tables, invcdf, sizeof(float) * kp.nphase, cudaMemcpyHostToDevice, s->st));
+    }
+    if (kp.nangle) {
+        MCXG_TRY(cudaMemcpyAsync(s->d_tables + kp.nphase, angleinvcdf, sizeof(float) * kp.nangle,
+                                 cudaMemcpyHostToDevice, s->st));
+    }
+    if (npattern) {
+        MCXG_TRY(cudaMemcpyAsync(s->d_pattern, srcpattern, sizeof(float) * npattern, cudaMemcpyHostToDevice, s->st));
+    }
+    s->h_det.assign(detpos ? detpos : prop, detpos ? detpos + 4 * kp.detnum : prop);
+    s->h_srcx.assign(srcextra ? srcextra : prop, srcextra ? srcextra + 16 * kp.extrasrclen : prop);
+    s->up_fast = s->up_exact = false;
+    s->has_problem = true;
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_set_params(mcxg_session* s, const void* kparams, size_t kparams_size) {
+    if (!s || !kparams || kparams_size != sizeof(mcxg_kparams)) {
+        return MCXG_ERR_ARG;
+    }
+    if (!s->has_problem) {
+        return MCXG_ERR_STATE;
+    }
+    const mcxg_kparams& kp = *(const mcxg_kparams*)kparams;
+    if (kp.nvox != s->kp.nvox || kp.fieldlen != s->kp.fieldlen || kp.medianum != s->kp.medianum ||
+            kp.detnum != s->kp.detnum || kp.extrasrclen != s->kp.extrasrclen || kp.nphase != s->kp.nphase ||
+            kp.nangle != s->kp.nangle || kp.savedet != s->kp.savedet || kp.maxdetphoton != s->kp.maxdetphoton ||
+            kp.reclen != s->kp.reclen) {
+        return MCXG_ERR_ARG;    /* buffer shapes change only through mcxg_set_problem */
+    }
+    uint32_t mw = s->kp.mediaword, np = s->kp.npattern;
+    s->kp = kp;
+    s->kp.mediaword = mw;
+    s->kp.npattern = np;
+    s->up_fast = s->up_exact = false;
+    return MCXG_OK;
+}
+
+int mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread) {
+    if (!s || !seeds || nthread == 0) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    int rc = ensure(&s->d_seeds, &s->seeds_cap, nthread);
+    if (!rc) {
+        rc = ensure(&s->d_energy, &s->energy_cap, nthread);
+    }
+    if (rc) {
+        return rc;
+    }
+    MCXG_TRY(cudaMemcpyAsync(s->d_seeds, seeds, sizeof(uint4) * nthread, cudaMemcpyHostToDevice, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    s->has_seeds = true;
+    return MCXG_OK;
+}
+
+int mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm) {
+    if (!s || block < 0 || block > 256 || (block % 32) || blocks_per_sm < 0) {
+        return MCXG_ERR_ARG;
+    }
+    s->block_req = block;
+    s->bpsm_req = blocks_per_sm;
+    return MCXG_OK;
+}
+
+int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
+    if (!s) {
+        return MCXG_ERR_ARG;
+    }
+    if (!s->has_problem || !s->has_seeds || s->seeds_cap < s->kp.nthread || s->energy_cap < s->kp.nthread) {
+        return MCXG_ERR_STATE;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    const mcxg_kparams& kp = s->kp;
+    const bool exact = (flags & (MCXG_EXACT | MCXG_RNGDUMP)) != 0;
+
+    if (exact && !s->up_exact) {
+        MCXG_TRY(mcxg::exact_upload(&kp, s->h_det.data(), kp.detnum, s->h_srcx.data(), kp.extrasrclen, s->st));
+        s->up_exact = true;
+    }
+    if (!exact && !s->up_fast) {
+        MCXG_TRY(mcxg::fast_upload(&kp, s->h_det.data(), kp.detnum, s->h_srcx.data(), kp.extrasrclen, s->st));
+        s->up_fast = true;
+    }
+    if (!(flags & MCXG_KEEP)) {
+        MCXG_TRY(cudaMemsetAsync(s->d_field, 0, sizeof(float) * 2 * (size_t)kp.fieldlen, s->st));
+    }
+    MCXG_TRY(cudaMemsetAsync(s->d_energy, 0, sizeof(float2) * kp.nthread, s->st));
+    MCXG_TRY(cudaMemsetAsync(s->d_words, 0, 8 * sizeof(unsigned int), s->st));
+    MCXG_TRY(cudaMemsetAsync(s->d_events, 0, 8 * sizeof(unsigned long long), s->st));
+
+    KArgs a;
+    a.media8 = (const uint8_t*)s->d_media;
+    a.media32 = (const uint32_t*)s->d_media;
+    a.gprop = s->d_prop;
+    a.invcdf = s->d_tables;
+    a.angleinvcdf = s->d_tables + kp.nphase;
+    a.srcpattern = s->d_pattern;
+    a.seeds = s->d_seeds;
+    a.field = s->d_field;
+    a.energy = s->d_energy;
+    a.detp = s->d_detp;
+    a.detseed = s->d_detseed;
+    a.detcount = s->d_words + 0;
+    a.vtcounter = s->d_words + 1;
+    a.status = s->d_words + 2;
+    a.counters = s->d_events;
+
+    int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
+                 ((flags & MCXG_NOAGG) ? 0 : mcxg::LF_WAGG);
+    int block = s->block_req ? s->block_req : 256;
+    size_t smem = shared_bytes(kp, block);
+    if (smem > s->info.sharedmem_per_block) {
+        return MCXG_ERR_LIMIT;
+    }
+    int bpsm = s->bpsm_req;
+    if (!bpsm) {
+        if (exact) {
+            bpsm = 2;
+        } else {
+            MCXG_TRY(mcxg::fast_occupancy(lflags, block, smem, &bpsm));
+        }
+        if (bpsm < 1) {
+            bpsm = 1;
+        }
+    }
+    int grid = s->info.sm * bpsm;
+    s->grid = grid;
+    s->block = block;
+    if (!exact) {
+        cudaFuncAttributes fa;
+        if (mcxg::fast_attributes(lflags, &fa) == cudaSuccess) {
+            s->regs = fa.numRegs;
+        }
+    }
+
+    MCXG_TRY(cudaEventRecord(s->e0, s->st));
+    if (flags & MCXG_RNGDUMP) {
+        MCXG_TRY(mcxg::exact_rngdump(a, s->info.sm * 4, 256, s->st));
+    } else if (exact) {
+        MCXG_TRY(mcxg::exact_launch(a, lflags, grid, block, smem, s->st));
+    } else {
+        MCXG_TRY(mcxg::fast_launch(a, lflags, grid, block, smem, s->st));
+    }
+    MCXG_TRY(cudaEventRecord(s->e1, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    MCXG_TRY(cudaGetLastError());
+    if (kernel_ms) {
+        float ms = 0.f;
+        MCXG_TRY(cudaEventElapsedTime(&ms, s->e0, s->e1));
+        *kernel_ms = ms;
+    }
+    return MCXG_OK;
+}
+
+int mcxg_get_energy(mcxg_session* s, double* escaped, double* launched) {
+    if (!s || !s->has_seeds) {
+        return MCXG_ERR_STATE;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    energy_partials<<<kRedBlocks, kRedThreads, 0, s->st>>>(s->d_energy, s->kp.nthread, s->d_red);
+    energy_final<<<1, 32, 0, s->st>>>(s->d_red, kRedBlocks);
+    double h[2];
+    MCXG_TRY(cudaMemcpyAsync(h, s->d_red + 2 * kRedBlocks, sizeof(h), cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    if (escaped) {
+        *escaped = h[0];
+    }
+    if (launched) {
+        *launched = h[1];
+    }
+    return MCXG_OK;
+}
+
+int mcxg_get_thread_energy(mcxg_session* s, float* out) {
+    if (!s || !out || !s->has_seeds) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_energy, sizeof(float2) * s->kp.nthread, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_get_field(mcxg_session* s, float* out, double scale) {
+    if (!s || !out || !s->has_problem) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    size_t n = s->kp.fieldlen;
+    int rc = ensure((double**)&s->d_out, &s->out_cap, n);
+    if (rc) {
+        return rc;
+    }
+    field_merge_f32<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, scale, (float*)s->d_out);
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_get_field_f64(mcxg_session* s, double* out) {
+    if (!s || !out || !s->has_problem) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    size_t n = s->kp.fieldlen;
+    int rc = ensure((double**)&s->d_out, &s->out_cap, n);
+    if (rc) {
+        return rc;
+    }
+    field_merge_f64<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, (double*)s->d_out);
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_get_detected(mcxg_session* s, float* detp, uint64_t* seeds, uint32_t* detected) {
+    if (!s || !s->has_problem) {
+        return MCXG_ERR_STATE;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    unsigned int cnt = 0;
+    MCXG_TRY(cudaMemcpyAsync(&cnt, s->d_words, sizeof(cnt), cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    if (detected) {
+        *detected = cnt;
+    }
+    if (!s->kp.savedet) {
+        return MCXG_OK;
+    }
+    size_t saved = cnt < s->kp.maxdetphoton ? cnt : s->kp.maxdetphoton;
+    if (detp && saved && s->kp.reclen) {
+        MCXG_TRY(cudaMemcpyAsync(detp, s->d_detp, sizeof(float) * saved * s->kp.reclen, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (seeds && saved && s->kp.issaveseed) {
+        MCXG_TRY(cudaMemcpyAsync(seeds, s->d_detseed, sizeof(uint64_t) * 2 * saved, cudaMemcpyDeviceToHost, s->st));
+    }
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_get_counters(mcxg_session* s, uint64_t counters[5], uint32_t status[2]) {
+    if (!s) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    unsigned long long ev[8];
+    unsigned int w[8];
+    MCXG_TRY(cudaMemcpyAsync(ev, s->d_events, sizeof(ev), cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaMemcpyAsync(w, s->d_words, sizeof(w), cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    if (counters) {
+        for (int i = 0; i < 5; i++) {
+            counters[i] = ev[i];
+        }
+    }
+    if (status) {
+        status[0] = w[2];
+        status[1] = w[3];
+    }
+    return MCXG_OK;
+}
+
+int mcxg_get_launch(mcxg_session* s, int* grid, int* block, int* regs) {
+    if (!s) {
+        return MCXG_ERR_ARG;
+    }
+    if (grid) {
+        *grid = s->grid;
+    }
+    if (block) {
+        *block = s->block;
+    }
+    if (regs) {
+        *regs = s->regs;
+    }
+    return MCXG_OK;
+}
+
+}  // extern "C"

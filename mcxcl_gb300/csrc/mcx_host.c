@@ -1,0 +1,979 @@
+/*
+ * mcx_host.c -- the C host driver of the GB300 transport path.
+ *
+ * Drop-in for the reference's simulation driver mcx_run_simulation
+ * (src/mcx_host.cpp:438-1849) and the parts of its configuration layer the
+ * path needs (src/mcx_utils.c: mcx_initcfg 203-366, mcx_clearcfg 368-476,
+ * mcx_validatecfg 1822-1964, mcx_preprocess 1521-1809, mcx_maskdet
+ * 4085-4198, mcx_normalize 1208-1218).  It keeps the reference's
+ * observable semantics -- glibc rand() seeding per reference thread, the
+ * float arithmetic of the photon split, the energy bookkeeping and the
+ * normalisation factors -- and calls CUDA only through the mcxg_* layer.
+ *
+ * What is new: a persistent device session cached per GPU (buffers are reused
+ * across calls), the label volume packed to one byte per voxel when every
+ * label fits in seven bits, and the FP64 energy sums and field normalisation
+ * done on the GPU.
+ */
+#define _GNU_SOURCE
+#include <math.h>
+#include <setjmp.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "../../include/mcx_gb300.h"
+#include "mcx_kparams.h"
+
+#define H_EPS        1e-10f        /* mcx_const.h:30 */
+#define H_VERY_BIG   1e10f         /* mcx_const.h:35 */
+#define R_C0         3.335640951981520e-12f
+#define DET_MASK     0x80000000u
+#define MED_MASK     0x7FFFFFFFu
+
+/* ------------------------------------------------------------------ errors */
+
+static __thread jmp_buf* g_jump = NULL;
+static __thread Config* g_errcfg = NULL;
+
+void mcx_error(const int id, const char* msg, const char* file, const int linenum) {
+    if (g_jump && g_errcfg) {
+        g_errcfg->errorcode = id ? id : -1;
+        snprintf(g_errcfg->errormsg, sizeof(g_errcfg->errormsg), "%s", msg);
+        longjmp(*g_jump, 1);
+    }
+    fprintf(stderr, "\nMCX ERROR(%d):%s in unit %s:%d\n", id, msg, file, linenum);
+    exit(id);
+}
+
+#define MCX_ERROR(id, msg) mcx_error((id), (msg), __FILE__, __LINE__)
+
+int mcx_last_error(const Config* cfg, const char** msg) {
+    if (msg) {
+        *msg = cfg->errormsg;
+    }
+    return cfg->errorcode;
+}
+
+const char* mcx_version(void) {
+    return MCX_GB300_VERSION;
+}
+
+/* library mode: a failing public call returns instead of exiting */
+#define MCX_ENTER(cfg)                                   \
+    jmp_buf _jb;                                         \
+    jmp_buf* _prev_jump = g_jump;                        \
+    Config* _prev_cfg = g_errcfg;                        \
+    (cfg)->errorcode = 0;                                \
+    (cfg)->errormsg[0] = '\0';                           \
+    if ((cfg)->parentid != mpStandalone) {               \
+        g_jump = &_jb;                                   \
+        g_errcfg = (cfg);                                \
+        if (setjmp(_jb)) {                               \
+            g_jump = _prev_jump;                         \
+            g_errcfg = _prev_cfg;                        \
+            return;                                      \
+        }                                                \
+    }
+
+#define MCX_LEAVE()          \
+    do {                     \
+        g_jump = _prev_jump; \
+        g_errcfg = _prev_cfg; \
+    } while (0)
+
+/* ------------------------------------------------------------------ config */
+
+void mcx_initcfg(Config* cfg) {
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->tstart = 0.f;
+    cfg->tend = 5e-9f;
+    cfg->tstep = 5e-9f;
+    cfg->mediabyte = 1;
+    cfg->steps.x = cfg->steps.y = cfg->steps.z = 1.f;
+    cfg->nblocksize = 64;
+    cfg->nthread = (1 << 14);
+    cfg->seed = 0x623F9A9E;
+    cfg->isreflect = 1;
+    cfg->isnormalized = 1;
+    cfg->issavedet = 1;
+    cfg->respin = 1;
+    cfg->issave2pt = 1;
+    cfg->unitinmm = 1.f;
+    cfg->flog = stdout;
+    cfg->savedetflag = 0x5;
+    cfg->his.savedetflag = cfg->savedetflag;
+    cfg->gscatter = 1000000000u;
+    cfg->maxvoidstep = 1000;
+    cfg->voidtime = 1;
+    cfg->maxdetphoton = 1000000;
+    cfg->autopilot = 1;
+    cfg->srcnum = 1;
+    cfg->deviceid[0] = '1';
+    cfg->isatomic = 1;
+    cfg->srcpos.w = 1.f;
+    memcpy(cfg->his.magic, "MCXH", 4);
+    cfg->his.version = 1;
+    cfg->his.unitinmm = 1.f;
+    cfg->his.normalizer = 1.f;
+    cfg->his.srcnum = 1;
+    cfg->his.respin = 1;
+    cfg->parentid = mpStandalone;
+    cfg->outputtype = otFlux;
+}
+
+void mcx_clearcfg(Config* cfg) {
+    free(cfg->prop);
+    free(cfg->detpos);
+    free(cfg->vol);
+    free(cfg->srcpattern);
+    free(cfg->exportfield);
+    free(cfg->exportdetected);
+    free(cfg->seeddata);
+    free(cfg->invcdf);
+    free(cfg->angleinvcdf);
+    free(cfg->srcdata);
+    free(cfg->exportenergy);
+    cfg->exportenergy = NULL;
+    cfg->prop = NULL;
+    cfg->detpos = NULL;
+    cfg->vol = NULL;
+    cfg->srcpattern = NULL;
+    cfg->exportfield = NULL;
+    cfg->exportdetected = NULL;
+    cfg->seeddata = NULL;
+    cfg->invcdf = NULL;
+    cfg->angleinvcdf = NULL;
+    cfg->srcdata = NULL;
+    cfg->medianum = 0;
+    cfg->detnum = 0;
+    cfg->extrasrclen = 0;
+}
+
+void mcx_normalize(float field[], float scale, int fieldlen, int option, int pidx, int srcnum) {
+    for (int i = 0; i < fieldlen; i++) {
+        if (option == 2 && field[i * srcnum + pidx] < 0.f) {
+            continue;
+        }
+        field[i * srcnum + pidx] *= scale;
+    }
+}
+
+unsigned int mcx_detreclen(const Config* cfg) {
+    unsigned int f = cfg->savedetflag;
+    unsigned int partial = (cfg->medianum - 1) * (SAVE_NSCAT(f) + SAVE_PPATH(f) + SAVE_MOM(f));
+    return partial + SAVE_DETID(f) + 3 * (SAVE_PEXIT(f) + SAVE_VEXIT(f)) + SAVE_W0(f);
+}
+
+/* mcx_lookupindex (mcx_utils.c:5292-5305): face conditions "_ramc", detector flags "01" */
+static int lookup_index(char* key, const char* table) {
+    for (int i = 0; table[i]; i++) {
+        char c = *key;
+        if (c >= 'A' && c <= 'Z') {
+            c = (char)(c - 'A' + 'a');
+        }
+        if (c == table[i]) {
+            *key = (char)i;
+            return 0;
+        }
+    }
+    return 1;
+}
+
+/* mcx_maskdet (mcx_utils.c:4085-4198): mark the boundary voxels within a
+   detector's reach with the detector bit */
+static void maskdet(Config* cfg) {
+    unsigned int nx = cfg->dim.x, ny = cfg->dim.y, nz = cfg->dim.z;
+    unsigned int dx = nx + 2, dy = ny + 2, dz = nz + 2;
+    int isonecube = (nx == 1) && (ny == 1) && (nz == 1);
+    static const float corners[8][3] = {{0.f, 0.f, 0.f}, {1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f},
+        {1.f, 1.f, 0.f}, {1.f, 0.f, 1.f}, {0.f, 1.f, 1.f}, {1.f, 1.f, 1.f}
+    };
+    uint32_t* pad = (uint32_t*)calloc((size_t)dx * dy * dz, sizeof(uint32_t));
+    if (!pad) {
+        MCX_ERROR(-2, "out of host memory while masking detectors");
+    }
+    for (unsigned int zi = 1; zi <= nz; zi++) {
+        for (unsigned int yi = 1; yi <= ny; yi++) {
+            memcpy(pad + (size_t)zi * dy * dx + yi * dx + 1, cfg->vol + (size_t)(zi - 1) * ny * nx + (yi - 1) * nx,
+                   nx * sizeof(uint32_t));
+        }
+    }
+    for (unsigned int d = 0; d < cfg->detnum; d++) {
+        const mcx_float4 dp = cfg->detpos[d];
+        float d2max = (dp.w + 1.7321f) * (dp.w + 1.7321f);
+        unsigned int count = 0;
+        for (float z = -dp.w - 1.f; z <= dp.w + 1.f; z += 0.5f) {
+            float iz = z + dp.z;
+            for (float y = -dp.w - 1.f; y <= dp.w + 1.f; y += 0.5f) {
+                float iy = y + dp.y;
+                for (float x = -dp.w - 1.f; x <= dp.w + 1.f; x += 0.5f) {
+                    float ix = x + dp.x;
+                    if (iz < 0 || ix < 0 || iy < 0 || ix >= nx || iy >= ny || iz >= nz ||
+                            x * x + y * y + z * z > (dp.w + 1.f) * (dp.w + 1.f)) {
+                        continue;
+                    }
+                    float mind2 = H_VERY_BIG;
+                    for (int c = 0; c < 8; c++) {
+                        float rx = (int)ix - dp.x + corners[c][0];
+                        float ry = (int)iy - dp.y + corners[c][1];
+                        float rz = (int)iz - dp.z + corners[c][2];
+                        float d2 = rx * rx + ry * ry + rz * rz;
+                        if (d2 > d2max) {
+                            mind2 = H_VERY_BIG;
+                            break;
+                        }
+                        if (d2 < mind2) {
+                            mind2 = d2;
+                        }
+                    }
+                    if (mind2 == H_VERY_BIG ||
+                            mind2 >= (dp.w + 0.5f * (1.f + isonecube)) * (dp.w + 0.5f * (1.f + isonecube))) {
+                        continue;
+                    }
+                    size_t i = ((size_t)(int)(iz + 1.f) * dy * dx + (size_t)(int)(iy + 1.f) * dx + (size_t)(int)(ix + 1.f));
+                    size_t dxy = (size_t)dy * dx;
+                    if (pad[i] &&
+                            !(pad[i + 1] && pad[i - 1] && pad[i + dx] && pad[i - dx] && pad[i + dxy] && pad[i - dxy] &&
+                              pad[i + dx + 1] && pad[i + dx - 1] && pad[i - dx + 1] && pad[i - dx - 1] &&
+                              pad[i + dxy + 1] && pad[i + dxy - 1] && pad[i - dxy + 1] && pad[i - dxy - 1] &&
+                              pad[i + dxy + dx] && pad[i + dxy - dx] && pad[i - dxy + dx] && pad[i - dxy - dx] &&
+                              pad[i + dxy + dx + 1] && pad[i + dxy + dx - 1] && pad[i + dxy - dx + 1] &&
+                              pad[i + dxy - dx - 1] && pad[i - dxy + dx + 1] && pad[i - dxy + dx - 1] &&
+                              pad[i - dxy - dx + 1] && pad[i - dxy - dx - 1])) {
+                        cfg->vol[(int)iz * ny * nx + (int)iy * nx + (int)ix] |= DET_MASK;
+                        count++;
+                    }
+                }
+            }
+        }
+        if (count == 0 && cfg->flog) {
+            fprintf(cfg->flog, "MCX WARNING: detector %u is not located on an interface, please check coordinates.\n",
+                    d + 1);
+        }
+    }
+    free(pad);
+}
+
+/* row-major (C) to column-major volume, mcx_convertrow2col */
+static void row2col(Config* cfg) {
+    size_t nx = cfg->dim.x, ny = cfg->dim.y, nz = cfg->dim.z;
+    uint32_t* out = (uint32_t*)malloc(nx * ny * nz * sizeof(uint32_t));
+    if (!out) {
+        MCX_ERROR(-2, "out of host memory");
+    }
+    for (size_t x = 0; x < nx; x++) {
+        for (size_t y = 0; y < ny; y++) {
+            for (size_t z = 0; z < nz; z++) {
+                out[z * ny * nx + y * nx + x] = cfg->vol[x * ny * nz + y * nz + z];
+            }
+        }
+    }
+    free(cfg->vol);
+    cfg->vol = out;
+}
+
+static void point_src_voxel(const Config* cfg, mcx_float4 pos, mcx_float4* p2) {
+    union {
+        float f;
+        uint32_t u;
+    } f2i;
+    if (pos.x < 0.f || pos.y < 0.f || pos.z < 0.f || pos.x >= cfg->dim.x || pos.y >= cfg->dim.y || pos.z >= cfg->dim.z) {
+        f2i.u = 0;
+        p2->z = f2i.f;
+        p2->w = f2i.f;
+    } else {
+        uint32_t idx = (uint32_t)((int)(floorf(pos.z)) * (cfg->dim.y * cfg->dim.x) + (int)(floorf(pos.y)) * cfg->dim.x +
+                                  (int)(floorf(pos.x)));
+        f2i.u = idx;
+        p2->z = f2i.f;
+        f2i.u = cfg->vol[idx] & MED_MASK;
+        p2->w = f2i.f;
+    }
+}
+
+/* mcx_preprocess, mcx_utils.c:1521-1809 (the parts the transport path reads) */
+static void preprocess(Config* cfg) {
+    int isbcdet = 0;
+    double tmp = sqrt((double)cfg->srcdir.x * cfg->srcdir.x + (double)cfg->srcdir.y * cfg->srcdir.y +
+                      (double)cfg->srcdir.z * cfg->srcdir.z);
+    if (tmp < H_EPS) {
+        MCX_ERROR(-4, "source initial direction vector can not have a length of 0");
+    }
+    tmp = 1.f / tmp;
+    cfg->srcdir.x *= tmp;
+    cfg->srcdir.y *= tmp;
+    cfg->srcdir.z *= tmp;
+
+    for (int i = 0; i < 6; i++) {
+        if (cfg->bc[i] && lookup_index(cfg->bc + i, "_ramc")) {
+            MCX_ERROR(-4, "unknown boundary condition specifier");
+        }
+    }
+    for (int i = 6; i < 12; i++) {
+        if (cfg->bc[i] && lookup_index(cfg->bc + i, "01")) {
+            MCX_ERROR(-4, "unknown boundary detection flags");
+        }
+        if (cfg->bc[i]) {
+            isbcdet = 1;
+        }
+    }
+    if (cfg->medianum == 0) {
+        MCX_ERROR(-4, "you must define the 'prop' field in the input structure");
+    }
+    if (cfg->dim.x == 0 || cfg->dim.y == 0 || cfg->dim.z == 0 || !cfg->vol) {
+        MCX_ERROR(-4, "the 'vol' field in the input structure can not be empty");
+    }
+    if ((cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D) && cfg->srcpattern == NULL) {
+        MCX_ERROR(-4, "the 'srcpattern' field can not be empty when your 'srctype' is 'pattern'");
+    }
+    if (cfg->steps.x != 1.f && cfg->unitinmm == 1.f) {
+        cfg->unitinmm = cfg->steps.x;
+    }
+    if (cfg->unitinmm != 1.f) {
+        cfg->steps.x = cfg->steps.y = cfg->steps.z = cfg->unitinmm;
+        for (unsigned int i = 1; i < cfg->medianum; i++) {
+            cfg->prop[i].mus *= cfg->unitinmm;
+            cfg->prop[i].mua *= cfg->unitinmm;
+        }
+    }
+    if (cfg->isrowmajor) {
+        row2col(cfg);
+        cfg->isrowmajor = 0;
+    }
+    if (cfg->issavedet && cfg->detnum == 0 && isbcdet == 0) {
+        cfg->issavedet = 0;
+    }
+    if (cfg->issavedet == 0) {
+        cfg->issaveexit = 0;
+        cfg->ismomentum = 0;
+        cfg->savedetflag = 0;
+    }
+    if (cfg->respin == 0) {
+        MCX_ERROR(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
+    }
+    if (cfg->respin < 0) {
+        MCX_ERROR(-1, "negative respin (photon divisions) is not supported by this build");
+    }
+    for (unsigned int i = 0; i < cfg->medianum; i++) {
+        if (cfg->prop[i].mus == 0.f) {
+            cfg->prop[i].mus = H_EPS;
+        }
+    }
+    if (cfg->srcpos.w == 0.f) {
+        cfg->srcpos.w = 1.f;
+    }
+    if (cfg->extrasrclen) {
+        if (cfg->srcnum > 1) {
+            MCX_ERROR(-4, "simulating multiple sources currently can not be used with photon-sharing");
+        }
+        if (cfg->srcid > (int)cfg->extrasrclen + 1) {
+            MCX_ERROR(-4, "srcid exceeds total defined source count");
+        }
+        for (unsigned int i = 0; i < cfg->extrasrclen; i++) {
+            if (cfg->srcdata[i].srcpos.w == 0.f) {
+                cfg->srcdata[i].srcpos.w = 1.f;
+            }
+        }
+    }
+    if (cfg->srcnum > 1) {
+        MCX_ERROR(-4, "photon sharing (srcnum > 1) is not supported by this build");
+    }
+    size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+    if (cfg->mediabyte <= 4) {
+        unsigned int maxlabel = 0;
+        for (size_t i = 0; i < nvox; i++) {
+            unsigned int l = cfg->vol[i] & MED_MASK;
+            maxlabel = l > maxlabel ? l : maxlabel;
+        }
+        if (cfg->medianum <= maxlabel) {
+            MCX_ERROR(-4, "input media optical properties are less than the labels in the volume");
+        }
+    } else if (cfg->mediabyte != MEDIA_MUA_FLOAT) {
+        MCX_ERROR(-4, "this build supports label volumes (mediabyte 1/2/4) and float mua (101)");
+    }
+    if (cfg->srctype <= MCX_SRC_CONE || cfg->srctype == MCX_SRC_ARCSINE || cfg->srctype == MCX_SRC_ZGAUSSIAN) {
+        point_src_voxel(cfg, cfg->srcpos, &cfg->srcparam2);
+        for (unsigned int i = 0; i < cfg->extrasrclen; i++) {
+            point_src_voxel(cfg, cfg->srcdata[i].srcpos, &cfg->srcdata[i].srcparam2);
+        }
+    }
+    if (cfg->issavedet && cfg->mediabyte <= 4) {
+        maskdet(cfg);
+    }
+    for (int i = 0; i < MAX_DEVICE; i++) {
+        if (cfg->deviceid[i] == '0') {
+            cfg->deviceid[i] = '\0';
+        }
+    }
+    if (cfg->mediabyte == MEDIA_MUA_FLOAT && cfg->medianum < 2) {
+        MCX_ERROR(-4, "the 'prop' field must contain at least 2 rows for the requested media format");
+    }
+    if (cfg->ismomentum) {
+        cfg->savedetflag |= 0x8;
+    }
+    if (cfg->issaveexit) {
+        cfg->savedetflag |= 0x10 | 0x20;
+    }
+    cfg->savedetflag &= ~0x80u;
+    if (cfg->issavedet && cfg->savedetflag == 0) {
+        cfg->savedetflag = 0x5;
+    }
+    if (cfg->mediabyte >= 100 && cfg->savedetflag) {
+        cfg->savedetflag &= ~(0x2u | 0x4u | 0x8u);
+    }
+    if (cfg->issaveref > 1) {
+        MCX_ERROR(-4, "issaveref > 1 (per-voxel exit partial paths) is not supported by this build");
+    }
+}
+
+void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte) {
+    MCX_ENTER(cfg);
+    (void)dimdetps;
+    (void)seedbyte;
+    if (cfg->seed == SEED_FROM_FILE || detps) {
+        MCX_ERROR(-6, "photon replay is not part of this build");
+    }
+    if (!cfg->issrcfrom0) {
+        cfg->srcpos.x--;
+        cfg->srcpos.y--;
+        cfg->srcpos.z--;
+        for (unsigned int i = 0; i < cfg->extrasrclen; i++) {
+            cfg->srcdata[i].srcpos.x--;
+            cfg->srcdata[i].srcpos.y--;
+            cfg->srcdata[i].srcpos.z--;
+        }
+    }
+    if (cfg->tstart > cfg->tend || cfg->tstep == 0.f) {
+        MCX_ERROR(-6, "incorrect time gate settings");
+    }
+    if (fabs(cfg->srcdir.x * cfg->srcdir.x + cfg->srcdir.y * cfg->srcdir.y + cfg->srcdir.z * cfg->srcdir.z - 1.f) > 1e-5) {
+        MCX_ERROR(-6, "field 'srcdir' must be a unitary vector");
+    }
+    if (cfg->steps.x == 0.f || cfg->steps.y == 0.f || cfg->steps.z == 0.f) {
+        MCX_ERROR(-6, "field 'steps' can not have zero elements");
+    }
+    if (cfg->tend <= cfg->tstart) {
+        MCX_ERROR(-6, "field 'tend' must be greater than field 'tstart'");
+    }
+    int gates = (int)((cfg->tend - cfg->tstart) / cfg->tstep + 0.5);
+    if (cfg->maxgate > (unsigned int)gates) {
+        cfg->maxgate = gates;
+    }
+    if (cfg->outputtype == otJacobian || cfg->outputtype == otWP || cfg->outputtype == otDCS || cfg->outputtype == otRF) {
+        MCX_ERROR(-6, "Jacobian output is only valid in the reply mode. Please define cfg.seed");
+    }
+    if (cfg->outputtype != otFlux && cfg->outputtype != otFluence && cfg->outputtype != otEnergy && cfg->outputtype != otL) {
+        MCX_ERROR(-6, "unsupported output type");
+    }
+    if (!cfg->issrcfrom0) {
+        for (unsigned int i = 0; i < cfg->detnum; i++) {
+            cfg->detpos[i].x--;
+            cfg->detpos[i].y--;
+            cfg->detpos[i].z--;
+        }
+    }
+    preprocess(cfg);
+    cfg->his.maxmedia = cfg->medianum - 1;
+    cfg->his.detnum = cfg->detnum;
+    cfg->his.srcnum = cfg->srcnum;
+    cfg->his.colcount = mcx_detreclen(cfg);
+    cfg->his.savedetflag = cfg->savedetflag;
+    cfg->his.totalsource = ((cfg->srcid <= 0) ? cfg->extrasrclen + 1 : 1);
+    MCX_LEAVE();
+}
+
+/* ----------------------------------------------------------------- devices */
+
+/* mcx_nv_corecount (mcx_host.cpp:224-240) */
+static int nv_corecount(int v1, int v2) {
+    int v = v1 * 10 + v2;
+    if (v < 20) {
+        return 8;
+    } else if (v < 21) {
+        return 32;
+    } else if (v < 30) {
+        return 48;
+    } else if (v < 50) {
+        return 192;
+    } else if (v < 60 || v == 61 || v >= 89) {
+        return 128;
+    }
+    return 64;
+}
+
+int mcx_list_gpu(Config* cfg, unsigned int* activedev, GPUInfo** info) {
+    int n = 0;
+    unsigned int act = 0;
+    *info = NULL;
+    if (activedev) {
+        *activedev = 0;
+    }
+    if (mcxg_device_count(&n) != MCXG_OK || n <= 0) {
+        return 0;
+    }
+    *info = (GPUInfo*)calloc((size_t)n, sizeof(GPUInfo));
+    for (int i = 0; i < n; i++) {
+        mcxg_devinfo d;
+        if (mcxg_device_info(i, &d) != MCXG_OK) {
+            continue;
+        }
+        int selected = (i < MAX_DEVICE && cfg->deviceid[i] == '1');
+        if (!selected && activedev) {
+            continue;
+        }
+        GPUInfo* g = (*info) + act;
+        memset(g, 0, sizeof(*g));
+        strncpy(g->name, d.name, MAX_SESSION_LENGTH - 1);
+        g->id = i + 1;
+        g->devcount = n;
+        g->major = d.major;
+        g->minor = d.minor;
+        g->globalmem = d.globalmem;
+        g->constmem = d.constmem;
+        g->sharedmem = d.sharedmem_per_block;
+        g->regcount = d.regs_per_block;
+        g->clock = d.clock_khz / 1000;
+        g->sm = d.sm;
+        g->core = d.sm * nv_corecount(d.major, d.minor);
+        g->autoblock = 64;
+        g->autothread = g->autoblock * (size_t)g->core;
+        g->maxgate = cfg->maxgate;
+        g->maxmpthread = d.max_threads_per_sm;
+        g->vendor = 1;
+        if (cfg->isgpuinfo && cfg->flog) {
+            fprintf(cfg->flog, "============ GPU device ID %d [%d of %d]: %s  ============\n", i, i + 1, n, g->name);
+            fprintf(cfg->flog, " Compute units   :\t%d core(s)\n", g->sm);
+            fprintf(cfg->flog, " Global memory   :\t%.0f B\n", (double)g->globalmem);
+            fprintf(cfg->flog, " Local memory    :\t%.0f B\n", (double)g->sharedmem);
+            fprintf(cfg->flog, " Constant memory :\t%.0f B\n", (double)g->constmem);
+            fprintf(cfg->flog, " Clock speed     :\t%d MHz\n", g->clock);
+            fprintf(cfg->flog, " Compute Capacity:\t%d.%d\n", g->major, g->minor);
+            fprintf(cfg->flog, " Stream Processor:\t%d\n", g->core);
+        }
+        act++;
+    }
+    if (activedev) {
+        *activedev = act;
+    }
+    return (int)act;
+}
+
+void mcx_cleargpuinfo(GPUInfo** info) {
+    if (info && *info) {
+        free(*info);
+        *info = NULL;
+    }
+}
+
+/* one cached device session per GPU; buffers are reused across calls */
+static mcxg_session* g_sessions[MAX_DEVICE];
+
+static mcxg_session* session_for(int device) {
+    if (device < 0 || device >= MAX_DEVICE) {
+        return NULL;
+    }
+    if (!g_sessions[device]) {
+        if (mcxg_create(device, &g_sessions[device]) != MCXG_OK) {
+            g_sessions[device] = NULL;
+        }
+    }
+    return g_sessions[device];
+}
+
+void mcx_release_sessions(void) {
+    for (int i = 0; i < MAX_DEVICE; i++) {
+        if (g_sessions[i]) {
+            mcxg_destroy(g_sessions[i]);
+            g_sessions[i] = NULL;
+        }
+    }
+}
+
+static void device_check(int rc, const char* what) {
+    if (rc != MCXG_OK) {
+        char msg[256];
+        snprintf(msg, sizeof(msg), "%s failed: %s", what, mcxg_error_string(rc));
+        MCX_ERROR(-(100 + rc), msg);
+    }
+}
+
+/* --------------------------------------------------------------- the driver */
+
+void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
+    (void)fluence;
+    (void)totalenergy;
+    GPUInfo* gpu = NULL;
+    /* temporaries live in thread-local slots so the library-mode error path
+       (longjmp back to this frame) can free them */
+    static __thread void* tmp[5];
+    for (int i = 0; i < 5; i++) {
+        free(tmp[i]);
+        tmp[i] = NULL;
+    }
+#define packed   (*(uint8_t**)&tmp[0])
+#define seeds    (*(uint32_t**)&tmp[1])
+#define detbuf   (*(float**)&tmp[2])
+#define seedbuf  (*(uint64_t**)&tmp[3])
+#define fieldtmp (*(float**)&tmp[4])
+    MCX_ENTER(cfg);
+
+    unsigned int partialdata = (cfg->medianum - 1) *
+                               (SAVE_NSCAT(cfg->savedetflag) + SAVE_PPATH(cfg->savedetflag) + SAVE_MOM(cfg->savedetflag));
+    unsigned int hostdetreclen = mcx_detreclen(cfg);
+    unsigned int is2d = (cfg->dim.x == 1 ? 1 : (cfg->dim.y == 1 ? 2 : (cfg->dim.z == 1 ? 3 : 0)));
+    if (is2d) {
+        is2d = is2d * (((cfg->dim.x > 1) + (cfg->dim.y > 1) + (cfg->dim.z > 1)) == 2);
+    }
+    unsigned int workdev = 0;
+    mcx_list_gpu(cfg, &workdev, &gpu);
+    if (workdev == 0) {
+        free(gpu);
+        MCX_ERROR(-99, "Specified GPU does not exist");
+    }
+    /* one GPU per call: the first selected device runs every photon */
+    GPUInfo g = gpu[0];
+    free(gpu);
+    gpu = NULL;
+    int device = g.id - 1;
+
+    size_t autothread, autoblock;
+    if (cfg->autopilot) {
+        /* the reference's NVIDIA compute >= 6 choice (mcx_host.cpp:617-620) */
+        autoblock = 64;
+        autothread = autoblock * 64 * (size_t)g.sm;
+    } else {
+        autothread = cfg->nthread;
+        autoblock = cfg->nblocksize ? cfg->nblocksize : 64;
+    }
+    if (autothread % autoblock) {
+        autothread = (autothread / autoblock) * autoblock;
+    }
+    if (autothread == 0) {
+        MCX_ERROR(-1, "thread number must be at least the block size");
+    }
+    if (is2d) {
+        float* vec = &(cfg->srcdir.x);
+        if (fabsf(vec[is2d - 1]) > H_EPS) {
+            MCX_ERROR(-1, "input domain is 2D, the initial direction can not have non-zero value in the singular dimension");
+        }
+    }
+    cfg->maxgate = (unsigned int)(int)((cfg->tend - cfg->tstart) / cfg->tstep + 0.5);
+    size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+    size_t mult = (cfg->extrasrclen && cfg->srcid < 0) ? (cfg->extrasrclen + 1) : 1;
+    size_t fieldlen = nvox * cfg->maxgate * mult;
+    if (fieldlen > 0xFFFFFFFFull || nvox > 0x7FFFFFFFull) {
+        MCX_ERROR(-1, "volume x gates too large for 32-bit field indices");
+    }
+
+    float fullload = 0.f;
+    for (unsigned int i = 0; i < workdev && i < MAX_DEVICE; i++) {
+        fullload += cfg->workload[i];
+    }
+    float workload0 = cfg->workload[0];
+    if (fullload < H_EPS) {
+        workload0 = (float)g.core;
+        fullload = (float)g.core;
+    }
+
+    /* kernel constant block (mcx_host.cpp:507-524, 674-693) */
+    mcxg_kparams kp;
+    memset(&kp, 0, sizeof(kp));
+    kp.srcpos = (mcxg_float4) {cfg->srcpos.x, cfg->srcpos.y, cfg->srcpos.z, cfg->srcpos.w};
+    kp.srcdir = (mcxg_float4) {cfg->srcdir.x, cfg->srcdir.y, cfg->srcdir.z, cfg->srcdir.w};
+    kp.srcparam1 = (mcxg_float4) {cfg->srcparam1.x, cfg->srcparam1.y, cfg->srcparam1.z, cfg->srcparam1.w};
+    kp.srcparam2 = (mcxg_float4) {cfg->srcparam2.x, cfg->srcparam2.y, cfg->srcparam2.z, cfg->srcparam2.w};
+    kp.maxidx = (mcxg_float4) {(float)cfg->dim.x, (float)cfg->dim.y, (float)cfg->dim.z, 0.f};
+    kp.dimx = cfg->dim.x;
+    kp.dimxy = cfg->dim.x * cfg->dim.y;
+    kp.nvox = (uint32_t)nvox;
+    kp.fieldlen = (uint32_t)fieldlen;
+    kp.twin0 = cfg->tstart;
+    kp.twin1 = cfg->tstart + cfg->tstep * cfg->maxgate;
+    float minstep = fminf(fminf(cfg->steps.x, cfg->steps.y), cfg->steps.z);
+    kp.oneoverc0 = R_C0 * cfg->unitinmm;
+    kp.Rtstep = 1.f / cfg->tstep;
+    kp.minenergy = cfg->minenergy;
+    kp.minaccumtime = minstep * R_C0 * cfg->unitinmm;
+    kp.doreflect = (uint32_t)cfg->isreflect;
+    {
+        const char allabsorb[6] = {bcAbsorb, bcAbsorb, bcAbsorb, bcAbsorb, bcAbsorb, bcAbsorb};
+        const char allunknown[6] = {0, 0, 0, 0, 0, 0};
+        int refl = cfg->isreflect || (memcmp(cfg->bc, allabsorb, 6) && memcmp(cfg->bc, allunknown, 6));
+        for (int i = 0; i < 6; i++) {
+            if (cfg->bc[i] == bcReflect || cfg->bc[i] == bcMirror) {
+                refl = 1;
+            }
+        }
+        kp.dorefl_compiled = (uint32_t)refl;
+    }
+    kp.save2pt = cfg->issave2pt ? 1 : 0;
+    kp.savedet = (uint32_t)cfg->issavedet;
+    kp.maxdetphoton = cfg->maxdetphoton;
+    kp.maxmedia = cfg->medianum - 1;
+    kp.medianum = cfg->medianum;
+    kp.detnum = cfg->detnum;
+    kp.voidtime = (uint32_t)cfg->voidtime;
+    kp.srctype = (uint32_t)cfg->srctype;
+    kp.maxvoidstep = (uint32_t)cfg->maxvoidstep;
+    kp.issaveseed = cfg->issaveseed > 0;
+    kp.issaveref = (uint32_t)cfg->issaveref;
+    kp.isspecular = cfg->isspecular > 0;
+    kp.maxgate = cfg->maxgate;
+    kp.outputtype = (uint32_t)cfg->outputtype;
+    kp.savedetflag = cfg->savedetflag;
+    kp.reclen = hostdetreclen;
+    kp.partialdata = partialdata;
+    kp.mediaformat = cfg->mediabyte;
+    kp.gscatter = cfg->gscatter;
+    kp.is2d = is2d;
+    kp.nphase = cfg->nphase;
+    kp.nangle = cfg->nangle;
+    kp.extrasrclen = cfg->extrasrclen;
+    kp.srcid = cfg->srcid;
+    kp.nthread = (uint32_t)autothread;
+    for (int i = 0; i < 12; i++) {
+        kp.bc[i] = (uint8_t)cfg->bc[i];
+    }
+
+    /* the label volume: one byte per voxel (label | detector bit << 7) when
+       every label fits in seven bits, else the reference's 32-bit words */
+    uint32_t mediaword = 4;
+    if (cfg->mediabyte <= 4) {
+        int fits = cfg->medianum <= 128;
+        if (fits) {
+            packed = (uint8_t*)malloc(nvox);
+            if (!packed) {
+                MCX_ERROR(-2, "out of host memory");
+            }
+            for (size_t i = 0; i < nvox; i++) {
+                uint32_t v = cfg->vol[i];
+                packed[i] = (uint8_t)((v & 0x7Fu) | ((v & DET_MASK) ? 0x80u : 0u));
+            }
+            mediaword = 1;
+        }
+    }
+
+    mcxg_session* s = session_for(device);
+    if (!s) {
+        free(packed);
+        MCX_ERROR(-99, "failed to open a CUDA session on the selected GPU");
+    }
+    int rc = mcxg_set_problem(s, &kp, sizeof(kp), mediaword == 1 ? (const void*)packed : (const void*)cfg->vol, mediaword,
+                              (const float*)cfg->prop, (const float*)cfg->detpos, (const float*)cfg->srcdata,
+                              cfg->invcdf, cfg->angleinvcdf, cfg->srcpattern,
+                              cfg->srctype == MCX_SRC_PATTERN ? (size_t)((int)(cfg->srcparam1.w * cfg->srcparam2.w) * cfg->srcnum)
+                              : (cfg->srctype == MCX_SRC_PATTERN3D ?
+                                 (size_t)((int)(cfg->srcparam1.x * cfg->srcparam1.y * cfg->srcparam1.z) * cfg->srcnum) : 0));
+    free(packed);
+    packed = NULL;
+    device_check(rc, "uploading the problem");
+
+    /* seeds: srand(seed) then 4 rand() words per reference thread
+       (mcx_host.cpp:696-700, 759-768) */
+    if (cfg->seed > 0) {
+        srand((unsigned int)cfg->seed);
+    } else {
+        srand((unsigned int)time(0));
+    }
+    seeds = (uint32_t*)malloc(sizeof(uint32_t) * 4 * autothread);
+    if (!seeds) {
+        MCX_ERROR(-2, "out of host memory");
+    }
+    if (cfg->issavedet) {
+        detbuf = (float*)malloc(sizeof(float) * (size_t)cfg->maxdetphoton * (hostdetreclen ? hostdetreclen : 1));
+        seedbuf = cfg->issaveseed ? (uint64_t*)malloc(sizeof(uint64_t) * 2 * (size_t)cfg->maxdetphoton) : NULL;
+    }
+    cfg->detectedcount = 0;
+    cfg->his.detected = 0;
+    cfg->his.respin = cfg->respin;
+    cfg->his.colcount = hostdetreclen;
+    cfg->energytot = 0.0;
+    cfg->energyesc = 0.0;
+    cfg->runtime = 0;
+    cfg->kernelms = 0.f;
+    cfg->failedlaunch = 0;
+    memset(cfg->eventcount, 0, sizeof(cfg->eventcount));
+
+    float kms_total = 0.f;
+    for (int iter = 0; iter < cfg->respin; iter++) {
+        for (size_t j = 0; j < autothread * 4; j++) {
+            seeds[j] = (uint32_t)rand();
+        }
+        device_check(mcxg_set_seeds(s, seeds, (uint32_t)autothread), "uploading seeds");
+        /* photon split in the reference's float arithmetic (mcx_host.cpp:1101-1102) */
+        float tp = (float)cfg->nphoton * workload0 / (fullload * (float)autothread * (float)cfg->respin);
+        kp.threadphoton = (uint32_t)(int)tp;
+        kp.oddphoton = (int)((float)cfg->nphoton * workload0 / (fullload * (float)cfg->respin) -
+                             (float)((size_t)kp.threadphoton * autothread));
+        device_check(mcxg_set_params(s, &kp, sizeof(kp)), "updating parameters");
+        unsigned int flags = (cfg->exactmath ? MCXG_EXACT : 0u) | (iter ? MCXG_KEEP : 0u) |
+                             ((cfg->debuglevel & 1) ? MCXG_RNGDUMP : 0u);
+        float kms = 0.f;
+        device_check(mcxg_simulate(s, flags, &kms), "running the transport kernel");
+        kms_total += kms;
+
+        double esc = 0.0, tot = 0.0;
+        device_check(mcxg_get_energy(s, &esc, &tot), "reducing energies");
+        if (cfg->savethreadenergy && iter == 0) {
+            free(cfg->exportenergy);
+            cfg->exportenergy = (float*)malloc(sizeof(float) * 2 * autothread);
+            if (!cfg->exportenergy) {
+                MCX_ERROR(-2, "out of host memory");
+            }
+            device_check(mcxg_get_thread_energy(s, cfg->exportenergy), "reading per-thread energies");
+        }
+        cfg->energyesc += esc;
+        cfg->energytot += tot;
+        uint64_t ev[5];
+        uint32_t stw[2];
+        device_check(mcxg_get_counters(s, ev, stw), "reading counters");
+        for (int k = 0; k < 5; k++) {
+            cfg->eventcount[k] += ev[k];
+        }
+        cfg->failedlaunch += stw[0];
+
+        if (cfg->issavedet) {
+            uint32_t detected = 0;
+            device_check(mcxg_get_detected(s, detbuf, seedbuf, &detected), "reading detected photons");
+            if (detected > cfg->maxdetphoton && cfg->flog) {
+                fprintf(cfg->flog, "WARNING: the detected photon number is more than what your have specified (%u > %u), "
+                        "please use the -H option to specify a greater number\t", detected, cfg->maxdetphoton);
+            }
+            cfg->his.detected += detected;
+            uint32_t saved = detected < cfg->maxdetphoton ? detected : cfg->maxdetphoton;
+            if (saved) {
+                float* nd = (float*)realloc(cfg->exportdetected,
+                                            sizeof(float) * ((size_t)cfg->detectedcount + saved) * (hostdetreclen ? hostdetreclen : 1));
+                if (!nd) {
+                    MCX_ERROR(-2, "out of host memory");
+                }
+                cfg->exportdetected = nd;
+                memcpy(cfg->exportdetected + (size_t)cfg->detectedcount * hostdetreclen, detbuf,
+                       sizeof(float) * saved * hostdetreclen);
+                if (cfg->issaveseed) {
+                    void* ns = realloc(cfg->seeddata, sizeof(uint64_t) * 2 * ((size_t)cfg->detectedcount + saved));
+                    if (!ns) {
+                        MCX_ERROR(-2, "out of host memory");
+                    }
+                    cfg->seeddata = ns;
+                    memcpy((uint64_t*)cfg->seeddata + (size_t)cfg->detectedcount * 2, seedbuf, sizeof(uint64_t) * 2 * saved);
+                }
+                cfg->detectedcount += saved;
+            }
+        }
+    }
+    cfg->kernelms = kms_total;
+    cfg->threadused = (unsigned int)autothread;
+    cfg->runtime = (unsigned int)(kms_total + 0.5f);
+
+    /* normalisation (mcx_host.cpp:1382-1465), applied in FP64 on the GPU */
+    double scale = 1.0;
+    if (cfg->issave2pt) {
+        if (cfg->isnormalized) {
+            float Vvox = cfg->steps.x * cfg->steps.y * cfg->steps.z;
+            float sc = 1.f;
+            cfg->energyabs += cfg->energytot - cfg->energyesc;
+            if (cfg->outputtype == otFlux || cfg->outputtype == otFluence) {
+                sc = (float)(cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep));
+                if (cfg->outputtype == otFluence) {
+                    sc *= cfg->tstep;
+                }
+            } else if (cfg->outputtype == otEnergy || cfg->outputtype == otL) {
+                sc = (float)(1.0 / cfg->energytot);
+            }
+            if (cfg->extrasrclen && cfg->srcid < 0) {
+                sc *= (float)(cfg->extrasrclen + 1);
+            }
+            cfg->normalizer = sc;
+            cfg->his.normalizer = sc;
+            scale = (double)sc;
+        }
+        if (cfg->debuglevel & 1) {
+            scale = 1.0;
+        }
+        if (!cfg->exportfield) {
+            cfg->exportfield = (float*)calloc(fieldlen, sizeof(float));
+            if (!cfg->exportfield) {
+                MCX_ERROR(-2, "out of host memory");
+            }
+            device_check(mcxg_get_field(s, cfg->exportfield, scale), "reading the field");
+        } else {
+            /* caller-supplied buffer: add, as the reference does (mcx_host.cpp:1292-1296) */
+            fieldtmp = (float*)malloc(sizeof(float) * fieldlen);
+            if (!fieldtmp) {
+                MCX_ERROR(-2, "out of host memory");
+            }
+            device_check(mcxg_get_field(s, fieldtmp, scale), "reading the field");
+            for (size_t i = 0; i < fieldlen; i++) {
+                cfg->exportfield[i] += fieldtmp[i];
+            }
+        }
+    }
+    cfg->his.unitinmm = cfg->unitinmm;
+    cfg->his.totalphoton = (unsigned int)cfg->nphoton;
+    cfg->his.savedphoton = cfg->detectedcount;
+
+    if (cfg->flog && cfg->parentid == mpStandalone) {
+        fprintf(cfg->flog, "simulated %zu photons (%zu) with 1 devices (repeat x%d)\nMCX simulation speed: %.2f photon/ms\n",
+                cfg->nphoton, cfg->nphoton, cfg->respin,
+                (double)cfg->nphoton * (cfg->respin > 1 ? cfg->respin : 1) / (kms_total > 0.f ? kms_total : 1.f));
+        fprintf(cfg->flog, "total simulated energy: %.2f\tabsorbed: %5.5f%%\n(loss due to initial specular reflection is "
+                "excluded in the total)\n", cfg->energytot,
+                (cfg->energytot - cfg->energyesc) / cfg->energytot * 100.f);
+    }
+    for (int i = 0; i < 5; i++) {
+        free(tmp[i]);
+        tmp[i] = NULL;
+    }
+#undef packed
+#undef seeds
+#undef detbuf
+#undef seedbuf
+#undef fieldtmp
+    MCX_LEAVE();
+}
+
+/* ---- layout introspection, so foreign-function mirrors of Config can be checked */
+
+#include <stddef.h>
+#define MCX_FIELD(f) {#f, offsetof(Config, f)}
+static const struct {
+    const char* name;
+    size_t off;
+} g_cfg_fields[] = {
+    MCX_FIELD(nphoton), MCX_FIELD(nblocksize), MCX_FIELD(nthread), MCX_FIELD(seed), MCX_FIELD(srcpos),
+    MCX_FIELD(srcdir), MCX_FIELD(tstart), MCX_FIELD(tstep), MCX_FIELD(tend), MCX_FIELD(steps), MCX_FIELD(dim),
+    MCX_FIELD(medianum), MCX_FIELD(detnum), MCX_FIELD(maxdetphoton), MCX_FIELD(prop), MCX_FIELD(detpos),
+    MCX_FIELD(maxgate), MCX_FIELD(respin), MCX_FIELD(gpuid), MCX_FIELD(vol), MCX_FIELD(session),
+    MCX_FIELD(isrowmajor), MCX_FIELD(isreflect), MCX_FIELD(isrefint), MCX_FIELD(isnormalized), MCX_FIELD(issavedet),
+    MCX_FIELD(issave2pt), MCX_FIELD(isgpuinfo), MCX_FIELD(isspecular), MCX_FIELD(issrcfrom0), MCX_FIELD(ismomentum),
+    MCX_FIELD(internalsrc), MCX_FIELD(issaveseed), MCX_FIELD(issaveexit), MCX_FIELD(isatomic), MCX_FIELD(issaveref),
+    MCX_FIELD(srctype), MCX_FIELD(autopilot), MCX_FIELD(outputtype), MCX_FIELD(minenergy), MCX_FIELD(unitinmm),
+    MCX_FIELD(flog), MCX_FIELD(his), MCX_FIELD(energytot), MCX_FIELD(energyabs), MCX_FIELD(energyesc),
+    MCX_FIELD(maxvoidstep), MCX_FIELD(voidtime), MCX_FIELD(srcparam1), MCX_FIELD(srcparam2), MCX_FIELD(srcnum),
+    MCX_FIELD(srcpattern), MCX_FIELD(deviceid), MCX_FIELD(workload), MCX_FIELD(exportfield),
+    MCX_FIELD(exportdetected), MCX_FIELD(debuglevel), MCX_FIELD(normalizer), MCX_FIELD(seeddata), MCX_FIELD(gscatter),
+    MCX_FIELD(savedetflag), MCX_FIELD(detectedcount), MCX_FIELD(runtime), MCX_FIELD(parentid), MCX_FIELD(mediabyte),
+    MCX_FIELD(bc), MCX_FIELD(nphase), MCX_FIELD(invcdf), MCX_FIELD(nangle), MCX_FIELD(angleinvcdf), MCX_FIELD(srcid),
+    MCX_FIELD(extrasrclen), MCX_FIELD(srcdata), MCX_FIELD(exactmath), MCX_FIELD(kernelms), MCX_FIELD(eventcount),
+    MCX_FIELD(failedlaunch), MCX_FIELD(threadused), MCX_FIELD(exportenergy), MCX_FIELD(savethreadenergy),
+    MCX_FIELD(errorcode), MCX_FIELD(errormsg),
+};
+
+size_t mcx_config_sizeof(void) {
+    return sizeof(Config);
+}
+
+/* offset of a named Config field, or (size_t)-1 */
+size_t mcx_config_offsetof(const char* name) {
+    for (size_t i = 0; i < sizeof(g_cfg_fields) / sizeof(g_cfg_fields[0]); i++) {
+        if (!strcmp(g_cfg_fields[i].name, name)) {
+            return g_cfg_fields[i].off;
+        }
+    }
+    return (size_t)-1;
+}

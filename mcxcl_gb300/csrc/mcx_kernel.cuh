@@ -1,0 +1,1288 @@
+/*
+ * mcx_kernel.cuh -- the GB300 photon-transport kernel.
+ *
+ * Replaces the reference's mcx_main_loop (src/mcx_core.cl:2307-3307) and its
+ * launchnewphoton (1463-2275).  The physics, its branch structure and the
+ * order of floating-point operations follow the reference's OpenCL branch so
+ * that, in the exact instantiation, a photon's path is the same bits as in
+ * the CPU oracle; the GPU-specific structure is new:
+ *
+ *  - Persistent threads.  The reference assigns one RNG stream ("reference
+ *    thread", vt) per OpenCL work item.  Here each GPU thread repeatedly
+ *    claims the next vt from a global counter and runs all of its photons,
+ *    so results do not depend on the launch shape and long-lived photons do
+ *    not leave the rest of a warp idle at the end of the grid.
+ *  - One launch site.  Every photon termination (exit, time-out, roulette,
+ *    transmission into air) sets a relaunch request handled at the top of the
+ *    step loop, so the large source-sampling code is instantiated once.
+ *  - Parameters in constant memory, optical properties and inverse-CDF tables
+ *    staged in shared memory (label lookups diverge across a warp), the label
+ *    volume as one byte per voxel (label | detector bit << 7) read through
+ *    the read-only path.
+ *  - Fluence accumulated in two float planes with an error-free transform:
+ *    the high plane takes the deposit with an atomic that returns the old
+ *    value, the exact rounding error of that sum goes to the low plane.
+ *    Deposits to the same voxel and gate by several lanes of a warp are
+ *    merged first (match, shuffle-sum, one leader atomic).
+ *  - Detected-photon partial data in shared memory, strided per thread.
+ *
+ * Template flags: EXACT (IEEE-only math, no contraction: compile this TU with
+ * -fmad=false -prec-div=true -prec-sqrt=true -ftz=false), DET (detector
+ * bookkeeping compiled in), REFL (Fresnel / boundary-condition block
+ * compiled in), WAGG (warp aggregation of deposits), COUNT (event counters).
+ * DET and REFL are upper bounds: the runtime flags in the constant block
+ * still decide, so the exact build runs every configuration.
+ */
+#ifndef MCX_KERNEL_CUH
+#define MCX_KERNEL_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mcx_kparams.h"
+#include "mcx_launch.h"
+#include "mcx_pmath.cuh"
+
+namespace mcxg {
+/* each kernel translation unit gets its own copy (internal linkage): the two
+   units are compiled with different floating-point flags */
+namespace {
+
+#define K_EPS            1.19209290E-07F
+#define K_VERY_BIG       (1.f / K_EPS)
+#define K_ONE_PI         3.1415926535897932f
+#define K_TWO_PI         6.28318530717959f
+#define K_JUST_BELOW_ONE 0.9998f
+#define K_MAX_ACCUM      1000.f
+#define K_ROULETTE       10.f
+#define K_OUT_MIN        0xFFFFFFFFu
+#define K_OUT_MAX        0x7FFFFFFFu
+#define K_DET_MASK       0x80000000u
+#define K_MED_MASK       0x7FFFFFFFu
+#define K_LAUNCH_CAP     (1u << 16)     /* launch attempts per photon before giving up */
+#define K_STEP_CAP       (1u << 27)     /* propagation steps per photon before it is dropped */
+#define K_CONE_CAP       (1u << 16)     /* rejection draws of the cone source */
+
+enum { bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic };
+enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL };
+enum { S_PENCIL, S_ISOTROPIC, S_CONE, S_GAUSSIAN, S_PLANAR, S_PATTERN, S_FOURIER, S_ARCSINE,
+       S_DISK, S_FOURIERX, S_FOURIERX2D, S_ZGAUSSIAN, S_LINE, S_SLIT, S_PENCILARRAY, S_PATTERN3D,
+       S_HYPERBOLOID, S_RING };
+
+#define SAVE_DETID(a) ((a) & 0x1)
+#define SAVE_NSCAT(a) ((a) >> 1 & 0x1)
+#define SAVE_PPATH(a) ((a) >> 2 & 0x1)
+#define SAVE_MOM(a)   ((a) >> 3 & 0x1)
+#define SAVE_PEXIT(a) ((a) >> 4 & 0x1)
+#define SAVE_VEXIT(a) ((a) >> 5 & 0x1)
+#define SAVE_W0(a)    ((a) >> 6 & 0x1)
+
+/* status words written by the kernel */
+#define ST_FAILED_LAUNCH 0   /* reference threads whose launch failed (NO_LAUNCH) */
+#define ST_GUARD         1   /* photons stopped by a safety cap (steps, cone draws) or an index guard */
+
+__constant__ mcxg_kparams c_p;
+__constant__ float4 c_det[MCXG_MAX_DET];
+__constant__ float4 c_srcx[MCXG_MAX_EXTRASRC * 4];
+
+
+
+/* ------------------------------------------------------------------ math */
+
+template <bool EXACT> struct Mth;
+
+template <> struct Mth<true> {
+    static __device__ __forceinline__ float log(float x) { return pm_logf(x); }
+    static __device__ __forceinline__ float exp(float x) { return pm_expf(x); }
+    static __device__ __forceinline__ void sincos(float x, float* s, float* c) { pm_sincosf(x, s, c); }
+    static __device__ __forceinline__ float sin(float x) { return pm_sinf(x); }
+    static __device__ __forceinline__ float cos(float x) { return pm_cosf(x); }
+    static __device__ __forceinline__ float acos(float x) { return pm_acosf(x); }
+    static __device__ __forceinline__ float rsqrt(float x) { return 1.f / sqrtf(x); }
+    static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+    static __device__ __forceinline__ float sqrt(float x) { return sqrtf(x); }
+};
+
+template <> struct Mth<false> {
+    static __device__ __forceinline__ float log(float x) { return __logf(x); }
+    static __device__ __forceinline__ float exp(float x) { return __expf(x); }
+    static __device__ __forceinline__ void sincos(float x, float* s, float* c) { __sincosf(x, s, c); }
+    static __device__ __forceinline__ float sin(float x) { return __sinf(x); }
+    static __device__ __forceinline__ float cos(float x) { return __cosf(x); }
+    static __device__ __forceinline__ float acos(float x) { return acosf(x); }
+    static __device__ __forceinline__ float rsqrt(float x) { return rsqrtf(x); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ float sqrt(float x) { return sqrtf(x); }
+};
+
+/* xorshift128+ (mcx_core.cl:684-698): 64-bit state pair, the low word of the
+   sum fills a float mantissa in [1,2) */
+struct Rng {
+    unsigned long long a, b;
+};
+
+__device__ __forceinline__ float rnd(Rng& t) {
+    unsigned long long s1 = t.a;
+    const unsigned long long s0 = t.b;
+    t.a = s0;
+    s1 ^= s1 << 23;
+    t.b = s1 ^ s0 ^ (s1 >> 18) ^ (s0 >> 5);
+    unsigned int r = (unsigned int)(t.b + s0);
+    return __fsub_rn(__uint_as_float(0x3F800000u | (r >> 9)), 1.0f);
+}
+
+template <bool EXACT>
+__device__ __forceinline__ float rnd_scatlen(Rng& t) {
+    return -Mth<EXACT>::log(rnd(t) + K_EPS);
+}
+
+/* mcx_core.cl:965-973 */
+__device__ __forceinline__ float nextafter_ref(float a, int dir) {
+    unsigned int i = __float_as_uint(a + 1000.f);
+    i += (unsigned int)dir ^ (i & 0x80000000U);
+    return __uint_as_float(i) - 1000.f;
+}
+
+__device__ __forceinline__ float4 f4(const mcxg_float4& q) {
+    return make_float4(q.x, q.y, q.z, q.w);
+}
+
+/* ----------------------------------------------------------- photon state */
+
+struct Photon {
+    float4 p, v, f, prop;
+    int fx, fy, fz, fw;            /* voxel index and last crossed face (the reference's short4 flipdir) */
+    unsigned int idx1d, mediaid, isdet;
+    float w0, Lmove, pathlen, n1;
+    float esc, launched, w0init, srcsel;   /* reference ppath[partialdata .. +3] */
+    Rng t;
+    unsigned long long ps0, ps1;   /* RNG state at launch, saved with detected photons */
+};
+
+struct Shared {
+    const float4* prop;            /* medianum rows */
+    const float* invcdf;
+    const float* angleinvcdf;
+    float* pp;                     /* this thread's partial data, stride blockDim.x */
+    unsigned int stride;
+};
+
+__device__ __forceinline__ unsigned int media_at(const KArgs& a, unsigned int idx) {
+    if (c_p.mediaword == 1) {
+        unsigned int m = __ldg(a.media8 + idx);
+        return (m & 0x7Fu) | ((m & 0x80u) << 24);
+    }
+    return __ldg(a.media32 + idx);
+}
+
+/* updateproperty, mcx_core.cl:1079-1096 */
+__device__ __forceinline__ void updateprop(const Shared& S, float4& prop, unsigned int mediaid) {
+    if (c_p.mediaformat <= 4) {
+        prop = S.prop[mediaid & K_MED_MASK];
+    } else {
+        prop.x = fabsf(__uint_as_float(mediaid));
+        prop.w = S.prop[(!(mediaid & K_MED_MASK)) == 0].w;
+    }
+}
+
+__device__ __forceinline__ bool inside_u(int x, int y, int z) {
+    return (float)(unsigned short)x < c_p.maxidx.x && (float)(unsigned short)y < c_p.maxidx.y &&
+           (float)(unsigned short)z < c_p.maxidx.z;
+}
+
+__device__ __forceinline__ unsigned int vox_index(int x, int y, int z) {
+    return (unsigned int)(z * (int)c_p.dimxy + y * (int)c_p.dimx + x);
+}
+
+/* hitgrid, OpenCL branch (mcx_core.cl:988-993): distance to the next voxel
+   face along v, face id into fw */
+template <bool EXACT>
+__device__ __forceinline__ float hitgrid(const float4& p, const float4& v, int fx, int fy, int fz, int& fw) {
+    float hx = fabsf((float)fx - (v.x > 0.f ? -1.f : 0.f) - p.x);
+    float hy = fabsf((float)fy - (v.y > 0.f ? -1.f : 0.f) - p.y);
+    float hz = fabsf((float)fz - (v.z > 0.f ? -1.f : 0.f) - p.z);
+    hx = fabsf(Mth<EXACT>::div(hx + K_EPS, v.x));
+    hy = fabsf(Mth<EXACT>::div(hy + K_EPS, v.y));
+    hz = fabsf(Mth<EXACT>::div(hz + K_EPS, v.z));
+    float dist = fminf(fminf(hx, hy), hz);
+    fw = (dist == hx ? 0 : (dist == hy ? 1 : 2));
+    return dist;
+}
+
+/* rotatevector, mcx_core.cl:1025-1042 */
+template <bool EXACT>
+__device__ __forceinline__ void rotatevector(float4& v, float st, float ct, float sp, float cp) {
+    if (v.z > -1.f + K_EPS && v.z < 1.f - K_EPS) {
+        float tmp0 = 1.f - v.z * v.z;
+        float tmp1 = st * Mth<EXACT>::rsqrt(tmp0);
+        float nx = tmp1 * (v.x * v.z * cp - v.y * sp) + v.x * ct;
+        float ny = tmp1 * (v.y * v.z * cp + v.x * sp) + v.y * ct;
+        float nz = -tmp1 * tmp0 * cp + v.z * ct;
+        v.x = nx;
+        v.y = ny;
+        v.z = nz;
+    } else {
+        v.x = st * cp;
+        v.y = st * sp;
+        v.z = (v.z > 0.f) ? ct : -ct;
+    }
+    if (EXACT) {
+        /* the reference renormalises component by component */
+        v.x *= Mth<EXACT>::rsqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+        v.y *= Mth<EXACT>::rsqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+        v.z *= Mth<EXACT>::rsqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+    } else {
+        float r = Mth<EXACT>::rsqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+        v.x *= r;
+        v.y *= r;
+        v.z *= r;
+    }
+}
+
+/* rotatevector2d, mcx_core.cl:1008-1023 */
+template <bool EXACT>
+__device__ __forceinline__ void rotatevector2d(float4& v, float st, float ct, unsigned int is2d) {
+    float nx = v.x, ny = v.y, nz = v.z;
+    if (is2d == 1) {
+        nx = 0.f;
+        ny = v.y * ct - v.z * st;
+        nz = v.y * st + v.z * ct;
+    } else if (is2d == 2) {
+        nx = v.x * ct - v.z * st;
+        ny = 0.f;
+        nz = v.x * st + v.z * ct;
+    } else if (is2d == 3) {
+        nx = v.x * ct - v.y * st;
+        ny = v.x * st + v.y * ct;
+        nz = 0.f;
+    }
+    float tmp0 = Mth<EXACT>::rsqrt(nx * nx + ny * ny + nz * nz);
+    v.x = nx * tmp0;
+    v.y = ny * tmp0;
+    v.z = nz * tmp0;
+}
+
+__device__ __forceinline__ float vcomp(const float4& v, int k) {
+    return k == 0 ? v.x : (k == 1 ? v.y : v.z);
+}
+
+/* transmit, mcx_core.cl:1044-1055 */
+template <bool EXACT>
+__device__ __forceinline__ void transmit(float4& v, float n1, float n2, int fw) {
+    float tmp0 = Mth<EXACT>::div(n1, n2);
+    v.x *= tmp0;
+    v.y *= tmp0;
+    v.z *= tmp0;
+    if (fw == 0) {
+        v.x = Mth<EXACT>::sqrt(1.f - v.y * v.y - v.z * v.z) * (float)((v.x > 0.f) - (v.x < 0.f));
+    } else if (fw == 1) {
+        v.y = Mth<EXACT>::sqrt(1.f - v.x * v.x - v.z * v.z) * (float)((v.y > 0.f) - (v.y < 0.f));
+    } else {
+        v.z = Mth<EXACT>::sqrt(1.f - v.x * v.x - v.y * v.y) * (float)((v.z > 0.f) - (v.z < 0.f));
+    }
+}
+
+/* reflectcoeff, mcx_core.cl:1057-1075 */
+template <bool EXACT>
+__device__ float reflectcoeff(const float4& v, float n1, float n2, int fw) {
+    float Icos = fabsf(vcomp(v, fw));
+    float tmp0 = n1 * n1;
+    float tmp1 = n2 * n2;
+    float tmp2 = 1.f - tmp0 / tmp1 * (1.f - Icos * Icos);
+    if (tmp2 > 0.f) {
+        float Re = tmp0 * Icos * Icos + tmp1 * tmp2;
+        tmp2 = sqrtf(tmp2);
+        float Im = 2.f * n1 * n2 * Icos * tmp2;
+        float Rtotal = (Re - Im) / (Re + Im);
+        Re = tmp1 * Icos * Icos + tmp0 * tmp2 * tmp2;
+        Rtotal = (Rtotal + (Re - Im) / (Re + Im)) * 0.5f;
+        return Rtotal;
+    }
+    return 1.f;
+}
+
+/* skipvoid, mcx_core.cl:1350-1455: march through background voxels to the
+   first labelled voxel on the ray */
+template <bool EXACT>
+__device__ int skipvoid(const KArgs& a, const Shared& S, float4& p, float4& v, float4& f, int& fx, int& fy,
+                        int& fz, int& fw) {
+    int count = 1;
+    fx = (int)(short)floorf(p.x);
+    fy = (int)(short)floorf(p.y);
+    fz = (int)(short)floorf(p.z);
+    fw = -1;
+    for (;;) {
+        if (inside_u(fx, fy, fz)) {
+            int idx1d = (int)vox_index(fx, fy, fz);
+            if (media_at(a, idx1d) & K_MED_MASK) {
+                p.x -= v.x;
+                p.y -= v.y;
+                p.z -= v.z;
+                fx = (int)(short)floorf(p.x);
+                fy = (int)(short)floorf(p.y);
+                fz = (int)(short)floorf(p.z);
+                f.y -= c_p.minaccumtime;
+                idx1d = (int)vox_index(fx, fy, fz);
+                count = 0;
+                while (!inside_u(fx, fy, fz) || !(media_at(a, idx1d) & K_MED_MASK)) {
+                    float dist = hitgrid<EXACT>(p, v, fx, fy, fz, fw);
+                    f.y += c_p.minaccumtime * dist;
+                    p.x = p.x + dist * v.x;
+                    p.y = p.y + dist * v.y;
+                    p.z = p.z + dist * v.z;
+                    if (fw == 0) {
+                        fx += (v.x > 0.f ? 1 : -1);
+                    }
+                    if (fw == 1) {
+                        fy += (v.y > 0.f ? 1 : -1);
+                    }
+                    if (fw == 2) {
+                        fz += (v.z > 0.f ? 1 : -1);
+                    }
+                    idx1d = (int)vox_index(fx, fy, fz);
+                    if (count++ > 3) {
+                        break;
+                    }
+                }
+                f.y = (c_p.voidtime) ? f.y : 0.f;
+                {
+                    unsigned int m = media_at(a, idx1d);
+                    float4 ht = make_float4(0.f, 0.f, 0.f, 0.f);
+                    updateprop(S, ht, m);
+                    if (c_p.isspecular && ht.w != S.prop[0].w) {
+                        p.w *= 1.f - reflectcoeff<EXACT>(v, S.prop[0].w, S.prop[m & K_MED_MASK].w, fw);
+                        if (p.w > K_EPS) {
+                            transmit<EXACT>(v, S.prop[0].w, S.prop[m & K_MED_MASK].w, fw);
+                        }
+                    }
+                }
+                return idx1d;
+            }
+        }
+        if (((p.x < 0.f) && (v.x <= 0.f)) || ((p.x >= c_p.maxidx.x) && (v.x >= 0.f)) ||
+            ((p.y < 0.f) && (v.y <= 0.f)) || ((p.y >= c_p.maxidx.y) && (v.y >= 0.f)) ||
+            ((p.z < 0.f) && (v.z <= 0.f)) || ((p.z >= c_p.maxidx.z) && (v.z >= 0.f))) {
+            return -1;
+        }
+        p.x = p.x + v.x;
+        p.y = p.y + v.y;
+        p.z = p.z + v.z;
+        fx = (int)(short)floorf(p.x);
+        fy = (int)(short)floorf(p.y);
+        fz = (int)(short)floorf(p.z);
+        f.y += c_p.minaccumtime;
+        if ((unsigned int)count++ > c_p.maxvoidstep) {
+            return -1;
+        }
+    }
+}
+
+/* finddetector, mcx_core.cl:838-850 */
+__device__ __forceinline__ unsigned int finddetector(const float4& p) {
+    for (unsigned int i = 0; i < c_p.detnum; i++) {
+        float4 d = c_det[i];
+        if ((d.x - p.x) * (d.x - p.x) + (d.y - p.y) * (d.y - p.y) + (d.z - p.z) * (d.z - p.z) < d.w * d.w) {
+            return i + 1;
+        }
+    }
+    return 0;
+}
+
+/* savedetphoton, mcx_core.cl:867-926 */
+__device__ void savedetphoton(const KArgs& a, const Shared& S, Photon& s, unsigned int isdet) {
+    int detid = (isdet == K_OUT_MIN) ? -1 : (int)finddetector(s.p);
+    if (!detid) {
+        return;
+    }
+    unsigned int slot = atomicAdd(a.detcount, 1u);
+    if (slot < c_p.maxdetphoton) {
+        if (c_p.issaveseed) {
+            a.detseed[slot * 2] = s.ps0;
+            a.detseed[slot * 2 + 1] = s.ps1;
+        }
+        float* rec = a.detp + (size_t)slot * c_p.reclen;
+        unsigned int k = 0;
+        if (SAVE_DETID(c_p.savedetflag)) {
+            if (c_p.extrasrclen && (c_p.srcid <= 0)) {
+                detid |= (((int)s.srcsel) << 16);
+            }
+            rec[k++] = (float)detid;
+        }
+        for (unsigned int i = 0; i < c_p.partialdata; i++) {
+            rec[k++] = S.pp[i * S.stride];
+        }
+        if (SAVE_PEXIT(c_p.savedetflag)) {
+            rec[k++] = s.p.x;
+            rec[k++] = s.p.y;
+            rec[k++] = s.p.z;
+        }
+        if (SAVE_VEXIT(c_p.savedetflag)) {
+            rec[k++] = s.v.x;
+            rec[k++] = s.v.y;
+            rec[k++] = s.v.z;
+        }
+        if (SAVE_W0(c_p.savedetflag)) {
+            rec[k++] = s.w0init;
+        }
+    } else if (c_p.savedet == 3) {
+        atomicSub(a.detcount, 1u);
+    }
+}
+
+/* ---------------------------------------------------------------- deposit */
+
+/* Two-plane compensated add: the high plane takes w, the exact rounding error
+   of that add (TwoSum on the value the atomic returned) goes to the low
+   plane.  hi + lo then carries the sum to ~2^-48 relative. */
+__device__ __forceinline__ void field_add2(float* field, unsigned int fieldlen, unsigned int i, float w) {
+    float old = atomicAdd(field + i, w);
+    float s = __fadd_rn(old, w);
+    float bp = __fsub_rn(s, old);
+    float e = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bp)), __fsub_rn(w, bp));
+    if (e != 0.f) {
+        atomicAdd(field + fieldlen + i, e);
+    }
+}
+
+/* Deposit from every lane that has one; lanes of the warp hitting the same
+   field element are summed first and one leader commits. */
+template <bool WAGG>
+__device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, bool doit, unsigned int key, float w) {
+    if (!WAGG) {
+        if (doit) {
+            field_add2(field, fieldlen, key, w);
+        }
+        return;
+    }
+    unsigned int act = __activemask();
+    unsigned int m = __ballot_sync(act, doit);
+    if (!doit) {
+        return;
+    }
+    unsigned int peers = __match_any_sync(m, key);
+    unsigned int lane = threadIdx.x & 31u;
+    if (peers == (1u << lane)) {
+        field_add2(field, fieldlen, key, w);
+        return;
+    }
+    float total = 0.f;
+    unsigned int rest = peers;
+    while (rest) {
+        int src = __ffs(rest) - 1;
+        rest &= rest - 1;
+        total += __shfl_sync(peers, w, src);
+    }
+    if ((int)lane == __ffs(peers) - 1) {
+        field_add2(field, fieldlen, key, total);
+    }
+}
+
+/* ------------------------------------------------------------------ launch */
+
+__device__ __forceinline__ void set_launch_voxel(const KArgs& a, Photon& s) {
+    s.idx1d = (unsigned int)((int)(floorf(s.p.z)) * (int)c_p.dimxy + (int)(floorf(s.p.y)) * (int)c_p.dimx +
+                             (int)(floorf(s.p.x)));
+    if (s.p.x < 0.f || s.p.y < 0.f || s.p.z < 0.f || s.p.x >= c_p.maxidx.x || s.p.y >= c_p.maxidx.y ||
+            s.p.z >= c_p.maxidx.z) {
+        s.mediaid = 0;
+    } else {
+        s.mediaid = media_at(a, s.idx1d);
+    }
+}
+
+/*
+ * launchnewphoton (mcx_core.cl:1463-2275): close the current photon (escaped
+ * weight, saved reflectance, detection) and launch the next one of this
+ * reference thread.  Returns 0 on launch, 1 when the thread's quota is done,
+ * -1 when no launch position was found.
+ */
+template <bool EXACT, bool DET>
+__device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsigned int isdet, unsigned int vt,
+                               unsigned long long* nfailed) {
+    typedef Mth<EXACT> M;
+    s.w0 = 1.f;
+    s.Lmove = -1.f;
+
+    if (DET && c_p.savedet == 3 && *(volatile unsigned int*)a.detcount >= c_p.maxdetphoton) {
+        return 1;
+    }
+
+    if (fabsf(s.p.w) >= 0.f) {
+        s.esc += s.p.w;
+        if (s.mediaid == 0 && s.idx1d != K_OUT_MIN && s.idx1d != K_OUT_MAX && c_p.issaveref && s.p.w > 0.f) {
+            int tshift = (int)floorf((s.f.y - c_p.twin0) * c_p.Rtstep);
+            if ((int)c_p.maxgate - 1 < tshift) {
+                tshift = (int)c_p.maxgate - 1;
+            }
+            if (c_p.extrasrclen && (c_p.srcid < 0)) {
+                tshift += ((int)s.srcsel - 1) * (int)c_p.maxgate;
+            }
+            field_add2(a.field, c_p.fieldlen, s.idx1d + (unsigned int)tshift * c_p.nvox, -s.p.w);
+        }
+        if (DET && c_p.savedet && (isdet & K_DET_MASK) == K_DET_MASK && s.mediaid == 0 && c_p.issaveref < 2) {
+            savedetphoton(a, S, s, isdet);
+        }
+    }
+    if (DET) {
+        for (unsigned int i = 0; i < c_p.partialdata; i++) {
+            S.pp[i * S.stride] = 0.f;
+        }
+    }
+
+    if (s.f.w >= (float)(c_p.threadphoton + (vt < (unsigned int)c_p.oddphoton))) {
+        return 1;
+    }
+
+    if (DET && c_p.issaveseed) {
+        s.ps0 = s.t.a;
+        s.ps1 = s.t.b;
+    }
+
+    float4 lpos = f4(c_p.srcpos), ldir = f4(c_p.srcdir), lp1 = f4(c_p.srcparam1), lp2 = f4(c_p.srcparam2);
+    if (c_p.extrasrclen && (c_p.srcid != 1)) {
+        int sel = -1;
+        if (c_p.srcid > 1) {
+            sel = c_p.srcid - 2;
+        } else {
+            s.srcsel = (float)((int)(rnd(s.t) * K_JUST_BELOW_ONE * (float)(c_p.extrasrclen + 1)) + 1);
+            if ((int)s.srcsel > 1) {
+                sel = (int)(s.srcsel - 2);
+            }
+        }
+        if (sel >= 0) {
+            lpos = c_srcx[sel * 4];
+            ldir = c_srcx[sel * 4 + 1];
+            lp1 = c_srcx[sel * 4 + 2];
+            lp2 = c_srcx[sel * 4 + 3];
+        }
+    }
+
+    unsigned int attempts = 0;
+    for (;;) {
+        if (++attempts > K_LAUNCH_CAP) {
+            return -1;
+        }
+        s.p = lpos;
+        s.v = ldir;
+        s.f.x = 0.f;
+        s.f.y = 0.f;
+        s.f.z = c_p.minaccumtime;
+        s.idx1d = __float_as_uint(lp2.z);
+        s.mediaid = __float_as_uint(lp2.w);
+        s.prop = make_float4(lpos.x, lpos.y, lpos.z, 0.f);
+
+        const unsigned int st = c_p.srctype;
+        if (st == S_PENCIL) {
+            /* position and direction already set */
+        } else if (st == S_PLANAR || st == S_PATTERN || st == S_PATTERN3D || st == S_FOURIER || st == S_PENCILARRAY) {
+            float rx = rnd(s.t);
+            float ry = rnd(s.t);
+            float rz = 0.f;
+            if (st == S_PATTERN3D) {
+                rz = rnd(s.t);
+                s.p.x = s.p.x + rx * lp1.x;
+                s.p.y = s.p.y + ry * lp1.y;
+                s.p.z = s.p.z + rz * lp1.z;
+            } else {
+                s.p.x = s.p.x + rx * lp1.x + ry * lp2.x;
+                s.p.y = s.p.y + rx * lp1.y + ry * lp2.y;
+                s.p.z = s.p.z + rx * lp1.z + ry * lp2.z;
+            }
+            if (st == S_PATTERN) {
+                unsigned int pi = (unsigned int)((int)(ry * K_JUST_BELOW_ONE * lp2.w) * (int)(lp1.w) +
+                                                 (int)(rx * K_JUST_BELOW_ONE * lp1.w));
+                s.p.w = lpos.w * a.srcpattern[min(pi, c_p.npattern - 1)];
+            } else if (st == S_PATTERN3D) {
+                unsigned int pi = (unsigned int)((int)(rz * K_JUST_BELOW_ONE * lp1.z) * (int)(lp1.y) * (int)(lp1.x) +
+                                                 (int)(ry * K_JUST_BELOW_ONE * lp1.y) * (int)(lp1.x) +
+                                                 (int)(rx * K_JUST_BELOW_ONE * lp1.x));
+                s.p.w = lpos.w * a.srcpattern[min(pi, c_p.npattern - 1)];
+            } else if (st == S_FOURIER) {
+                s.p.w = lpos.w * (M::cos((floorf(lp1.w) * rx + floorf(lp2.w) * ry + lp1.w - floorf(lp1.w)) * K_TWO_PI) *
+                                  (1.f - lp2.w + floorf(lp2.w)) + 1.f) * 0.5f;
+            } else if (st == S_PENCILARRAY) {
+                s.p.x = lpos.x + floorf(rx * lp1.w) * lp1.x / (lp1.w - 1.f) + floorf(ry * lp2.w) * lp2.x / (lp2.w - 1.f);
+                s.p.y = lpos.y + floorf(rx * lp1.w) * lp1.y / (lp1.w - 1.f) + floorf(ry * lp2.w) * lp2.y / (lp2.w - 1.f);
+                s.p.z = lpos.z + floorf(rx * lp1.w) * lp1.z / (lp1.w - 1.f) + floorf(ry * lp2.w) * lp2.z / (lp2.w - 1.f);
+            }
+            set_launch_voxel(a, s);
+            s.prop.x = s.prop.x + (lp1.x + lp2.x) * 0.5f;
+            s.prop.y = s.prop.y + (lp1.y + lp2.y) * 0.5f;
+            s.prop.z = s.prop.z + (lp1.z + lp2.z) * 0.5f;
+            s.prop.w = 0.f;
+        } else if (st == S_FOURIERX || st == S_FOURIERX2D) {
+            float rx = rnd(s.t);
+            float ry = rnd(s.t);
+            float4 v2 = lp1;
+            v2.w *= M::rsqrt(lp1.x * lp1.x + lp1.y * lp1.y + lp1.z * lp1.z);
+            v2.x = v2.w * (ldir.y * lp1.z - ldir.z * lp1.y);
+            v2.y = v2.w * (ldir.z * lp1.x - ldir.x * lp1.z);
+            v2.z = v2.w * (ldir.x * lp1.y - ldir.y * lp1.x);
+            s.p.x = s.p.x + rx * lp1.x + ry * v2.x;
+            s.p.y = s.p.y + rx * lp1.y + ry * v2.y;
+            s.p.z = s.p.z + rx * lp1.z + ry * v2.z;
+            if (st == S_FOURIERX2D) {
+                s.p.w = lpos.w * (M::sin((lp2.x * rx + lp2.z) * K_TWO_PI) * M::sin((lp2.y * ry + lp2.w) * K_TWO_PI) + 1.f) * 0.5f;
+            } else {
+                s.p.w = lpos.w * (M::cos((lp2.x * rx + lp2.y * ry + lp2.z) * K_TWO_PI) * (1.f - lp2.w) + 1.f) * 0.5f;
+            }
+            set_launch_voxel(a, s);
+            s.prop.x = s.prop.x + (lp1.x + v2.x) * 0.5f;
+            s.prop.y = s.prop.y + (lp1.y + v2.y) * 0.5f;
+            s.prop.z = s.prop.z + (lp1.z + v2.z) * 0.5f;
+            s.prop.w = 0.f;
+        } else if (st == S_HYPERBOLOID) {
+            float sphi, cphi, r;
+            r = K_TWO_PI * rnd(s.t);
+            M::sincos(r, &sphi, &cphi);
+            r = M::sqrt(0.5f * rnd_scatlen<EXACT>(s.t)) * lp1.x;
+            s.prop.x = -lp1.y / lp1.z;
+            s.prop.y = M::rsqrt(r * r + lp1.z * lp1.z);
+            s.p.x = r * (cphi - s.prop.x * sphi);
+            s.p.y = r * (sphi + s.prop.x * cphi);
+            s.p.z = 0.f;
+            {
+                float4 np;
+                np.x = -r * sphi * s.prop.y;
+                np.y = r * cphi * s.prop.y;
+                np.z = lp1.z * s.prop.y;
+                np.w = 0.f;
+                s.prop = np;
+            }
+            if (s.v.z > -1.f + K_EPS && s.v.z < 1.f - K_EPS) {
+                r = 1.f - s.v.z * s.v.z;
+                float sth = M::sqrt(r);
+                r = M::rsqrt(r);
+                cphi = s.v.x * r;
+                sphi = s.v.y * r;
+                float px = s.p.x * cphi * s.v.z - s.p.y * sphi;
+                float py = s.p.x * sphi * s.v.z + s.p.y * cphi;
+                float pz = -s.p.x * sth;
+                s.p.x = px;
+                s.p.y = py;
+                s.p.z = pz;
+                float vx = s.prop.x * cphi * s.v.z - s.prop.y * sphi + s.prop.z * cphi * sth;
+                float vy = s.prop.x * sphi * s.v.z + s.prop.y * cphi + s.prop.z * sphi * sth;
+                float vz = -s.prop.x * sth + s.prop.z * s.v.z;
+                s.v.x = vx;
+                s.v.y = vy;
+                s.v.z = vz;
+            } else {
+                s.v.x = s.prop.x;
+                s.v.y = s.prop.y;
+                s.v.z = (s.v.z > 0.f) ? s.prop.z : -s.prop.z;
+            }
+            s.p.x = s.p.x + lpos.x;
+            s.p.y = s.p.y + lpos.y;
+            s.p.z = s.p.z + lpos.z;
+            s.prop = make_float4(lpos.x, lpos.y, lpos.z, 0.f);
+            s.Lmove = 0.f;
+        } else if (st == S_DISK || st == S_GAUSSIAN || st == S_RING) {
+            float sphi, cphi, phi, r;
+            if (st == S_DISK || st == S_RING) {
+                if (lp1.z > 0.f || lp1.w > 0.f) {
+                    phi = fabsf(lp1.z - lp1.w) * rnd(s.t) + fminf(lp1.z, lp1.w);
+                } else {
+                    phi = K_TWO_PI * rnd(s.t);
+                }
+            } else {
+                phi = K_TWO_PI * rnd(s.t);
+            }
+            M::sincos(phi, &sphi, &cphi);
+            if (st == S_DISK || st == S_RING) {
+                r = M::sqrt(rnd(s.t) * fabsf(lp1.x * lp1.x - lp1.y * lp1.y) + lp1.y * lp1.y);
+            } else {
+                if (fabsf(ldir.w) < 1e-5f || fabsf(lp1.y) < 1e-5f) {
+                    r = M::sqrt(-0.5f * M::log(rnd(s.t))) * lp1.x;
+                } else {
+                    r = lp1.x * lp1.x * K_ONE_PI / lp1.y;
+                    r = M::sqrt(-0.5f * M::log(rnd(s.t)) * (1.f + (ldir.w * ldir.w / (r * r)))) * lp1.x;
+                }
+            }
+            if (s.v.z > -1.f + K_EPS && s.v.z < 1.f - K_EPS) {
+                float tmp0 = 1.f - s.v.z * s.v.z;
+                float tmp1 = r * M::rsqrt(tmp0);
+                s.p.x = s.p.x + tmp1 * (s.v.x * s.v.z * cphi - s.v.y * sphi);
+                s.p.y = s.p.y + tmp1 * (s.v.y * s.v.z * cphi + s.v.x * sphi);
+                s.p.z = s.p.z - tmp1 * tmp0 * cphi;
+            } else {
+                s.p.x += r * cphi;
+                s.p.y += r * sphi;
+            }
+            set_launch_voxel(a, s);
+        } else if (st == S_CONE || st == S_ISOTROPIC || st == S_ARCSINE) {
+            float ang, sth, cth, sphi, cphi;
+            ang = K_TWO_PI * rnd(s.t);
+            M::sincos(ang, &sphi, &cphi);
+            if (st == S_CONE) {
+                /* the reference loops until a draw falls inside the cone; a cone
+                   of zero half-angle would never end, so the draws are capped */
+                unsigned int tries = 0;
+                do {
+                    ang = (lp1.y > 0) ? K_TWO_PI * rnd(s.t) : M::acos(2.f * rnd(s.t) - 1.f);
+                } while (ang > lp1.x && ++tries < K_CONE_CAP);
+            } else if (st == S_ISOTROPIC) {
+                ang = M::acos(2.f * rnd(s.t) - 1.f);
+            } else {
+                ang = K_ONE_PI * rnd(s.t);
+            }
+            M::sincos(ang, &sth, &cth);
+            rotatevector<EXACT>(s.v, sth, cth, sphi, cphi);
+            s.Lmove = 0.f;
+        } else if (st == S_ZGAUSSIAN) {
+            float ang, sth, cth, sphi, cphi;
+            ang = K_TWO_PI * rnd(s.t);
+            M::sincos(ang, &sphi, &cphi);
+            ang = M::sqrt(-2.f * M::log(rnd(s.t))) * (1.f - 2.f * rnd(s.t)) * lp1.x;
+            M::sincos(ang, &sth, &cth);
+            rotatevector<EXACT>(s.v, sth, cth, sphi, cphi);
+            s.Lmove = 0.f;
+        } else if (st == S_LINE || st == S_SLIT) {
+            float r_l = rnd(s.t);
+            s.p.x = s.p.x + r_l * lp1.x;
+            s.p.y = s.p.y + r_l * lp1.y;
+            s.p.z = s.p.z + r_l * lp1.z;
+            if (st == S_LINE) {
+                float sphi_l, cphi_l;
+                r_l = M::rsqrt(lp1.x * lp1.x + lp1.y * lp1.y + lp1.z * lp1.z);
+                if (lp2.x > 0.f) {
+                    float lx = lp1.x * r_l, ly = lp1.y * r_l, lz = lp1.z * r_l;
+                    float vd = s.v.x * lx + s.v.y * ly + s.v.z * lz;
+                    s.v.x = s.v.x - vd * lx;
+                    s.v.y = s.v.y - vd * ly;
+                    s.v.z = s.v.z - vd * lz;
+                    float vn = M::rsqrt(s.v.x * s.v.x + s.v.y * s.v.y + s.v.z * s.v.z);
+                    s.v.x = s.v.x * vn;
+                    s.v.y = s.v.y * vn;
+                    s.v.z = s.v.z * vn;
+                    r_l = lp2.x * (2.f * rnd(s.t) - 1.f);
+                    M::sincos(r_l, &sphi_l, &cphi_l);
+                    /* rotate_perpendicular_vector, mcx_core.cl:997-1006 */
+                    float cx = ly * s.v.z - lz * s.v.y;
+                    float cy = lz * s.v.x - lx * s.v.z;
+                    float cz = lx * s.v.y - ly * s.v.x;
+                    s.v.x = s.v.x * cphi_l + cx * sphi_l;
+                    s.v.y = s.v.y * cphi_l + cy * sphi_l;
+                    s.v.z = s.v.z * cphi_l + cz * sphi_l;
+                } else {
+                    s.v.x = lp1.x * r_l;
+                    s.v.y = lp1.y * r_l;
+                    s.v.z = lp1.z * r_l;
+                    r_l = K_TWO_PI * rnd(s.t);
+                    M::sincos(r_l, &sphi_l, &cphi_l);
+                    rotatevector<EXACT>(s.v, 1.f, 0.f, sphi_l, cphi_l);
+                }
+            } else {
+                if (lp2.x > 0.f || lp2.y > 0.f) {
+                    float sphi_s, cphi_s;
+                    r_l = K_TWO_PI * rnd(s.t);
+                    M::sincos(r_l, &sphi_s, &cphi_s);
+                    r_l = M::sqrt(2.f * rnd_scatlen<EXACT>(s.t));
+                    cphi_s *= lp2.x * r_l;
+                    sphi_s *= lp2.y * r_l;
+                    sphi_s *= M::rsqrt(lp1.x * lp1.x + lp1.y * lp1.y + lp1.z * lp1.z);
+                    s.prop.x = lp1.y * s.v.z - lp1.z * s.v.y;
+                    s.prop.y = lp1.z * s.v.x - lp1.x * s.v.z;
+                    s.prop.z = lp1.x * s.v.y - lp1.y * s.v.x;
+                    s.prop.w = 0.f;
+                    cphi_s *= M::rsqrt(s.prop.x * s.prop.x + s.prop.y * s.prop.y + s.prop.z * s.prop.z);
+                    s.v.x += cphi_s * s.prop.x + sphi_s * lp1.x;
+                    s.v.y += cphi_s * s.prop.y + sphi_s * lp1.y;
+                    s.v.z += cphi_s * s.prop.z + sphi_s * lp1.z;
+                    r_l = M::rsqrt(s.v.x * s.v.x + s.v.y * s.v.y + s.v.z * s.v.z);
+                    s.v.x *= r_l;
+                    s.v.y *= r_l;
+                    s.v.z *= r_l;
+                }
+            }
+            set_launch_voxel(a, s);
+            s.prop = make_float4(lpos.x + (lp1.x) * 0.5f, lpos.y + (lp1.y) * 0.5f, lpos.z + (lp1.z) * 0.5f, 0.f);
+            s.Lmove = -1.f;
+        }
+
+        if (fabsf(s.p.w) <= c_p.minenergy) {
+            continue;
+        }
+
+        if (c_p.nangle) {
+            float ang, sth, cth, sphi, cphi;
+            unsigned int na = c_p.nangle;
+            if (ldir.w > 0.f) {
+                ang = fminf(rnd(s.t) * (float)na, (float)na - K_EPS);
+                cphi = S.angleinvcdf[(int)(ang)];
+            } else {
+                ang = fminf(rnd(s.t) * (float)(na - 1), (float)(na - 1) - K_EPS);
+                sphi = ang - (float)((int)ang);
+                unsigned int a0 = ((unsigned int)ang >= na - 1 ? na - 1 : (unsigned int)(int)(ang));
+                unsigned int a1 = ((unsigned int)ang + 1 >= na - 1 ? na - 1 : (unsigned int)((int)(ang) + 1));
+                cphi = ((1.f - sphi) * S.angleinvcdf[a0] + sphi * S.angleinvcdf[a1]);
+            }
+            cphi *= K_ONE_PI;
+            M::sincos(cphi, &sth, &cth);
+            ang = K_TWO_PI * rnd(s.t);
+            M::sincos(ang, &sphi, &cphi);
+            if (ldir.w < 1.5f && ldir.w >= 0.f) {
+                s.v = ldir;
+            }
+            rotatevector<EXACT>(s.v, sth, cth, sphi, cphi);
+        } else if (s.Lmove < 0.f) {
+            if (isnan(ldir.w)) {
+                float ang, sth, cth, sphi, cphi;
+                ang = K_TWO_PI * rnd(s.t);
+                M::sincos(ang, &sphi, &cphi);
+                ang = M::acos(2.f * rnd(s.t) - 1.f);
+                M::sincos(ang, &sth, &cth);
+                rotatevector<EXACT>(s.v, sth, cth, sphi, cphi);
+            } else if (ldir.w < 0.f && isinf(ldir.w)) {
+                float ang, sth, cth, sphi, cphi;
+                ang = K_TWO_PI * rnd(s.t);
+                M::sincos(ang, &sphi, &cphi);
+                sth = M::sqrt(rnd(s.t));
+                cth = M::sqrt(1.f - sth * sth);
+                rotatevector<EXACT>(s.v, sth, cth, sphi, cphi);
+            } else if (ldir.w != 0.f) {
+                float Rn2 = (float)((ldir.w > 0.f) - (ldir.w < 0.f));
+                s.prop.x += ldir.w * s.v.x;
+                s.prop.y += ldir.w * s.v.y;
+                s.prop.z += ldir.w * s.v.z;
+                s.v.x = Rn2 * (s.prop.x - s.p.x);
+                s.v.y = Rn2 * (s.prop.y - s.p.y);
+                s.v.z = Rn2 * (s.prop.z - s.p.z);
+                Rn2 = M::rsqrt(s.v.x * s.v.x + s.v.y * s.v.y + s.v.z * s.v.z);
+                s.v.x *= Rn2;
+                s.v.y *= Rn2;
+                s.v.z *= Rn2;
+            }
+        }
+
+        if ((s.mediaid & K_MED_MASK) == 0) {
+            int idx = skipvoid<EXACT>(a, S, s.p, s.v, s.f, s.fx, s.fy, s.fz, s.fw);
+            if (idx >= 0) {
+                s.idx1d = (unsigned int)idx;
+                s.mediaid = media_at(a, s.idx1d);
+            }
+        }
+        s.fx = (int)(short)floorf(s.p.x);
+        s.fy = (int)(short)floorf(s.p.y);
+        s.fz = (int)(short)floorf(s.p.z);
+
+        s.w0 += 1.f;
+        if (s.w0 > (float)c_p.maxvoidstep) {
+            (*nfailed)++;
+            return -1;
+        }
+        if (!((s.mediaid & K_MED_MASK) == 0 || fabsf(s.p.w) <= c_p.minenergy)) {
+            break;
+        }
+    }
+
+    s.f.w += 1.f;
+    s.prop = S.prop[1];
+    updateprop(S, s.prop, s.mediaid);
+    s.launched += s.p.w;
+    s.w0 = s.p.w;
+    s.w0init = s.p.w;
+    s.v.w = K_EPS;
+    s.Lmove = 0.f;
+    return 0;
+}
+
+/* ------------------------------------------------------------------ kernel */
+
+/* exit flag of a relaunch through a detecting face (mcx_core.cl:3001, 3181) */
+__device__ __forceinline__ unsigned int exit_detflag(const Photon& s, unsigned int mediaidold) {
+    return (((s.idx1d == K_OUT_MAX && c_p.bc[9 + s.fw]) || (s.idx1d == K_OUT_MIN && c_p.bc[6 + s.fw]))
+            ? K_OUT_MIN : (mediaidold & K_DET_MASK));
+}
+
+__device__ __forceinline__ void vt_begin(const KArgs& a, Photon& s, unsigned int vt) {
+    s.p = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7fffffff));
+    s.v = make_float4(0.f, 0.f, 0.f, 0.f);
+    s.f = make_float4(0.f, 0.f, 0.f, 0.f);
+    s.mediaid = __float_as_uint(c_p.srcparam2.w);
+    s.isdet = 0;
+    s.idx1d = 0;
+    s.pathlen = 0.f;
+    s.fx = s.fy = s.fz = 0;
+    s.fw = -1;
+    s.esc = 0.f;
+    s.launched = 0.f;
+    s.w0init = 0.f;
+    s.srcsel = 0.f;
+    uint4 sd = __ldg(a.seeds + vt);
+    s.t.a = (unsigned long long)sd.x << 32 | sd.y;
+    s.t.b = (unsigned long long)sd.z << 32 | sd.w;
+}
+
+template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT>
+__global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
+    typedef Mth<EXACT> M;
+    extern __shared__ float4 smem4[];
+
+    /* stage the property table and inverse-CDF tables */
+    float4* sprop = smem4;
+    for (unsigned int i = threadIdx.x; i < c_p.medianum; i += blockDim.x) {
+        sprop[i] = a.gprop[i];
+    }
+    float* sf = (float*)(smem4 + c_p.medianum);
+    float* sinvcdf = sf;
+    for (unsigned int i = threadIdx.x; i < c_p.nphase; i += blockDim.x) {
+        sinvcdf[i] = a.invcdf[i];
+    }
+    float* sangle = sinvcdf + c_p.nphase;
+    for (unsigned int i = threadIdx.x; i < c_p.nangle; i += blockDim.x) {
+        sangle[i] = a.angleinvcdf[i];
+    }
+    __syncthreads();
+
+    Shared S;
+    S.prop = sprop;
+    S.invcdf = sinvcdf;
+    S.angleinvcdf = sangle;
+    S.pp = sangle + c_p.nangle + threadIdx.x;
+    S.stride = blockDim.x;
+
+    unsigned long long cnt_step = 0, cnt_scat = 0, cnt_launch = 0, cnt_refl = 0, cnt_fail = 0;
+
+    Photon s;
+    unsigned int vt = atomicAdd(a.vtcounter, 1u);
+    bool relaunch = false;         /* a relaunch request from the previous step */
+    unsigned int relaunch_isdet = 0;
+    bool fresh = true;             /* vt just claimed: initial launch */
+    unsigned int mediaidold = 0, idx1dold = 0;
+    unsigned int nsteps = 0;       /* steps of the current photon, against K_STEP_CAP */
+
+    while (vt < c_p.nthread) {
+        if (fresh || relaunch) {
+            int r;
+            if (fresh) {
+                vt_begin(a, s, vt);
+                if ((unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
+                    r = 1;
+                } else {
+                    r = launchnewphoton<EXACT, DET>(a, S, s, 0u, vt, &cnt_fail);
+                    if (r) {
+                        atomicAdd(a.status + ST_FAILED_LAUNCH, 1u);
+                        r = 2;       /* NO_LAUNCH: the reference returns without writing energies */
+                    }
+                }
+            } else {
+                r = launchnewphoton<EXACT, DET>(a, S, s, relaunch_isdet, vt, &cnt_fail);
+            }
+            fresh = false;
+            relaunch = false;
+            if (r) {
+                if (r != 2) {
+                    a.energy[vt] = make_float2(s.esc, s.launched);
+                }
+                vt = atomicAdd(a.vtcounter, 1u);
+                fresh = true;
+                continue;
+            }
+            if (COUNT) {
+                cnt_launch++;
+            }
+            nsteps = 0;
+            s.isdet = s.mediaid & K_DET_MASK;
+            s.mediaid &= K_MED_MASK;
+        }
+        if (++nsteps > K_STEP_CAP) {
+            atomicAdd(a.status + ST_GUARD, 1u);
+            relaunch = true;
+            relaunch_isdet = 0;
+            continue;
+        }
+
+        if (COUNT) {
+            cnt_step++;
+        }
+        /* ---- scattering (mcx_core.cl:2446-2649) */
+        if (s.f.x <= 0.f) {
+            s.f.x = rnd_scatlen<EXACT>(s.t);
+            if (s.v.w != K_EPS) {
+                float cphi = 1.f, sphi = 0.f, theta, stheta, ctheta, tmp0 = 0.f;
+                if (COUNT) {
+                    cnt_scat++;
+                }
+                if (!c_p.is2d) {
+                    tmp0 = K_TWO_PI * rnd(s.t);
+                    M::sincos(tmp0, &sphi, &cphi);
+                }
+                if (c_p.nphase > 2) {
+                    unsigned int np = c_p.nphase;
+                    tmp0 = rnd(s.t) * (float)(np - 1);
+                    theta = tmp0 - (float)((int)tmp0);
+                    unsigned int i0 = (unsigned int)tmp0 >= np ? np - 1 : (unsigned int)(int)(tmp0);
+                    unsigned int i1 = (unsigned int)tmp0 + 1 >= np ? np - 1 : (unsigned int)((int)(tmp0) + 1);
+                    tmp0 = (1.f - theta) * S.invcdf[i0] + theta * S.invcdf[i1];
+                    if (EXACT) {
+                        theta = M::acos(tmp0);
+                        stheta = M::sin(theta);
+                    } else {
+                        stheta = M::sqrt(fmaxf(0.f, 1.f - tmp0 * tmp0));
+                    }
+                    ctheta = tmp0;
+                } else {
+                    tmp0 = (s.v.w > (float)c_p.gscatter) ? 0.f : s.prop.z;
+                    if (fabsf(tmp0) > K_EPS) {
+                        /* Henyey-Greenstein, mcx_core.cl:2487-2493 */
+                        tmp0 = (1.f - s.prop.z * s.prop.z) / (1.f - s.prop.z + 2.f * s.prop.z * rnd(s.t));
+                        tmp0 *= tmp0;
+                        tmp0 = (1.f + s.prop.z * s.prop.z - tmp0) / (2.f * s.prop.z);
+                        tmp0 = fmaxf(-1.f, fminf(1.f, tmp0));
+                        if (EXACT) {
+                            theta = M::acos(tmp0);
+                            stheta = M::sin(theta);
+                        } else {
+                            stheta = M::sqrt(1.f - tmp0 * tmp0);
+                        }
+                        ctheta = tmp0;
+                    } else {
+                        if (EXACT) {
+                            theta = M::acos(2.f * rnd(s.t) - 1.f);
+                            M::sincos(theta, &stheta, &ctheta);
+                        } else {
+                            ctheta = 2.f * rnd(s.t) - 1.f;
+                            stheta = M::sqrt(1.f - ctheta * ctheta);
+                        }
+                    }
+                }
+                if (DET && c_p.savedet) {
+                    unsigned int med = (s.mediaid & K_MED_MASK) - 1;
+                    if (SAVE_NSCAT(c_p.savedetflag)) {
+                        float* q = S.pp + med * S.stride;
+                        *q = __uint_as_float(__float_as_uint(*q) + 1u);
+                    }
+                    if (SAVE_MOM(c_p.savedetflag)) {
+                        S.pp[(c_p.maxmedia * (SAVE_NSCAT(c_p.savedetflag) + SAVE_PPATH(c_p.savedetflag)) + med) * S.stride] += 1.f - ctheta;
+                    }
+                }
+                if (c_p.is2d) {
+                    rotatevector2d<EXACT>(s.v, (rnd(s.t) > 0.5f ? stheta : -stheta), ctheta, c_p.is2d);
+                } else {
+                    rotatevector<EXACT>(s.v, stheta, ctheta, sphi, cphi);
+                }
+                s.v.w += 1.f;
+            }
+            s.v.w = (float)(int)s.v.w;
+        }
+
+        s.n1 = s.prop.w;
+        updateprop(S, s.prop, s.mediaid);
+
+        /* ---- move to the next voxel face or the end of the free path */
+        s.f.z = hitgrid<EXACT>(s.p, s.v, s.fx, s.fy, s.fz, s.fw);
+        {
+            float slen = s.f.z * s.prop.y * (s.v.w + 1.f > (float)c_p.gscatter ? (1.f - s.prop.z) : 1.f);
+            slen = fminf(slen, s.f.x);
+            s.f.z = M::div(slen, s.prop.y * (s.v.w + 1.f > (float)c_p.gscatter ? (1.f - s.prop.z) : 1.f));
+            s.pathlen += s.f.z;
+            s.p.x = s.p.x + s.f.z * s.v.x;
+            s.p.y = s.p.y + s.f.z * s.v.y;
+            s.p.z = s.p.z + s.f.z * s.v.z;
+            bool scat_here = (slen == s.f.x);
+            if (s.fw == 0) {
+                s.fx += scat_here ? 0 : (s.v.x > 0.f ? 1 : -1);
+            }
+            if (s.fw == 1) {
+                s.fy += scat_here ? 0 : (s.v.y > 0.f ? 1 : -1);
+            }
+            if (s.fw == 2) {
+                s.fz += scat_here ? 0 : (s.v.z > 0.f ? 1 : -1);
+            }
+            s.p.w *= M::exp(-s.prop.x * s.f.z);
+            s.f.x -= slen;
+            s.f.y += s.f.z * s.prop.w * c_p.oneoverc0;
+        }
+        if (DET && c_p.savedet && SAVE_PPATH(c_p.savedetflag)) {
+            S.pp[(c_p.maxmedia * SAVE_NSCAT(c_p.savedetflag) + (s.mediaid & K_MED_MASK) - 1) * S.stride] += s.f.z;
+        }
+
+        /* ---- new voxel (mcx_core.cl:2795-2811) */
+        mediaidold = s.mediaid | s.isdet;
+        idx1dold = s.idx1d;
+        s.idx1d = vox_index(s.fx, s.fy, s.fz);
+        if (!inside_u(s.fx, s.fy, s.fz)) {
+            s.mediaid = 0;
+            s.idx1d = (s.fx < 0 || s.fy < 0 || s.fz < 0) ? K_OUT_MIN : K_OUT_MAX;
+            s.isdet = c_p.bc[(s.idx1d == K_OUT_MAX) * 3 + s.fw];
+            s.isdet = ((s.isdet & 0xF) == bcUnknown) ? (c_p.doreflect ? bcReflect : bcAbsorb) : s.isdet;
+        } else {
+            s.mediaid = media_at(a, s.idx1d);
+            s.isdet = s.mediaid & K_DET_MASK;
+            s.mediaid &= K_MED_MASK;
+        }
+
+        /* ---- deposit on a voxel change (mcx_core.cl:2816-2929) */
+        {
+            bool dep = false;
+            unsigned int key = 0;
+            float weight = 0.f;
+            if (s.idx1d != idx1dold && idx1dold < c_p.nvox && mediaidold) {
+                if (c_p.save2pt && s.f.y >= c_p.twin0 && s.f.y < c_p.twin1) {
+                    int tshift = (int)(floorf((s.f.y - c_p.twin0) * c_p.Rtstep));
+                    if (c_p.outputtype == otEnergy) {
+                        weight = s.w0 - s.p.w;
+                    } else if (c_p.outputtype == otFluence || c_p.outputtype == otFlux) {
+                        weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen) : M::div(s.w0 - s.p.w, s.prop.x);
+                    } else if (c_p.outputtype == otL) {
+                        weight = s.w0 * s.pathlen;
+                    }
+                    if (c_p.extrasrclen && (c_p.srcid < 0)) {
+                        tshift += ((int)s.srcsel - 1) * (int)c_p.maxgate;
+                    }
+                    dep = fabsf(weight) > 0.f;
+                    key = idx1dold + (unsigned int)tshift * c_p.nvox;
+                    /* a time of flight a rounding below twin1 can give tshift == maxgate;
+                       the reference then writes into its shadow half, which its host adds
+                       to gate 0 -- the low plane here plays that role */
+                    if (key >= c_p.fieldlen) {
+                        key -= c_p.fieldlen;
+                    }
+                }
+                s.w0 = s.p.w;
+                s.pathlen = 0.f;
+            } else {
+                s.mediaid = mediaidold;
+            }
+            deposit<WAGG>(a.field, c_p.fieldlen, dep, key, weight);
+        }
+
+        /* ---- exit, time-out or cyclic boundary (mcx_core.cl:2958-3028) */
+        if ((s.mediaid == 0 && ((s.isdet & 0xF) == bcAbsorb || (s.isdet & 0xF) == bcCyclic ||
+                                ((s.isdet & 0xF) == bcReflect && s.n1 == S.prop[0].w))) || s.f.y > c_p.twin1) {
+            if (s.isdet == bcCyclic) {
+                if (s.fw == 0) {
+                    s.p.x = nextafter_ref(rintf(((s.idx1d == K_OUT_MIN) ? c_p.maxidx.x : 0)), (s.v.x > 0.f) - (s.v.x < 0.f));
+                    s.fx = (int)(short)floorf(s.p.x);
+                }
+                if (s.fw == 1) {
+                    s.p.y = nextafter_ref(rintf(((s.idx1d == K_OUT_MIN) ? c_p.maxidx.y : 0)), (s.v.y > 0.f) - (s.v.y < 0.f));
+                    s.fy = (int)(short)floorf(s.p.y);
+                }
+                if (s.fw == 2) {
+                    s.p.z = nextafter_ref(rintf(((s.idx1d == K_OUT_MIN) ? c_p.maxidx.z : 0)), (s.v.z > 0.f) - (s.v.z < 0.f));
+                    s.fz = (int)(short)floorf(s.p.z);
+                }
+                if (inside_u(s.fx, s.fy, s.fz)) {
+                    s.idx1d = vox_index(s.fx, s.fy, s.fz);
+                    s.mediaid = media_at(a, s.idx1d);
+                    s.isdet = s.mediaid & K_DET_MASK;
+                    s.mediaid &= K_MED_MASK;
+                    continue;
+                }
+            }
+            relaunch = true;
+            relaunch_isdet = exit_detflag(s, mediaidold);
+            continue;
+        }
+
+        /* ---- Russian roulette (mcx_core.cl:3031-3061) */
+        if (fabsf(s.p.w) < c_p.minenergy) {
+            if (rnd(s.t) * K_ROULETTE <= 1.f) {
+                s.p.w *= K_ROULETTE;
+            } else {
+                relaunch = true;
+                relaunch_isdet = mediaidold & K_DET_MASK;
+                continue;
+            }
+        }
+
+        /* ---- Fresnel reflection / refraction (mcx_core.cl:3126-3278) */
+        if (REFL && c_p.dorefl_compiled) {
+            updateprop(S, s.prop, s.mediaid);
+            if (((s.mediaid && c_p.doreflect) ||
+                 (s.mediaid == 0 && (((s.isdet & 0xF) == bcUnknown && c_p.doreflect) ||
+                                     ((s.isdet & 0xF) == bcReflect || (s.isdet & 0xF) == bcMirror)))) &&
+                (((s.isdet & 0xF) == bcMirror) ||
+                 s.n1 != ((c_p.mediaformat < 100) ? (s.prop.w)
+                          : (S.prop[(s.mediaid > 0 && c_p.mediaformat >= 100) ? 1 : s.mediaid].w)))) {
+                float Rtotal = 1.f;
+                if (COUNT) {
+                    cnt_refl++;
+                }
+                updateprop(S, s.prop, s.mediaid);
+                float tmp0 = s.n1 * s.n1;
+                float tmp1 = s.prop.w * s.prop.w;
+                float cphi = fabsf(vcomp(s.v, s.fw));
+                float sphi = 1.f - cphi * cphi;
+                s.f.z = 1.f - M::div(tmp0, tmp1) * sphi;
+                if (s.f.z > 0.f && (s.isdet & 0xF) != bcMirror) {
+                    float ctheta = tmp0 * cphi * cphi + tmp1 * s.f.z;
+                    float stheta = 2.f * s.n1 * s.prop.w * cphi * M::sqrt(s.f.z);
+                    Rtotal = M::div(ctheta - stheta, ctheta + stheta);
+                    ctheta = tmp1 * cphi * cphi + tmp0 * s.f.z;
+                    Rtotal = (Rtotal + M::div(ctheta - stheta, ctheta + stheta)) * 0.5f;
+                }
+                if (Rtotal < 1.f && (!(s.mediaid == 0 && ((s.isdet & 0xF) == bcMirror))) && rnd(s.t) > Rtotal) {
+                    transmit<EXACT>(s.v, s.n1, s.prop.w, s.fw);
+                    if (s.mediaid == 0) {
+                        relaunch = true;
+                        relaunch_isdet = exit_detflag(s, mediaidold);
+                        continue;
+                    }
+                } else {
+                    if (s.fw == 0) {
+                        s.v.x = -s.v.x;
+                        s.p.x = nextafter_ref(rintf(s.p.x), (int)((float)(s.v.x > 0.f) - 0.5f));
+                        s.fx = (int)(short)rintf(s.p.x);
+                    } else if (s.fw == 1) {
+                        s.v.y = -s.v.y;
+                        s.p.y = nextafter_ref(rintf(s.p.y), (int)((float)(s.v.y > 0.f) - 0.5f));
+                        s.fy = (int)(short)rintf(s.p.y);
+                    } else {
+                        s.v.z = -s.v.z;
+                        s.p.z = nextafter_ref(rintf(s.p.z), (int)((float)(s.v.z > 0.f) - 0.5f));
+                        s.fz = (int)(short)rintf(s.p.z);
+                    }
+                    if (idx1dold >= c_p.nvox) {
+                        /* unreachable for a photon that came from inside the volume */
+                        atomicAdd(a.status + ST_GUARD, 1u);
+                        relaunch = true;
+                        relaunch_isdet = 0;
+                        continue;
+                    }
+                    s.idx1d = idx1dold;
+                    unsigned int m = media_at(a, s.idx1d);
+                    s.mediaid = m & K_MED_MASK;
+                    /* take the detector bit of the voxel the photon is back in (the
+                       reference keeps the face code here, which mcx_core.cl:2796 then
+                       ORs into the medium index) */
+                    s.isdet = m & K_DET_MASK;
+                    updateprop(S, s.prop, s.mediaid);
+                    s.n1 = s.prop.w;
+                }
+            }
+        }
+    }
+
+    if (COUNT) {
+        atomicAdd(a.counters + 0, cnt_step);
+        atomicAdd(a.counters + 1, cnt_scat);
+        atomicAdd(a.counters + 2, cnt_launch);
+        atomicAdd(a.counters + 3, cnt_refl);
+        atomicAdd(a.counters + 4, cnt_fail);
+    }
+}
+
+/* -D R: each reference thread writes its RNG stream into the field
+   (mcx_core.cl:2408-2414) */
+__global__ void mcx_rng_dump(const KArgs a) {
+    for (unsigned int vt = blockIdx.x * blockDim.x + threadIdx.x; vt < c_p.nthread; vt += gridDim.x * blockDim.x) {
+        if ((unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
+            continue;
+        }
+        uint4 sd = a.seeds[vt];
+        Rng t;
+        t.a = (unsigned long long)sd.x << 32 | sd.y;
+        t.b = (unsigned long long)sd.z << 32 | sd.w;
+        for (unsigned int j = vt; j < c_p.fieldlen; j += c_p.nthread) {
+            a.field[j] = rnd(t);
+        }
+    }
+}
+
+}  // namespace
+}  // namespace mcxg
+
+#endif

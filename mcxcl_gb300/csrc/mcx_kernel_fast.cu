@@ -1,0 +1,62 @@
+/*
+ * mcx_kernel_fast.cu -- the production instantiations of the transport
+ * kernel: MUFU transcendentals (__logf, __expf, __sincosf, rsqrtf,
+ * __fdividef).  Compiled with --use_fast_math.
+ */
+#include "mcx_kernel.cuh"
+#include "mcx_launch.h"
+
+namespace mcxg {
+
+cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,
+                        unsigned int nsrcx, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_p, p, sizeof(*p), 0, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && ndet) {
+        e = cudaMemcpyToSymbolAsync(c_det, det4, sizeof(float) * 4 * ndet, 0, cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess && nsrcx) {
+        e = cudaMemcpyToSymbolAsync(c_srcx, srcx16, sizeof(float) * 16 * nsrcx, 0, cudaMemcpyHostToDevice, st);
+    }
+    return e;
+}
+
+template <bool DET, bool REFL, bool WAGG>
+static void* kfun() {
+    return (void*)mcx_transport<false, DET, REFL, WAGG, false>;
+}
+
+static void* select(int flags) {
+    const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG;
+    if (wagg) {
+        if (det) {
+            return refl ? kfun<true, true, true>() : kfun<true, false, true>();
+        }
+        return refl ? kfun<false, true, true>() : kfun<false, false, true>();
+    }
+    if (det) {
+        return refl ? kfun<true, true, false>() : kfun<true, false, false>();
+    }
+    return refl ? kfun<false, true, false>() : kfun<false, false, false>();
+}
+
+cudaError_t fast_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st) {
+    void* f = select(flags);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) {
+            return e;
+        }
+    }
+    void* args[] = {(void*)&a};
+    return cudaLaunchKernel(f, dim3(grid), dim3(block), args, smem, st);
+}
+
+cudaError_t fast_occupancy(int flags, int block, size_t smem, int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, select(flags), block, smem);
+}
+
+cudaError_t fast_attributes(int flags, cudaFuncAttributes* attr) {
+    return cudaFuncGetAttributes(attr, select(flags));
+}
+
+}  // namespace mcxg

@@ -1,0 +1,67 @@
+/*
+ * mcx_kparams.h -- the transport kernel's constant parameter block.
+ *
+ * Plain C so the C host driver and the CUDA translation units share one
+ * definition.  Field meanings follow the reference's MCXParam
+ * (src/mcx_host.h:106-166); fields the GB300 kernel does not read (cache box,
+ * polarisation, RF, trajectory debug) are left out, and a few are added for
+ * the persistent work queue and the uint8 volume.
+ */
+#ifndef MCX_KPARAMS_H
+#define MCX_KPARAMS_H
+
+#include <stdint.h>
+
+#define MCXG_MAX_DET       1024   /* detectors held in constant memory */
+#define MCXG_MAX_EXTRASRC  64     /* additional sources held in constant memory */
+#define MCXG_MAX_MEDIA     1024   /* property rows staged in shared memory */
+
+typedef struct mcxg_float4 {
+    float x, y, z, w;
+} mcxg_float4;
+
+typedef struct mcxg_kparams {
+    mcxg_float4 srcpos, srcdir, srcparam1, srcparam2; /* launch source; param2.z/.w carry the
+                                                          launch voxel / medium bits of a point source */
+    mcxg_float4 maxidx;            /* volume extent (x, y, z) as floats, for bounds tests */
+    uint32_t dimx, dimxy, nvox;    /* strides: x fastest, then y, then z */
+    uint32_t fieldlen;             /* gates x voxels (x sources when srcid < 0) */
+    float twin0, twin1;            /* time window of this launch (s) */
+    float oneoverc0;               /* 1/c0 in s per grid unit */
+    float Rtstep;                  /* 1/tstep */
+    float minenergy;               /* Russian-roulette threshold */
+    float minaccumtime;            /* time per void step in skipvoid */
+    uint32_t doreflect;            /* Fresnel at label boundaries */
+    uint32_t dorefl_compiled;      /* reflection block active (isreflect or an r/m face) */
+    uint32_t save2pt;              /* deposit into the field */
+    uint32_t savedet;              /* 0 off, 1 on, 3 stop when the record buffer fills */
+    uint32_t maxdetphoton;
+    uint32_t maxmedia;             /* medianum - 1 */
+    uint32_t medianum;
+    uint32_t detnum;
+    uint32_t voidtime;
+    uint32_t srctype;
+    uint32_t maxvoidstep;
+    uint32_t issaveseed;
+    uint32_t issaveref;
+    uint32_t isspecular;
+    uint32_t maxgate;
+    uint32_t outputtype;
+    uint32_t threadphoton;         /* photons per reference thread */
+    int32_t  oddphoton;            /* the first oddphoton threads run one more */
+    uint32_t savedetflag;
+    uint32_t reclen;               /* floats per detected-photon record */
+    uint32_t partialdata;          /* per-medium record floats */
+    uint32_t mediaformat;          /* 1/2/4 labels, 101 float mua */
+    uint32_t gscatter;
+    uint32_t is2d;
+    uint32_t nphase, nangle;       /* inverse-CDF table lengths */
+    uint32_t extrasrclen;
+    int32_t  srcid;
+    uint32_t nthread;              /* reference threads = independent RNG streams */
+    uint32_t mediaword;            /* bytes per voxel in device memory: 1 (label | det<<7) or 4 */
+    uint32_t npattern;             /* source pattern length, for index clamping */
+    uint8_t  bc[12];               /* face conditions then detector flags, as small integers */
+} mcxg_kparams;
+
+#endif

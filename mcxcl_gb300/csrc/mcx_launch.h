@@ -1,0 +1,51 @@
+/*
+ * mcx_launch.h -- internal interface between the session code (mcx_device.cu)
+ * and the two kernel translation units.  Each unit owns its own copy of the
+ * constant block, so each exports its own upload and launch entry.
+ */
+#ifndef MCX_LAUNCH_H
+#define MCX_LAUNCH_H
+
+#include <cuda_runtime.h>
+
+#include "mcx_kparams.h"
+
+namespace mcxg {
+
+/* device pointers handed to the transport kernel */
+struct KArgs {
+    const uint8_t* media8;
+    const uint32_t* media32;
+    const float4* gprop;
+    const float* invcdf;
+    const float* angleinvcdf;
+    const float* srcpattern;
+    const uint4* seeds;            /* 4 x 32-bit seed words per reference thread */
+    float* field;                  /* [fieldlen] high plane, then [fieldlen] low plane */
+    float2* energy;                /* per reference thread: escaped, launched weight */
+    float* detp;                   /* maxdetphoton x reclen */
+    unsigned long long* detseed;   /* maxdetphoton x 2 */
+    unsigned int* detcount;
+    unsigned int* vtcounter;       /* work queue head */
+    unsigned int* status;
+    unsigned long long* counters;  /* step, scatter, launch, reflect, failed */
+};
+
+/* flag bits for the launch entries */
+enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4 };
+
+/* fast instantiation: hardware transcendental approximations */
+cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,
+                        unsigned int nsrcx, cudaStream_t st);
+cudaError_t fast_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st);
+cudaError_t fast_occupancy(int flags, int block, size_t smem, int* blocks_per_sm);
+cudaError_t fast_attributes(int flags, cudaFuncAttributes* attr);
+
+/* exact instantiation: IEEE basic operations only, bit-identical to the oracle */
+cudaError_t exact_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,
+                         unsigned int nsrcx, cudaStream_t st);
+cudaError_t exact_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st);
+cudaError_t exact_rngdump(const KArgs& a, int grid, int block, cudaStream_t st);
+}  // namespace mcxg
+
+#endif

@@ -1,0 +1,312 @@
+"""The ``pmcxcl`` Python interface, backed by the GB300 transport path.
+
+``run(**cfg)`` takes the reference module's keys and returns the same output
+dictionary (src/pmcxcl.cpp:428-1553): the dict is turned into a `Config`
+(parse_config, 428-1110), validated, simulated through the C ABI
+(mcx_run_simulation) and unpacked (1263-1521).  ``gpuinfo()`` and
+``version()`` mirror the reference's module functions (1600-1664).
+
+Arrays follow the reference's conventions: volumes and outputs are
+Fortran-ordered (x fastest), ``flux`` is ``[Nx, Ny, Nz, gates]``, ``detp`` is
+``[reclen, ndetected]`` and ``seeds`` is ``uint8 [16, ndetected]``.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import Config, ExtraSrc, Float4, GPUInfo, Medium
+
+SRCTYPES = ["pencil", "isotropic", "cone", "gaussian", "planar", "pattern", "fourier", "arcsine", "disk",
+            "fourierx", "fourierx2d", "zgaussian", "line", "slit", "pencilarray", "pattern3d", "hyperboloid",
+            "ring"]
+OUTPUTTYPES = ["flux", "fluence", "energy", "jacobian", "nscat", "wl", "wp", "wm", "rf", "length", "rfmus",
+               "wltof", "wptof", "adjoint", "adjoint_dcoeff", "adjoint_mus", "adjoint_musp", "adjoint_mua_d",
+               "adjoint_mua_musp"]
+SAVEFLAGS = "DSPMXVWI"
+DEBUGFLAGS = "RMP"
+
+_SCALARS_INT = ["nphoton", "nblocksize", "nthread", "maxdetphoton", "maxgate", "respin", "isreflect", "isrefint",
+                "isnormalized", "isgpuinfo", "issrcfrom0", "autopilot", "voidtime", "issaveref", "maxvoidstep",
+                "gscatter", "srcnum", "srcid", "isatomic", "internalsrc", "issavedet", "exactmath",
+                "savethreadenergy"]
+_SCALARS_BOOL = ["issaveexit", "ismomentum", "isspecular", "issave2pt", "issaveseed"]
+_SCALARS_FLOAT = ["tstart", "tstep", "tend", "minenergy", "unitinmm"]
+
+
+class MCXError(RuntimeError):
+    """Raised when the simulation reports an error (the reference raises RuntimeError)."""
+
+
+def _cbuf(arr, ctype):
+    """Copy a numpy array into malloc'd memory owned by the Config (freed by mcx_clearcfg)."""
+    arr = np.ascontiguousarray(arr)
+    libc = _lib.libc()
+    libc.malloc.restype = ctypes.c_void_p
+    libc.malloc.argtypes = [ctypes.c_size_t]
+    p = libc.malloc(max(arr.nbytes, 1))
+    if not p:
+        raise MemoryError("malloc failed")
+    ctypes.memmove(p, arr.ctypes.data, arr.nbytes)
+    return ctypes.cast(p, ctypes.POINTER(ctype))
+
+
+def _rows(v, ncol):
+    a = np.asarray(v, dtype=np.float32)
+    if a.ndim == 1:
+        a = a.reshape(1, -1)
+    if a.shape[1] > ncol:
+        raise ValueError("too many columns")
+    return a
+
+
+def _flags(s, letters):
+    if isinstance(s, (int, np.integer)):
+        return int(s)
+    v = 0
+    for ch in str(s).upper():
+        if ch in letters:
+            v |= 1 << letters.index(ch)
+    return v
+
+
+def _set_volume(C, vol):
+    """parseVolume (src/pmcxcl.cpp:93-426): dtype decides the media format."""
+    vol = np.asarray(vol)
+    if vol.dtype == np.float32 and vol.ndim == 4 and vol.shape[0] == 1:
+        words = np.asfortranarray(vol[0]).reshape(-1, order="F").view(np.uint32)
+        C.mediabyte = 101
+        dims = vol.shape[1:]
+    elif vol.dtype in (np.uint8, np.int8, np.uint16, np.int16, np.int32, np.uint32, np.int64, np.bool_):
+        if vol.ndim == 2:
+            vol = vol.reshape(vol.shape + (1,))
+        if vol.ndim != 3:
+            raise ValueError("the 'vol' field must be a 3D array of labels (or float32 [1,Nx,Ny,Nz] mua)")
+        words = np.asfortranarray(vol).reshape(-1, order="F").astype(np.uint32)
+        C.mediabyte = {1: 1, 2: 2}.get(vol.dtype.itemsize, 4)
+        dims = vol.shape
+    else:
+        raise TypeError("unsupported volume dtype %s" % vol.dtype)
+    C.dim.x, C.dim.y, C.dim.z = [int(d) for d in dims]
+    C.vol = _cbuf(words, ctypes.c_uint)
+
+
+def _set_sources(C, cfg):
+    keys = ("srcpos", "srcdir", "srcparam1", "srcparam2")
+    rows = {k: _rows(cfg[k], 4) for k in keys if k in cfg}
+    n = max([r.shape[0] for r in rows.values()] + [1])
+    for k, r in rows.items():
+        f = getattr(C, k)
+        vals = list(r[0]) + [None] * (4 - r.shape[1])
+        for comp, v in zip("xyzw", vals):
+            if v is not None:
+                setattr(f, comp, float(v))
+    if n > 1:
+        extra = (ExtraSrc * (n - 1))()
+        for i in range(1, n):
+            e = extra[i - 1]
+            e.srcpos.w = 1.0
+            for k, r in rows.items():
+                if i < r.shape[0]:
+                    f = getattr(e, k)
+                    for comp, v in zip("xyzw", r[i]):
+                        setattr(f, comp, float(v))
+        C.extrasrclen = n - 1
+        arr = np.frombuffer(extra, dtype=np.float32).copy()
+        C.srcdata = _cbuf(arr, ExtraSrc)
+
+
+def parse_config(cfg, C):
+    """Fill a Config from a pmcxcl-style dict (src/pmcxcl.cpp:428-1110)."""
+    L = _lib.load()
+    L.mcx_initcfg(ctypes.byref(C))
+    C.parentid = _lib.mpPython
+    C.flog = None
+    for k in _SCALARS_INT:
+        if k in cfg:
+            v = int(cfg[k])
+            setattr(C, k, bytes([v & 0xFF]) if isinstance(getattr(C, k), bytes) else v)
+    for k in _SCALARS_BOOL:
+        if k in cfg:
+            setattr(C, k, bytes([1 if cfg[k] else 0]))
+    for k in _SCALARS_FLOAT:
+        if k in cfg:
+            setattr(C, k, float(cfg[k]))
+    if "steps" in cfg:
+        s = np.asarray(cfg["steps"], np.float32).ravel()
+        C.steps.x, C.steps.y, C.steps.z = [float(x) for x in s[:3]]
+    if "vol" not in cfg:
+        raise ValueError("Configuration must specify a 2/3/4D volume.")
+    _set_volume(C, cfg["vol"])
+    _set_sources(C, cfg)
+    if "detpos" in cfg and np.asarray(cfg["detpos"]).size:
+        d = _rows(cfg["detpos"], 4)
+        if d.shape[1] != 4:
+            raise ValueError("the 'detpos' field must have 4 columns (x,y,z,radius)")
+        C.detnum = d.shape[0]
+        C.detpos = _cbuf(d, Float4)
+    if "prop" not in cfg:
+        raise ValueError("You must define 'vol' and 'prop' field.")
+    p = _rows(cfg["prop"], 4)
+    if p.shape[1] != 4:
+        raise ValueError("the 'prop' field must have 4 columns (mua,mus,g,n)")
+    C.medianum = p.shape[0]
+    C.prop = _cbuf(p, Medium)
+    if "session" in cfg:
+        C.session = str(cfg["session"]).encode()[:63]
+    if "srctype" in cfg:
+        st = str(cfg["srctype"]).lower()
+        if st not in SRCTYPES:
+            raise ValueError("the specified source type is not supported")
+        C.srctype = bytes([SRCTYPES.index(st)])
+    if "outputtype" in cfg:
+        ot = str(cfg["outputtype"]).lower()
+        if ot not in OUTPUTTYPES:
+            raise ValueError("the specified output type is not supported")
+        idx = OUTPUTTYPES.index(ot)
+        if idx >= 5:                 # the reference maps wl to jacobian, wp to nscat
+            idx -= 2
+        C.outputtype = bytes([idx])
+    if "debuglevel" in cfg:
+        C.debuglevel = _flags(cfg["debuglevel"], DEBUGFLAGS)
+    if "savedetflag" in cfg:
+        C.savedetflag = _flags(cfg["savedetflag"], SAVEFLAGS)
+    if "srcpattern" in cfg:
+        pat = np.asarray(cfg["srcpattern"], np.float32).reshape(-1, order="F")
+        C.srcpattern = _cbuf(pat, ctypes.c_float)
+    if "invcdf" in cfg:
+        t = np.asarray(cfg["invcdf"], np.float32).ravel()
+        C.nphase = t.size
+        C.invcdf = _cbuf(t, ctypes.c_float)
+    if "angleinvcdf" in cfg:
+        t = np.asarray(cfg["angleinvcdf"], np.float32).ravel()
+        C.nangle = t.size
+        C.angleinvcdf = _cbuf(t, ctypes.c_float)
+    if "bc" in cfg:
+        b = str(cfg["bc"]).encode()
+        if not b or len(b) > 12:
+            raise ValueError("the 'bc' field must be a non-empty string of at most 12 characters")
+        C.bc = b + b"\0" * (13 - len(b))
+    if "seed" in cfg:
+        sv = cfg["seed"]
+        if isinstance(sv, (int, float, np.integer, np.floating)):
+            C.seed = int(sv)
+        else:
+            raise ValueError("photon replay (cfg.seed as a seed array) is not part of this build")
+    if "gpuid" in cfg:
+        g = cfg["gpuid"]
+        C.deviceid = b"\0" * 256
+        if isinstance(g, (int, np.integer)):
+            if not 0 < g < 256:
+                raise ValueError("GPU id must be positive and can not be more than 256")
+            C.deviceid = b"0" * (g - 1) + b"1"
+        else:
+            C.deviceid = str(g).encode()[:256]
+    if "workload" in cfg:
+        w = np.asarray(cfg["workload"], np.float32).ravel()
+        for i, v in enumerate(w[:256]):
+            C.workload[i] = float(v)
+    return C
+
+
+def _check(C):
+    if C.errorcode:
+        raise MCXError("MCX ERROR(%d): %s" % (C.errorcode, C.errormsg.decode(errors="replace")))
+
+
+def run(cfg=None, **kwargs):
+    """Run one simulation; returns the reference's output dictionary.
+
+    Extra (GB300) keys accepted: ``exactmath`` -- run the IEEE-only kernel
+    that reproduces the CPU oracle bit for bit (slower, for verification)."""
+    cfg = dict(cfg or {}, **kwargs)
+    L = _lib.load()
+    C = Config()
+    try:
+        parse_config(cfg, C)
+        L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
+        _check(C)
+        L.mcx_run_simulation(ctypes.byref(C), None, None)
+        _check(C)
+        return _outputs(cfg, C)
+    finally:
+        L.mcx_clearcfg(ctypes.byref(C))
+
+
+def _outputs(cfg, C):
+    """Assemble the output dictionary (src/pmcxcl.cpp:1263-1521)."""
+    L = _lib.load()
+    out = {}
+    reclen = L.mcx_detreclen(ctypes.byref(C))
+    ndet = C.detectedcount
+    if C.issaveseed != b"\0" and ndet:
+        seeds = np.ctypeslib.as_array(ctypes.cast(C.seeddata, ctypes.POINTER(ctypes.c_uint8)), shape=(ndet * 16,))
+        out["seeds"] = seeds.copy().reshape(ndet, 16).T
+    if C.issavedet != b"\0" and ndet:
+        d = np.ctypeslib.as_array(C.exportdetected, shape=(ndet * reclen,))
+        out["detp"] = d.copy().reshape(ndet, reclen).T
+    if C.issave2pt != b"\0":
+        gates = int((C.tend - C.tstart) / C.tstep + 0.5)
+        nsrc = C.extrasrclen + 1 if (C.extrasrclen and C.srcid < 0) else 1
+        n = C.dim.x * C.dim.y * C.dim.z * gates * nsrc
+        f = np.ctypeslib.as_array(C.exportfield, shape=(n,)).copy()
+        if nsrc > 1:
+            dims = (C.dim.x, C.dim.y, C.dim.z, gates, 1, nsrc)
+        else:
+            dims = (C.dim.x, C.dim.y, C.dim.z, gates)
+        flux = f.reshape(dims, order="F")
+        if C.issaveref:
+            vol = np.ctypeslib.as_array(C.vol, shape=(C.dim.x * C.dim.y * C.dim.z,))
+            mask = (vol & 0x7FFFFFFF).reshape((C.dim.x, C.dim.y, C.dim.z), order="F") != 0
+            dref = np.where(mask[..., None], 0.0, -flux.reshape(C.dim.x, C.dim.y, C.dim.z, -1)).astype(np.float32)
+            flux = np.where(mask[..., None], flux.reshape(C.dim.x, C.dim.y, C.dim.z, -1), 0.0).astype(np.float32)
+            out["dref"] = dref.reshape(dims, order="F") if dref.shape != dims else dref
+            flux = flux.reshape(dims)
+        out["flux"] = flux
+        out["stat"] = {
+            "runtime": C.runtime,
+            "nphoton": C.nphoton * (C.respin if C.respin > 1 else 1),
+            "energytot": C.energytot,
+            "energyabs": C.energyabs,
+            "normalizer": C.normalizer,
+            "unitinmm": C.unitinmm,
+            "workload": [C.workload[0]],
+            # GB300 additions
+            "kernelms": C.kernelms,
+            "detected": C.his.detected,
+            "energyesc": C.energyesc,
+            "failedlaunch": C.failedlaunch,
+        }
+        if C.exactmath:
+            out["stat"]["eventcount"] = dict(zip(("step", "scatter", "launch", "reflect", "failed"),
+                                                 [int(x) for x in C.eventcount]))
+    if C.savethreadenergy and C.exportenergy:
+        e = np.ctypeslib.as_array(C.exportenergy, shape=(2 * C.threadused,)).copy()
+        out["threadenergy"] = e.reshape(C.threadused, 2)
+    if cfg.get("dumpmask"):
+        vol = np.ctypeslib.as_array(C.vol, shape=(C.dim.x * C.dim.y * C.dim.z,)).copy()
+        out["vol"] = vol.reshape((C.dim.x, C.dim.y, C.dim.z), order="F")
+    return out
+
+
+def gpuinfo():
+    """List CUDA devices as the reference's pmcxcl.gpuinfo() lists OpenCL ones."""
+    L = _lib.load()
+    C = Config()
+    L.mcx_initcfg(ctypes.byref(C))
+    C.flog = None
+    info = ctypes.POINTER(GPUInfo)()
+    n = L.mcx_list_gpu(ctypes.byref(C), None, ctypes.byref(info))
+    out = []
+    for i in range(n):
+        g = info[i]
+        out.append({k: (getattr(g, k).decode() if k == "name" else getattr(g, k))
+                    for k in ("name", "id", "devcount", "major", "minor", "globalmem", "constmem", "sharedmem",
+                              "regcount", "clock", "sm", "core", "autoblock", "autothread", "maxgate")})
+    if n:
+        L.mcx_cleargpuinfo(ctypes.byref(info))
+    return out
+
+
+def version():
+    return _lib.load().mcx_version().decode()

@@ -45,7 +45,8 @@
 #define MED_MASK         0x7FFFFFFFu
 #define FILL_MAXDET      3
 #define MEDIA_MUA_FLOAT  101
-#define LAUNCH_ATTEMPT_CAP (1u << 24)  /* guard against a source that never yields weight */
+#define LAUNCH_ATTEMPT_CAP (1u << 16)  /* guard against a source that never yields weight */
+#define CONE_DRAW_CAP      (1u << 16)  /* guard against a cone of zero half-angle */
 
 enum { bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic };
 enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL };
@@ -694,9 +695,10 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
                 ang = K_TWO_PI * rng_next(s->t);
                 m_sincos(c, ang, &sphi, &cphi);
                 if (c->srctype == S_CONE) {
+                    unsigned int tries = 0;
                     do {
                         ang = (ls->p1.y > 0) ? K_TWO_PI * rng_next(s->t) : m_acos(c, 2.f * rng_next(s->t) - 1.f);
-                    } while (ang > ls->p1.x);
+                    } while (ang > ls->p1.x && ++tries < CONE_DRAW_CAP);
                 } else if (c->srctype == S_ISOTROPIC || c->variant == MCXO_VARIANT_NVCC) {
                     ang = m_acos(c, 2.f * rng_next(s->t) - 1.f);
                 } else {

@@ -1,0 +1,154 @@
+"""The C ABI without a GPU: the library loads, exports every symbol the public
+header declares, the Python mirror of Config matches the C layout, and
+errors come back as exceptions (library mode) instead of exiting."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "mcx_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mcxcl_gb300 import build
+    build.build()
+    from mcxcl_gb300 import _lib
+    return _lib.load()
+
+
+def _declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = set(re.findall(r"\b(mcxg?_[a-z0-9_]+)\s*\(", text))
+    return sorted(n for n in names if not n.isupper())
+
+
+def test_header_declarations_are_exported(lib):
+    from mcxcl_gb300 import _lib
+    declared = _declared_functions()
+    assert declared, "no declarations parsed"
+    missing = [n for n in declared if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(_lib.EXPORTS) == declared
+
+
+def test_config_layout_matches(lib):
+    from mcxcl_gb300 import _lib
+    assert lib.mcx_config_sizeof() == ctypes.sizeof(_lib.Config)
+    for name, _ in _lib.Config._fields_:
+        assert lib.mcx_config_offsetof(name.encode()) == getattr(_lib.Config, name).offset, name
+    assert lib.mcx_config_offsetof(b"no_such_field") == ctypes.c_size_t(-1).value
+
+
+def test_initcfg_defaults(lib):
+    """mcx_initcfg defaults, src/mcx_utils.c:203-366."""
+    from mcxcl_gb300 import _lib
+    C = _lib.Config()
+    lib.mcx_initcfg(ctypes.byref(C))
+    assert C.tend == pytest.approx(5e-9) and C.tstep == pytest.approx(5e-9)
+    assert C.nthread == 16384 and C.nblocksize == 64 and C.seed == 0x623F9A9E
+    assert C.isreflect == b"\x01" and C.isnormalized == b"\x01" and C.issavedet == b"\x01"
+    assert C.savedetflag == 5 and C.maxdetphoton == 1000000 and C.gscatter == 1000000000
+    assert C.maxvoidstep == 1000 and C.autopilot == b"\x01" and C.srcpos.w == 1.0
+    assert C.deviceid[0:1] == b"1"
+
+
+def test_device_layer_reports_no_device_cleanly(lib):
+    n = ctypes.c_int(-1)
+    rc = lib.mcxg_device_count(ctypes.byref(n))
+    if rc != 0:
+        assert n.value == 0
+    assert lib.mcxg_error_string(6) == b"no CUDA device"
+
+
+def test_validate_errors_raise(lib):
+    import mcxcl_gb300
+    vol = np.ones((4, 4, 4), np.uint8) * 3
+    with pytest.raises(mcxcl_gb300.MCXError, match="less than the labels"):
+        mcxcl_gb300.run(nphoton=10, vol=vol, prop=[[0, 0, 1, 1], [0.1, 1, 0, 1]], srcpos=[1, 1, 0],
+                        srcdir=[0, 0, 1])
+    with pytest.raises(mcxcl_gb300.MCXError, match="time gate"):
+        mcxcl_gb300.run(nphoton=10, vol=np.ones((4, 4, 4), np.uint8), prop=[[0, 0, 1, 1], [0.1, 1, 0, 1]],
+                        srcpos=[1, 1, 0], srcdir=[0, 0, 1], tstart=1e-9, tend=0.5e-9)
+    with pytest.raises(mcxcl_gb300.MCXError, match="unitary"):
+        mcxcl_gb300.run(nphoton=10, vol=np.ones((4, 4, 4), np.uint8), prop=[[0, 0, 1, 1], [0.1, 1, 0, 1]],
+                        srcpos=[1, 1, 0], srcdir=[0, 0, 2])
+    with pytest.raises(mcxcl_gb300.MCXError, match="Jacobian output"):
+        mcxcl_gb300.run(nphoton=10, vol=np.ones((4, 4, 4), np.uint8), prop=[[0, 0, 1, 1], [0.1, 1, 0, 1]],
+                        srcpos=[1, 1, 0], srcdir=[0, 0, 1], outputtype="jacobian")
+    with pytest.raises(ValueError):
+        mcxcl_gb300.run(nphoton=10, vol=np.ones((4, 4, 4), np.uint8), prop=[[0, 0, 1]], srcpos=[1, 1, 0])
+
+
+def test_pmath_bits_match_oracle_copy():
+    """The kernel's exact-math header and the oracle's copy produce the same bits."""
+    import subprocess
+    import tempfile
+    src = r'''
+#include <stdio.h>
+#include <stdint.h>
+#include <string.h>
+#include "mcx_pmath.cuh"
+#include "oracle_pmath.h"
+int main(void) {
+    uint32_t bad = 0, n = 0;
+    for (uint32_t k = 0; k < 2000000; k++) {
+        float u = (float)k / 2000000.f;
+        float xs[5] = {u + 1.19209290e-07f, -u * 40.f, u * 6.28318530717959f, 2.f * u - 1.f, u * 1e3f};
+        float a = pm_logf(xs[0]), b = opm_logf(xs[0]);
+        float c = pm_expf(xs[1]), d = opm_expf(xs[1]);
+        float s1, c1, s2, c2;
+        pm_sincosf(xs[2], &s1, &c1);
+        opm_sincosf(xs[2], &s2, &c2);
+        float e = pm_acosf(xs[3]), f = opm_acosf(xs[3]);
+        float g1, h1, g2, h2;
+        pm_sincosf(xs[4], &g1, &h1);
+        opm_sincosf(xs[4], &g2, &h2);
+        bad += memcmp(&a, &b, 4) != 0;
+        bad += memcmp(&c, &d, 4) != 0;
+        bad += memcmp(&s1, &s2, 4) != 0;
+        bad += memcmp(&c1, &c2, 4) != 0;
+        bad += memcmp(&e, &f, 4) != 0;
+        bad += memcmp(&g1, &g2, 4) != 0;
+        bad += memcmp(&h1, &h2, 4) != 0;
+        n += 7;
+    }
+    printf("%u %u\n", bad, n);
+    return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "mcxcl_gb300", "csrc"),
+                        "-I", os.path.join(ROOT, "oracle"), c, "-o", exe, "-lm"], check=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    assert out[0] == "0", out
+
+
+def test_pmath_accuracy():
+    """The oracle's deterministic math stays within a few ulp of double precision."""
+    import oracle
+    L = oracle.lib()
+    rs = np.random.RandomState(0)
+    for fn, ref, xs in (
+            (L.mcxo_pm_logf, np.log, rs.uniform(1.2e-7, 1.0, 20000)),
+            (L.mcxo_pm_expf, np.exp, rs.uniform(-80, 5, 20000)),
+            (L.mcxo_pm_acosf, np.arccos, rs.uniform(-1, 1, 20000))):
+        xs = xs.astype(np.float32)
+        got = np.array([fn(float(x)) for x in xs], np.float64)
+        want = ref(xs.astype(np.float64))
+        ulp = np.spacing(np.abs(want).astype(np.float32)).astype(np.float64)
+        err = np.abs(got - want) / np.maximum(ulp, 1e-45)
+        assert err.max() < 4.0, (fn.__name__, err.max())
+    s = ctypes.c_float()
+    c = ctypes.c_float()
+    for x in rs.uniform(0, 2 * np.pi, 20000).astype(np.float32):
+        L.mcxo_pm_sincosf(ctypes.c_float(x), ctypes.byref(s), ctypes.byref(c))
+        assert abs(s.value - np.sin(np.float64(x))) < 3e-7
+        assert abs(c.value - np.cos(np.float64(x))) < 3e-7
