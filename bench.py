@@ -1,0 +1,334 @@
+"""Benchmark: photons/ms of the GB300 transport kernel on the cube-with-sphere
+workload (60^3 voxels, radius-15 sphere of a second medium, Fresnel on, 50
+gates of 0.1 ns, four disk detectors saving detector id, per-medium scatter
+counts and partial paths; 1e8 photons per step).
+
+One step = one full simulation of the workload.  Prints one JSON line.
+
+  value  : photons / ms of kernel time with every input resident in HBM
+           (the problem is uploaded once; each step launches the transport
+           kernel on it; CUDA events on the launching stream; L2 flushed
+           between steps by a 256 MB write, since the working set -- volume,
+           field, records -- fits in L2).
+  e2e    : the same metric through the public API (mcxcl_gb300.run) with host
+           buffers: dict -> Config, validation, detector masking, upload of
+           the volume and seeds, the kernel, FP64 reductions, readback of the
+           normalised field and the detected-photon records.
+  roofline: FP32 issue -- the kernel's FP32 operations from a frozen operation
+           model (48 per step + 65 per scattering + 20 per launch + 10 per
+           Fresnel test) times event counts measured by the exact kernel on a
+           sample of the same workload, over kernel time, against the FP32
+           issue peak measured in the same run.
+  cpu_baseline: the CPU oracle (a C restatement of the reference kernel) on
+           all host cores, on a bounded sample of the workload.
+
+--impl reference times the reference's CPU path (the oracle, since the
+reference's OpenCL build does not run on this machine) on the host cores.
+Multi-GPU: replicas only (photons do not exchange anything); each rank runs
+the full workload with its own seed.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# frozen FP32 operation model (weights per event)
+OPS_PER_STEP, OPS_PER_SCATTER, OPS_PER_LAUNCH, OPS_PER_REFLECT = 48, 65, 20, 10
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_mcx_transport_config2.txt")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--photons", type=float, default=None, help="override photons per step")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) while the timed region runs."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(photons=None):
+    from mcxcl_gb300 import workloads
+    cfg = workloads.config(2)
+    if photons:
+        cfg["nphoton"] = int(photons)
+    return cfg
+
+
+def cpu_baseline(cfg, target_s=15.0, kind="port"):
+    """The oracle on every host core, on a sample sized to ~target_s seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    ncores = os.cpu_count() or 1
+    nthread = 16384
+    probe = dict(cfg, nphoton=20000)
+    t0 = time.perf_counter()
+    oracle.run(probe, nthread=nthread, core=nthread, mathmode=oracle.MATH_LIBM, nworkers=ncores)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    n = int(min(cfg["nphoton"], max(20000, 20000 * target_s / dt)))
+    sample = dict(cfg, nphoton=n)
+    t0 = time.perf_counter()
+    r = oracle.run(sample, nthread=nthread, core=nthread, mathmode=oracle.MATH_LIBM, nworkers=ncores)
+    dt = time.perf_counter() - t0
+    return {"value": n / (dt * 1e3), "unit": "photons/ms", "cores": ncores, "kind": kind,
+            "sample": "%d photons of the %d-photon workload, %d reference threads, OpenMP over %d cores, %.1f s"
+                      % (n, int(cfg["nphoton"]), nthread, ncores, dt),
+            "absorbed": (r["stat"]["energytot"] - r["stat"]["energyesc"]) / r["stat"]["energytot"]}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    cfg = workload(args.photons)
+    res = None
+    vals = []
+    for i in range(args.warmup + args.steps):
+        res = cpu_baseline(cfg, target_s=5.0, kind="port")
+        if i >= args.warmup:
+            vals.append(res["value"])
+    v = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": "photons/ms", "value": v, "unit": "photons/ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "60^3 cube + r15 sphere, Fresnel, 50x0.1ns gates, 4 detectors (dsp), "
+                               "%d photons per step" % int(cfg["nphoton"])},
+        "cpu_baseline": dict(res, value=v),
+        "e2e": {"value": v, "unit": "photons/ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own CPU path is its OpenCL kernel, which needs an OpenCL CPU driver absent "
+                "from this box; the C restatement of that kernel (oracle/) is timed instead",
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+    import ctypes
+    import torch
+    import mcxcl_gb300
+    from mcxcl_gb300 import _lib, pmcxcl
+
+    torch.cuda.set_device(local)
+    L = _lib.load()
+    cfg = workload(args.photons)
+    cfg["gpuid"] = local + 1
+    cfg["seed"] = int(cfg["seed"]) + rank
+    nphoton = int(cfg["nphoton"])
+
+    # ---- device-resident session
+    C = _lib.Config()
+    pmcxcl.parse_config(cfg, C)
+    L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
+    pmcxcl._check(C)
+    sess = L.mcx_prepare_simulation(ctypes.byref(C))
+    pmcxcl._check(C)
+    nthread = C.threadused
+
+    def simulate(flags=0):
+        ms = ctypes.c_float()
+        rc = L.mcxg_simulate(sess, flags, ctypes.byref(ms))
+        if rc:
+            raise RuntimeError(L.mcxg_error_string(rc).decode())
+        return ms.value
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    for _ in range(max(3, args.warmup)):
+        simulate()
+    barrier(world)
+    torch.cuda.synchronize()
+    kms = []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            kms.append(simulate())
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(world)
+    tot_ms = sum(kms)
+    ms_per_step = allmax(tot_ms / args.steps, world)
+    photons_all = allsum(nphoton * args.steps, world)
+    value = photons_all / (ms_per_step * args.steps)
+    grid = ctypes.c_int()
+    block = ctypes.c_int()
+    regs = ctypes.c_int()
+    L.mcxg_get_launch(sess, ctypes.byref(grid), ctypes.byref(block), ctypes.byref(regs))
+
+    # ---- event counts from the exact kernel on a sample, and the FP32 peak
+    sample = min(nphoton, 5000000)
+    cx = dict(cfg, nphoton=sample, exactmath=1)
+    rx = mcxcl_gb300.run(cx)
+    ev = rx["stat"]["eventcount"]
+    per_photon = {k: ev[k] / float(sample) for k in ("step", "scatter", "launch", "reflect")}
+    ops_per_photon = (OPS_PER_STEP * per_photon["step"] + OPS_PER_SCATTER * per_photon["scatter"] +
+                      OPS_PER_LAUNCH * per_photon["launch"] + OPS_PER_REFLECT * per_photon["reflect"])
+    peak = ctypes.c_double()
+    sess2 = L.mcx_prepare_simulation(ctypes.byref(C))
+    L.mcxg_fp32_peak(sess2, ctypes.byref(peak))
+    achieved = ops_per_photon * nphoton / (tot_ms / args.steps * 1e-3) / 1e9
+    traffic = None
+    if os.path.exists(TRAFFIC_FILE):
+        for ln in open(TRAFFIC_FILE):
+            if ln.startswith("dram_bytes_per_launch:"):
+                traffic = float(ln.split(":")[1])
+
+    # ---- end to end through the public API, host buffers in and out
+    e2e_steps = args.e2e_steps or max(2, min(args.steps, 3))
+    mcxcl_gb300.run(dict(cfg))           # warm the path (session cache, page-ins)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    last = None
+    for _ in range(e2e_steps):
+        last = mcxcl_gb300.run(dict(cfg))
+    torch.cuda.synchronize()
+    e2e_wall = allmax(time.perf_counter() - t0, world)
+    e2e_value = allsum(nphoton * e2e_steps, world) / (e2e_wall * 1e3)
+    nvox = 60 ** 3
+    gates = last["flux"].shape[3]
+    ndet = last["detp"].shape[1] if "detp" in last else 0
+    reclen = last["detp"].shape[0] if "detp" in last else 0
+    h2d = nvox * 1 + 16 * 3 + 16 * 4 + 16 * nthread
+    d2h = nvox * gates * 4 + ndet * reclen * 4 + 16 + 8 * 4 + 8 * 8
+
+    out = None
+    if rank == 0:
+        cpu = None if args.no_cpu_baseline else cpu_baseline(cfg)
+        absorbed = last["stat"]["energyabs"] / last["stat"]["energytot"]
+        out = {
+            "metric": "photons/ms", "value": value, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "60^3 cube + r15 sphere (label 2), Fresnel on, 50 gates x 0.1 ns, 4 r=1 "
+                                   "detectors on z=0 saving detid/nscat/ppath, pencil (29,29,0) +z",
+                       "photons_per_step": nphoton, "reference_threads": nthread,
+                       "launch": {"grid": grid.value, "block": block.value, "regs": regs.value},
+                       "l2": "flushed between timed steps (256 MB write); working set < L2",
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "Gop/s",
+                         "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
+                         "peak_source": "measured in this run: 8-chain FMA kernel, one FMA = one op",
+                         "ops_per_photon": ops_per_photon, "events_per_photon": per_photon,
+                         "model": "48*step + 65*scatter + 20*launch + 10*Fresnel FP32 ops",
+                         "events_from": "exact kernel (bit-identical to the oracle), %d-photon sample" % sample},
+            "e2e": {"value": e2e_value, "unit": "photons/ms", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps,
+            "absorbed": absorbed,
+            "detected_per_step": int(last["stat"]["detected"]),
+        }
+        print(json.dumps(out))
+    L.mcx_clearcfg(ctypes.byref(C))
+
+
+if __name__ == "__main__":
+    main()

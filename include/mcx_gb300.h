@@ -206,6 +206,12 @@ int  mcx_last_error(const Config* cfg, const char** msg);
 /* Number of floats in one detected-photon record for this Config. */
 unsigned int mcx_detreclen(const Config* cfg);
 const char* mcx_version(void);
+/* Everything mcx_run_simulation does before its first launch -- device
+   selection, parameter block, volume packing, upload, seeds of the first
+   repetition -- and nothing after: returns the ready device session so a
+   caller can launch the resident problem repeatedly with mcxg_simulate
+   (benchmarks, repeated solves).  NULL on error (cfg->errorcode). */
+struct mcxg_session* mcx_prepare_simulation(Config* cfg);
 /* sizeof(Config) and the byte offset of a named field ((size_t)-1 if
    unknown), for checking foreign-function mirrors of the struct. */
 size_t mcx_config_sizeof(void);
@@ -278,6 +284,9 @@ int  mcxg_get_field_f64(mcxg_session* s, double* out);
 int  mcxg_get_detected(mcxg_session* s, float* detp, uint64_t* seeds, uint32_t* detected);
 /* Event counters (exact kernel) and status words. */
 int  mcxg_get_counters(mcxg_session* s, uint64_t counters[5], uint32_t status[2]);
+/* Measured FP32 issue peak of the session's GPU in G FMA/s (one FMA = one
+   FP32 operation): the denominator of the kernel's FP32 roofline. */
+int  mcxg_fp32_peak(mcxg_session* s, double* gops);
 /* The persistent grid actually used by the last launch. */
 int  mcxg_get_launch(mcxg_session* s, int* grid, int* block, int* regs);
 

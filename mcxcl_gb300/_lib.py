@@ -96,11 +96,11 @@ class DevInfo(ctypes.Structure):
 EXPORTS = [
     "mcx_initcfg", "mcx_clearcfg", "mcx_validatecfg", "mcx_list_gpu", "mcx_cleargpuinfo", "mcx_run_simulation",
     "mcx_normalize", "mcx_error", "mcx_last_error", "mcx_detreclen", "mcx_version", "mcx_config_sizeof",
-    "mcx_config_offsetof", "mcx_release_sessions",
+    "mcx_config_offsetof", "mcx_release_sessions", "mcx_prepare_simulation",
     "mcxg_device_count", "mcxg_device_info", "mcxg_error_string", "mcxg_create", "mcxg_destroy",
     "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_launch", "mcxg_simulate",
     "mcxg_get_energy", "mcxg_get_thread_energy", "mcxg_get_field", "mcxg_get_field_f64", "mcxg_get_detected",
-    "mcxg_get_counters", "mcxg_get_launch",
+    "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak",
 ]
 
 _lib = None
@@ -128,6 +128,8 @@ def load():
     L.mcx_detreclen.argtypes = [P(Config)]
     L.mcx_detreclen.restype = ctypes.c_uint
     L.mcx_version.restype = ctypes.c_char_p
+    L.mcx_prepare_simulation.argtypes = [P(Config)]
+    L.mcx_prepare_simulation.restype = vp
     L.mcx_config_sizeof.restype = ctypes.c_size_t
     L.mcx_config_offsetof.argtypes = [ctypes.c_char_p]
     L.mcx_config_offsetof.restype = ctypes.c_size_t
@@ -150,6 +152,7 @@ def load():
     L.mcxg_get_detected.argtypes = [vp, vp, vp, P(ctypes.c_uint32)]
     L.mcxg_get_counters.argtypes = [vp, vp, vp]
     L.mcxg_get_launch.argtypes = [vp, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)]
+    L.mcxg_fp32_peak.argtypes = [vp, P(ctypes.c_double)]
     _lib = L
     return L
 

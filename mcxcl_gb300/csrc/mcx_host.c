@@ -603,6 +603,10 @@ static void device_check(int rc, const char* what) {
 
 /* --------------------------------------------------------------- the driver */
 
+/* set by mcx_prepare_simulation: stop once the problem and the first seeds are resident */
+static __thread int prepare_only = 0;
+static __thread mcxg_session* prepared_session = NULL;
+
 void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     (void)fluence;
     (void)totalenergy;
@@ -810,6 +814,12 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
         kp.oddphoton = (int)((float)cfg->nphoton * workload0 / (fullload * (float)cfg->respin) -
                              (float)((size_t)kp.threadphoton * autothread));
         device_check(mcxg_set_params(s, &kp, sizeof(kp)), "updating parameters");
+        if (prepare_only) {
+            /* mcx_prepare_simulation: everything is resident, nothing has run */
+            prepared_session = s;
+            cfg->threadused = (unsigned int)autothread;
+            break;
+        }
         unsigned int flags = (cfg->exactmath ? MCXG_EXACT : 0u) | (iter ? MCXG_KEEP : 0u) |
                              ((cfg->debuglevel & 1) ? MCXG_RNGDUMP : 0u);
         float kms = 0.f;
@@ -865,6 +875,14 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
                 cfg->detectedcount += saved;
             }
         }
+    }
+    if (prepare_only) {
+        for (int i = 0; i < 5; i++) {
+            free(tmp[i]);
+            tmp[i] = NULL;
+        }
+        MCX_LEAVE();
+        return;
     }
     cfg->kernelms = kms_total;
     cfg->threadused = (unsigned int)autothread;
@@ -935,6 +953,14 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
 #undef seedbuf
 #undef fieldtmp
     MCX_LEAVE();
+}
+
+mcxg_session* mcx_prepare_simulation(Config* cfg) {
+    prepare_only = 1;
+    prepared_session = NULL;
+    mcx_run_simulation(cfg, NULL, NULL);
+    prepare_only = 0;
+    return cfg->errorcode ? NULL : prepared_session;
 }
 
 /* ---- layout introspection, so foreign-function mirrors of Config can be checked */

@@ -1,0 +1,108 @@
+"""Named simulation inputs: the reference's built-in benchmarks and the
+benchmark configurations this build is measured on.
+
+Every entry is a ``run()`` dictionary.  Volumes are generated, never loaded.
+
+* ``cube60``, ``cube60b``, ``cube60planar``, ``cubesph60b``: the reference's
+  built-in benchmarks (src/mcx_bench.h:33-252, pmcxcl/pmcxcl/bench.py).
+* ``config1`` .. ``config3``: the homogeneous cube, the cube with a
+  scattering sphere (50 gates, four detectors) and the synthetic layered head
+  used to measure this build (the head replaces the colin27 atlas, whose data
+  is not used: nested ellipsoids of five tissue labels).
+"""
+import copy
+
+import numpy as np
+
+
+def sphere_volume(n=60, center=(30, 30, 30), radius=15, inner=2, outer=1):
+    """A cube of label `outer` holding a sphere of label `inner`; a voxel is
+    inside when its centre is (mcx_raster_sphere, src/mcx_shapes.c:234-293)."""
+    idx = np.arange(n, dtype=np.float64) + 0.5
+    x, y, z = np.meshgrid(idx, idx, idx, indexing="ij")
+    d2 = (x - center[0]) ** 2 + (y - center[1]) ** 2 + (z - center[2]) ** 2
+    vol = np.full((n, n, n), outer, dtype=np.uint8)
+    vol[d2 < radius * radius] = inner
+    return vol
+
+
+def head_volume(shape=(181, 217, 181), axes=((88, 106, 88), (84, 102, 84), (79, 97, 79), (77, 95, 77),
+                                             (60, 75, 60))):
+    """Nested ellipsoids centred in the volume: label k+1 inside the k-th shell
+    (innermost wins), 0 outside the head."""
+    c = [(s - 1) / 2.0 for s in shape]
+    x, y, z = np.meshgrid(*[np.arange(s, dtype=np.float32) for s in shape], indexing="ij")
+    vol = np.zeros(shape, np.uint8)
+    for label, (a, b, cc) in enumerate(axes, start=1):
+        inside = ((x - c[0]) / a) ** 2 + ((y - c[1]) / b) ** 2 + ((z - c[2]) / cc) ** 2 <= 1.0
+        vol[inside] = label
+    return vol
+
+
+def _cube60():
+    return {
+        "nphoton": 1000000,
+        "vol": np.ones((60, 60, 60), dtype=np.uint8),
+        "tstart": 0, "tend": 5e-9, "tstep": 5e-9,
+        "srcpos": [29, 29, 0], "srcdir": [0, 0, 1],
+        "prop": [[0, 0, 1, 1], [0.005, 1, 0.01, 1.37], [0.002, 5, 0.9, 1]],
+        "isreflect": 0, "seed": 1648335518, "session": "cube60",
+        "detpos": [[29, 19, 0, 1], [29, 39, 0, 1], [19, 29, 0, 1], [39, 29, 0, 1]],
+        "issrcfrom0": 1,
+    }
+
+
+def builtin(name):
+    """The reference's built-in benchmark of that name."""
+    if name == "cube60":
+        return _cube60()
+    if name == "cube60b":
+        return dict(_cube60(), isreflect=1, session="cube60b")
+    if name == "cube60planar":
+        return dict(_cube60(), isreflect=1, srctype="planar", srcpos=[10, 10, -10], srcparam1=[40, 0, 0, 0],
+                    srcparam2=[0, 40, 0, 0], session="cube60planar")
+    if name == "cubesph60b":
+        return dict(_cube60(), isreflect=1, vol=sphere_volume(), session="cubesph60b")
+    raise KeyError(name)
+
+
+def config(n):
+    """Benchmark configuration n (1-based): 1 homogeneous cube, 2 cube with
+    sphere and detectors, 3 synthetic layered head."""
+    if n == 1:
+        cfg = _cube60()
+        cfg.pop("detpos")
+        cfg.update(issavedet=0, session="config1")
+        return cfg
+    if n == 2:
+        cfg = _cube60()
+        cfg.update(vol=sphere_volume(), prop=[[0, 0, 1, 1], [0.005, 1.0, 0.01, 1.37], [0.002, 5.0, 0.9, 1.0]],
+                   isreflect=1, tstep=1e-10, nphoton=100000000,
+                   detpos=[[30, 20, 0, 1], [30, 40, 0, 1], [20, 30, 0, 1], [40, 30, 0, 1]],
+                   savedetflag="dsp", session="config2")
+        return cfg
+    if n == 3:
+        vol = head_volume()
+        cx, cy = 90, 108
+        # source at the outer-shell apex on the minimum-z side, pointing +z
+        ztop = int(np.argmax(vol[cx, cy, :] > 0))
+        dets = []
+        for k in range(16):
+            ang = 2 * np.pi * k / 16
+            dx, dy = 30 * np.cos(ang), 30 * np.sin(ang)
+            ix, iy = int(round(cx + dx)), int(round(cy + dy))
+            iz = int(np.argmax(vol[ix, iy, :] > 0))
+            dets.append([ix, iy, iz, 2])
+        return {
+            "nphoton": 100000000, "vol": vol,
+            "prop": [[0, 0, 1, 1], [0.019, 7.8, 0.89, 1.37], [0.019, 7.8, 0.89, 1.37], [0.004, 0.009, 0.89, 1.37],
+                     [0.02, 9.0, 0.89, 1.37], [0.08, 40.9, 0.84, 1.37]],
+            "tstart": 0, "tend": 5e-9, "tstep": 5e-10,
+            "srcpos": [cx, cy, ztop], "srcdir": [0, 0, 1], "issrcfrom0": 1,
+            "detpos": dets, "minenergy": 1e-4, "seed": 12345, "savedetflag": "dsp", "session": "config3",
+        }
+    raise KeyError(n)
+
+
+def copy_cfg(cfg):
+    return copy.deepcopy(cfg)

@@ -39,13 +39,14 @@ def _gpu_run(cfg, nthread, **kw):
     return mcxcl_gb300.run(c)
 
 
-def _sorted_records(detp, seeds):
-    """Detected records in a canonical order (atomic slots differ run to run)."""
+def _sorted_records(detp, seeds16):
+    """Detected records in a canonical order (atomic slots differ run to run).
+    detp: [reclen, n] floats; seeds16: [n, 16] uint8 or None."""
     if detp is None or detp.size == 0:
         return np.zeros((0,), np.uint32), None
     bits = np.ascontiguousarray(detp.T).view(np.uint32)
-    if seeds is not None:
-        key = np.ascontiguousarray(seeds).view(np.uint64).reshape(seeds.shape[0], -1)
+    if seeds16 is not None:
+        key = np.ascontiguousarray(seeds16).view(np.uint64).reshape(seeds16.shape[0], 2)
         order = np.lexsort(key.T[::-1])
         return bits[order], key[order]
     order = np.lexsort(bits.T[::-1])
@@ -75,10 +76,11 @@ def test_exact_kernel_matches_oracle_bits(gpu, O, name):
     assert ev["launch"] == r["stat"]["nlaunch"]
     assert ev["reflect"] == r["stat"]["nreflect"]
     assert g["stat"]["detected"] == r["stat"]["detected"]
-    rg, sg = _sorted_records(g.get("detp"), g.get("seeds"))
+    seeds_gpu = g["seeds"].T if g.get("seeds") is not None else None
+    rg, sg = _sorted_records(g.get("detp"), seeds_gpu)
     seeds_cpu = None
     if r["seeds"] is not None and r["seeds"].size:
-        seeds_cpu = r["seeds"].view(np.uint8).reshape(-1, 16)
+        seeds_cpu = np.ascontiguousarray(r["seeds"]).view(np.uint8).reshape(-1, 16)
     rc, sc = _sorted_records(r["detp"] if r["detp"].size else None, seeds_cpu)
     assert np.array_equal(rg, rc)
     if sg is not None:
