@@ -87,7 +87,7 @@ def test_exact_kernel_matches_oracle_bits(gpu, O, name):
         assert np.array_equal(sg, sc)
     # the field differs only by the order of the float atomics
     raw = np.asarray(r["field_raw"]) * r["stat"]["normalizer"]
-    flux = g["flux"].reshape(raw.shape)
+    flux = g["flux"].reshape(raw.shape, order="F")
     scale = max(np.abs(raw).max(), 1e-30)
     np.testing.assert_allclose(flux, raw, rtol=1e-4, atol=1e-6 * scale)
 
@@ -134,8 +134,10 @@ KNOWN = [
     ("B1 0.1769", cases.cube60(nphoton=10000000, seed=29012392, issavedet=0), 0.1769, 0.005),
     ("B2 0.2701", cases.cube60(nphoton=10000000, seed=29012392, vol=cases.sphere_volume(), isreflect=1,
                                issavedet=0), 0.2701, 0.005),
+    # B3 inherits isreflect=1 from B2 in mcx_gpu_benchmarks.m:94-115
     ("B3 0.2551", cases.cube60(nphoton=10000000, seed=29012392, srctype="planar", srcpos=[10, 10, -10],
-                               srcparam1=[40, 0, 0, 0], srcparam2=[0, 40, 0, 0], issavedet=0), 0.2551, 0.005),
+                               srcparam1=[40, 0, 0, 0], srcparam2=[0, 40, 0, 0], isreflect=1, issavedet=0),
+     0.2551, 0.005),
 ]
 
 
@@ -149,16 +151,21 @@ def test_fast_kernel_reference_known_answers(gpu, name, cfg, want, tol):
 
 
 def test_fast_kernel_voxel_fluence_within_3_sigma(gpu, O):
-    """Per-voxel fluence within 3 sigma of the Monte Carlo noise wherever the
-    relative standard error is below 5% (sigma from 10 GPU seeds)."""
+    """Per-voxel fluence of the fast kernel within 3 sigma of the Monte Carlo
+    noise wherever the relative standard error is below 5%.  Sigma comes from
+    10 independent seeds of each side; the other side is the exact kernel,
+    which reproduces the CPU oracle bit for bit (pinned above), so this is the
+    fast kernel against the oracle.  With 10+10 samples the statistic is close
+    to Student's t with 18 degrees of freedom: ~0.8% of voxels exceed 3."""
     import mcxcl_gb300
     base = cases.cube60(nphoton=200000, issavedet=0, tstep=5e-10, tend=5e-9)
-    runs = np.stack([mcxcl_gb300.run(dict(base, seed=1000 + k))["flux"] for k in range(10)])
-    mean = runs.mean(0)
-    sd = runs.std(0, ddof=1)
-    r = O.run(dict(base, seed=1000), nthread=16384, core=gpu["core"], mathmode=O.MATH_LIBM)
-    ref = np.asarray(r["flux"], np.float64)
-    ok = (mean > 0) & (sd / np.sqrt(10) < 0.05 * mean)
-    z = np.abs(ref[ok] - mean[ok]) / (sd[ok] * np.sqrt(1 + 1 / 10.))
+    fast = np.stack([mcxcl_gb300.run(dict(base, seed=1000 + k))["flux"] for k in range(10)])
+    exact = np.stack([mcxcl_gb300.run(dict(base, seed=2000 + k, exactmath=1))["flux"] for k in range(10)])
+    mf, me = fast.mean(0), exact.mean(0)
+    vf, ve = fast.var(0, ddof=1) / 10, exact.var(0, ddof=1) / 10
+    ok = (me > 0) & (np.sqrt(ve) < 0.05 * me) & (np.sqrt(vf) < 0.05 * mf)
+    z = np.abs(mf[ok] - me[ok]) / np.sqrt(vf[ok] + ve[ok])
     assert ok.sum() > 1000
-    assert np.mean(z > 3) < 0.01, np.mean(z > 3)
+    assert np.mean(z > 3) < 0.02, np.mean(z > 3)
+    # and the total fluence of the two 10-seed means agrees to 0.5%
+    assert abs(mf.sum() - me.sum()) <= 0.005 * me.sum()
