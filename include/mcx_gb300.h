@@ -287,6 +287,23 @@ int  mcxg_get_counters(mcxg_session* s, uint64_t counters[5], uint32_t status[2]
 /* Measured FP32 issue peak of the session's GPU in G FMA/s (one FMA = one
    FP32 operation): the denominator of the kernel's FP32 roofline. */
 int  mcxg_fp32_peak(mcxg_session* s, double* gops);
+/*
+ * FP64 sums of per-thread {escaped, launched} weights, allocating nothing.
+ * No counterpart in the reference (its host sums the weights in double after
+ * reading them back, src/mcx_host.cpp:1303-1306).  For callers that cannot let
+ * the library allocate device memory -- a service that reserves its device
+ * budget at start-up, or a framework that owns every device buffer -- since
+ * mcxg_get_energy needs a session and a session allocates with cudaMalloc.
+ * d_energy: device array of 2 x nthread floats {escaped, launched} per thread;
+ * d_sums: device array receiving 2 doubles {escaped, launched}.  Runs on the
+ * legacy default stream of `device` and returns after the sums are written.
+ * Scratch: a static 64 KB device array, so nthread may not exceed 8,388,608
+ * (MCXG_ERR_LIMIT beyond).  The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress); make the first call before any
+ * stream capture.  Every call shares the array: calls that overlap on the GPU
+ * (other host threads, other streams) race.
+ */
+int  mcxg_energy_sum_noalloc(int device, const float* d_energy, uint32_t nthread, double* d_sums);
 /* The persistent grid actually used by the last launch. */
 int  mcxg_get_launch(mcxg_session* s, int* grid, int* block, int* regs);
 

@@ -100,7 +100,7 @@ EXPORTS = [
     "mcxg_device_count", "mcxg_device_info", "mcxg_error_string", "mcxg_create", "mcxg_destroy",
     "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_launch", "mcxg_simulate",
     "mcxg_get_energy", "mcxg_get_thread_energy", "mcxg_get_field", "mcxg_get_field_f64", "mcxg_get_detected",
-    "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak",
+    "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc",
 ]
 
 _lib = None
@@ -153,6 +153,7 @@ def load():
     L.mcxg_get_counters.argtypes = [vp, vp, vp]
     L.mcxg_get_launch.argtypes = [vp, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)]
     L.mcxg_fp32_peak.argtypes = [vp, P(ctypes.c_double)]
+    L.mcxg_energy_sum_noalloc.argtypes = [ctypes.c_int, vp, ctypes.c_uint32, vp]
     _lib = L
     return L
 

@@ -663,6 +663,54 @@ int mcxg_fp32_peak(mcxg_session* s, double* gops) {
     return MCXG_OK;
 }
 
+
+/* ---- allocation-free FP64 energy sum ---------------------------------------
+ *
+ * For callers that cannot let this library allocate device memory: a service
+ * that reserves its whole device budget at start-up, or a host framework that
+ * owns every device buffer and only lends the library pointers into them.
+ * mcxg_get_energy needs a session, and a session allocates its buffers with
+ * cudaMalloc; this entry point reduces a caller-owned array of per-thread
+ * {escaped, launched} weights with no allocation at all.  Its scratch -- one
+ * {escaped, launched} FP64 pair per block of 2048 threads, plus the result --
+ * is the static device array below, sized for MCXG_NOALLOC_MAX_THREADS
+ * threads (64 KB on every GPU that loads the library, held until exit).
+ */
+#define MCXG_NOALLOC_CHUNK        2048u
+#define MCXG_NOALLOC_MAX_BLOCKS   4096u
+#define MCXG_NOALLOC_MAX_DEVICES  64
+
+static __device__ __align__(256) double g_noalloc_scratch[2 * MCXG_NOALLOC_MAX_BLOCKS + 2];
+static double* g_noalloc_scratch_addr[MCXG_NOALLOC_MAX_DEVICES];
+
+int mcxg_energy_sum_noalloc(int device, const float* d_energy, uint32_t nthread, double* d_sums) {
+    if (!d_energy || !d_sums || nthread == 0 || device < 0 || device >= MCXG_NOALLOC_MAX_DEVICES) {
+        return MCXG_ERR_ARG;
+    }
+    uint32_t nblocks = (nthread + MCXG_NOALLOC_CHUNK - 1) / MCXG_NOALLOC_CHUNK;
+    if (nblocks > MCXG_NOALLOC_MAX_BLOCKS) {
+        return MCXG_ERR_LIMIT;
+    }
+    MCXG_TRY(cudaSetDevice(device));
+    if (!g_noalloc_scratch_addr[device]) {
+        /* once per device, with that device current: the device address of the
+           static array (its host-side name is not a device address) */
+        void* p = nullptr;
+        MCXG_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_scratch_addr[device] = (double*)p;
+    }
+    double* scratch = g_noalloc_scratch_addr[device];
+    /* the array keeps the previous call's contents: clear the part this call uses */
+    MCXG_TRY(cudaMemsetAsync(scratch, 0, sizeof(double) * (2 * (size_t)nblocks + 2), 0));
+    energy_partials<<<nblocks, kRedThreads, 0, 0>>>((const float2*)d_energy, nthread, scratch);
+    MCXG_TRY(cudaGetLastError());
+    energy_final<<<1, 32, 0, 0>>>(scratch, (int)nblocks);
+    MCXG_TRY(cudaGetLastError());
+    MCXG_TRY(cudaMemcpyAsync(d_sums, scratch + 2 * nblocks, 2 * sizeof(double), cudaMemcpyDeviceToDevice, 0));
+    MCXG_TRY(cudaStreamSynchronize(0));
+    return MCXG_OK;
+}
+
 int mcxg_get_launch(mcxg_session* s, int* grid, int* block, int* regs) {
     if (!s) {
         return MCXG_ERR_ARG;
