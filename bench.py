@@ -44,6 +44,8 @@ sys.path.insert(0, ROOT)
 
 # frozen FP32 operation model (weights per event)
 OPS_PER_STEP, OPS_PER_SCATTER, OPS_PER_LAUNCH, OPS_PER_REFLECT = 48, 65, 20, 10
+MUFU_PER_STEP, MUFU_PER_SCATTER = 6, 11
+MUFU_PER_SM_CLK = 16          # special-function results per SM per clock
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_mcx_transport_config2.txt")
 
 
@@ -163,11 +165,16 @@ def cpu_baseline(cfg, target_s=15.0, kind="port"):
     import oracle
     ncores = os.cpu_count() or 1
     nthread = 16384
-    probe = dict(cfg, nphoton=20000)
-    t0 = time.perf_counter()
-    oracle.run(probe, nthread=nthread, core=nthread, mathmode=oracle.MATH_LIBM, nworkers=ncores)
-    dt = max(time.perf_counter() - t0, 1e-3)
-    n = int(min(cfg["nphoton"], max(20000, 20000 * target_s / dt)))
+    # grow a probe until it runs for a tenth of the target, then scale to the target
+    n = 20000
+    while True:
+        t0 = time.perf_counter()
+        oracle.run(dict(cfg, nphoton=n), nthread=nthread, core=nthread, mathmode=oracle.MATH_LIBM, nworkers=ncores)
+        dt = max(time.perf_counter() - t0, 1e-3)
+        if dt >= 0.1 * target_s or n >= cfg["nphoton"]:
+            break
+        n = int(min(cfg["nphoton"], n * max(2.0, 0.15 * target_s / dt)))
+    n = int(min(cfg["nphoton"], max(20000, n * target_s / dt)))
     sample = dict(cfg, nphoton=n)
     t0 = time.perf_counter()
     r = oracle.run(sample, nthread=nthread, core=nthread, mathmode=oracle.MATH_LIBM, nworkers=ncores)
@@ -230,6 +237,13 @@ def main():
     pmcxcl._check(C)
     nthread = C.threadused
 
+    # launch shape: the autotuner times the candidates on 2e6 photons of this workload
+    tb, tp, tn = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    rc = L.mcxg_autotune(sess, 2000000, ctypes.byref(tb), ctypes.byref(tp), ctypes.byref(tn))
+    if rc:
+        raise RuntimeError(L.mcxg_error_string(rc).decode())
+    tuned = {"block": tb.value, "blocks_per_sm": tp.value, "warp_aggregation": not tn.value}
+
     def simulate(flags=0):
         ms = ctypes.c_float()
         rc = L.mcxg_simulate(sess, flags, ctypes.byref(ms))
@@ -274,6 +288,13 @@ def main():
     sess2 = L.mcx_prepare_simulation(ctypes.byref(C))
     L.mcxg_fp32_peak(sess2, ctypes.byref(peak))
     achieved = ops_per_photon * nphoton / (tot_ms / args.steps * 1e-3) / 1e9
+    mufu_per_photon = MUFU_PER_STEP * per_photon["step"] + MUFU_PER_SCATTER * per_photon["scatter"]
+    mufu_achieved = mufu_per_photon * nphoton / (tot_ms / args.steps * 1e-3) / 1e9
+    info = mcxcl_gb300.gpuinfo()[local]
+    clock_summary = clk.summary()
+    sm_mhz = clock_summary["sm_mhz"] or clock_summary["sm_max_mhz"] or 2070.0
+    mufu_peak = info["sm"] * MUFU_PER_SM_CLK * sm_mhz * 1e6 / 1e9
+    fp32_nominal = info["sm"] * 128 * sm_mhz * 1e6 / 1e9
     traffic = None
     if os.path.exists(TRAFFIC_FILE):
         for ln in open(TRAFFIC_FILE):
@@ -295,8 +316,9 @@ def main():
     gates = last["flux"].shape[3]
     ndet = last["detp"].shape[1] if "detp" in last else 0
     reclen = last["detp"].shape[0] if "detp" in last else 0
+    nseed = last["seeds"].shape[1] if last.get("seeds") is not None else 0
     h2d = nvox * 1 + 16 * 3 + 16 * 4 + 16 * nthread
-    d2h = nvox * gates * 4 + ndet * reclen * 4 + 16 + 8 * 4 + 8 * 8
+    d2h = nvox * gates * 4 + ndet * reclen * 4 + nseed * 16 + 16 + 8 * 4 + 8 * 8
 
     out = None
     if rank == 0:
@@ -309,7 +331,8 @@ def main():
             "config": {"workload": "60^3 cube + r15 sphere (label 2), Fresnel on, 50 gates x 0.1 ns, 4 r=1 "
                                    "detectors on z=0 saving detid/nscat/ppath, pencil (29,29,0) +z",
                        "photons_per_step": nphoton, "reference_threads": nthread,
-                       "launch": {"grid": grid.value, "block": block.value, "regs": regs.value},
+                       "launch": {"grid": grid.value, "block": block.value, "regs": regs.value,
+                                  "autotuned": tuned},
                        "l2": "flushed between timed steps (256 MB write); working set < L2",
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "Gop/s",
@@ -317,11 +340,15 @@ def main():
                          "peak_source": "measured in this run: 8-chain FMA kernel, one FMA = one op",
                          "ops_per_photon": ops_per_photon, "events_per_photon": per_photon,
                          "model": "48*step + 65*scatter + 20*launch + 10*Fresnel FP32 ops",
-                         "events_from": "exact kernel (bit-identical to the oracle), %d-photon sample" % sample},
+                         "events_from": "exact kernel (bit-identical to the oracle), %d-photon sample" % sample,
+                         "fp32_nominal": fp32_nominal,
+                         "mufu": {"achieved": mufu_achieved, "peak": mufu_peak, "unit": "Gop/s",
+                                  "frac": mufu_achieved / mufu_peak,
+                                  "model": "6*step + 11*scatter MUFU ops; peak 16/SM/clock at the sampled clock"}},
             "e2e": {"value": e2e_value, "unit": "photons/ms", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "clocks": clock_summary,
             "gpu_launches": args.steps,
             "absorbed": absorbed,
             "detected_per_step": int(last["stat"]["detected"]),

@@ -172,6 +172,7 @@ typedef struct MCXConfig {
     unsigned int threadused;      /* reference threads (RNG streams) of the last run */
     float* exportenergy;          /* when savethreadenergy: 2 x threadused {escaped, launched} floats */
     int savethreadenergy;
+    int autotune;                 /* 1: time the launch shapes on a photon sample, once per problem shape, keep the fastest */
     int errorcode;                /* last error in library mode */
     char errormsg[256];
 } Config;
@@ -231,9 +232,10 @@ void mcx_release_sessions(void);
 
 /* mcxg_simulate flags */
 #define MCXG_EXACT    1u   /* IEEE-only kernel with event counters */
-#define MCXG_NOAGG    2u   /* disable warp aggregation of deposits */
+#define MCXG_NOAGG    2u   /* no warp aggregation of deposits (the default unless autotuned) */
 #define MCXG_RNGDUMP  4u   /* write each thread's RNG stream into the field (-D R) */
 #define MCXG_KEEP     8u   /* keep accumulating into the field (respin); energies, records and counters restart */
+#define MCXG_AGG     16u   /* aggregate same-voxel deposits of a warp before the atomics */
 
 typedef struct mcxg_devinfo {
     char name[64];
@@ -266,8 +268,17 @@ int  mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size,
 int  mcxg_set_params(mcxg_session* s, const void* kparams, size_t kparams_size);
 /* 4 seed words per reference thread, as the reference draws them with rand(). */
 int  mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread);
-/* Launch shape of the persistent grid (0 = automatic). */
+/* Launch shape of the persistent grid (0 = automatic).  blocks_per_sm = 3
+   selects the instantiation whose registers are capped for three resident
+   256-thread blocks per SM (also the automatic choice); 2 the uncapped one. */
 int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
+/* Pick the launch shape of the fast kernel for the current problem: time
+   each candidate (256 threads x 2 or 3 resident blocks per SM, warp
+   aggregation of deposits on or off) on the first sample_photons photons
+   and keep the fastest for later mcxg_simulate calls (unless a shape was
+   set with mcxg_set_launch).  Outputs may be NULL.  The trial runs
+   overwrite the field and energies. */
+int  mcxg_autotune(mcxg_session* s, uint32_t sample_photons, int* block, int* blocks_per_sm, int* noagg);
 /* Run all photons once; kernel time (CUDA events) into *kernel_ms. */
 int  mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms);
 /* FP64 sums over threads of escaped and launched weight. */

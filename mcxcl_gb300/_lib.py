@@ -80,7 +80,7 @@ class Config(ctypes.Structure):
         ("srcdata", ctypes.POINTER(ExtraSrc)), ("exactmath", ctypes.c_int), ("kernelms", ctypes.c_float),
         ("eventcount", ctypes.c_uint64 * 5), ("failedlaunch", ctypes.c_uint), ("threadused", ctypes.c_uint),
         ("exportenergy", ctypes.POINTER(ctypes.c_float)), ("savethreadenergy", ctypes.c_int),
-        ("errorcode", ctypes.c_int),
+        ("autotune", ctypes.c_int), ("errorcode", ctypes.c_int),
         ("errormsg", ctypes.c_char * 256),
     ]
 
@@ -100,7 +100,7 @@ EXPORTS = [
     "mcxg_device_count", "mcxg_device_info", "mcxg_error_string", "mcxg_create", "mcxg_destroy",
     "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_launch", "mcxg_simulate",
     "mcxg_get_energy", "mcxg_get_thread_energy", "mcxg_get_field", "mcxg_get_field_f64", "mcxg_get_detected",
-    "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc",
+    "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc", "mcxg_autotune",
 ]
 
 _lib = None
@@ -154,6 +154,7 @@ def load():
     L.mcxg_get_launch.argtypes = [vp, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)]
     L.mcxg_fp32_peak.argtypes = [vp, P(ctypes.c_double)]
     L.mcxg_energy_sum_noalloc.argtypes = [ctypes.c_int, vp, ctypes.c_uint32, vp]
+    L.mcxg_autotune.argtypes = [vp, ctypes.c_uint32, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)]
     _lib = L
     return L
 

@@ -63,6 +63,8 @@ struct mcxg_session {
 
     std::vector<float> h_det, h_srcx;
     int block_req = 0, bpsm_req = 0;
+    int tuned = 0;                   /* 1 once mcxg_autotune picked a shape for this problem */
+    int tuned_noagg = 0;
     int grid = 0, block = 0, regs = 0;
 };
 
@@ -193,7 +195,7 @@ int grid_for(const mcxg_session* s, size_t n) {
 
 size_t shared_bytes(const mcxg_kparams& kp, int block) {
     size_t det = (kp.savedet ? kp.partialdata : 0);
-    return (size_t)kp.medianum * 16 + (size_t)(kp.nphase + kp.nangle) * 4 + det * (size_t)block * 4;
+    return (size_t)kp.medianum * 32 + (size_t)(kp.nphase + kp.nangle) * 4 + det * (size_t)block * 4;
 }
 
 }  // namespace
@@ -388,6 +390,7 @@ int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, 
     s->h_srcx.assign(srcextra ? srcextra : prop, srcextra ? srcextra + 16 * kp.extrasrclen : prop);
     s->up_fast = s->up_exact = false;
     s->has_problem = true;
+    s->tuned = 0;
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
 }
@@ -484,23 +487,28 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     a.status = s->d_words + 2;
     a.counters = s->d_events;
 
+    /* deposits go straight to the field unless aggregation is asked for or
+       the autotuner found it faster for this problem */
+    const bool noagg = (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
+    const int bpsm_sel = s->bpsm_req ? s->bpsm_req : 3;
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
-                 ((flags & MCXG_NOAGG) ? 0 : mcxg::LF_WAGG);
+                 (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0);
     int block = s->block_req ? s->block_req : 256;
     size_t smem = shared_bytes(kp, block);
     if (smem > s->info.sharedmem_per_block) {
         return MCXG_ERR_LIMIT;
     }
-    int bpsm = s->bpsm_req;
-    if (!bpsm) {
-        if (exact) {
-            bpsm = 2;
-        } else {
-            MCXG_TRY(mcxg::fast_occupancy(lflags, block, smem, &bpsm));
+    int bpsm = s->bpsm_req ? s->bpsm_req : (exact ? 2 : bpsm_sel);
+    if (!exact) {
+        /* never more blocks than fit at once: a persistent grid must be resident */
+        int occ = 0;
+        MCXG_TRY(mcxg::fast_occupancy(lflags, block, smem, &occ));
+        if (occ >= 1 && bpsm > occ) {
+            bpsm = occ;
         }
-        if (bpsm < 1) {
-            bpsm = 1;
-        }
+    }
+    if (bpsm < 1) {
+        bpsm = 1;
     }
     int grid = s->info.sm * bpsm;
     s->grid = grid;
@@ -527,6 +535,74 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
         float ms = 0.f;
         MCXG_TRY(cudaEventElapsedTime(&ms, s->e0, s->e1));
         *kernel_ms = ms;
+    }
+    return MCXG_OK;
+}
+
+int mcxg_autotune(mcxg_session* s, uint32_t sample_photons, int* block, int* blocks_per_sm, int* noagg) {
+    if (!s) {
+        return MCXG_ERR_ARG;
+    }
+    if (!s->has_problem || !s->has_seeds) {
+        return MCXG_ERR_STATE;
+    }
+    /* run a sample of the problem: the first sample_photons photons of the
+       reference threads (same seeds), with each candidate shape */
+    mcxg_kparams full = s->kp;
+    mcxg_kparams samp = full;
+    unsigned long long total = (unsigned long long)full.threadphoton * full.nthread + (unsigned int)full.oddphoton;
+    if (sample_photons && sample_photons < total) {
+        samp.threadphoton = sample_photons / full.nthread;
+        samp.oddphoton = (int)(sample_photons - samp.threadphoton * full.nthread);
+    }
+    s->kp = samp;
+    s->up_fast = false;
+    struct Cand {
+        int block, bpsm, noagg;
+    } cands[] = {{256, 3, 1}, {256, 3, 0}, {256, 2, 1}, {256, 2, 0}};
+    float best = 1e30f;
+    Cand pick = cands[0];
+    int keep_block = s->block_req, keep_bpsm = s->bpsm_req;
+    int rc = MCXG_OK;
+    for (const Cand& c : cands) {
+        s->block_req = c.block;
+        s->bpsm_req = c.bpsm;
+        float ms = 0.f, t = 1e30f;
+        for (int rep = 0; rep < 2 && !rc; rep++) {
+            rc = mcxg_simulate(s, c.noagg ? MCXG_NOAGG : MCXG_AGG, &ms);
+            if (ms < t) {
+                t = ms;
+            }
+        }
+        if (rc) {
+            break;
+        }
+        if (t < best) {
+            best = t;
+            pick = c;
+        }
+    }
+    s->kp = full;
+    s->up_fast = false;
+    s->block_req = keep_block;
+    s->bpsm_req = keep_bpsm;
+    if (rc) {
+        return rc;
+    }
+    if (!keep_block && !keep_bpsm) {
+        s->block_req = pick.block;
+        s->bpsm_req = pick.bpsm;
+    }
+    s->tuned = 1;
+    s->tuned_noagg = pick.noagg;
+    if (block) {
+        *block = pick.block;
+    }
+    if (blocks_per_sm) {
+        *blocks_per_sm = pick.bpsm;
+    }
+    if (noagg) {
+        *noagg = pick.noagg;
     }
     return MCXG_OK;
 }
@@ -644,10 +720,12 @@ int mcxg_fp32_peak(mcxg_session* s, double* gops) {
         return MCXG_ERR_ARG;
     }
     MCXG_TRY(cudaSetDevice(s->device));
-    const int block = 256, iters = 1 << 16;
+    /* ~0.25 s per repetition at full clock: long enough to time, short
+       enough that the power limit does not pull the clock down */
+    const int block = 256, iters = 1 << 12;
     const int grid = s->info.sm * 8;
     float best = 1e30f;
-    for (int rep = 0; rep < 4; rep++) {
+    for (int rep = 0; rep < 12; rep++) {
         MCXG_TRY(cudaEventRecord(s->e0, s->st));
         fma_peak<<<grid, block, 0, s->st>>>((float*)s->d_red, iters, 0.999999f, 1e-7f);
         MCXG_TRY(cudaEventRecord(s->e1, s->st));

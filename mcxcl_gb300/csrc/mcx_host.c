@@ -584,6 +584,40 @@ static mcxg_session* session_for(int device) {
     return g_sessions[device];
 }
 
+/* launch shape picked by the autotuner, per device, for the last problem shape tuned */
+typedef struct {
+    int valid;
+    uint64_t sig;
+    int block, bpsm, noagg;
+} TuneCache;
+static TuneCache g_tune[MAX_DEVICE];
+
+static uint64_t mix64(uint64_t h, uint64_t v) {
+    h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+    return h;
+}
+
+/* what the launch shape depends on: the volume, the media, the source, the
+   outputs compiled in and the photon budget per thread */
+static uint64_t tune_signature(const Config* cfg, const mcxg_kparams* kp) {
+    uint64_t h = 1469598103934665603ull;
+    h = mix64(h, kp->nvox);
+    h = mix64(h, kp->dimx);
+    h = mix64(h, kp->fieldlen);
+    h = mix64(h, (uint64_t)kp->medianum << 32 | (uint32_t)kp->srctype);
+    h = mix64(h, (uint64_t)kp->savedet << 8 | (uint64_t)kp->dorefl_compiled << 4 | (uint64_t)kp->issaveref);
+    h = mix64(h, kp->nthread);
+    h = mix64(h, (uint64_t)(cfg->nphoton / 1000));
+    h = mix64(h, (uint64_t)cfg->dim.y << 32 | cfg->dim.z);
+    for (unsigned int i = 0; i < cfg->medianum && i < 16; i++) {
+        uint32_t w[4];
+        memcpy(w, &cfg->prop[i], sizeof(w));
+        h = mix64(h, (uint64_t)w[0] << 32 | w[1]);
+        h = mix64(h, (uint64_t)w[2] << 32 | w[3]);
+    }
+    return h;
+}
+
 void mcx_release_sessions(void) {
     for (int i = 0; i < MAX_DEVICE; i++) {
         if (g_sessions[i]) {
@@ -822,6 +856,27 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
         }
         unsigned int flags = (cfg->exactmath ? MCXG_EXACT : 0u) | (iter ? MCXG_KEEP : 0u) |
                              ((cfg->debuglevel & 1) ? MCXG_RNGDUMP : 0u);
+        if (iter == 0) {
+            device_check(mcxg_set_launch(s, 0, 0), "resetting the launch shape");
+        }
+        if (cfg->autotune && !cfg->exactmath && !(cfg->debuglevel & 1)) {
+            uint64_t sig = tune_signature(cfg, &kp);
+            TuneCache* tc = &g_tune[device];
+            if (!tc->valid || tc->sig != sig) {
+                /* 1/64 of the photons per candidate, at most 2e6 and at least 2e5 */
+                double want = cfg->nphoton / 64.0;
+                uint32_t sample = (uint32_t)(want > 2e6 ? 2e6 : (want < 2e5 ? 2e5 : want));
+                int blk = 0, bpsm = 0, noagg = 1;
+                device_check(mcxg_autotune(s, sample, &blk, &bpsm, &noagg), "autotuning the launch shape");
+                tc->valid = 1;
+                tc->sig = sig;
+                tc->block = blk;
+                tc->bpsm = bpsm;
+                tc->noagg = noagg;
+            }
+            device_check(mcxg_set_launch(s, tc->block, tc->bpsm), "setting the launch shape");
+            flags |= tc->noagg ? MCXG_NOAGG : MCXG_AGG;
+        }
         float kms = 0.f;
         device_check(mcxg_simulate(s, flags, &kms), "running the transport kernel");
         kms_total += kms;
@@ -987,7 +1042,7 @@ static const struct {
     MCX_FIELD(bc), MCX_FIELD(nphase), MCX_FIELD(invcdf), MCX_FIELD(nangle), MCX_FIELD(angleinvcdf), MCX_FIELD(srcid),
     MCX_FIELD(extrasrclen), MCX_FIELD(srcdata), MCX_FIELD(exactmath), MCX_FIELD(kernelms), MCX_FIELD(eventcount),
     MCX_FIELD(failedlaunch), MCX_FIELD(threadused), MCX_FIELD(exportenergy), MCX_FIELD(savethreadenergy),
-    MCX_FIELD(errorcode), MCX_FIELD(errormsg),
+    MCX_FIELD(autotune), MCX_FIELD(errorcode), MCX_FIELD(errormsg),
 };
 
 size_t mcx_config_sizeof(void) {

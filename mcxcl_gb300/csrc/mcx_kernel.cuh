@@ -29,7 +29,8 @@
  * Template flags: EXACT (IEEE-only math, no contraction: compile this TU with
  * -fmad=false -prec-div=true -prec-sqrt=true -ftz=false), DET (detector
  * bookkeeping compiled in), REFL (Fresnel / boundary-condition block
- * compiled in), WAGG (warp aggregation of deposits), COUNT (event counters).
+ * compiled in), WAGG (warp aggregation of deposits), COUNT (event counters),
+ * MINB (resident 256-thread blocks per SM the register allocation targets).
  * DET and REFL are upper bounds: the runtime flags in the constant block
  * still decide, so the exact build runs every configuration.
  */
@@ -161,6 +162,7 @@ struct Photon {
 
 struct Shared {
     const float4* prop;            /* medianum rows */
+    const float4* recip;           /* per medium: 1/mus, 1/(mus (1-g)), 1/mua (fast kernel) */
     const float* invcdf;
     const float* angleinvcdf;
     float* pp;                     /* this thread's partial data, stride blockDim.x */
@@ -204,6 +206,21 @@ __device__ __forceinline__ float hitgrid(const float4& p, const float4& v, int f
     hx = fabsf(Mth<EXACT>::div(hx + K_EPS, v.x));
     hy = fabsf(Mth<EXACT>::div(hy + K_EPS, v.y));
     hz = fabsf(Mth<EXACT>::div(hz + K_EPS, v.z));
+    float dist = fminf(fminf(hx, hy), hz);
+    fw = (dist == hx ? 0 : (dist == hy ? 1 : 2));
+    return dist;
+}
+
+/* hitgrid of the fast kernel with the direction's reciprocals cached:
+   __fdividef(h, v) == h * rcp(v), so the result is the same bits */
+__device__ __forceinline__ float hitgrid_rcp(const float4& p, const float4& v, const float3& rv, int fx, int fy, int fz,
+                                             int& fw) {
+    float hx = fabsf((float)fx - (v.x > 0.f ? -1.f : 0.f) - p.x);
+    float hy = fabsf((float)fy - (v.y > 0.f ? -1.f : 0.f) - p.y);
+    float hz = fabsf((float)fz - (v.z > 0.f ? -1.f : 0.f) - p.z);
+    hx = fabsf((hx + K_EPS) * rv.x);
+    hy = fabsf((hy + K_EPS) * rv.y);
+    hz = fabsf((hz + K_EPS) * rv.z);
     float dist = fminf(fminf(hx, hy), hz);
     fw = (dist == hx ? 0 : (dist == hy ? 1 : 2));
     return dist;
@@ -444,13 +461,43 @@ __device__ __forceinline__ void field_add2(float* field, unsigned int fieldlen, 
     }
 }
 
+/* A high-plane atomic whose rounding error is still to be sent to the low
+   plane.  The old value returns from L2 while the photon takes its next step;
+   completing the add one deposit later keeps the warp from waiting on it. */
+struct Pending {
+    unsigned int idx;
+    float old, w;
+    bool on;
+};
+
+__device__ __forceinline__ void pend_complete(float* field, unsigned int fieldlen, Pending& pd) {
+    if (pd.on) {
+        float s = __fadd_rn(pd.old, pd.w);
+        float bp = __fsub_rn(s, pd.old);
+        float e = __fadd_rn(__fsub_rn(pd.old, __fsub_rn(s, bp)), __fsub_rn(pd.w, bp));
+        if (e != 0.f) {
+            atomicAdd(field + fieldlen + pd.idx, e);
+        }
+        pd.on = false;
+    }
+}
+
+__device__ __forceinline__ void pend_issue(float* field, Pending& pd, unsigned int i, float w) {
+    pd.old = atomicAdd(field + i, w);
+    pd.idx = i;
+    pd.w = w;
+    pd.on = true;
+}
+
 /* Deposit from every lane that has one; lanes of the warp hitting the same
    field element are summed first and one leader commits. */
 template <bool WAGG>
-__device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, bool doit, unsigned int key, float w) {
+__device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, bool doit, unsigned int key, float w,
+                                        Pending& pd) {
     if (!WAGG) {
         if (doit) {
-            field_add2(field, fieldlen, key, w);
+            pend_complete(field, fieldlen, pd);
+            pend_issue(field, pd, key, w);
         }
         return;
     }
@@ -462,7 +509,8 @@ __device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, boo
     unsigned int peers = __match_any_sync(m, key);
     unsigned int lane = threadIdx.x & 31u;
     if (peers == (1u << lane)) {
-        field_add2(field, fieldlen, key, w);
+        pend_complete(field, fieldlen, pd);
+        pend_issue(field, pd, key, w);
         return;
     }
     float total = 0.f;
@@ -473,7 +521,8 @@ __device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, boo
         total += __shfl_sync(peers, w, src);
     }
     if ((int)lane == __ffs(peers) - 1) {
-        field_add2(field, fieldlen, key, total);
+        pend_complete(field, fieldlen, pd);
+        pend_issue(field, pd, key, total);
     }
 }
 
@@ -914,8 +963,8 @@ __device__ __forceinline__ void vt_begin(const KArgs& a, Photon& s, unsigned int
     s.t.b = (unsigned long long)sd.z << 32 | sd.w;
 }
 
-template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT>
-__global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
+template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB>
+__global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
     extern __shared__ float4 smem4[];
 
@@ -924,7 +973,14 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
     for (unsigned int i = threadIdx.x; i < c_p.medianum; i += blockDim.x) {
         sprop[i] = a.gprop[i];
     }
-    float* sf = (float*)(smem4 + c_p.medianum);
+    float4* srecip = smem4 + c_p.medianum;
+    for (unsigned int i = threadIdx.x; i < c_p.medianum; i += blockDim.x) {
+        float4 q = a.gprop[i];
+        /* __fdividef(x, y) is x * rcp(y): keeping rcp(y) per medium gives the
+           fast kernel the same bits with one MUFU op fewer per use */
+        srecip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x), 0.f);
+    }
+    float* sf = (float*)(smem4 + 2 * c_p.medianum);
     float* sinvcdf = sf;
     for (unsigned int i = threadIdx.x; i < c_p.nphase; i += blockDim.x) {
         sinvcdf[i] = a.invcdf[i];
@@ -937,6 +993,7 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
 
     Shared S;
     S.prop = sprop;
+    S.recip = srecip;
     S.invcdf = sinvcdf;
     S.angleinvcdf = sangle;
     S.pp = sangle + c_p.nangle + threadIdx.x;
@@ -951,6 +1008,13 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
     bool fresh = true;             /* vt just claimed: initial launch */
     unsigned int mediaidold = 0, idx1dold = 0;
     unsigned int nsteps = 0;       /* steps of the current photon, against K_STEP_CAP */
+    Pending pd;
+    pd.on = false;
+    pd.idx = 0;
+    pd.old = pd.w = 0.f;
+    float3 rv = make_float3(0.f, 0.f, 0.f);   /* fast kernel: rcp of the direction */
+    bool vdirty = true;
+    const float gscat = (float)c_p.gscatter;
 
     while (vt < c_p.nthread) {
         if (fresh || relaunch) {
@@ -983,6 +1047,7 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
                 cnt_launch++;
             }
             nsteps = 0;
+            vdirty = true;
             s.isdet = s.mediaid & K_DET_MASK;
             s.mediaid &= K_MED_MASK;
         }
@@ -1063,6 +1128,7 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
                     rotatevector<EXACT>(s.v, stheta, ctheta, sphi, cphi);
                 }
                 s.v.w += 1.f;
+                vdirty = true;
             }
             s.v.w = (float)(int)s.v.w;
         }
@@ -1071,11 +1137,25 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
         updateprop(S, s.prop, s.mediaid);
 
         /* ---- move to the next voxel face or the end of the free path */
-        s.f.z = hitgrid<EXACT>(s.p, s.v, s.fx, s.fy, s.fz, s.fw);
+        if (EXACT) {
+            s.f.z = hitgrid<EXACT>(s.p, s.v, s.fx, s.fy, s.fz, s.fw);
+        } else {
+            if (vdirty) {
+                rv = make_float3(__fdividef(1.f, s.v.x), __fdividef(1.f, s.v.y), __fdividef(1.f, s.v.z));
+                vdirty = false;
+            }
+            s.f.z = hitgrid_rcp(s.p, s.v, rv, s.fx, s.fy, s.fz, s.fw);
+        }
         {
-            float slen = s.f.z * s.prop.y * (s.v.w + 1.f > (float)c_p.gscatter ? (1.f - s.prop.z) : 1.f);
+            const bool reduced = s.v.w + 1.f > gscat;
+            float slen = s.f.z * s.prop.y * (reduced ? (1.f - s.prop.z) : 1.f);
             slen = fminf(slen, s.f.x);
-            s.f.z = M::div(slen, s.prop.y * (s.v.w + 1.f > (float)c_p.gscatter ? (1.f - s.prop.z) : 1.f));
+            if (EXACT || c_p.mediaformat > 4) {
+                s.f.z = M::div(slen, s.prop.y * (reduced ? (1.f - s.prop.z) : 1.f));
+            } else {
+                const float4 rc = S.recip[s.mediaid & K_MED_MASK];
+                s.f.z = slen * (reduced ? rc.y : rc.x);
+            }
             s.pathlen += s.f.z;
             s.p.x = s.p.x + s.f.z * s.v.x;
             s.p.y = s.p.y + s.f.z * s.v.y;
@@ -1124,7 +1204,13 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
                     if (c_p.outputtype == otEnergy) {
                         weight = s.w0 - s.p.w;
                     } else if (c_p.outputtype == otFluence || c_p.outputtype == otFlux) {
-                        weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen) : M::div(s.w0 - s.p.w, s.prop.x);
+                        if (EXACT || c_p.mediaformat > 4) {
+                            weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen) : M::div(s.w0 - s.p.w, s.prop.x);
+                        } else {
+                            /* prop still holds the medium the photon deposited in */
+                            weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen)
+                                     : (s.w0 - s.p.w) * S.recip[mediaidold & K_MED_MASK].z;
+                        }
                     } else if (c_p.outputtype == otL) {
                         weight = s.w0 * s.pathlen;
                     }
@@ -1145,7 +1231,7 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
             } else {
                 s.mediaid = mediaidold;
             }
-            deposit<WAGG>(a.field, c_p.fieldlen, dep, key, weight);
+            deposit<WAGG>(a.field, c_p.fieldlen, dep, key, weight, pd);
         }
 
         /* ---- exit, time-out or cyclic boundary (mcx_core.cl:2958-3028) */
@@ -1201,7 +1287,6 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
                 if (COUNT) {
                     cnt_refl++;
                 }
-                updateprop(S, s.prop, s.mediaid);
                 float tmp0 = s.n1 * s.n1;
                 float tmp1 = s.prop.w * s.prop.w;
                 float cphi = fabsf(vcomp(s.v, s.fw));
@@ -1214,6 +1299,7 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
                     ctheta = tmp1 * cphi * cphi + tmp0 * s.f.z;
                     Rtotal = (Rtotal + M::div(ctheta - stheta, ctheta + stheta)) * 0.5f;
                 }
+                vdirty = true;
                 if (Rtotal < 1.f && (!(s.mediaid == 0 && ((s.isdet & 0xF) == bcMirror))) && rnd(s.t) > Rtotal) {
                     transmit<EXACT>(s.v, s.n1, s.prop.w, s.fw);
                     if (s.mediaid == 0) {
@@ -1256,6 +1342,7 @@ __global__ void __launch_bounds__(256) mcx_transport(const KArgs a) {
         }
     }
 
+    pend_complete(a.field, c_p.fieldlen, pd);
     if (COUNT) {
         atomicAdd(a.counters + 0, cnt_step);
         atomicAdd(a.counters + 1, cnt_scat);

@@ -21,22 +21,23 @@ cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int n
 }
 
 template <bool DET, bool REFL, bool WAGG>
-static void* kfun() {
-    return (void*)mcx_transport<false, DET, REFL, WAGG, false>;
+static void* kfun(bool occ3) {
+    return occ3 ? (void*)mcx_transport<false, DET, REFL, WAGG, false, 3>
+           : (void*)mcx_transport<false, DET, REFL, WAGG, false, 2>;
 }
 
 static void* select(int flags) {
-    const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG;
+    const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
     if (wagg) {
         if (det) {
-            return refl ? kfun<true, true, true>() : kfun<true, false, true>();
+            return refl ? kfun<true, true, true>(o3) : kfun<true, false, true>(o3);
         }
-        return refl ? kfun<false, true, true>() : kfun<false, false, true>();
+        return refl ? kfun<false, true, true>(o3) : kfun<false, false, true>(o3);
     }
     if (det) {
-        return refl ? kfun<true, true, false>() : kfun<true, false, false>();
+        return refl ? kfun<true, true, false>(o3) : kfun<true, false, false>(o3);
     }
-    return refl ? kfun<false, true, false>() : kfun<false, false, false>();
+    return refl ? kfun<false, true, false>(o3) : kfun<false, false, false>(o3);
 }
 
 cudaError_t fast_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st) {

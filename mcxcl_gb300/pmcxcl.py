@@ -29,7 +29,7 @@ DEBUGFLAGS = "RMP"
 _SCALARS_INT = ["nphoton", "nblocksize", "nthread", "maxdetphoton", "maxgate", "respin", "isreflect", "isrefint",
                 "isnormalized", "isgpuinfo", "issrcfrom0", "autopilot", "voidtime", "issaveref", "maxvoidstep",
                 "gscatter", "srcnum", "srcid", "isatomic", "internalsrc", "issavedet", "exactmath",
-                "savethreadenergy"]
+                "savethreadenergy", "autotune"]
 _SCALARS_BOOL = ["issaveexit", "ismomentum", "isspecular", "issave2pt", "issaveseed"]
 _SCALARS_FLOAT = ["tstart", "tstep", "tend", "minenergy", "unitinmm"]
 
@@ -218,7 +218,10 @@ def run(cfg=None, **kwargs):
     """Run one simulation; returns the reference's output dictionary.
 
     Extra (GB300) keys accepted: ``exactmath`` -- run the IEEE-only kernel
-    that reproduces the CPU oracle bit for bit (slower, for verification)."""
+    that reproduces the CPU oracle bit for bit (slower, for verification);
+    ``autotune`` -- time the launch shapes on a photon sample (once per
+    problem shape and GPU) and run with the fastest; ``savethreadenergy`` --
+    return each reference thread's escaped and launched weight."""
     cfg = dict(cfg or {}, **kwargs)
     L = _lib.load()
     C = Config()

@@ -79,7 +79,7 @@ def config(n):
         cfg.update(vol=sphere_volume(), prop=[[0, 0, 1, 1], [0.005, 1.0, 0.01, 1.37], [0.002, 5.0, 0.9, 1.0]],
                    isreflect=1, tstep=1e-10, nphoton=100000000,
                    detpos=[[30, 20, 0, 1], [30, 40, 0, 1], [20, 30, 0, 1], [40, 30, 0, 1]],
-                   savedetflag="dsp", session="config2")
+                   savedetflag="dsp", issaveseed=1, session="config2")
         return cfg
     if n == 3:
         vol = head_volume()
@@ -99,7 +99,8 @@ def config(n):
                      [0.02, 9.0, 0.89, 1.37], [0.08, 40.9, 0.84, 1.37]],
             "tstart": 0, "tend": 5e-9, "tstep": 5e-10,
             "srcpos": [cx, cy, ztop], "srcdir": [0, 0, 1], "issrcfrom0": 1,
-            "detpos": dets, "minenergy": 1e-4, "seed": 12345, "savedetflag": "dsp", "session": "config3",
+            "detpos": dets, "minenergy": 1e-4, "seed": 12345, "savedetflag": "dsp", "issaveseed": 1,
+            "session": "config3",
         }
     raise KeyError(n)
 

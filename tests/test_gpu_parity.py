@@ -169,3 +169,17 @@ def test_fast_kernel_voxel_fluence_within_3_sigma(gpu, O):
     assert np.mean(z > 3) < 0.02, np.mean(z > 3)
     # and the total fluence of the two 10-seed means agrees to 0.5%
     assert abs(mf.sum() - me.sum()) <= 0.005 * me.sum()
+
+
+def test_autotuned_launch_keeps_the_answer(gpu):
+    """The autotuner only changes the launch shape: the cube60 known answer
+    and the photon budget hold with it on, and a second run of the same
+    problem shape reuses the tuned choice."""
+    import mcxcl_gb300
+    cfg = cases.cube60(nphoton=3000000, seed=29012392, issavedet=0, autotune=1)
+    a = mcxcl_gb300.run(cfg)
+    b = mcxcl_gb300.run(dict(cfg, seed=29012393))
+    for g in (a, b):
+        assert abs(_absorbed(g) - 0.1769) <= 0.005
+        assert abs(g["stat"]["energytot"] - cfg["nphoton"]) <= 10
+    assert b["stat"]["kernelms"] > 0
