@@ -61,7 +61,7 @@ extern "C" {
 #define SEED_FROM_FILE       -999
 #define FILL_MAXDETPHOTON    3
 
-enum TOutputType {otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL};
+enum TOutputType {otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF};
 enum TBoundary {bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic};
 enum TMCXParent {mpStandalone, mpMATLAB, mpPython};
 
@@ -86,6 +86,16 @@ typedef struct MCXMedium {
 typedef struct MCXExtraSource {
     mcx_float4 srcpos, srcdir, srcparam1, srcparam2;
 } ExtraSrc;
+
+/* Photon replay inputs (PhotonReplay, src/mcx_utils.h:136-141).  The caller
+   sets seed (16 bytes per photon, malloc'd; cfg.seed = SEED_FROM_FILE);
+   mcx_validatecfg keeps the photons to replay and fills weight, tof, detid. */
+typedef struct MCXReplay {
+    void* seed;
+    float* weight;                /* detected weight: w0 * prod exp(-mua * partial path) */
+    float* tof;                   /* detected time of flight, s */
+    int* detid;                   /* detector id | source id << 16 */
+} Replay;
 
 /* src/mcx_utils.h:113-130: the .mch header, filled for detected photons */
 typedef struct MCXHistoryHeader {
@@ -164,6 +174,8 @@ typedef struct MCXConfig {
     int srcid;
     unsigned int extrasrclen;
     ExtraSrc* srcdata;
+    Replay replay;
+    int replaydet;                /* replay: 0 all detectors, -1 one output per detector, k detector k only */
     /* GB300 additions */
     int exactmath;                /* 1: run the IEEE-only kernel (bit-identical to the CPU oracle) */
     float kernelms;               /* kernel time from CUDA events, ms */
@@ -185,8 +197,11 @@ void mcx_initcfg(Config* cfg);
 void mcx_clearcfg(Config* cfg);
 /* Checks inputs, converts to 0-based positions, scales by unitinmm, builds the
    detector mask and launch voxel (src/mcx_utils.c:1822-1964, 1521-1809).
-   detps/dimdetps/seedbyte are accepted for signature compatibility; photon
-   replay is not part of this build and must be NULL/0. */
+   Replay (cfg.seed == SEED_FROM_FILE, cfg.replay.seed set): detps holds the
+   baseline run's records, dimdetps {reclen, count}, seedbyte 16; the photons
+   of detector replaydet (all when <= 0) whose time of flight lies in the time
+   window are kept, with their detected weights (mcx_replayinit,
+   src/mcx_utils.c:1355-1421). */
 void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte);
 /* Lists CUDA devices into *info (caller frees with mcx_cleargpuinfo); replaces
    mcx_list_gpu(Config*, unsigned*, cl_device_id*, GPUInfo**)
@@ -272,6 +287,11 @@ int  mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread);
    selects the instantiation whose registers are capped for three resident
    256-thread blocks per SM (also the automatic choice); 2 the uncapped one. */
 int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
+/* Replay inputs, one entry per replayed photon: the saved xorshift128+ state
+   (16 bytes), detected weight, time of flight and detector id.  Used when
+   the parameter block has replay = 1; n = 0 releases nothing and clears. */
+int  mcxg_set_replay(mcxg_session* s, const void* seeds16, const float* weight, const float* tof, const int* detid,
+                     uint32_t n);
 /* Pick the launch shape of the fast kernel for the current problem: time
    each candidate (256 threads x 2 or 3 resident blocks per SM, warp
    aggregation of deposits on or off) on the first sample_photons photons
@@ -287,6 +307,9 @@ int  mcxg_get_energy(mcxg_session* s, double* escaped, double* launched);
 int  mcxg_get_thread_energy(mcxg_session* s, float* out);
 /* Field: (hi + lo) in FP64, times scale, rounded to float; fieldlen values. */
 int  mcxg_get_field(mcxg_session* s, float* out, double scale);
+/* Field split into nblocks equal blocks, block b scaled by scales[b]
+   (a replay with one output per detector). */
+int  mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uint32_t nblocks);
 /* Field: (hi + lo) in FP64, unscaled. */
 int  mcxg_get_field_f64(mcxg_session* s, double* out);
 /* Detected photons: up to maxdetphoton records (reclen floats) and seeds

@@ -48,6 +48,11 @@ class GPUInfo(ctypes.Structure):
                 ("maxmpthread", ctypes.c_int), ("iscpu", ctypes.c_int), ("vendor", ctypes.c_int)]
 
 
+class Replay(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_void_p), ("weight", ctypes.POINTER(ctypes.c_float)),
+                ("tof", ctypes.POINTER(ctypes.c_float)), ("detid", ctypes.POINTER(ctypes.c_int))]
+
+
 class Config(ctypes.Structure):
     """Mirror of `Config` in include/mcx_gb300.h (checked field by field
     against mcx_config_offsetof by the test suite)."""
@@ -77,7 +82,8 @@ class Config(ctypes.Structure):
         ("parentid", ctypes.c_int), ("mediabyte", ctypes.c_uint), ("bc", ctypes.c_char * 13),
         ("nphase", ctypes.c_uint), ("invcdf", ctypes.POINTER(ctypes.c_float)), ("nangle", ctypes.c_uint),
         ("angleinvcdf", ctypes.POINTER(ctypes.c_float)), ("srcid", ctypes.c_int), ("extrasrclen", ctypes.c_uint),
-        ("srcdata", ctypes.POINTER(ExtraSrc)), ("exactmath", ctypes.c_int), ("kernelms", ctypes.c_float),
+        ("srcdata", ctypes.POINTER(ExtraSrc)), ("replay", Replay), ("replaydet", ctypes.c_int),
+        ("exactmath", ctypes.c_int), ("kernelms", ctypes.c_float),
         ("eventcount", ctypes.c_uint64 * 5), ("failedlaunch", ctypes.c_uint), ("threadused", ctypes.c_uint),
         ("exportenergy", ctypes.POINTER(ctypes.c_float)), ("savethreadenergy", ctypes.c_int),
         ("autotune", ctypes.c_int), ("errorcode", ctypes.c_int),
@@ -101,6 +107,7 @@ EXPORTS = [
     "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_launch", "mcxg_simulate",
     "mcxg_get_energy", "mcxg_get_thread_energy", "mcxg_get_field", "mcxg_get_field_f64", "mcxg_get_detected",
     "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc", "mcxg_autotune",
+    "mcxg_set_replay", "mcxg_get_field_blocks",
 ]
 
 _lib = None

@@ -61,6 +61,18 @@ struct mcxg_session {
     void* d_out = nullptr;           /* merged field, float or double */
     size_t out_cap = 0;
 
+    ulonglong2* d_rseed = nullptr;   /* replay: per photon RNG state, weight, tof, detector id */
+    size_t rseed_cap = 0;
+    float* d_rweight = nullptr;
+    size_t rweight_cap = 0;
+    float* d_rtof = nullptr;
+    size_t rtof_cap = 0;
+    int* d_rdetid = nullptr;
+    size_t rdetid_cap = 0;
+    uint32_t nreplay = 0;
+    double* d_scales = nullptr;      /* per-block normalisation factors */
+    size_t scales_cap = 0;
+
     std::vector<float> h_det, h_srcx;
     int block_req = 0, bpsm_req = 0;
     int tuned = 0;                   /* 1 once mcxg_autotune picked a shape for this problem */
@@ -154,6 +166,13 @@ __global__ void energy_final(double* part, int nblocks) {
 __global__ void field_merge_f32(const float* __restrict__ f, size_t n, double scale, float* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         out[i] = (float)(((double)f[i] + (double)f[i + n]) * scale);
+    }
+}
+
+__global__ void field_merge_blocks(const float* __restrict__ f, size_t n, size_t blocklen,
+                                   const double* __restrict__ scales, float* __restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        out[i] = (float)(((double)f[i] + (double)f[i + n]) * scales[i / blocklen]);
     }
 }
 
@@ -304,7 +323,8 @@ int mcxg_destroy(mcxg_session* s) {
         cudaStreamSynchronize(s->st);
     }
     void* bufs[] = {s->d_media, s->d_prop, s->d_tables, s->d_pattern, s->d_seeds, s->d_field, s->d_energy,
-                    s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out};
+                    s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
+                    s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales};
     for (void* b : bufs) {
         if (b) {
             cudaFree(b);
@@ -435,6 +455,37 @@ int mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread) {
     return MCXG_OK;
 }
 
+int mcxg_set_replay(mcxg_session* s, const void* seeds16, const float* weight, const float* tof, const int* detid,
+                    uint32_t n) {
+    if (!s || (n && (!seeds16 || !weight || !tof || !detid))) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    /* one spare entry so an empty replay still has valid pointers */
+    int rc = ensure(&s->d_rseed, &s->rseed_cap, (size_t)n + 1);
+    if (!rc) {
+        rc = ensure(&s->d_rweight, &s->rweight_cap, (size_t)n + 1);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_rtof, &s->rtof_cap, (size_t)n + 1);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_rdetid, &s->rdetid_cap, (size_t)n + 1);
+    }
+    if (rc) {
+        return rc;
+    }
+    if (n) {
+        MCXG_TRY(cudaMemcpyAsync(s->d_rseed, seeds16, 16 * (size_t)n, cudaMemcpyHostToDevice, s->st));
+        MCXG_TRY(cudaMemcpyAsync(s->d_rweight, weight, sizeof(float) * n, cudaMemcpyHostToDevice, s->st));
+        MCXG_TRY(cudaMemcpyAsync(s->d_rtof, tof, sizeof(float) * n, cudaMemcpyHostToDevice, s->st));
+        MCXG_TRY(cudaMemcpyAsync(s->d_rdetid, detid, sizeof(int) * n, cudaMemcpyHostToDevice, s->st));
+    }
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    s->nreplay = n;
+    return MCXG_OK;
+}
+
 int mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm) {
     if (!s || block < 0 || block > 256 || (block % 32) || blocks_per_sm < 0) {
         return MCXG_ERR_ARG;
@@ -486,6 +537,13 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     a.vtcounter = s->d_words + 1;
     a.status = s->d_words + 2;
     a.counters = s->d_events;
+    a.rseed = s->d_rseed;
+    a.rweight = s->d_rweight;
+    a.rtof = s->d_rtof;
+    a.rdetid = s->d_rdetid;
+    if (kp.replay && (kp.nreplay > s->nreplay || !s->d_rseed)) {
+        return MCXG_ERR_STATE;
+    }
 
     /* deposits go straight to the field unless aggregation is asked for or
        the autotuner found it faster for this problem */
@@ -647,6 +705,26 @@ int mcxg_get_field(mcxg_session* s, float* out, double scale) {
         return rc;
     }
     field_merge_f32<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, scale, (float*)s->d_out);
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uint32_t nblocks) {
+    if (!s || !out || !scales || nblocks == 0 || !s->has_problem || s->kp.fieldlen % nblocks) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    size_t n = s->kp.fieldlen;
+    int rc = ensure((double**)&s->d_out, &s->out_cap, n);
+    if (!rc) {
+        rc = ensure(&s->d_scales, &s->scales_cap, nblocks);
+    }
+    if (rc) {
+        return rc;
+    }
+    MCXG_TRY(cudaMemcpyAsync(s->d_scales, scales, sizeof(double) * nblocks, cudaMemcpyHostToDevice, s->st));
+    field_merge_blocks<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, n / nblocks, s->d_scales, (float*)s->d_out);
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;

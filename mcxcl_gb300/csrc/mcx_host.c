@@ -137,6 +137,11 @@ void mcx_clearcfg(Config* cfg) {
     free(cfg->angleinvcdf);
     free(cfg->srcdata);
     free(cfg->exportenergy);
+    free(cfg->replay.seed);
+    free(cfg->replay.weight);
+    free(cfg->replay.tof);
+    free(cfg->replay.detid);
+    memset(&cfg->replay, 0, sizeof(cfg->replay));
     cfg->exportenergy = NULL;
     cfg->prop = NULL;
     cfg->detpos = NULL;
@@ -350,7 +355,9 @@ static void preprocess(Config* cfg) {
     if (cfg->issavedet == 0) {
         cfg->issaveexit = 0;
         cfg->ismomentum = 0;
-        cfg->savedetflag = 0;
+        if (cfg->seed != SEED_FROM_FILE) {
+            cfg->savedetflag = 0;  /* a replay keeps the flags describing its input records */
+        }
     }
     if (cfg->respin == 0) {
         MCX_ERROR(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
@@ -430,12 +437,90 @@ static void preprocess(Config* cfg) {
     }
 }
 
+/* mcx_replayinit (mcx_utils.c:1355-1421): keep the records of detector
+   replaydet (all when <= 0) and of source srcid, compute each one's detected
+   weight and time of flight from its partial paths, drop those outside the
+   time window, and compact the seeds to match. */
+static void replayinit(Config* cfg, const float* detps, const int dimdetps[2], int seedbyte) {
+    if (cfg->seed == SEED_FROM_FILE && detps == NULL) {
+        MCX_ERROR(-6, "you give cfg.seed for replay, but did not specify cfg.detphotons.\nPlease define it as the "
+                  "detphoton output from the baseline simulation\n");
+    }
+    if (detps == NULL || cfg->seed != SEED_FROM_FILE) {
+        return;
+    }
+    if (!cfg->replay.seed) {
+        MCX_ERROR(-6, "the seed input is empty");
+    }
+    if (cfg->nphoton != (size_t)dimdetps[1]) {
+        MCX_ERROR(-6, "the column numbers of detphotons and seed do not match\n");
+    }
+    if (seedbyte == 0) {
+        MCX_ERROR(-6, "the seed input is empty");
+    }
+    if (seedbyte != 16) {
+        MCX_ERROR(-6, "the row number of cfg.seed does not match RNG seed byte-length");
+    }
+    int hasdetid = SAVE_DETID(cfg->savedetflag);
+    unsigned int offset = SAVE_NSCAT(cfg->savedetflag) * (cfg->medianum - 1);
+    if (((!hasdetid) && cfg->detnum > 1) || !SAVE_PPATH(cfg->savedetflag)) {
+        MCX_ERROR(-6, "please rerun the baseline simulation and save detector ID (D) and partial-path (P) using "
+                  "cfg.savedetflag='dp' ");
+    }
+    if ((unsigned int)dimdetps[0] < (unsigned int)hasdetid + offset + cfg->medianum - 1) {
+        MCX_ERROR(-6, "the row number of detphotons is less than the record length implied by savedetflag");
+    }
+    size_t n = (size_t)dimdetps[1];
+    free(cfg->replay.weight);
+    free(cfg->replay.tof);
+    free(cfg->replay.detid);
+    cfg->replay.weight = (float*)malloc(sizeof(float) * (n ? n : 1));
+    cfg->replay.tof = (float*)calloc(n ? n : 1, sizeof(float));
+    cfg->replay.detid = (int*)calloc(n ? n : 1, sizeof(int));
+    if (!cfg->replay.weight || !cfg->replay.tof || !cfg->replay.detid) {
+        MCX_ERROR(-2, "out of host memory");
+    }
+    size_t kept = 0;
+    for (size_t i = 0; i < n; i++) {
+        const float* rec = detps + i * (size_t)dimdetps[0];
+        int did = (int)rec[0];
+        if (!(cfg->replaydet <= 0 || cfg->replaydet == (did & 0xFFFF))) {
+            continue;
+        }
+        if (!(cfg->srcid <= 0 || ((did & 0xFFFF0000) && cfg->srcid == ((did & 0xFFFF0000) >> 16)))) {
+            continue;
+        }
+        if (i != kept) {
+            memmove((char*)cfg->replay.seed + kept * 16, (char*)cfg->replay.seed + i * 16, 16);
+        }
+        cfg->replay.weight[kept] = 1.f;
+        cfg->replay.tof[kept] = 0.f;
+        cfg->replay.detid[kept] = hasdetid ? did : 1;
+        for (unsigned int j = (unsigned int)hasdetid; j < cfg->medianum - 1 + (unsigned int)hasdetid; j++) {
+            float plen = rec[offset + j];
+            cfg->replay.weight[kept] *= expf(-cfg->prop[j - hasdetid + 1].mua * plen);
+            plen *= cfg->unitinmm;
+            cfg->replay.tof[kept] += plen * R_C0 * cfg->prop[j - hasdetid + 1].n;
+        }
+        if (cfg->replay.tof[kept] < cfg->tstart || cfg->replay.tof[kept] > cfg->tend) {
+            continue;
+        }
+        if (cfg->replaydet == -1 && ((cfg->replay.detid[kept] & 0xFFFF) < 1 ||
+                                     (cfg->replay.detid[kept] & 0xFFFF) > (int)cfg->detnum)) {
+            MCX_ERROR(-6, "a replayed record carries a detector id outside 1..detnum");
+        }
+        kept++;
+    }
+    cfg->nphoton = kept;
+}
+
 void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte) {
     MCX_ENTER(cfg);
-    (void)dimdetps;
-    (void)seedbyte;
-    if (cfg->seed == SEED_FROM_FILE || detps) {
-        MCX_ERROR(-6, "photon replay is not part of this build");
+    if (cfg->seed == SEED_FROM_FILE && cfg->replaydet > (int)cfg->detnum) {
+        MCX_ERROR(-4, "replay detector ID exceeds the maximum detector number");
+    }
+    if (cfg->replaydet == -1 && cfg->detnum == 1) {
+        cfg->replaydet = 1;
     }
     if (!cfg->issrcfrom0) {
         cfg->srcpos.x--;
@@ -463,10 +548,17 @@ void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte) {
     if (cfg->maxgate > (unsigned int)gates) {
         cfg->maxgate = gates;
     }
-    if (cfg->outputtype == otJacobian || cfg->outputtype == otWP || cfg->outputtype == otDCS || cfg->outputtype == otRF) {
+    int replayout = cfg->outputtype == otJacobian || cfg->outputtype == otWP || cfg->outputtype == otDCS ||
+                    cfg->outputtype == otRF || cfg->outputtype == otRFmus || cfg->outputtype == otWLTOF ||
+                    cfg->outputtype == otWPTOF;
+    if (replayout && cfg->seed != SEED_FROM_FILE) {
         MCX_ERROR(-6, "Jacobian output is only valid in the reply mode. Please define cfg.seed");
     }
-    if (cfg->outputtype != otFlux && cfg->outputtype != otFluence && cfg->outputtype != otEnergy && cfg->outputtype != otL) {
+    if (cfg->outputtype == otRF || cfg->outputtype == otRFmus) {
+        MCX_ERROR(-6, "RF replay outputs need the frequency-domain transport, which this build does not include");
+    }
+    if (!replayout && cfg->outputtype != otFlux && cfg->outputtype != otFluence && cfg->outputtype != otEnergy &&
+            cfg->outputtype != otL) {
         MCX_ERROR(-6, "unsupported output type");
     }
     if (!cfg->issrcfrom0) {
@@ -483,6 +575,7 @@ void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte) {
     cfg->his.colcount = mcx_detreclen(cfg);
     cfg->his.savedetflag = cfg->savedetflag;
     cfg->his.totalsource = ((cfg->srcid <= 0) ? cfg->extrasrclen + 1 : 1);
+    replayinit(cfg, detps, dimdetps, seedbyte);
     MCX_LEAVE();
 }
 
@@ -647,8 +740,8 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     GPUInfo* gpu = NULL;
     /* temporaries live in thread-local slots so the library-mode error path
        (longjmp back to this frame) can free them */
-    static __thread void* tmp[5];
-    for (int i = 0; i < 5; i++) {
+    static __thread void* tmp[6];
+    for (int i = 0; i < 6; i++) {
         free(tmp[i]);
         tmp[i] = NULL;
     }
@@ -657,6 +750,7 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
 #define detbuf   (*(float**)&tmp[2])
 #define seedbuf  (*(uint64_t**)&tmp[3])
 #define fieldtmp (*(float**)&tmp[4])
+#define blockscale (*(double**)&tmp[5])
     MCX_ENTER(cfg);
 
     unsigned int partialdata = (cfg->medianum - 1) *
@@ -702,6 +796,13 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     cfg->maxgate = (unsigned int)(int)((cfg->tend - cfg->tstart) / cfg->tstep + 0.5);
     size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
     size_t mult = (cfg->extrasrclen && cfg->srcid < 0) ? (cfg->extrasrclen + 1) : 1;
+    const int replay = (cfg->seed == SEED_FROM_FILE);
+    if (replay && cfg->replaydet == -1) {
+        mult *= cfg->detnum;    /* one block of gates per detector (mcx_host.cpp:684-687) */
+    }
+    if (replay && cfg->nphoton && (!cfg->replay.seed || !cfg->replay.weight || !cfg->replay.tof || !cfg->replay.detid)) {
+        MCX_ERROR(-6, "replay inputs are missing: call mcx_validatecfg with the baseline records first");
+    }
     size_t fieldlen = nvox * cfg->maxgate * mult;
     if (fieldlen > 0xFFFFFFFFull || nvox > 0x7FFFFFFFull) {
         MCX_ERROR(-1, "volume x gates too large for 32-bit field indices");
@@ -773,6 +874,12 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     kp.extrasrclen = cfg->extrasrclen;
     kp.srcid = cfg->srcid;
     kp.nthread = (uint32_t)autothread;
+    if (replay) {
+        kp.replay = 1;
+        kp.nreplay = (uint32_t)cfg->nphoton;
+        kp.replaydet = cfg->replaydet;
+        kp.siteshift = 1;
+    }
     for (int i = 0; i < 12; i++) {
         kp.bc[i] = (uint8_t)cfg->bc[i];
     }
@@ -809,13 +916,16 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     free(packed);
     packed = NULL;
     device_check(rc, "uploading the problem");
+    device_check(mcxg_set_replay(s, cfg->replay.seed, cfg->replay.weight, cfg->replay.tof, cfg->replay.detid,
+                                 replay ? (uint32_t)cfg->nphoton : 0u), "uploading the replay inputs");
 
     /* seeds: srand(seed) then 4 rand() words per reference thread
-       (mcx_host.cpp:696-700, 759-768) */
+       (mcx_host.cpp:696-700, 759-768); a replay launches every photon from its
+       saved state, so its per-thread words are never drawn from */
     if (cfg->seed > 0) {
         srand((unsigned int)cfg->seed);
     } else {
-        srand((unsigned int)time(0));
+        srand(replay ? 1u : (unsigned int)time(0));
     }
     seeds = (uint32_t*)malloc(sizeof(uint32_t) * 4 * autothread);
     if (!seeds) {
@@ -932,7 +1042,7 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
         }
     }
     if (prepare_only) {
-        for (int i = 0; i < 5; i++) {
+        for (int i = 0; i < 6; i++) {
             free(tmp[i]);
             tmp[i] = NULL;
         }
@@ -943,9 +1053,14 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     cfg->threadused = (unsigned int)autothread;
     cfg->runtime = (unsigned int)(kms_total + 0.5f);
 
-    /* normalisation (mcx_host.cpp:1382-1465), applied in FP64 on the GPU */
+    /* normalisation (mcx_host.cpp:1382-1465), applied in FP64 on the GPU; a
+       replay with one output per detector scales each detector's block by its
+       own replayed weight (1398-1419) */
     double scale = 1.0;
+    uint32_t nblocks = 1;
     if (cfg->issave2pt) {
+        int replayout = cfg->outputtype == otJacobian || cfg->outputtype == otWP || cfg->outputtype == otDCS ||
+                        cfg->outputtype == otWLTOF || cfg->outputtype == otWPTOF;
         if (cfg->isnormalized) {
             float Vvox = cfg->steps.x * cfg->steps.y * cfg->steps.z;
             float sc = 1.f;
@@ -957,9 +1072,45 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
                 }
             } else if (cfg->outputtype == otEnergy || cfg->outputtype == otL) {
                 sc = (float)(1.0 / cfg->energytot);
+            } else if (replayout) {
+                if (replay && cfg->replaydet == -1) {
+                    nblocks = cfg->detnum * (uint32_t)mult / cfg->detnum;
+                    blockscale = (double*)calloc(nblocks, sizeof(double));
+                    if (!blockscale) {
+                        MCX_ERROR(-2, "out of host memory");
+                    }
+                    for (uint32_t d = 0; d < cfg->detnum; d++) {
+                        float w = 0.f;
+                        for (size_t i = 0; i < cfg->nphoton; i++) {
+                            if ((cfg->replay.detid[i] & 0xFFFF) == (int)d + 1) {
+                                w += cfg->replay.weight[i];
+                            }
+                        }
+                        if (w > 0.f) {
+                            w = cfg->unitinmm / w;
+                        }
+                        for (uint32_t b = d; b < nblocks; b += cfg->detnum) {
+                            blockscale[b] = (double)w;
+                        }
+                        sc = w;    /* the reference leaves the last detector's factor as the normaliser */
+                    }
+                } else {
+                    sc = 0.f;
+                    for (size_t i = 0; i < cfg->nphoton; i++) {
+                        sc += cfg->replay.weight[i];
+                    }
+                    if (sc > 0.f) {
+                        sc = cfg->unitinmm / sc;
+                    }
+                }
             }
             if (cfg->extrasrclen && cfg->srcid < 0) {
                 sc *= (float)(cfg->extrasrclen + 1);
+                if (blockscale) {
+                    for (uint32_t b = 0; b < nblocks; b++) {
+                        blockscale[b] *= (double)(cfg->extrasrclen + 1);
+                    }
+                }
             }
             cfg->normalizer = sc;
             cfg->his.normalizer = sc;
@@ -967,20 +1118,30 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
         }
         if (cfg->debuglevel & 1) {
             scale = 1.0;
+            free(blockscale);
+            blockscale = NULL;
         }
-        if (!cfg->exportfield) {
+        float* dst = cfg->exportfield;
+        if (!dst) {
             cfg->exportfield = (float*)calloc(fieldlen, sizeof(float));
             if (!cfg->exportfield) {
                 MCX_ERROR(-2, "out of host memory");
             }
-            device_check(mcxg_get_field(s, cfg->exportfield, scale), "reading the field");
+            dst = cfg->exportfield;
         } else {
             /* caller-supplied buffer: add, as the reference does (mcx_host.cpp:1292-1296) */
             fieldtmp = (float*)malloc(sizeof(float) * fieldlen);
             if (!fieldtmp) {
                 MCX_ERROR(-2, "out of host memory");
             }
-            device_check(mcxg_get_field(s, fieldtmp, scale), "reading the field");
+            dst = fieldtmp;
+        }
+        if (blockscale) {
+            device_check(mcxg_get_field_blocks(s, dst, blockscale, nblocks), "reading the field");
+        } else {
+            device_check(mcxg_get_field(s, dst, scale), "reading the field");
+        }
+        if (dst == fieldtmp) {
             for (size_t i = 0; i < fieldlen; i++) {
                 cfg->exportfield[i] += fieldtmp[i];
             }
@@ -998,7 +1159,7 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
                 "excluded in the total)\n", cfg->energytot,
                 (cfg->energytot - cfg->energyesc) / cfg->energytot * 100.f);
     }
-    for (int i = 0; i < 5; i++) {
+    for (int i = 0; i < 6; i++) {
         free(tmp[i]);
         tmp[i] = NULL;
     }
@@ -1007,6 +1168,7 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
 #undef detbuf
 #undef seedbuf
 #undef fieldtmp
+#undef blockscale
     MCX_LEAVE();
 }
 
@@ -1040,7 +1202,7 @@ static const struct {
     MCX_FIELD(exportdetected), MCX_FIELD(debuglevel), MCX_FIELD(normalizer), MCX_FIELD(seeddata), MCX_FIELD(gscatter),
     MCX_FIELD(savedetflag), MCX_FIELD(detectedcount), MCX_FIELD(runtime), MCX_FIELD(parentid), MCX_FIELD(mediabyte),
     MCX_FIELD(bc), MCX_FIELD(nphase), MCX_FIELD(invcdf), MCX_FIELD(nangle), MCX_FIELD(angleinvcdf), MCX_FIELD(srcid),
-    MCX_FIELD(extrasrclen), MCX_FIELD(srcdata), MCX_FIELD(exactmath), MCX_FIELD(kernelms), MCX_FIELD(eventcount),
+    MCX_FIELD(extrasrclen), MCX_FIELD(srcdata), MCX_FIELD(replay), MCX_FIELD(replaydet), MCX_FIELD(exactmath), MCX_FIELD(kernelms), MCX_FIELD(eventcount),
     MCX_FIELD(failedlaunch), MCX_FIELD(threadused), MCX_FIELD(exportenergy), MCX_FIELD(savethreadenergy),
     MCX_FIELD(autotune), MCX_FIELD(errorcode), MCX_FIELD(errormsg),
 };

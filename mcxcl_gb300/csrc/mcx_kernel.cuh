@@ -65,7 +65,7 @@ namespace {
 #define K_CONE_CAP       (1u << 16)     /* rejection draws of the cone source */
 
 enum { bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic };
-enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL };
+enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF };
 enum { S_PENCIL, S_ISOTROPIC, S_CONE, S_GAUSSIAN, S_PLANAR, S_PATTERN, S_FOURIER, S_ARCSINE,
        S_DISK, S_FOURIERX, S_FOURIERX2D, S_ZGAUSSIAN, S_LINE, S_SLIT, S_PENCILARRAY, S_PATTERN3D,
        S_HYPERBOLOID, S_RING };
@@ -526,6 +526,47 @@ __device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, boo
     }
 }
 
+/* ------------------------------------------------------------------ replay */
+
+/* index of the photon a replay quantity belongs to: the reference's
+   vt*threadphoton + min(vt, oddphoton-1) + offset (mcx_core.cl:1591, 2571, 2847) */
+__device__ __forceinline__ long long replay_index(unsigned int vt, long long offset) {
+    long long m = (long long)c_p.oddphoton - 1;
+    long long t = (long long)vt;
+    return t * (long long)c_p.threadphoton + (t < m ? t : m) + offset;
+}
+
+/* replay deposit at a scattering site (mcx_core.cl:2567-2604): the detected
+   weight (x (1 - cos theta) for the momentum-transfer output, x time of
+   flight for wptof) into the gate of the photon's detected time of flight */
+__device__ void replay_site_deposit(const KArgs& a, const Photon& s, unsigned int vt, float ctheta) {
+    long long k = replay_index(vt, (long long)(int)s.f.w - 1 + (long long)c_p.siteshift);
+    if (k < 0 || k >= (long long)c_p.nreplay) {
+        return;        /* the reference reads one photon past its arrays here */
+    }
+    float rt = __ldg(a.rtof + k);
+    float rw = __ldg(a.rweight + k);
+    float tmp0 = (c_p.outputtype == otDCS) ? (1.f - ctheta) : 1.f;
+    if (c_p.outputtype == otWPTOF) {
+        tmp0 = rt;
+        tmp0 *= rw;
+    } else {
+        tmp0 *= rw;
+    }
+    int tshift = (int)(floorf((rt - c_p.twin0) * c_p.Rtstep)) +
+                 ((c_p.replaydet == -1) ? (((__ldg(a.rdetid + k) & 0xFFFF) - 1) * (int)c_p.maxgate) : 0);
+    if (c_p.extrasrclen && (c_p.srcid < 0)) {
+        tshift += ((int)s.srcsel - 1) * ((c_p.replaydet == -1) ? (int)c_p.detnum : 1) * (int)c_p.maxgate;
+    }
+    tshift = ((int)c_p.maxgate - 1 < tshift) ? (int)c_p.maxgate - 1 : tshift;
+    long long key = (long long)s.idx1d + (long long)tshift * c_p.nvox;
+    if (key < 0 || key >= (long long)c_p.fieldlen) {
+        atomicAdd(a.status + ST_GUARD, 1u);
+        return;
+    }
+    field_add2(a.field, c_p.fieldlen, (unsigned int)key, tmp0);
+}
+
 /* ------------------------------------------------------------------ launch */
 
 __device__ __forceinline__ void set_launch_voxel(const KArgs& a, Photon& s) {
@@ -582,6 +623,18 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
         return 1;
     }
 
+    if (c_p.replay) {
+        /* the saved launch state of this photon (mcx_core.cl:1590-1596) */
+        long long k = replay_index(vt, (long long)((int)s.f.w > 0 ? (int)s.f.w : 0));
+        if (k < 0 || k >= (long long)c_p.nreplay) {
+            atomicAdd(a.status + ST_GUARD, 1u);
+            return 1;
+        }
+        ulonglong2 st = a.rseed[k];
+        s.t.a = st.x;
+        s.t.b = st.y;
+    }
+
     if (DET && c_p.issaveseed) {
         s.ps0 = s.t.a;
         s.ps1 = s.t.b;
@@ -604,6 +657,10 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
             lp1 = c_srcx[sel * 4 + 2];
             lp2 = c_srcx[sel * 4 + 3];
         }
+    }
+
+    if (c_p.replay && c_p.srcid >= 1) {
+        rnd(s.t);      /* keeps the stream in step with a run that picked a source (1614-1616) */
     }
 
     unsigned int attempts = 0;
@@ -1129,6 +1186,9 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 }
                 s.v.w += 1.f;
                 vdirty = true;
+                if (c_p.replay && (c_p.outputtype == otWP || c_p.outputtype == otDCS || c_p.outputtype == otWPTOF)) {
+                    replay_site_deposit(a, s, vt, ctheta);
+                }
             }
             s.v.w = (float)(int)s.v.w;
         }
@@ -1211,11 +1271,34 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                             weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen)
                                      : (s.w0 - s.p.w) * S.recip[mediaidold & K_MED_MASK].z;
                         }
+                    } else if (c_p.replay) {
+                        /* replay Jacobian (mcx_core.cl:2845-2858): detected weight times
+                           the path length in the voxel, gated by the detected time of flight */
+                        if (c_p.outputtype == otJacobian || c_p.outputtype == otWLTOF) {
+                            long long k = replay_index(vt, (long long)(int)s.f.w - 1);
+                            if (k >= 0 && k < (long long)c_p.nreplay) {
+                                float rt = __ldg(a.rtof + k);
+                                int d = __ldg(a.rdetid + k) & 0xFFFF;
+                                weight = __ldg(a.rweight + k) * s.pathlen;
+                                tshift = (int)(floorf((rt - c_p.twin0) * c_p.Rtstep)) +
+                                         ((c_p.replaydet == -1) ? ((d - 1) * (int)c_p.maxgate) : 0);
+                                if (c_p.outputtype == otWLTOF) {
+                                    weight = weight * rt;
+                                }
+                                if (tshift < 0 || (c_p.replaydet == -1 && (d < 1 || d > (int)c_p.detnum))) {
+                                    /* the host filters these out; never index with them */
+                                    atomicAdd(a.status + ST_GUARD, 1u);
+                                    weight = 0.f;
+                                    tshift = 0;
+                                }
+                            }
+                        }
                     } else if (c_p.outputtype == otL) {
                         weight = s.w0 * s.pathlen;
                     }
                     if (c_p.extrasrclen && (c_p.srcid < 0)) {
-                        tshift += ((int)s.srcsel - 1) * (int)c_p.maxgate;
+                        tshift += ((int)s.srcsel - 1) * ((c_p.replay && c_p.replaydet == -1) ? (int)c_p.detnum : 1) *
+                                  (int)c_p.maxgate;
                     }
                     dep = fabsf(weight) > 0.f;
                     key = idx1dold + (unsigned int)tshift * c_p.nvox;

@@ -62,6 +62,10 @@ typedef struct mcxg_kparams {
     uint32_t mediaword;            /* bytes per voxel in device memory: 1 (label | det<<7) or 4 */
     uint32_t npattern;             /* source pattern length, for index clamping */
     uint8_t  bc[12];               /* face conditions then detector flags, as small integers */
+    uint32_t replay;               /* 1: photons start from saved RNG states (the reference's SEED_FROM_FILE) */
+    uint32_t nreplay;              /* replayed photons */
+    int32_t  replaydet;            /* 0 all detectors, -1 one gate block per detector, k detector k */
+    uint32_t siteshift;            /* scattering-site replay deposits read photon k+siteshift (the reference: 1) */
 } mcxg_kparams;
 
 #endif

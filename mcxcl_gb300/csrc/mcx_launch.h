@@ -29,6 +29,11 @@ struct KArgs {
     unsigned int* vtcounter;       /* work queue head */
     unsigned int* status;
     unsigned long long* counters;  /* step, scatter, launch, reflect, failed */
+    /* replay: per photon, the saved RNG state, detected weight, time of flight, detector id */
+    const ulonglong2* rseed;
+    const float* rweight;
+    const float* rtof;
+    const int* rdetid;
 };
 
 /* flag bits for the launch entries */

@@ -17,6 +17,8 @@ import numpy as np
 from . import _lib
 from ._lib import Config, ExtraSrc, Float4, GPUInfo, Medium
 
+SEED_FROM_FILE = -999
+
 SRCTYPES = ["pencil", "isotropic", "cone", "gaussian", "planar", "pattern", "fourier", "arcsine", "disk",
             "fourierx", "fourierx2d", "zgaussian", "line", "slit", "pencilarray", "pattern3d", "hyperboloid",
             "ring"]
@@ -192,7 +194,18 @@ def parse_config(cfg, C):
         if isinstance(sv, (int, float, np.integer, np.floating)):
             C.seed = int(sv)
         else:
-            raise ValueError("photon replay (cfg.seed as a seed array) is not part of this build")
+            # replay: the uint8 [16, N] seeds of a previous run's detected photons (src/pmcxcl.cpp:1021-1047)
+            s8 = np.asfortranarray(np.asarray(sv), dtype=np.uint8)
+            if s8.ndim != 2 or s8.shape[0] != 16:
+                raise ValueError("the row number of cfg.seed does not match RNG seed byte-length")
+            raw = np.ascontiguousarray(s8.T).tobytes()
+            buf = _libc_malloc(max(len(raw), 1))
+            ctypes.memmove(buf, raw, len(raw))
+            C.replay.seed = buf
+            C.seed = SEED_FROM_FILE
+            C.nphoton = s8.shape[1]
+    if "replaydet" in cfg:
+        C.replaydet = int(cfg["replaydet"])
     if "gpuid" in cfg:
         g = cfg["gpuid"]
         C.deviceid = b"\0" * 256
@@ -207,6 +220,36 @@ def parse_config(cfg, C):
         for i, v in enumerate(w[:256]):
             C.workload[i] = float(v)
     return C
+
+
+_libc = None
+
+
+def _libc_malloc(n):
+    """Host buffers the Config owns are freed by mcx_clearcfg, so they come from malloc."""
+    global _libc
+    if _libc is None:
+        _libc = ctypes.CDLL(None)
+        _libc.malloc.restype = ctypes.c_void_p
+        _libc.malloc.argtypes = [ctypes.c_size_t]
+    p = _libc.malloc(n)
+    if not p:
+        raise MemoryError("malloc failed")
+    return p
+
+
+def _detphotons(cfg):
+    """cfg['detphotons']: the float32 [reclen, N] records of the baseline run
+    (src/pmcxcl.cpp:1006-1018); a dict with a 'data' entry is accepted too."""
+    d = cfg.get("detphotons")
+    if d is None:
+        return None
+    if isinstance(d, dict):
+        d = d.get("data", d.get("detp"))
+    d = np.asarray(d, np.float32)
+    if d.ndim != 2:
+        raise ValueError("Invalid detphotons field value")
+    return np.ascontiguousarray(d.T)
 
 
 def _check(C):
@@ -227,7 +270,13 @@ def run(cfg=None, **kwargs):
     C = Config()
     try:
         parse_config(cfg, C)
-        L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
+        recs = _detphotons(cfg)
+        if recs is not None:
+            dims = (ctypes.c_int * 2)(recs.shape[1], recs.shape[0])
+            seedbyte = 16 if C.seed == SEED_FROM_FILE else 0
+            L.mcx_validatecfg(ctypes.byref(C), recs.ctypes.data_as(ctypes.c_void_p), dims, seedbyte)
+        else:
+            L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
         _check(C)
         L.mcx_run_simulation(ctypes.byref(C), None, None)
         _check(C)
@@ -251,10 +300,13 @@ def _outputs(cfg, C):
     if C.issave2pt != b"\0":
         gates = int((C.tend - C.tstart) / C.tstep + 0.5)
         nsrc = C.extrasrclen + 1 if (C.extrasrclen and C.srcid < 0) else 1
-        n = C.dim.x * C.dim.y * C.dim.z * gates * nsrc
+        ndetblk = C.detnum if (C.seed == SEED_FROM_FILE and C.replaydet == -1) else 1
+        n = C.dim.x * C.dim.y * C.dim.z * gates * nsrc * ndetblk
         f = np.ctypeslib.as_array(C.exportfield, shape=(n,)).copy()
         if nsrc > 1:
-            dims = (C.dim.x, C.dim.y, C.dim.z, gates, 1, nsrc)
+            dims = (C.dim.x, C.dim.y, C.dim.z, gates, ndetblk, nsrc)
+        elif ndetblk > 1:
+            dims = (C.dim.x, C.dim.y, C.dim.z, gates, ndetblk)
         else:
             dims = (C.dim.x, C.dim.y, C.dim.z, gates)
         flux = f.reshape(dims, order="F")

@@ -49,7 +49,7 @@
 #define CONE_DRAW_CAP      (1u << 16)  /* guard against a cone of zero half-angle */
 
 enum { bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic };
-enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL };
+enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF };
 enum { S_PENCIL, S_ISOTROPIC, S_CONE, S_GAUSSIAN, S_PLANAR, S_PATTERN, S_FOURIER, S_ARCSINE,
        S_DISK, S_FOURIERX, S_FOURIERX2D, S_ZGAUSSIAN, S_LINE, S_SLIT, S_PENCILARRAY, S_PATTERN3D,
        S_HYPERBOLOID, S_RING };
@@ -89,6 +89,13 @@ typedef struct {
     const float* angleinvcdf;     /* nangle entries */
     int mathmode, variant, fieldmode;
     unsigned int nthread;
+    /* replay */
+    int replay, replaydet;
+    unsigned int nreplay;
+    const uint64_t* rseed;
+    const float* rweight;
+    const float* rtof;
+    const int* rdetid;
 } ocfg;
 
 typedef struct {
@@ -167,8 +174,37 @@ static inline void field_add(octx* X, size_t i, float w) {
             X->ff[i + c->dimlen[3]] += ((old > 0.f) ? K_MAX_ACCUM : -K_MAX_ACCUM);
         }
     } else {
-        X->fd[i] += (double)w;
+        X->fd[i >= c->dimlen[3] ? i - c->dimlen[3] : i] += (double)w;
     }
+}
+
+/* the scattering-site deposit of the replay outputs moves a saturated value
+   whole into the shadow half (mcx_core.cl:2597-2604) */
+static inline void field_add_site(octx* X, size_t i, float w) {
+    const ocfg* c = X->c;
+    if (c->fieldmode == MCXO_FIELD_FLOAT_SPILL) {
+        float old = X->ff[i];
+        X->ff[i] = old + w;
+        if (fabsf(old) > K_MAX_ACCUM) {
+            float r = X->ff[i];
+            X->ff[i] = r - old;
+            if (r < 0.f) {
+                X->ff[i] += old;
+            } else {
+                X->ff[i + c->dimlen[3]] += old;
+            }
+        }
+    } else {
+        X->fd[i >= c->dimlen[3] ? i - c->dimlen[3] : i] += (double)w;
+    }
+}
+
+/* index of the photon a replay quantity is read for: the reference's
+   idx*threadphoton + min(idx, oddphoton-1) + offset (mcx_core.cl:1591, 2571, 2847) */
+static inline long long replay_index(const ocfg* c, unsigned int tid, long long offset) {
+    long long m = (long long)c->oddphoton - 1;
+    long long t = (long long)tid;
+    return t * (long long)c->threadphoton + (t < m ? t : m) + offset;
 }
 
 /* updateproperty, mcx_core.cl:1079-1096 (label and MEDIA_MUA_FLOAT formats) */
@@ -488,6 +524,17 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
         return 1;
     }
 
+    if (c->replay) {
+        /* the saved launch state of this photon, mcx_core.cl:1590-1596 */
+        long long k = replay_index(c, X->tid, (long long)((int)s->f.w > 0 ? (int)s->f.w : 0));
+        if (k < 0 || k >= (long long)c->nreplay) {
+            X->nfailed++;
+            return 1;
+        }
+        s->t[0] = c->rseed[2 * k];
+        s->t[1] = c->rseed[2 * k + 1];
+    }
+
     if (c->issaveseed) {
         s->photonseed[0] = s->t[0];
         s->photonseed[1] = s->t[1];
@@ -503,6 +550,11 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
                 ls = extra + ((int)(s->ppath[c->w0offset - 1] - 2));
             }
         }
+    }
+
+    if (c->replay && c->srcid >= 1) {
+        /* keeps the stream in step with a run that picked a source, 1614-1616 */
+        rng_next(s->t);
     }
 
     pp = s->ppath + c->partialdata;
@@ -964,6 +1016,28 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                     rotatevector(c, &s.v, stheta, ctheta, sphi, cphi);
                 }
                 s.v.w += 1.f;
+                if (c->replay && (c->outputtype == otWP || c->outputtype == otDCS || c->outputtype == otWPTOF)) {
+                    /* replay deposit at the scattering site, mcx_core.cl:2567-2604; the
+                       reference indexes these with the launch counter itself (no -1) */
+                    long long k = replay_index(c, tid, (long long)(int)s.f.w);
+                    if (k >= 0 && k < (long long)c->nreplay) {
+                        int tshift;
+                        tmp0 = (c->outputtype == otDCS) ? (1.f - ctheta) : 1.f;
+                        if (c->outputtype == otWPTOF) {
+                            tmp0 = c->rtof[k];
+                            tmp0 *= c->rweight[k];
+                        } else {
+                            tmp0 *= c->rweight[k];
+                        }
+                        tshift = (int)(floorf((c->rtof[k] - c->twin0) * c->Rtstep)) +
+                                 ((c->replaydet == -1) ? (((c->rdetid[k] & 0xFFFF) - 1) * (int)c->maxgate) : 0);
+                        if (c->extrasrclen && (c->srcid < 0)) {
+                            tshift += ((int)s.ppath[c->w0offset - 1] - 1) * ((c->replaydet == -1) ? (int)c->detnum : 1) * (int)c->maxgate;
+                        }
+                        tshift = ((int)c->maxgate - 1 < tshift) ? (int)c->maxgate - 1 : tshift;
+                        field_add_site(X, (size_t)s.idx1d + (size_t)(long long)tshift * c->dimlen[2], tmp0);
+                    }
+                }
             }
             s.v.w = (float)(int)s.v.w;
         }
@@ -1023,14 +1097,30 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                     weight = s.w0 - s.p.w;
                 } else if (c->outputtype == otFluence || c->outputtype == otFlux) {
                     weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen) : ((s.w0 - s.p.w) / (s.prop.x));
+                } else if (c->replay) {
+                    /* replay Jacobian deposit, mcx_core.cl:2845-2858: the detected
+                       weight times the path length in the voxel, in the gate of the
+                       photon's detected time of flight */
+                    if (c->outputtype == otJacobian || c->outputtype == otWLTOF) {
+                        long long k = replay_index(c, tid, (long long)(int)s.f.w - 1);
+                        if (k >= 0 && k < (long long)c->nreplay) {
+                            weight = c->rweight[k] * s.pathlen;
+                            tshift = (int)(floorf((c->rtof[k] - c->twin0) * c->Rtstep)) +
+                                     ((c->replaydet == -1) ? (((c->rdetid[k] & 0xFFFF) - 1) * (int)c->maxgate) : 0);
+                            if (c->outputtype == otWLTOF) {
+                                weight = weight * c->rtof[k];
+                            }
+                        }
+                    }
                 } else if (c->outputtype == otL) {
                     weight = s.w0 * s.pathlen;
                 }
                 if (c->extrasrclen && (c->srcid < 0)) {
-                    tshift += ((int)s.ppath[c->w0offset - 1] - 1) * (int)c->maxgate;
+                    tshift += ((int)s.ppath[c->w0offset - 1] - 1) * ((c->replay && c->replaydet == -1) ? (int)c->detnum : 1) *
+                              (int)c->maxgate;
                 }
                 if (fabsf(weight) > 0.f) {
-                    field_add(X, (size_t)idx1dold + (size_t)tshift * c->dimlen[2], weight);
+                    field_add(X, (size_t)idx1dold + (size_t)(long long)tshift * c->dimlen[2], weight);
                 }
             }
             s.w0 = s.p.w;
@@ -1229,6 +1319,10 @@ static unsigned int gates_of(const mcxo_input* in) {
     return (unsigned int)(int)((in->tend - in->tstart) / in->tstep + 0.5);
 }
 
+static int is_replay(const mcxo_input* in) {
+    return in->seed == MCXO_SEED_FROM_FILE;
+}
+
 static unsigned int savedetflag_eff(const mcxo_input* in) {
     /* mcx_preprocess, mcx_utils.c:1631-1638, 1763-1791 */
     unsigned int f = in->savedetflag;
@@ -1243,7 +1337,8 @@ static unsigned int savedetflag_eff(const mcxo_input* in) {
         issavedet = 0;
     }
     if (!issavedet) {
-        return 0;
+        /* a replay keeps the flags that describe its input records, mcx_utils.c:1619-1625 */
+        return (is_replay(in) ? (f & ~0x80u) : 0u) & ((in->mediabyte >= 100) ? ~(0x2u | 0x4u | 0x8u) : ~0u);
     }
     if (in->ismomentum) {
         f |= 0x8;
@@ -1282,6 +1377,9 @@ unsigned int mcxo_reclen(const mcxo_input* in) {
 
 unsigned int mcxo_fieldlen(const mcxo_input* in) {
     unsigned int mult = (in->extrasrclen && in->srcid < 0) ? (in->extrasrclen + 1) : 1;
+    if (is_replay(in) && in->replaydet == -1) {
+        mult *= in->detnum;    /* one block of gates per detector, mcx_host.cpp:684-687 */
+    }
     return in->dimx * in->dimy * in->dimz * gates_of(in) * mult;
 }
 
@@ -1491,6 +1589,22 @@ static int prepare(const mcxo_input* in, oprep* P) {
     c.variant = in->variant;
     c.fieldmode = in->fieldmode;
     c.nthread = in->nthread;
+    if (is_replay(in)) {
+        if (!in->replayseed || !in->replayweight || !in->replaytof || !in->replaydetid ||
+                (double)in->nreplay != in->nphoton) {
+            free(gprop);
+            free(gdet);
+            free(media);
+            return -5;
+        }
+        c.replay = 1;
+        c.replaydet = in->replaydet;
+        c.nreplay = in->nreplay;
+        c.rseed = in->replayseed;
+        c.rweight = in->replayweight;
+        c.rtof = in->replaytof;
+        c.rdetid = in->replaydetid;
+    }
     {
         unsigned int is2d = (in->dimx == 1 ? 1 : (in->dimy == 1 ? 2 : (in->dimz == 1 ? 3 : 0)));
         if (is2d) {
@@ -1748,6 +1862,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
     {
         double etot = 0.0, eesc = 0.0;
         float scale = 1.f;
+        float* blockscale = NULL;
         float Vvox = steps * steps * steps;
         for (i = 0; i < in->nthread; i++) {
             eesc += energy[i * 2];
@@ -1764,6 +1879,27 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
                 }
             } else if (in->outputtype == otEnergy || in->outputtype == otL) {
                 scale = (float)(1.0 / etot);
+            } else if (c.replay && (in->outputtype == otJacobian || in->outputtype == otWP || in->outputtype == otDCS ||
+                                    in->outputtype == otWLTOF || in->outputtype == otWPTOF)) {
+                /* replay outputs, mcx_host.cpp:1396-1431: unitinmm over the replayed
+                   detected weight, per detector when each has its own block */
+                unsigned int d, nd = (c.replaydet == -1) ? c.detnum : 1;
+                for (d = 1; d <= nd; d++) {
+                    float sw = 0.f;
+                    unsigned int k;
+                    for (k = 0; k < c.nreplay; k++) {
+                        if (nd == 1 || (c.rdetid[k] & 0xFFFF) == (int)d) {
+                            sw += c.rweight[k];
+                        }
+                    }
+                    scale = (sw > 0.f) ? in->unitinmm / sw : 0.f;
+                    if (nd > 1) {
+                        if (!blockscale) {
+                            blockscale = (float*)calloc(nd, sizeof(float));
+                        }
+                        blockscale[d - 1] = scale;
+                    }
+                }
             }
             if (in->extrasrclen && in->srcid < 0) {
                 scale *= (float)(in->extrasrclen + 1);
@@ -1784,9 +1920,11 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
                 field_out[i] = raw;
             }
             if (fieldnorm) {
-                fieldnorm[i] = in->isnormalized ? merged * scale : merged;
+                float sc = blockscale ? blockscale[i / (fieldlen / c.detnum)] : scale;
+                fieldnorm[i] = in->isnormalized ? merged * sc : merged;
             }
         }
+        free(blockscale);
     }
     stats.detected = total_det;
     stats.saved = saved;
@@ -1814,6 +1952,52 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
     free(media);
     (void)nworkers;
     return 0;
+}
+
+int mcxo_replayinit(const mcxo_input* in, const float* detp, unsigned int reclen, unsigned int ndet,
+                    const uint64_t* seeds, uint64_t* seed_out, float* weight, float* tof, int* detid) {
+    /* mcx_replayinit, mcx_utils.c:1355-1421, after mcx_preprocess has fixed
+       savedetflag and scaled mua by unitinmm */
+    unsigned int f = savedetflag_eff(in);
+    int hasdetid = SAVE_DETID(f);
+    unsigned int offset = SAVE_NSCAT(f) * (in->medianum - 1);
+    unsigned int i, j, n = 0;
+    if (!detp || !seeds || reclen == 0) {
+        return -6;
+    }
+    if (((!hasdetid) && in->detnum > 1) || !SAVE_PPATH(f)) {
+        return -7;      /* the baseline run must save detector ids and partial paths ('dp') */
+    }
+    for (i = 0; i < ndet; i++) {
+        const float* rec = detp + (size_t)i * reclen;
+        int did = (int)rec[0];
+        if (!(in->replaydet <= 0 || in->replaydet == (did & 0xFFFF))) {
+            continue;
+        }
+        if (!(in->srcid <= 0 || ((did & 0xFFFF0000) && in->srcid == ((did & 0xFFFF0000) >> 16)))) {
+            continue;
+        }
+        seed_out[2 * n] = seeds[2 * (size_t)i];
+        seed_out[2 * n + 1] = seeds[2 * (size_t)i + 1];
+        weight[n] = 1.f;
+        tof[n] = 0.f;
+        detid[n] = hasdetid ? did : 1;
+        for (j = (unsigned int)hasdetid; j < in->medianum - 1 + (unsigned int)hasdetid; j++) {
+            float mua = in->prop[(j - hasdetid + 1) * 4];
+            float plen = rec[offset + j];
+            if (in->unitinmm != 1.f) {
+                mua *= in->unitinmm;
+            }
+            weight[n] *= expf(-mua * plen);
+            plen *= in->unitinmm;
+            tof[n] += plen * K_R_C0 * in->prop[(j - hasdetid + 1) * 4 + 3];
+        }
+        if (tof[n] < in->tstart || tof[n] > in->tend) {
+            continue;
+        }
+        n++;
+    }
+    return (int)n;
 }
 
 /* Prepared inputs for the reference-kernel harness (oracle/ref_harness.cpp). */

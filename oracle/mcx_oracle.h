@@ -40,6 +40,8 @@ extern "C" {
 #define MCXO_FIELD_FLOAT_SPILL 0 /* float atomics with the +-1000 spill half, as mcx_core.cl:2880-2886 */
 #define MCXO_FIELD_DOUBLE      1 /* FP64 accumulation of the same deposits */
 
+#define MCXO_SEED_FROM_FILE  (-999) /* seed value that selects replay, mcx_core.cl:503-505 */
+
 typedef struct mcxo_input {
     /* domain: vol holds one 32-bit word per voxel, x fastest (the layout
        mcx_preprocess leaves in cfg->vol); labels for mediabyte 1/2/4, float
@@ -82,7 +84,7 @@ typedef struct mcxo_input {
     int voidtime;
     int isspecular;
     int maxvoidstep;
-    int outputtype;             /* 0 flux, 1 fluence, 2 energy, 7 length */
+    int outputtype;             /* 0 flux, 1 fluence, 2 energy, 3 jacobian, 4 wp, 5 dcs, 7 length, 9 wltof, 10 wptof */
     int isnormalized;
     int issrcfrom0;
     const float* invcdf;
@@ -102,6 +104,16 @@ typedef struct mcxo_input {
     int variant;
     int fieldmode;
     int nworkers;               /* OpenMP workers (0 = library default); FLOAT_SPILL always runs serially */
+
+    /* replay (the reference's seed = SEED_FROM_FILE): each photon is launched
+       from a saved xorshift128+ state; nphoton must equal nreplay.  The
+       per-photon arrays come from mcxo_replayinit. */
+    const uint64_t* replayseed; /* nreplay x 2 words */
+    const float* replayweight;  /* nreplay */
+    const float* replaytof;     /* nreplay, seconds */
+    const int* replaydetid;     /* nreplay */
+    unsigned int nreplay;
+    int replaydet;              /* 0 all detectors into one field, -1 one field per detector, k detector k */
 } mcxo_input;
 
 typedef struct mcxo_stats {
@@ -117,6 +129,16 @@ typedef struct mcxo_stats {
 } mcxo_stats;
 
 /* Size queries so the caller can allocate outputs. */
+/*
+ * mcx_replayinit (mcx_utils.c:1355-1421): select the detected photons to
+ * replay and compute each one's detected weight and time of flight from its
+ * record.  detp: ndet records of reclen floats (host layout); seeds: ndet x 2
+ * words.  Writes up to ndet entries of seed_out/weight/tof/detid and returns
+ * the number kept, or a negative error code.
+ */
+int mcxo_replayinit(const mcxo_input* in, const float* detp, unsigned int reclen, unsigned int ndet,
+                    const uint64_t* seeds, uint64_t* seed_out, float* weight, float* tof, int* detid);
+
 unsigned int mcxo_reclen(const mcxo_input* in);
 unsigned int mcxo_fieldlen(const mcxo_input* in);
 

@@ -27,7 +27,11 @@ FIELD_FLOAT_SPILL, FIELD_DOUBLE = 0, 1
 SRCTYPES = ["pencil", "isotropic", "cone", "gaussian", "planar", "pattern", "fourier", "arcsine", "disk",
             "fourierx", "fourierx2d", "zgaussian", "line", "slit", "pencilarray", "pattern3d", "hyperboloid",
             "ring"]
-OUTPUTTYPES = {"flux": 0, "fluence": 1, "energy": 2, "length": 7}
+# pmcxcl's outputtype names (src/pmcxcl.cpp:854-872): from "wl" on the index drops by two
+_OT_NAMES = ["flux", "fluence", "energy", "jacobian", "nscat", "wl", "wp", "wm", "rf", "length", "rfmus", "wltof",
+             "wptof"]
+OUTPUTTYPES = {n: (i - 2 if i >= 5 else i) for i, n in enumerate(_OT_NAMES)}
+SEED_FROM_FILE = -999
 SAVEFLAGS = "DSPMXVWI"
 
 
@@ -53,6 +57,8 @@ class MCXOInput(ctypes.Structure):
         ("seed", ctypes.c_int), ("debugrng", ctypes.c_int),
         ("mathmode", ctypes.c_int), ("variant", ctypes.c_int), ("fieldmode", ctypes.c_int),
         ("nworkers", ctypes.c_int),
+        ("replayseed", ctypes.c_void_p), ("replayweight", ctypes.c_void_p), ("replaytof", ctypes.c_void_p),
+        ("replaydetid", ctypes.c_void_p), ("nreplay", ctypes.c_uint), ("replaydet", ctypes.c_int),
     ]
 
 
@@ -94,6 +100,7 @@ def lib():
         _lib.mcxo_pm_expf.argtypes = [ctypes.c_float]
         _lib.mcxo_pm_acosf.restype = ctypes.c_float
         _lib.mcxo_pm_acosf.argtypes = [ctypes.c_float]
+        _lib.mcxo_replayinit.restype = ctypes.c_int
     return _lib
 
 
@@ -225,16 +232,51 @@ def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT
         keep["angleinvcdf"] = acdf
         inp.angleinvcdf = _ptr(acdf)
         inp.nangle = acdf.size
-    inp.nphoton = float(cfg["nphoton"])
+    inp.nphoton = float(cfg.get("nphoton", 0))
     inp.nthread = int(nthread)
     inp.core = int(core if core is not None else nthread)
-    inp.seed = int(cfg.get("seed", 0x623F9A9E))
     inp.debugrng = int("R" in str(cfg.get("debuglevel", "")).upper())
     inp.mathmode = mathmode
     inp.variant = variant
     inp.fieldmode = fieldmode
     inp.nworkers = nworkers
+    seed = cfg.get("seed", 0x623F9A9E)
+    if isinstance(seed, np.ndarray) and seed.ndim == 2:
+        _replay_input(inp, keep, cfg, seed)
+    else:
+        inp.seed = int(seed)
     return inp, keep
+
+
+def _replay_input(inp, keep, cfg, seed):
+    """Replay: cfg['seed'] is the uint8 [16, N] seed array and
+    cfg['detphotons'] the float32 [reclen, N] records of a previous run
+    (src/pmcxcl.cpp:1006-1047); mcxo_replayinit picks and weights them."""
+    s8 = np.asarray(seed, np.uint8)
+    if s8.shape[0] != 16:
+        raise ValueError("the row number of cfg.seed does not match RNG seed byte-length")
+    n = s8.shape[1]
+    seeds = np.ascontiguousarray(s8.T).view(np.uint64).reshape(n, 2).copy()
+    detp = np.asarray(cfg["detphotons"], np.float32)
+    if detp.ndim != 2 or detp.shape[1] != n:
+        raise ValueError("the column numbers of detphotons and seed do not match")
+    recs = np.ascontiguousarray(detp.T)
+    inp.seed = SEED_FROM_FILE
+    inp.replaydet = int(cfg.get("replaydet", 0))
+    out_seed = np.zeros((max(n, 1), 2), np.uint64)
+    w = np.zeros(max(n, 1), np.float32)
+    tof = np.zeros(max(n, 1), np.float32)
+    did = np.zeros(max(n, 1), np.int32)
+    k = lib().mcxo_replayinit(ctypes.byref(inp), _ptr(recs), ctypes.c_uint(recs.shape[1]), ctypes.c_uint(n),
+                              _ptr(seeds), _ptr(out_seed), _ptr(w), _ptr(tof), _ptr(did))
+    if k < 0:
+        raise ValueError("replay initialisation failed with code %d" % k)
+    for name, a in (("rseed", out_seed), ("rw", w), ("rtof", tof), ("rdid", did)):
+        keep[name] = a
+    inp.replayseed, inp.replayweight = _ptr(out_seed), _ptr(w)
+    inp.replaytof, inp.replaydetid = _ptr(tof), _ptr(did)
+    inp.nreplay = k
+    inp.nphoton = float(k)
 
 
 def run(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL, fieldmode=FIELD_DOUBLE,
@@ -271,6 +313,10 @@ def run(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL
         "stat": {k: getattr(st, k) for k, _ in MCXOStats._fields_},
         "gates": gates,
     }
+    if inp.seed == SEED_FROM_FILE:
+        n = inp.nreplay
+        out["replay"] = {"weight": keep["rw"][:n].copy(), "tof": keep["rtof"][:n].copy(),
+                         "detid": keep["rdid"][:n].copy(), "seed": keep["rseed"][:n].copy()}
     return out
 
 

@@ -15,13 +15,21 @@
 
 #include "mcx_oracle.h"
 
+#include <algorithm>
 #include <vector>
+
+struct ReplayBufs {
+    float* weight = nullptr;
+    float* tof = nullptr;
+    int* detid = nullptr;
+};
 
 template <int ispencil, int isreflect>
 static void run_blocks(const mcxo_refprep& R, unsigned int nblock, unsigned int bsize, unsigned int* media,
                        float* field, float* genergy, unsigned int* seeds, float* detp, unsigned int* detcount,
                        float* gprop, float* gdet, RandType* gseed, float* srcpattern, const float* invcdf,
-                       unsigned int nphase, const float* angleinvcdf, unsigned int nangle, int nworkers) {
+                       unsigned int nphase, const float* angleinvcdf, unsigned int nangle, int nworkers,
+                       const ReplayBufs& rp) {
     (void)nworkers;
     for (long b = 0; b < (long)nblock; b++) {
         unsigned int progress = 0;
@@ -41,7 +49,7 @@ static void run_blocks(const mcxo_refprep& R, unsigned int nblock, unsigned int 
             threadIdx = make_uint3(t, 0, 0);
             mcx_main_loop<ispencil, isreflect, 1, 0, 0>(
                 media, field, genergy, seeds, detp, (const float4*)gprop, srcpattern, (const float4*)gdet,
-                &progress, detcount, nullptr, nullptr, nullptr, gseed, nullptr, nullptr, (float*)invcdf, (float*)angleinvcdf,
+                &progress, detcount, rp.weight, rp.tof, rp.detid, gseed, nullptr, nullptr, (float*)invcdf, (float*)angleinvcdf,
                 (RandType*)sharedmem_raw, nullptr);
         }
     }
@@ -94,6 +102,7 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     P.isspecular = R.isspecular;
     P.maxgate = R.maxgate;
     P.seed = in->seed;
+    P.replaydet = in->replaydet;
     P.outputtype = R.outputtype;
     P.threadphoton = R.threadphoton;
     P.oddphoton = R.oddphoton;
@@ -119,6 +128,28 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     std::vector<float> field(2 * (size_t)R.fieldlen, 0.f);
     std::vector<float> genergy(2 * (size_t)in->nthread, 0.f);
     std::vector<unsigned int> seeds(R.seedwords, R.seedwords + 4 * (size_t)in->nthread);
+    /* replay: the seed buffer holds one saved state per photon (the kernel
+       also reads a start state per thread from it, which the launch then
+       overwrites); one zero-weight photon pads the per-photon arrays, which
+       the reference's scattering-site deposits read one photon ahead */
+    const bool replay = (in->seed == MCXO_SEED_FROM_FILE);
+    ReplayBufs rp;
+    std::vector<float> rweight, rtof;
+    std::vector<int> rdetid;
+    if (replay) {
+        size_t nw = std::max((size_t)in->nreplay * 4 + 8, (size_t)in->nthread * 4 + 8);
+        seeds.assign(nw, 0u);
+        std::memcpy(seeds.data(), in->replayseed, sizeof(uint64_t) * 2 * in->nreplay);
+        rweight.assign(in->nreplay + 1, 0.f);
+        rtof.assign(in->nreplay + 1, in->tstart);
+        rdetid.assign(in->nreplay + 1, 1);
+        std::memcpy(rweight.data(), in->replayweight, sizeof(float) * in->nreplay);
+        std::memcpy(rtof.data(), in->replaytof, sizeof(float) * in->nreplay);
+        std::memcpy(rdetid.data(), in->replaydetid, sizeof(int) * in->nreplay);
+        rp.weight = rweight.data();
+        rp.tof = rtof.data();
+        rp.detid = rdetid.data();
+    }
     size_t reclen = R.reclen ? R.reclen : 1;
     std::vector<float> detp((size_t)R.maxdetphoton * reclen + 1, 0.f);
     std::vector<RandType> gseed((size_t)R.maxdetphoton * 2 + 2, 0);
@@ -133,7 +164,7 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     int isreflect = R.dorefl_compiled;
 #define RUN(a, b) run_blocks<a, b>(R, nblock, nblocksize, media.data(), field.data(), genergy.data(), seeds.data(), \
                                    detp.data(), &detcount, gprop.data(), gdet.data(), gseed.data(), (float*)in->srcpattern, \
-                                   in->invcdf, in->nphase, in->angleinvcdf, in->nangle, nworkers)
+                                   in->invcdf, in->nphase, in->angleinvcdf, in->nangle, nworkers, rp)
     if (ispencil && isreflect) {
         RUN(1, 1);
     } else if (ispencil) {

@@ -130,3 +130,29 @@ def pin_cases():
     for k in VARIANTS:
         out.append((k, variant(k), 128))
     return out
+
+
+def replay_cfg(base, detp, seeds, **kw):
+    """A replay of base's detected photons: detp [reclen, N] records and
+    seeds [N, 2] uint64 (or [16, N] uint8) from a baseline run."""
+    s = np.asarray(seeds)
+    if s.dtype != np.uint8:
+        s = np.ascontiguousarray(s, dtype=np.uint64).view(np.uint8).reshape(-1, 16).T
+    cfg = dict(base, seed=np.asfortranarray(s), detphotons=np.asarray(detp, np.float32))
+    cfg.pop("nphoton", None)
+    cfg.update(kw)
+    return cfg
+
+
+# (name, baseline, replay keys, reference threads) -- replays pinned against the reference kernel
+REPLAY_PINS = [
+    ("replay_jacobian", dict(nphoton=3000), dict(outputtype="jacobian"), 128),
+    ("replay_jacobian_perdet", dict(nphoton=3000), dict(outputtype="jacobian", replaydet=-1), 128),
+    ("replay_jacobian_det1", dict(nphoton=3000), dict(outputtype="jacobian", replaydet=1), 128),
+    ("replay_jacobian_fewthreads", dict(nphoton=3000), dict(outputtype="jacobian"), 16),
+    ("replay_nscat", dict(nphoton=3000), dict(outputtype="nscat"), 128),
+    ("replay_wm_perdet", dict(nphoton=3000), dict(outputtype="wm", replaydet=-1), 128),
+    ("replay_wltof", dict(nphoton=3000), dict(outputtype="wltof"), 128),
+    ("replay_wptof", dict(nphoton=3000), dict(outputtype="wptof"), 16),
+    ("replay_flux", dict(nphoton=3000), dict(outputtype="flux"), 128),
+]

@@ -2,7 +2,9 @@
 
 Builds oracle/_ref/libmcxref.so from the reference sources (src/mcx_core.cl
 compiled as host C++ in place, see oracle/Makefile), runs every case of
-tests/cases.py:pin_cases() one reference thread at a time, and records
+tests/cases.py:pin_cases() and the photon replays of REPLAY_PINS (each
+replaying the reference's own baseline records) one reference thread at a
+time, and records
 SHA-256 digests of the raw output bits (per-thread energies, merged fluence
 field, detected-photon records, saved seeds) plus a few readable values.
 tests/test_oracle_pins.py recomputes the same digests with the oracle.
@@ -60,6 +62,13 @@ def main():
         r = oracle.run_reference(cfg, nthread=nthread, core=nthread)
         out[name] = dict(summarize(r), nthread=nthread)
         print(name, out[name]["ndet"], out[name]["energy_tot"])
+    for name, bkw, rkw, nthread in cases.REPLAY_PINS:
+        base = cases.small_two_media(**bkw)
+        b = oracle.run_reference(base, nthread=128, core=128)
+        cfg = cases.replay_cfg(base, b["detp"], b["seeds"], **rkw)
+        r = oracle.run_reference(cfg, nthread=nthread, core=nthread, nblocksize=16)
+        out[name] = dict(summarize(r), nthread=nthread)
+        print(name, out[name]["ndet"], out[name]["field_sum"])
     with open(os.path.join(HERE, "ref_pins.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
 
