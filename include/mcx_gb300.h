@@ -185,6 +185,10 @@ typedef struct MCXConfig {
     float* exportenergy;          /* when savethreadenergy: 2 x threadused {escaped, launched} floats */
     int savethreadenergy;
     int autotune;                 /* 1: time the launch shapes on a photon sample, once per problem shape, keep the fastest */
+    int savedetweight;            /* 1: fill exportdetweight */
+    float* exportdetweight;       /* 2 x detectedcount: weight and time of flight (s) of each saved photon when detected */
+    int replaysiteown;            /* replay: 1 = scattering-site outputs use the replayed photon's own weight and time
+                                     (the reference reads the next photon's, mcx_core.cl:2571) */
     int errorcode;                /* last error in library mode */
     char errormsg[256];
 } Config;
@@ -312,6 +316,9 @@ int  mcxg_get_field(mcxg_session* s, float* out, double scale);
 int  mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uint32_t nblocks);
 /* Field: (hi + lo) in FP64, unscaled. */
 int  mcxg_get_field_f64(mcxg_session* s, double* out);
+/* Weight and time of flight (s) of each saved detected photon when it was
+   detected, 2 floats per record, in record order. */
+int  mcxg_get_detweight(mcxg_session* s, float* out);
 /* Detected photons: up to maxdetphoton records (reclen floats) and seeds
    (2 x uint64 each, when enabled); *detected = all detections, including
    those beyond the buffer. */

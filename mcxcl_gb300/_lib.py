@@ -86,7 +86,9 @@ class Config(ctypes.Structure):
         ("exactmath", ctypes.c_int), ("kernelms", ctypes.c_float),
         ("eventcount", ctypes.c_uint64 * 5), ("failedlaunch", ctypes.c_uint), ("threadused", ctypes.c_uint),
         ("exportenergy", ctypes.POINTER(ctypes.c_float)), ("savethreadenergy", ctypes.c_int),
-        ("autotune", ctypes.c_int), ("errorcode", ctypes.c_int),
+        ("autotune", ctypes.c_int), ("savedetweight", ctypes.c_int),
+        ("exportdetweight", ctypes.POINTER(ctypes.c_float)), ("replaysiteown", ctypes.c_int),
+        ("errorcode", ctypes.c_int),
         ("errormsg", ctypes.c_char * 256),
     ]
 
@@ -107,7 +109,7 @@ EXPORTS = [
     "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_launch", "mcxg_simulate",
     "mcxg_get_energy", "mcxg_get_thread_energy", "mcxg_get_field", "mcxg_get_field_f64", "mcxg_get_detected",
     "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc", "mcxg_autotune",
-    "mcxg_set_replay", "mcxg_get_field_blocks",
+    "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_detweight",
 ]
 
 _lib = None

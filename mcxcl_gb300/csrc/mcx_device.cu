@@ -55,6 +55,8 @@ struct mcxg_session {
     size_t detp_cap = 0;             /* floats */
     unsigned long long* d_detseed = nullptr;
     size_t detseed_cap = 0;
+    float2* d_detw = nullptr;
+    size_t detw_cap = 0;
     unsigned int* d_words = nullptr; /* detcount, vtcounter, status[2] */
     unsigned long long* d_events = nullptr;
     double* d_red = nullptr;         /* reduction partials + result */
@@ -324,7 +326,7 @@ int mcxg_destroy(mcxg_session* s) {
     }
     void* bufs[] = {s->d_media, s->d_prop, s->d_tables, s->d_pattern, s->d_seeds, s->d_field, s->d_energy,
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
-                    s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales};
+                    s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw};
     for (void* b : bufs) {
         if (b) {
             cudaFree(b);
@@ -389,6 +391,9 @@ int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, 
         rc = ensure(&s->d_detp, &s->detp_cap, recs * (kp.reclen ? kp.reclen : 1));
         if (!rc && kp.issaveseed) {
             rc = ensure(&s->d_detseed, &s->detseed_cap, recs * 2 + 2);
+        }
+        if (!rc) {
+            rc = ensure(&s->d_detw, &s->detw_cap, recs + 1);
         }
     }
     if (rc) {
@@ -533,6 +538,7 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     a.energy = s->d_energy;
     a.detp = s->d_detp;
     a.detseed = s->d_detseed;
+    a.detw = kp.savedet ? s->d_detw : nullptr;
     a.detcount = s->d_words + 0;
     a.vtcounter = s->d_words + 1;
     a.status = s->d_words + 2;
@@ -768,6 +774,25 @@ int mcxg_get_detected(mcxg_session* s, float* detp, uint64_t* seeds, uint32_t* d
         MCXG_TRY(cudaMemcpyAsync(seeds, s->d_detseed, sizeof(uint64_t) * 2 * saved, cudaMemcpyDeviceToHost, s->st));
     }
     MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_get_detweight(mcxg_session* s, float* out) {
+    if (!s || !out || !s->has_problem) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    unsigned int cnt = 0;
+    MCXG_TRY(cudaMemcpyAsync(&cnt, s->d_words, sizeof(cnt), cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    if (!s->kp.savedet) {
+        return MCXG_OK;
+    }
+    size_t saved = cnt < s->kp.maxdetphoton ? cnt : s->kp.maxdetphoton;
+    if (saved) {
+        MCXG_TRY(cudaMemcpyAsync(out, s->d_detw, sizeof(float2) * saved, cudaMemcpyDeviceToHost, s->st));
+        MCXG_TRY(cudaStreamSynchronize(s->st));
+    }
     return MCXG_OK;
 }
 

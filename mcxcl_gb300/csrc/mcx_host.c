@@ -137,6 +137,8 @@ void mcx_clearcfg(Config* cfg) {
     free(cfg->angleinvcdf);
     free(cfg->srcdata);
     free(cfg->exportenergy);
+    free(cfg->exportdetweight);
+    cfg->exportdetweight = NULL;
     free(cfg->replay.seed);
     free(cfg->replay.weight);
     free(cfg->replay.tof);
@@ -408,7 +410,7 @@ static void preprocess(Config* cfg) {
             point_src_voxel(cfg, cfg->srcdata[i].srcpos, &cfg->srcdata[i].srcparam2);
         }
     }
-    if (cfg->issavedet && cfg->mediabyte <= 4) {
+    if (cfg->issavedet) {
         maskdet(cfg);
     }
     for (int i = 0; i < MAX_DEVICE; i++) {
@@ -442,6 +444,22 @@ static void preprocess(Config* cfg) {
    weight and time of flight from its partial paths, drop those outside the
    time window, and compact the seeds to match. */
 static void replayinit(Config* cfg, const float* detps, const int dimdetps[2], int seedbyte) {
+    if (cfg->seed == SEED_FROM_FILE && detps == NULL && cfg->replay.seed && cfg->replay.weight && cfg->replay.tof &&
+            cfg->replay.detid) {
+        /* the caller gave each photon's weight, time of flight and detector id
+           directly (replays of float-mua volumes, whose records carry no
+           partial paths, and gradient replays with per-photon factors) */
+        for (size_t i = 0; i < cfg->nphoton; i++) {
+            int d = cfg->replay.detid[i] & 0xFFFF;
+            if (cfg->replaydet == -1 && (d < 1 || d > (int)cfg->detnum)) {
+                MCX_ERROR(-6, "a replayed record carries a detector id outside 1..detnum");
+            }
+            if (cfg->replay.tof[i] < cfg->tstart || cfg->replay.tof[i] > cfg->tend) {
+                MCX_ERROR(-6, "a replayed photon's time of flight lies outside the time window");
+            }
+        }
+        return;
+    }
     if (cfg->seed == SEED_FROM_FILE && detps == NULL) {
         MCX_ERROR(-6, "you give cfg.seed for replay, but did not specify cfg.detphotons.\nPlease define it as the "
                   "detphoton output from the baseline simulation\n");
@@ -878,7 +896,7 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
         kp.replay = 1;
         kp.nreplay = (uint32_t)cfg->nphoton;
         kp.replaydet = cfg->replaydet;
-        kp.siteshift = 1;
+        kp.siteshift = cfg->replaysiteown ? 0u : 1u;
     }
     for (int i = 0; i < 12; i++) {
         kp.bc[i] = (uint8_t)cfg->bc[i];
@@ -1029,6 +1047,15 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
                 cfg->exportdetected = nd;
                 memcpy(cfg->exportdetected + (size_t)cfg->detectedcount * hostdetreclen, detbuf,
                        sizeof(float) * saved * hostdetreclen);
+                if (cfg->savedetweight) {
+                    float* nw = (float*)realloc(cfg->exportdetweight, sizeof(float) * 2 * ((size_t)cfg->detectedcount + saved));
+                    if (!nw) {
+                        MCX_ERROR(-2, "out of host memory");
+                    }
+                    cfg->exportdetweight = nw;
+                    device_check(mcxg_get_detweight(s, cfg->exportdetweight + (size_t)cfg->detectedcount * 2),
+                                 "reading detected weights");
+                }
                 if (cfg->issaveseed) {
                     void* ns = realloc(cfg->seeddata, sizeof(uint64_t) * 2 * ((size_t)cfg->detectedcount + saved));
                     if (!ns) {
@@ -1204,7 +1231,8 @@ static const struct {
     MCX_FIELD(bc), MCX_FIELD(nphase), MCX_FIELD(invcdf), MCX_FIELD(nangle), MCX_FIELD(angleinvcdf), MCX_FIELD(srcid),
     MCX_FIELD(extrasrclen), MCX_FIELD(srcdata), MCX_FIELD(replay), MCX_FIELD(replaydet), MCX_FIELD(exactmath), MCX_FIELD(kernelms), MCX_FIELD(eventcount),
     MCX_FIELD(failedlaunch), MCX_FIELD(threadused), MCX_FIELD(exportenergy), MCX_FIELD(savethreadenergy),
-    MCX_FIELD(autotune), MCX_FIELD(errorcode), MCX_FIELD(errormsg),
+    MCX_FIELD(autotune), MCX_FIELD(savedetweight), MCX_FIELD(exportdetweight), MCX_FIELD(replaysiteown),
+    MCX_FIELD(errorcode), MCX_FIELD(errormsg),
 };
 
 size_t mcx_config_sizeof(void) {

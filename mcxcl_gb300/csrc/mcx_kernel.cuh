@@ -366,10 +366,13 @@ __device__ int skipvoid(const KArgs& a, const Shared& S, float4& p, float4& v, f
                     unsigned int m = media_at(a, idx1d);
                     float4 ht = make_float4(0.f, 0.f, 0.f, 0.f);
                     updateprop(S, ht, m);
+                    /* ht.w is the entry voxel's index of refraction; the reference reads
+                       gproperty[label].w, the same value for label volumes and an index past
+                       the table for float-mua volumes */
                     if (c_p.isspecular && ht.w != S.prop[0].w) {
-                        p.w *= 1.f - reflectcoeff<EXACT>(v, S.prop[0].w, S.prop[m & K_MED_MASK].w, fw);
+                        p.w *= 1.f - reflectcoeff<EXACT>(v, S.prop[0].w, ht.w, fw);
                         if (p.w > K_EPS) {
-                            transmit<EXACT>(v, S.prop[0].w, S.prop[m & K_MED_MASK].w, fw);
+                            transmit<EXACT>(v, S.prop[0].w, ht.w, fw);
                         }
                     }
                 }
@@ -440,6 +443,9 @@ __device__ void savedetphoton(const KArgs& a, const Shared& S, Photon& s, unsign
         }
         if (SAVE_W0(c_p.savedetflag)) {
             rec[k++] = s.w0init;
+        }
+        if (a.detw) {
+            a.detw[slot] = make_float2(s.p.w, s.f.y);
         }
     } else if (c_p.savedet == 3) {
         atomicSub(a.detcount, 1u);

@@ -25,6 +25,7 @@ struct KArgs {
     float2* energy;                /* per reference thread: escaped, launched weight */
     float* detp;                   /* maxdetphoton x reclen */
     unsigned long long* detseed;   /* maxdetphoton x 2 */
+    float2* detw;                  /* maxdetphoton x {weight, time of flight} when detected, or null */
     unsigned int* detcount;
     unsigned int* vtcounter;       /* work queue head */
     unsigned int* status;

@@ -1,0 +1,132 @@
+"""Differentiable detector readings: d(readings)/d(mua, mus) by photon replay.
+
+The forward pass runs the transport kernel on a per-voxel float mua volume
+(the reference's MEDIA_MUA_FLOAT format, src/mcx_core.cl:1093-1096) and
+records, for every detected photon, its detector, its launch RNG state and
+its weight when detected.  The reading of detector d is
+
+    R_d = (1/N) sum_{i detected by d} w_i,   w_i = exp(-sum_v mua_v u L_iv)
+
+(N launched photons, u the voxel size in mm, L_iv the path length of photon
+i in voxel v in voxels).  A photon's path does not depend on mua, so
+
+    dR_d/dmua_v = -(u/N) sum_{i in d} w_i L_iv
+
+and, by the likelihood ratio of the free-flight lengths and scattering
+events (path density ~ mus^n exp(-mus u L) per medium),
+
+    dR_d/dmus_v = (1/N) sum_{i in d} w_i (n_iv / mus_v - u L_iv).
+
+The backward pass replays only the detected photons from their saved
+states -- nothing but the seeds is stored, so memory is O(detected photons)
+-- with the per-photon factor a_i = (dLoss/dR_d(i)) w_i / N as the replay
+weight: the replay Jacobian output (mcx_core.cl:2845-2858) accumulates
+sum a_i L_iv per voxel and the scattering-count output (2567-2604, with each
+photon's own factor) sum a_i n_iv.
+
+torch is the plumbing here: the transport runs in the CUDA library through
+the pmcxcl-compatible ``run()``; tensors cross as host arrays.
+"""
+import numpy as np
+
+from . import pmcxcl
+
+
+class ReplayGradient:
+    """One differentiable simulation setup: everything but the mua volume
+    (and optionally the scattering coefficient of label 1) is fixed.  The
+    seed is fixed too, so repeated forward passes use common random numbers.
+
+    cfg: a ``run()`` dictionary without ``vol``; prop row 1 gives mus, g, n
+    of the medium (its mua column is ignored), row 0 the outside."""
+
+    def __init__(self, cfg, run=None):
+        self.run = run or pmcxcl.run
+        self.cfg = dict(cfg)
+        self.cfg.pop("vol", None)
+        self.cfg.update(issavedet=1, issaveseed=1, savedetweight=1, savedetflag="d")
+        self.nphoton = float(self.cfg["nphoton"])
+        self.ndet = int(np.asarray(self.cfg["detpos"]).reshape(-1, 4).shape[0])
+        self.unitinmm = float(self.cfg.get("unitinmm", 1.0))
+        self.last = None
+
+    def _prop(self, mus):
+        prop = np.array(self.cfg["prop"], np.float32).reshape(-1, 4).copy()
+        if mus is not None:
+            prop[1, 1] = mus
+        return prop
+
+    def forward(self, mua, mus=None):
+        """mua: float32 [Nx, Ny, Nz] per mm.  Returns the readings R [ndet] (float64)."""
+        mua = np.asarray(mua, np.float32)
+        prop = self._prop(mus)
+        res = self.run(dict(self.cfg, vol=mua[None], prop=prop))
+        if "detp" in res:
+            detid = res["detp"][0].astype(np.int64) & 0xFFFF
+            w = res["detweight"][0].astype(np.float64)
+            tof = res["detweight"][1].astype(np.float32)
+            seeds = res["seeds"]
+        else:
+            detid = np.zeros(0, np.int64)
+            w = np.zeros(0)
+            tof = np.zeros(0, np.float32)
+            seeds = np.zeros((16, 0), np.uint8)
+        R = np.bincount(detid - 1, weights=w, minlength=self.ndet)[:self.ndet] / self.nphoton
+        self.last = dict(mua=mua, prop=prop, detid=detid, w=w, tof=tof, seeds=seeds, stat=res["stat"])
+        return R
+
+    def _replay(self, a, outputtype, siteown=0):
+        L = self.last
+        cfg = dict(self.cfg, vol=L["mua"][None], prop=L["prop"], seed=L["seeds"],
+                   replayweight=a.astype(np.float32), replaytof=L["tof"], replaydetid=L["detid"].astype(np.int32),
+                   outputtype=outputtype, isnormalized=0, issaveseed=0, savedetweight=0, replaysiteown=siteown)
+        res = self.run(cfg)
+        return res["flux"][..., 0].astype(np.float64), res
+
+    def backward(self, grad_R, want_mus=False):
+        """grad_R: dLoss/dR [ndet].  Returns dLoss/dmua [Nx, Ny, Nz] and, when
+        want_mus, dLoss/dmus per voxel."""
+        L = self.last
+        if L is None:
+            raise RuntimeError("backward() needs a forward() first")
+        g = np.asarray(grad_R, np.float64).ravel()
+        a = g[L["detid"] - 1] * L["w"] / self.nphoton
+        shape = L["mua"].shape
+        if a.size == 0:
+            z = np.zeros(shape)
+            return (z, z) if want_mus else z
+        FJ, res = self._replay(a, "jacobian")
+        self.last["redetected"] = res["stat"]["detected"]
+        gmua = -self.unitinmm * FJ
+        if not want_mus:
+            return gmua
+        FN, _ = self._replay(a, "nscat", siteown=1)
+        mus = float(L["prop"][1, 1]) * self.unitinmm
+        return gmua, FN / mus - self.unitinmm * FJ
+
+
+def readings(sim, mua, mus=None):
+    """Detector readings as a differentiable torch function of mua (and of
+    the scalar mus of label 1 when given as a tensor)."""
+    import torch
+
+    class _Readings(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, mua_t, mus_t):
+            m = None if mus_t is None else float(mus_t.detach().cpu())
+            R = sim.forward(mua_t.detach().cpu().numpy(), m)
+            ctx.dev, ctx.dtype = mua_t.device, mua_t.dtype
+            ctx.want_mus = mus_t is not None and mus_t.requires_grad
+            return torch.as_tensor(R, dtype=torch.float64, device=mua_t.device)
+
+        @staticmethod
+        def backward(ctx, gR):
+            out = sim.backward(gR.detach().cpu().numpy(), want_mus=ctx.want_mus)
+            if ctx.want_mus:
+                gmua, gmus = out
+                gm = torch.as_tensor(gmus.sum(), dtype=torch.float64, device=ctx.dev)
+            else:
+                gmua, gm = out, None
+            return torch.as_tensor(gmua, dtype=ctx.dtype, device=ctx.dev), gm
+
+    return _Readings.apply(mua, mus)

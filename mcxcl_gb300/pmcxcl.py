@@ -206,6 +206,21 @@ def parse_config(cfg, C):
             C.nphoton = s8.shape[1]
     if "replaydet" in cfg:
         C.replaydet = int(cfg["replaydet"])
+    if C.seed == SEED_FROM_FILE and "detphotons" not in cfg and "replayweight" in cfg:
+        # GB300 addition: each replayed photon's weight, time of flight and detector id given directly
+        n = int(C.nphoton)
+        for key, field, dt, ct in (("replayweight", "weight", np.float32, ctypes.c_float),
+                                   ("replaytof", "tof", np.float32, ctypes.c_float),
+                                   ("replaydetid", "detid", np.int32, ctypes.c_int)):
+            a = np.ascontiguousarray(np.asarray(cfg[key], dt).ravel())
+            if a.size != n:
+                raise ValueError("'%s' must have one entry per replayed photon" % key)
+            buf = _libc_malloc(max(a.nbytes, 4))
+            ctypes.memmove(buf, a.ctypes.data, a.nbytes)
+            setattr(C.replay, field, ctypes.cast(buf, ctypes.POINTER(ct)))
+    for key in ("savedetweight", "replaysiteown"):
+        if key in cfg:
+            setattr(C, key, int(cfg[key]))
     if "gpuid" in cfg:
         g = cfg["gpuid"]
         C.deviceid = b"\0" * 256
@@ -264,7 +279,12 @@ def run(cfg=None, **kwargs):
     that reproduces the CPU oracle bit for bit (slower, for verification);
     ``autotune`` -- time the launch shapes on a photon sample (once per
     problem shape and GPU) and run with the fastest; ``savethreadenergy`` --
-    return each reference thread's escaped and launched weight."""
+    return each reference thread's escaped and launched weight;
+    ``savedetweight`` -- return ``detweight`` [2, N], each detected photon's
+    weight and time of flight when detected; a replay may give
+    ``replayweight``/``replaytof``/``replaydetid`` (one entry per seed column)
+    instead of ``detphotons``, and ``replaysiteown`` = 1 makes the
+    scattering-site outputs use each photon's own entries."""
     cfg = dict(cfg or {}, **kwargs)
     L = _lib.load()
     C = Config()
@@ -297,6 +317,9 @@ def _outputs(cfg, C):
     if C.issavedet != b"\0" and ndet:
         d = np.ctypeslib.as_array(C.exportdetected, shape=(ndet * reclen,))
         out["detp"] = d.copy().reshape(ndet, reclen).T
+        if C.savedetweight and C.exportdetweight:
+            w = np.ctypeslib.as_array(C.exportdetweight, shape=(ndet * 2,))
+            out["detweight"] = w.copy().reshape(ndet, 2).T
     if C.issave2pt != b"\0":
         gates = int((C.tend - C.tstart) / C.tstep + 0.5)
         nsrc = C.extrasrclen + 1 if (C.extrasrclen and C.srcid < 0) else 1

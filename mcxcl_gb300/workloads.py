@@ -105,5 +105,38 @@ def config(n):
     raise KeyError(n)
 
 
+def gaussian_field(shape, corr, seed):
+    """Unit-variance Gaussian random field: seeded white noise convolved
+    (periodically, by FFT) with a Gaussian of standard deviation corr voxels."""
+    rng = np.random.default_rng(seed)
+    white = rng.standard_normal(shape)
+    freqs = [np.fft.fftfreq(n) for n in shape]
+    k2 = sum(np.meshgrid(*[f * f for f in freqs], indexing="ij"))
+    kernel = np.exp(-2.0 * (np.pi ** 2) * (corr ** 2) * k2)
+    z = np.real(np.fft.ifftn(np.fft.fftn(white) * kernel))
+    z -= z.mean()
+    return z / z.std()
+
+
+def diff_config(n=100, nphoton=10000000, seed=2024):
+    """Differentiation workload: an n^3 volume of per-voxel mua
+    0.01 (1 + 0.2 z) per mm (z a unit-variance Gaussian random field of 5-voxel
+    correlation length), mus 1/mm, g 0.9, n 1.37; pencil source at the centre
+    of the z = 0 face pointing +z; 16 detectors of radius 1 mm on a 10 mm ring
+    around it.  Returns (cfg without 'vol', mua, target mua): the target
+    readings come from a second seeded field."""
+    c = n / 2.0
+    dets = [[c + 10 * np.cos(2 * np.pi * k / 16), c + 10 * np.sin(2 * np.pi * k / 16), 0, 1] for k in range(16)]
+    cfg = {
+        "nphoton": nphoton, "prop": [[0, 0, 1, 1], [0.01, 1.0, 0.9, 1.37]],
+        "tstart": 0, "tend": 5e-9, "tstep": 5e-9, "srcpos": [c, c, 0], "srcdir": [0, 0, 1], "issrcfrom0": 1,
+        "detpos": dets, "seed": seed, "isreflect": 1, "session": "diff",
+    }
+    shape = (n, n, n)
+    mua = (0.01 * (1 + 0.2 * gaussian_field(shape, 5.0, 11))).astype(np.float32)
+    target = (0.01 * (1 + 0.2 * gaussian_field(shape, 5.0, 12))).astype(np.float32)
+    return cfg, np.maximum(mua, 1e-4), np.maximum(target, 1e-4)
+
+
 def copy_cfg(cfg):
     return copy.deepcopy(cfg)

@@ -90,7 +90,7 @@ typedef struct {
     int mathmode, variant, fieldmode;
     unsigned int nthread;
     /* replay */
-    int replay, replaydet;
+    int replay, replaydet, replaysiteown;
     unsigned int nreplay;
     const uint64_t* rseed;
     const float* rweight;
@@ -103,6 +103,7 @@ typedef struct {
     float* ff;            /* FLOAT_SPILL: 2*fieldlen */
     double* fd;           /* DOUBLE: fieldlen */
     float* detp;          /* record buffer for this worker */
+    float* detw;          /* weight and time of flight of each record when detected, or NULL */
     uint64_t* dseed;
     unsigned int detcap;  /* records this worker may store */
     unsigned int detcount;
@@ -388,10 +389,12 @@ static int skipvoid(const ocfg* c, f4* p, f4* v, f4* f, short fid[4]) {
                 {
                     f4 htime = {0.f, 0.f, 0.f, 0.f};
                     updateprop(c, &htime, c->media[idx1d]);
+                    /* htime.w equals gproperty[label].w of mcx_core.cl:1425-1429 for labels;
+                       for float-mua volumes the reference indexes past the table there */
                     if (c->isspecular && htime.w != c->gprop[0].w) {
-                        p->w *= 1.f - reflectcoeff(v, c->gprop[0].w, c->gprop[c->media[idx1d] & MED_MASK].w, fid[3]);
+                        p->w *= 1.f - reflectcoeff(v, c->gprop[0].w, htime.w, fid[3]);
                         if (p->w > K_EPS) {
-                            transmit(v, c->gprop[0].w, c->gprop[c->media[idx1d] & MED_MASK].w, fid[3]);
+                            transmit(v, c->gprop[0].w, htime.w, fid[3]);
                         }
                     }
                 }
@@ -440,6 +443,10 @@ static void savedetphoton(octx* X, ostate* s, uint32_t isdet) {
             if (c->issaveseed) {
                 X->dseed[slot * 2] = s->photonseed[0];
                 X->dseed[slot * 2 + 1] = s->photonseed[1];
+            }
+            if (X->detw) {
+                X->detw[slot * 2] = s->p.w;
+                X->detw[slot * 2 + 1] = s->f.y;
             }
             base = slot * c->reclen;
             if (SAVE_DETID(c->savedetflag)) {
@@ -1019,7 +1026,7 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                 if (c->replay && (c->outputtype == otWP || c->outputtype == otDCS || c->outputtype == otWPTOF)) {
                     /* replay deposit at the scattering site, mcx_core.cl:2567-2604; the
                        reference indexes these with the launch counter itself (no -1) */
-                    long long k = replay_index(c, tid, (long long)(int)s.f.w);
+                    long long k = replay_index(c, tid, (long long)(int)s.f.w - (c->replaysiteown ? 1 : 0));
                     if (k >= 0 && k < (long long)c->nreplay) {
                         int tshift;
                         tmp0 = (c->outputtype == otDCS) ? (1.f - ctheta) : 1.f;
@@ -1244,7 +1251,7 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
 
 /* ------------------------------------------------------------ host steps */
 
-/* mcx_maskdet, mcx_utils.c:4085-4198 (label volumes) */
+/* mcx_maskdet, mcx_utils.c:4085-4198 */
 static void maskdet(uint32_t* vol, unsigned int nx, unsigned int ny, unsigned int nz, const float* detpos,
                     unsigned int detnum) {
     unsigned int dx = nx + 2, dy = ny + 2, dz = nz + 2;
@@ -1530,7 +1537,7 @@ static int prepare(const mcxo_input* in, oprep* P) {
             isbcdet = 1;
         }
     }
-    if (savedet_eff(in) && in->mediabyte <= 4) {
+    if (savedet_eff(in)) {
         float* dp = (float*)malloc(sizeof(float) * 4 * (in->detnum + 1));
         for (i = 0; i < in->detnum; i++) {
             dp[i * 4] = gdet[i].x;
@@ -1599,6 +1606,7 @@ static int prepare(const mcxo_input* in, oprep* P) {
         }
         c.replay = 1;
         c.replaydet = in->replaydet;
+        c.replaysiteown = in->replaysiteown;
         c.nreplay = in->nreplay;
         c.rseed = in->replayseed;
         c.rweight = in->replayweight;
@@ -1679,6 +1687,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
     unsigned int nworkers = 1;
     float* wdetp = NULL;
     uint64_t* wdseed = NULL;
+    float* wdetw = NULL;
     unsigned int total_det = 0, saved = 0;
     uint64_t cnt[5] = {0, 0, 0, 0, 0};
     int rc = prepare(in, &P);
@@ -1762,6 +1771,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
         X.detcap = in->maxdetphoton;
         X.detp = detp_out ? detp_out : (float*)calloc((size_t)in->maxdetphoton * (hostreclen ? hostreclen : 1), sizeof(float));
         X.dseed = seeds_out ? seeds_out : (uint64_t*)calloc((size_t)in->maxdetphoton * 2 + 2, sizeof(uint64_t));
+        X.detw = in->detweight_out;
         for (i = 0; i < in->nthread; i++) {
             run_thread(&X, seedwords, energy, i);
         }
@@ -1801,6 +1811,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
         wcnt = calloc(nworkers, sizeof(*wcnt));
         wdetp = (float*)calloc((size_t)nworkers * in->maxdetphoton * (hostreclen ? hostreclen : 1) + 1, sizeof(float));
         wdseed = (uint64_t*)calloc((size_t)nworkers * in->maxdetphoton * 2 + 2, sizeof(uint64_t));
+        wdetw = in->detweight_out ? (float*)calloc((size_t)nworkers * in->maxdetphoton * 2 + 2, sizeof(float)) : NULL;
 #ifdef _OPENMP
         #pragma omp parallel for num_threads(nworkers) schedule(static, 1)
 #endif
@@ -1814,6 +1825,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
             X.detcap = in->maxdetphoton;
             X.detp = wdetp + (size_t)w * in->maxdetphoton * (hostreclen ? hostreclen : 1);
             X.dseed = wdseed + (size_t)w * in->maxdetphoton * 2;
+            X.detw = wdetw ? wdetw + (size_t)w * in->maxdetphoton * 2 : NULL;
             if (t1 > in->nthread) {
                 t1 = in->nthread;
             }
@@ -1846,6 +1858,9 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
             if (seeds_out && c.issaveseed) {
                 memcpy(seeds_out + (size_t)saved * 2, wdseed + (size_t)w * in->maxdetphoton * 2, sizeof(uint64_t) * 2 * take);
             }
+            if (wdetw) {
+                memcpy(in->detweight_out + (size_t)saved * 2, wdetw + (size_t)w * in->maxdetphoton * 2, sizeof(float) * 2 * take);
+            }
             saved += take;
             for (k = 0; k < 5; k++) {
                 cnt[k] += wcnt[w][k];
@@ -1856,6 +1871,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
         free(wcnt);
         free(wdetp);
         free(wdseed);
+        free(wdetw);
     }
 
     /* --- merge, energies and normalisation (mcx_host.cpp:1252-1306, 1382-1465) --- */

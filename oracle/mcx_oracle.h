@@ -114,6 +114,11 @@ typedef struct mcxo_input {
     const int* replaydetid;     /* nreplay */
     unsigned int nreplay;
     int replaydet;              /* 0 all detectors into one field, -1 one field per detector, k detector k */
+    int replaysiteown;          /* 1: scattering-site replay outputs read the replayed photon's own entries */
+
+    /* optional output: weight and time of flight of each saved detected photon
+       when it was detected (maxdetphoton x 2 floats), or NULL */
+    float* detweight_out;
 } mcxo_input;
 
 typedef struct mcxo_stats {

@@ -59,6 +59,7 @@ class MCXOInput(ctypes.Structure):
         ("nworkers", ctypes.c_int),
         ("replayseed", ctypes.c_void_p), ("replayweight", ctypes.c_void_p), ("replaytof", ctypes.c_void_p),
         ("replaydetid", ctypes.c_void_p), ("nreplay", ctypes.c_uint), ("replaydet", ctypes.c_int),
+        ("replaysiteown", ctypes.c_int), ("detweight_out", ctypes.c_void_p),
     ]
 
 
@@ -257,12 +258,25 @@ def _replay_input(inp, keep, cfg, seed):
         raise ValueError("the row number of cfg.seed does not match RNG seed byte-length")
     n = s8.shape[1]
     seeds = np.ascontiguousarray(s8.T).view(np.uint64).reshape(n, 2).copy()
+    inp.seed = SEED_FROM_FILE
+    inp.replaydet = int(cfg.get("replaydet", 0))
+    inp.replaysiteown = int(cfg.get("replaysiteown", 0))
+    if "detphotons" not in cfg:
+        # per-photon weight, time of flight and detector id given directly
+        w = np.ascontiguousarray(np.asarray(cfg["replayweight"], np.float32).ravel())
+        tof = np.ascontiguousarray(np.asarray(cfg["replaytof"], np.float32).ravel())
+        did = np.ascontiguousarray(np.asarray(cfg["replaydetid"], np.int32).ravel())
+        for name, a in (("rseed", seeds), ("rw", w), ("rtof", tof), ("rdid", did)):
+            keep[name] = a
+        inp.replayseed, inp.replayweight = _ptr(seeds), _ptr(w)
+        inp.replaytof, inp.replaydetid = _ptr(tof), _ptr(did)
+        inp.nreplay = n
+        inp.nphoton = float(n)
+        return
     detp = np.asarray(cfg["detphotons"], np.float32)
     if detp.ndim != 2 or detp.shape[1] != n:
         raise ValueError("the column numbers of detphotons and seed do not match")
     recs = np.ascontiguousarray(detp.T)
-    inp.seed = SEED_FROM_FILE
-    inp.replaydet = int(cfg.get("replaydet", 0))
     out_seed = np.zeros((max(n, 1), 2), np.uint64)
     w = np.zeros(max(n, 1), np.float32)
     tof = np.zeros(max(n, 1), np.float32)
@@ -295,6 +309,8 @@ def run(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL
     detp = np.zeros(max(1, maxdet * max(reclen, 1)), np.float32)
     seeds = np.zeros(max(2, maxdet * 2), np.uint64)
     masked = np.zeros(inp.dimx * inp.dimy * inp.dimz, np.uint32)
+    detw = np.zeros(max(2, maxdet * 2), np.float32)
+    inp.detweight_out = _ptr(detw)
     st = MCXOStats()
     rc = L.mcxo_run(ctypes.byref(inp), _ptr(field), _ptr(fnorm), _ptr(energy), _ptr(detp), _ptr(seeds),
                     _ptr(masked), ctypes.byref(st))
@@ -309,6 +325,7 @@ def run(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL
         "energy": energy.reshape(-1, 2),
         "detp": detp[:nsaved * reclen].reshape(nsaved, reclen).T if reclen else np.zeros((0, 0), np.float32),
         "seeds": seeds[:2 * nsaved].reshape(nsaved, 2) if inp.issaveseed else None,
+        "detweight": detw[:2 * nsaved].reshape(nsaved, 2).T.copy(),
         "masked": masked.reshape(inp.dimx, inp.dimy, inp.dimz, order="F"),
         "stat": {k: getattr(st, k) for k, _ in MCXOStats._fields_},
         "gates": gates,

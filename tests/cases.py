@@ -106,7 +106,11 @@ VARIANTS = {
     "invcdf": dict(invcdf=(np.sign(np.linspace(-1, 1, 101)) *
                            np.abs(np.linspace(-1, 1, 101)) ** 0.7).astype(np.float32)),
     "angleinvcdf": dict(angleinvcdf=np.linspace(0, 0.3, 21).astype(np.float32)),
+    # per-voxel float mua (MEDIA_MUA_FLOAT); the reference's __NVCC__ branch cannot run it
+    "muafloat": dict(vol=(0.005 + 0.02 * np.random.RandomState(3).rand(1, 40, 40, 40)).astype(np.float32),
+                     prop=[[0, 0, 1, 1], [0.01, 1, 0.5, 1.37]], savedetflag="dxvw"),
 }
+NOT_PINNED = {"muafloat"}
 
 
 def variant(name, **kw):
@@ -128,7 +132,8 @@ def pin_cases():
            ("cube60b_dspmxvw", cube60(nphoton=3000, isreflect=1, savedetflag="dspmxvw", issaveseed=1), 256),
            ("twod", twod(), 128)]
     for k in VARIANTS:
-        out.append((k, variant(k), 128))
+        if k not in NOT_PINNED:
+            out.append((k, variant(k), 128))
     return out
 
 
