@@ -232,6 +232,15 @@ const char* mcx_version(void);
    caller can launch the resident problem repeatedly with mcxg_simulate
    (benchmarks, repeated solves).  NULL on error (cfg->errorcode). */
 struct mcxg_session* mcx_prepare_simulation(Config* cfg);
+/* Runs n validated configurations in one persistent launch: a GB300
+   addition, no counterpart in the reference (one simulation per
+   mcx_run_simulation call).  Each simulation gets ceil(nphoton /
+   photons_per_thread) reference threads (0 = 64) with seeds derived from its
+   cfg.seed; flags: MCXG_GRAPH, MCXG_AGG.  Outputs go to each Config as
+   mcx_run_simulation's do; an error is reported on cfgs[0].  Label volumes
+   of at most 128 labels, one respin, no detectors, replay, extra sources,
+   patterns or phase tables. */
+void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsigned int flags);
 /* sizeof(Config) and the byte offset of a named field ((size_t)-1 if
    unknown), for checking foreign-function mirrors of the struct. */
 size_t mcx_config_sizeof(void);
@@ -255,6 +264,7 @@ void mcx_release_sessions(void);
 #define MCXG_RNGDUMP  4u   /* write each thread's RNG stream into the field (-D R) */
 #define MCXG_KEEP     8u   /* keep accumulating into the field (respin); energies, records and counters restart */
 #define MCXG_AGG     16u   /* aggregate same-voxel deposits of a warp before the atomics */
+#define MCXG_GRAPH   32u   /* batch: capture the run as a CUDA graph once, replay it afterwards */
 
 typedef struct mcxg_devinfo {
     char name[64];
@@ -291,6 +301,25 @@ int  mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread);
    selects the instantiation whose registers are capped for three resident
    256-thread blocks per SM (also the automatic choice); 2 the uncapped one. */
 int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
+/* ---- batches: many simulations in one persistent launch (no counterpart in
+   the reference, which launches once per simulation).  sims[i] holds the
+   parameter block of simulation i (nthread = its reference threads,
+   fieldlen = its field) and its offsets into the concatenated buffers:
+   media (one byte per voxel, label | detector bit << 7), prop4 (rows of
+   {mua, mus, g, n}) and the field.  Reference threads are numbered
+   contiguously across the batch (vt_off); seeds come from splitmix64 of the
+   simulation's seed.  Not supported in a batch: detectors, replay, extra
+   sources, patterns, phase tables. */
+int  mcxg_batch_set(mcxg_session* s, const void* sims, size_t desc_size, uint32_t nsim, const uint8_t* media,
+                    uint64_t nmedia, const float* prop4, uint32_t nprop);
+/* Runs every simulation of the batch; MCXG_GRAPH replays a captured graph,
+   MCXG_AGG aggregates deposits.  *kernel_ms covers the clear, transport and
+   per-simulation sums. */
+int  mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms);
+/* Per simulation: FP64 {escaped, launched} weight, 2 x nsim. */
+int  mcxg_batch_get_energy(mcxg_session* s, double* out);
+/* Every simulation's field, (hi + lo) x scales[i], at its field offset. */
+int  mcxg_batch_get_field(mcxg_session* s, float* out, const double* scales);
 /* Replay inputs, one entry per replayed photon: the saved xorshift128+ state
    (16 bytes), detected weight, time of flight and detector id.  Used when
    the parameter block has replay = 1; n = 0 releases nothing and clears. */

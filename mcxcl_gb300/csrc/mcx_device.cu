@@ -15,6 +15,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -74,6 +75,31 @@ struct mcxg_session {
     uint32_t nreplay = 0;
     double* d_scales = nullptr;      /* per-block normalisation factors */
     size_t scales_cap = 0;
+
+    /* batch of simulations in one persistent launch */
+    std::vector<mcxg_simdesc> h_sims;
+    mcxg_simdesc* d_sims = nullptr;
+    size_t sims_cap = 0;
+    unsigned long long* d_simvt = nullptr;
+    size_t simvt_cap = 0;
+    uint8_t* d_bmedia = nullptr;
+    size_t bmedia_cap = 0;
+    float4* d_bprop = nullptr;       /* property rows, then their reciprocals */
+    size_t bprop_cap = 0;
+    float* d_bfield = nullptr;       /* 2 x totalfield */
+    size_t bfield_cap = 0;
+    float2* d_benergy = nullptr;     /* per reference thread of the batch */
+    size_t benergy_cap = 0;
+    double* d_bsum = nullptr;        /* per simulation: escaped, launched */
+    size_t bsum_cap = 0;
+    float* d_bout = nullptr;
+    size_t bout_cap = 0;
+    uint32_t nsim = 0, nbprop = 0;
+    unsigned long long totalvt = 0, totalfield = 0;
+    bool has_batch = false;
+    int bt_block = 256, bt_bpsm = 3, bt_grid = 0;
+    cudaGraph_t bgraph = nullptr;
+    cudaGraphExec_t bgraph_exec = nullptr;
 
     std::vector<float> h_det, h_srcx;
     int block_req = 0, bpsm_req = 0;
@@ -175,6 +201,59 @@ __global__ void field_merge_blocks(const float* __restrict__ f, size_t n, size_t
                                    const double* __restrict__ scales, float* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         out[i] = (float)(((double)f[i] + (double)f[i + n]) * scales[i / blocklen]);
+    }
+}
+
+/* reciprocals of each property row, as the single-simulation kernel stages them */
+__global__ void batch_recip(const float4* __restrict__ prop, unsigned int n, float4* __restrict__ recip) {
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 q = prop[i];
+        recip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x), 0.f);
+    }
+}
+
+/* per-simulation FP64 energy sums: one block per simulation, fixed order */
+__global__ void batch_energy(const float2* __restrict__ e, const mcxg_simdesc* __restrict__ sims,
+                             double* __restrict__ out) {
+    const mcxg_simdesc& d = sims[blockIdx.x];
+    const unsigned long long base = d.vt_off;
+    const unsigned int n = d.kp.nthread;
+    double se = 0.0, sl = 0.0;
+    for (unsigned int i = threadIdx.x; i < n; i += blockDim.x) {
+        float2 v = e[base + i];
+        se += (double)v.x;
+        sl += (double)v.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        se += __shfl_down_sync(0xffffffffu, se, o);
+        sl += __shfl_down_sync(0xffffffffu, sl, o);
+    }
+    __shared__ double wse[32], wsl[32];
+    if ((threadIdx.x & 31) == 0) {
+        wse[threadIdx.x >> 5] = se;
+        wsl[threadIdx.x >> 5] = sl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (unsigned int w = 0; w < (blockDim.x + 31) / 32; w++) {
+            a += wse[w];
+            b += wsl[w];
+        }
+        out[blockIdx.x * 2] = a;
+        out[blockIdx.x * 2 + 1] = b;
+    }
+}
+
+/* merged, scaled field of every simulation: row y of the grid is simulation y */
+__global__ void batch_merge(const float* __restrict__ f, unsigned long long total, const mcxg_simdesc* __restrict__ sims,
+                            const double* __restrict__ scales, float* __restrict__ out) {
+    const mcxg_simdesc& d = sims[blockIdx.y];
+    const unsigned long long off = d.field_off;
+    const unsigned int n = d.kp.fieldlen;
+    const double sc = scales[blockIdx.y];
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        out[off + i] = (float)(((double)f[off + i] + (double)f[off + i + total]) * sc);
     }
 }
 
@@ -326,7 +405,14 @@ int mcxg_destroy(mcxg_session* s) {
     }
     void* bufs[] = {s->d_media, s->d_prop, s->d_tables, s->d_pattern, s->d_seeds, s->d_field, s->d_energy,
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
-                    s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw};
+                    s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw,
+                    s->d_sims, s->d_simvt, s->d_bmedia, s->d_bprop, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout};
+    if (s->bgraph_exec) {
+        cudaGraphExecDestroy(s->bgraph_exec);
+    }
+    if (s->bgraph) {
+        cudaGraphDestroy(s->bgraph);
+    }
     for (void* b : bufs) {
         if (b) {
             cudaFree(b);
@@ -527,6 +613,7 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     MCXG_TRY(cudaMemsetAsync(s->d_events, 0, 8 * sizeof(unsigned long long), s->st));
 
     KArgs a;
+    memset(&a, 0, sizeof(a));
     a.media8 = (const uint8_t*)s->d_media;
     a.media32 = (const uint32_t*)s->d_media;
     a.gprop = s->d_prop;
@@ -844,6 +931,221 @@ int mcxg_fp32_peak(mcxg_session* s, double* gops) {
     return MCXG_OK;
 }
 
+
+/* ---- batch of simulations ---------------------------------------------------
+ *
+ * Many independent simulations share one persistent launch.  Their volumes,
+ * fields and property rows are concatenated; each simulation's descriptor
+ * (parameter block + offsets) sits in global memory and the threads claim
+ * reference threads from one counter over the concatenated numbering, so a
+ * simulation of 1e5 photons does not leave the GPU idle at the end of its
+ * own launch, and many small simulations cost one launch.
+ */
+namespace {
+
+int batch_reset_graph(mcxg_session* s) {
+    if (s->bgraph_exec) {
+        cudaGraphExecDestroy(s->bgraph_exec);
+        s->bgraph_exec = nullptr;
+    }
+    if (s->bgraph) {
+        cudaGraphDestroy(s->bgraph);
+        s->bgraph = nullptr;
+    }
+    return MCXG_OK;
+}
+
+/* the work of one batch run, on s->st: clear, transport, per-simulation sums */
+int batch_enqueue(mcxg_session* s, int lflags) {
+    MCXG_TRY(cudaMemsetAsync(s->d_bfield, 0, sizeof(float) * 2 * (size_t)s->totalfield, s->st));
+    MCXG_TRY(cudaMemsetAsync(s->d_benergy, 0, sizeof(float2) * (size_t)s->totalvt, s->st));
+    MCXG_TRY(cudaMemsetAsync(s->d_words, 0, 8 * sizeof(unsigned int), s->st));
+    KArgs a;
+    memset(&a, 0, sizeof(a));
+    a.media8 = s->d_bmedia;
+    a.media32 = (const uint32_t*)s->d_bmedia;
+    a.gprop = s->d_bprop;
+    a.grecip = s->d_bprop + s->nbprop;
+    a.field = s->d_bfield;
+    a.energy = s->d_benergy;
+    a.detcount = s->d_words + 0;
+    a.vtcounter = s->d_words + 1;
+    a.status = s->d_words + 2;
+    a.counters = s->d_events;
+    a.sims = s->d_sims;
+    a.simvt = s->d_simvt;
+    a.nsim = s->nsim;
+    a.totalvt = s->totalvt;
+    MCXG_TRY(mcxg::fast_launch(a, lflags, s->bt_grid, s->bt_block, 0, s->st));
+    batch_energy<<<s->nsim, 256, 0, s->st>>>(s->d_benergy, s->d_sims, s->d_bsum);
+    return MCXG_OK;
+}
+
+}  // namespace
+
+int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_t nsim, const uint8_t* media,
+                   uint64_t nmedia, const float* prop4, uint32_t nprop) {
+    const mcxg_simdesc* sims = (const mcxg_simdesc*)sims_;
+    if (!s || !sims || desc_size != sizeof(mcxg_simdesc) || nsim == 0 || !media || !prop4 || nprop == 0) {
+        return MCXG_ERR_ARG;
+    }
+    /* the simulations' reference threads must number 0.. contiguously, and
+       every offset must stay inside the buffers given */
+    std::vector<unsigned long long> simvt(nsim + 1);
+    unsigned long long vt = 0, field = 0;
+    for (uint32_t i = 0; i < nsim; i++) {
+        const mcxg_simdesc& d = sims[i];
+        if (d.vt_off != vt || d.kp.nthread == 0 || d.kp.mediaword != 1 || d.kp.savedet || d.kp.replay ||
+                d.kp.extrasrclen || d.kp.nphase || d.kp.nangle || d.kp.npattern ||
+                d.media_off + d.kp.nvox > nmedia || d.prop_off + d.kp.medianum > nprop ||
+                (unsigned long long)d.kp.threadphoton * d.kp.nthread + (unsigned int)d.kp.oddphoton == 0) {
+            return MCXG_ERR_ARG;
+        }
+        simvt[i] = vt;
+        vt += d.kp.nthread;
+        field = std::max(field, (unsigned long long)d.field_off + d.kp.fieldlen);
+    }
+    simvt[nsim] = vt;
+    if (vt >= 0xFFFFFFFFull - 65536ull * 1024 || 2 * field >= 0xFFFFFFFFull) {
+        return MCXG_ERR_LIMIT;          /* 32-bit thread counter and field indices */
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    int rc = ensure(&s->d_sims, &s->sims_cap, nsim);
+    if (!rc) {
+        rc = ensure(&s->d_simvt, &s->simvt_cap, (size_t)nsim + 1);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_bmedia, &s->bmedia_cap, (size_t)nmedia);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_bprop, &s->bprop_cap, 2 * (size_t)nprop);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_bfield, &s->bfield_cap, 2 * (size_t)field);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_benergy, &s->benergy_cap, (size_t)vt);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_bsum, &s->bsum_cap, 2 * (size_t)nsim);
+    }
+    if (rc) {
+        return rc;
+    }
+    MCXG_TRY(cudaMemcpyAsync(s->d_sims, sims, sizeof(mcxg_simdesc) * nsim, cudaMemcpyHostToDevice, s->st));
+    MCXG_TRY(cudaMemcpyAsync(s->d_simvt, simvt.data(), sizeof(unsigned long long) * (nsim + 1), cudaMemcpyHostToDevice,
+                             s->st));
+    MCXG_TRY(cudaMemcpyAsync(s->d_bmedia, media, (size_t)nmedia, cudaMemcpyHostToDevice, s->st));
+    MCXG_TRY(cudaMemcpyAsync(s->d_bprop, prop4, sizeof(float4) * nprop, cudaMemcpyHostToDevice, s->st));
+    batch_recip<<<grid_for(s, nprop), 256, 0, s->st>>>(s->d_bprop, nprop, s->d_bprop + nprop);
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    MCXG_TRY(cudaGetLastError());
+    s->h_sims.assign(sims, sims + nsim);
+    s->nsim = nsim;
+    s->nbprop = nprop;
+    s->totalvt = vt;
+    s->totalfield = field;
+    s->has_batch = true;
+    return batch_reset_graph(s);
+}
+
+int mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
+    if (!s) {
+        return MCXG_ERR_ARG;
+    }
+    if (!s->has_batch) {
+        return MCXG_ERR_STATE;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    bool refl = false;
+    for (const mcxg_simdesc& d : s->h_sims) {
+        refl = refl || d.kp.dorefl_compiled;
+    }
+    const bool agg = (flags & MCXG_AGG) != 0;
+    const int bpsm_req = s->bpsm_req ? s->bpsm_req : 3;
+    int lflags = mcxg::LF_BATCH | (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) |
+                 (bpsm_req == 3 ? mcxg::LF_OCC3 : 0);
+    int block = s->block_req ? s->block_req : 256;
+    int occ = 0;
+    MCXG_TRY(mcxg::fast_occupancy(lflags, block, 0, &occ));
+    int bpsm = std::max(1, std::min(bpsm_req, occ > 0 ? occ : bpsm_req));
+    const int grid = s->info.sm * bpsm;
+    if (grid != s->bt_grid || block != s->bt_block) {
+        batch_reset_graph(s);
+    }
+    s->bt_grid = grid;
+    s->bt_block = block;
+    s->grid = grid;
+    s->block = block;
+
+    if (flags & MCXG_GRAPH) {
+        /* the clear + transport + sums sequence, captured once and replayed */
+        if (!s->bgraph_exec) {
+            MCXG_TRY(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+            int rc = batch_enqueue(s, lflags);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(s->st, &g);
+            if (rc) {
+                if (g) {
+                    cudaGraphDestroy(g);
+                }
+                return rc;
+            }
+            MCXG_TRY(e);
+            s->bgraph = g;
+            MCXG_TRY(cudaGraphInstantiate(&s->bgraph_exec, g, 0));
+        }
+        MCXG_TRY(cudaEventRecord(s->e0, s->st));
+        MCXG_TRY(cudaGraphLaunch(s->bgraph_exec, s->st));
+        MCXG_TRY(cudaEventRecord(s->e1, s->st));
+    } else {
+        MCXG_TRY(cudaEventRecord(s->e0, s->st));
+        int rc = batch_enqueue(s, lflags);
+        if (rc) {
+            return rc;
+        }
+        MCXG_TRY(cudaEventRecord(s->e1, s->st));
+    }
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    MCXG_TRY(cudaGetLastError());
+    if (kernel_ms) {
+        float ms = 0.f;
+        MCXG_TRY(cudaEventElapsedTime(&ms, s->e0, s->e1));
+        *kernel_ms = ms;
+    }
+    return MCXG_OK;
+}
+
+int mcxg_batch_get_energy(mcxg_session* s, double* out) {
+    if (!s || !out || !s->has_batch) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_bsum, sizeof(double) * 2 * s->nsim, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_batch_get_field(mcxg_session* s, float* out, const double* scales) {
+    if (!s || !out || !scales || !s->has_batch) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    int rc = ensure(&s->d_bout, &s->bout_cap, (size_t)s->totalfield);
+    if (!rc) {
+        rc = ensure(&s->d_scales, &s->scales_cap, s->nsim);
+    }
+    if (rc) {
+        return rc;
+    }
+    MCXG_TRY(cudaMemcpyAsync(s->d_scales, scales, sizeof(double) * s->nsim, cudaMemcpyHostToDevice, s->st));
+    MCXG_TRY(cudaMemsetAsync(s->d_bout, 0, sizeof(float) * (size_t)s->totalfield, s->st));
+    batch_merge<<<dim3(64, s->nsim), 256, 0, s->st>>>(s->d_bfield, s->totalfield, s->d_sims, s->d_scales, s->d_bout);
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_bout, sizeof(float) * (size_t)s->totalfield, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    MCXG_TRY(cudaGetLastError());
+    return MCXG_OK;
+}
 
 /* ---- allocation-free FP64 energy sum ---------------------------------------
  *

@@ -746,6 +746,74 @@ static void device_check(int rc, const char* what) {
     }
 }
 
+/* the kernel constant block of one simulation (mcx_host.cpp:507-524, 674-693) */
+static void make_kparams(const Config* cfg, size_t nvox, size_t fieldlen, size_t autothread, unsigned int hostdetreclen,
+                         unsigned int partialdata, unsigned int is2d, int replay, mcxg_kparams* kp) {
+    memset(kp, 0, sizeof(*kp));
+    kp->srcpos = (mcxg_float4) {cfg->srcpos.x, cfg->srcpos.y, cfg->srcpos.z, cfg->srcpos.w};
+    kp->srcdir = (mcxg_float4) {cfg->srcdir.x, cfg->srcdir.y, cfg->srcdir.z, cfg->srcdir.w};
+    kp->srcparam1 = (mcxg_float4) {cfg->srcparam1.x, cfg->srcparam1.y, cfg->srcparam1.z, cfg->srcparam1.w};
+    kp->srcparam2 = (mcxg_float4) {cfg->srcparam2.x, cfg->srcparam2.y, cfg->srcparam2.z, cfg->srcparam2.w};
+    kp->maxidx = (mcxg_float4) {(float)cfg->dim.x, (float)cfg->dim.y, (float)cfg->dim.z, 0.f};
+    kp->dimx = cfg->dim.x;
+    kp->dimxy = cfg->dim.x * cfg->dim.y;
+    kp->nvox = (uint32_t)nvox;
+    kp->fieldlen = (uint32_t)fieldlen;
+    kp->twin0 = cfg->tstart;
+    kp->twin1 = cfg->tstart + cfg->tstep * cfg->maxgate;
+    float minstep = fminf(fminf(cfg->steps.x, cfg->steps.y), cfg->steps.z);
+    kp->oneoverc0 = R_C0 * cfg->unitinmm;
+    kp->Rtstep = 1.f / cfg->tstep;
+    kp->minenergy = cfg->minenergy;
+    kp->minaccumtime = minstep * R_C0 * cfg->unitinmm;
+    kp->doreflect = (uint32_t)cfg->isreflect;
+    {
+        const char allabsorb[6] = {bcAbsorb, bcAbsorb, bcAbsorb, bcAbsorb, bcAbsorb, bcAbsorb};
+        const char allunknown[6] = {0, 0, 0, 0, 0, 0};
+        int refl = cfg->isreflect || (memcmp(cfg->bc, allabsorb, 6) && memcmp(cfg->bc, allunknown, 6));
+        for (int i = 0; i < 6; i++) {
+            if (cfg->bc[i] == bcReflect || cfg->bc[i] == bcMirror) {
+                refl = 1;
+            }
+        }
+        kp->dorefl_compiled = (uint32_t)refl;
+    }
+    kp->save2pt = cfg->issave2pt ? 1 : 0;
+    kp->savedet = (uint32_t)cfg->issavedet;
+    kp->maxdetphoton = cfg->maxdetphoton;
+    kp->maxmedia = cfg->medianum - 1;
+    kp->medianum = cfg->medianum;
+    kp->detnum = cfg->detnum;
+    kp->voidtime = (uint32_t)cfg->voidtime;
+    kp->srctype = (uint32_t)cfg->srctype;
+    kp->maxvoidstep = (uint32_t)cfg->maxvoidstep;
+    kp->issaveseed = cfg->issaveseed > 0;
+    kp->issaveref = (uint32_t)cfg->issaveref;
+    kp->isspecular = cfg->isspecular > 0;
+    kp->maxgate = cfg->maxgate;
+    kp->outputtype = (uint32_t)cfg->outputtype;
+    kp->savedetflag = cfg->savedetflag;
+    kp->reclen = hostdetreclen;
+    kp->partialdata = partialdata;
+    kp->mediaformat = cfg->mediabyte;
+    kp->gscatter = cfg->gscatter;
+    kp->is2d = is2d;
+    kp->nphase = cfg->nphase;
+    kp->nangle = cfg->nangle;
+    kp->extrasrclen = cfg->extrasrclen;
+    kp->srcid = cfg->srcid;
+    kp->nthread = (uint32_t)autothread;
+    if (replay) {
+        kp->replay = 1;
+        kp->nreplay = (uint32_t)cfg->nphoton;
+        kp->replaydet = cfg->replaydet;
+        kp->siteshift = cfg->replaysiteown ? 0u : 1u;
+    }
+    for (int i = 0; i < 12; i++) {
+        kp->bc[i] = (uint8_t)cfg->bc[i];
+    }
+}
+
 /* --------------------------------------------------------------- the driver */
 
 /* set by mcx_prepare_simulation: stop once the problem and the first seeds are resident */
@@ -836,71 +904,8 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
         fullload = (float)g.core;
     }
 
-    /* kernel constant block (mcx_host.cpp:507-524, 674-693) */
     mcxg_kparams kp;
-    memset(&kp, 0, sizeof(kp));
-    kp.srcpos = (mcxg_float4) {cfg->srcpos.x, cfg->srcpos.y, cfg->srcpos.z, cfg->srcpos.w};
-    kp.srcdir = (mcxg_float4) {cfg->srcdir.x, cfg->srcdir.y, cfg->srcdir.z, cfg->srcdir.w};
-    kp.srcparam1 = (mcxg_float4) {cfg->srcparam1.x, cfg->srcparam1.y, cfg->srcparam1.z, cfg->srcparam1.w};
-    kp.srcparam2 = (mcxg_float4) {cfg->srcparam2.x, cfg->srcparam2.y, cfg->srcparam2.z, cfg->srcparam2.w};
-    kp.maxidx = (mcxg_float4) {(float)cfg->dim.x, (float)cfg->dim.y, (float)cfg->dim.z, 0.f};
-    kp.dimx = cfg->dim.x;
-    kp.dimxy = cfg->dim.x * cfg->dim.y;
-    kp.nvox = (uint32_t)nvox;
-    kp.fieldlen = (uint32_t)fieldlen;
-    kp.twin0 = cfg->tstart;
-    kp.twin1 = cfg->tstart + cfg->tstep * cfg->maxgate;
-    float minstep = fminf(fminf(cfg->steps.x, cfg->steps.y), cfg->steps.z);
-    kp.oneoverc0 = R_C0 * cfg->unitinmm;
-    kp.Rtstep = 1.f / cfg->tstep;
-    kp.minenergy = cfg->minenergy;
-    kp.minaccumtime = minstep * R_C0 * cfg->unitinmm;
-    kp.doreflect = (uint32_t)cfg->isreflect;
-    {
-        const char allabsorb[6] = {bcAbsorb, bcAbsorb, bcAbsorb, bcAbsorb, bcAbsorb, bcAbsorb};
-        const char allunknown[6] = {0, 0, 0, 0, 0, 0};
-        int refl = cfg->isreflect || (memcmp(cfg->bc, allabsorb, 6) && memcmp(cfg->bc, allunknown, 6));
-        for (int i = 0; i < 6; i++) {
-            if (cfg->bc[i] == bcReflect || cfg->bc[i] == bcMirror) {
-                refl = 1;
-            }
-        }
-        kp.dorefl_compiled = (uint32_t)refl;
-    }
-    kp.save2pt = cfg->issave2pt ? 1 : 0;
-    kp.savedet = (uint32_t)cfg->issavedet;
-    kp.maxdetphoton = cfg->maxdetphoton;
-    kp.maxmedia = cfg->medianum - 1;
-    kp.medianum = cfg->medianum;
-    kp.detnum = cfg->detnum;
-    kp.voidtime = (uint32_t)cfg->voidtime;
-    kp.srctype = (uint32_t)cfg->srctype;
-    kp.maxvoidstep = (uint32_t)cfg->maxvoidstep;
-    kp.issaveseed = cfg->issaveseed > 0;
-    kp.issaveref = (uint32_t)cfg->issaveref;
-    kp.isspecular = cfg->isspecular > 0;
-    kp.maxgate = cfg->maxgate;
-    kp.outputtype = (uint32_t)cfg->outputtype;
-    kp.savedetflag = cfg->savedetflag;
-    kp.reclen = hostdetreclen;
-    kp.partialdata = partialdata;
-    kp.mediaformat = cfg->mediabyte;
-    kp.gscatter = cfg->gscatter;
-    kp.is2d = is2d;
-    kp.nphase = cfg->nphase;
-    kp.nangle = cfg->nangle;
-    kp.extrasrclen = cfg->extrasrclen;
-    kp.srcid = cfg->srcid;
-    kp.nthread = (uint32_t)autothread;
-    if (replay) {
-        kp.replay = 1;
-        kp.nreplay = (uint32_t)cfg->nphoton;
-        kp.replaydet = cfg->replaydet;
-        kp.siteshift = cfg->replaysiteown ? 0u : 1u;
-    }
-    for (int i = 0; i < 12; i++) {
-        kp.bc[i] = (uint8_t)cfg->bc[i];
-    }
+    make_kparams(cfg, nvox, fieldlen, autothread, hostdetreclen, partialdata, is2d, replay, &kp);
 
     /* the label volume: one byte per voxel (label | detector bit << 7) when
        every label fits in seven bits, else the reference's 32-bit words */
@@ -1196,6 +1201,178 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
 #undef seedbuf
 #undef fieldtmp
 #undef blockscale
+    MCX_LEAVE();
+}
+
+/* Runs n validated configurations in one persistent launch (a GB300
+   addition: the reference runs one simulation per call).  Outputs go to each
+   Config as mcx_run_simulation's do; errors are reported on cfgs[0]. */
+void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsigned int flags) {
+    static __thread void* btmp[5];
+    for (int i = 0; i < 5; i++) {
+        free(btmp[i]);
+        btmp[i] = NULL;
+    }
+#define bdesc  (*(mcxg_simdesc**)&btmp[0])
+#define bmedia (*(uint8_t**)&btmp[1])
+#define bprop  (*(float**)&btmp[2])
+#define bfield (*(float**)&btmp[3])
+#define bsums  (*(double**)&btmp[4])
+    if (n <= 0 || !cfgs || !cfgs[0]) {
+        return;
+    }
+    Config* cfg0 = cfgs[0];
+    MCX_ENTER(cfg0);
+    unsigned int ppt = photons_per_thread ? photons_per_thread : 64;
+    uint64_t nmedia = 0, nfield = 0, nvt = 0;
+    uint32_t nprop = 0;
+    for (int k = 0; k < n; k++) {
+        Config* cfg = cfgs[k];
+        if (!cfg || cfg->issavedet || cfg->seed == SEED_FROM_FILE || cfg->extrasrclen || cfg->nphase || cfg->nangle ||
+                cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D || cfg->mediabyte > 4 ||
+                cfg->medianum > 128 || cfg->respin != 1 || cfg->issaveref || (cfg->debuglevel & 1)) {
+            MCX_ERROR(-4, "a batch simulation takes label volumes of at most 128 labels, one respin, and no "
+                      "detectors, replay, extra sources, patterns, phase tables or saved reflectance");
+        }
+        if (cfg->nphoton == 0) {
+            MCX_ERROR(-4, "every simulation of a batch needs at least one photon");
+        }
+        cfg->maxgate = (unsigned int)(int)((cfg->tend - cfg->tstart) / cfg->tstep + 0.5);
+        size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+        nmedia += nvox;
+        nfield += nvox * cfg->maxgate;
+        nvt += (cfg->nphoton + ppt - 1) / ppt;
+        nprop += cfg->medianum;
+    }
+    if (nfield >= 0x7FFFFFFFull || nvt >= 0xF0000000ull) {
+        MCX_ERROR(-1, "batch too large for 32-bit field indices or thread numbering");
+    }
+    unsigned int workdev = 0;
+    GPUInfo* gpu = NULL;
+    mcx_list_gpu(cfg0, &workdev, &gpu);
+    if (workdev == 0) {
+        free(gpu);
+        MCX_ERROR(-99, "Specified GPU does not exist");
+    }
+    int device = gpu[0].id - 1;
+    free(gpu);
+
+    bdesc = (mcxg_simdesc*)calloc((size_t)n, sizeof(mcxg_simdesc));
+    bmedia = (uint8_t*)malloc(nmedia ? nmedia : 1);
+    bprop = (float*)malloc(sizeof(float) * 4 * nprop);
+    if (!bdesc || !bmedia || !bprop) {
+        MCX_ERROR(-2, "out of host memory");
+    }
+    uint64_t moff = 0, foff = 0, voff = 0;
+    uint32_t poff = 0;
+    for (int k = 0; k < n; k++) {
+        Config* cfg = cfgs[k];
+        size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+        size_t fieldlen = nvox * cfg->maxgate;
+        size_t vts = (cfg->nphoton + ppt - 1) / ppt;
+        unsigned int is2d = (cfg->dim.x == 1 ? 1 : (cfg->dim.y == 1 ? 2 : (cfg->dim.z == 1 ? 3 : 0)));
+        if (is2d) {
+            is2d = is2d * (((cfg->dim.x > 1) + (cfg->dim.y > 1) + (cfg->dim.z > 1)) == 2);
+        }
+        mcxg_simdesc* d = &bdesc[k];
+        make_kparams(cfg, nvox, fieldlen, vts, 0, 0, is2d, 0, &d->kp);
+        d->kp.threadphoton = (uint32_t)(cfg->nphoton / vts);
+        d->kp.oddphoton = (int32_t)(cfg->nphoton - (size_t)d->kp.threadphoton * vts);
+        d->kp.mediaword = 1;
+        d->kp.savedet = 0;
+        d->media_off = moff;
+        d->field_off = foff;
+        d->vt_off = voff;
+        d->prop_off = poff;
+        d->seed = (uint64_t)(uint32_t)(cfg->seed > 0 ? cfg->seed : (int)time(0) + k) * 0x100000001B3ull;
+        for (size_t i = 0; i < nvox; i++) {
+            bmedia[moff + i] = (uint8_t)(cfg->vol[i] & 0x7Fu);
+        }
+        memcpy(bprop + 4 * (size_t)poff, cfg->prop, sizeof(float) * 4 * cfg->medianum);
+        moff += nvox;
+        foff += fieldlen;
+        voff += vts;
+        poff += cfg->medianum;
+        cfg->threadused = (unsigned int)vts;
+    }
+
+    mcxg_session* s = session_for(device);
+    if (!s) {
+        MCX_ERROR(-99, "failed to open a CUDA session on the selected GPU");
+    }
+    device_check(mcxg_batch_set(s, bdesc, sizeof(mcxg_simdesc), (uint32_t)n, bmedia, nmedia, bprop, nprop),
+                 "uploading the batch");
+    float kms = 0.f;
+    device_check(mcxg_batch_simulate(s, flags, &kms), "running the batch");
+    /* the volume and property copies are resident now; their slots take the
+       sums and the scales (every slot is freed on both exit paths) */
+    free(btmp[1]);
+    free(btmp[2]);
+    btmp[1] = NULL;
+    btmp[2] = malloc(sizeof(double) * (size_t)n);
+    double* scales = (double*)btmp[2];
+    bsums = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+    if (!bsums || !scales) {
+        MCX_ERROR(-2, "out of host memory");
+    }
+    device_check(mcxg_batch_get_energy(s, bsums), "reducing energies");
+    for (int k = 0; k < n; k++) {
+        Config* cfg = cfgs[k];
+        cfg->energyesc = bsums[2 * k];
+        cfg->energytot = bsums[2 * k + 1];
+        cfg->energyabs = 0.0;
+        cfg->kernelms = kms;
+        cfg->runtime = (unsigned int)(kms + 0.5f);
+        cfg->detectedcount = 0;
+        double sc = 1.0;
+        if (cfg->isnormalized) {
+            float Vvox = cfg->steps.x * cfg->steps.y * cfg->steps.z;
+            float f = 1.f;
+            cfg->energyabs = cfg->energytot - cfg->energyesc;
+            if (cfg->outputtype == otFlux || cfg->outputtype == otFluence) {
+                f = (float)(cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep));
+                if (cfg->outputtype == otFluence) {
+                    f *= cfg->tstep;
+                }
+            } else if (cfg->outputtype == otEnergy || cfg->outputtype == otL) {
+                f = (float)(1.0 / cfg->energytot);
+            }
+            cfg->normalizer = f;
+            cfg->his.normalizer = f;
+            sc = (double)f;
+        }
+        scales[k] = sc;
+        cfg->his.unitinmm = cfg->unitinmm;
+        cfg->his.totalphoton = (unsigned int)cfg->nphoton;
+    }
+    bfield = (float*)malloc(sizeof(float) * (nfield ? nfield : 1));
+    if (!bfield) {
+        MCX_ERROR(-2, "out of host memory");
+    }
+    device_check(mcxg_batch_get_field(s, bfield, scales), "reading the fields");
+    for (int k = 0; k < n; k++) {
+        Config* cfg = cfgs[k];
+        size_t len = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z * cfg->maxgate;
+        if (!cfg->exportfield) {
+            cfg->exportfield = (float*)calloc(len, sizeof(float));
+            if (!cfg->exportfield) {
+                MCX_ERROR(-2, "out of host memory");
+            }
+        }
+        const float* src = bfield + bdesc[k].field_off;
+        for (size_t i = 0; i < len; i++) {
+            cfg->exportfield[i] += src[i];
+        }
+    }
+    for (int i = 0; i < 5; i++) {
+        free(btmp[i]);
+        btmp[i] = NULL;
+    }
+#undef bdesc
+#undef bmedia
+#undef bprop
+#undef bfield
+#undef bsums
     MCX_LEAVE();
 }
 

@@ -40,6 +40,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "mcx_kparams.h"
 #include "mcx_launch.h"
 #include "mcx_pmath.cuh"
@@ -87,6 +89,45 @@ __constant__ float4 c_det[MCXG_MAX_DET];
 __constant__ float4 c_srcx[MCXG_MAX_EXTRASRC * 4];
 
 
+
+/* --------------------------------------------------------- parameter source
+ *
+ * Where the kernel reads its parameters.  One simulation keeps them in
+ * constant memory (ConstPS).  A batch of simulations (BatchPS) keeps one
+ * descriptor per simulation in global memory -- the parameter block plus the
+ * simulation's offsets into the batch's volume, field, property and
+ * reference-thread numbering -- and each thread follows the descriptor of the
+ * reference thread it is running.  Every device function that reads a
+ * parameter takes the source and binds `c_p` to it locally, so the physics
+ * code is the same text for both.
+ */
+struct ConstPS {
+    static constexpr bool kBatch = false;
+    __device__ __forceinline__ const mcxg_kparams& p() const { return c_p; }
+    __device__ __forceinline__ const float4* det() const { return c_det; }
+    __device__ __forceinline__ const float4* srcx() const { return c_srcx; }
+    __device__ __forceinline__ unsigned long long media_off() const { return 0ull; }
+    __device__ __forceinline__ unsigned int field_off() const { return 0u; }
+    __device__ __forceinline__ unsigned int lo_plane() const { return c_p.fieldlen; }
+    __device__ __forceinline__ unsigned long long vt_off() const { return 0ull; }
+    __device__ __forceinline__ unsigned int prop_off() const { return 0u; }
+    __device__ __forceinline__ unsigned long long seed() const { return 0ull; }
+};
+
+struct BatchPS {
+    static constexpr bool kBatch = true;
+    const mcxg_simdesc* d;
+    unsigned int lo;               /* low-plane offset: the batch's total field length */
+    __device__ __forceinline__ const mcxg_kparams& p() const { return d->kp; }
+    __device__ __forceinline__ const float4* det() const { return c_det; }   /* batches save no detectors */
+    __device__ __forceinline__ const float4* srcx() const { return c_srcx; } /* nor use extra sources */
+    __device__ __forceinline__ unsigned long long media_off() const { return d->media_off; }
+    __device__ __forceinline__ unsigned int field_off() const { return (unsigned int)d->field_off; }
+    __device__ __forceinline__ unsigned int lo_plane() const { return lo; }
+    __device__ __forceinline__ unsigned long long vt_off() const { return d->vt_off; }
+    __device__ __forceinline__ unsigned int prop_off() const { return d->prop_off; }
+    __device__ __forceinline__ unsigned long long seed() const { return d->seed; }
+};
 
 /* ------------------------------------------------------------------ math */
 
@@ -169,16 +210,21 @@ struct Shared {
     unsigned int stride;
 };
 
-__device__ __forceinline__ unsigned int media_at(const KArgs& a, unsigned int idx) {
+template <class PS>
+__device__ __forceinline__ unsigned int media_at(const KArgs& a, const PS& ps, unsigned int idx) {
+    const mcxg_kparams& c_p = ps.p();
+    const unsigned long long i = ps.media_off() + idx;
     if (c_p.mediaword == 1) {
-        unsigned int m = __ldg(a.media8 + idx);
+        unsigned int m = __ldg(a.media8 + i);
         return (m & 0x7Fu) | ((m & 0x80u) << 24);
     }
-    return __ldg(a.media32 + idx);
+    return __ldg(a.media32 + i);
 }
 
 /* updateproperty, mcx_core.cl:1079-1096 */
-__device__ __forceinline__ void updateprop(const Shared& S, float4& prop, unsigned int mediaid) {
+template <class PS>
+__device__ __forceinline__ void updateprop(const PS& ps, const Shared& S, float4& prop, unsigned int mediaid) {
+    const mcxg_kparams& c_p = ps.p();
     if (c_p.mediaformat <= 4) {
         prop = S.prop[mediaid & K_MED_MASK];
     } else {
@@ -187,12 +233,16 @@ __device__ __forceinline__ void updateprop(const Shared& S, float4& prop, unsign
     }
 }
 
-__device__ __forceinline__ bool inside_u(int x, int y, int z) {
+template <class PS>
+__device__ __forceinline__ bool inside_u(const PS& ps, int x, int y, int z) {
+    const mcxg_kparams& c_p = ps.p();
     return (float)(unsigned short)x < c_p.maxidx.x && (float)(unsigned short)y < c_p.maxidx.y &&
            (float)(unsigned short)z < c_p.maxidx.z;
 }
 
-__device__ __forceinline__ unsigned int vox_index(int x, int y, int z) {
+template <class PS>
+__device__ __forceinline__ unsigned int vox_index(const PS& ps, int x, int y, int z) {
+    const mcxg_kparams& c_p = ps.p();
     return (unsigned int)(z * (int)c_p.dimxy + y * (int)c_p.dimx + x);
 }
 
@@ -320,18 +370,19 @@ __device__ float reflectcoeff(const float4& v, float n1, float n2, int fw) {
 
 /* skipvoid, mcx_core.cl:1350-1455: march through background voxels to the
    first labelled voxel on the ray */
-template <bool EXACT>
-__device__ int skipvoid(const KArgs& a, const Shared& S, float4& p, float4& v, float4& f, int& fx, int& fy,
-                        int& fz, int& fw) {
+template <bool EXACT, class PS>
+__device__ int skipvoid(const KArgs& a, const PS& ps, const Shared& S, float4& p, float4& v, float4& f, int& fx,
+                        int& fy, int& fz, int& fw) {
+    const mcxg_kparams& c_p = ps.p();
     int count = 1;
     fx = (int)(short)floorf(p.x);
     fy = (int)(short)floorf(p.y);
     fz = (int)(short)floorf(p.z);
     fw = -1;
     for (;;) {
-        if (inside_u(fx, fy, fz)) {
-            int idx1d = (int)vox_index(fx, fy, fz);
-            if (media_at(a, idx1d) & K_MED_MASK) {
+        if (inside_u(ps, fx, fy, fz)) {
+            int idx1d = (int)vox_index(ps, fx, fy, fz);
+            if (media_at(a, ps, idx1d) & K_MED_MASK) {
                 p.x -= v.x;
                 p.y -= v.y;
                 p.z -= v.z;
@@ -339,9 +390,9 @@ __device__ int skipvoid(const KArgs& a, const Shared& S, float4& p, float4& v, f
                 fy = (int)(short)floorf(p.y);
                 fz = (int)(short)floorf(p.z);
                 f.y -= c_p.minaccumtime;
-                idx1d = (int)vox_index(fx, fy, fz);
+                idx1d = (int)vox_index(ps, fx, fy, fz);
                 count = 0;
-                while (!inside_u(fx, fy, fz) || !(media_at(a, idx1d) & K_MED_MASK)) {
+                while (!inside_u(ps, fx, fy, fz) || !(media_at(a, ps, idx1d) & K_MED_MASK)) {
                     float dist = hitgrid<EXACT>(p, v, fx, fy, fz, fw);
                     f.y += c_p.minaccumtime * dist;
                     p.x = p.x + dist * v.x;
@@ -356,16 +407,16 @@ __device__ int skipvoid(const KArgs& a, const Shared& S, float4& p, float4& v, f
                     if (fw == 2) {
                         fz += (v.z > 0.f ? 1 : -1);
                     }
-                    idx1d = (int)vox_index(fx, fy, fz);
+                    idx1d = (int)vox_index(ps, fx, fy, fz);
                     if (count++ > 3) {
                         break;
                     }
                 }
                 f.y = (c_p.voidtime) ? f.y : 0.f;
                 {
-                    unsigned int m = media_at(a, idx1d);
+                    unsigned int m = media_at(a, ps, idx1d);
                     float4 ht = make_float4(0.f, 0.f, 0.f, 0.f);
-                    updateprop(S, ht, m);
+                    updateprop(ps, S, ht, m);
                     /* ht.w is the entry voxel's index of refraction; the reference reads
                        gproperty[label].w, the same value for label volumes and an index past
                        the table for float-mua volumes */
@@ -398,7 +449,10 @@ __device__ int skipvoid(const KArgs& a, const Shared& S, float4& p, float4& v, f
 }
 
 /* finddetector, mcx_core.cl:838-850 */
-__device__ __forceinline__ unsigned int finddetector(const float4& p) {
+template <class PS>
+__device__ __forceinline__ unsigned int finddetector(const PS& ps, const float4& p) {
+    const mcxg_kparams& c_p = ps.p();
+    const float4* c_det = ps.det();
     for (unsigned int i = 0; i < c_p.detnum; i++) {
         float4 d = c_det[i];
         if ((d.x - p.x) * (d.x - p.x) + (d.y - p.y) * (d.y - p.y) + (d.z - p.z) * (d.z - p.z) < d.w * d.w) {
@@ -409,8 +463,10 @@ __device__ __forceinline__ unsigned int finddetector(const float4& p) {
 }
 
 /* savedetphoton, mcx_core.cl:867-926 */
-__device__ void savedetphoton(const KArgs& a, const Shared& S, Photon& s, unsigned int isdet) {
-    int detid = (isdet == K_OUT_MIN) ? -1 : (int)finddetector(s.p);
+template <class PS>
+__device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Photon& s, unsigned int isdet) {
+    const mcxg_kparams& c_p = ps.p();
+    int detid = (isdet == K_OUT_MIN) ? -1 : (int)finddetector(ps, s.p);
     if (!detid) {
         return;
     }
@@ -536,7 +592,9 @@ __device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, boo
 
 /* index of the photon a replay quantity belongs to: the reference's
    vt*threadphoton + min(vt, oddphoton-1) + offset (mcx_core.cl:1591, 2571, 2847) */
-__device__ __forceinline__ long long replay_index(unsigned int vt, long long offset) {
+template <class PS>
+__device__ __forceinline__ long long replay_index(const PS& ps, unsigned int vt, long long offset) {
+    const mcxg_kparams& c_p = ps.p();
     long long m = (long long)c_p.oddphoton - 1;
     long long t = (long long)vt;
     return t * (long long)c_p.threadphoton + (t < m ? t : m) + offset;
@@ -545,8 +603,10 @@ __device__ __forceinline__ long long replay_index(unsigned int vt, long long off
 /* replay deposit at a scattering site (mcx_core.cl:2567-2604): the detected
    weight (x (1 - cos theta) for the momentum-transfer output, x time of
    flight for wptof) into the gate of the photon's detected time of flight */
-__device__ void replay_site_deposit(const KArgs& a, const Photon& s, unsigned int vt, float ctheta) {
-    long long k = replay_index(vt, (long long)(int)s.f.w - 1 + (long long)c_p.siteshift);
+template <class PS>
+__device__ void replay_site_deposit(const KArgs& a, const PS& ps, const Photon& s, unsigned int vt, float ctheta) {
+    const mcxg_kparams& c_p = ps.p();
+    long long k = replay_index(ps, vt, (long long)(int)s.f.w - 1 + (long long)c_p.siteshift);
     if (k < 0 || k >= (long long)c_p.nreplay) {
         return;        /* the reference reads one photon past its arrays here */
     }
@@ -570,19 +630,21 @@ __device__ void replay_site_deposit(const KArgs& a, const Photon& s, unsigned in
         atomicAdd(a.status + ST_GUARD, 1u);
         return;
     }
-    field_add2(a.field, c_p.fieldlen, (unsigned int)key, tmp0);
+    field_add2(a.field, ps.lo_plane(), ps.field_off() + (unsigned int)key, tmp0);
 }
 
 /* ------------------------------------------------------------------ launch */
 
-__device__ __forceinline__ void set_launch_voxel(const KArgs& a, Photon& s) {
+template <class PS>
+__device__ __forceinline__ void set_launch_voxel(const KArgs& a, const PS& ps, Photon& s) {
+    const mcxg_kparams& c_p = ps.p();
     s.idx1d = (unsigned int)((int)(floorf(s.p.z)) * (int)c_p.dimxy + (int)(floorf(s.p.y)) * (int)c_p.dimx +
                              (int)(floorf(s.p.x)));
     if (s.p.x < 0.f || s.p.y < 0.f || s.p.z < 0.f || s.p.x >= c_p.maxidx.x || s.p.y >= c_p.maxidx.y ||
             s.p.z >= c_p.maxidx.z) {
         s.mediaid = 0;
     } else {
-        s.mediaid = media_at(a, s.idx1d);
+        s.mediaid = media_at(a, ps, s.idx1d);
     }
 }
 
@@ -592,9 +654,11 @@ __device__ __forceinline__ void set_launch_voxel(const KArgs& a, Photon& s) {
  * reference thread.  Returns 0 on launch, 1 when the thread's quota is done,
  * -1 when no launch position was found.
  */
-template <bool EXACT, bool DET>
-__device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsigned int isdet, unsigned int vt,
-                               unsigned long long* nfailed) {
+template <bool EXACT, bool DET, class PS>
+__device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Photon& s, unsigned int isdet,
+                               unsigned int vt, unsigned long long* nfailed) {
+    const mcxg_kparams& c_p = ps.p();
+    const float4* c_srcx = ps.srcx();
     typedef Mth<EXACT> M;
     s.w0 = 1.f;
     s.Lmove = -1.f;
@@ -613,10 +677,10 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
             if (c_p.extrasrclen && (c_p.srcid < 0)) {
                 tshift += ((int)s.srcsel - 1) * (int)c_p.maxgate;
             }
-            field_add2(a.field, c_p.fieldlen, s.idx1d + (unsigned int)tshift * c_p.nvox, -s.p.w);
+            field_add2(a.field, ps.lo_plane(), ps.field_off() + s.idx1d + (unsigned int)tshift * c_p.nvox, -s.p.w);
         }
         if (DET && c_p.savedet && (isdet & K_DET_MASK) == K_DET_MASK && s.mediaid == 0 && c_p.issaveref < 2) {
-            savedetphoton(a, S, s, isdet);
+            savedetphoton(a, ps, S, s, isdet);
         }
     }
     if (DET) {
@@ -631,7 +695,7 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
 
     if (c_p.replay) {
         /* the saved launch state of this photon (mcx_core.cl:1590-1596) */
-        long long k = replay_index(vt, (long long)((int)s.f.w > 0 ? (int)s.f.w : 0));
+        long long k = replay_index(ps, vt, (long long)((int)s.f.w > 0 ? (int)s.f.w : 0));
         if (k < 0 || k >= (long long)c_p.nreplay) {
             atomicAdd(a.status + ST_GUARD, 1u);
             return 1;
@@ -717,7 +781,7 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
                 s.p.y = lpos.y + floorf(rx * lp1.w) * lp1.y / (lp1.w - 1.f) + floorf(ry * lp2.w) * lp2.y / (lp2.w - 1.f);
                 s.p.z = lpos.z + floorf(rx * lp1.w) * lp1.z / (lp1.w - 1.f) + floorf(ry * lp2.w) * lp2.z / (lp2.w - 1.f);
             }
-            set_launch_voxel(a, s);
+            set_launch_voxel(a, ps, s);
             s.prop.x = s.prop.x + (lp1.x + lp2.x) * 0.5f;
             s.prop.y = s.prop.y + (lp1.y + lp2.y) * 0.5f;
             s.prop.z = s.prop.z + (lp1.z + lp2.z) * 0.5f;
@@ -738,7 +802,7 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
             } else {
                 s.p.w = lpos.w * (M::cos((lp2.x * rx + lp2.y * ry + lp2.z) * K_TWO_PI) * (1.f - lp2.w) + 1.f) * 0.5f;
             }
-            set_launch_voxel(a, s);
+            set_launch_voxel(a, ps, s);
             s.prop.x = s.prop.x + (lp1.x + v2.x) * 0.5f;
             s.prop.y = s.prop.y + (lp1.y + v2.y) * 0.5f;
             s.prop.z = s.prop.z + (lp1.z + v2.z) * 0.5f;
@@ -821,7 +885,7 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
                 s.p.x += r * cphi;
                 s.p.y += r * sphi;
             }
-            set_launch_voxel(a, s);
+            set_launch_voxel(a, ps, s);
         } else if (st == S_CONE || st == S_ISOTROPIC || st == S_ARCSINE) {
             float ang, sth, cth, sphi, cphi;
             ang = K_TWO_PI * rnd(s.t);
@@ -907,7 +971,7 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
                     s.v.z *= r_l;
                 }
             }
-            set_launch_voxel(a, s);
+            set_launch_voxel(a, ps, s);
             s.prop = make_float4(lpos.x + (lp1.x) * 0.5f, lpos.y + (lp1.y) * 0.5f, lpos.z + (lp1.z) * 0.5f, 0.f);
             s.Lmove = -1.f;
         }
@@ -968,10 +1032,10 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
         }
 
         if ((s.mediaid & K_MED_MASK) == 0) {
-            int idx = skipvoid<EXACT>(a, S, s.p, s.v, s.f, s.fx, s.fy, s.fz, s.fw);
+            int idx = skipvoid<EXACT>(a, ps, S, s.p, s.v, s.f, s.fx, s.fy, s.fz, s.fw);
             if (idx >= 0) {
                 s.idx1d = (unsigned int)idx;
-                s.mediaid = media_at(a, s.idx1d);
+                s.mediaid = media_at(a, ps, s.idx1d);
             }
         }
         s.fx = (int)(short)floorf(s.p.x);
@@ -990,7 +1054,7 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
 
     s.f.w += 1.f;
     s.prop = S.prop[1];
-    updateprop(S, s.prop, s.mediaid);
+    updateprop(ps, S, s.prop, s.mediaid);
     s.launched += s.p.w;
     s.w0 = s.p.w;
     s.w0init = s.p.w;
@@ -1002,12 +1066,25 @@ __device__ int launchnewphoton(const KArgs& a, const Shared& S, Photon& s, unsig
 /* ------------------------------------------------------------------ kernel */
 
 /* exit flag of a relaunch through a detecting face (mcx_core.cl:3001, 3181) */
-__device__ __forceinline__ unsigned int exit_detflag(const Photon& s, unsigned int mediaidold) {
+template <class PS>
+__device__ __forceinline__ unsigned int exit_detflag(const PS& ps, const Photon& s, unsigned int mediaidold) {
+    const mcxg_kparams& c_p = ps.p();
     return (((s.idx1d == K_OUT_MAX && c_p.bc[9 + s.fw]) || (s.idx1d == K_OUT_MIN && c_p.bc[6 + s.fw]))
             ? K_OUT_MIN : (mediaidold & K_DET_MASK));
 }
 
-__device__ __forceinline__ void vt_begin(const KArgs& a, Photon& s, unsigned int vt) {
+/* splitmix64 (Steele, Lea and Flood, "Fast splittable pseudorandom number
+   generators", OOPSLA 2014): seeds of a batch's reference threads */
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+template <class PS>
+__device__ __forceinline__ void vt_begin(const KArgs& a, const PS& ps, Photon& s, unsigned int vt) {
+    const mcxg_kparams& c_p = ps.p();
     s.p = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7fffffff));
     s.v = make_float4(0.f, 0.f, 0.f, 0.f);
     s.f = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1021,51 +1098,94 @@ __device__ __forceinline__ void vt_begin(const KArgs& a, Photon& s, unsigned int
     s.launched = 0.f;
     s.w0init = 0.f;
     s.srcsel = 0.f;
-    uint4 sd = __ldg(a.seeds + vt);
-    s.t.a = (unsigned long long)sd.x << 32 | sd.y;
-    s.t.b = (unsigned long long)sd.z << 32 | sd.w;
+    if (PS::kBatch) {
+        const unsigned long long k = ps.seed() ^ ((unsigned long long)vt << 1);
+        s.t.a = splitmix64(k);
+        s.t.b = splitmix64(k ^ 0xD1B54A32D192ED03ull);
+    } else {
+        uint4 sd = __ldg(a.seeds + vt);
+        s.t.a = (unsigned long long)sd.x << 32 | sd.y;
+        s.t.b = (unsigned long long)sd.z << 32 | sd.w;
+    }
 }
 
-template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB>
+/* Next reference thread for this GPU thread: a global counter over the
+   single simulation's threads, or over the concatenated threads of a batch
+   (the simulation found by binary search in the prefix of thread counts). */
+__device__ __forceinline__ bool claim_vt(const KArgs& a, ConstPS&, unsigned int& vt) {
+    vt = atomicAdd(a.vtcounter, 1u);
+    return vt < c_p.nthread;
+}
+
+__device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPS& ps, unsigned int& vt) {
+    const unsigned long long g = atomicAdd(a.vtcounter, 1u);
+    if (g >= a.totalvt) {
+        return false;
+    }
+    unsigned int lo = 0, hi = a.nsim;          /* simvt[lo] <= g < simvt[hi] */
+    while (hi - lo > 1) {
+        const unsigned int mid = (lo + hi) >> 1;
+        if (__ldg(a.simvt + mid) <= g) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    ps.d = a.sims + lo;
+    vt = (unsigned int)(g - __ldg(a.simvt + lo));
+    return true;
+}
+
+template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
+    typedef typename std::conditional<BATCH, BatchPS, ConstPS>::type PS;
     extern __shared__ float4 smem4[];
 
-    /* stage the property table and inverse-CDF tables */
-    float4* sprop = smem4;
-    for (unsigned int i = threadIdx.x; i < c_p.medianum; i += blockDim.x) {
-        sprop[i] = a.gprop[i];
-    }
-    float4* srecip = smem4 + c_p.medianum;
-    for (unsigned int i = threadIdx.x; i < c_p.medianum; i += blockDim.x) {
-        float4 q = a.gprop[i];
-        /* __fdividef(x, y) is x * rcp(y): keeping rcp(y) per medium gives the
-           fast kernel the same bits with one MUFU op fewer per use */
-        srecip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x), 0.f);
-    }
-    float* sf = (float*)(smem4 + 2 * c_p.medianum);
-    float* sinvcdf = sf;
-    for (unsigned int i = threadIdx.x; i < c_p.nphase; i += blockDim.x) {
-        sinvcdf[i] = a.invcdf[i];
-    }
-    float* sangle = sinvcdf + c_p.nphase;
-    for (unsigned int i = threadIdx.x; i < c_p.nangle; i += blockDim.x) {
-        sangle[i] = a.angleinvcdf[i];
-    }
-    __syncthreads();
-
+    PS ps;
     Shared S;
-    S.prop = sprop;
-    S.recip = srecip;
-    S.invcdf = sinvcdf;
-    S.angleinvcdf = sangle;
-    S.pp = sangle + c_p.nangle + threadIdx.x;
+    if (!BATCH) {
+        /* stage the property table and inverse-CDF tables */
+        float4* sprop = smem4;
+        for (unsigned int i = threadIdx.x; i < c_p.medianum; i += blockDim.x) {
+            sprop[i] = a.gprop[i];
+        }
+        float4* srecip = smem4 + c_p.medianum;
+        for (unsigned int i = threadIdx.x; i < c_p.medianum; i += blockDim.x) {
+            float4 q = a.gprop[i];
+            /* __fdividef(x, y) is x * rcp(y): keeping rcp(y) per medium gives the
+               fast kernel the same bits with one MUFU op fewer per use */
+            srecip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x), 0.f);
+        }
+        float* sf = (float*)(smem4 + 2 * c_p.medianum);
+        float* sinvcdf = sf;
+        for (unsigned int i = threadIdx.x; i < c_p.nphase; i += blockDim.x) {
+            sinvcdf[i] = a.invcdf[i];
+        }
+        float* sangle = sinvcdf + c_p.nphase;
+        for (unsigned int i = threadIdx.x; i < c_p.nangle; i += blockDim.x) {
+            sangle[i] = a.angleinvcdf[i];
+        }
+        __syncthreads();
+        S.prop = sprop;
+        S.recip = srecip;
+        S.invcdf = sinvcdf;
+        S.angleinvcdf = sangle;
+        S.pp = sangle + c_p.nangle + threadIdx.x;
+    } else {
+        /* a batch reads each simulation's tables from global memory (L1-resident):
+           the threads of a block run different simulations */
+        S.prop = S.recip = a.gprop;
+        S.invcdf = S.angleinvcdf = a.invcdf;
+        S.pp = (float*)smem4;
+    }
     S.stride = blockDim.x;
 
     unsigned long long cnt_step = 0, cnt_scat = 0, cnt_launch = 0, cnt_refl = 0, cnt_fail = 0;
 
     Photon s;
-    unsigned int vt = atomicAdd(a.vtcounter, 1u);
+    unsigned int vt = 0;
+    bool claimed = claim_vt(a, ps, vt);
     bool relaunch = false;         /* a relaunch request from the previous step */
     unsigned int relaunch_isdet = 0;
     bool fresh = true;             /* vt just claimed: initial launch */
@@ -1077,32 +1197,37 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     pd.old = pd.w = 0.f;
     float3 rv = make_float3(0.f, 0.f, 0.f);   /* fast kernel: rcp of the direction */
     bool vdirty = true;
-    const float gscat = (float)c_p.gscatter;
 
-    while (vt < c_p.nthread) {
+    while (claimed) {
+        const mcxg_kparams& c_p = ps.p();
+        const float gscat = (float)c_p.gscatter;
         if (fresh || relaunch) {
             int r;
             if (fresh) {
-                vt_begin(a, s, vt);
+                if (BATCH) {
+                    S.prop = a.gprop + ps.prop_off();
+                    S.recip = a.grecip + ps.prop_off();
+                }
+                vt_begin(a, ps, s, vt);
                 if ((unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
                     r = 1;
                 } else {
-                    r = launchnewphoton<EXACT, DET>(a, S, s, 0u, vt, &cnt_fail);
+                    r = launchnewphoton<EXACT, DET>(a, ps, S, s, 0u, vt, &cnt_fail);
                     if (r) {
                         atomicAdd(a.status + ST_FAILED_LAUNCH, 1u);
                         r = 2;       /* NO_LAUNCH: the reference returns without writing energies */
                     }
                 }
             } else {
-                r = launchnewphoton<EXACT, DET>(a, S, s, relaunch_isdet, vt, &cnt_fail);
+                r = launchnewphoton<EXACT, DET>(a, ps, S, s, relaunch_isdet, vt, &cnt_fail);
             }
             fresh = false;
             relaunch = false;
             if (r) {
                 if (r != 2) {
-                    a.energy[vt] = make_float2(s.esc, s.launched);
+                    a.energy[ps.vt_off() + vt] = make_float2(s.esc, s.launched);
                 }
-                vt = atomicAdd(a.vtcounter, 1u);
+                claimed = claim_vt(a, ps, vt);
                 fresh = true;
                 continue;
             }
@@ -1193,14 +1318,14 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 s.v.w += 1.f;
                 vdirty = true;
                 if (c_p.replay && (c_p.outputtype == otWP || c_p.outputtype == otDCS || c_p.outputtype == otWPTOF)) {
-                    replay_site_deposit(a, s, vt, ctheta);
+                    replay_site_deposit(a, ps, s, vt, ctheta);
                 }
             }
             s.v.w = (float)(int)s.v.w;
         }
 
         s.n1 = s.prop.w;
-        updateprop(S, s.prop, s.mediaid);
+        updateprop(ps, S, s.prop, s.mediaid);
 
         /* ---- move to the next voxel face or the end of the free path */
         if (EXACT) {
@@ -1247,14 +1372,14 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         /* ---- new voxel (mcx_core.cl:2795-2811) */
         mediaidold = s.mediaid | s.isdet;
         idx1dold = s.idx1d;
-        s.idx1d = vox_index(s.fx, s.fy, s.fz);
-        if (!inside_u(s.fx, s.fy, s.fz)) {
+        s.idx1d = vox_index(ps, s.fx, s.fy, s.fz);
+        if (!inside_u(ps, s.fx, s.fy, s.fz)) {
             s.mediaid = 0;
             s.idx1d = (s.fx < 0 || s.fy < 0 || s.fz < 0) ? K_OUT_MIN : K_OUT_MAX;
             s.isdet = c_p.bc[(s.idx1d == K_OUT_MAX) * 3 + s.fw];
             s.isdet = ((s.isdet & 0xF) == bcUnknown) ? (c_p.doreflect ? bcReflect : bcAbsorb) : s.isdet;
         } else {
-            s.mediaid = media_at(a, s.idx1d);
+            s.mediaid = media_at(a, ps, s.idx1d);
             s.isdet = s.mediaid & K_DET_MASK;
             s.mediaid &= K_MED_MASK;
         }
@@ -1281,7 +1406,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         /* replay Jacobian (mcx_core.cl:2845-2858): detected weight times
                            the path length in the voxel, gated by the detected time of flight */
                         if (c_p.outputtype == otJacobian || c_p.outputtype == otWLTOF) {
-                            long long k = replay_index(vt, (long long)(int)s.f.w - 1);
+                            long long k = replay_index(ps, vt, (long long)(int)s.f.w - 1);
                             if (k >= 0 && k < (long long)c_p.nreplay) {
                                 float rt = __ldg(a.rtof + k);
                                 int d = __ldg(a.rdetid + k) & 0xFFFF;
@@ -1320,7 +1445,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             } else {
                 s.mediaid = mediaidold;
             }
-            deposit<WAGG>(a.field, c_p.fieldlen, dep, key, weight, pd);
+            deposit<WAGG>(a.field, ps.lo_plane(), dep, ps.field_off() + key, weight, pd);
         }
 
         /* ---- exit, time-out or cyclic boundary (mcx_core.cl:2958-3028) */
@@ -1339,16 +1464,16 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     s.p.z = nextafter_ref(rintf(((s.idx1d == K_OUT_MIN) ? c_p.maxidx.z : 0)), (s.v.z > 0.f) - (s.v.z < 0.f));
                     s.fz = (int)(short)floorf(s.p.z);
                 }
-                if (inside_u(s.fx, s.fy, s.fz)) {
-                    s.idx1d = vox_index(s.fx, s.fy, s.fz);
-                    s.mediaid = media_at(a, s.idx1d);
+                if (inside_u(ps, s.fx, s.fy, s.fz)) {
+                    s.idx1d = vox_index(ps, s.fx, s.fy, s.fz);
+                    s.mediaid = media_at(a, ps, s.idx1d);
                     s.isdet = s.mediaid & K_DET_MASK;
                     s.mediaid &= K_MED_MASK;
                     continue;
                 }
             }
             relaunch = true;
-            relaunch_isdet = exit_detflag(s, mediaidold);
+            relaunch_isdet = exit_detflag(ps, s, mediaidold);
             continue;
         }
 
@@ -1365,7 +1490,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
 
         /* ---- Fresnel reflection / refraction (mcx_core.cl:3126-3278) */
         if (REFL && c_p.dorefl_compiled) {
-            updateprop(S, s.prop, s.mediaid);
+            updateprop(ps, S, s.prop, s.mediaid);
             if (((s.mediaid && c_p.doreflect) ||
                  (s.mediaid == 0 && (((s.isdet & 0xF) == bcUnknown && c_p.doreflect) ||
                                      ((s.isdet & 0xF) == bcReflect || (s.isdet & 0xF) == bcMirror)))) &&
@@ -1393,7 +1518,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     transmit<EXACT>(s.v, s.n1, s.prop.w, s.fw);
                     if (s.mediaid == 0) {
                         relaunch = true;
-                        relaunch_isdet = exit_detflag(s, mediaidold);
+                        relaunch_isdet = exit_detflag(ps, s, mediaidold);
                         continue;
                     }
                 } else {
@@ -1418,20 +1543,20 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         continue;
                     }
                     s.idx1d = idx1dold;
-                    unsigned int m = media_at(a, s.idx1d);
+                    unsigned int m = media_at(a, ps, s.idx1d);
                     s.mediaid = m & K_MED_MASK;
                     /* take the detector bit of the voxel the photon is back in (the
                        reference keeps the face code here, which mcx_core.cl:2796 then
                        ORs into the medium index) */
                     s.isdet = m & K_DET_MASK;
-                    updateprop(S, s.prop, s.mediaid);
+                    updateprop(ps, S, s.prop, s.mediaid);
                     s.n1 = s.prop.w;
                 }
             }
         }
     }
 
-    pend_complete(a.field, c_p.fieldlen, pd);
+    pend_complete(a.field, ps.lo_plane(), pd);
     if (COUNT) {
         atomicAdd(a.counters + 0, cnt_step);
         atomicAdd(a.counters + 1, cnt_scat);

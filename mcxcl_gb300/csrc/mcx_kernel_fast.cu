@@ -26,8 +26,21 @@ static void* kfun(bool occ3) {
            : (void*)mcx_transport<false, DET, REFL, WAGG, false, 2>;
 }
 
+/* a batch of simulations: no detectors, parameters per simulation in global memory */
+template <bool REFL, bool WAGG>
+static void* kbatch(bool occ3) {
+    return occ3 ? (void*)mcx_transport<false, false, REFL, WAGG, false, 3, true>
+           : (void*)mcx_transport<false, false, REFL, WAGG, false, 2, true>;
+}
+
 static void* select(int flags) {
     const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    if (flags & LF_BATCH) {
+        if (wagg) {
+            return refl ? kbatch<true, true>(o3) : kbatch<false, true>(o3);
+        }
+        return refl ? kbatch<true, false>(o3) : kbatch<false, false>(o3);
+    }
     if (wagg) {
         if (det) {
             return refl ? kfun<true, true, true>(o3) : kfun<true, false, true>(o3);

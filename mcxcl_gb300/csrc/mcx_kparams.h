@@ -68,4 +68,17 @@ typedef struct mcxg_kparams {
     uint32_t siteshift;            /* scattering-site replay deposits read photon k+siteshift (the reference: 1) */
 } mcxg_kparams;
 
+/* One simulation of a batch: its parameter block (nthread = its reference
+   threads, fieldlen = its own field) and where its data sit in the batch's
+   concatenated buffers. */
+typedef struct mcxg_simdesc {
+    mcxg_kparams kp;
+    uint64_t media_off;            /* first voxel in the batch volume */
+    uint64_t field_off;            /* first element in the batch field planes */
+    uint64_t vt_off;               /* first reference thread in the batch numbering */
+    uint64_t seed;                 /* seeds of its reference threads: splitmix64 of seed ^ (vt << 1) */
+    uint32_t prop_off;             /* first row in the batch property table */
+    uint32_t pad;
+} mcxg_simdesc;
+
 #endif

@@ -35,10 +35,18 @@ struct KArgs {
     const float* rweight;
     const float* rtof;
     const int* rdetid;
+    /* batch: per-simulation descriptors, the prefix of their reference-thread
+       counts (nsim + 1 entries), the concatenated property rows and their
+       reciprocals (fast kernel) */
+    const mcxg_simdesc* sims;
+    const unsigned long long* simvt;
+    unsigned int nsim;
+    unsigned long long totalvt;
+    const float4* grecip;
 };
 
 /* flag bits for the launch entries */
-enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8 };
+enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_BATCH = 16 };
 
 /* fast instantiation: hardware transcendental approximations */
 cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,

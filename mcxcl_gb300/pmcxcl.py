@@ -305,6 +305,30 @@ def run(cfg=None, **kwargs):
         L.mcx_clearcfg(ctypes.byref(C))
 
 
+def run_batch(cfgs, photons_per_thread=64, graph=False, aggregate=False):
+    """Run many simulations in one persistent launch (a GB300 addition).
+
+    cfgs: a list of run() dictionaries (label volumes, no detectors).  Returns
+    the list of their output dictionaries, as run() would give one by one.
+    photons_per_thread sets how many photons each reference thread (RNG
+    stream) runs; graph=True captures the launch as a CUDA graph."""
+    L = _lib.load()
+    Cs = [Config() for _ in cfgs]
+    try:
+        for cfg, C in zip(cfgs, Cs):
+            parse_config(dict(cfg), C)
+            L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
+            _check(C)
+        arr = (ctypes.POINTER(Config) * len(Cs))(*[ctypes.pointer(C) for C in Cs])
+        flags = (32 if graph else 0) | (16 if aggregate else 0)
+        L.mcx_run_batch(arr, len(Cs), ctypes.c_uint(int(photons_per_thread)), ctypes.c_uint(flags))
+        _check(Cs[0])
+        return [_outputs(cfg, C) for cfg, C in zip(cfgs, Cs)]
+    finally:
+        for C in Cs:
+            L.mcx_clearcfg(ctypes.byref(C))
+
+
 def _outputs(cfg, C):
     """Assemble the output dictionary (src/pmcxcl.cpp:1263-1521)."""
     L = _lib.load()

@@ -138,5 +138,40 @@ def diff_config(n=100, nphoton=10000000, seed=2024):
     return cfg, np.maximum(mua, 1e-4), np.maximum(target, 1e-4)
 
 
+def batch_configs(nsim=512, master_seed=7, edge=(32, 128), photons=(1e5, 1e7)):
+    """Batch workload: nsim independent cubes with an integer edge uniform in
+    [edge], with probability 0.5 a spherical inclusion of random centre and
+    radius; mua log-uniform in [0.001, 0.1]/mm, mus uniform in [0.5, 2.0]/mm,
+    g uniform in [0.6, 0.95], n uniform in [1.33, 1.45] (inclusion drawn the
+    same way); photon counts log-uniform in [photons]; pencil source at the
+    centre of the z = 0 face; one 5 ns gate.  Seeds come from numpy's
+    SeedSequence(master_seed).spawn(nsim)."""
+    seqs = np.random.SeedSequence(master_seed).spawn(nsim)
+    out = []
+    for k, ss in enumerate(seqs):
+        rng = np.random.default_rng(ss)
+        n = int(rng.integers(edge[0], edge[1] + 1))
+
+        def medium():
+            return [float(np.exp(rng.uniform(np.log(1e-3), np.log(1e-1)))), float(rng.uniform(0.5, 2.0)),
+                    float(rng.uniform(0.6, 0.95)), float(rng.uniform(1.33, 1.45))]
+        prop = [[0, 0, 1, 1], medium()]
+        vol = np.ones((n, n, n), np.uint8)
+        if rng.random() < 0.5:
+            r = float(rng.uniform(0.1, 0.3)) * n
+            c = rng.uniform(r, n - r, size=3)
+            idx = np.arange(n) + 0.5
+            x, y, z = np.meshgrid(idx, idx, idx, indexing="ij")
+            vol[(x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 < r * r] = 2
+            prop.append(medium())
+        nph = int(np.exp(rng.uniform(np.log(photons[0]), np.log(photons[1]))))
+        out.append({
+            "nphoton": nph, "vol": vol, "prop": prop, "tstart": 0, "tend": 5e-9, "tstep": 5e-9,
+            "srcpos": [n / 2.0, n / 2.0, 0], "srcdir": [0, 0, 1], "issrcfrom0": 1, "isreflect": 1,
+            "issavedet": 0, "seed": int(rng.integers(1, 2 ** 31 - 1)), "session": "batch%d" % k,
+        })
+    return out
+
+
 def copy_cfg(cfg):
     return copy.deepcopy(cfg)
