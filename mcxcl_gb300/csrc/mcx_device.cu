@@ -208,7 +208,8 @@ __global__ void field_merge_blocks(const float* __restrict__ f, size_t n, size_t
 __global__ void batch_recip(const float4* __restrict__ prop, unsigned int n, float4* __restrict__ recip) {
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 q = prop[i];
-        recip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x), 0.f);
+        recip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x),
+                               __fdividef(1.f, 2.f * q.z));
     }
 }
 
@@ -293,9 +294,12 @@ int grid_for(const mcxg_session* s, size_t n) {
     return g < 1 ? 1 : (int)g;
 }
 
+/* property rows and their reciprocals (2 x 16 B per medium), 32 B of
+   launch-time state per thread, the phase tables, and the detector partial
+   data per thread */
 size_t shared_bytes(const mcxg_kparams& kp, int block) {
     size_t det = (kp.savedet ? kp.partialdata : 0);
-    return (size_t)kp.medianum * 32 + (size_t)(kp.nphase + kp.nangle) * 4 + det * (size_t)block * 4;
+    return (size_t)kp.medianum * 32 + (size_t)block * 32 + (size_t)(kp.nphase + kp.nangle) * 4 + det * (size_t)block * 4;
 }
 
 }  // namespace
@@ -976,7 +980,7 @@ int batch_enqueue(mcxg_session* s, int lflags) {
     a.simvt = s->d_simvt;
     a.nsim = s->nsim;
     a.totalvt = s->totalvt;
-    MCXG_TRY(mcxg::fast_launch(a, lflags, s->bt_grid, s->bt_block, 0, s->st));
+    MCXG_TRY(mcxg::fast_launch(a, lflags, s->bt_grid, s->bt_block, (size_t)s->bt_block * 32, s->st));
     batch_energy<<<s->nsim, 256, 0, s->st>>>(s->d_benergy, s->d_sims, s->d_bsum);
     return MCXG_OK;
 }
@@ -1067,7 +1071,7 @@ int mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
                  (bpsm_req == 3 ? mcxg::LF_OCC3 : 0);
     int block = s->block_req ? s->block_req : 256;
     int occ = 0;
-    MCXG_TRY(mcxg::fast_occupancy(lflags, block, 0, &occ));
+    MCXG_TRY(mcxg::fast_occupancy(lflags, block, (size_t)block * 32, &occ));
     int bpsm = std::max(1, std::min(bpsm_req, occ > 0 ? occ : bpsm_req));
     const int grid = s->info.sm * bpsm;
     if (grid != s->bt_grid || block != s->bt_block) {

@@ -756,6 +756,8 @@ static void make_kparams(const Config* cfg, size_t nvox, size_t fieldlen, size_t
     kp->srcparam2 = (mcxg_float4) {cfg->srcparam2.x, cfg->srcparam2.y, cfg->srcparam2.z, cfg->srcparam2.w};
     kp->maxidx = (mcxg_float4) {(float)cfg->dim.x, (float)cfg->dim.y, (float)cfg->dim.z, 0.f};
     kp->dimx = cfg->dim.x;
+    kp->dimy = cfg->dim.y;
+    kp->dimz = cfg->dim.z;
     kp->dimxy = cfg->dim.x * cfg->dim.y;
     kp->nvox = (uint32_t)nvox;
     kp->fieldlen = (uint32_t)fieldlen;

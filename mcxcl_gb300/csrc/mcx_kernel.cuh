@@ -196,9 +196,15 @@ struct Photon {
     int fx, fy, fz, fw;            /* voxel index and last crossed face (the reference's short4 flipdir) */
     unsigned int idx1d, mediaid, isdet;
     float w0, Lmove, pathlen, n1;
-    float esc, launched, w0init, srcsel;   /* reference ppath[partialdata .. +3] */
     Rng t;
+};
+
+/* Per-thread state written at a launch and read only at a detection or at
+   the end of the reference thread: kept in shared memory, out of the
+   registers of the step loop. */
+struct ColdState {
     unsigned long long ps0, ps1;   /* RNG state at launch, saved with detected photons */
+    float esc, launched, w0init, srcsel;   /* reference ppath[partialdata .. +3] */
 };
 
 struct Shared {
@@ -208,6 +214,7 @@ struct Shared {
     const float* angleinvcdf;
     float* pp;                     /* this thread's partial data, stride blockDim.x */
     unsigned int stride;
+    ColdState* cold;               /* this thread's launch-time state */
 };
 
 template <class PS>
@@ -233,11 +240,13 @@ __device__ __forceinline__ void updateprop(const PS& ps, const Shared& S, float4
     }
 }
 
+/* the reference's (ushort)flipdir < maxidx test (mcx_core.cl:2803) in
+   integers: the voxel index wrapped to 16 bits against the extent */
 template <class PS>
 __device__ __forceinline__ bool inside_u(const PS& ps, int x, int y, int z) {
     const mcxg_kparams& c_p = ps.p();
-    return (float)(unsigned short)x < c_p.maxidx.x && (float)(unsigned short)y < c_p.maxidx.y &&
-           (float)(unsigned short)z < c_p.maxidx.z;
+    return ((unsigned int)x & 0xFFFFu) < c_p.dimx && ((unsigned int)y & 0xFFFFu) < c_p.dimy &&
+           ((unsigned int)z & 0xFFFFu) < c_p.dimz;
 }
 
 template <class PS>
@@ -473,14 +482,14 @@ __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Pho
     unsigned int slot = atomicAdd(a.detcount, 1u);
     if (slot < c_p.maxdetphoton) {
         if (c_p.issaveseed) {
-            a.detseed[slot * 2] = s.ps0;
-            a.detseed[slot * 2 + 1] = s.ps1;
+            a.detseed[slot * 2] = S.cold->ps0;
+            a.detseed[slot * 2 + 1] = S.cold->ps1;
         }
         float* rec = a.detp + (size_t)slot * c_p.reclen;
         unsigned int k = 0;
         if (SAVE_DETID(c_p.savedetflag)) {
             if (c_p.extrasrclen && (c_p.srcid <= 0)) {
-                detid |= (((int)s.srcsel) << 16);
+                detid |= (((int)S.cold->srcsel) << 16);
             }
             rec[k++] = (float)detid;
         }
@@ -498,7 +507,7 @@ __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Pho
             rec[k++] = s.v.z;
         }
         if (SAVE_W0(c_p.savedetflag)) {
-            rec[k++] = s.w0init;
+            rec[k++] = S.cold->w0init;
         }
         if (a.detw) {
             a.detw[slot] = make_float2(s.p.w, s.f.y);
@@ -604,7 +613,8 @@ __device__ __forceinline__ long long replay_index(const PS& ps, unsigned int vt,
    weight (x (1 - cos theta) for the momentum-transfer output, x time of
    flight for wptof) into the gate of the photon's detected time of flight */
 template <class PS>
-__device__ void replay_site_deposit(const KArgs& a, const PS& ps, const Photon& s, unsigned int vt, float ctheta) {
+__device__ void replay_site_deposit(const KArgs& a, const PS& ps, const Shared& S, const Photon& s, unsigned int vt,
+                                    float ctheta) {
     const mcxg_kparams& c_p = ps.p();
     long long k = replay_index(ps, vt, (long long)(int)s.f.w - 1 + (long long)c_p.siteshift);
     if (k < 0 || k >= (long long)c_p.nreplay) {
@@ -622,7 +632,7 @@ __device__ void replay_site_deposit(const KArgs& a, const PS& ps, const Photon& 
     int tshift = (int)(floorf((rt - c_p.twin0) * c_p.Rtstep)) +
                  ((c_p.replaydet == -1) ? (((__ldg(a.rdetid + k) & 0xFFFF) - 1) * (int)c_p.maxgate) : 0);
     if (c_p.extrasrclen && (c_p.srcid < 0)) {
-        tshift += ((int)s.srcsel - 1) * ((c_p.replaydet == -1) ? (int)c_p.detnum : 1) * (int)c_p.maxgate;
+        tshift += ((int)S.cold->srcsel - 1) * ((c_p.replaydet == -1) ? (int)c_p.detnum : 1) * (int)c_p.maxgate;
     }
     tshift = ((int)c_p.maxgate - 1 < tshift) ? (int)c_p.maxgate - 1 : tshift;
     long long key = (long long)s.idx1d + (long long)tshift * c_p.nvox;
@@ -668,14 +678,14 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     }
 
     if (fabsf(s.p.w) >= 0.f) {
-        s.esc += s.p.w;
+        S.cold->esc += s.p.w;
         if (s.mediaid == 0 && s.idx1d != K_OUT_MIN && s.idx1d != K_OUT_MAX && c_p.issaveref && s.p.w > 0.f) {
             int tshift = (int)floorf((s.f.y - c_p.twin0) * c_p.Rtstep);
             if ((int)c_p.maxgate - 1 < tshift) {
                 tshift = (int)c_p.maxgate - 1;
             }
             if (c_p.extrasrclen && (c_p.srcid < 0)) {
-                tshift += ((int)s.srcsel - 1) * (int)c_p.maxgate;
+                tshift += ((int)S.cold->srcsel - 1) * (int)c_p.maxgate;
             }
             field_add2(a.field, ps.lo_plane(), ps.field_off() + s.idx1d + (unsigned int)tshift * c_p.nvox, -s.p.w);
         }
@@ -706,8 +716,8 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     }
 
     if (DET && c_p.issaveseed) {
-        s.ps0 = s.t.a;
-        s.ps1 = s.t.b;
+        S.cold->ps0 = s.t.a;
+        S.cold->ps1 = s.t.b;
     }
 
     float4 lpos = f4(c_p.srcpos), ldir = f4(c_p.srcdir), lp1 = f4(c_p.srcparam1), lp2 = f4(c_p.srcparam2);
@@ -716,9 +726,9 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
         if (c_p.srcid > 1) {
             sel = c_p.srcid - 2;
         } else {
-            s.srcsel = (float)((int)(rnd(s.t) * K_JUST_BELOW_ONE * (float)(c_p.extrasrclen + 1)) + 1);
-            if ((int)s.srcsel > 1) {
-                sel = (int)(s.srcsel - 2);
+            S.cold->srcsel = (float)((int)(rnd(s.t) * K_JUST_BELOW_ONE * (float)(c_p.extrasrclen + 1)) + 1);
+            if ((int)S.cold->srcsel > 1) {
+                sel = (int)(S.cold->srcsel - 2);
             }
         }
         if (sel >= 0) {
@@ -1055,9 +1065,9 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     s.f.w += 1.f;
     s.prop = S.prop[1];
     updateprop(ps, S, s.prop, s.mediaid);
-    s.launched += s.p.w;
+    S.cold->launched += s.p.w;
     s.w0 = s.p.w;
-    s.w0init = s.p.w;
+    S.cold->w0init = s.p.w;
     s.v.w = K_EPS;
     s.Lmove = 0.f;
     return 0;
@@ -1083,7 +1093,7 @@ __device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
 }
 
 template <class PS>
-__device__ __forceinline__ void vt_begin(const KArgs& a, const PS& ps, Photon& s, unsigned int vt) {
+__device__ __forceinline__ void vt_begin(const KArgs& a, const PS& ps, const Shared& S, Photon& s, unsigned int vt) {
     const mcxg_kparams& c_p = ps.p();
     s.p = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7fffffff));
     s.v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1094,10 +1104,10 @@ __device__ __forceinline__ void vt_begin(const KArgs& a, const PS& ps, Photon& s
     s.pathlen = 0.f;
     s.fx = s.fy = s.fz = 0;
     s.fw = -1;
-    s.esc = 0.f;
-    s.launched = 0.f;
-    s.w0init = 0.f;
-    s.srcsel = 0.f;
+    S.cold->esc = 0.f;
+    S.cold->launched = 0.f;
+    S.cold->w0init = 0.f;
+    S.cold->srcsel = 0.f;
     if (PS::kBatch) {
         const unsigned long long k = ps.seed() ^ ((unsigned long long)vt << 1);
         s.t.a = splitmix64(k);
@@ -1155,9 +1165,11 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             float4 q = a.gprop[i];
             /* __fdividef(x, y) is x * rcp(y): keeping rcp(y) per medium gives the
                fast kernel the same bits with one MUFU op fewer per use */
-            srecip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x), 0.f);
+            srecip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x),
+                                    __fdividef(1.f, 2.f * q.z));
         }
-        float* sf = (float*)(smem4 + 2 * c_p.medianum);
+        S.cold = (ColdState*)(smem4 + 2 * c_p.medianum) + threadIdx.x;
+        float* sf = (float*)((ColdState*)(smem4 + 2 * c_p.medianum) + blockDim.x);
         float* sinvcdf = sf;
         for (unsigned int i = threadIdx.x; i < c_p.nphase; i += blockDim.x) {
             sinvcdf[i] = a.invcdf[i];
@@ -1177,7 +1189,8 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
            the threads of a block run different simulations */
         S.prop = S.recip = a.gprop;
         S.invcdf = S.angleinvcdf = a.invcdf;
-        S.pp = (float*)smem4;
+        S.cold = (ColdState*)smem4 + threadIdx.x;
+        S.pp = (float*)((ColdState*)smem4 + blockDim.x);
     }
     S.stride = blockDim.x;
 
@@ -1208,7 +1221,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     S.prop = a.gprop + ps.prop_off();
                     S.recip = a.grecip + ps.prop_off();
                 }
-                vt_begin(a, ps, s, vt);
+                vt_begin(a, ps, S, s, vt);
                 if ((unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
                     r = 1;
                 } else {
@@ -1225,7 +1238,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             relaunch = false;
             if (r) {
                 if (r != 2) {
-                    a.energy[ps.vt_off() + vt] = make_float2(s.esc, s.launched);
+                    a.energy[ps.vt_off() + vt] = make_float2(S.cold->esc, S.cold->launched);
                 }
                 claimed = claim_vt(a, ps, vt);
                 fresh = true;
@@ -1281,7 +1294,13 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         /* Henyey-Greenstein, mcx_core.cl:2487-2493 */
                         tmp0 = (1.f - s.prop.z * s.prop.z) / (1.f - s.prop.z + 2.f * s.prop.z * rnd(s.t));
                         tmp0 *= tmp0;
-                        tmp0 = (1.f + s.prop.z * s.prop.z - tmp0) / (2.f * s.prop.z);
+                        if (EXACT) {
+                            tmp0 = (1.f + s.prop.z * s.prop.z - tmp0) / (2.f * s.prop.z);
+                        } else {
+                            /* __fdividef(a, 2g) == a * rcp(2g): the medium's rcp(2g) is staged */
+                            tmp0 = (1.f + s.prop.z * s.prop.z - tmp0) *
+                                   S.recip[c_p.mediaformat <= 4 ? (s.mediaid & K_MED_MASK) : 1u].w;
+                        }
                         tmp0 = fmaxf(-1.f, fminf(1.f, tmp0));
                         if (EXACT) {
                             theta = M::acos(tmp0);
@@ -1300,7 +1319,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         }
                     }
                 }
-                if (DET && c_p.savedet) {
+                if (DET && c_p.savedet && (s.mediaid & K_MED_MASK)) {
                     unsigned int med = (s.mediaid & K_MED_MASK) - 1;
                     if (SAVE_NSCAT(c_p.savedetflag)) {
                         float* q = S.pp + med * S.stride;
@@ -1318,7 +1337,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 s.v.w += 1.f;
                 vdirty = true;
                 if (c_p.replay && (c_p.outputtype == otWP || c_p.outputtype == otDCS || c_p.outputtype == otWPTOF)) {
-                    replay_site_deposit(a, ps, s, vt, ctheta);
+                    replay_site_deposit(a, ps, S, s, vt, ctheta);
                 }
             }
             s.v.w = (float)(int)s.v.w;
@@ -1365,7 +1384,9 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             s.f.x -= slen;
             s.f.y += s.f.z * s.prop.w * c_p.oneoverc0;
         }
-        if (DET && c_p.savedet && SAVE_PPATH(c_p.savedetflag)) {
+        /* a photon in a label-0 voxel (entered from a medium of the same index)
+           has no partial-path slot; the reference writes one slot early there */
+        if (DET && c_p.savedet && SAVE_PPATH(c_p.savedetflag) && (s.mediaid & K_MED_MASK)) {
             S.pp[(c_p.maxmedia * SAVE_NSCAT(c_p.savedetflag) + (s.mediaid & K_MED_MASK) - 1) * S.stride] += s.f.z;
         }
 
@@ -1428,7 +1449,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         weight = s.w0 * s.pathlen;
                     }
                     if (c_p.extrasrclen && (c_p.srcid < 0)) {
-                        tshift += ((int)s.srcsel - 1) * ((c_p.replay && c_p.replaydet == -1) ? (int)c_p.detnum : 1) *
+                        tshift += ((int)S.cold->srcsel - 1) * ((c_p.replay && c_p.replaydet == -1) ? (int)c_p.detnum : 1) *
                                   (int)c_p.maxgate;
                     }
                     dep = fabsf(weight) > 0.f;
@@ -1489,7 +1510,9 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         }
 
         /* ---- Fresnel reflection / refraction (mcx_core.cl:3126-3278) */
-        if (REFL && c_p.dorefl_compiled) {
+        /* within the same voxel the medium and index are unchanged, so the test
+           below cannot fire */
+        if (REFL && c_p.dorefl_compiled && s.idx1d != idx1dold) {
             updateprop(ps, S, s.prop, s.mediaid);
             if (((s.mediaid && c_p.doreflect) ||
                  (s.mediaid == 0 && (((s.isdet & 0xF) == bcUnknown && c_p.doreflect) ||

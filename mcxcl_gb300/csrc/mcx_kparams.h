@@ -66,6 +66,7 @@ typedef struct mcxg_kparams {
     uint32_t nreplay;              /* replayed photons */
     int32_t  replaydet;            /* 0 all detectors, -1 one gate block per detector, k detector k */
     uint32_t siteshift;            /* scattering-site replay deposits read photon k+siteshift (the reference: 1) */
+    uint32_t dimy, dimz;           /* voxel counts along y and z */
 } mcxg_kparams;
 
 /* One simulation of a batch: its parameter block (nthread = its reference
