@@ -90,6 +90,26 @@ __constant__ float4 c_srcx[MCXG_MAX_EXTRASRC * 4];
 
 
 
+/* Per-thread state written at a launch and read only at a detection or at
+   the end of the reference thread: kept in shared memory, out of the
+   registers of the step loop. */
+struct ColdState {
+    unsigned long long ps0, ps1;   /* RNG state at launch, saved with detected photons */
+    float esc, launched, w0init, srcsel;   /* reference ppath[partialdata .. +3] */
+};
+
+/* Per-thread view of the tables.  A single simulation stages them in shared
+   memory at fixed offsets, so their addresses are recomputed where used
+   instead of held in registers; a batch reads the rows of the thread's
+   current simulation from global memory through these two pointers. */
+struct Shared {
+    const float4* bprop;           /* batch: property rows of the current simulation */
+    const float4* brecip;          /* batch: their reciprocals */
+};
+
+
+extern __shared__ float4 mcxg_smem[];
+
 /* --------------------------------------------------------- parameter source
  *
  * Where the kernel reads its parameters.  One simulation keeps them in
@@ -112,6 +132,23 @@ struct ConstPS {
     __device__ __forceinline__ unsigned long long vt_off() const { return 0ull; }
     __device__ __forceinline__ unsigned int prop_off() const { return 0u; }
     __device__ __forceinline__ unsigned long long seed() const { return 0ull; }
+    /* shared layout: prop[medianum], recip[medianum] (float4), ColdState[blockDim],
+       invcdf[nphase], angleinvcdf[nangle], partial data[partialdata][blockDim] */
+    __device__ __forceinline__ const float4& prop(const Shared&, unsigned int i) const { return mcxg_smem[i]; }
+    __device__ __forceinline__ const float4& recip(const Shared&, unsigned int i) const {
+        return mcxg_smem[c_p.medianum + i];
+    }
+    __device__ __forceinline__ ColdState* cold() const {
+        return (ColdState*)(mcxg_smem + 2 * c_p.medianum) + threadIdx.x;
+    }
+    __device__ __forceinline__ float* tables() const {
+        return (float*)((ColdState*)(mcxg_smem + 2 * c_p.medianum) + blockDim.x);
+    }
+    __device__ __forceinline__ float invcdf(unsigned int i) const { return tables()[i]; }
+    __device__ __forceinline__ float angle(unsigned int i) const { return tables()[c_p.nphase + i]; }
+    __device__ __forceinline__ float& pp(unsigned int slot) const {
+        return tables()[c_p.nphase + c_p.nangle + slot * blockDim.x + threadIdx.x];
+    }
 };
 
 struct BatchPS {
@@ -127,6 +164,14 @@ struct BatchPS {
     __device__ __forceinline__ unsigned long long vt_off() const { return d->vt_off; }
     __device__ __forceinline__ unsigned int prop_off() const { return d->prop_off; }
     __device__ __forceinline__ unsigned long long seed() const { return d->seed; }
+    /* shared layout: ColdState[blockDim]; batches have no phase tables or detectors */
+    __device__ __forceinline__ const float4& prop(const Shared& S, unsigned int i) const { return S.bprop[i]; }
+    __device__ __forceinline__ const float4& recip(const Shared& S, unsigned int i) const { return S.brecip[i]; }
+    __device__ __forceinline__ ColdState* cold() const { return (ColdState*)mcxg_smem + threadIdx.x; }
+    __device__ __forceinline__ float* tables() const { return (float*)((ColdState*)mcxg_smem + blockDim.x); }
+    __device__ __forceinline__ float invcdf(unsigned int i) const { return tables()[i]; }
+    __device__ __forceinline__ float angle(unsigned int i) const { return tables()[i]; }
+    __device__ __forceinline__ float& pp(unsigned int slot) const { return tables()[slot * blockDim.x + threadIdx.x]; }
 };
 
 /* ------------------------------------------------------------------ math */
@@ -199,24 +244,6 @@ struct Photon {
     Rng t;
 };
 
-/* Per-thread state written at a launch and read only at a detection or at
-   the end of the reference thread: kept in shared memory, out of the
-   registers of the step loop. */
-struct ColdState {
-    unsigned long long ps0, ps1;   /* RNG state at launch, saved with detected photons */
-    float esc, launched, w0init, srcsel;   /* reference ppath[partialdata .. +3] */
-};
-
-struct Shared {
-    const float4* prop;            /* medianum rows */
-    const float4* recip;           /* per medium: 1/mus, 1/(mus (1-g)), 1/mua (fast kernel) */
-    const float* invcdf;
-    const float* angleinvcdf;
-    float* pp;                     /* this thread's partial data, stride blockDim.x */
-    unsigned int stride;
-    ColdState* cold;               /* this thread's launch-time state */
-};
-
 template <class PS>
 __device__ __forceinline__ unsigned int media_at(const KArgs& a, const PS& ps, unsigned int idx) {
     const mcxg_kparams& c_p = ps.p();
@@ -233,10 +260,10 @@ template <class PS>
 __device__ __forceinline__ void updateprop(const PS& ps, const Shared& S, float4& prop, unsigned int mediaid) {
     const mcxg_kparams& c_p = ps.p();
     if (c_p.mediaformat <= 4) {
-        prop = S.prop[mediaid & K_MED_MASK];
+        prop = ps.prop(S, mediaid & K_MED_MASK);
     } else {
         prop.x = fabsf(__uint_as_float(mediaid));
-        prop.w = S.prop[(!(mediaid & K_MED_MASK)) == 0].w;
+        prop.w = ps.prop(S, (!(mediaid & K_MED_MASK)) == 0).w;
     }
 }
 
@@ -429,10 +456,10 @@ __device__ int skipvoid(const KArgs& a, const PS& ps, const Shared& S, float4& p
                     /* ht.w is the entry voxel's index of refraction; the reference reads
                        gproperty[label].w, the same value for label volumes and an index past
                        the table for float-mua volumes */
-                    if (c_p.isspecular && ht.w != S.prop[0].w) {
-                        p.w *= 1.f - reflectcoeff<EXACT>(v, S.prop[0].w, ht.w, fw);
+                    if (c_p.isspecular && ht.w != ps.prop(S, 0).w) {
+                        p.w *= 1.f - reflectcoeff<EXACT>(v, ps.prop(S, 0).w, ht.w, fw);
                         if (p.w > K_EPS) {
-                            transmit<EXACT>(v, S.prop[0].w, ht.w, fw);
+                            transmit<EXACT>(v, ps.prop(S, 0).w, ht.w, fw);
                         }
                     }
                 }
@@ -482,19 +509,19 @@ __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Pho
     unsigned int slot = atomicAdd(a.detcount, 1u);
     if (slot < c_p.maxdetphoton) {
         if (c_p.issaveseed) {
-            a.detseed[slot * 2] = S.cold->ps0;
-            a.detseed[slot * 2 + 1] = S.cold->ps1;
+            a.detseed[slot * 2] = ps.cold()->ps0;
+            a.detseed[slot * 2 + 1] = ps.cold()->ps1;
         }
         float* rec = a.detp + (size_t)slot * c_p.reclen;
         unsigned int k = 0;
         if (SAVE_DETID(c_p.savedetflag)) {
             if (c_p.extrasrclen && (c_p.srcid <= 0)) {
-                detid |= (((int)S.cold->srcsel) << 16);
+                detid |= (((int)ps.cold()->srcsel) << 16);
             }
             rec[k++] = (float)detid;
         }
         for (unsigned int i = 0; i < c_p.partialdata; i++) {
-            rec[k++] = S.pp[i * S.stride];
+            rec[k++] = ps.pp(i);
         }
         if (SAVE_PEXIT(c_p.savedetflag)) {
             rec[k++] = s.p.x;
@@ -507,7 +534,7 @@ __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Pho
             rec[k++] = s.v.z;
         }
         if (SAVE_W0(c_p.savedetflag)) {
-            rec[k++] = S.cold->w0init;
+            rec[k++] = ps.cold()->w0init;
         }
         if (a.detw) {
             a.detw[slot] = make_float2(s.p.w, s.f.y);
@@ -632,7 +659,7 @@ __device__ void replay_site_deposit(const KArgs& a, const PS& ps, const Shared& 
     int tshift = (int)(floorf((rt - c_p.twin0) * c_p.Rtstep)) +
                  ((c_p.replaydet == -1) ? (((__ldg(a.rdetid + k) & 0xFFFF) - 1) * (int)c_p.maxgate) : 0);
     if (c_p.extrasrclen && (c_p.srcid < 0)) {
-        tshift += ((int)S.cold->srcsel - 1) * ((c_p.replaydet == -1) ? (int)c_p.detnum : 1) * (int)c_p.maxgate;
+        tshift += ((int)ps.cold()->srcsel - 1) * ((c_p.replaydet == -1) ? (int)c_p.detnum : 1) * (int)c_p.maxgate;
     }
     tshift = ((int)c_p.maxgate - 1 < tshift) ? (int)c_p.maxgate - 1 : tshift;
     long long key = (long long)s.idx1d + (long long)tshift * c_p.nvox;
@@ -678,14 +705,14 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     }
 
     if (fabsf(s.p.w) >= 0.f) {
-        S.cold->esc += s.p.w;
+        ps.cold()->esc += s.p.w;
         if (s.mediaid == 0 && s.idx1d != K_OUT_MIN && s.idx1d != K_OUT_MAX && c_p.issaveref && s.p.w > 0.f) {
             int tshift = (int)floorf((s.f.y - c_p.twin0) * c_p.Rtstep);
             if ((int)c_p.maxgate - 1 < tshift) {
                 tshift = (int)c_p.maxgate - 1;
             }
             if (c_p.extrasrclen && (c_p.srcid < 0)) {
-                tshift += ((int)S.cold->srcsel - 1) * (int)c_p.maxgate;
+                tshift += ((int)ps.cold()->srcsel - 1) * (int)c_p.maxgate;
             }
             field_add2(a.field, ps.lo_plane(), ps.field_off() + s.idx1d + (unsigned int)tshift * c_p.nvox, -s.p.w);
         }
@@ -695,7 +722,7 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     }
     if (DET) {
         for (unsigned int i = 0; i < c_p.partialdata; i++) {
-            S.pp[i * S.stride] = 0.f;
+            ps.pp(i) = 0.f;
         }
     }
 
@@ -716,8 +743,8 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     }
 
     if (DET && c_p.issaveseed) {
-        S.cold->ps0 = s.t.a;
-        S.cold->ps1 = s.t.b;
+        ps.cold()->ps0 = s.t.a;
+        ps.cold()->ps1 = s.t.b;
     }
 
     float4 lpos = f4(c_p.srcpos), ldir = f4(c_p.srcdir), lp1 = f4(c_p.srcparam1), lp2 = f4(c_p.srcparam2);
@@ -726,9 +753,9 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
         if (c_p.srcid > 1) {
             sel = c_p.srcid - 2;
         } else {
-            S.cold->srcsel = (float)((int)(rnd(s.t) * K_JUST_BELOW_ONE * (float)(c_p.extrasrclen + 1)) + 1);
-            if ((int)S.cold->srcsel > 1) {
-                sel = (int)(S.cold->srcsel - 2);
+            ps.cold()->srcsel = (float)((int)(rnd(s.t) * K_JUST_BELOW_ONE * (float)(c_p.extrasrclen + 1)) + 1);
+            if ((int)ps.cold()->srcsel > 1) {
+                sel = (int)(ps.cold()->srcsel - 2);
             }
         }
         if (sel >= 0) {
@@ -995,13 +1022,13 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
             unsigned int na = c_p.nangle;
             if (ldir.w > 0.f) {
                 ang = fminf(rnd(s.t) * (float)na, (float)na - K_EPS);
-                cphi = S.angleinvcdf[(int)(ang)];
+                cphi = ps.angle((int)(ang));
             } else {
                 ang = fminf(rnd(s.t) * (float)(na - 1), (float)(na - 1) - K_EPS);
                 sphi = ang - (float)((int)ang);
                 unsigned int a0 = ((unsigned int)ang >= na - 1 ? na - 1 : (unsigned int)(int)(ang));
                 unsigned int a1 = ((unsigned int)ang + 1 >= na - 1 ? na - 1 : (unsigned int)((int)(ang) + 1));
-                cphi = ((1.f - sphi) * S.angleinvcdf[a0] + sphi * S.angleinvcdf[a1]);
+                cphi = ((1.f - sphi) * ps.angle(a0) + sphi * ps.angle(a1));
             }
             cphi *= K_ONE_PI;
             M::sincos(cphi, &sth, &cth);
@@ -1063,11 +1090,11 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     }
 
     s.f.w += 1.f;
-    s.prop = S.prop[1];
+    s.prop = ps.prop(S, 1);
     updateprop(ps, S, s.prop, s.mediaid);
-    S.cold->launched += s.p.w;
+    ps.cold()->launched += s.p.w;
     s.w0 = s.p.w;
-    S.cold->w0init = s.p.w;
+    ps.cold()->w0init = s.p.w;
     s.v.w = K_EPS;
     s.Lmove = 0.f;
     return 0;
@@ -1104,10 +1131,10 @@ __device__ __forceinline__ void vt_begin(const KArgs& a, const PS& ps, const Sha
     s.pathlen = 0.f;
     s.fx = s.fy = s.fz = 0;
     s.fw = -1;
-    S.cold->esc = 0.f;
-    S.cold->launched = 0.f;
-    S.cold->w0init = 0.f;
-    S.cold->srcsel = 0.f;
+    ps.cold()->esc = 0.f;
+    ps.cold()->launched = 0.f;
+    ps.cold()->w0init = 0.f;
+    ps.cold()->srcsel = 0.f;
     if (PS::kBatch) {
         const unsigned long long k = ps.seed() ^ ((unsigned long long)vt << 1);
         s.t.a = splitmix64(k);
@@ -1150,49 +1177,28 @@ template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
     typedef typename std::conditional<BATCH, BatchPS, ConstPS>::type PS;
-    extern __shared__ float4 smem4[];
-
     PS ps;
     Shared S;
+    S.bprop = S.brecip = a.gprop;
     if (!BATCH) {
-        /* stage the property table and inverse-CDF tables */
-        float4* sprop = smem4;
-        for (unsigned int i = threadIdx.x; i < c_p.medianum; i += blockDim.x) {
-            sprop[i] = a.gprop[i];
-        }
-        float4* srecip = smem4 + c_p.medianum;
+        /* stage the property table, its reciprocals and the inverse-CDF tables */
         for (unsigned int i = threadIdx.x; i < c_p.medianum; i += blockDim.x) {
             float4 q = a.gprop[i];
+            mcxg_smem[i] = q;
             /* __fdividef(x, y) is x * rcp(y): keeping rcp(y) per medium gives the
                fast kernel the same bits with one MUFU op fewer per use */
-            srecip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x),
-                                    __fdividef(1.f, 2.f * q.z));
+            mcxg_smem[c_p.medianum + i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)),
+                                                      __fdividef(1.f, q.x), __fdividef(1.f, 2.f * q.z));
         }
-        S.cold = (ColdState*)(smem4 + 2 * c_p.medianum) + threadIdx.x;
-        float* sf = (float*)((ColdState*)(smem4 + 2 * c_p.medianum) + blockDim.x);
-        float* sinvcdf = sf;
+        float* tab = ps.tables();
         for (unsigned int i = threadIdx.x; i < c_p.nphase; i += blockDim.x) {
-            sinvcdf[i] = a.invcdf[i];
+            tab[i] = a.invcdf[i];
         }
-        float* sangle = sinvcdf + c_p.nphase;
         for (unsigned int i = threadIdx.x; i < c_p.nangle; i += blockDim.x) {
-            sangle[i] = a.angleinvcdf[i];
+            tab[c_p.nphase + i] = a.angleinvcdf[i];
         }
         __syncthreads();
-        S.prop = sprop;
-        S.recip = srecip;
-        S.invcdf = sinvcdf;
-        S.angleinvcdf = sangle;
-        S.pp = sangle + c_p.nangle + threadIdx.x;
-    } else {
-        /* a batch reads each simulation's tables from global memory (L1-resident):
-           the threads of a block run different simulations */
-        S.prop = S.recip = a.gprop;
-        S.invcdf = S.angleinvcdf = a.invcdf;
-        S.cold = (ColdState*)smem4 + threadIdx.x;
-        S.pp = (float*)((ColdState*)smem4 + blockDim.x);
     }
-    S.stride = blockDim.x;
 
     unsigned long long cnt_step = 0, cnt_scat = 0, cnt_launch = 0, cnt_refl = 0, cnt_fail = 0;
 
@@ -1218,8 +1224,10 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             int r;
             if (fresh) {
                 if (BATCH) {
-                    S.prop = a.gprop + ps.prop_off();
-                    S.recip = a.grecip + ps.prop_off();
+                    /* a batch reads each simulation's rows from global memory (L1-resident):
+                       the threads of a block run different simulations */
+                    S.bprop = a.gprop + ps.prop_off();
+                    S.brecip = a.grecip + ps.prop_off();
                 }
                 vt_begin(a, ps, S, s, vt);
                 if ((unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
@@ -1238,7 +1246,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             relaunch = false;
             if (r) {
                 if (r != 2) {
-                    a.energy[ps.vt_off() + vt] = make_float2(S.cold->esc, S.cold->launched);
+                    a.energy[ps.vt_off() + vt] = make_float2(ps.cold()->esc, ps.cold()->launched);
                 }
                 claimed = claim_vt(a, ps, vt);
                 fresh = true;
@@ -1280,7 +1288,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     theta = tmp0 - (float)((int)tmp0);
                     unsigned int i0 = (unsigned int)tmp0 >= np ? np - 1 : (unsigned int)(int)(tmp0);
                     unsigned int i1 = (unsigned int)tmp0 + 1 >= np ? np - 1 : (unsigned int)((int)(tmp0) + 1);
-                    tmp0 = (1.f - theta) * S.invcdf[i0] + theta * S.invcdf[i1];
+                    tmp0 = (1.f - theta) * ps.invcdf(i0) + theta * ps.invcdf(i1);
                     if (EXACT) {
                         theta = M::acos(tmp0);
                         stheta = M::sin(theta);
@@ -1299,7 +1307,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         } else {
                             /* __fdividef(a, 2g) == a * rcp(2g): the medium's rcp(2g) is staged */
                             tmp0 = (1.f + s.prop.z * s.prop.z - tmp0) *
-                                   S.recip[c_p.mediaformat <= 4 ? (s.mediaid & K_MED_MASK) : 1u].w;
+                                   ps.recip(S, c_p.mediaformat <= 4 ? (s.mediaid & K_MED_MASK) : 1u).w;
                         }
                         tmp0 = fmaxf(-1.f, fminf(1.f, tmp0));
                         if (EXACT) {
@@ -1322,11 +1330,11 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 if (DET && c_p.savedet && (s.mediaid & K_MED_MASK)) {
                     unsigned int med = (s.mediaid & K_MED_MASK) - 1;
                     if (SAVE_NSCAT(c_p.savedetflag)) {
-                        float* q = S.pp + med * S.stride;
+                        float* q = &ps.pp(med);
                         *q = __uint_as_float(__float_as_uint(*q) + 1u);
                     }
                     if (SAVE_MOM(c_p.savedetflag)) {
-                        S.pp[(c_p.maxmedia * (SAVE_NSCAT(c_p.savedetflag) + SAVE_PPATH(c_p.savedetflag)) + med) * S.stride] += 1.f - ctheta;
+                        ps.pp(c_p.maxmedia * (SAVE_NSCAT(c_p.savedetflag) + SAVE_PPATH(c_p.savedetflag)) + med) += 1.f - ctheta;
                     }
                 }
                 if (c_p.is2d) {
@@ -1363,7 +1371,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             if (EXACT || c_p.mediaformat > 4) {
                 s.f.z = M::div(slen, s.prop.y * (reduced ? (1.f - s.prop.z) : 1.f));
             } else {
-                const float4 rc = S.recip[s.mediaid & K_MED_MASK];
+                const float4 rc = ps.recip(S, s.mediaid & K_MED_MASK);
                 s.f.z = slen * (reduced ? rc.y : rc.x);
             }
             s.pathlen += s.f.z;
@@ -1387,7 +1395,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         /* a photon in a label-0 voxel (entered from a medium of the same index)
            has no partial-path slot; the reference writes one slot early there */
         if (DET && c_p.savedet && SAVE_PPATH(c_p.savedetflag) && (s.mediaid & K_MED_MASK)) {
-            S.pp[(c_p.maxmedia * SAVE_NSCAT(c_p.savedetflag) + (s.mediaid & K_MED_MASK) - 1) * S.stride] += s.f.z;
+            ps.pp(c_p.maxmedia * SAVE_NSCAT(c_p.savedetflag) + (s.mediaid & K_MED_MASK) - 1) += s.f.z;
         }
 
         /* ---- new voxel (mcx_core.cl:2795-2811) */
@@ -1421,7 +1429,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         } else {
                             /* prop still holds the medium the photon deposited in */
                             weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen)
-                                     : (s.w0 - s.p.w) * S.recip[mediaidold & K_MED_MASK].z;
+                                     : (s.w0 - s.p.w) * ps.recip(S, mediaidold & K_MED_MASK).z;
                         }
                     } else if (c_p.replay) {
                         /* replay Jacobian (mcx_core.cl:2845-2858): detected weight times
@@ -1449,7 +1457,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         weight = s.w0 * s.pathlen;
                     }
                     if (c_p.extrasrclen && (c_p.srcid < 0)) {
-                        tshift += ((int)S.cold->srcsel - 1) * ((c_p.replay && c_p.replaydet == -1) ? (int)c_p.detnum : 1) *
+                        tshift += ((int)ps.cold()->srcsel - 1) * ((c_p.replay && c_p.replaydet == -1) ? (int)c_p.detnum : 1) *
                                   (int)c_p.maxgate;
                     }
                     dep = fabsf(weight) > 0.f;
@@ -1471,7 +1479,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
 
         /* ---- exit, time-out or cyclic boundary (mcx_core.cl:2958-3028) */
         if ((s.mediaid == 0 && ((s.isdet & 0xF) == bcAbsorb || (s.isdet & 0xF) == bcCyclic ||
-                                ((s.isdet & 0xF) == bcReflect && s.n1 == S.prop[0].w))) || s.f.y > c_p.twin1) {
+                                ((s.isdet & 0xF) == bcReflect && s.n1 == ps.prop(S, 0).w))) || s.f.y > c_p.twin1) {
             if (s.isdet == bcCyclic) {
                 if (s.fw == 0) {
                     s.p.x = nextafter_ref(rintf(((s.idx1d == K_OUT_MIN) ? c_p.maxidx.x : 0)), (s.v.x > 0.f) - (s.v.x < 0.f));
@@ -1519,7 +1527,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                                      ((s.isdet & 0xF) == bcReflect || (s.isdet & 0xF) == bcMirror)))) &&
                 (((s.isdet & 0xF) == bcMirror) ||
                  s.n1 != ((c_p.mediaformat < 100) ? (s.prop.w)
-                          : (S.prop[(s.mediaid > 0 && c_p.mediaformat >= 100) ? 1 : s.mediaid].w)))) {
+                          : (ps.prop(S, (s.mediaid > 0 && c_p.mediaformat >= 100) ? 1 : s.mediaid).w)))) {
                 float Rtotal = 1.f;
                 if (COUNT) {
                     cnt_refl++;
