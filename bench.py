@@ -22,6 +22,11 @@ One step = one full simulation of the workload.  Prints one JSON line.
   cpu_baseline: the CPU oracle (a C restatement of the reference kernel) on
            all host cores, on a bounded sample of the workload.
 
+Also reported: "batched" -- the batched workload's simulations/s in one
+persistent launch against one launch per simulation; "gradient" -- forward
+and replay-backward times of the differentiation workload and the backward
+pass's agreement with central differences.
+
 --impl reference times the reference's CPU path (the oracle, since the
 reference's OpenCL build does not run on this machine) on the host cores.
 Multi-GPU: replicas only (photons do not exchange anything); each rank runs
@@ -58,6 +63,8 @@ def parse_args():
     ap.add_argument("--photons", type=float, default=None, help="override photons per step")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-sims", type=int, default=512, help="simulations in the batched comparison (0: skip)")
+    ap.add_argument("--no-gradient", action="store_true", help="skip the replay-gradient timing")
     return ap.parse_args()
 
 
@@ -183,6 +190,72 @@ def cpu_baseline(cfg, target_s=15.0, kind="port"):
             "sample": "%d photons of the %d-photon workload, %d reference threads, OpenMP over %d cores, %.1f s"
                       % (n, int(cfg["nphoton"]), nthread, ncores, dt),
             "absorbed": (r["stat"]["energytot"] - r["stat"]["energyesc"]) / r["stat"]["energytot"]}
+
+
+def batch_measure(nsim):
+    """The batched workload (nsim cubes of edge 32-128, random media and
+    inclusions, 1e5-1e7 photons each): all of them in one persistent launch
+    against the same simulations run one launch each, both through the
+    public API with host inputs and outputs.  Each simulation runs the same
+    photon count in both arms, so the fluence error is equal by construction."""
+    import mcxcl_gb300
+    from mcxcl_gb300 import workloads
+    sims = workloads.batch_configs(nsim=nsim, master_seed=7)
+    photons = float(sum(c["nphoton"] for c in sims))
+    mcxcl_gb300.run_batch(sims[:2])
+    mcxcl_gb300.run(sims[0])
+    t0 = time.perf_counter()
+    res = mcxcl_gb300.run_batch(sims)
+    tb = time.perf_counter() - t0
+    kb = res[0]["stat"]["kernelms"]
+    t0 = time.perf_counter()
+    ks = 0.0
+    for c in sims:
+        ks += mcxcl_gb300.run(c)["stat"]["kernelms"]
+    ts = time.perf_counter() - t0
+    return {"simulations": nsim, "photons": photons, "batched_sims_per_s": nsim / tb,
+            "one_launch_per_sim_sims_per_s": nsim / ts, "ratio": ts / tb,
+            "batched_wall_s": tb, "batched_kernel_ms": kb, "one_launch_per_sim_wall_s": ts,
+            "one_launch_per_sim_kernel_ms": ks,
+            "equal_error": "same photons per simulation in both arms"}
+
+
+def gradient_measure():
+    """The differentiation workload (100^3 float-mua field, 16 detectors, 1e7
+    photons): forward readings, backward replay for d loss / d mua, and
+    central differences (relative step 1e-3, common random numbers) on 8
+    voxels drawn among those the detected photons visit."""
+    from mcxcl_gb300 import diff, workloads
+    cfg, mua, target = workloads.diff_config()
+    sim = diff.ReplayGradient(cfg)
+    Rt = sim.forward(target)
+
+    def loss(R):
+        return float(np.sum((np.log(R) - np.log(Rt)) ** 2))
+    tf, tb = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        R = sim.forward(mua)
+        tf.append(time.perf_counter() - t0)
+        g = 2 * (np.log(R) - np.log(Rt)) / R
+        t0 = time.perf_counter()
+        gm = sim.backward(g)
+        tb.append(time.perf_counter() - t0)
+    rng = np.random.default_rng(64)
+    support = np.flatnonzero(np.abs(gm).ravel() > 1e-3 * np.abs(gm).max())
+    bw, fd = [], []
+    for f in rng.choice(support, size=8, replace=False):
+        v = np.unravel_index(f, mua.shape)
+        h = np.float32(1e-3) * mua[v]
+        mp, mm = mua.copy(), mua.copy()
+        mp[v] += h
+        mm[v] -= h
+        fd.append((loss(sim.forward(mp)) - loss(sim.forward(mm))) / float(mp[v] - mm[v]))
+        bw.append(gm[v])
+    bw, fd = np.array(bw), np.array(fd)
+    return {"forward_ms": 1e3 * min(tf), "backward_ms": 1e3 * min(tb), "backward_over_forward": min(tb) / min(tf),
+            "detected_replayed": int(len(sim.last["w"])),
+            "fd_rel_err_8_voxels": float(np.linalg.norm(bw - fd) / np.linalg.norm(fd))}
 
 
 def run_reference_arm(args, rank, world):
@@ -322,6 +395,8 @@ def main():
 
     out = None
     if rank == 0:
+        batched = batch_measure(args.batch_sims) if args.batch_sims > 0 else None
+        gradient = None if args.no_gradient else gradient_measure()
         cpu = None if args.no_cpu_baseline else cpu_baseline(cfg)
         absorbed = last["stat"]["energyabs"] / last["stat"]["energytot"]
         out = {
@@ -351,6 +426,8 @@ def main():
             "clocks": clock_summary,
             "gpu_launches": args.steps,
             "absorbed": absorbed,
+            "batched": batched,
+            "gradient": gradient,
             "detected_per_step": int(last["stat"]["detected"]),
         }
         print(json.dumps(out))
