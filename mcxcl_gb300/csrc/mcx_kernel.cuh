@@ -1230,17 +1230,16 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     S.brecip = a.grecip + ps.prop_off();
                 }
                 vt_begin(a, ps, S, s, vt);
-                if ((unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
-                    r = 1;
-                } else {
-                    r = launchnewphoton<EXACT, DET>(a, ps, S, s, 0u, vt, &cnt_fail);
-                    if (r) {
-                        atomicAdd(a.status + ST_FAILED_LAUNCH, 1u);
-                        r = 2;       /* NO_LAUNCH: the reference returns without writing energies */
-                    }
-                }
+            }
+            /* one call site for the first and every later launch keeps the hot loop small */
+            if (fresh && (unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
+                r = 1;
             } else {
-                r = launchnewphoton<EXACT, DET>(a, ps, S, s, relaunch_isdet, vt, &cnt_fail);
+                r = launchnewphoton<EXACT, DET>(a, ps, S, s, fresh ? 0u : relaunch_isdet, vt, &cnt_fail);
+                if (r && fresh) {
+                    atomicAdd(a.status + ST_FAILED_LAUNCH, 1u);
+                    r = 2;       /* NO_LAUNCH: the reference returns without writing energies */
+                }
             }
             fresh = false;
             relaunch = false;
