@@ -216,6 +216,9 @@ void mcx_cleargpuinfo(GPUInfo** info);
    as in the reference.  Outputs go to cfg: exportfield, exportdetected,
    seeddata, detectedcount, energytot/energyesc/energyabs, normalizer, runtime. */
 void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy);
+/* Writes detected photons as <session>.mch: the History header, count records
+   of his.colcount floats, then the seeds (src/mcx_utils.c:963-998). */
+void mcx_savedetphoton(float* ppath, void* seeds, int count, int doappend, Config* cfg);
 /* Scales field[i*srcnum+pidx] by scale (src/mcx_utils.c:1208-1218). */
 void mcx_normalize(float field[], float scale, int fieldlen, int option, int pidx, int srcnum);
 /* Error reporting.  Standalone: print and exit(id).  Library mode

@@ -1184,6 +1184,7 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     cfg->his.unitinmm = cfg->unitinmm;
     cfg->his.totalphoton = (unsigned int)cfg->nphoton;
     cfg->his.savedphoton = cfg->detectedcount;
+    cfg->his.seedbyte = cfg->issaveseed ? 16u : 0u;
 
     if (cfg->flog && cfg->parentid == mpStandalone) {
         fprintf(cfg->flog, "simulated %zu photons (%zu) with 1 devices (repeat x%d)\nMCX simulation speed: %.2f photon/ms\n",
@@ -1203,6 +1204,32 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
 #undef seedbuf
 #undef fieldtmp
 #undef blockscale
+    MCX_LEAVE();
+}
+
+/* mcx_savedetphoton (mcx_utils.c:963-998): the History header, count
+   records of his.colcount floats and, when seeds are saved, count seeds of
+   his.seedbyte bytes, to <session>.mch (<session>.mct for trajectories). */
+void mcx_savedetphoton(float* ppath, void* seeds, int count, int doappend, Config* cfg) {
+    MCX_ENTER(cfg);
+    char fname[MAX_SESSION_LENGTH + 8];
+    char filetag = (cfg->his.detected == 0 && cfg->his.savedphoton) ? 't' : 'h';
+    snprintf(fname, sizeof(fname), "%s.mc%c", cfg->session, filetag);
+    FILE* fp = fopen(fname, doappend ? "ab" : "wb");
+    if (fp == NULL) {
+        MCX_ERROR(-2, "can not save data to disk");
+    }
+    size_t ok = fwrite(&(cfg->his), sizeof(History), 1, fp);
+    if (count > 0 && ppath) {
+        ok &= fwrite(ppath, sizeof(float), (size_t)count * cfg->his.colcount, fp) == (size_t)count * cfg->his.colcount;
+    }
+    if (cfg->issaveseed && seeds != NULL && count > 0) {
+        ok &= fwrite(seeds, cfg->his.seedbyte, (size_t)count, fp) == (size_t)count;
+    }
+    fclose(fp);
+    if (!ok) {
+        MCX_ERROR(-2, "can not save data to disk");
+    }
     MCX_LEAVE();
 }
 
