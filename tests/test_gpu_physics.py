@@ -49,18 +49,21 @@ def test_homogeneous_cube_follows_cw_diffusion(gpu):
     phi = r["flux"][..., 0]                    # CW fluence per unit source weight, 1/mm^2
     src = np.array([29.0, 29.0, 0.0])
     mua, musp = 0.005, 1.0 * (1 - 0.01)
+    # diffusion holds beyond ~10 transport mean free paths (1 mm here) from the
+    # pencil beam's entry: a depth profile from 10 mm and a lateral profile
+    # 8 mm deep, 8.5-14.5 mm from the entry point, well inside the lateral faces
     pts = []
-    for z in range(4, 20):                     # depth profile under the source
+    for z in range(10, 20):
         pts.append((29, 29, z))
-    for x in range(31, 42):                    # lateral profile at 8 mm depth
+    for x in range(31, 42):
         pts.append((x, 29, 8))
     pts = np.array(pts)
     centres = pts + 0.5
     mc = np.array([phi[tuple(p)] + phi[28 - (p[0] - 29) if p[0] != 29 else 28, p[1], p[2]] for p in pts]) / 2
     dif = cwdiffusion(mua, musp, 0.0, src, centres)
     ratio = mc / dif
-    assert np.all(np.abs(ratio - 1) < 0.10), np.round(ratio, 3)
-    assert abs(np.median(ratio) - 1) < 0.04, np.median(ratio)
+    assert np.all(np.abs(ratio - 1) < 0.06), np.round(ratio, 3)
+    assert abs(np.median(ratio) - 1) < 0.03, np.median(ratio)
 
 
 def test_head_exact_kernel_matches_oracle_bits(gpu, oracle_mod):
