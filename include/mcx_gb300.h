@@ -61,7 +61,10 @@ extern "C" {
 #define SEED_FROM_FILE       -999
 #define FILL_MAXDETPHOTON    3
 
-enum TOutputType {otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF};
+enum TOutputType {otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF, otAdjoint,
+                  otAdjointDcoeff, otAdjointMus, otAdjointMusp, otAdjointMuaD, otAdjointMuaMusp};
+#define MCX_IS_ADJOINT_TYPE(t)      ((int)(t) >= (int)otAdjoint)
+#define MCX_IS_DUAL_ADJOINT_TYPE(t) ((int)(t) >= (int)otAdjointMuaD)
 enum TBoundary {bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic};
 enum TMCXParent {mpStandalone, mpMATLAB, mpPython};
 
@@ -175,7 +178,9 @@ typedef struct MCXConfig {
     unsigned int extrasrclen;
     ExtraSrc* srcdata;
     Replay replay;
-    int replaydet;                /* replay: 0 all detectors, -1 one output per detector, k detector k only */
+    int replaydet;
+    mcx_float4* detdir;           /* adjoint outputs: per detector {direction, focal length}; detectors become sources */
+    float* exportjacob;           /* adjoint Jacobians: [Nx,Ny,Nz, sources x detectors] (x2 for the dual types) */                /* replay: 0 all detectors, -1 one output per detector, k detector k only */
     /* GB300 additions */
     int exactmath;                /* 1: run the IEEE-only kernel (bit-identical to the CPU oracle) */
     float kernelms;               /* kernel time from CUDA events, ms */
@@ -346,6 +351,14 @@ int  mcxg_get_field(mcxg_session* s, float* out, double scale);
 /* Field split into nblocks equal blocks, block b scaled by scales[b]
    (a replay with one output per detector). */
 int  mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uint32_t nblocks);
+/* Adjoint Jacobians from the normalised float field of the last
+   mcxg_get_field: fieldlen = nx ny nz maxgate (ns + nd), the first ns gate
+   blocks the sources, the next nd the detectors run as sources.  kind 0:
+   time-integrated phi_src x phi_det per voxel; kind 1: the dot product of
+   their finite-difference gradients.  out: nx ny nz x ns x nd floats,
+   source-major over detector (src/mcx_core.cl:3320-3512). */
+int  mcxg_adjoint(mcxg_session* s, int kind, uint32_t ns, uint32_t nd, uint32_t nx, uint32_t ny, uint32_t nz,
+                  uint32_t maxgate, float* out);
 /* Field: (hi + lo) in FP64, unscaled. */
 int  mcxg_get_field_f64(mcxg_session* s, double* out);
 /* Weight and time of flight (s) of each saved detected photon when it was

@@ -83,6 +83,7 @@ class Config(ctypes.Structure):
         ("nphase", ctypes.c_uint), ("invcdf", ctypes.POINTER(ctypes.c_float)), ("nangle", ctypes.c_uint),
         ("angleinvcdf", ctypes.POINTER(ctypes.c_float)), ("srcid", ctypes.c_int), ("extrasrclen", ctypes.c_uint),
         ("srcdata", ctypes.POINTER(ExtraSrc)), ("replay", Replay), ("replaydet", ctypes.c_int),
+        ("detdir", ctypes.POINTER(Float4)), ("exportjacob", ctypes.POINTER(ctypes.c_float)),
         ("exactmath", ctypes.c_int), ("kernelms", ctypes.c_float),
         ("eventcount", ctypes.c_uint64 * 5), ("failedlaunch", ctypes.c_uint), ("threadused", ctypes.c_uint),
         ("exportenergy", ctypes.POINTER(ctypes.c_float)), ("savethreadenergy", ctypes.c_int),
@@ -111,6 +112,7 @@ EXPORTS = [
     "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc", "mcxg_autotune",
     "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",
     "mcxg_batch_simulate", "mcxg_batch_get_energy", "mcxg_batch_get_field", "mcx_savedetphoton",
+    "mcxg_adjoint",
 ]
 
 _lib = None

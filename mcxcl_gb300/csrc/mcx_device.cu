@@ -75,6 +75,9 @@ struct mcxg_session {
     uint32_t nreplay = 0;
     double* d_scales = nullptr;      /* per-block normalisation factors */
     size_t scales_cap = 0;
+    bool out_valid = false;          /* d_out holds the last normalised float field */
+    float* d_adj = nullptr;          /* adjoint Jacobians */
+    size_t adj_cap = 0;
 
     /* batch of simulations in one persistent launch */
     std::vector<mcxg_simdesc> h_sims;
@@ -258,6 +261,81 @@ __global__ void batch_merge(const float* __restrict__ f, unsigned long long tota
     }
 }
 
+/* Adjoint post-kernels (the reference's mcx_adjoint_kernel and
+   mcx_adjoint_dcoeff_kernel, mcx_core.cl:3320-3512) on the normalised float
+   field: per voxel, the time-integrated fluence of each source times that of
+   each detector, or the dot product of their finite-difference gradients.
+   Explicit _rn operations keep the reference's evaluation order (no
+   contraction). */
+__device__ __forceinline__ float adj_cw(const float* f, unsigned int vox, unsigned int slot, unsigned int maxgate,
+                                        unsigned int nvox) {
+    float sum = 0.f;
+    for (unsigned int t = 0; t < maxgate; t++) {
+        sum = __fadd_rn(sum, f[vox + (size_t)(t + slot * maxgate) * nvox]);
+    }
+    return sum;
+}
+
+__device__ __forceinline__ float adj_grad(const float* f, unsigned int vox, unsigned int slot, unsigned int maxgate,
+                                          unsigned int nvox, unsigned int i, unsigned int n, unsigned int stride) {
+    if (n <= 1) {
+        return 0.f;
+    }
+    const float f0 = adj_cw(f, vox, slot, maxgate, nvox);
+    if (i == 0) {
+        const float fp1 = adj_cw(f, vox + stride, slot, maxgate, nvox);
+        if (n == 2) {
+            return __fsub_rn(fp1, f0);
+        }
+        const float fp2 = adj_cw(f, vox + 2 * stride, slot, maxgate, nvox);
+        return __fmul_rn(__fsub_rn(__fadd_rn(__fmul_rn(-3.f, f0), __fmul_rn(4.f, fp1)), fp2), 0.5f);
+    } else if (i == n - 1) {
+        const float fm1 = adj_cw(f, vox - stride, slot, maxgate, nvox);
+        if (n == 2) {
+            return __fsub_rn(f0, fm1);
+        }
+        const float fm2 = adj_cw(f, vox - 2 * stride, slot, maxgate, nvox);
+        return __fmul_rn(__fadd_rn(__fsub_rn(fm2, __fmul_rn(4.f, fm1)), __fmul_rn(3.f, f0)), 0.5f);
+    }
+    const float fp1 = adj_cw(f, vox + stride, slot, maxgate, nvox);
+    const float fm1 = adj_cw(f, vox - stride, slot, maxgate, nvox);
+    return __fmul_rn(__fsub_rn(fp1, fm1), 0.5f);
+}
+
+__global__ void adjoint_mua(const float* __restrict__ f, float* __restrict__ out, unsigned int nvox,
+                            unsigned int maxgate, unsigned int ns, unsigned int nd) {
+    for (unsigned int vox = blockIdx.x * blockDim.x + threadIdx.x; vox < nvox; vox += gridDim.x * blockDim.x) {
+        for (unsigned int s = 0; s < ns; s++) {
+            const float cs = adj_cw(f, vox, s, maxgate, nvox);
+            for (unsigned int d = 0; d < nd; d++) {
+                const float cd = adj_cw(f, vox, ns + d, maxgate, nvox);
+                out[vox + (size_t)(s * nd + d) * nvox] = __fsub_rn(__fmul_rn(cs, cd), __fmul_rn(0.f, 0.f));
+            }
+        }
+    }
+}
+
+__global__ void adjoint_dcoeff(const float* __restrict__ f, float* __restrict__ out, unsigned int nvox,
+                               unsigned int maxgate, unsigned int ns, unsigned int nd, unsigned int nx,
+                               unsigned int ny) {
+    const unsigned int nxy = nx * ny, nz = nvox / nxy;
+    for (unsigned int vox = blockIdx.x * blockDim.x + threadIdx.x; vox < nvox; vox += gridDim.x * blockDim.x) {
+        const unsigned int ix = vox % nx, iy = (vox / nx) % ny, iz = vox / nxy;
+        for (unsigned int s = 0; s < ns; s++) {
+            const float sx = adj_grad(f, vox, s, maxgate, nvox, ix, nx, 1);
+            const float sy = adj_grad(f, vox, s, maxgate, nvox, iy, ny, nx);
+            const float sz = adj_grad(f, vox, s, maxgate, nvox, iz, nz, nxy);
+            for (unsigned int d = 0; d < nd; d++) {
+                const float dx = adj_grad(f, vox, ns + d, maxgate, nvox, ix, nx, 1);
+                const float dy = adj_grad(f, vox, ns + d, maxgate, nvox, iy, ny, nx);
+                const float dz = adj_grad(f, vox, ns + d, maxgate, nvox, iz, nz, nxy);
+                out[vox + (size_t)(s * nd + d) * nvox] =
+                    __fadd_rn(__fadd_rn(__fmul_rn(sx, dx), __fmul_rn(sy, dy)), __fmul_rn(sz, dz));
+            }
+        }
+    }
+}
+
 __global__ void field_merge_f64(const float* __restrict__ f, size_t n, double* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         out[i] = (double)f[i] + (double)f[i + n];
@@ -410,7 +488,8 @@ int mcxg_destroy(mcxg_session* s) {
     void* bufs[] = {s->d_media, s->d_prop, s->d_tables, s->d_pattern, s->d_seeds, s->d_field, s->d_energy,
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
                     s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw,
-                    s->d_sims, s->d_simvt, s->d_bmedia, s->d_bprop, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout};
+                    s->d_sims, s->d_simvt, s->d_bmedia, s->d_bprop, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
+                    s->d_adj};
     if (s->bgraph_exec) {
         cudaGraphExecDestroy(s->bgraph_exec);
     }
@@ -612,6 +691,7 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     if (!(flags & MCXG_KEEP)) {
         MCXG_TRY(cudaMemsetAsync(s->d_field, 0, sizeof(float) * 2 * (size_t)kp.fieldlen, s->st));
     }
+    s->out_valid = false;
     MCXG_TRY(cudaMemsetAsync(s->d_energy, 0, sizeof(float2) * kp.nthread, s->st));
     MCXG_TRY(cudaMemsetAsync(s->d_words, 0, 8 * sizeof(unsigned int), s->st));
     MCXG_TRY(cudaMemsetAsync(s->d_events, 0, 8 * sizeof(unsigned long long), s->st));
@@ -802,6 +882,7 @@ int mcxg_get_field(mcxg_session* s, float* out, double scale) {
         return rc;
     }
     field_merge_f32<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, scale, (float*)s->d_out);
+    s->out_valid = true;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
@@ -822,8 +903,34 @@ int mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uin
     }
     MCXG_TRY(cudaMemcpyAsync(s->d_scales, scales, sizeof(double) * nblocks, cudaMemcpyHostToDevice, s->st));
     field_merge_blocks<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, n / nblocks, s->d_scales, (float*)s->d_out);
+    s->out_valid = true;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_adjoint(mcxg_session* s, int kind, uint32_t ns, uint32_t nd, uint32_t nx, uint32_t ny, uint32_t nz,
+                 uint32_t maxgate, float* out) {
+    if (!s || !out || !s->has_problem || !s->out_valid || ns == 0 || nd == 0 || nx == 0 || ny == 0 || nz == 0 ||
+            (unsigned long long)nx * ny * nz * maxgate * (ns + nd) != s->kp.fieldlen) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    const unsigned int nvox = nx * ny * nz;
+    const size_t len = (size_t)nvox * ns * nd;
+    int rc = ensure(&s->d_adj, &s->adj_cap, len);
+    if (rc) {
+        return rc;
+    }
+    const int grid = grid_for(s, nvox);
+    if (kind == 0) {
+        adjoint_mua<<<grid, 256, 0, s->st>>>((const float*)s->d_out, s->d_adj, nvox, maxgate, ns, nd);
+    } else {
+        adjoint_dcoeff<<<grid, 256, 0, s->st>>>((const float*)s->d_out, s->d_adj, nvox, maxgate, ns, nd, nx, ny);
+    }
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_adj, sizeof(float) * len, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    MCXG_TRY(cudaGetLastError());
     return MCXG_OK;
 }
 
@@ -838,6 +945,7 @@ int mcxg_get_field_f64(mcxg_session* s, double* out) {
         return rc;
     }
     field_merge_f64<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, (double*)s->d_out);
+    s->out_valid = false;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;

@@ -139,6 +139,10 @@ void mcx_clearcfg(Config* cfg) {
     free(cfg->exportenergy);
     free(cfg->exportdetweight);
     cfg->exportdetweight = NULL;
+    free(cfg->detdir);
+    free(cfg->exportjacob);
+    cfg->detdir = NULL;
+    cfg->exportjacob = NULL;
     free(cfg->replay.seed);
     free(cfg->replay.weight);
     free(cfg->replay.tof);
@@ -576,8 +580,37 @@ void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte) {
         MCX_ERROR(-6, "RF replay outputs need the frequency-domain transport, which this build does not include");
     }
     if (!replayout && cfg->outputtype != otFlux && cfg->outputtype != otFluence && cfg->outputtype != otEnergy &&
-            cfg->outputtype != otL) {
+            cfg->outputtype != otL && !MCX_IS_ADJOINT_TYPE(cfg->outputtype)) {
         MCX_ERROR(-6, "unsupported output type");
+    }
+    if (MCX_IS_ADJOINT_TYPE(cfg->outputtype) && (cfg->detnum == 0 || cfg->detdir == NULL)) {
+        MCX_ERROR(-6, "adjoint outputs need detectors with directions (cfg.detdir)");
+    }
+    /* adjoint outputs: each detector becomes an extra source at its position,
+       along its direction, radius in srcparam1.x, sharing photons with the
+       sources (mcx_utils.c:1902-1926; the positions are taken before the
+       detectors' own conversion to 0-based, as there) */
+    if ((MCX_IS_ADJOINT_TYPE(cfg->outputtype) || cfg->srcid == -2) && cfg->seed != SEED_FROM_FILE && cfg->detnum > 0 &&
+            cfg->detdir != NULL) {
+        unsigned int orig = cfg->extrasrclen;
+        ExtraSrc* ns = (ExtraSrc*)realloc(cfg->srcdata, (orig + cfg->detnum) * sizeof(ExtraSrc));
+        if (!ns) {
+            MCX_ERROR(-2, "out of host memory");
+        }
+        cfg->srcdata = ns;
+        memset(cfg->srcdata + orig, 0, cfg->detnum * sizeof(ExtraSrc));
+        for (unsigned int i = 0; i < cfg->detnum; i++) {
+            cfg->srcdata[orig + i].srcpos.x = cfg->detpos[i].x;
+            cfg->srcdata[orig + i].srcpos.y = cfg->detpos[i].y;
+            cfg->srcdata[orig + i].srcpos.z = cfg->detpos[i].z;
+            cfg->srcdata[orig + i].srcpos.w = 1.f;
+            cfg->srcdata[orig + i].srcdir = cfg->detdir[i];
+            cfg->srcdata[orig + i].srcparam1.x = cfg->detpos[i].w;
+        }
+        cfg->extrasrclen += cfg->detnum;
+        if (MCX_IS_ADJOINT_TYPE(cfg->outputtype)) {
+            cfg->srcid = -1;
+        }
     }
     if (!cfg->issrcfrom0) {
         for (unsigned int i = 0; i < cfg->detnum; i++) {
@@ -813,6 +846,64 @@ static void make_kparams(const Config* cfg, size_t nvox, size_t fieldlen, size_t
     }
     for (int i = 0; i < 12; i++) {
         kp->bc[i] = (uint8_t)cfg->bc[i];
+    }
+}
+
+/* Adjoint Jacobians from the normalised forward fluences of the sources and
+   of the detectors run as sources (mcx_host.cpp:1466-1642): phi_src phi_det
+   (mua) and/or grad phi_src . grad phi_det (diffusion coefficient), scaled
+   by -Vvox and -unitinmm, and for the mus / mus' types by the medium's
+   1 / (3 (1-g) mus^2) or 1 / (3 (1-g)^2 mus^2). */
+static void adjoint_jacobians(Config* cfg, mcxg_session* s, size_t nvox) {
+    const int isdual = MCX_IS_DUAL_ADJOINT_TYPE(cfg->outputtype);
+    const unsigned int Ns = cfg->extrasrclen + 1 - cfg->detnum, Nd = cfg->detnum;
+    const size_t adjlen = nvox * Ns * Nd;
+    const float Vvox = cfg->steps.x * cfg->steps.y * cfg->steps.z;
+    free(cfg->exportjacob);
+    cfg->exportjacob = (float*)malloc(sizeof(float) * adjlen * (isdual ? 2 : 1));
+    if (!cfg->exportjacob) {
+        MCX_ERROR(-2, "out of host memory");
+    }
+    float* first = cfg->exportjacob;
+    float* second = isdual ? cfg->exportjacob + adjlen : cfg->exportjacob;
+    if (isdual || cfg->outputtype == otAdjoint) {
+        device_check(mcxg_adjoint(s, 0, Ns, Nd, cfg->dim.x, cfg->dim.y, cfg->dim.z, cfg->maxgate, first),
+                     "computing the adjoint mua Jacobian");
+    }
+    if (isdual || cfg->outputtype != otAdjoint) {
+        device_check(mcxg_adjoint(s, 1, Ns, Nd, cfg->dim.x, cfg->dim.y, cfg->dim.z, cfg->maxgate, second),
+                     "computing the adjoint diffusion Jacobian");
+    }
+    if (isdual) {
+        for (size_t k = 0; k < adjlen; k++) {
+            first[k] *= -Vvox;
+        }
+        for (size_t k = 0; k < adjlen; k++) {
+            second[k] *= -cfg->unitinmm;
+        }
+    } else {
+        const float adj_scale = (cfg->outputtype == otAdjoint) ? -Vvox : -cfg->unitinmm;
+        for (size_t k = 0; k < adjlen; k++) {
+            first[k] *= adj_scale;
+        }
+    }
+    const int musform = (cfg->outputtype == otAdjointMus) ? 1 :
+                        ((cfg->outputtype == otAdjointMusp || cfg->outputtype == otAdjointMuaMusp) ? 2 : 0);
+    if (musform) {
+        for (size_t vox = 0; vox < nvox; vox++) {
+            unsigned int medid = cfg->vol[vox] & 0xFF;
+            float opscale = 0.f;
+            if (medid < cfg->medianum) {
+                float mus = cfg->prop[medid].mus;
+                float onemg = 1.f - cfg->prop[medid].g;
+                if (mus > 0.f && onemg > 0.f) {
+                    opscale = (musform == 1) ? 1.f / (3.f * onemg * mus * mus) : 1.f / (3.f * onemg * onemg * mus * mus);
+                }
+            }
+            for (unsigned int sd = 0; sd < Ns * Nd; sd++) {
+                second[vox + (size_t)sd * nvox] *= opscale;
+            }
+        }
     }
 }
 
@@ -1099,9 +1190,9 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
             float Vvox = cfg->steps.x * cfg->steps.y * cfg->steps.z;
             float sc = 1.f;
             cfg->energyabs += cfg->energytot - cfg->energyesc;
-            if (cfg->outputtype == otFlux || cfg->outputtype == otFluence) {
+            if (cfg->outputtype == otFlux || cfg->outputtype == otFluence || MCX_IS_ADJOINT_TYPE(cfg->outputtype)) {
                 sc = (float)(cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep));
-                if (cfg->outputtype == otFluence) {
+                if (cfg->outputtype == otFluence || MCX_IS_ADJOINT_TYPE(cfg->outputtype)) {
                     sc *= cfg->tstep;
                 }
             } else if (cfg->outputtype == otEnergy || cfg->outputtype == otL) {
@@ -1179,6 +1270,9 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
             for (size_t i = 0; i < fieldlen; i++) {
                 cfg->exportfield[i] += fieldtmp[i];
             }
+        }
+        if (MCX_IS_ADJOINT_TYPE(cfg->outputtype) && cfg->detdir && !(cfg->debuglevel & 1)) {
+            adjoint_jacobians(cfg, s, nvox);
         }
     }
     cfg->his.unitinmm = cfg->unitinmm;
@@ -1435,7 +1529,7 @@ static const struct {
     MCX_FIELD(exportdetected), MCX_FIELD(debuglevel), MCX_FIELD(normalizer), MCX_FIELD(seeddata), MCX_FIELD(gscatter),
     MCX_FIELD(savedetflag), MCX_FIELD(detectedcount), MCX_FIELD(runtime), MCX_FIELD(parentid), MCX_FIELD(mediabyte),
     MCX_FIELD(bc), MCX_FIELD(nphase), MCX_FIELD(invcdf), MCX_FIELD(nangle), MCX_FIELD(angleinvcdf), MCX_FIELD(srcid),
-    MCX_FIELD(extrasrclen), MCX_FIELD(srcdata), MCX_FIELD(replay), MCX_FIELD(replaydet), MCX_FIELD(exactmath), MCX_FIELD(kernelms), MCX_FIELD(eventcount),
+    MCX_FIELD(extrasrclen), MCX_FIELD(srcdata), MCX_FIELD(replay), MCX_FIELD(replaydet), MCX_FIELD(detdir), MCX_FIELD(exportjacob), MCX_FIELD(exactmath), MCX_FIELD(kernelms), MCX_FIELD(eventcount),
     MCX_FIELD(failedlaunch), MCX_FIELD(threadused), MCX_FIELD(exportenergy), MCX_FIELD(savethreadenergy),
     MCX_FIELD(autotune), MCX_FIELD(savedetweight), MCX_FIELD(exportdetweight), MCX_FIELD(replaysiteown),
     MCX_FIELD(errorcode), MCX_FIELD(errormsg),

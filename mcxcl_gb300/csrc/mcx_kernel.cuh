@@ -67,7 +67,7 @@ namespace {
 #define K_CONE_CAP       (1u << 16)     /* rejection draws of the cone source */
 
 enum { bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic };
-enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF };
+enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF, otAdjoint };
 enum { S_PENCIL, S_ISOTROPIC, S_CONE, S_GAUSSIAN, S_PLANAR, S_PATTERN, S_FOURIER, S_ARCSINE,
        S_DISK, S_FOURIERX, S_FOURIERX2D, S_ZGAUSSIAN, S_LINE, S_SLIT, S_PENCILARRAY, S_PATTERN3D,
        S_HYPERBOLOID, S_RING };
@@ -1422,7 +1422,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     int tshift = (int)(floorf((s.f.y - c_p.twin0) * c_p.Rtstep));
                     if (c_p.outputtype == otEnergy) {
                         weight = s.w0 - s.p.w;
-                    } else if (c_p.outputtype == otFluence || c_p.outputtype == otFlux) {
+                    } else if (c_p.outputtype == otFluence || c_p.outputtype == otFlux || c_p.outputtype >= otAdjoint) {
                         if (EXACT || c_p.mediaformat > 4) {
                             weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen) : M::div(s.w0 - s.p.w, s.prop.x);
                         } else {

@@ -147,6 +147,16 @@ def parse_config(cfg, C):
             raise ValueError("the 'detpos' field must have 4 columns (x,y,z,radius)")
         C.detnum = d.shape[0]
         C.detpos = _cbuf(d, Float4)
+    if "detdir" in cfg:
+        # per detector {vx, vy, vz, focal length}: detectors run as sources for the adjoint outputs
+        # (src/pmcxcl.cpp:693-724)
+        dd = np.asarray(cfg["detdir"], np.float32)
+        dd = dd.reshape(1, -1) if dd.ndim == 1 else dd
+        if dd.shape[1] != 4:
+            raise ValueError("the 'detdir' field must have 4 columns (vx,vy,vz,focallength)")
+        if dd.shape[0] != C.detnum:
+            raise ValueError("the number of rows in 'detdir' must match 'detpos'")
+        C.detdir = _cbuf(dd, Float4)
     if "prop" not in cfg:
         raise ValueError("You must define 'vol' and 'prop' field.")
     p = _rows(cfg["prop"], 4)
@@ -382,6 +392,16 @@ def _outputs(cfg, C):
         if C.exactmath:
             out["stat"]["eventcount"] = dict(zip(("step", "scatter", "launch", "reflect", "failed"),
                                                  [int(x) for x in C.eventcount]))
+    if C.outputtype[0] >= 11 and C.exportjacob:
+        # adjoint Jacobians by name, [Nx, Ny, Nz, sources x detectors] (src/pmcxcl.cpp:1413-1480)
+        ot = C.outputtype[0]
+        ns = C.extrasrclen + 1 - C.detnum
+        npair = ns * C.detnum
+        n = C.dim.x * C.dim.y * C.dim.z * npair
+        names = {11: ("jmua",), 12: ("jd",), 13: ("jmus",), 14: ("jmusp",), 15: ("jmua", "jd"), 16: ("jmua", "jmusp")}[ot]
+        j = np.ctypeslib.as_array(C.exportjacob, shape=(n * len(names),)).copy()
+        for k, name in enumerate(names):
+            out[name] = j[k * n:(k + 1) * n].reshape((C.dim.x, C.dim.y, C.dim.z, npair), order="F")
     if C.savethreadenergy and C.exportenergy:
         e = np.ctypeslib.as_array(C.exportenergy, shape=(2 * C.threadused,)).copy()
         out["threadenergy"] = e.reshape(C.threadused, 2)

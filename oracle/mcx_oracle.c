@@ -49,7 +49,7 @@
 #define CONE_DRAW_CAP      (1u << 16)  /* guard against a cone of zero half-angle */
 
 enum { bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic };
-enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF };
+enum { otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF, otAdjoint };
 enum { S_PENCIL, S_ISOTROPIC, S_CONE, S_GAUSSIAN, S_PLANAR, S_PATTERN, S_FOURIER, S_ARCSINE,
        S_DISK, S_FOURIERX, S_FOURIERX2D, S_ZGAUSSIAN, S_LINE, S_SLIT, S_PENCILARRAY, S_PATTERN3D,
        S_HYPERBOLOID, S_RING };
@@ -1102,7 +1102,7 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                 int tshift = (int)(floorf((s.f.y - c->twin0) * c->Rtstep));
                 if (c->outputtype == otEnergy) {
                     weight = s.w0 - s.p.w;
-                } else if (c->outputtype == otFluence || c->outputtype == otFlux) {
+                } else if (c->outputtype == otFluence || c->outputtype == otFlux || c->outputtype >= otAdjoint) {
                     weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen) : ((s.w0 - s.p.w) / (s.prop.x));
                 } else if (c->replay) {
                     /* replay Jacobian deposit, mcx_core.cl:2845-2858: the detected
@@ -1888,9 +1888,9 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
         stats.energyesc = eesc;
         if (in->isnormalized) {
             stats.energyabs = etot - eesc;
-            if (in->outputtype == otFlux || in->outputtype == otFluence) {
+            if (in->outputtype == otFlux || in->outputtype == otFluence || in->outputtype >= otAdjoint) {
                 scale = (float)((double)in->unitinmm / (etot * (double)Vvox * (double)in->tstep));
-                if (in->outputtype == otFluence) {
+                if (in->outputtype == otFluence || in->outputtype >= otAdjoint) {
                     scale *= in->tstep;
                 }
             } else if (in->outputtype == otEnergy || in->outputtype == otL) {
