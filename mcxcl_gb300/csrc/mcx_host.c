@@ -405,8 +405,15 @@ static void preprocess(Config* cfg) {
         if (cfg->medianum <= maxlabel) {
             MCX_ERROR(-4, "input media optical properties are less than the labels in the volume");
         }
-    } else if (cfg->mediabyte != MEDIA_MUA_FLOAT) {
-        MCX_ERROR(-4, "this build supports label volumes (mediabyte 1/2/4) and float mua (101)");
+    } else if (cfg->mediabyte == 99) {
+        for (size_t i = 0; i < nvox; i++) {
+            if ((cfg->vol[i] & 0x3FFFu) >= cfg->medianum) {
+                MCX_ERROR(-4, "input media optical properties are less than the labels in the volume");
+            }
+        }
+    } else if (cfg->mediabyte < 100 || cfg->mediabyte > 104) {
+        MCX_ERROR(-4, "this build supports label volumes (mediabyte 1/2/4), label + half property (99), half "
+                  "mua/mus (100, 102), float mua (101), byte (103) and short (104) mixtures");
     }
     if (cfg->srctype <= MCX_SRC_CONE || cfg->srctype == MCX_SRC_ARCSINE || cfg->srctype == MCX_SRC_ZGAUSSIAN) {
         point_src_voxel(cfg, cfg->srcpos, &cfg->srcparam2);
@@ -422,8 +429,11 @@ static void preprocess(Config* cfg) {
             cfg->deviceid[i] = '\0';
         }
     }
-    if (cfg->mediabyte == MEDIA_MUA_FLOAT && cfg->medianum < 2) {
+    if ((cfg->mediabyte == 100 || cfg->mediabyte == MEDIA_MUA_FLOAT || cfg->mediabyte == 102) && cfg->medianum < 2) {
         MCX_ERROR(-4, "the 'prop' field must contain at least 2 rows for the requested media format");
+    }
+    if ((cfg->mediabyte == 103 || cfg->mediabyte == 104) && cfg->medianum < 3) {
+        MCX_ERROR(-4, "the 'prop' field must contain at least 3 rows for the requested media format");
     }
     if (cfg->ismomentum) {
         cfg->savedetflag |= 0x8;

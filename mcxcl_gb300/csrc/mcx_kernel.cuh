@@ -40,6 +40,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cuda_fp16.h>
+
 #include <type_traits>
 
 #include "mcx_kparams.h"
@@ -255,15 +257,49 @@ __device__ __forceinline__ unsigned int media_at(const KArgs& a, const PS& ps, u
     return __ldg(a.media32 + i);
 }
 
-/* updateproperty, mcx_core.cl:1079-1096 */
+/* the less common encodings of updateproperty (mcx_core.cl:1099-1187) */
+template <class PS>
+__device__ __noinline__ void media_other(const PS& ps, const Shared& S, float4& prop, unsigned int w) {
+    const mcxg_kparams& c_p = ps.p();
+    if (c_p.mediaformat == 100 || c_p.mediaformat == 102) {
+        prop.x = fabsf(__half2float(__ushort_as_half((unsigned short)(w & 0xFFFFu))));
+        prop.y = fabsf(__half2float(__ushort_as_half((unsigned short)(w >> 16))));
+        prop.w = ps.prop(S, (!w) == 0).w;
+    } else if (c_p.mediaformat == 99) {
+        prop = ps.prop(S, w & 0x3FFFu);
+        const float v = fabsf(__half2float(__ushort_as_half((unsigned short)(w >> 16))));
+        const unsigned int k = (w & 0xC000u) >> 14;
+        prop.x = (k == 0) ? v : prop.x;
+        prop.y = (k == 1) ? v : prop.y;
+        prop.z = (k == 2) ? v : prop.z;
+        prop.w = (k == 3) ? v : prop.w;
+    } else if (c_p.mediaformat == 103) {
+        const float4 a = ps.prop(S, 1), b = ps.prop(S, 2);
+        prop.x = (float)(w & 0xFFu) * (1.f / 255.f) * (b.x - a.x) + a.x;
+        prop.y = (float)((w >> 8) & 0xFFu) * (1.f / 255.f) * (b.y - a.y) + a.y;
+        prop.z = (float)((w >> 16) & 0xFFu) * (1.f / 255.f) * (b.z - a.z) + a.z;
+        prop.w = (float)(w >> 24) * (1.f / 127.f) * (b.w - a.w) + a.w;
+    } else if (c_p.mediaformat == 104) {
+        const float4 a = ps.prop(S, 1), b = ps.prop(S, 2);
+        prop.x = (float)(w & 0xFFFFu) * (1.f / 65535.f) * (b.x - a.x) + a.x;
+        prop.y = (float)(w >> 16) * (1.f / 65535.f) * (b.y - a.y) + a.y;
+        prop.w = ps.prop(S, (!w) == 0).w;
+    }
+}
+
+/* updateproperty, mcx_core.cl:1079-1187: labels, float mua, half mua/mus,
+   label + one half-precision property, byte and short mixtures of rows 1-2 */
 template <class PS>
 __device__ __forceinline__ void updateprop(const PS& ps, const Shared& S, float4& prop, unsigned int mediaid) {
     const mcxg_kparams& c_p = ps.p();
+    const unsigned int w = mediaid & K_MED_MASK;
     if (c_p.mediaformat <= 4) {
-        prop = ps.prop(S, mediaid & K_MED_MASK);
-    } else {
+        prop = ps.prop(S, w);
+    } else if (c_p.mediaformat == 101) {
         prop.x = fabsf(__uint_as_float(mediaid));
-        prop.w = ps.prop(S, (!(mediaid & K_MED_MASK)) == 0).w;
+        prop.w = ps.prop(S, (!w) == 0).w;
+    } else {
+        media_other(ps, S, prop, w);
     }
 }
 
@@ -1301,12 +1337,11 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         /* Henyey-Greenstein, mcx_core.cl:2487-2493 */
                         tmp0 = (1.f - s.prop.z * s.prop.z) / (1.f - s.prop.z + 2.f * s.prop.z * rnd(s.t));
                         tmp0 *= tmp0;
-                        if (EXACT) {
-                            tmp0 = (1.f + s.prop.z * s.prop.z - tmp0) / (2.f * s.prop.z);
+                        if (EXACT || c_p.mediaformat > 4) {
+                            tmp0 = M::div(1.f + s.prop.z * s.prop.z - tmp0, 2.f * s.prop.z);
                         } else {
-                            /* __fdividef(a, 2g) == a * rcp(2g): the medium's rcp(2g) is staged */
-                            tmp0 = (1.f + s.prop.z * s.prop.z - tmp0) *
-                                   ps.recip(S, c_p.mediaformat <= 4 ? (s.mediaid & K_MED_MASK) : 1u).w;
+                            /* __fdividef(a, 2g) == a * rcp(2g): the label's rcp(2g) is staged */
+                            tmp0 = (1.f + s.prop.z * s.prop.z - tmp0) * ps.recip(S, s.mediaid & K_MED_MASK).w;
                         }
                         tmp0 = fmaxf(-1.f, fminf(1.f, tmp0));
                         if (EXACT) {
@@ -1326,7 +1361,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         }
                     }
                 }
-                if (DET && c_p.savedet && (s.mediaid & K_MED_MASK)) {
+                if (DET && c_p.savedet && (s.mediaid & K_MED_MASK) - 1u < c_p.maxmedia) {
                     unsigned int med = (s.mediaid & K_MED_MASK) - 1;
                     if (SAVE_NSCAT(c_p.savedetflag)) {
                         float* q = &ps.pp(med);
@@ -1393,7 +1428,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         }
         /* a photon in a label-0 voxel (entered from a medium of the same index)
            has no partial-path slot; the reference writes one slot early there */
-        if (DET && c_p.savedet && SAVE_PPATH(c_p.savedetflag) && (s.mediaid & K_MED_MASK)) {
+        if (DET && c_p.savedet && SAVE_PPATH(c_p.savedetflag) && (s.mediaid & K_MED_MASK) - 1u < c_p.maxmedia) {
             ps.pp(c_p.maxmedia * SAVE_NSCAT(c_p.savedetflag) + (s.mediaid & K_MED_MASK) - 1) += s.f.z;
         }
 
@@ -1518,8 +1553,9 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
 
         /* ---- Fresnel reflection / refraction (mcx_core.cl:3126-3278) */
         /* within the same voxel the medium and index are unchanged, so the test
-           below cannot fire */
-        if (REFL && c_p.dorefl_compiled && s.idx1d != idx1dold) {
+           below cannot fire -- except for the encodings from 100 on, whose test
+           compares with row 1's index rather than the voxel's */
+        if (REFL && c_p.dorefl_compiled && (s.idx1d != idx1dold || c_p.mediaformat >= 100)) {
             updateprop(ps, S, s.prop, s.mediaid);
             if (((s.mediaid && c_p.doreflect) ||
                  (s.mediaid == 0 && (((s.isdet & 0xF) == bcUnknown && c_p.doreflect) ||

@@ -14,7 +14,7 @@ import ctypes
 
 import numpy as np
 
-from . import _lib
+from . import _lib, media
 from ._lib import Config, ExtraSrc, Float4, GPUInfo, Medium
 
 SEED_FROM_FILE = -999
@@ -72,23 +72,10 @@ def _flags(s, letters):
     return v
 
 
-def _set_volume(C, vol):
-    """parseVolume (src/pmcxcl.cpp:93-426): dtype decides the media format."""
-    vol = np.asarray(vol)
-    if vol.dtype == np.float32 and vol.ndim == 4 and vol.shape[0] == 1:
-        words = np.asfortranarray(vol[0]).reshape(-1, order="F").view(np.uint32)
-        C.mediabyte = 101
-        dims = vol.shape[1:]
-    elif vol.dtype in (np.uint8, np.int8, np.uint16, np.int16, np.int32, np.uint32, np.int64, np.bool_):
-        if vol.ndim == 2:
-            vol = vol.reshape(vol.shape + (1,))
-        if vol.ndim != 3:
-            raise ValueError("the 'vol' field must be a 3D array of labels (or float32 [1,Nx,Ny,Nz] mua)")
-        words = np.asfortranarray(vol).reshape(-1, order="F").astype(np.uint32)
-        C.mediabyte = {1: 1, 2: 2}.get(vol.dtype.itemsize, 4)
-        dims = vol.shape
-    else:
-        raise TypeError("unsupported volume dtype %s" % vol.dtype)
+def _set_volume(C, vol, unitinmm=1.0):
+    """parseVolume (src/pmcxcl.cpp:93-426): dtype and leading dimension decide
+    the media format (mcxcl_gb300.media)."""
+    words, C.mediabyte, dims = media.encode(vol, unitinmm)
     C.dim.x, C.dim.y, C.dim.z = [int(d) for d in dims]
     C.vol = _cbuf(words, ctypes.c_uint)
 
@@ -139,7 +126,7 @@ def parse_config(cfg, C):
         C.steps.x, C.steps.y, C.steps.z = [float(x) for x in s[:3]]
     if "vol" not in cfg:
         raise ValueError("Configuration must specify a 2/3/4D volume.")
-    _set_volume(C, cfg["vol"])
+    _set_volume(C, cfg["vol"], float(cfg.get("unitinmm", 1.0)))
     _set_sources(C, cfg)
     if "detpos" in cfg and np.asarray(cfg["detpos"]).size:
         d = _rows(cfg["detpos"], 4)

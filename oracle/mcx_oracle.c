@@ -208,13 +208,47 @@ static inline long long replay_index(const ocfg* c, unsigned int tid, long long 
     return t * (long long)c->threadphoton + (t < m ? t : m) + offset;
 }
 
-/* updateproperty, mcx_core.cl:1079-1096 (label and MEDIA_MUA_FLOAT formats) */
+/* IEEE half -> float (exact) */
+static inline float half2f(uint32_t h) {
+    uint32_t s = (h & 0x8000u) << 16, e = (h >> 10) & 0x1Fu, m = h & 0x3FFu;
+    if (e == 0) {
+        float v = (float)m * (1.f / 16777216.f);     /* m * 2^-24, exact */
+        return s ? -v : v;
+    }
+    if (e == 31) {
+        return bits2f(s | 0x7F800000u | (m << 13));
+    }
+    return bits2f(s | ((e + 112u) << 23) | (m << 13));
+}
+
+/* updateproperty, mcx_core.cl:1079-1187: labels, float mua, half mua/mus,
+   label + one half-precision property, byte and short mixtures of rows 1-2 */
 static inline void updateprop(const ocfg* c, f4* prop, uint32_t mediaid) {
+    const uint32_t w = mediaid & MED_MASK;
     if (c->mediaformat <= 4) {
-        *prop = c->gprop[mediaid & MED_MASK];
-    } else {
+        *prop = c->gprop[w];
+    } else if (c->mediaformat == MEDIA_MUA_FLOAT) {
         prop->x = fabsf(bits2f(mediaid));
-        prop->w = c->gprop[(!(mediaid & MED_MASK)) == 0].w;
+        prop->w = c->gprop[(!w) == 0].w;
+    } else if (c->mediaformat == 100 || c->mediaformat == 102) {
+        prop->x = fabsf(half2f(w & 0xFFFFu));
+        prop->y = fabsf(half2f(w >> 16));
+        prop->w = c->gprop[(!w) == 0].w;
+    } else if (c->mediaformat == 99) {
+        float* p = (float*)prop;
+        *prop = c->gprop[w & 0x3FFFu];
+        p[(w & 0xC000u) >> 14] = fabsf(half2f(w >> 16));
+    } else if (c->mediaformat == 103) {
+        const f4 a = c->gprop[1], b = c->gprop[2];
+        prop->x = (float)(w & 0xFF) * (1.f / 255.f) * (b.x - a.x) + a.x;
+        prop->y = (float)((w >> 8) & 0xFF) * (1.f / 255.f) * (b.y - a.y) + a.y;
+        prop->z = (float)((w >> 16) & 0xFF) * (1.f / 255.f) * (b.z - a.z) + a.z;
+        prop->w = (float)(w >> 24) * (1.f / 127.f) * (b.w - a.w) + a.w;
+    } else if (c->mediaformat == 104) {
+        const f4 a = c->gprop[1], b = c->gprop[2];
+        prop->x = (float)(w & 0xFFFF) * (1.f / 65535.f) * (b.x - a.x) + a.x;
+        prop->y = (float)(w >> 16) * (1.f / 65535.f) * (b.y - a.y) + a.y;
+        prop->w = c->gprop[(!w) == 0].w;
     }
 }
 
@@ -1010,11 +1044,13 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                         m_sincos(c, theta, &stheta, &ctheta);
                     }
                 }
-                if (SAVE_NSCAT(c->savedetflag)) {
+                /* per-medium slots exist for labels 1..maxmedia; the reference indexes
+                   outside them for label 0 and for label-half words */
+                if (SAVE_NSCAT(c->savedetflag) && (s.mediaid & MED_MASK) - 1u < c->maxmedia) {
                     uint32_t n = f2bits(s.ppath[(s.mediaid & MED_MASK) - 1]) + 1u;
                     s.ppath[(s.mediaid & MED_MASK) - 1] = bits2f(n);
                 }
-                if (SAVE_MOM(c->savedetflag)) {
+                if (SAVE_MOM(c->savedetflag) && (s.mediaid & MED_MASK) - 1u < c->maxmedia) {
                     s.ppath[c->maxmedia * (SAVE_NSCAT(c->savedetflag) + SAVE_PPATH(c->savedetflag)) + (s.mediaid & MED_MASK) - 1] += 1.f - ctheta;
                 }
                 if (c->is2d) {
@@ -1076,7 +1112,7 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
             s.f.x -= slen;
             s.f.y += s.f.z * s.prop.w * c->oneoverc0;
         }
-        if (c->savedet && SAVE_PPATH(c->savedetflag)) {
+        if (c->savedet && SAVE_PPATH(c->savedetflag) && (s.mediaid & MED_MASK) - 1u < c->maxmedia) {
             s.ppath[c->maxmedia * (SAVE_NSCAT(c->savedetflag)) + (s.mediaid & MED_MASK) - 1] += s.f.z;
         }
 
@@ -1448,7 +1484,7 @@ static int prepare(const mcxo_input* in, oprep* P) {
     if (in->dimx == 0 || in->dimy == 0 || in->dimz == 0 || in->medianum == 0 || in->nthread == 0) {
         return -1;
     }
-    if (in->mediabyte != 1 && in->mediabyte != 2 && in->mediabyte != 4 && in->mediabyte != MEDIA_MUA_FLOAT) {
+    if (in->mediabyte != 1 && in->mediabyte != 2 && in->mediabyte != 4 && !(in->mediabyte >= 99 && in->mediabyte <= 104)) {
         return -2;
     }
     if (in->srcnum > 1 || in->issaveref > 1) {

@@ -147,16 +147,14 @@ def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT
     Returns (struct, keepalive) -- keepalive holds the numpy buffers."""
     keep = {}
     inp = MCXOInput()
-    vol = np.asarray(cfg["vol"])
-    if vol.dtype == np.float32 and vol.ndim == 4 and vol.shape[0] == 1:
-        words = np.asfortranarray(vol[0]).view(np.uint32)
-        inp.mediabyte = 101
-        dims = vol.shape[1:]
-    else:
-        words = np.asfortranarray(vol).astype(np.uint32)
-        inp.mediabyte = {1: 1, 2: 2, 4: 4}.get(np.dtype(vol.dtype).itemsize, 4)
-        dims = vol.shape
-    words = np.ascontiguousarray(words.reshape(-1, order="F"))
+    # the pmcxcl volume encoding (src/pmcxcl.cpp:93-426): the oracle decodes the
+    # same words the kernel gets
+    import sys
+    if os.path.dirname(HERE) not in sys.path:
+        sys.path.insert(0, os.path.dirname(HERE))
+    from mcxcl_gb300 import media
+    words, inp.mediabyte, dims = media.encode(cfg["vol"], float(cfg.get("unitinmm", 1.0)))
+    words = np.ascontiguousarray(words)
     keep["vol"] = words
     inp.dimx, inp.dimy, inp.dimz = [int(d) for d in dims]
     inp.vol = _ptr(words)

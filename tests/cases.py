@@ -110,7 +110,38 @@ VARIANTS = {
     "muafloat": dict(vol=(0.005 + 0.02 * np.random.RandomState(3).rand(1, 40, 40, 40)).astype(np.float32),
                      prop=[[0, 0, 1, 1], [0.01, 1, 0.5, 1.37]], savedetflag="dxvw"),
 }
-NOT_PINNED = {"muafloat"}
+def _f2h_vol():
+    r = np.random.RandomState(4)
+    v = np.zeros((2, 40, 40, 40), np.float32)
+    v[0] = 0.005 + 0.02 * r.rand(40, 40, 40)
+    v[1] = 0.5 + 1.5 * r.rand(40, 40, 40)
+    return v
+
+
+def _labelhalf_vol():
+    v = np.zeros((3, 40, 40, 40), np.float32)
+    v[2] = 1
+    v[2, 10:30, 10:30, 10:30] = 2
+    v[1, 10:30, 10:30, 10:30] = 2               # replace g of label 2 ...
+    v[0, 10:30, 10:30, 10:30] = 0.7             # ... by 0.7
+    return v
+
+
+VARIANTS.update({
+    # half-precision mua/mus per voxel (MEDIA_AS_F2H)
+    "asf2h": dict(vol=_f2h_vol(), prop=[[0, 0, 1, 1], [0.01, 1, 0.5, 1.37]], savedetflag="dxvw"),
+    # labels with one property overridden in half precision (MEDIA_LABEL_HALF)
+    "labelhalf": dict(vol=_labelhalf_vol(), savedetflag="dxvw"),
+    # byte and short mixtures of property rows 1 and 2 (MEDIA_ASGN_BYTE, MEDIA_AS_SHORT)
+    # (the top bit of each word is the detector flag, so the last byte/short stays below 2^7 / 2^15)
+    "asgnbyte": dict(vol=(np.random.RandomState(5).randint(0, 256, (4, 40, 40, 40)) |
+                          np.array([1, 0, 0, 0])[:, None, None, None]).astype(np.uint8) &
+                         np.array([255, 255, 255, 127], np.uint8)[:, None, None, None],
+                     savedetflag="dxvw"),
+    "asshort": dict(vol=np.random.RandomState(6).randint(1, 32767, (2, 40, 40, 40)).astype(np.int16),
+                    savedetflag="dxvw"),
+})
+NOT_PINNED = {"muafloat", "asf2h", "labelhalf", "asgnbyte", "asshort"}
 
 
 def variant(name, **kw):

@@ -152,3 +152,43 @@ def test_pmath_accuracy():
         L.mcxo_pm_sincosf(ctypes.c_float(x), ctypes.byref(s), ctypes.byref(c))
         assert abs(s.value - np.sin(np.float64(x))) < 3e-7
         assert abs(c.value - np.cos(np.float64(x))) < 3e-7
+
+
+def test_volume_encodings():
+    """pmcxcl's volume encodings (src/pmcxcl.cpp:93-426): float mua scaled by
+    unitinmm with 0 -> EPS and NaN -> 0; the reference's truncating
+    float -> half conversion; label + half property; byte and short words."""
+    from mcxcl_gb300 import media
+    v = np.zeros((1, 2, 1, 1), np.float32)
+    v[0, 0], v[0, 1] = 0.0, np.nan
+    w, mb, dims = media.encode(v, 0.5)
+    assert mb == 101 and dims == (2, 1, 1)
+    assert w[0] == np.float32(1e-10).view(np.uint32) and w[1] == 0
+    w, _, _ = media.encode(np.full((1, 1, 1, 1), 0.02, np.float32), 0.5)
+    assert w[0] == np.float32(np.float32(0.02) * np.float32(0.5)).view(np.uint32)
+    # normal numbers: sign | (exponent - 112) << 10 | top ten mantissa bits (truncation, not rounding)
+    x = np.array([1.0, 0.5, 0.01, 1.37, 3.0, 0.333333], np.float32)
+    b = x.view(np.uint32).astype(np.int64)
+    want = ((((b >> 31) << 5) | (((b >> 23) & 0xFF) - 112)) << 10) | ((b >> 13) & 0x3FF)
+    assert np.array_equal(media.float_to_half_bits(x).astype(np.int64), want)
+    v2 = np.zeros((2, 1, 1, 1), np.float32)
+    v2[:, 0, 0, 0] = [0.01, 1.0]
+    w, mb, _ = media.encode(v2)
+    assert mb == 100 and w[0] == (0x211E | (0x3C00 << 16))
+    w, mb, _ = media.encode(np.zeros((2, 1, 1, 1), np.float32))
+    assert w[0] == 0x00010000                       # an all-zero voxel is not void
+    v3 = np.zeros((3, 1, 1, 1), np.float32)
+    v3[:, 0, 0, 0] = [0.7, 2, 5]                    # g of label 5 -> 0.7
+    w, mb, _ = media.encode(v3)
+    assert mb == 99 and (w[0] & 0x3FFF) == 5 and ((w[0] >> 14) & 3) == 2
+    assert (w[0] >> 16) == media.float_to_half_bits(np.array([0.7], np.float32))[0]
+    v4 = np.zeros((4, 2, 1, 1), np.uint8)
+    v4[:, 1, 0, 0] = [1, 2, 3, 4]
+    w, mb, _ = media.encode(v4)
+    assert mb == 103 and w[1] == 0x04030201
+    v5 = np.zeros((2, 1, 1, 1), np.int16)
+    v5[:, 0, 0, 0] = [7, 9]
+    w, mb, _ = media.encode(v5)
+    assert mb == 104 and w[0] == (9 << 16 | 7)
+    with pytest.raises(ValueError):
+        media.encode(np.zeros((8, 2, 2, 2), np.uint8))

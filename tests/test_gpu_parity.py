@@ -57,7 +57,7 @@ EXACT_CASES = ["pencil_gates", "isotropic", "cone", "gaussian", "planar", "fouri
                "fourierx", "fourierx2d", "zgaussian", "line", "slit", "pencilarray", "hyperboloid", "ring",
                "pattern", "pattern3d", "focus", "lambert", "noreflect", "cyclic", "facedet", "roulette",
                "unitinmm", "gscatter", "outside_src_specular", "multisrc", "multisrc_id", "energy_out",
-               "fluence_out", "invcdf", "angleinvcdf", "muafloat"]
+               "fluence_out", "invcdf", "angleinvcdf", "muafloat", "asf2h", "labelhalf", "asgnbyte", "asshort"]
 
 
 @pytest.mark.parametrize("name", EXACT_CASES)
