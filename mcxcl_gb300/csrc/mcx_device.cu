@@ -725,15 +725,16 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     /* deposits go straight to the field unless aggregation is asked for or
        the autotuner found it faster for this problem */
     const bool noagg = (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
-    const int bpsm_sel = s->bpsm_req ? s->bpsm_req : 3;
+    const bool xmedia = kp.mediaformat > 4 && kp.mediaformat != 101;
+    const int bpsm_sel = xmedia ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
-                 (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0);
+                 (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0);
     int block = s->block_req ? s->block_req : 256;
     size_t smem = shared_bytes(kp, block);
     if (smem > s->info.sharedmem_per_block) {
         return MCXG_ERR_LIMIT;
     }
-    int bpsm = s->bpsm_req ? s->bpsm_req : (exact ? 2 : bpsm_sel);
+    int bpsm = (s->bpsm_req && !xmedia) ? s->bpsm_req : (exact ? 2 : bpsm_sel);
     if (!exact) {
         /* never more blocks than fit at once: a persistent grid must be resident */
         int occ = 0;

@@ -123,8 +123,10 @@ extern __shared__ float4 mcxg_smem[];
  * parameter takes the source and binds `c_p` to it locally, so the physics
  * code is the same text for both.
  */
-struct ConstPS {
+template <bool XMEDIA>
+struct ConstPST {
     static constexpr bool kBatch = false;
+    static constexpr bool kXMedia = XMEDIA;   /* decode the encodings beyond labels and float mua */
     __device__ __forceinline__ const mcxg_kparams& p() const { return c_p; }
     __device__ __forceinline__ const float4* det() const { return c_det; }
     __device__ __forceinline__ const float4* srcx() const { return c_srcx; }
@@ -153,8 +155,11 @@ struct ConstPS {
     }
 };
 
+using ConstPS = ConstPST<false>;
+
 struct BatchPS {
     static constexpr bool kBatch = true;
+    static constexpr bool kXMedia = false;
     const mcxg_simdesc* d;
     unsigned int lo;               /* low-plane offset: the batch's total field length */
     __device__ __forceinline__ const mcxg_kparams& p() const { return d->kp; }
@@ -257,9 +262,10 @@ __device__ __forceinline__ unsigned int media_at(const KArgs& a, const PS& ps, u
     return __ldg(a.media32 + i);
 }
 
-/* the less common encodings of updateproperty (mcx_core.cl:1099-1187) */
+/* the less common encodings of updateproperty (mcx_core.cl:1099-1187),
+   compiled only into the instantiations that take them */
 template <class PS>
-__device__ __noinline__ void media_other(const PS& ps, const Shared& S, float4& prop, unsigned int w) {
+__device__ __forceinline__ void media_other(const PS& ps, const Shared& S, float4& prop, unsigned int w) {
     const mcxg_kparams& c_p = ps.p();
     if (c_p.mediaformat == 100 || c_p.mediaformat == 102) {
         prop.x = fabsf(__half2float(__ushort_as_half((unsigned short)(w & 0xFFFFu))));
@@ -299,7 +305,9 @@ __device__ __forceinline__ void updateprop(const PS& ps, const Shared& S, float4
         prop.x = fabsf(__uint_as_float(mediaid));
         prop.w = ps.prop(S, (!w) == 0).w;
     } else {
-        media_other(ps, S, prop, w);
+        if (PS::kXMedia) {
+            media_other(ps, S, prop, w);
+        }
     }
 }
 
@@ -1185,7 +1193,8 @@ __device__ __forceinline__ void vt_begin(const KArgs& a, const PS& ps, const Sha
 /* Next reference thread for this GPU thread: a global counter over the
    single simulation's threads, or over the concatenated threads of a batch
    (the simulation found by binary search in the prefix of thread counts). */
-__device__ __forceinline__ bool claim_vt(const KArgs& a, ConstPS&, unsigned int& vt) {
+template <bool X>
+__device__ __forceinline__ bool claim_vt(const KArgs& a, ConstPST<X>&, unsigned int& vt) {
     vt = atomicAdd(a.vtcounter, 1u);
     return vt < c_p.nthread;
 }
@@ -1209,10 +1218,10 @@ __device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPS& ps, unsigned i
     return true;
 }
 
-template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false>
+template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
-    typedef typename std::conditional<BATCH, BatchPS, ConstPS>::type PS;
+    typedef typename std::conditional<BATCH, BatchPS, ConstPST<XMEDIA>>::type PS;
     PS ps;
     Shared S;
     S.bprop = S.brecip = a.gprop;
@@ -1555,7 +1564,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         /* within the same voxel the medium and index are unchanged, so the test
            below cannot fire -- except for the encodings from 100 on, whose test
            compares with row 1's index rather than the voxel's */
-        if (REFL && c_p.dorefl_compiled && (s.idx1d != idx1dold || c_p.mediaformat >= 100)) {
+        if (REFL && c_p.dorefl_compiled && (s.idx1d != idx1dold || (PS::kXMedia && c_p.mediaformat >= 100))) {
             updateprop(ps, S, s.prop, s.mediaid);
             if (((s.mediaid && c_p.doreflect) ||
                  (s.mediaid == 0 && (((s.isdet & 0xF) == bcUnknown && c_p.doreflect) ||

@@ -33,8 +33,18 @@ static void* kbatch(bool occ3) {
            : (void*)mcx_transport<false, false, REFL, WAGG, false, 2, true>;
 }
 
+/* volumes in the less common encodings: 3 blocks/SM, direct deposits */
+template <bool DET, bool REFL>
+static void* kxmedia() {
+    return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, true>;
+}
+
 static void* select(int flags) {
     const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    if (flags & LF_XMEDIA) {
+        return det ? (refl ? kxmedia<true, true>() : kxmedia<true, false>())
+                   : (refl ? kxmedia<false, true>() : kxmedia<false, false>());
+    }
     if (flags & LF_BATCH) {
         if (wagg) {
             return refl ? kbatch<true, true>(o3) : kbatch<false, true>(o3);
