@@ -243,8 +243,8 @@ struct mcxg_session* mcx_prepare_simulation(Config* cfg);
 /* Runs n validated configurations in one persistent launch: a GB300
    addition, no counterpart in the reference (one simulation per
    mcx_run_simulation call).  Each simulation gets ceil(nphoton /
-   photons_per_thread) reference threads (0 = 64) with seeds derived from its
-   cfg.seed; flags: MCXG_GRAPH, MCXG_AGG.  Outputs go to each Config as
+   photons_per_thread) reference threads (0: ceil(nphoton / 2^18) photons a
+   thread, clamped to 1..64) with seeds derived from its cfg.seed; flags: MCXG_GRAPH, MCXG_AGG.  Outputs go to each Config as
    mcx_run_simulation's do; an error is reported on cfgs[0].  Label volumes
    of at most 128 labels, one respin, no detectors, replay, extra sources,
    patterns or phase tables. */
@@ -310,16 +310,18 @@ int  mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread);
    256-thread blocks per SM (also the automatic choice); 2 the uncapped one. */
 int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
 /* ---- batches: many simulations in one persistent launch (no counterpart in
-   the reference, which launches once per simulation).  sims[i] holds the
-   parameter block of simulation i (nthread = its reference threads,
-   fieldlen = its field) and its offsets into the concatenated buffers:
-   media (one byte per voxel, label | detector bit << 7), prop4 (rows of
-   {mua, mus, g, n}) and the field.  Reference threads are numbered
-   contiguously across the batch (vt_off); seeds come from splitmix64 of the
-   simulation's seed.  Not supported in a batch: detectors, replay, extra
-   sources, patterns, phase tables. */
+   the reference, which launches once per simulation).  sims points to nsim
+   mcxg_simdesc (csrc/mcx_kparams.h, desc_size bytes each): the parameter
+   block of simulation i (nthread = its reference threads, fieldlen = its
+   field), its property rows (at most MCXG_BATCH_MAXMEDIA) and its offsets
+   into the concatenated volume (one byte per voxel, label | detector
+   bit << 7) and field.  Reference threads are numbered contiguously across
+   the batch (vt_off); seeds come from splitmix64 of the simulation's seed.
+   The simulations run in waves of 140, whose descriptors the kernel reads
+   from constant memory.  Not supported in a batch: detectors, replay, extra
+   sources, patterns, phase tables, encodings other than labels. */
 int  mcxg_batch_set(mcxg_session* s, const void* sims, size_t desc_size, uint32_t nsim, const uint8_t* media,
-                    uint64_t nmedia, const float* prop4, uint32_t nprop);
+                    uint64_t nmedia);
 /* Runs every simulation of the batch; MCXG_GRAPH replays a captured graph,
    MCXG_AGG aggregates deposits.  *kernel_ms covers the clear, transport and
    per-simulation sums. */

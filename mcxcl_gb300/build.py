@@ -21,6 +21,7 @@ NVCC_COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + C
 # exactly as written so it reproduces the CPU oracle bit for bit
 UNITS = {
     "mcx_kernel_fast.cu": ["--use_fast_math"],
+    "mcx_kernel_batch.cu": ["--use_fast_math"],
     "mcx_kernel_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
     "mcx_device.cu": [],
 }

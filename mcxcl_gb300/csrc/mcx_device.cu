@@ -85,10 +85,11 @@ struct mcxg_session {
     size_t sims_cap = 0;
     unsigned long long* d_simvt = nullptr;
     size_t simvt_cap = 0;
+    unsigned int* d_simctr = nullptr;   /* per-simulation reference-thread counters */
+    size_t simctr_cap = 0;
     uint8_t* d_bmedia = nullptr;
     size_t bmedia_cap = 0;
-    float4* d_bprop = nullptr;       /* property rows, then their reciprocals */
-    size_t bprop_cap = 0;
+    std::vector<unsigned long long> h_simvt;
     float* d_bfield = nullptr;       /* 2 x totalfield */
     size_t bfield_cap = 0;
     float2* d_benergy = nullptr;     /* per reference thread of the batch */
@@ -97,7 +98,7 @@ struct mcxg_session {
     size_t bsum_cap = 0;
     float* d_bout = nullptr;
     size_t bout_cap = 0;
-    uint32_t nsim = 0, nbprop = 0;
+    uint32_t nsim = 0;
     unsigned long long totalvt = 0, totalfield = 0;
     bool has_batch = false;
     int bt_block = 256, bt_bpsm = 3, bt_grid = 0;
@@ -207,12 +208,18 @@ __global__ void field_merge_blocks(const float* __restrict__ f, size_t n, size_t
     }
 }
 
-/* reciprocals of each property row, as the single-simulation kernel stages them */
-__global__ void batch_recip(const float4* __restrict__ prop, unsigned int n, float4* __restrict__ recip) {
+/* reciprocals of each simulation's property rows, as the single-simulation
+   kernel stages them */
+__global__ void batch_recip(mcxg_simdesc* __restrict__ sims, unsigned int nsim) {
+    const unsigned int n = nsim * MCXG_BATCH_MAXMEDIA;
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 q = prop[i];
-        recip[i] = make_float4(__fdividef(1.f, q.y), __fdividef(1.f, q.y * (1.f - q.z)), __fdividef(1.f, q.x),
-                               __fdividef(1.f, 2.f * q.z));
+        mcxg_simdesc& d = sims[i / MCXG_BATCH_MAXMEDIA];
+        const mcxg_float4 q = d.prop[i % MCXG_BATCH_MAXMEDIA];
+        mcxg_float4& r = d.recip[i % MCXG_BATCH_MAXMEDIA];
+        r.x = __fdividef(1.f, q.y);
+        r.y = __fdividef(1.f, q.y * (1.f - q.z));
+        r.z = __fdividef(1.f, q.x);
+        r.w = __fdividef(1.f, 2.f * q.z);
     }
 }
 
@@ -488,7 +495,7 @@ int mcxg_destroy(mcxg_session* s) {
     void* bufs[] = {s->d_media, s->d_prop, s->d_tables, s->d_pattern, s->d_seeds, s->d_field, s->d_energy,
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
                     s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw,
-                    s->d_sims, s->d_simvt, s->d_bmedia, s->d_bprop, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
+                    s->d_sims, s->d_simvt, s->d_simctr, s->d_bmedia, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
                     s->d_adj};
     if (s->bgraph_exec) {
         cudaGraphExecDestroy(s->bgraph_exec);
@@ -1068,7 +1075,9 @@ int batch_reset_graph(mcxg_session* s) {
     return MCXG_OK;
 }
 
-/* the work of one batch run, on s->st: clear, transport, per-simulation sums */
+/* the work of one batch run, on s->st: clear; per wave of simulations, their
+   descriptors into constant memory and the transport launch; per-simulation
+   sums */
 int batch_enqueue(mcxg_session* s, int lflags) {
     MCXG_TRY(cudaMemsetAsync(s->d_bfield, 0, sizeof(float) * 2 * (size_t)s->totalfield, s->st));
     MCXG_TRY(cudaMemsetAsync(s->d_benergy, 0, sizeof(float2) * (size_t)s->totalvt, s->st));
@@ -1077,19 +1086,22 @@ int batch_enqueue(mcxg_session* s, int lflags) {
     memset(&a, 0, sizeof(a));
     a.media8 = s->d_bmedia;
     a.media32 = (const uint32_t*)s->d_bmedia;
-    a.gprop = s->d_bprop;
-    a.grecip = s->d_bprop + s->nbprop;
     a.field = s->d_bfield;
     a.energy = s->d_benergy;
     a.detcount = s->d_words + 0;
     a.vtcounter = s->d_words + 1;
     a.status = s->d_words + 2;
     a.counters = s->d_events;
-    a.sims = s->d_sims;
-    a.simvt = s->d_simvt;
-    a.nsim = s->nsim;
-    a.totalvt = s->totalvt;
-    MCXG_TRY(mcxg::fast_launch(a, lflags, s->bt_grid, s->bt_block, (size_t)s->bt_block * 32, s->st));
+    a.lo = (unsigned int)s->totalfield;
+    MCXG_TRY(cudaMemsetAsync(s->d_simctr, 0, sizeof(unsigned int) * s->nsim, s->st));
+    for (uint32_t w0 = 0; w0 < s->nsim; w0 += mcxg::kBatchWave) {
+        const uint32_t n = std::min<uint32_t>(mcxg::kBatchWave, s->nsim - w0);
+        MCXG_TRY(mcxg::batch_wave_upload(s->d_sims + w0, n, s->st));
+        MCXG_TRY(cudaMemsetAsync(s->d_words + 1, 0, sizeof(unsigned int), s->st));
+        a.simctr = s->d_simctr + w0;
+        a.nsim = n;
+        MCXG_TRY(mcxg::batch_launch(a, lflags, s->bt_grid, s->bt_block, (size_t)s->bt_block * 32, s->st));
+    }
     batch_energy<<<s->nsim, 256, 0, s->st>>>(s->d_benergy, s->d_sims, s->d_bsum);
     return MCXG_OK;
 }
@@ -1097,9 +1109,9 @@ int batch_enqueue(mcxg_session* s, int lflags) {
 }  // namespace
 
 int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_t nsim, const uint8_t* media,
-                   uint64_t nmedia, const float* prop4, uint32_t nprop) {
+                   uint64_t nmedia) {
     const mcxg_simdesc* sims = (const mcxg_simdesc*)sims_;
-    if (!s || !sims || desc_size != sizeof(mcxg_simdesc) || nsim == 0 || !media || !prop4 || nprop == 0) {
+    if (!s || !sims || desc_size != sizeof(mcxg_simdesc) || nsim == 0 || !media) {
         return MCXG_ERR_ARG;
     }
     /* the simulations' reference threads must number 0.. contiguously, and
@@ -1109,8 +1121,8 @@ int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_
     for (uint32_t i = 0; i < nsim; i++) {
         const mcxg_simdesc& d = sims[i];
         if (d.vt_off != vt || d.kp.nthread == 0 || d.kp.mediaword != 1 || d.kp.savedet || d.kp.replay ||
-                d.kp.extrasrclen || d.kp.nphase || d.kp.nangle || d.kp.npattern ||
-                d.media_off + d.kp.nvox > nmedia || d.prop_off + d.kp.medianum > nprop ||
+                d.kp.extrasrclen || d.kp.nphase || d.kp.nangle || d.kp.npattern || d.kp.mediaformat > 4 ||
+                d.kp.medianum > MCXG_BATCH_MAXMEDIA || d.media_off + d.kp.nvox > nmedia ||
                 (unsigned long long)d.kp.threadphoton * d.kp.nthread + (unsigned int)d.kp.oddphoton == 0) {
             return MCXG_ERR_ARG;
         }
@@ -1128,10 +1140,10 @@ int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_
         rc = ensure(&s->d_simvt, &s->simvt_cap, (size_t)nsim + 1);
     }
     if (!rc) {
-        rc = ensure(&s->d_bmedia, &s->bmedia_cap, (size_t)nmedia);
+        rc = ensure(&s->d_simctr, &s->simctr_cap, (size_t)nsim);
     }
     if (!rc) {
-        rc = ensure(&s->d_bprop, &s->bprop_cap, 2 * (size_t)nprop);
+        rc = ensure(&s->d_bmedia, &s->bmedia_cap, (size_t)nmedia);
     }
     if (!rc) {
         rc = ensure(&s->d_bfield, &s->bfield_cap, 2 * (size_t)field);
@@ -1149,13 +1161,12 @@ int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_
     MCXG_TRY(cudaMemcpyAsync(s->d_simvt, simvt.data(), sizeof(unsigned long long) * (nsim + 1), cudaMemcpyHostToDevice,
                              s->st));
     MCXG_TRY(cudaMemcpyAsync(s->d_bmedia, media, (size_t)nmedia, cudaMemcpyHostToDevice, s->st));
-    MCXG_TRY(cudaMemcpyAsync(s->d_bprop, prop4, sizeof(float4) * nprop, cudaMemcpyHostToDevice, s->st));
-    batch_recip<<<grid_for(s, nprop), 256, 0, s->st>>>(s->d_bprop, nprop, s->d_bprop + nprop);
+    batch_recip<<<grid_for(s, (size_t)nsim * MCXG_BATCH_MAXMEDIA), 256, 0, s->st>>>(s->d_sims, nsim);
     MCXG_TRY(cudaStreamSynchronize(s->st));
     MCXG_TRY(cudaGetLastError());
     s->h_sims.assign(sims, sims + nsim);
+    s->h_simvt = simvt;
     s->nsim = nsim;
-    s->nbprop = nprop;
     s->totalvt = vt;
     s->totalfield = field;
     s->has_batch = true;
@@ -1176,11 +1187,10 @@ int mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     }
     const bool agg = (flags & MCXG_AGG) != 0;
     const int bpsm_req = s->bpsm_req ? s->bpsm_req : 3;
-    int lflags = mcxg::LF_BATCH | (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) |
-                 (bpsm_req == 3 ? mcxg::LF_OCC3 : 0);
+    int lflags = (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) | (bpsm_req == 3 ? mcxg::LF_OCC3 : 0);
     int block = s->block_req ? s->block_req : 256;
     int occ = 0;
-    MCXG_TRY(mcxg::fast_occupancy(lflags, block, (size_t)block * 32, &occ));
+    MCXG_TRY(mcxg::batch_occupancy(lflags, block, (size_t)block * 32, &occ));
     int bpsm = std::max(1, std::min(bpsm_req, occ > 0 ? occ : bpsm_req));
     const int grid = s->info.sm * bpsm;
     if (grid != s->bt_grid || block != s->bt_block) {

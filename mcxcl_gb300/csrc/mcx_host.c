@@ -1337,6 +1337,20 @@ void mcx_savedetphoton(float* ppath, void* seeds, int count, int doappend, Confi
     MCX_LEAVE();
 }
 
+/* Reference threads of one batch simulation: ceil(nphoton / ppt), and with
+   ppt 0 a photon count per thread of ceil(nphoton / 2^18) clamped to 1..64.
+   The automatic count gives every simulation at least twice as many threads
+   as a GB300 keeps resident (152 SMs x 3 x 256), so the resident threads work
+   on one or two simulations at a time and a warp's lanes read one
+   descriptor, and it keeps the last threads of a wave short. */
+static size_t batch_threads(size_t nphoton, unsigned int ppt) {
+    if (!ppt) {
+        size_t p = (nphoton + (1u << 18) - 1) >> 18;
+        ppt = (unsigned int)(p < 1 ? 1 : (p > 64 ? 64 : p));
+    }
+    return (nphoton + ppt - 1) / ppt;
+}
+
 /* Runs n validated configurations in one persistent launch (a GB300
    addition: the reference runs one simulation per call).  Outputs go to each
    Config as mcx_run_simulation's do; errors are reported on cfgs[0]. */
@@ -1348,7 +1362,7 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
     }
 #define bdesc  (*(mcxg_simdesc**)&btmp[0])
 #define bmedia (*(uint8_t**)&btmp[1])
-#define bprop  (*(float**)&btmp[2])
+#define bscale (*(double**)&btmp[2])
 #define bfield (*(float**)&btmp[3])
 #define bsums  (*(double**)&btmp[4])
     if (n <= 0 || !cfgs || !cfgs[0]) {
@@ -1356,15 +1370,13 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
     }
     Config* cfg0 = cfgs[0];
     MCX_ENTER(cfg0);
-    unsigned int ppt = photons_per_thread ? photons_per_thread : 64;
     uint64_t nmedia = 0, nfield = 0, nvt = 0;
-    uint32_t nprop = 0;
     for (int k = 0; k < n; k++) {
         Config* cfg = cfgs[k];
         if (!cfg || cfg->issavedet || cfg->seed == SEED_FROM_FILE || cfg->extrasrclen || cfg->nphase || cfg->nangle ||
                 cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D || cfg->mediabyte > 4 ||
-                cfg->medianum > 128 || cfg->respin != 1 || cfg->issaveref || (cfg->debuglevel & 1)) {
-            MCX_ERROR(-4, "a batch simulation takes label volumes of at most 128 labels, one respin, and no "
+                cfg->medianum > MCXG_BATCH_MAXMEDIA || cfg->respin != 1 || cfg->issaveref || (cfg->debuglevel & 1)) {
+            MCX_ERROR(-4, "a batch simulation takes label volumes of at most 4 property rows, one respin, and no "
                       "detectors, replay, extra sources, patterns, phase tables or saved reflectance");
         }
         if (cfg->nphoton == 0) {
@@ -1374,8 +1386,7 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
         size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
         nmedia += nvox;
         nfield += nvox * cfg->maxgate;
-        nvt += (cfg->nphoton + ppt - 1) / ppt;
-        nprop += cfg->medianum;
+        nvt += batch_threads(cfg->nphoton, photons_per_thread);
     }
     if (nfield >= 0x7FFFFFFFull || nvt >= 0xF0000000ull) {
         MCX_ERROR(-1, "batch too large for 32-bit field indices or thread numbering");
@@ -1392,17 +1403,15 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
 
     bdesc = (mcxg_simdesc*)calloc((size_t)n, sizeof(mcxg_simdesc));
     bmedia = (uint8_t*)malloc(nmedia ? nmedia : 1);
-    bprop = (float*)malloc(sizeof(float) * 4 * nprop);
-    if (!bdesc || !bmedia || !bprop) {
+    if (!bdesc || !bmedia) {
         MCX_ERROR(-2, "out of host memory");
     }
     uint64_t moff = 0, foff = 0, voff = 0;
-    uint32_t poff = 0;
     for (int k = 0; k < n; k++) {
         Config* cfg = cfgs[k];
         size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
         size_t fieldlen = nvox * cfg->maxgate;
-        size_t vts = (cfg->nphoton + ppt - 1) / ppt;
+        size_t vts = batch_threads(cfg->nphoton, photons_per_thread);
         unsigned int is2d = (cfg->dim.x == 1 ? 1 : (cfg->dim.y == 1 ? 2 : (cfg->dim.z == 1 ? 3 : 0)));
         if (is2d) {
             is2d = is2d * (((cfg->dim.x > 1) + (cfg->dim.y > 1) + (cfg->dim.z > 1)) == 2);
@@ -1416,16 +1425,14 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
         d->media_off = moff;
         d->field_off = foff;
         d->vt_off = voff;
-        d->prop_off = poff;
         d->seed = (uint64_t)(uint32_t)(cfg->seed > 0 ? cfg->seed : (int)time(0) + k) * 0x100000001B3ull;
         for (size_t i = 0; i < nvox; i++) {
             bmedia[moff + i] = (uint8_t)(cfg->vol[i] & 0x7Fu);
         }
-        memcpy(bprop + 4 * (size_t)poff, cfg->prop, sizeof(float) * 4 * cfg->medianum);
+        memcpy(d->prop, cfg->prop, sizeof(float) * 4 * cfg->medianum);
         moff += nvox;
         foff += fieldlen;
         voff += vts;
-        poff += cfg->medianum;
         cfg->threadused = (unsigned int)vts;
     }
 
@@ -1433,17 +1440,14 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
     if (!s) {
         MCX_ERROR(-99, "failed to open a CUDA session on the selected GPU");
     }
-    device_check(mcxg_batch_set(s, bdesc, sizeof(mcxg_simdesc), (uint32_t)n, bmedia, nmedia, bprop, nprop),
-                 "uploading the batch");
+    device_check(mcxg_batch_set(s, bdesc, sizeof(mcxg_simdesc), (uint32_t)n, bmedia, nmedia), "uploading the batch");
     float kms = 0.f;
     device_check(mcxg_batch_simulate(s, flags, &kms), "running the batch");
-    /* the volume and property copies are resident now; their slots take the
-       sums and the scales (every slot is freed on both exit paths) */
+    /* the volume copy is resident now (every slot is freed on both exit paths) */
     free(btmp[1]);
-    free(btmp[2]);
     btmp[1] = NULL;
-    btmp[2] = malloc(sizeof(double) * (size_t)n);
-    double* scales = (double*)btmp[2];
+    bscale = (double*)malloc(sizeof(double) * (size_t)n);
+    double* scales = bscale;
     bsums = (double*)malloc(sizeof(double) * 2 * (size_t)n);
     if (!bsums || !scales) {
         MCX_ERROR(-2, "out of host memory");
@@ -1503,7 +1507,7 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
     }
 #undef bdesc
 #undef bmedia
-#undef bprop
+#undef bscale
 #undef bfield
 #undef bsums
     MCX_LEAVE();

@@ -87,8 +87,18 @@ enum { S_PENCIL, S_ISOTROPIC, S_CONE, S_GAUSSIAN, S_PLANAR, S_PATTERN, S_FOURIER
 #define ST_GUARD         1   /* photons stopped by a safety cap (steps, cone draws) or an index guard */
 
 __constant__ mcxg_kparams c_p;
+#ifdef MCXG_BATCH_TU
+/* the batch translation unit spends its constant bank on the descriptors of
+   the simulations of one wave; batches have no detectors or extra sources */
+#define MCXG_BATCH_WAVE 140
+__constant__ float4 c_det[1];
+__constant__ float4 c_srcx[4];
+__constant__ mcxg_simdesc c_sims[MCXG_BATCH_WAVE];
+#else
 __constant__ float4 c_det[MCXG_MAX_DET];
 __constant__ float4 c_srcx[MCXG_MAX_EXTRASRC * 4];
+__constant__ mcxg_simdesc c_sims[1];
+#endif
 
 
 
@@ -127,6 +137,7 @@ template <bool XMEDIA>
 struct ConstPST {
     static constexpr bool kBatch = false;
     static constexpr bool kXMedia = XMEDIA;   /* decode the encodings beyond labels and float mua */
+    __device__ __forceinline__ void init(const KArgs&) {}
     __device__ __forceinline__ const mcxg_kparams& p() const { return c_p; }
     __device__ __forceinline__ const float4* det() const { return c_det; }
     __device__ __forceinline__ const float4* srcx() const { return c_srcx; }
@@ -160,20 +171,30 @@ using ConstPS = ConstPST<false>;
 struct BatchPS {
     static constexpr bool kBatch = true;
     static constexpr bool kXMedia = false;
-    const mcxg_simdesc* d;
+    unsigned int sid;              /* the simulation of this wave the thread is running */
     unsigned int lo;               /* low-plane offset: the batch's total field length */
-    __device__ __forceinline__ const mcxg_kparams& p() const { return d->kp; }
+    __device__ __forceinline__ void init(const KArgs& a) {
+        sid = 0;
+        lo = a.lo;
+    }
+    __device__ __forceinline__ const mcxg_kparams& p() const { return c_sims[sid].kp; }
     __device__ __forceinline__ const float4* det() const { return c_det; }   /* batches save no detectors */
     __device__ __forceinline__ const float4* srcx() const { return c_srcx; } /* nor use extra sources */
-    __device__ __forceinline__ unsigned long long media_off() const { return d->media_off; }
-    __device__ __forceinline__ unsigned int field_off() const { return (unsigned int)d->field_off; }
+    __device__ __forceinline__ unsigned long long media_off() const { return c_sims[sid].media_off; }
+    __device__ __forceinline__ unsigned int field_off() const { return (unsigned int)c_sims[sid].field_off; }
     __device__ __forceinline__ unsigned int lo_plane() const { return lo; }
-    __device__ __forceinline__ unsigned long long vt_off() const { return d->vt_off; }
-    __device__ __forceinline__ unsigned int prop_off() const { return d->prop_off; }
-    __device__ __forceinline__ unsigned long long seed() const { return d->seed; }
+    __device__ __forceinline__ unsigned long long vt_off() const { return c_sims[sid].vt_off; }
+    __device__ __forceinline__ unsigned int prop_off() const { return 0u; }
+    __device__ __forceinline__ unsigned long long seed() const { return c_sims[sid].seed; }
     /* shared layout: ColdState[blockDim]; batches have no phase tables or detectors */
-    __device__ __forceinline__ const float4& prop(const Shared& S, unsigned int i) const { return S.bprop[i]; }
-    __device__ __forceinline__ const float4& recip(const Shared& S, unsigned int i) const { return S.brecip[i]; }
+    __device__ __forceinline__ float4 prop(const Shared&, unsigned int i) const {
+        const mcxg_float4& q = c_sims[sid].prop[i];
+        return make_float4(q.x, q.y, q.z, q.w);
+    }
+    __device__ __forceinline__ float4 recip(const Shared&, unsigned int i) const {
+        const mcxg_float4& q = c_sims[sid].recip[i];
+        return make_float4(q.x, q.y, q.z, q.w);
+    }
     __device__ __forceinline__ ColdState* cold() const { return (ColdState*)mcxg_smem + threadIdx.x; }
     __device__ __forceinline__ float* tables() const { return (float*)((ColdState*)mcxg_smem + blockDim.x); }
     __device__ __forceinline__ float invcdf(unsigned int i) const { return tables()[i]; }
@@ -1199,23 +1220,30 @@ __device__ __forceinline__ bool claim_vt(const KArgs& a, ConstPST<X>&, unsigned 
     return vt < c_p.nthread;
 }
 
+/* A batch thread keeps claiming reference threads of the simulation it is
+   in (one counter per simulation) and moves to the next open simulation only
+   when that one is exhausted, so the lanes of a warp stay in the same
+   simulation and read the same constant-memory descriptor.  A simulation is
+   left only once its counter has run out, so every reference thread is
+   claimed; `open` (the shared counter word) is one past the highest
+   simulation found exhausted. */
 __device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPS& ps, unsigned int& vt) {
-    const unsigned long long g = atomicAdd(a.vtcounter, 1u);
-    if (g >= a.totalvt) {
-        return false;
-    }
-    unsigned int lo = 0, hi = a.nsim;          /* simvt[lo] <= g < simvt[hi] */
-    while (hi - lo > 1) {
-        const unsigned int mid = (lo + hi) >> 1;
-        if (__ldg(a.simvt + mid) <= g) {
-            lo = mid;
-        } else {
-            hi = mid;
+    for (;;) {
+        if (ps.sid < a.nsim) {
+            const unsigned int v = atomicAdd(a.simctr + ps.sid, 1u);
+            if (v < c_sims[ps.sid].kp.nthread) {
+                vt = v;
+                return true;
+            }
+            atomicMax(a.vtcounter, ps.sid + 1);
         }
+        const unsigned int open = *(volatile unsigned int*)a.vtcounter;
+        const unsigned int next = open > ps.sid + 1 ? open : ps.sid + 1;
+        if (next >= a.nsim) {
+            return false;
+        }
+        ps.sid = next;
     }
-    ps.d = a.sims + lo;
-    vt = (unsigned int)(g - __ldg(a.simvt + lo));
-    return true;
 }
 
 template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false>
@@ -1223,6 +1251,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
     typedef typename std::conditional<BATCH, BatchPS, ConstPST<XMEDIA>>::type PS;
     PS ps;
+    ps.init(a);
     Shared S;
     S.bprop = S.brecip = a.gprop;
     if (!BATCH) {
@@ -1268,12 +1297,6 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         if (fresh || relaunch) {
             int r;
             if (fresh) {
-                if (BATCH) {
-                    /* a batch reads each simulation's rows from global memory (L1-resident):
-                       the threads of a block run different simulations */
-                    S.bprop = a.gprop + ps.prop_off();
-                    S.brecip = a.grecip + ps.prop_off();
-                }
                 vt_begin(a, ps, S, s, vt);
             }
             /* one call site for the first and every later launch keeps the hot loop small */

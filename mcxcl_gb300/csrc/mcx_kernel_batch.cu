@@ -1,0 +1,47 @@
+/*
+ * mcx_kernel_batch.cu -- the batch instantiations of the transport kernel
+ * (fast math, as mcx_kernel_fast.cu).  A separate translation unit so that
+ * its constant bank holds the descriptors of a whole wave of simulations:
+ * every thread reads the parameter block of the simulation it is running
+ * from constant memory, as the single-simulation kernel does.
+ */
+#define MCXG_BATCH_TU
+#include "mcx_kernel.cuh"
+#include "mcx_launch.h"
+
+namespace mcxg {
+
+static_assert(kBatchWave == MCXG_BATCH_WAVE, "wave size of the batch unit");
+static_assert(sizeof(c_sims) + sizeof(c_p) + 1024 <= 65536, "a wave of descriptors fits the constant bank");
+
+cudaError_t batch_wave_upload(const mcxg_simdesc* d_descs, unsigned int n, cudaStream_t st) {
+    if (n > MCXG_BATCH_WAVE) {
+        return cudaErrorInvalidValue;
+    }
+    return cudaMemcpyToSymbolAsync(c_sims, d_descs, sizeof(mcxg_simdesc) * n, 0, cudaMemcpyDeviceToDevice, st);
+}
+
+template <bool REFL, bool WAGG>
+static void* kbatch(bool occ3) {
+    return occ3 ? (void*)mcx_transport<false, false, REFL, WAGG, false, 3, true>
+           : (void*)mcx_transport<false, false, REFL, WAGG, false, 2, true>;
+}
+
+static void* select(int flags) {
+    const bool refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    if (wagg) {
+        return refl ? kbatch<true, true>(o3) : kbatch<false, true>(o3);
+    }
+    return refl ? kbatch<true, false>(o3) : kbatch<false, false>(o3);
+}
+
+cudaError_t batch_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st) {
+    void* args[] = {(void*)&a};
+    return cudaLaunchKernel(select(flags), dim3(grid), dim3(block), args, smem, st);
+}
+
+cudaError_t batch_occupancy(int flags, int block, size_t smem, int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, select(flags), block, smem);
+}
+
+}  // namespace mcxg

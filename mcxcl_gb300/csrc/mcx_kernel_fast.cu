@@ -26,13 +26,6 @@ static void* kfun(bool occ3) {
            : (void*)mcx_transport<false, DET, REFL, WAGG, false, 2>;
 }
 
-/* a batch of simulations: no detectors, parameters per simulation in global memory */
-template <bool REFL, bool WAGG>
-static void* kbatch(bool occ3) {
-    return occ3 ? (void*)mcx_transport<false, false, REFL, WAGG, false, 3, true>
-           : (void*)mcx_transport<false, false, REFL, WAGG, false, 2, true>;
-}
-
 /* volumes in the less common encodings: 3 blocks/SM, direct deposits */
 template <bool DET, bool REFL>
 static void* kxmedia() {
@@ -44,12 +37,6 @@ static void* select(int flags) {
     if (flags & LF_XMEDIA) {
         return det ? (refl ? kxmedia<true, true>() : kxmedia<true, false>())
                    : (refl ? kxmedia<false, true>() : kxmedia<false, false>());
-    }
-    if (flags & LF_BATCH) {
-        if (wagg) {
-            return refl ? kbatch<true, true>(o3) : kbatch<false, true>(o3);
-        }
-        return refl ? kbatch<true, false>(o3) : kbatch<false, false>(o3);
     }
     if (wagg) {
         if (det) {

@@ -72,14 +72,17 @@ typedef struct mcxg_kparams {
 /* One simulation of a batch: its parameter block (nthread = its reference
    threads, fieldlen = its own field) and where its data sit in the batch's
    concatenated buffers. */
+#define MCXG_BATCH_MAXMEDIA 4   /* property rows a batch simulation may have */
+
 typedef struct mcxg_simdesc {
     mcxg_kparams kp;
     uint64_t media_off;            /* first voxel in the batch volume */
     uint64_t field_off;            /* first element in the batch field planes */
     uint64_t vt_off;               /* first reference thread in the batch numbering */
     uint64_t seed;                 /* seeds of its reference threads: splitmix64 of seed ^ (vt << 1) */
-    uint32_t prop_off;             /* first row in the batch property table */
-    uint32_t pad;
+    uint64_t pad;
+    mcxg_float4 prop[MCXG_BATCH_MAXMEDIA];   /* {mua, mus, g, n} per label */
+    mcxg_float4 recip[MCXG_BATCH_MAXMEDIA];  /* filled on the device: 1/mus, 1/(mus (1-g)), 1/mua, 1/(2g) */
 } mcxg_simdesc;
 
 #endif

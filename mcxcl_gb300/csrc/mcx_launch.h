@@ -35,18 +35,15 @@ struct KArgs {
     const float* rweight;
     const float* rtof;
     const int* rdetid;
-    /* batch: per-simulation descriptors, the prefix of their reference-thread
-       counts (nsim + 1 entries), the concatenated property rows and their
-       reciprocals (fast kernel) */
-    const mcxg_simdesc* sims;
-    const unsigned long long* simvt;
+    /* batch wave: per-simulation reference-thread counters (nsim, zeroed),
+       the number of simulations in the wave, the batch's field length */
+    unsigned int* simctr;
     unsigned int nsim;
-    unsigned long long totalvt;
-    const float4* grecip;
+    unsigned int lo;
 };
 
 /* flag bits for the launch entries */
-enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_BATCH = 16, LF_XMEDIA = 32 };
+enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32 };
 
 /* fast instantiation: hardware transcendental approximations */
 cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,
@@ -60,6 +57,13 @@ cudaError_t exact_upload(const mcxg_kparams* p, const float* det4, unsigned int 
                          unsigned int nsrcx, cudaStream_t st);
 cudaError_t exact_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st);
 cudaError_t exact_rngdump(const KArgs& a, int grid, int block, cudaStream_t st);
+
+/* batch instantiations: simulation descriptors of one wave into constant
+   memory (from device memory), then the launch */
+constexpr int kBatchWave = 140;
+cudaError_t batch_wave_upload(const mcxg_simdesc* d_descs, unsigned int n, cudaStream_t st);
+cudaError_t batch_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st);
+cudaError_t batch_occupancy(int flags, int block, size_t smem, int* blocks_per_sm);
 }  // namespace mcxg
 
 #endif

@@ -302,13 +302,13 @@ def run(cfg=None, **kwargs):
         L.mcx_clearcfg(ctypes.byref(C))
 
 
-def run_batch(cfgs, photons_per_thread=64, graph=False, aggregate=False):
+def run_batch(cfgs, photons_per_thread=0, graph=False, aggregate=False):
     """Run many simulations in one persistent launch (a GB300 addition).
 
     cfgs: a list of run() dictionaries (label volumes, no detectors).  Returns
     the list of their output dictionaries, as run() would give one by one.
     photons_per_thread sets how many photons each reference thread (RNG
-    stream) runs; graph=True captures the launch as a CUDA graph."""
+    stream) runs (0: ceil(nphoton / 2**18), clamped to 1..64); graph=True captures the launch as a CUDA graph."""
     L = _lib.load()
     Cs = [Config() for _ in cfgs]
     try:
