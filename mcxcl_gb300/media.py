@@ -40,8 +40,9 @@ def float_to_half_bits(x):
     return (np.where(den, h_den, h_norm) & 0xFFFF).astype(np.uint16)
 
 
-def encode(vol, unitinmm=1.0):
-    """Returns (words uint32 [Nx*Ny*Nz], mediabyte, (Nx, Ny, Nz))."""
+def encode(vol, unitinmm=1.0, alloc=None):
+    """Returns (words uint32 [Nx*Ny*Nz], mediabyte, (Nx, Ny, Nz)).  alloc(n),
+    when given, supplies the uint32 array a label volume is written into."""
     vol = np.asarray(vol)
     u = np.float32(unitinmm)
     if vol.ndim == 4:
@@ -90,6 +91,8 @@ def encode(vol, unitinmm=1.0):
         raise ValueError("the 'vol' field must be a 2-D or 3-D array of labels or a 4-D array of properties")
     if vol.dtype.kind not in "uifb":
         raise TypeError("unsupported volume dtype %s" % vol.dtype)
-    words = np.asfortranarray(vol).reshape(-1, order="F").astype(np.uint32)
+    # x fastest: one strided pass that transposes and widens
+    words = alloc(vol.size) if alloc else np.empty(vol.size, np.uint32)
+    words.reshape(vol.shape[::-1])[...] = vol.T
     mb = {1: 1, 2: 2}.get(vol.dtype.itemsize, 4) if vol.dtype.kind in "uib" else 4
     return words, mb, vol.shape

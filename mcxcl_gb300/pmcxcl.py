@@ -53,6 +53,19 @@ def _cbuf(arr, ctype):
     return ctypes.cast(p, ctypes.POINTER(ctype))
 
 
+def _cempty(n, ctype, dtype):
+    """malloc'd memory owned by the Config (freed by mcx_clearcfg), as a
+    pointer and a numpy view of n elements."""
+    libc = _lib.libc()
+    libc.malloc.restype = ctypes.c_void_p
+    libc.malloc.argtypes = [ctypes.c_size_t]
+    p = libc.malloc(max(n * np.dtype(dtype).itemsize, 1))
+    if not p:
+        raise MemoryError("malloc failed")
+    ptr = ctypes.cast(p, ctypes.POINTER(ctype))
+    return ptr, np.ctypeslib.as_array(ptr, shape=(n,)).view(dtype)
+
+
 def _rows(v, ncol):
     a = np.asarray(v, dtype=np.float32)
     if a.ndim == 1:
@@ -75,9 +88,21 @@ def _flags(s, letters):
 def _set_volume(C, vol, unitinmm=1.0):
     """parseVolume (src/pmcxcl.cpp:93-426): dtype and leading dimension decide
     the media format (mcxcl_gb300.media)."""
-    words, C.mediabyte, dims = media.encode(vol, unitinmm)
+    held = []
+
+    def alloc(n):
+        ptr, view = _cempty(n, ctypes.c_uint, np.uint32)
+        held.append((ptr, view))
+        return view
+
+    words, C.mediabyte, dims = media.encode(vol, unitinmm, alloc)
     C.dim.x, C.dim.y, C.dim.z = [int(d) for d in dims]
-    C.vol = _cbuf(words, ctypes.c_uint)
+    if held and words is held[0][1]:
+        C.vol = held[0][0]
+    else:
+        for ptr, _ in held:
+            _lib.libc().free(ptr)
+        C.vol = _cbuf(words, ctypes.c_uint)
 
 
 def _set_sources(C, cfg):
