@@ -273,6 +273,8 @@ void mcx_release_sessions(void);
 #define MCXG_KEEP     8u   /* keep accumulating into the field (respin); energies, records and counters restart */
 #define MCXG_AGG     16u   /* aggregate same-voxel deposits of a warp before the atomics */
 #define MCXG_GRAPH   32u   /* batch: capture the run as a CUDA graph once, replay it afterwards */
+#define MCXG_GENERAL 64u   /* fast kernel: the general instantiation even where the one specialised for the
+                              common configuration (label volume, 3-D, Henyey-Greenstein) applies */
 
 typedef struct mcxg_devinfo {
     char name[64];

@@ -733,9 +733,12 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
        the autotuner found it faster for this problem */
     const bool noagg = (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
     const bool xmedia = kp.mediaformat > 4 && kp.mediaformat != 101;
+    /* the instantiations that fix the common configuration's parameters */
+    const bool common = !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2;
     const int bpsm_sel = xmedia ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
-                 (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0);
+                 (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
+                 (common ? mcxg::LF_COMMON : 0);
     int block = s->block_req ? s->block_req : 256;
     size_t smem = shared_bytes(kp, block);
     if (smem > s->info.sharedmem_per_block) {

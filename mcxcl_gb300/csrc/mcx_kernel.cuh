@@ -126,17 +126,18 @@ extern __shared__ float4 mcxg_smem[];
  *
  * Where the kernel reads its parameters.  One simulation keeps them in
  * constant memory (ConstPS).  A batch of simulations (BatchPS) keeps one
- * descriptor per simulation in global memory -- the parameter block plus the
- * simulation's offsets into the batch's volume, field, property and
- * reference-thread numbering -- and each thread follows the descriptor of the
- * reference thread it is running.  Every device function that reads a
+ * descriptor per simulation in constant memory -- the parameter block, the
+ * simulation's offsets into the batch's volume, field and reference-thread
+ * numbering, its seed and property rows -- and each thread follows the
+ * descriptor of the reference thread it is running.  Every device function that reads a
  * parameter takes the source and binds `c_p` to it locally, so the physics
  * code is the same text for both.
  */
-template <bool XMEDIA>
+template <bool XMEDIA, bool COMMON = false>
 struct ConstPST {
     static constexpr bool kBatch = false;
     static constexpr bool kXMedia = XMEDIA;   /* decode the encodings beyond labels and float mua */
+    static constexpr bool kCommon = COMMON;   /* the common configuration (KP_* below) */
     __device__ __forceinline__ void init(const KArgs&) {}
     __device__ __forceinline__ const mcxg_kparams& p() const { return c_p; }
     __device__ __forceinline__ const float4* det() const { return c_det; }
@@ -171,6 +172,7 @@ using ConstPS = ConstPST<false>;
 struct BatchPS {
     static constexpr bool kBatch = true;
     static constexpr bool kXMedia = false;
+    static constexpr bool kCommon = false;
     unsigned int sid;              /* the simulation of this wave the thread is running */
     unsigned int lo;               /* low-plane offset: the batch's total field length */
     __device__ __forceinline__ void init(const KArgs& a) {
@@ -201,6 +203,18 @@ struct BatchPS {
     __device__ __forceinline__ float angle(unsigned int i) const { return tables()[i]; }
     __device__ __forceinline__ float& pp(unsigned int slot) const { return tables()[slot * blockDim.x + threadIdx.x]; }
 };
+
+/* Parameters that the common-configuration instantiations fix at compile
+   time: label volumes (media format 1, 2 or 4), a 3-D domain and the
+   Henyey-Greenstein phase function.  These describe the medium, so a run and
+   the replay of its detected photons always take the same instantiation and
+   follow the same arithmetic.  The host selects the common instantiations
+   only for a configuration that has all three; the others read the parameter
+   block.  Used inside functions templated on the parameter source `PS` that
+   bind `c_p`. */
+#define KP_IS2D (PS::kCommon ? 0u : c_p.is2d)
+#define KP_NPHASE_GT2 (!PS::kCommon && c_p.nphase > 2)
+#define KP_MEDIAFORMAT (PS::kCommon ? 1u : c_p.mediaformat)
 
 /* ------------------------------------------------------------------ math */
 
@@ -320,9 +334,9 @@ template <class PS>
 __device__ __forceinline__ void updateprop(const PS& ps, const Shared& S, float4& prop, unsigned int mediaid) {
     const mcxg_kparams& c_p = ps.p();
     const unsigned int w = mediaid & K_MED_MASK;
-    if (c_p.mediaformat <= 4) {
+    if (KP_MEDIAFORMAT <= 4) {
         prop = ps.prop(S, w);
-    } else if (c_p.mediaformat == 101) {
+    } else if (KP_MEDIAFORMAT == 101) {
         prop.x = fabsf(__uint_as_float(mediaid));
         prop.w = ps.prop(S, (!w) == 0).w;
     } else {
@@ -1214,8 +1228,8 @@ __device__ __forceinline__ void vt_begin(const KArgs& a, const PS& ps, const Sha
 /* Next reference thread for this GPU thread: a global counter over the
    single simulation's threads, or over the concatenated threads of a batch
    (the simulation found by binary search in the prefix of thread counts). */
-template <bool X>
-__device__ __forceinline__ bool claim_vt(const KArgs& a, ConstPST<X>&, unsigned int& vt) {
+template <bool X, bool C>
+__device__ __forceinline__ bool claim_vt(const KArgs& a, ConstPST<X, C>&, unsigned int& vt) {
     vt = atomicAdd(a.vtcounter, 1u);
     return vt < c_p.nthread;
 }
@@ -1246,10 +1260,11 @@ __device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPS& ps, unsigned i
     }
 }
 
-template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false>
+template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false,
+          bool COMMON = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
-    typedef typename std::conditional<BATCH, BatchPS, ConstPST<XMEDIA>>::type PS;
+    typedef typename std::conditional<BATCH, BatchPS, ConstPST<XMEDIA, COMMON>>::type PS;
     PS ps;
     ps.init(a);
     Shared S;
@@ -1345,11 +1360,11 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 if (COUNT) {
                     cnt_scat++;
                 }
-                if (!c_p.is2d) {
+                if (!KP_IS2D) {
                     tmp0 = K_TWO_PI * rnd(s.t);
                     M::sincos(tmp0, &sphi, &cphi);
                 }
-                if (c_p.nphase > 2) {
+                if (KP_NPHASE_GT2) {
                     unsigned int np = c_p.nphase;
                     tmp0 = rnd(s.t) * (float)(np - 1);
                     theta = tmp0 - (float)((int)tmp0);
@@ -1369,7 +1384,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         /* Henyey-Greenstein, mcx_core.cl:2487-2493 */
                         tmp0 = (1.f - s.prop.z * s.prop.z) / (1.f - s.prop.z + 2.f * s.prop.z * rnd(s.t));
                         tmp0 *= tmp0;
-                        if (EXACT || c_p.mediaformat > 4) {
+                        if (EXACT || KP_MEDIAFORMAT > 4) {
                             tmp0 = M::div(1.f + s.prop.z * s.prop.z - tmp0, 2.f * s.prop.z);
                         } else {
                             /* __fdividef(a, 2g) == a * rcp(2g): the label's rcp(2g) is staged */
@@ -1403,8 +1418,8 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         ps.pp(c_p.maxmedia * (SAVE_NSCAT(c_p.savedetflag) + SAVE_PPATH(c_p.savedetflag)) + med) += 1.f - ctheta;
                     }
                 }
-                if (c_p.is2d) {
-                    rotatevector2d<EXACT>(s.v, (rnd(s.t) > 0.5f ? stheta : -stheta), ctheta, c_p.is2d);
+                if (KP_IS2D) {
+                    rotatevector2d<EXACT>(s.v, (rnd(s.t) > 0.5f ? stheta : -stheta), ctheta, KP_IS2D);
                 } else {
                     rotatevector<EXACT>(s.v, stheta, ctheta, sphi, cphi);
                 }
@@ -1434,7 +1449,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             const bool reduced = s.v.w + 1.f > gscat;
             float slen = s.f.z * s.prop.y * (reduced ? (1.f - s.prop.z) : 1.f);
             slen = fminf(slen, s.f.x);
-            if (EXACT || c_p.mediaformat > 4) {
+            if (EXACT || KP_MEDIAFORMAT > 4) {
                 s.f.z = M::div(slen, s.prop.y * (reduced ? (1.f - s.prop.z) : 1.f));
             } else {
                 const float4 rc = ps.recip(S, s.mediaid & K_MED_MASK);
@@ -1490,7 +1505,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     if (c_p.outputtype == otEnergy) {
                         weight = s.w0 - s.p.w;
                     } else if (c_p.outputtype == otFluence || c_p.outputtype == otFlux || c_p.outputtype >= otAdjoint) {
-                        if (EXACT || c_p.mediaformat > 4) {
+                        if (EXACT || KP_MEDIAFORMAT > 4) {
                             weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen) : M::div(s.w0 - s.p.w, s.prop.x);
                         } else {
                             /* prop still holds the medium the photon deposited in */
@@ -1587,14 +1602,14 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         /* within the same voxel the medium and index are unchanged, so the test
            below cannot fire -- except for the encodings from 100 on, whose test
            compares with row 1's index rather than the voxel's */
-        if (REFL && c_p.dorefl_compiled && (s.idx1d != idx1dold || (PS::kXMedia && c_p.mediaformat >= 100))) {
+        if (REFL && c_p.dorefl_compiled && (s.idx1d != idx1dold || (PS::kXMedia && KP_MEDIAFORMAT >= 100))) {
             updateprop(ps, S, s.prop, s.mediaid);
             if (((s.mediaid && c_p.doreflect) ||
                  (s.mediaid == 0 && (((s.isdet & 0xF) == bcUnknown && c_p.doreflect) ||
                                      ((s.isdet & 0xF) == bcReflect || (s.isdet & 0xF) == bcMirror)))) &&
                 (((s.isdet & 0xF) == bcMirror) ||
-                 s.n1 != ((c_p.mediaformat < 100) ? (s.prop.w)
-                          : (ps.prop(S, (s.mediaid > 0 && c_p.mediaformat >= 100) ? 1 : s.mediaid).w)))) {
+                 s.n1 != ((KP_MEDIAFORMAT < 100) ? (s.prop.w)
+                          : (ps.prop(S, (s.mediaid > 0 && KP_MEDIAFORMAT >= 100) ? 1 : s.mediaid).w)))) {
                 float Rtotal = 1.f;
                 if (COUNT) {
                     cnt_refl++;
@@ -1683,5 +1698,9 @@ __global__ void mcx_rng_dump(const KArgs a) {
 
 }  // namespace
 }  // namespace mcxg
+
+#undef KP_IS2D
+#undef KP_NPHASE_GT2
+#undef KP_MEDIAFORMAT
 
 #endif

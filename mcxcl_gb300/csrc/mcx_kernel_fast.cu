@@ -20,10 +20,24 @@ cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int n
     return e;
 }
 
-template <bool DET, bool REFL, bool WAGG>
+template <bool DET, bool REFL, bool WAGG, bool COMMON>
 static void* kfun(bool occ3) {
-    return occ3 ? (void*)mcx_transport<false, DET, REFL, WAGG, false, 3>
-           : (void*)mcx_transport<false, DET, REFL, WAGG, false, 2>;
+    return occ3 ? (void*)mcx_transport<false, DET, REFL, WAGG, false, 3, false, false, COMMON>
+           : (void*)mcx_transport<false, DET, REFL, WAGG, false, 2, false, false, COMMON>;
+}
+
+template <bool COMMON>
+static void* kshape(bool det, bool refl, bool wagg, bool o3) {
+    if (wagg) {
+        if (det) {
+            return refl ? kfun<true, true, true, COMMON>(o3) : kfun<true, false, true, COMMON>(o3);
+        }
+        return refl ? kfun<false, true, true, COMMON>(o3) : kfun<false, false, true, COMMON>(o3);
+    }
+    if (det) {
+        return refl ? kfun<true, true, false, COMMON>(o3) : kfun<true, false, false, COMMON>(o3);
+    }
+    return refl ? kfun<false, true, false, COMMON>(o3) : kfun<false, false, false, COMMON>(o3);
 }
 
 /* volumes in the less common encodings: 3 blocks/SM, direct deposits */
@@ -38,16 +52,7 @@ static void* select(int flags) {
         return det ? (refl ? kxmedia<true, true>() : kxmedia<true, false>())
                    : (refl ? kxmedia<false, true>() : kxmedia<false, false>());
     }
-    if (wagg) {
-        if (det) {
-            return refl ? kfun<true, true, true>(o3) : kfun<true, false, true>(o3);
-        }
-        return refl ? kfun<false, true, true>(o3) : kfun<false, false, true>(o3);
-    }
-    if (det) {
-        return refl ? kfun<true, true, false>(o3) : kfun<true, false, false>(o3);
-    }
-    return refl ? kfun<false, true, false>(o3) : kfun<false, false, false>(o3);
+    return (flags & LF_COMMON) ? kshape<true>(det, refl, wagg, o3) : kshape<false>(det, refl, wagg, o3);
 }
 
 cudaError_t fast_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st) {

@@ -37,7 +37,7 @@ def sphere_volume(n=60, center=(30, 30, 30), radius=15, inner=2, outer=1):
 def cubesph60(**kw):
     """60^3 cube with a radius-15 sphere of label 2, Fresnel on, 50 gates of
     0.1 ns and four disk detectors on the z=0 face: the two-medium benchmark
-    (BASELINE config 2; src/mcx_bench.h:200-252 is the 1-gate original)."""
+    (the benchmark workload; src/mcx_bench.h:200-252 is the 1-gate original)."""
     cfg = cube60(
         vol=sphere_volume(),
         prop=[[0, 0, 1, 1], [0.005, 1.0, 0.01, 1.37], [0.002, 5.0, 0.9, 1.0]],

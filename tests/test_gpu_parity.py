@@ -183,3 +183,42 @@ def test_autotuned_launch_keeps_the_answer(gpu):
         assert abs(_absorbed(g) - 0.1769) <= 0.005
         assert abs(g["stat"]["energytot"] - cfg["nphoton"]) <= 10
     assert b["stat"]["kernelms"] > 0
+
+
+def test_common_and_general_fast_kernels_agree(gpu):
+    """The fast instantiation specialised for label volumes in 3-D with the
+    Henyey-Greenstein phase function and the general one run the same physics
+    on the same RNG streams (their float arithmetic may round differently, and
+    a photon whose path then departs is an independent sample): the cube +
+    sphere problem gives the same absorbed fraction, temporal point spread
+    and depth profile from both."""
+    import ctypes
+    from mcxcl_gb300 import _lib, pmcxcl
+    L = _lib.load()
+    cfg = cases.cubesph60(nphoton=1000000, seed=4711, issavedet=0, issaveseed=0)
+    C = _lib.Config()
+    try:
+        pmcxcl.parse_config(dict(cfg), C)
+        L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
+        pmcxcl._check(C)
+        s = L.mcx_prepare_simulation(ctypes.byref(C))
+        pmcxcl._check(C)
+        n = 60 * 60 * 60 * 50
+        out = {}
+        for flags in (2, 2 | 64):      # MCXG_NOAGG, MCXG_NOAGG | MCXG_GENERAL
+            ms = ctypes.c_float()
+            assert L.mcxg_simulate(s, flags, ctypes.byref(ms)) == 0
+            esc, tot = ctypes.c_double(), ctypes.c_double()
+            assert L.mcxg_get_energy(s, ctypes.byref(esc), ctypes.byref(tot)) == 0
+            f = np.zeros(n, np.float32)
+            assert L.mcxg_get_field(s, f.ctypes.data, 1.0) == 0
+            out[flags] = (1.0 - esc.value / tot.value, f)
+    finally:
+        L.mcx_clearcfg(ctypes.byref(C))
+    (a0, f0), (a1, f1) = out[2], out[66]
+    assert abs(a0 - a1) < 2e-3, (a0, a1)
+    g0, g1 = [f.reshape(50, -1).sum(axis=1) for f in (f0, f1)]          # per gate
+    d0, d1 = [f.reshape(50, 60, 3600).sum(axis=(0, 2)) for f in (f0, f1)]  # per z slice
+    for u, v in ((g0, g1), (d0, d1)):
+        m = v > 0.01 * v.max()
+        assert np.all(np.abs(u[m] - v[m]) <= 0.02 * v[m]), np.abs(u[m] / v[m] - 1).max()
