@@ -234,6 +234,9 @@ int  mcx_last_error(const Config* cfg, const char** msg);
 /* Number of floats in one detected-photon record for this Config. */
 unsigned int mcx_detreclen(const Config* cfg);
 const char* mcx_version(void);
+/* The n words rand() returns after srand(seed) in glibc (the reference's
+   per-thread seed words), without the C library's per-call lock. */
+void mcx_rand_words(unsigned int seed, uint32_t* out, size_t n);
 /* Everything mcx_run_simulation does before its first launch -- device
    selection, parameter block, volume packing, upload, seeds of the first
    repetition -- and nothing after: returns the ready device session so a

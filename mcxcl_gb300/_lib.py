@@ -104,7 +104,7 @@ class DevInfo(ctypes.Structure):
 # every symbol include/mcx_gb300.h declares
 EXPORTS = [
     "mcx_initcfg", "mcx_clearcfg", "mcx_validatecfg", "mcx_list_gpu", "mcx_cleargpuinfo", "mcx_run_simulation",
-    "mcx_normalize", "mcx_error", "mcx_last_error", "mcx_detreclen", "mcx_version", "mcx_config_sizeof",
+    "mcx_normalize", "mcx_error", "mcx_last_error", "mcx_detreclen", "mcx_version", "mcx_rand_words", "mcx_config_sizeof",
     "mcx_config_offsetof", "mcx_release_sessions", "mcx_prepare_simulation",
     "mcxg_device_count", "mcxg_device_info", "mcxg_error_string", "mcxg_create", "mcxg_destroy",
     "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_launch", "mcxg_simulate",
@@ -140,6 +140,7 @@ def load():
     L.mcx_detreclen.argtypes = [P(Config)]
     L.mcx_detreclen.restype = ctypes.c_uint
     L.mcx_version.restype = ctypes.c_char_p
+    L.mcx_rand_words.argtypes = [ctypes.c_uint, vp, ctypes.c_size_t]
     L.mcx_prepare_simulation.argtypes = [P(Config)]
     L.mcx_prepare_simulation.restype = vp
     L.mcx_config_sizeof.restype = ctypes.c_size_t

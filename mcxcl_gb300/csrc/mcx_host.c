@@ -790,6 +790,55 @@ static void device_check(int rc, const char* what) {
 }
 
 /* the kernel constant block of one simulation (mcx_host.cpp:507-524, 674-693) */
+/* The words rand() returns after srand(seed) in the C library the reference
+   runs on (glibc's default generator): an additive lagged-Fibonacci
+   generator x[n] = x[n-3] + x[n-31] (mod 2^32) whose 31 words of state come
+   from the Park-Miller minimal standard generator (16807 x mod 2^31 - 1, in
+   Schrage's factorisation), the first 310 outputs discarded and each output
+   x >> 1.  Restated here because the library's rand() takes a lock on every
+   call and the reference draws four words per reference thread. */
+typedef struct AddRand {
+    uint32_t x[31];
+    int f, b;                      /* the x[n-3] and x[n-31] taps into the ring */
+} AddRand;
+
+static inline uint32_t addrand_next(AddRand* g) {
+    const uint32_t v = (g->x[g->f] += g->x[g->b]);
+    g->f = (g->f == 30) ? 0 : g->f + 1;
+    g->b = (g->b == 30) ? 0 : g->b + 1;
+    return v >> 1;
+}
+
+static void addrand_seed(AddRand* g, unsigned int seed) {
+    int32_t w = (int32_t)(seed ? seed : 1u);
+    g->x[0] = (uint32_t)w;
+    for (int i = 1; i < 31; i++) {
+        const int64_t hi = w / 127773, lo = w % 127773;
+        w = (int32_t)(16807 * lo - 2836 * hi);
+        if (w < 0) {
+            w += 2147483647;
+        }
+        g->x[i] = (uint32_t)w;
+    }
+    g->f = 3;
+    g->b = 0;
+    for (int i = 0; i < 310; i++) {
+        (void)addrand_next(g);
+    }
+}
+
+static void addrand_fill(AddRand* g, uint32_t* out, size_t n) {
+    for (size_t i = 0; i < n; i++) {
+        out[i] = addrand_next(g);
+    }
+}
+
+void mcx_rand_words(unsigned int seed, uint32_t* out, size_t n) {
+    AddRand g;
+    addrand_seed(&g, seed);
+    addrand_fill(&g, out, n);
+}
+
 static void make_kparams(const Config* cfg, size_t nvox, size_t fieldlen, size_t autothread, unsigned int hostdetreclen,
                          unsigned int partialdata, unsigned int is2d, int replay, mcxg_kparams* kp) {
     memset(kp, 0, sizeof(*kp));
@@ -963,9 +1012,19 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
 
     size_t autothread, autoblock;
     if (cfg->autopilot) {
-        /* the reference's NVIDIA compute >= 6 choice (mcx_host.cpp:617-620) */
+        /* the reference's NVIDIA compute >= 6 choice (mcx_host.cpp:617-620),
+           which the exact kernel keeps.  The fast kernel's persistent grid
+           ends when its slowest reference thread does, so it takes up to 8
+           times as many threads as long as each keeps ~16 photons: shorter
+           threads shorten the end of the launch (+10 % on the cube + sphere
+           workload at 1e8 photons) */
         autoblock = 64;
         autothread = autoblock * 64 * (size_t)g.sm;
+        if (!cfg->exactmath && !(cfg->debuglevel & 1)) {
+            const size_t per = (size_t)(cfg->nphoton / (cfg->respin > 0 ? cfg->respin : 1)) / 16;
+            const size_t cap = 8 * autothread;
+            autothread = per > cap ? cap : (per > autothread ? per : autothread);
+        }
     } else {
         autothread = cfg->nthread;
         autoblock = cfg->nblocksize ? cfg->nblocksize : 64;
@@ -1048,11 +1107,8 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     /* seeds: srand(seed) then 4 rand() words per reference thread
        (mcx_host.cpp:696-700, 759-768); a replay launches every photon from its
        saved state, so its per-thread words are never drawn from */
-    if (cfg->seed > 0) {
-        srand((unsigned int)cfg->seed);
-    } else {
-        srand(replay ? 1u : (unsigned int)time(0));
-    }
+    AddRand ar;
+    addrand_seed(&ar, cfg->seed > 0 ? (unsigned int)cfg->seed : (replay ? 1u : (unsigned int)time(0)));
     seeds = (uint32_t*)malloc(sizeof(uint32_t) * 4 * autothread);
     if (!seeds) {
         MCX_ERROR(-2, "out of host memory");
@@ -1074,9 +1130,7 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
 
     float kms_total = 0.f;
     for (int iter = 0; iter < cfg->respin; iter++) {
-        for (size_t j = 0; j < autothread * 4; j++) {
-            seeds[j] = (uint32_t)rand();
-        }
+        addrand_fill(&ar, seeds, autothread * 4);
         device_check(mcxg_set_seeds(s, seeds, (uint32_t)autothread), "uploading seeds");
         /* photon split in the reference's float arithmetic (mcx_host.cpp:1101-1102) */
         float tp = (float)cfg->nphoton * workload0 / (fullload * (float)autothread * (float)cfg->respin);

@@ -192,3 +192,21 @@ def test_volume_encodings():
     assert mb == 104 and w[0] == (9 << 16 | 7)
     with pytest.raises(ValueError):
         media.encode(np.zeros((8, 2, 2, 2), np.uint8))
+
+
+def test_seed_words_match_the_c_library(lib):
+    """The per-thread seed words (mcx_host.cpp:696-700, 759-768: srand(seed)
+    then rand() four times per reference thread) come from the library's own
+    copy of glibc's generator: the same words as the C library's rand() for
+    ordinary, zero and above-2^31 seeds."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.srand.argtypes = [ctypes.c_uint]
+    libc.rand.restype = ctypes.c_int
+    n = 5000
+    for seed in (1648335518, 0, 1, 29012392, 2**31, 2**32 - 1, 12345):
+        libc.srand(seed)
+        want = np.array([libc.rand() for _ in range(n)], np.uint32)
+        got = np.zeros(n, np.uint32)
+        lib.mcx_rand_words(seed, got.ctypes.data, n)
+        assert np.array_equal(got, want), seed
