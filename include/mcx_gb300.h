@@ -358,6 +358,9 @@ int  mcxg_get_field(mcxg_session* s, float* out, double scale);
 /* Field split into nblocks equal blocks, block b scaled by scales[b]
    (a replay with one output per detector). */
 int  mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uint32_t nblocks);
+/* As mcxg_get_field with element i scaled by scales[i % nsrc]: the per-pattern
+   normalisation of photon sharing, whose field interleaves the patterns. */
+int  mcxg_get_field_interleaved(mcxg_session* s, float* out, const double* scales, uint32_t nsrc);
 /* Adjoint Jacobians from the normalised float field of the last
    mcxg_get_field: fieldlen = nx ny nz maxgate (ns + nd), the first ns gate
    blocks the sources, the next nd the detectors run as sources.  kind 0:

@@ -110,7 +110,7 @@ EXPORTS = [
     "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_launch", "mcxg_simulate",
     "mcxg_get_energy", "mcxg_get_thread_energy", "mcxg_get_field", "mcxg_get_field_f64", "mcxg_get_detected",
     "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc", "mcxg_autotune",
-    "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",
+    "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_field_interleaved", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",
     "mcxg_batch_simulate", "mcxg_batch_get_energy", "mcxg_batch_get_field", "mcx_savedetphoton",
     "mcxg_adjoint",
 ]

@@ -201,6 +201,15 @@ __global__ void field_merge_f32(const float* __restrict__ f, size_t n, double sc
     }
 }
 
+/* element i belongs to source i % nsrc (photon sharing interleaves the
+   patterns innermost) */
+__global__ void field_merge_interleaved(const float* __restrict__ f, size_t n, unsigned int nsrc,
+                                        const double* __restrict__ scales, float* __restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        out[i] = (float)(((double)f[i] + (double)f[i + n]) * scales[i % nsrc]);
+    }
+}
+
 __global__ void field_merge_blocks(const float* __restrict__ f, size_t n, size_t blocklen,
                                    const double* __restrict__ scales, float* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -383,7 +392,9 @@ int grid_for(const mcxg_session* s, size_t n) {
    launch-time state per thread, the phase tables, and the detector partial
    data per thread */
 size_t shared_bytes(const mcxg_kparams& kp, int block) {
-    size_t det = (kp.savedet ? kp.partialdata : 0);
+    /* per-thread slots: detector partial data, then one weight per shared
+       pattern (their slots start after the partial data) */
+    size_t det = (kp.srcnum > 1) ? (size_t)kp.partialdata + kp.srcnum : (kp.savedet ? kp.partialdata : 0);
     return (size_t)kp.medianum * 32 + (size_t)block * 32 + (size_t)(kp.nphase + kp.nangle) * 4 + det * (size_t)block * 4;
 }
 
@@ -734,7 +745,7 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     const bool noagg = (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
     const bool xmedia = kp.mediaformat > 4 && kp.mediaformat != 101;
     /* the instantiations that fix the common configuration's parameters */
-    const bool common = !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2;
+    const bool common = !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2 && kp.srcnum <= 1;
     const int bpsm_sel = xmedia ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
                  (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
@@ -914,6 +925,27 @@ int mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uin
     }
     MCXG_TRY(cudaMemcpyAsync(s->d_scales, scales, sizeof(double) * nblocks, cudaMemcpyHostToDevice, s->st));
     field_merge_blocks<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, n / nblocks, s->d_scales, (float*)s->d_out);
+    s->out_valid = true;
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_get_field_interleaved(mcxg_session* s, float* out, const double* scales, uint32_t nsrc) {
+    if (!s || !out || !scales || nsrc == 0 || !s->has_problem || s->kp.fieldlen % nsrc) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    size_t n = s->kp.fieldlen;
+    int rc = ensure((double**)&s->d_out, &s->out_cap, n);
+    if (!rc) {
+        rc = ensure(&s->d_scales, &s->scales_cap, nsrc);
+    }
+    if (rc) {
+        return rc;
+    }
+    MCXG_TRY(cudaMemcpyAsync(s->d_scales, scales, sizeof(double) * nsrc, cudaMemcpyHostToDevice, s->st));
+    field_merge_interleaved<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, nsrc, s->d_scales, (float*)s->d_out);
     s->out_valid = true;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));

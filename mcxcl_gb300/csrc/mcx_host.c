@@ -392,8 +392,13 @@ static void preprocess(Config* cfg) {
             }
         }
     }
-    if (cfg->srcnum > 1) {
-        MCX_ERROR(-4, "photon sharing (srcnum > 1) is not supported by this build");
+    if (cfg->srcnum > 1 && (cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D)) {
+        if (cfg->seed == SEED_FROM_FILE) {
+            MCX_ERROR(-4, "photon sharing (srcnum > 1) can not be replayed by this build");
+        }
+        if (cfg->srcnum > 256) {
+            MCX_ERROR(-4, "photon sharing takes at most 256 patterns");
+        }
     }
     size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
     if (cfg->mediabyte <= 4) {
@@ -896,6 +901,8 @@ static void make_kparams(const Config* cfg, size_t nvox, size_t fieldlen, size_t
     kp->nangle = cfg->nangle;
     kp->extrasrclen = cfg->extrasrclen;
     kp->srcid = cfg->srcid;
+    kp->srcnum = (cfg->srcnum > 1 && (cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D))
+                 ? cfg->srcnum : 1u;
     kp->nthread = (uint32_t)autothread;
     if (replay) {
         kp->replay = 1;
@@ -1044,6 +1051,11 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     cfg->maxgate = (unsigned int)(int)((cfg->tend - cfg->tstart) / cfg->tstep + 0.5);
     size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
     size_t mult = (cfg->extrasrclen && cfg->srcid < 0) ? (cfg->extrasrclen + 1) : 1;
+    /* photon sharing: one field per pattern, interleaved innermost
+       (mcx_host.cpp:474, 679) */
+    const unsigned int nshare = (cfg->srcnum > 1 && (cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D))
+                                ? cfg->srcnum : 1u;
+    mult *= nshare;
     const int replay = (cfg->seed == SEED_FROM_FILE);
     if (replay && cfg->replaydet == -1) {
         mult *= cfg->detnum;    /* one block of gates per detector (mcx_host.cpp:684-687) */
@@ -1293,6 +1305,33 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
                     }
                 }
             }
+            if (nshare > 1) {
+                /* each pattern by its total weight (mcx_host.cpp:1436-1447): the
+                   pattern sums in the reference's float Kahan summation */
+                int psize = (cfg->srctype == MCX_SRC_PATTERN3D)
+                            ? (int)cfg->srcparam1.x * (int)cfg->srcparam1.y * (int)cfg->srcparam1.z
+                            : (int)cfg->srcparam1.w * (int)cfg->srcparam2.w;
+                nblocks = nshare;
+                blockscale = (double*)calloc(nblocks, sizeof(double));
+                if (!blockscale) {
+                    MCX_ERROR(-2, "out of host memory");
+                }
+                const float scaleref = sc;
+                for (uint32_t i = 0; i < nshare; i++) {
+                    float sum = 0.f, comp = 0.f;
+                    for (int j = 0; j < psize; j++) {
+                        const float y = cfg->srcpattern[(size_t)j * nshare + i] - comp;
+                        const float t = sum + y;
+                        comp = (t - sum) - y;
+                        sum = t;
+                    }
+                    const float si = (float)psize / sum * scaleref;
+                    blockscale[i] = (double)si;
+                    if (i == 0) {
+                        sc = si;
+                    }
+                }
+            }
             if (cfg->extrasrclen && cfg->srcid < 0) {
                 sc *= (float)(cfg->extrasrclen + 1);
                 if (blockscale) {
@@ -1325,7 +1364,9 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
             }
             dst = fieldtmp;
         }
-        if (blockscale) {
+        if (blockscale && nshare > 1) {
+            device_check(mcxg_get_field_interleaved(s, dst, blockscale, nblocks), "reading the field");
+        } else if (blockscale) {
             device_check(mcxg_get_field_blocks(s, dst, blockscale, nblocks), "reading the field");
         } else {
             device_check(mcxg_get_field(s, dst, scale), "reading the field");

@@ -215,6 +215,7 @@ struct BatchPS {
 #define KP_IS2D (PS::kCommon ? 0u : c_p.is2d)
 #define KP_NPHASE_GT2 (!PS::kCommon && c_p.nphase > 2)
 #define KP_MEDIAFORMAT (PS::kCommon ? 1u : c_p.mediaformat)
+#define KP_SHARING (!PS::kCommon && c_p.srcnum > 1)
 
 /* ------------------------------------------------------------------ math */
 
@@ -703,6 +704,26 @@ __device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, boo
     }
 }
 
+/* Photon sharing (mcx_core.cl:1527-1538, 2902-2911): a deposit goes to every
+   pattern with a non-zero weight, element (voxel + gate * nvox) * srcnum +
+   pattern, scaled by that weight.  An element one gate past the last folds
+   into the low plane at gate 0, as the single-pattern deposit does. */
+template <class PS>
+__device__ __forceinline__ void share_deposit(const KArgs& a, const PS& ps, unsigned int key, float w) {
+    const mcxg_kparams& c_p = ps.p();
+    const unsigned int n = c_p.srcnum;
+    for (unsigned int i = 0; i < n; i++) {
+        const float pw = ps.pp(c_p.partialdata + i);
+        if (fabsf(pw) > 0.f) {
+            unsigned int k = key * n + i;
+            if (k >= c_p.fieldlen) {
+                k -= c_p.fieldlen;
+            }
+            field_add2(a.field, ps.lo_plane(), k, w * pw);
+        }
+    }
+}
+
 /* ------------------------------------------------------------------ replay */
 
 /* index of the photon a replay quantity belongs to: the reference's
@@ -793,7 +814,12 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
             if (c_p.extrasrclen && (c_p.srcid < 0)) {
                 tshift += ((int)ps.cold()->srcsel - 1) * (int)c_p.maxgate;
             }
-            field_add2(a.field, ps.lo_plane(), ps.field_off() + s.idx1d + (unsigned int)tshift * c_p.nvox, -s.p.w);
+            const unsigned int key = ps.field_off() + s.idx1d + (unsigned int)tshift * c_p.nvox;
+            if (KP_SHARING) {
+                share_deposit(a, ps, key, -s.p.w);
+            } else {
+                field_add2(a.field, ps.lo_plane(), key, -s.p.w);
+            }
         }
         if (DET && c_p.savedet && (isdet & K_DET_MASK) == K_DET_MASK && s.mediaid == 0 && c_p.issaveref < 2) {
             savedetphoton(a, ps, S, s, isdet);
@@ -880,15 +906,29 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
                 s.p.y = s.p.y + rx * lp1.y + ry * lp2.y;
                 s.p.z = s.p.z + rx * lp1.z + ry * lp2.z;
             }
-            if (st == S_PATTERN) {
-                unsigned int pi = (unsigned int)((int)(ry * K_JUST_BELOW_ONE * lp2.w) * (int)(lp1.w) +
-                                                 (int)(rx * K_JUST_BELOW_ONE * lp1.w));
-                s.p.w = lpos.w * a.srcpattern[min(pi, c_p.npattern - 1)];
-            } else if (st == S_PATTERN3D) {
-                unsigned int pi = (unsigned int)((int)(rz * K_JUST_BELOW_ONE * lp1.z) * (int)(lp1.y) * (int)(lp1.x) +
-                                                 (int)(ry * K_JUST_BELOW_ONE * lp1.y) * (int)(lp1.x) +
-                                                 (int)(rx * K_JUST_BELOW_ONE * lp1.x));
-                s.p.w = lpos.w * a.srcpattern[min(pi, c_p.npattern - 1)];
+            if (st == S_PATTERN || st == S_PATTERN3D) {
+                unsigned int pi;
+                if (st == S_PATTERN) {
+                    pi = (unsigned int)((int)(ry * K_JUST_BELOW_ONE * lp2.w) * (int)(lp1.w) +
+                                        (int)(rx * K_JUST_BELOW_ONE * lp1.w));
+                } else {
+                    pi = (unsigned int)((int)(rz * K_JUST_BELOW_ONE * lp1.z) * (int)(lp1.y) * (int)(lp1.x) +
+                                        (int)(ry * K_JUST_BELOW_ONE * lp1.y) * (int)(lp1.x) +
+                                        (int)(rx * K_JUST_BELOW_ONE * lp1.x));
+                }
+                if (KP_SHARING) {
+                    /* photon sharing (mcx_core.cl:1697-1704, 1718-1726): the photon
+                       carries weight 1 and one weight per pattern; the pixel index
+                       takes the initial-weight slot */
+                    const unsigned int n = c_p.srcnum;
+                    for (unsigned int i = 0; i < n; i++) {
+                        ps.pp(c_p.partialdata + i) = a.srcpattern[min(pi * n + i, c_p.npattern - 1)];
+                    }
+                    ps.cold()->w0init = __uint_as_float(pi);
+                    s.p.w = 1.f;
+                } else {
+                    s.p.w = lpos.w * a.srcpattern[min(pi, c_p.npattern - 1)];
+                }
             } else if (st == S_FOURIER) {
                 s.p.w = lpos.w * (M::cos((floorf(lp1.w) * rx + floorf(lp2.w) * ry + lp1.w - floorf(lp1.w)) * K_TWO_PI) *
                                   (1.f - lp2.w + floorf(lp2.w)) + 1.f) * 0.5f;
@@ -1173,7 +1213,9 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     updateprop(ps, S, s.prop, s.mediaid);
     ps.cold()->launched += s.p.w;
     s.w0 = s.p.w;
-    ps.cold()->w0init = s.p.w;
+    if (!KP_SHARING) {
+        ps.cold()->w0init = s.p.w;
+    }
     s.v.w = K_EPS;
     s.Lmove = 0.f;
     return 0;
@@ -1555,7 +1597,13 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             } else {
                 s.mediaid = mediaidold;
             }
-            deposit<WAGG>(a.field, ps.lo_plane(), dep, ps.field_off() + key, weight, pd);
+            if (KP_SHARING) {
+                if (dep) {
+                    share_deposit(a, ps, key, weight);
+                }
+            } else {
+                deposit<WAGG>(a.field, ps.lo_plane(), dep, ps.field_off() + key, weight, pd);
+            }
         }
 
         /* ---- exit, time-out or cyclic boundary (mcx_core.cl:2958-3028) */
@@ -1702,5 +1750,6 @@ __global__ void mcx_rng_dump(const KArgs a) {
 #undef KP_IS2D
 #undef KP_NPHASE_GT2
 #undef KP_MEDIAFORMAT
+#undef KP_SHARING
 
 #endif

@@ -67,6 +67,8 @@ typedef struct mcxg_kparams {
     int32_t  replaydet;            /* 0 all detectors, -1 one gate block per detector, k detector k */
     uint32_t siteshift;            /* scattering-site replay deposits read photon k+siteshift (the reference: 1) */
     uint32_t dimy, dimz;           /* voxel counts along y and z */
+    uint32_t srcnum;               /* patterns sharing each photon (pattern sources), else 1 */
+    uint32_t reserved;
 } mcxg_kparams;
 
 /* One simulation of a batch: its parameter block (nthread = its reference

@@ -370,9 +370,13 @@ def _outputs(cfg, C):
         gates = int((C.tend - C.tstart) / C.tstep + 0.5)
         nsrc = C.extrasrclen + 1 if (C.extrasrclen and C.srcid < 0) else 1
         ndetblk = C.detnum if (C.seed == SEED_FROM_FILE and C.replaydet == -1) else 1
-        n = C.dim.x * C.dim.y * C.dim.z * gates * nsrc * ndetblk
+        # photon sharing: one field per pattern, patterns innermost (src/pmcxcl.cpp:1330)
+        nshare = C.srcnum if (C.srcnum > 1 and ord(C.srctype) in (5, 15)) else 1
+        n = C.dim.x * C.dim.y * C.dim.z * gates * nsrc * ndetblk * nshare
         f = np.ctypeslib.as_array(C.exportfield, shape=(n,)).copy()
-        if nsrc > 1:
+        if nshare > 1:
+            dims = (nshare * C.dim.x, C.dim.y, C.dim.z, gates)
+        elif nsrc > 1:
             dims = (C.dim.x, C.dim.y, C.dim.z, gates, ndetblk, nsrc)
         elif ndetblk > 1:
             dims = (C.dim.x, C.dim.y, C.dim.z, gates, ndetblk)
@@ -381,11 +385,11 @@ def _outputs(cfg, C):
         flux = f.reshape(dims, order="F")
         if C.issaveref:
             vol = np.ctypeslib.as_array(C.vol, shape=(C.dim.x * C.dim.y * C.dim.z,))
-            mask = (vol & 0x7FFFFFFF).reshape((C.dim.x, C.dim.y, C.dim.z), order="F") != 0
-            dref = np.where(mask[..., None], 0.0, -flux.reshape(C.dim.x, C.dim.y, C.dim.z, -1)).astype(np.float32)
-            flux = np.where(mask[..., None], flux.reshape(C.dim.x, C.dim.y, C.dim.z, -1), 0.0).astype(np.float32)
-            out["dref"] = dref.reshape(dims, order="F") if dref.shape != dims else dref
-            flux = flux.reshape(dims)
+            mask = (vol & 0x7FFFFFFF).reshape((1, C.dim.x, C.dim.y, C.dim.z), order="F") != 0
+            fl = flux.reshape((nshare, C.dim.x, C.dim.y, C.dim.z, -1), order="F")
+            dref = np.where(mask[..., None], 0.0, -fl).astype(np.float32).reshape(dims, order="F")
+            flux = np.where(mask[..., None], fl, 0.0).astype(np.float32).reshape(dims, order="F")
+            out["dref"] = dref
         out["flux"] = flux
         out["stat"] = {
             "runtime": C.runtime,

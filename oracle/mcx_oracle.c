@@ -179,6 +179,24 @@ static inline void field_add(octx* X, size_t i, float w) {
     }
 }
 
+/* a deposit with photon sharing (mcx_core.cl:1527-1538, 2902-2911, the
+   kernel built for pattern sources): each pattern with a non-zero share adds
+   weight x share at element i * srcnum + k; one pattern adds weight at i */
+static inline void share_add(octx* X, const ostate* s, size_t i, float w) {
+    const ocfg* c = X->c;
+    unsigned int k;
+    if (c->srcnum <= 1) {
+        field_add(X, i, w);
+        return;
+    }
+    for (k = 0; k < c->srcnum; k++) {
+        float pw = s->ppath[c->w0offset + k];
+        if (fabsf(pw) > 0.f) {
+            field_add(X, i * c->srcnum + k, w * pw);
+        }
+    }
+}
+
 /* the scattering-site deposit of the replay outputs moves a saturated value
    whole into the shadow half (mcx_core.cl:2597-2604) */
 static inline void field_add_site(octx* X, size_t i, float w) {
@@ -551,7 +569,7 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
                 if (c->extrasrclen && (c->srcid < 0)) {
                     tshift += ((int)s->ppath[c->w0offset - 1] - 1) * (int)c->maxgate;
                 }
-                field_add(X, (size_t)s->idx1d + (size_t)tshift * c->dimlen[2], -s->p.w);
+                share_add(X, s, (size_t)s->idx1d + (size_t)tshift * c->dimlen[2], -s->p.w);
             }
         }
         if ((isdet & DET_MASK) == DET_MASK && s->mediaid == 0 && c->issaveref < 2) {
@@ -638,15 +656,28 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
                     s->p.y = s->p.y + rx * ls->p1.y + ry * ls->p2.y;
                     s->p.z = s->p.z + rx * ls->p1.z + ry * ls->p2.z;
                 }
-                if (c->srctype == S_PATTERN) {
-                    s->p.w = ls->pos.w * c->srcpattern[(int)(ry * K_JUST_BELOW_ONE * ls->p2.w) * (int)(ls->p1.w) +
-                                                        (int)(rx * K_JUST_BELOW_ONE * ls->p1.w)];
-                    pp[4] = s->p.w;
-                } else if (c->srctype == S_PATTERN3D) {
-                    s->p.w = ls->pos.w * c->srcpattern[(int)(rz * K_JUST_BELOW_ONE * ls->p1.z) * (int)(ls->p1.y) * (int)(ls->p1.x) +
-                                                        (int)(ry * K_JUST_BELOW_ONE * ls->p1.y) * (int)(ls->p1.x) +
-                                                        (int)(rx * K_JUST_BELOW_ONE * ls->p1.x)];
-                    pp[4] = s->p.w;
+                if (c->srctype == S_PATTERN || c->srctype == S_PATTERN3D) {
+                    int pix;
+                    if (c->srctype == S_PATTERN) {
+                        pix = (int)(ry * K_JUST_BELOW_ONE * ls->p2.w) * (int)(ls->p1.w) + (int)(rx * K_JUST_BELOW_ONE * ls->p1.w);
+                    } else {
+                        pix = (int)(rz * K_JUST_BELOW_ONE * ls->p1.z) * (int)(ls->p1.y) * (int)(ls->p1.x) +
+                              (int)(ry * K_JUST_BELOW_ONE * ls->p1.y) * (int)(ls->p1.x) + (int)(rx * K_JUST_BELOW_ONE * ls->p1.x);
+                    }
+                    if (c->srcnum <= 1) {
+                        s->p.w = ls->pos.w * c->srcpattern[pix];
+                        pp[4] = s->p.w;
+                    } else {
+                        /* photon sharing, 1697-1704 / 1718-1726: weight 1, one weight per
+                           pattern, the pixel index in the initial-weight slot */
+                        unsigned int k;
+                        uint32_t upix = (uint32_t)pix;
+                        memcpy(&pp[2], &upix, sizeof(upix));
+                        for (k = 0; k < c->srcnum; k++) {
+                            pp[4 + k] = c->srcpattern[(size_t)pix * c->srcnum + k];
+                        }
+                        s->p.w = 1.f;
+                    }
                 } else if (c->srctype == S_FOURIER) {
                     s->p.w = ls->pos.w * (m_cos(c, (floorf(ls->p1.w) * rx + floorf(ls->p2.w) * ry + ls->p1.w - floorf(ls->p1.w)) * K_TWO_PI) *
                                           (1.f - ls->p2.w + floorf(ls->p2.w)) + 1.f) * 0.5f;
@@ -1163,7 +1194,7 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                               (int)c->maxgate;
                 }
                 if (fabsf(weight) > 0.f) {
-                    field_add(X, (size_t)idx1dold + (size_t)(long long)tshift * c->dimlen[2], weight);
+                    share_add(X, &s, (size_t)idx1dold + (size_t)(long long)tshift * c->dimlen[2], weight);
                 }
             }
             s.w0 = s.p.w;
@@ -1420,6 +1451,9 @@ unsigned int mcxo_reclen(const mcxo_input* in) {
 
 unsigned int mcxo_fieldlen(const mcxo_input* in) {
     unsigned int mult = (in->extrasrclen && in->srcid < 0) ? (in->extrasrclen + 1) : 1;
+    if (in->srcnum > 1 && (in->srctype == S_PATTERN || in->srctype == S_PATTERN3D)) {
+        mult *= in->srcnum;    /* one field per shared pattern, patterns innermost (mcx_host.cpp:474, 679) */
+    }
     if (is_replay(in) && in->replaydet == -1) {
         mult *= in->detnum;    /* one block of gates per detector, mcx_host.cpp:684-687 */
     }
@@ -1487,7 +1521,7 @@ static int prepare(const mcxo_input* in, oprep* P) {
     if (in->mediabyte != 1 && in->mediabyte != 2 && in->mediabyte != 4 && !(in->mediabyte >= 99 && in->mediabyte <= 104)) {
         return -2;
     }
-    if (in->srcnum > 1 || in->issaveref > 1) {
+    if (in->issaveref > 1 || (in->srcnum > 1 && is_replay(in))) {
         return -3;
     }
     nvox = in->dimx * in->dimy * in->dimz;
@@ -1619,7 +1653,7 @@ static int prepare(const mcxo_input* in, oprep* P) {
     c.w0offset = partialdata + 4;
     c.mediaformat = (unsigned int)in->mediabyte;
     c.gscatter = in->gscatter;
-    c.srcnum = in->srcnum ? in->srcnum : 1;
+    c.srcnum = (in->srcnum > 1 && (in->srctype == S_PATTERN || in->srctype == S_PATTERN3D)) ? in->srcnum : 1;
     c.nphase = in->nphase;
     c.nangle = in->nangle;
     c.invcdf = in->invcdf;
@@ -1915,6 +1949,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
         double etot = 0.0, eesc = 0.0;
         float scale = 1.f;
         float* blockscale = NULL;
+        float* sharescale = NULL;
         float Vvox = steps * steps * steps;
         for (i = 0; i < in->nthread; i++) {
             eesc += energy[i * 2];
@@ -1953,6 +1988,28 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
                     }
                 }
             }
+            if (c.srcnum > 1) {
+                /* per-pattern scale, 1436-1447: the pattern's pixel count over its
+                   float Kahan-summed weight */
+                unsigned int k;
+                int psize = (in->srctype == S_PATTERN3D)
+                            ? (int)in->srcparam1[0] * (int)in->srcparam1[1] * (int)in->srcparam1[2]
+                            : (int)in->srcparam1[3] * (int)in->srcparam2[3];
+                float scaleref = scale;
+                sharescale = (float*)calloc(c.srcnum, sizeof(float));
+                for (k = 0; k < c.srcnum; k++) {
+                    float sum = 0.f, comp = 0.f;
+                    int j;
+                    for (j = 0; j < psize; j++) {
+                        float y = in->srcpattern[(size_t)j * c.srcnum + k] - comp;
+                        float t = sum + y;
+                        comp = t - sum - y;
+                        sum = t;
+                    }
+                    sharescale[k] = psize / sum * scaleref;
+                }
+                scale = sharescale[0];
+            }
             if (in->extrasrclen && in->srcid < 0) {
                 scale *= (float)(in->extrasrclen + 1);
             }
@@ -1972,11 +2029,12 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
                 field_out[i] = raw;
             }
             if (fieldnorm) {
-                float sc = blockscale ? blockscale[i / (fieldlen / c.detnum)] : scale;
+                float sc = blockscale ? blockscale[i / (fieldlen / c.detnum)] : (sharescale ? sharescale[i % c.srcnum] : scale);
                 fieldnorm[i] = in->isnormalized ? merged * sc : merged;
             }
         }
         free(blockscale);
+        free(sharescale);
     }
     stats.detected = total_det;
     stats.saved = saved;

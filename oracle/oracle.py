@@ -75,7 +75,7 @@ class MCXOStats(ctypes.Structure):
 
 
 _lib = None
-_ref = None
+_ref = {}
 
 
 def build(ref=None):
@@ -109,12 +109,14 @@ def ref_available():
     return os.path.exists(REF_PATH)
 
 
-def reflib():
-    global _ref
-    if _ref is None:
-        _ref = ctypes.CDLL(REF_PATH)
-        _ref.mcxref_run.restype = ctypes.c_int
-    return _ref
+def reflib(pattern=False):
+    """The reference harness; pattern=True: the build for pattern sources
+    (photon-sharing deposits), as the reference compiles its kernel for them."""
+    path = REF_PATH.replace("libmcxref.so", "libmcxref_pat.so") if pattern else REF_PATH
+    if path not in _ref:
+        _ref[path] = ctypes.CDLL(path)
+        _ref[path].mcxref_run.restype = ctypes.c_int
+    return _ref[path]
 
 
 def _ptr(a):
@@ -340,7 +342,7 @@ def run_reference(cfg, nthread=4096, core=None, nblocksize=64, nworkers=1):
     Returns the merged raw float field, per-thread energies, records, seeds."""
     inp, keep = make_input(cfg, nthread, core, MATH_LIBM, VARIANT_NVCC, FIELD_FLOAT_SPILL, 1)
     L = lib()
-    R = reflib()
+    R = reflib(pattern=inp.srctype in (5, 15))
     fieldlen = L.mcxo_fieldlen(ctypes.byref(inp))
     reclen = L.mcxo_reclen(ctypes.byref(inp))
     field = np.zeros(fieldlen, np.float32)

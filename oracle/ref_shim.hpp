@@ -68,13 +68,24 @@ static inline unsigned int atomicSub(unsigned int* addr, unsigned int val) {
    flag for the pattern-source deposit path (mcx_core.cl:1513, 2881).  With
    the ids as macros (as mcx_const.h has them) the __NVCC__ branch would always
    take that path and deposit nothing for other sources; as enum constants the
-   host build follows the OpenCL build for every non-pattern source. */
+   host build follows the OpenCL build for every non-pattern source.  The
+   build for pattern sources (MCXREF_PATTERN_BUILD) makes the two pattern ids
+   macros, as the OpenCL JIT flags them for a pattern source, so the kernel
+   takes its photon-sharing deposit path. */
 enum {
     MCX_SRC_PENCIL = 0, MCX_SRC_ISOTROPIC = 1, MCX_SRC_CONE = 2, MCX_SRC_GAUSSIAN = 3, MCX_SRC_PLANAR = 4,
-    MCX_SRC_PATTERN = 5, MCX_SRC_FOURIER = 6, MCX_SRC_ARCSINE = 7, MCX_SRC_DISK = 8, MCX_SRC_FOURIERX = 9,
+#ifndef MCXREF_PATTERN_BUILD
+    MCX_SRC_PATTERN = 5,
+    MCX_SRC_PATTERN3D = 15,
+#endif
+    MCX_SRC_FOURIER = 6, MCX_SRC_ARCSINE = 7, MCX_SRC_DISK = 8, MCX_SRC_FOURIERX = 9,
     MCX_SRC_FOURIERX2D = 10, MCX_SRC_ZGAUSSIAN = 11, MCX_SRC_LINE = 12, MCX_SRC_SLIT = 13,
-    MCX_SRC_PENCILARRAY = 14, MCX_SRC_PATTERN3D = 15, MCX_SRC_HYPERBOLOID_GAUSSIAN = 16, MCX_SRC_RING = 17
+    MCX_SRC_PENCILARRAY = 14, MCX_SRC_HYPERBOLOID_GAUSSIAN = 16, MCX_SRC_RING = 17
 };
+#ifdef MCXREF_PATTERN_BUILD
+#define MCX_SRC_PATTERN 5
+#define MCX_SRC_PATTERN3D 15
+#endif
 
 enum TBoundary {bcUnknown, bcReflect, bcAbsorb, bcMirror, bcCyclic};
 enum TOutputType {otFlux, otFluence, otEnergy, otJacobian, otWP, otDCS, otRF, otL, otRFmus, otWLTOF, otWPTOF,

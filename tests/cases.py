@@ -62,6 +62,13 @@ def small_two_media(**kw):
     return cfg
 
 
+def _voidtop():
+    vol = np.ones((40, 40, 40), np.uint8)
+    vol[10:30, 10:30, 10:30] = 2
+    vol[:, :, 39] = 0
+    return vol
+
+
 def _pattern(n, seed):
     return np.random.RandomState(seed).rand(*n).astype(np.float32)
 
@@ -90,6 +97,12 @@ VARIANTS = {
                     srcpattern=_pattern((4, 4), 1)),
     "pattern3d": dict(srctype="pattern3d", srcpos=[5, 5, 5], srcparam1=[4, 4, 4, 0],
                       srcpattern=_pattern((4, 4, 4), 2)),
+    # photon sharing: one photon, srcnum patterns (srcpattern [srcnum, ...], patterns innermost);
+    # a void top layer gives the escaping photons' saved-reflectance deposits
+    "pattern_share": dict(srctype="pattern", srcpos=[5, 5, 0], srcparam1=[30, 0, 0, 4], srcparam2=[0, 30, 0, 4],
+                          srcnum=3, srcpattern=_pattern((3, 4, 4), 4), issaveref=1, vol=_voidtop()),
+    "pattern3d_share": dict(srctype="pattern3d", srcpos=[5, 5, 5], srcparam1=[4, 4, 4, 0], srcnum=2,
+                            srcpattern=_pattern((2, 4, 4, 4), 5)),
     "focus": dict(srcdir=[0, 0, 1, 10]),
     "lambert": dict(srcdir=[0, 0, 1, -np.inf]),
     "noreflect": dict(isreflect=0),
