@@ -88,6 +88,8 @@ typedef struct {
     const float* invcdf;          /* nphase entries */
     const float* angleinvcdf;     /* nangle entries */
     int mathmode, variant, fieldmode;
+    float omega;
+    int rfmode;                   /* 0 real, 1 RF forward (complex weights), 2 RF replay output */
     unsigned int nthread;
     /* replay */
     int replay, replaydet, replaysiteown;
@@ -118,7 +120,8 @@ typedef struct {
     float w0, Lmove, pathlen, n1;
     uint64_t t[2];
     uint64_t photonseed[2];
-    float* ppath;                 /* w0offset + srcnum floats */
+    float* ppath;                 /* w0offset + srcnum (+ 2 for an RF replay) floats */
+    float wre, wim, w0re, w0im;   /* RF forward: complex weight now and at the last voxel change */
 } ostate;
 
 /* ---------------------------------------------------------------- helpers */
@@ -165,7 +168,8 @@ static inline float nextafter_ref(float a, int dir) {
     return bits2f(i) - 1000.f;
 }
 
-static inline void field_add(octx* X, size_t i, float w) {
+/* returns 1 when the float accumulator spilled */
+static inline int field_add(octx* X, size_t i, float w) {
     const ocfg* c = X->c;
     if (c->fieldmode == MCXO_FIELD_FLOAT_SPILL) {
         float old = X->ff[i];
@@ -173,7 +177,43 @@ static inline void field_add(octx* X, size_t i, float w) {
         if (fabsf(old) > K_MAX_ACCUM) {
             X->ff[i] += ((old > 0.f) ? -K_MAX_ACCUM : K_MAX_ACCUM);
             X->ff[i + c->dimlen[3]] += ((old > 0.f) ? K_MAX_ACCUM : -K_MAX_ACCUM);
+            return 1;
         }
+    } else {
+        X->fd[i >= c->dimlen[3] ? i - c->dimlen[3] : i] += (double)w;
+    }
+    return 0;
+}
+
+/* RF deposits of the imaginary part (mcx_core.cl:2887-2898, 2609-2617): the
+   forward run and the rfmus scattering sites write the third quarter of the
+   field with its own +-1000 spill into the fourth; the rf replay output
+   writes the second half without a spill.  In FP64 the imaginary part is the
+   second fieldlen block. */
+static inline void field_add_im(octx* X, size_t i, float w, int quarter) {
+    const ocfg* c = X->c;
+    const size_t F = c->dimlen[3];
+    if (c->fieldmode == MCXO_FIELD_FLOAT_SPILL) {
+        if (quarter) {
+            float old = X->ff[i + 2 * F];
+            X->ff[i + 2 * F] = old + w;
+            if (fabsf(old) > K_MAX_ACCUM) {
+                X->ff[i + 2 * F] += ((old > 0.f) ? -K_MAX_ACCUM : K_MAX_ACCUM);
+                X->ff[i + 3 * F] += ((old > 0.f) ? K_MAX_ACCUM : -K_MAX_ACCUM);
+            }
+        } else {
+            X->ff[i + F] += w;
+        }
+    } else {
+        X->fd[F + (i >= F ? i - F : i)] += (double)w;
+    }
+}
+
+/* the rf replay output's real part has no spill (mcx_core.cl:2884) */
+static inline void field_add_nospill(octx* X, size_t i, float w) {
+    const ocfg* c = X->c;
+    if (c->fieldmode == MCXO_FIELD_FLOAT_SPILL) {
+        X->ff[i] += w;
     } else {
         X->fd[i >= c->dimlen[3] ? i - c->dimlen[3] : i] += (double)w;
     }
@@ -182,12 +222,11 @@ static inline void field_add(octx* X, size_t i, float w) {
 /* a deposit with photon sharing (mcx_core.cl:1527-1538, 2902-2911, the
    kernel built for pattern sources): each pattern with a non-zero share adds
    weight x share at element i * srcnum + k; one pattern adds weight at i */
-static inline void share_add(octx* X, const ostate* s, size_t i, float w) {
+static inline int share_add(octx* X, const ostate* s, size_t i, float w) {
     const ocfg* c = X->c;
     unsigned int k;
     if (c->srcnum <= 1) {
-        field_add(X, i, w);
-        return;
+        return field_add(X, i, w);
     }
     for (k = 0; k < c->srcnum; k++) {
         float pw = s->ppath[c->w0offset + k];
@@ -195,6 +234,7 @@ static inline void share_add(octx* X, const ostate* s, size_t i, float w) {
             field_add(X, i * c->srcnum + k, w * pw);
         }
     }
+    return 0;
 }
 
 /* the scattering-site deposit of the replay outputs moves a saturated value
@@ -999,6 +1039,26 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
     pp[2] = ((c->srcnum > 1) ? pp[2] : s->p.w);
     s->v.w = K_EPS;
     s->Lmove = 0.f;
+    if (c->rfmode == 1) {
+        /* the complex weight restarts with every launch (2427-2430, 3011, 3054, ...) */
+        s->wre = s->w0re = s->p.w;
+        s->wim = s->w0im = 0.f;
+    } else if (c->rfmode == 2) {
+        /* rf replay (2257-2262): the phase of the detected time of flight, read
+           with the launch counter itself (the next photon, as the scattering
+           sites do); the last photon reads the arrays' start-time pad.  The
+           reference stores it through the partial-data-shifted pointer of its
+           launch (1621), partialdata floats past the slots its deposits read,
+           which therefore stay zero: the float (reference-faithful) mode
+           reproduces that, the FP64 mode stores where the deposits read. */
+        long long k = replay_index(c, X->tid, (long long)(int)s->f.w - (c->replaysiteown ? 1 : 0));
+        float tof = (k >= 0 && k < (long long)c->nreplay) ? c->rtof[k] : c->twin0;
+        float rs, rc;
+        float* slot = s->ppath + c->w0offset + c->srcnum + (c->fieldmode == MCXO_FIELD_FLOAT_SPILL ? c->partialdata : 0);
+        m_sincos(c, c->omega * tof, &rs, &rc);
+        slot[0] = rc;
+        slot[1] = rs;
+    }
     X->nlaunch++;
     return 0;
 }
@@ -1021,7 +1081,7 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
     s.mediaid = f2bits(c->src.p2.w);
     s.fid[3] = -1;
     s.ppath = ppbuf;
-    memset(ppbuf, 0, sizeof(float) * (c->w0offset + c->srcnum));
+    memset(ppbuf, 0, sizeof(float) * (c->w0offset + c->srcnum + 2));
     X->tid = tid;
 
     if ((unsigned long long)tid >= (unsigned long long)c->threadphoton * c->nthread + (unsigned int)c->oddphoton) {
@@ -1090,14 +1150,19 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                     rotatevector(c, &s.v, stheta, ctheta, sphi, cphi);
                 }
                 s.v.w += 1.f;
-                if (c->replay && (c->outputtype == otWP || c->outputtype == otDCS || c->outputtype == otWPTOF)) {
+                if (c->replay && (c->outputtype == otWP || c->outputtype == otDCS || c->outputtype == otWPTOF ||
+                                  c->outputtype == otRFmus)) {
                     /* replay deposit at the scattering site, mcx_core.cl:2567-2604; the
                        reference indexes these with the launch counter itself (no -1) */
                     long long k = replay_index(c, tid, (long long)(int)s.f.w - (c->replaysiteown ? 1 : 0));
                     if (k >= 0 && k < (long long)c->nreplay) {
                         int tshift;
+                        float tim = 0.f;
                         tmp0 = (c->outputtype == otDCS) ? (1.f - ctheta) : 1.f;
-                        if (c->outputtype == otWPTOF) {
+                        if (c->outputtype == otRFmus) {
+                            tmp0 = c->rweight[k] * s.ppath[c->w0offset + c->srcnum];
+                            tim = c->rweight[k] * s.ppath[c->w0offset + c->srcnum + 1];
+                        } else if (c->outputtype == otWPTOF) {
                             tmp0 = c->rtof[k];
                             tmp0 *= c->rweight[k];
                         } else {
@@ -1110,6 +1175,9 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                         }
                         tshift = ((int)c->maxgate - 1 < tshift) ? (int)c->maxgate - 1 : tshift;
                         field_add_site(X, (size_t)s.idx1d + (size_t)(long long)tshift * c->dimlen[2], tmp0);
+                        if (c->outputtype == otRFmus) {
+                            field_add_im(X, (size_t)s.idx1d + (size_t)(long long)tshift * c->dimlen[2], tim, 1);
+                        }
                     }
                 }
             }
@@ -1139,7 +1207,19 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
             if (s.fid[3] == 2) {
                 s.fid[2] += (slen == s.f.x) ? 0 : (s.v.z > 0.f ? 1 : -1);
             }
-            s.p.w *= m_exp(c, -s.prop.x * s.f.z);
+            if (c->rfmode == 1) {
+                /* RF forward, 2750-2760: w <- w exp(-(mua + i omega n / c0) ds) */
+                float att = m_exp(c, -s.prop.x * s.f.z);
+                float rs, rc, tre, tim;
+                m_sincos(c, c->omega * s.prop.w * c->oneoverc0 * s.f.z, &rs, &rc);
+                tre = att * (s.wre * rc + s.wim * rs);
+                tim = att * (-s.wre * rs + s.wim * rc);
+                s.wre = tre;
+                s.wim = tim;
+                s.p.w = sqrtf(s.wre * s.wre + s.wim * s.wim);
+            } else {
+                s.p.w *= m_exp(c, -s.prop.x * s.f.z);
+            }
             s.f.x -= slen;
             s.f.y += s.f.z * s.prop.w * c->oneoverc0;
         }
@@ -1165,9 +1245,16 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
         /* deposit on a voxel change, 2816-2929 */
         if (s.idx1d != idx1dold && idx1dold < c->dimlen[2] && mediaidold) {
             if (c->save2pt && s.f.y >= c->twin0 && s.f.y < c->twin1) {
-                float weight = 0.f;
+                float weight = 0.f, weight_im = 0.f;
                 int tshift = (int)(floorf((s.f.y - c->twin0) * c->Rtstep));
-                if (c->outputtype == otEnergy) {
+                if (c->rfmode == 1) {
+                    /* RF forward, 2833-2840: (w0 - w) / (mua + i omega n / c0) */
+                    float dre = s.w0re - s.wre, dim = s.w0im - s.wim;
+                    float aim = c->omega * s.prop.w * c->oneoverc0;
+                    float am2 = s.prop.x * s.prop.x + aim * aim;
+                    weight = (am2 < K_EPS) ? (s.w0re * s.pathlen) : (dre * s.prop.x + dim * aim) / am2;
+                    weight_im = (am2 < K_EPS) ? (s.w0im * s.pathlen) : (dim * s.prop.x - dre * aim) / am2;
+                } else if (c->outputtype == otEnergy) {
                     weight = s.w0 - s.p.w;
                 } else if (c->outputtype == otFluence || c->outputtype == otFlux || c->outputtype >= otAdjoint) {
                     weight = (s.prop.x < K_EPS) ? (s.w0 * s.pathlen) : ((s.w0 - s.p.w) / (s.prop.x));
@@ -1175,13 +1262,17 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                     /* replay Jacobian deposit, mcx_core.cl:2845-2858: the detected
                        weight times the path length in the voxel, in the gate of the
                        photon's detected time of flight */
-                    if (c->outputtype == otJacobian || c->outputtype == otWLTOF) {
+                    if (c->outputtype == otJacobian || c->outputtype == otRF || c->outputtype == otWLTOF) {
                         long long k = replay_index(c, tid, (long long)(int)s.f.w - 1);
                         if (k >= 0 && k < (long long)c->nreplay) {
                             weight = c->rweight[k] * s.pathlen;
                             tshift = (int)(floorf((c->rtof[k] - c->twin0) * c->Rtstep)) +
                                      ((c->replaydet == -1) ? (((c->rdetid[k] & 0xFFFF) - 1) * (int)c->maxgate) : 0);
-                            if (c->outputtype == otWLTOF) {
+                            if (c->outputtype == otRF) {
+                                /* 2853-2855, 2875-2877: times cos / sin of the launch phase */
+                                weight = -weight * s.ppath[c->w0offset + c->srcnum];
+                                weight_im = -c->rweight[k] * s.pathlen * s.ppath[c->w0offset + c->srcnum + 1];
+                            } else if (c->outputtype == otWLTOF) {
                                 weight = weight * c->rtof[k];
                             }
                         }
@@ -1193,11 +1284,26 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                     tshift += ((int)s.ppath[c->w0offset - 1] - 1) * ((c->replay && c->replaydet == -1) ? (int)c->detnum : 1) *
                               (int)c->maxgate;
                 }
-                if (fabsf(weight) > 0.f) {
-                    share_add(X, &s, (size_t)idx1dold + (size_t)(long long)tshift * c->dimlen[2], weight);
+                if (c->outputtype == otRF && c->replay) {
+                    size_t at = (size_t)idx1dold + (size_t)(long long)tshift * c->dimlen[2];
+                    field_add_nospill(X, at, weight);
+                    if (c->omega > 0.f) {
+                        field_add_im(X, at, weight_im, 0);
+                    }
+                } else if (fabsf(weight) > 0.f) {
+                    int spilled = share_add(X, &s, (size_t)idx1dold + (size_t)(long long)tshift * c->dimlen[2], weight);
+                    if (c->rfmode == 1 && !spilled) {
+                        /* the reference deposits the imaginary part only when the real
+                           accumulator did not spill (its else-branch, 2887) */
+                        field_add_im(X, (size_t)idx1dold + (size_t)(long long)tshift * c->dimlen[2], weight_im, 1);
+                    }
                 }
             }
             s.w0 = s.p.w;
+            if (c->rfmode == 1) {
+                s.w0re = s.wre;
+                s.w0im = s.wim;
+            }
             s.pathlen = 0.f;
         } else {
             s.mediaid = mediaidold;
@@ -1239,6 +1345,12 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
         if (fabsf(s.p.w) < c->minenergy) {
             if (rng_next(s.t) * K_ROULETTE_SIZE <= 1.f) {
                 s.p.w *= K_ROULETTE_SIZE;
+                if (c->rfmode == 1) {
+                    s.wre *= K_ROULETTE_SIZE;
+                    s.wim *= K_ROULETTE_SIZE;
+                    s.w0re *= K_ROULETTE_SIZE;
+                    s.w0im *= K_ROULETTE_SIZE;
+                }
             } else {
                 if (launchnewphoton(X, &s, (mediaidold & DET_MASK))) {
                     break;
@@ -1449,6 +1561,19 @@ unsigned int mcxo_reclen(const mcxo_input* in) {
     return partial + SAVE_DETID(f) + 3 * (SAVE_PEXIT(f) + SAVE_VEXIT(f)) + SAVE_W0(f);
 }
 
+/* complex-weight transport (omega > 0, not a replay: mcx_host.cpp:473) or a
+   complex replay output (rf, rfmus) */
+static int rf_mode(const mcxo_input* in) {
+    if (in->omega > 0.f && !is_replay(in)) {
+        return 1;
+    }
+    return (is_replay(in) && (in->outputtype == otRF || in->outputtype == otRFmus)) ? 2 : 0;
+}
+
+unsigned int mcxo_fieldcomp(const mcxo_input* in) {
+    return rf_mode(in) ? 2u : 1u;
+}
+
 unsigned int mcxo_fieldlen(const mcxo_input* in) {
     unsigned int mult = (in->extrasrclen && in->srcid < 0) ? (in->extrasrclen + 1) : 1;
     if (in->srcnum > 1 && (in->srctype == S_PATTERN || in->srctype == S_PATTERN3D)) {
@@ -1521,7 +1646,8 @@ static int prepare(const mcxo_input* in, oprep* P) {
     if (in->mediabyte != 1 && in->mediabyte != 2 && in->mediabyte != 4 && !(in->mediabyte >= 99 && in->mediabyte <= 104)) {
         return -2;
     }
-    if (in->issaveref > 1 || (in->srcnum > 1 && is_replay(in))) {
+    if (in->issaveref > 1 || (in->srcnum > 1 && is_replay(in)) ||
+            (rf_mode(in) && in->srcnum > 1 && (in->srctype == S_PATTERN || in->srctype == S_PATTERN3D))) {
         return -3;
     }
     nvox = in->dimx * in->dimy * in->dimz;
@@ -1666,6 +1792,8 @@ static int prepare(const mcxo_input* in, oprep* P) {
     c.variant = in->variant;
     c.fieldmode = in->fieldmode;
     c.nthread = in->nthread;
+    c.omega = in->omega;
+    c.rfmode = rf_mode(in);
     if (is_replay(in)) {
         if (!in->replayseed || !in->replayweight || !in->replaytof || !in->replaydetid ||
                 (double)in->nreplay != in->nphoton) {
@@ -1753,6 +1881,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
     float steps;
     mcxo_stats stats;
     float* ffield = NULL;
+    unsigned int ncomp = 1;
     double* dfield = NULL;
     unsigned int nworkers = 1;
     float* wdetp = NULL;
@@ -1785,8 +1914,11 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
     energy = energy_out ? energy_out : (float*)malloc(sizeof(float) * 2 * in->nthread);
     memset(energy, 0, sizeof(float) * 2 * in->nthread);
 
+    /* complex fields: real and imaginary blocks; in float mode the four
+       quarters the RF deposits address (re, re spill, im, im spill) */
+    ncomp = c.rfmode ? 2u : 1u;
     if (c.fieldmode == MCXO_FIELD_FLOAT_SPILL || in->debugrng) {
-        ffield = (float*)calloc((size_t)fieldlen * 2, sizeof(float));
+        ffield = (float*)calloc((size_t)fieldlen * (c.rfmode ? 4 : 2), sizeof(float));
         c.fieldmode = MCXO_FIELD_FLOAT_SPILL;
     }
 
@@ -1890,7 +2022,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
             unsigned int t0 = w * chunk, t1 = (w + 1) * chunk, t;
             memset(&X, 0, sizeof(X));
             X.c = &c;
-            wfield[w] = (double*)calloc(fieldlen, sizeof(double));
+            wfield[w] = (double*)calloc((size_t)fieldlen * ncomp, sizeof(double));
             X.fd = wfield[w];
             X.detcap = in->maxdetphoton;
             X.detp = wdetp + (size_t)w * in->maxdetphoton * (hostreclen ? hostreclen : 1);
@@ -1909,10 +2041,10 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
             wcnt[w][3] = X.nreflect;
             wcnt[w][4] = X.nfailed;
         }
-        dfield = (double*)calloc(fieldlen, sizeof(double));
+        dfield = (double*)calloc((size_t)fieldlen * ncomp, sizeof(double));
         for (w = 0; w < nworkers; w++) {
             unsigned int k, take;
-            for (k = 0; k < fieldlen; k++) {
+            for (k = 0; k < fieldlen * ncomp; k++) {
                 dfield[k] += wfield[w][k];
             }
             free(wfield[w]);
@@ -1959,7 +2091,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
         stats.energyesc = eesc;
         if (in->isnormalized) {
             stats.energyabs = etot - eesc;
-            if (in->outputtype == otFlux || in->outputtype == otFluence || in->outputtype >= otAdjoint) {
+            if (in->outputtype == otFlux || in->outputtype == otFluence || in->outputtype >= otAdjoint || c.rfmode == 1) {
                 scale = (float)((double)in->unitinmm / (etot * (double)Vvox * (double)in->tstep));
                 if (in->outputtype == otFluence || in->outputtype >= otAdjoint) {
                     scale *= in->tstep;
@@ -1967,6 +2099,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
             } else if (in->outputtype == otEnergy || in->outputtype == otL) {
                 scale = (float)(1.0 / etot);
             } else if (c.replay && (in->outputtype == otJacobian || in->outputtype == otWP || in->outputtype == otDCS ||
+                                    in->outputtype == otRF || in->outputtype == otRFmus ||
                                     in->outputtype == otWLTOF || in->outputtype == otWPTOF)) {
                 /* replay outputs, mcx_host.cpp:1396-1431: unitinmm over the replayed
                    detected weight, per detector when each has its own block */
@@ -2015,11 +2148,21 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
             }
             stats.normalizer = scale;
         }
-        for (i = 0; i < fieldlen; i++) {
+        for (i = 0; i < fieldlen * ncomp; i++) {
             double raw;
             float merged;
+            const unsigned int j = i % fieldlen;
             if (ffield) {
-                merged = ffield[i] + ffield[i + fieldlen];
+                /* the reference host's merge (mcx_host.cpp:1251-1274): the spill half
+                   is added except for the rf replay outputs, whose imaginary part is
+                   the second half; the forward run's imaginary part is the third
+                   quarter plus its spill */
+                if (i < fieldlen) {
+                    merged = (c.rfmode == 2) ? ffield[i] : ffield[i] + ffield[i + fieldlen];
+                } else {
+                    merged = (c.rfmode == 1) ? ffield[j + 2 * (size_t)fieldlen] + ffield[j + 3 * (size_t)fieldlen]
+                                             : ffield[j + fieldlen];
+                }
                 raw = (double)merged;
             } else {
                 raw = dfield[i];
@@ -2029,7 +2172,7 @@ int mcxo_run(const mcxo_input* in, double* field_out, float* fieldnorm, float* e
                 field_out[i] = raw;
             }
             if (fieldnorm) {
-                float sc = blockscale ? blockscale[i / (fieldlen / c.detnum)] : (sharescale ? sharescale[i % c.srcnum] : scale);
+                float sc = blockscale ? blockscale[j / (fieldlen / c.detnum)] : (sharescale ? sharescale[j % c.srcnum] : scale);
                 fieldnorm[i] = in->isnormalized ? merged * sc : merged;
             }
         }
@@ -2170,6 +2313,8 @@ int mcxo_prepare_ref(const mcxo_input* in, mcxo_refprep* R) {
     R->seedwords = P.seedwords;
     R->nvox = P.nvox;
     R->fieldlen = P.fieldlen;
+    R->omega = P.c.omega;
+    R->rfmode = P.c.rfmode;
     return 0;
 }
 

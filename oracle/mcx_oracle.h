@@ -119,6 +119,11 @@ typedef struct mcxo_input {
     /* optional output: weight and time of flight of each saved detected photon
        when it was detected (maxdetphoton x 2 floats), or NULL */
     float* detweight_out;
+
+    /* modulation angular frequency (rad/s): with omega > 0 a forward run
+       carries complex photon weights (RF forward), and the replay outputs
+       'rf' and 'rfmus' are complex */
+    float omega;
 } mcxo_input;
 
 typedef struct mcxo_stats {
@@ -146,11 +151,14 @@ int mcxo_replayinit(const mcxo_input* in, const float* detp, unsigned int reclen
 
 unsigned int mcxo_reclen(const mcxo_input* in);
 unsigned int mcxo_fieldlen(const mcxo_input* in);
+/* 2 when the field is complex (RF forward, RF replay outputs): the outputs
+   then hold fieldlen real values followed by fieldlen imaginary values */
+unsigned int mcxo_fieldcomp(const mcxo_input* in);
 
 /*
  * Run the simulation.  Outputs (caller-allocated, may be NULL when unused):
- *   field     fieldlen doubles: the merged raw field (both spill halves summed)
- *   fieldnorm fieldlen floats : normalised as mcx_run_simulation does
+ *   field     fieldlen doubles (x mcxo_fieldcomp): the merged raw field
+ *   fieldnorm fieldlen floats (x mcxo_fieldcomp): normalised as mcx_run_simulation does
  *   energy    2*nthread floats: per-thread {escaped, launched} weight
  *   detp      maxdetphoton*reclen floats, in the host record layout
  *   seeds     maxdetphoton*2 uint64 (launch RNG state of each record)
@@ -184,6 +192,8 @@ typedef struct mcxo_refprep {
     uint32_t* media;            /* masked volume */
     uint32_t* seedwords;        /* 4 per thread */
     unsigned int nvox, fieldlen;
+    float omega;
+    int rfmode;                 /* 0 real, 1 RF forward, 2 RF replay output */
 } mcxo_refprep;
 
 int  mcxo_prepare_ref(const mcxo_input* in, mcxo_refprep* out);

@@ -59,7 +59,7 @@ class MCXOInput(ctypes.Structure):
         ("nworkers", ctypes.c_int),
         ("replayseed", ctypes.c_void_p), ("replayweight", ctypes.c_void_p), ("replaytof", ctypes.c_void_p),
         ("replaydetid", ctypes.c_void_p), ("nreplay", ctypes.c_uint), ("replaydet", ctypes.c_int),
-        ("replaysiteown", ctypes.c_int), ("detweight_out", ctypes.c_void_p),
+        ("replaysiteown", ctypes.c_int), ("detweight_out", ctypes.c_void_p), ("omega", ctypes.c_float),
     ]
 
 
@@ -95,6 +95,7 @@ def lib():
         _lib.mcxo_run.restype = ctypes.c_int
         _lib.mcxo_reclen.restype = ctypes.c_uint
         _lib.mcxo_fieldlen.restype = ctypes.c_uint
+        _lib.mcxo_fieldcomp.restype = ctypes.c_uint
         _lib.mcxo_pm_logf.restype = ctypes.c_float
         _lib.mcxo_pm_logf.argtypes = [ctypes.c_float]
         _lib.mcxo_pm_expf.restype = ctypes.c_float
@@ -195,6 +196,7 @@ def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT
         keep["srcpattern"] = pat
         inp.srcpattern = _ptr(pat)
     inp.srcnum = int(cfg.get("srcnum", 1))
+    inp.omega = float(cfg.get("omega", 0.0))
 
     if "detpos" in cfg and np.asarray(cfg["detpos"]).size:
         det = np.ascontiguousarray(_rows(cfg["detpos"]))
@@ -300,7 +302,7 @@ def run(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL
     detected-photon records, seeds, stats and event counters."""
     inp, keep = make_input(cfg, nthread, core, mathmode, variant, fieldmode, nworkers)
     L = lib()
-    fieldlen = L.mcxo_fieldlen(ctypes.byref(inp))
+    fieldlen = L.mcxo_fieldlen(ctypes.byref(inp)) * L.mcxo_fieldcomp(ctypes.byref(inp))
     reclen = L.mcxo_reclen(ctypes.byref(inp))
     field = np.zeros(fieldlen, np.float64)
     fnorm = np.zeros(fieldlen, np.float32)
@@ -343,7 +345,7 @@ def run_reference(cfg, nthread=4096, core=None, nblocksize=64, nworkers=1):
     inp, keep = make_input(cfg, nthread, core, MATH_LIBM, VARIANT_NVCC, FIELD_FLOAT_SPILL, 1)
     L = lib()
     R = reflib(pattern=inp.srctype in (5, 15))
-    fieldlen = L.mcxo_fieldlen(ctypes.byref(inp))
+    fieldlen = L.mcxo_fieldlen(ctypes.byref(inp)) * L.mcxo_fieldcomp(ctypes.byref(inp))
     reclen = L.mcxo_reclen(ctypes.byref(inp))
     field = np.zeros(fieldlen, np.float32)
     energy = np.zeros(2 * inp.nthread, np.float32)

@@ -114,6 +114,7 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     P.gscatter = R.gscatter;
     P.is2d = R.is2d;
     P.srcnum = R.srcnum;
+    P.omega = R.omega;
     P.nphase = R.nphase;
     P.nphaselen = R.nphase + (R.nphase & 1);
     P.nangle = R.nangle;
@@ -125,7 +126,9 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
        so the volume is padded with a zero second half */
     std::vector<unsigned int> media(2 * (size_t)R.nvox, 0u);
     std::memcpy(media.data(), R.media, sizeof(unsigned int) * R.nvox);
-    std::vector<float> field(2 * (size_t)R.fieldlen, 0.f);
+    /* RF: four quarters (re, re spill, im, im spill); the rfmus replay output
+       writes the third quarter although the reference allocates two */
+    std::vector<float> field((R.rfmode ? 4 : 2) * (size_t)R.fieldlen, 0.f);
     std::vector<float> genergy(2 * (size_t)in->nthread, 0.f);
     std::vector<unsigned int> seeds(R.seedwords, R.seedwords + 4 * (size_t)in->nthread);
     /* replay: the seed buffer holds one saved state per photon (the kernel
@@ -176,8 +179,19 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     }
 #undef RUN
 
-    for (size_t i = 0; i < R.fieldlen; i++) {
-        field_out[i] = field[i] + field[i + R.fieldlen];
+    /* the reference host's merge, mcx_host.cpp:1251-1274 */
+    const size_t F = R.fieldlen;
+    for (size_t i = 0; i < F; i++) {
+        field_out[i] = (R.rfmode == 2) ? field[i] : field[i] + field[i + F];
+    }
+    if (R.rfmode == 1) {
+        for (size_t i = 0; i < F; i++) {
+            field_out[F + i] = field[i + 2 * F] + field[i + 3 * F];
+        }
+    } else if (R.rfmode == 2) {
+        for (size_t i = 0; i < F; i++) {
+            field_out[F + i] = field[i + F];
+        }
     }
     if (energy_out) {
         std::memcpy(energy_out, genergy.data(), sizeof(float) * 2 * in->nthread);

@@ -103,6 +103,9 @@ VARIANTS = {
                           srcnum=3, srcpattern=_pattern((3, 4, 4), 4), issaveref=1, vol=_voidtop()),
     "pattern3d_share": dict(srctype="pattern3d", srcpos=[5, 5, 5], srcparam1=[4, 4, 4, 0], srcnum=2,
                             srcpattern=_pattern((2, 4, 4, 4), 5)),
+    # RF forward: complex photon weights at 100 MHz (omega in rad/s), and with roulette
+    "rf_forward": dict(omega=2 * np.pi * 1e8),
+    "rf_roulette": dict(omega=2 * np.pi * 3e8, minenergy=0.01, outputtype="fluence"),
     "focus": dict(srcdir=[0, 0, 1, 10]),
     "lambert": dict(srcdir=[0, 0, 1, -np.inf]),
     "noreflect": dict(isreflect=0),
@@ -204,4 +207,8 @@ REPLAY_PINS = [
     ("replay_wltof", dict(nphoton=3000), dict(outputtype="wltof"), 128),
     ("replay_wptof", dict(nphoton=3000), dict(outputtype="wptof"), 16),
     ("replay_flux", dict(nphoton=3000), dict(outputtype="flux"), 128),
+    # frequency-domain replay outputs at 100 MHz (omega in rad/s)
+    ("replay_rf", dict(nphoton=3000), dict(outputtype="rf", omega=2 * np.pi * 1e8), 128),
+    ("replay_rf_perdet", dict(nphoton=3000), dict(outputtype="rf", omega=2 * np.pi * 1e8, replaydet=-1), 128),
+    ("replay_rfmus", dict(nphoton=3000), dict(outputtype="rfmus", omega=2 * np.pi * 1e8), 128),
 ]
