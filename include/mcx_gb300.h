@@ -194,6 +194,8 @@ typedef struct MCXConfig {
     float* exportdetweight;       /* 2 x detectedcount: weight and time of flight (s) of each saved photon when detected */
     int replaysiteown;            /* replay: 1 = scattering-site outputs use the replayed photon's own weight and time
                                      (the reference reads the next photon's, mcx_core.cl:2571) */
+    float omega;                  /* modulation angular frequency 2 pi f (rad/s), mcx_utils.h:231: > 0 runs the
+                                     frequency-domain (RF) transport, or phases the rf/rfmus replay outputs */
     int errorcode;                /* last error in library mode */
     char errormsg[256];
 } Config;

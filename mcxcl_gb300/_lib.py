@@ -89,7 +89,7 @@ class Config(ctypes.Structure):
         ("exportenergy", ctypes.POINTER(ctypes.c_float)), ("savethreadenergy", ctypes.c_int),
         ("autotune", ctypes.c_int), ("savedetweight", ctypes.c_int),
         ("exportdetweight", ctypes.POINTER(ctypes.c_float)), ("replaysiteown", ctypes.c_int),
-        ("errorcode", ctypes.c_int),
+        ("omega", ctypes.c_float), ("errorcode", ctypes.c_int),
         ("errormsg", ctypes.c_char * 256),
     ]
 

@@ -195,25 +195,40 @@ __global__ void energy_final(double* part, int nblocks) {
     }
 }
 
-__global__ void field_merge_f32(const float* __restrict__ f, size_t n, double scale, float* __restrict__ out) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        out[i] = (float)(((double)f[i] + (double)f[i + n]) * scale);
+/* Output element i of a field of n elements per component: component
+   c = i / n (1 real, or real then imaginary for RF), element j = i % n; each
+   component is a high plane followed by its low plane. */
+__device__ __forceinline__ double merged_at(const float* __restrict__ f, size_t n, size_t i, size_t& j) {
+    const size_t c = i / n;
+    j = i - c * n;
+    return (double)f[2 * c * n + j] + (double)f[2 * c * n + n + j];
+}
+
+__global__ void field_merge_f32(const float* __restrict__ f, size_t n, size_t total, double scale,
+                                float* __restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        size_t j;
+        out[i] = (float)(merged_at(f, n, i, j) * scale);
     }
 }
 
-/* element i belongs to source i % nsrc (photon sharing interleaves the
+/* element j belongs to source j % nsrc (photon sharing interleaves the
    patterns innermost) */
-__global__ void field_merge_interleaved(const float* __restrict__ f, size_t n, unsigned int nsrc,
+__global__ void field_merge_interleaved(const float* __restrict__ f, size_t n, size_t total, unsigned int nsrc,
                                         const double* __restrict__ scales, float* __restrict__ out) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        out[i] = (float)(((double)f[i] + (double)f[i + n]) * scales[i % nsrc]);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        size_t j;
+        const double v = merged_at(f, n, i, j);
+        out[i] = (float)(v * scales[j % nsrc]);
     }
 }
 
-__global__ void field_merge_blocks(const float* __restrict__ f, size_t n, size_t blocklen,
+__global__ void field_merge_blocks(const float* __restrict__ f, size_t n, size_t total, size_t blocklen,
                                    const double* __restrict__ scales, float* __restrict__ out) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        out[i] = (float)(((double)f[i] + (double)f[i + n]) * scales[i / blocklen]);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        size_t j;
+        const double v = merged_at(f, n, i, j);
+        out[i] = (float)(v * scales[j / blocklen]);
     }
 }
 
@@ -352,9 +367,10 @@ __global__ void adjoint_dcoeff(const float* __restrict__ f, float* __restrict__ 
     }
 }
 
-__global__ void field_merge_f64(const float* __restrict__ f, size_t n, double* __restrict__ out) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        out[i] = (double)f[i] + (double)f[i + n];
+__global__ void field_merge_f64(const float* __restrict__ f, size_t n, size_t total, double* __restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        size_t j;
+        out[i] = merged_at(f, n, i, j);
     }
 }
 
@@ -391,10 +407,18 @@ int grid_for(const mcxg_session* s, size_t n) {
 /* property rows and their reciprocals (2 x 16 B per medium), 32 B of
    launch-time state per thread, the phase tables, and the detector partial
    data per thread */
+/* 2 for a complex (RF) field: the RF transport, or an rf / rfmus replay */
+unsigned int field_comps(const mcxg_kparams& kp) {
+    return ((kp.omega > 0.f && !kp.replay) || (kp.replay && (kp.outputtype == otRF || kp.outputtype == otRFmus))) ? 2u : 1u;
+}
+
 size_t shared_bytes(const mcxg_kparams& kp, int block) {
     /* per-thread slots: detector partial data, then one weight per shared
        pattern (their slots start after the partial data) */
     size_t det = (kp.srcnum > 1) ? (size_t)kp.partialdata + kp.srcnum : (kp.savedet ? kp.partialdata : 0);
+    if (kp.replay && (kp.outputtype == otRF || kp.outputtype == otRFmus)) {
+        det = (size_t)kp.partialdata + 2;    /* the launch phase's cos and sin follow the partial data */
+    }
     return (size_t)kp.medianum * 32 + (size_t)block * 32 + (size_t)(kp.nphase + kp.nangle) * 4 + det * (size_t)block * 4;
 }
 
@@ -571,7 +595,7 @@ int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, 
         rc = ensure(&s->d_pattern, &s->pattern_cap, npattern);
     }
     if (!rc) {
-        rc = ensure(&s->d_field, &s->field_cap, 2 * (size_t)kp.fieldlen);
+        rc = ensure(&s->d_field, &s->field_cap, 2 * (size_t)kp.fieldlen * field_comps(kp));
     }
     if (!rc && kp.savedet) {
         size_t recs = kp.maxdetphoton;
@@ -706,8 +730,21 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
         MCXG_TRY(mcxg::fast_upload(&kp, s->h_det.data(), kp.detnum, s->h_srcx.data(), kp.extrasrclen, s->st));
         s->up_fast = true;
     }
+    {
+        /* a run that turns on the complex field after mcxg_set_problem */
+        const size_t need = 2 * (size_t)kp.fieldlen * field_comps(kp);
+        if (need > s->field_cap) {
+            if (flags & MCXG_KEEP) {
+                return MCXG_ERR_STATE;
+            }
+            const int rc = ensure(&s->d_field, &s->field_cap, need);
+            if (rc) {
+                return rc;
+            }
+        }
+    }
     if (!(flags & MCXG_KEEP)) {
-        MCXG_TRY(cudaMemsetAsync(s->d_field, 0, sizeof(float) * 2 * (size_t)kp.fieldlen, s->st));
+        MCXG_TRY(cudaMemsetAsync(s->d_field, 0, sizeof(float) * 2 * (size_t)kp.fieldlen * field_comps(kp), s->st));
     }
     s->out_valid = false;
     MCXG_TRY(cudaMemsetAsync(s->d_energy, 0, sizeof(float2) * kp.nthread, s->st));
@@ -743,19 +780,21 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     /* deposits go straight to the field unless aggregation is asked for or
        the autotuner found it faster for this problem */
     const bool noagg = (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
-    const bool xmedia = kp.mediaformat > 4 && kp.mediaformat != 101;
+    const bool rf = kp.omega > 0.f && !kp.replay;
+    const bool xmedia = !rf && kp.mediaformat > 4 && kp.mediaformat != 101;
     /* the instantiations that fix the common configuration's parameters */
-    const bool common = !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2 && kp.srcnum <= 1;
-    const int bpsm_sel = xmedia ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
+    const bool common = !rf && !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2 &&
+                        kp.srcnum <= 1;
+    const int bpsm_sel = (xmedia || rf) ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
                  (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
-                 (common ? mcxg::LF_COMMON : 0);
+                 (common ? mcxg::LF_COMMON : 0) | (rf ? mcxg::LF_RF : 0);
     int block = s->block_req ? s->block_req : 256;
     size_t smem = shared_bytes(kp, block);
     if (smem > s->info.sharedmem_per_block) {
         return MCXG_ERR_LIMIT;
     }
-    int bpsm = (s->bpsm_req && !xmedia) ? s->bpsm_req : (exact ? 2 : bpsm_sel);
+    int bpsm = (s->bpsm_req && !xmedia && !rf) ? s->bpsm_req : (exact ? 2 : bpsm_sel);
     if (!exact) {
         /* never more blocks than fit at once: a persistent grid must be resident */
         int occ = 0;
@@ -898,14 +937,14 @@ int mcxg_get_field(mcxg_session* s, float* out, double scale) {
         return MCXG_ERR_ARG;
     }
     MCXG_TRY(cudaSetDevice(s->device));
-    size_t n = s->kp.fieldlen;
-    int rc = ensure((double**)&s->d_out, &s->out_cap, n);
+    size_t n = s->kp.fieldlen, total = n * field_comps(s->kp);
+    int rc = ensure((double**)&s->d_out, &s->out_cap, total);
     if (rc) {
         return rc;
     }
-    field_merge_f32<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, scale, (float*)s->d_out);
+    field_merge_f32<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, scale, (float*)s->d_out);
     s->out_valid = true;
-    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
 }
@@ -915,8 +954,8 @@ int mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uin
         return MCXG_ERR_ARG;
     }
     MCXG_TRY(cudaSetDevice(s->device));
-    size_t n = s->kp.fieldlen;
-    int rc = ensure((double**)&s->d_out, &s->out_cap, n);
+    size_t n = s->kp.fieldlen, total = n * field_comps(s->kp);
+    int rc = ensure((double**)&s->d_out, &s->out_cap, total);
     if (!rc) {
         rc = ensure(&s->d_scales, &s->scales_cap, nblocks);
     }
@@ -924,9 +963,10 @@ int mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uin
         return rc;
     }
     MCXG_TRY(cudaMemcpyAsync(s->d_scales, scales, sizeof(double) * nblocks, cudaMemcpyHostToDevice, s->st));
-    field_merge_blocks<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, n / nblocks, s->d_scales, (float*)s->d_out);
+    field_merge_blocks<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, n / nblocks, s->d_scales,
+                                                              (float*)s->d_out);
     s->out_valid = true;
-    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
 }
@@ -936,8 +976,8 @@ int mcxg_get_field_interleaved(mcxg_session* s, float* out, const double* scales
         return MCXG_ERR_ARG;
     }
     MCXG_TRY(cudaSetDevice(s->device));
-    size_t n = s->kp.fieldlen;
-    int rc = ensure((double**)&s->d_out, &s->out_cap, n);
+    size_t n = s->kp.fieldlen, total = n * field_comps(s->kp);
+    int rc = ensure((double**)&s->d_out, &s->out_cap, total);
     if (!rc) {
         rc = ensure(&s->d_scales, &s->scales_cap, nsrc);
     }
@@ -945,9 +985,10 @@ int mcxg_get_field_interleaved(mcxg_session* s, float* out, const double* scales
         return rc;
     }
     MCXG_TRY(cudaMemcpyAsync(s->d_scales, scales, sizeof(double) * nsrc, cudaMemcpyHostToDevice, s->st));
-    field_merge_interleaved<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, nsrc, s->d_scales, (float*)s->d_out);
+    field_merge_interleaved<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, nsrc, s->d_scales,
+                                                                   (float*)s->d_out);
     s->out_valid = true;
-    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
 }
@@ -982,14 +1023,14 @@ int mcxg_get_field_f64(mcxg_session* s, double* out) {
         return MCXG_ERR_ARG;
     }
     MCXG_TRY(cudaSetDevice(s->device));
-    size_t n = s->kp.fieldlen;
-    int rc = ensure((double**)&s->d_out, &s->out_cap, n);
+    size_t n = s->kp.fieldlen, total = n * field_comps(s->kp);
+    int rc = ensure((double**)&s->d_out, &s->out_cap, total);
     if (rc) {
         return rc;
     }
-    field_merge_f64<<<grid_for(s, n), 256, 0, s->st>>>(s->d_field, n, (double*)s->d_out);
+    field_merge_f64<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, (double*)s->d_out);
     s->out_valid = false;
-    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(double) * total, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
 }

@@ -591,8 +591,14 @@ void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte) {
     if (replayout && cfg->seed != SEED_FROM_FILE) {
         MCX_ERROR(-6, "Jacobian output is only valid in the reply mode. Please define cfg.seed");
     }
-    if (cfg->outputtype == otRF || cfg->outputtype == otRFmus) {
-        MCX_ERROR(-6, "RF replay outputs need the frequency-domain transport, which this build does not include");
+    if (cfg->omega < 0.f) {
+        MCX_ERROR(-6, "the modulation frequency omega must not be negative");
+    }
+    if (cfg->omega > 0.f && MCX_IS_ADJOINT_TYPE(cfg->outputtype)) {
+        MCX_ERROR(-6, "frequency-domain adjoint outputs are not supported by this build");
+    }
+    if (cfg->omega > 0.f && cfg->srcnum > 1 && (cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D)) {
+        MCX_ERROR(-6, "the frequency-domain transport can not be combined with photon sharing");
     }
     if (!replayout && cfg->outputtype != otFlux && cfg->outputtype != otFluence && cfg->outputtype != otEnergy &&
             cfg->outputtype != otL && !MCX_IS_ADJOINT_TYPE(cfg->outputtype)) {
@@ -903,6 +909,7 @@ static void make_kparams(const Config* cfg, size_t nvox, size_t fieldlen, size_t
     kp->srcid = cfg->srcid;
     kp->srcnum = (cfg->srcnum > 1 && (cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D))
                  ? cfg->srcnum : 1u;
+    kp->omega = cfg->omega;
     kp->nthread = (uint32_t)autothread;
     if (replay) {
         kp->replay = 1;
@@ -1261,12 +1268,14 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     uint32_t nblocks = 1;
     if (cfg->issave2pt) {
         int replayout = cfg->outputtype == otJacobian || cfg->outputtype == otWP || cfg->outputtype == otDCS ||
+                        cfg->outputtype == otRF || cfg->outputtype == otRFmus ||
                         cfg->outputtype == otWLTOF || cfg->outputtype == otWPTOF;
         if (cfg->isnormalized) {
             float Vvox = cfg->steps.x * cfg->steps.y * cfg->steps.z;
             float sc = 1.f;
             cfg->energyabs += cfg->energytot - cfg->energyesc;
-            if (cfg->outputtype == otFlux || cfg->outputtype == otFluence || MCX_IS_ADJOINT_TYPE(cfg->outputtype)) {
+            if (cfg->outputtype == otFlux || cfg->outputtype == otFluence || MCX_IS_ADJOINT_TYPE(cfg->outputtype) ||
+                    (cfg->omega > 0.f && !replay)) {
                 sc = (float)(cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep));
                 if (cfg->outputtype == otFluence || MCX_IS_ADJOINT_TYPE(cfg->outputtype)) {
                     sc *= cfg->tstep;
@@ -1349,16 +1358,20 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
             free(blockscale);
             blockscale = NULL;
         }
+        /* a complex field (RF transport, rf / rfmus replay) exports its real part
+           then its imaginary part (mcx_host.cpp:1050-1052, 1262-1274) */
+        const size_t fcomp = ((cfg->omega > 0.f && !replay) ||
+                              (replay && (cfg->outputtype == otRF || cfg->outputtype == otRFmus))) ? 2 : 1;
         float* dst = cfg->exportfield;
         if (!dst) {
-            cfg->exportfield = (float*)calloc(fieldlen, sizeof(float));
+            cfg->exportfield = (float*)calloc(fieldlen * fcomp, sizeof(float));
             if (!cfg->exportfield) {
                 MCX_ERROR(-2, "out of host memory");
             }
             dst = cfg->exportfield;
         } else {
             /* caller-supplied buffer: add, as the reference does (mcx_host.cpp:1292-1296) */
-            fieldtmp = (float*)malloc(sizeof(float) * fieldlen);
+            fieldtmp = (float*)malloc(sizeof(float) * fieldlen * fcomp);
             if (!fieldtmp) {
                 MCX_ERROR(-2, "out of host memory");
             }
@@ -1372,7 +1385,7 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
             device_check(mcxg_get_field(s, dst, scale), "reading the field");
         }
         if (dst == fieldtmp) {
-            for (size_t i = 0; i < fieldlen; i++) {
+            for (size_t i = 0; i < fieldlen * fcomp; i++) {
                 cfg->exportfield[i] += fieldtmp[i];
             }
         }
@@ -1469,10 +1482,10 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
     for (int k = 0; k < n; k++) {
         Config* cfg = cfgs[k];
         if (!cfg || cfg->issavedet || cfg->seed == SEED_FROM_FILE || cfg->extrasrclen || cfg->nphase || cfg->nangle ||
-                cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D || cfg->mediabyte > 4 ||
+                cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D || cfg->mediabyte > 4 || cfg->omega > 0.f ||
                 cfg->medianum > MCXG_BATCH_MAXMEDIA || cfg->respin != 1 || cfg->issaveref || (cfg->debuglevel & 1)) {
             MCX_ERROR(-4, "a batch simulation takes label volumes of at most 4 property rows, one respin, and no "
-                      "detectors, replay, extra sources, patterns, phase tables or saved reflectance");
+                      "detectors, replay, extra sources, patterns, phase tables, saved reflectance or RF");
         }
         if (cfg->nphoton == 0) {
             MCX_ERROR(-4, "every simulation of a batch needs at least one photon");
@@ -1640,7 +1653,7 @@ static const struct {
     MCX_FIELD(bc), MCX_FIELD(nphase), MCX_FIELD(invcdf), MCX_FIELD(nangle), MCX_FIELD(angleinvcdf), MCX_FIELD(srcid),
     MCX_FIELD(extrasrclen), MCX_FIELD(srcdata), MCX_FIELD(replay), MCX_FIELD(replaydet), MCX_FIELD(detdir), MCX_FIELD(exportjacob), MCX_FIELD(exactmath), MCX_FIELD(kernelms), MCX_FIELD(eventcount),
     MCX_FIELD(failedlaunch), MCX_FIELD(threadused), MCX_FIELD(exportenergy), MCX_FIELD(savethreadenergy),
-    MCX_FIELD(autotune), MCX_FIELD(savedetweight), MCX_FIELD(exportdetweight), MCX_FIELD(replaysiteown),
+    MCX_FIELD(autotune), MCX_FIELD(savedetweight), MCX_FIELD(exportdetweight), MCX_FIELD(replaysiteown), MCX_FIELD(omega),
     MCX_FIELD(errorcode), MCX_FIELD(errormsg),
 };
 

@@ -216,6 +216,10 @@ struct BatchPS {
 #define KP_NPHASE_GT2 (!PS::kCommon && c_p.nphase > 2)
 #define KP_MEDIAFORMAT (PS::kCommon ? 1u : c_p.mediaformat)
 #define KP_SHARING (!PS::kCommon && c_p.srcnum > 1)
+/* frequency-domain transport (complex photon weights) in the instantiations
+   compiled with it; the rf / rfmus replay outputs in every one that replays */
+#define KP_RFFWD (RF && c_p.omega > 0.f && !c_p.replay)
+#define KP_RFREPLAY (c_p.replay && (c_p.outputtype == otRF || c_p.outputtype == otRFmus))
 
 /* ------------------------------------------------------------------ math */
 
@@ -285,6 +289,7 @@ struct Photon {
     unsigned int idx1d, mediaid, isdet;
     float w0, Lmove, pathlen, n1;
     Rng t;
+    float wre, wim, w0re, w0im;    /* RF transport: complex weight now and at the last voxel change */
 };
 
 template <class PS>
@@ -704,6 +709,26 @@ __device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, boo
     }
 }
 
+/* rf replay output (mcx_core.cl:2853-2877): the real part (no spill) and,
+   with omega > 0, the imaginary part in the planes after the real ones; the
+   gate shift and its fold follow the deposit in the transport loop */
+template <class PS>
+__device__ __forceinline__ void rf_replay_deposit(const KArgs& a, const PS& ps, unsigned int idx, int tshift, float wre,
+                                                  float wim) {
+    const mcxg_kparams& c_p = ps.p();
+    if (c_p.extrasrclen && (c_p.srcid < 0)) {
+        tshift += ((int)ps.cold()->srcsel - 1) * ((c_p.replaydet == -1) ? (int)c_p.detnum : 1) * (int)c_p.maxgate;
+    }
+    unsigned int key = idx + (unsigned int)tshift * c_p.nvox;
+    if (key >= c_p.fieldlen) {
+        key -= c_p.fieldlen;
+    }
+    field_add2(a.field, ps.lo_plane(), key, wre);
+    if (c_p.omega > 0.f) {
+        field_add2(a.field + 2 * (size_t)c_p.fieldlen, c_p.fieldlen, key, wim);
+    }
+}
+
 /* Photon sharing (mcx_core.cl:1527-1538, 2902-2911): a deposit goes to every
    pattern with a non-zero weight, element (voxel + gate * nvox) * srcnum +
    pattern, scaled by that weight.  An element one gate past the last folds
@@ -750,7 +775,13 @@ __device__ void replay_site_deposit(const KArgs& a, const PS& ps, const Shared& 
     float rt = __ldg(a.rtof + k);
     float rw = __ldg(a.rweight + k);
     float tmp0 = (c_p.outputtype == otDCS) ? (1.f - ctheta) : 1.f;
-    if (c_p.outputtype == otWPTOF) {
+    float tim = 0.f;
+    if (c_p.outputtype == otRFmus) {
+        /* 2572-2576: the launch phase's cos / sin (the reference's imaginary
+           part goes to a quarter of the field it never allocated) */
+        tmp0 = rw * ps.pp(c_p.partialdata);
+        tim = rw * ps.pp(c_p.partialdata + 1);
+    } else if (c_p.outputtype == otWPTOF) {
         tmp0 = rt;
         tmp0 *= rw;
     } else {
@@ -768,6 +799,9 @@ __device__ void replay_site_deposit(const KArgs& a, const PS& ps, const Shared& 
         return;
     }
     field_add2(a.field, ps.lo_plane(), ps.field_off() + (unsigned int)key, tmp0);
+    if (c_p.outputtype == otRFmus) {
+        field_add2(a.field + 2 * (size_t)c_p.fieldlen, c_p.fieldlen, (unsigned int)key, tim);
+    }
 }
 
 /* ------------------------------------------------------------------ launch */
@@ -791,7 +825,7 @@ __device__ __forceinline__ void set_launch_voxel(const KArgs& a, const PS& ps, P
  * reference thread.  Returns 0 on launch, 1 when the thread's quota is done,
  * -1 when no launch position was found.
  */
-template <bool EXACT, bool DET, class PS>
+template <bool EXACT, bool DET, bool RF, class PS>
 __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Photon& s, unsigned int isdet,
                                unsigned int vt, unsigned long long* nfailed) {
     const mcxg_kparams& c_p = ps.p();
@@ -1218,6 +1252,24 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     }
     s.v.w = K_EPS;
     s.Lmove = 0.f;
+    if (KP_RFFWD) {
+        /* the complex weight restarts with every launch (mcx_core.cl:2427-2430, 3011, 3054, ...) */
+        s.wre = s.w0re = s.p.w;
+        s.wim = s.w0im = 0.f;
+    } else if (KP_RFREPLAY) {
+        /* rf / rfmus replay (2257-2262): cos and sin of omega times the detected
+           time of flight, read with the launch counter itself (the next photon,
+           as the scattering-site outputs do: siteshift 1); the last photon reads
+           the start time.  The reference stores them through its launch's
+           partial-data-shifted pointer (1621), past the slots its deposits read,
+           so its rf outputs come out zero; here they go where they are read. */
+        long long k = replay_index(ps, vt, (long long)(int)s.f.w - 1 + (long long)c_p.siteshift);
+        const float tof = (k >= 0 && k < (long long)c_p.nreplay) ? __ldg(a.rtof + k) : c_p.twin0;
+        float rs, rc;
+        M::sincos(c_p.omega * tof, &rs, &rc);
+        ps.pp(c_p.partialdata) = rc;
+        ps.pp(c_p.partialdata + 1) = rs;
+    }
     return 0;
 }
 
@@ -1303,7 +1355,7 @@ __device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPS& ps, unsigned i
 }
 
 template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false,
-          bool COMMON = false>
+          bool COMMON = false, bool RF = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
     typedef typename std::conditional<BATCH, BatchPS, ConstPST<XMEDIA, COMMON>>::type PS;
@@ -1360,7 +1412,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             if (fresh && (unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
                 r = 1;
             } else {
-                r = launchnewphoton<EXACT, DET>(a, ps, S, s, fresh ? 0u : relaunch_isdet, vt, &cnt_fail);
+                r = launchnewphoton<EXACT, DET, RF>(a, ps, S, s, fresh ? 0u : relaunch_isdet, vt, &cnt_fail);
                 if (r && fresh) {
                     atomicAdd(a.status + ST_FAILED_LAUNCH, 1u);
                     r = 2;       /* NO_LAUNCH: the reference returns without writing energies */
@@ -1467,7 +1519,8 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 }
                 s.v.w += 1.f;
                 vdirty = true;
-                if (c_p.replay && (c_p.outputtype == otWP || c_p.outputtype == otDCS || c_p.outputtype == otWPTOF)) {
+                if (c_p.replay && (c_p.outputtype == otWP || c_p.outputtype == otDCS || c_p.outputtype == otWPTOF ||
+                                   c_p.outputtype == otRFmus)) {
                     replay_site_deposit(a, ps, S, s, vt, ctheta);
                 }
             }
@@ -1511,7 +1564,19 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             if (s.fw == 2) {
                 s.fz += scat_here ? 0 : (s.v.z > 0.f ? 1 : -1);
             }
-            s.p.w *= M::exp(-s.prop.x * s.f.z);
+            if (KP_RFFWD) {
+                /* RF transport (mcx_core.cl:2750-2760): w <- w exp(-(mua + i omega n / c0) ds) */
+                const float att = M::exp(-s.prop.x * s.f.z);
+                float rs, rc;
+                M::sincos(c_p.omega * s.prop.w * c_p.oneoverc0 * s.f.z, &rs, &rc);
+                const float tre = att * (s.wre * rc + s.wim * rs);
+                const float tim = att * (-s.wre * rs + s.wim * rc);
+                s.wre = tre;
+                s.wim = tim;
+                s.p.w = M::sqrt(s.wre * s.wre + s.wim * s.wim);
+            } else {
+                s.p.w *= M::exp(-s.prop.x * s.f.z);
+            }
             s.f.x -= slen;
             s.f.y += s.f.z * s.prop.w * c_p.oneoverc0;
         }
@@ -1538,13 +1603,21 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
 
         /* ---- deposit on a voxel change (mcx_core.cl:2816-2929) */
         {
-            bool dep = false;
+            bool dep = false, depim = false;
             unsigned int key = 0;
-            float weight = 0.f;
+            float weight = 0.f, weight_im = 0.f;
             if (s.idx1d != idx1dold && idx1dold < c_p.nvox && mediaidold) {
                 if (c_p.save2pt && s.f.y >= c_p.twin0 && s.f.y < c_p.twin1) {
                     int tshift = (int)(floorf((s.f.y - c_p.twin0) * c_p.Rtstep));
-                    if (c_p.outputtype == otEnergy) {
+                    if (KP_RFFWD) {
+                        /* RF transport (2833-2840): (w0 - w) / (mua + i omega n / c0) */
+                        const float dre = s.w0re - s.wre, dim = s.w0im - s.wim;
+                        const float aim = c_p.omega * s.prop.w * c_p.oneoverc0;
+                        const float am2 = s.prop.x * s.prop.x + aim * aim;
+                        weight = (am2 < K_EPS) ? (s.w0re * s.pathlen) : M::div(dre * s.prop.x + dim * aim, am2);
+                        weight_im = (am2 < K_EPS) ? (s.w0im * s.pathlen) : M::div(dim * s.prop.x - dre * aim, am2);
+                        depim = fabsf(weight) > 0.f;
+                    } else if (c_p.outputtype == otEnergy) {
                         weight = s.w0 - s.p.w;
                     } else if (c_p.outputtype == otFluence || c_p.outputtype == otFlux || c_p.outputtype >= otAdjoint) {
                         if (EXACT || KP_MEDIAFORMAT > 4) {
@@ -1557,7 +1630,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     } else if (c_p.replay) {
                         /* replay Jacobian (mcx_core.cl:2845-2858): detected weight times
                            the path length in the voxel, gated by the detected time of flight */
-                        if (c_p.outputtype == otJacobian || c_p.outputtype == otWLTOF) {
+                        if (c_p.outputtype == otJacobian || c_p.outputtype == otRF || c_p.outputtype == otWLTOF) {
                             long long k = replay_index(ps, vt, (long long)(int)s.f.w - 1);
                             if (k >= 0 && k < (long long)c_p.nreplay) {
                                 float rt = __ldg(a.rtof + k);
@@ -1573,6 +1646,12 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                                     atomicAdd(a.status + ST_GUARD, 1u);
                                     weight = 0.f;
                                     tshift = 0;
+                                } else if (c_p.outputtype == otRF) {
+                                    /* 2853-2855, 2875-2877: times cos / sin of the launch phase,
+                                       deposited here (even when zero, as the reference does) */
+                                    rf_replay_deposit(a, ps, idx1dold, tshift, -weight * ps.pp(c_p.partialdata),
+                                                      -__ldg(a.rweight + k) * s.pathlen * ps.pp(c_p.partialdata + 1));
+                                    weight = 0.f;
                                 }
                             }
                         }
@@ -1593,6 +1672,10 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     }
                 }
                 s.w0 = s.p.w;
+                if (KP_RFFWD) {
+                    s.w0re = s.wre;
+                    s.w0im = s.wim;
+                }
                 s.pathlen = 0.f;
             } else {
                 s.mediaid = mediaidold;
@@ -1603,6 +1686,10 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 }
             } else {
                 deposit<WAGG>(a.field, ps.lo_plane(), dep, ps.field_off() + key, weight, pd);
+            }
+            if (RF && depim) {
+                /* the imaginary planes follow the real ones: [2F, 3F) and its low plane */
+                field_add2(a.field + 2 * (size_t)c_p.fieldlen, c_p.fieldlen, key, weight_im);
             }
         }
 
@@ -1639,6 +1726,12 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         if (fabsf(s.p.w) < c_p.minenergy) {
             if (rnd(s.t) * K_ROULETTE <= 1.f) {
                 s.p.w *= K_ROULETTE;
+                if (KP_RFFWD) {
+                    s.wre *= K_ROULETTE;
+                    s.wim *= K_ROULETTE;
+                    s.w0re *= K_ROULETTE;
+                    s.w0im *= K_ROULETTE;
+                }
             } else {
                 relaunch = true;
                 relaunch_isdet = mediaidold & K_DET_MASK;
@@ -1751,5 +1844,7 @@ __global__ void mcx_rng_dump(const KArgs a) {
 #undef KP_NPHASE_GT2
 #undef KP_MEDIAFORMAT
 #undef KP_SHARING
+#undef KP_RFFWD
+#undef KP_RFREPLAY
 
 #endif

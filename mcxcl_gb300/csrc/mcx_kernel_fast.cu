@@ -40,6 +40,13 @@ static void* kshape(bool det, bool refl, bool wagg, bool o3) {
     return refl ? kfun<false, true, false, COMMON>(o3) : kfun<false, false, false, COMMON>(o3);
 }
 
+/* the RF (frequency-domain) transport: complex photon weights, 3 blocks/SM,
+   direct deposits */
+template <bool DET, bool REFL>
+static void* krf() {
+    return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, false, true>;
+}
+
 /* volumes in the less common encodings: 3 blocks/SM, direct deposits */
 template <bool DET, bool REFL>
 static void* kxmedia() {
@@ -48,6 +55,9 @@ static void* kxmedia() {
 
 static void* select(int flags) {
     const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    if (flags & LF_RF) {
+        return det ? (refl ? krf<true, true>() : krf<true, false>()) : (refl ? krf<false, true>() : krf<false, false>());
+    }
     if (flags & LF_XMEDIA) {
         return det ? (refl ? kxmedia<true, true>() : kxmedia<true, false>())
                    : (refl ? kxmedia<false, true>() : kxmedia<false, false>());

@@ -4,7 +4,7 @@
  * Plain C so the C host driver and the CUDA translation units share one
  * definition.  Field meanings follow the reference's MCXParam
  * (src/mcx_host.h:106-166); fields the GB300 kernel does not read (cache box,
- * polarisation, RF, trajectory debug) are left out, and a few are added for
+ * polarisation, trajectory debug) are left out, and a few are added for
  * the persistent work queue and the uint8 volume.
  */
 #ifndef MCX_KPARAMS_H
@@ -68,7 +68,7 @@ typedef struct mcxg_kparams {
     uint32_t siteshift;            /* scattering-site replay deposits read photon k+siteshift (the reference: 1) */
     uint32_t dimy, dimz;           /* voxel counts along y and z */
     uint32_t srcnum;               /* patterns sharing each photon (pattern sources), else 1 */
-    uint32_t reserved;
+    float omega;                   /* modulation angular frequency (rad/s); > 0 without replay: RF transport */
 } mcxg_kparams;
 
 /* One simulation of a batch: its parameter block (nthread = its reference

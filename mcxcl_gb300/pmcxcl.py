@@ -33,7 +33,7 @@ _SCALARS_INT = ["nphoton", "nblocksize", "nthread", "maxdetphoton", "maxgate", "
                 "gscatter", "srcnum", "srcid", "isatomic", "internalsrc", "issavedet", "exactmath",
                 "savethreadenergy", "autotune"]
 _SCALARS_BOOL = ["issaveexit", "ismomentum", "isspecular", "issave2pt", "issaveseed"]
-_SCALARS_FLOAT = ["tstart", "tstep", "tend", "minenergy", "unitinmm"]
+_SCALARS_FLOAT = ["tstart", "tstep", "tend", "minenergy", "unitinmm", "omega"]
 
 
 class MCXError(RuntimeError):
@@ -372,9 +372,20 @@ def _outputs(cfg, C):
         ndetblk = C.detnum if (C.seed == SEED_FROM_FILE and C.replaydet == -1) else 1
         # photon sharing: one field per pattern, patterns innermost (src/pmcxcl.cpp:1330)
         nshare = C.srcnum if (C.srcnum > 1 and ord(C.srctype) in (5, 15)) else 1
+        # complex fields (src/pmcxcl.cpp:1339-1341, 1388-1409): the RF transport
+        # returns complex64, the rf / rfmus replay outputs a trailing axis of 2
+        replay = C.seed == SEED_FROM_FILE
+        rffwd = C.omega > 0 and not replay
+        rfrep = replay and ord(C.outputtype) in (OUTPUTTYPES.index("rf") - 2, OUTPUTTYPES.index("rfmus") - 2)
+        comps = 2 if (rffwd or rfrep) else 1
         n = C.dim.x * C.dim.y * C.dim.z * gates * nsrc * ndetblk * nshare
-        f = np.ctypeslib.as_array(C.exportfield, shape=(n,)).copy()
-        if nshare > 1:
+        f = np.ctypeslib.as_array(C.exportfield, shape=(n * comps,)).copy()
+        if rffwd:
+            f = f[:n] + 1j * f[n:]
+            f = f.astype(np.complex64)
+        if rfrep:
+            dims = (C.dim.x, C.dim.y, C.dim.z, gates) + ((ndetblk,) if ndetblk > 1 else (1,)) + (2,)
+        elif nshare > 1:
             dims = (nshare * C.dim.x, C.dim.y, C.dim.z, gates)
         elif nsrc > 1:
             dims = (C.dim.x, C.dim.y, C.dim.z, gates, ndetblk, nsrc)
@@ -387,8 +398,9 @@ def _outputs(cfg, C):
             vol = np.ctypeslib.as_array(C.vol, shape=(C.dim.x * C.dim.y * C.dim.z,))
             mask = (vol & 0x7FFFFFFF).reshape((1, C.dim.x, C.dim.y, C.dim.z), order="F") != 0
             fl = flux.reshape((nshare, C.dim.x, C.dim.y, C.dim.z, -1), order="F")
-            dref = np.where(mask[..., None], 0.0, -fl).astype(np.float32).reshape(dims, order="F")
-            flux = np.where(mask[..., None], fl, 0.0).astype(np.float32).reshape(dims, order="F")
+            dt = np.complex64 if np.iscomplexobj(fl) else np.float32
+            dref = np.where(mask[..., None], 0.0, -fl).astype(dt).reshape(dims, order="F")
+            flux = np.where(mask[..., None], fl, 0.0).astype(dt).reshape(dims, order="F")
             out["dref"] = dref
         out["flux"] = flux
         out["stat"] = {

@@ -58,7 +58,7 @@ EXACT_CASES = ["pencil_gates", "isotropic", "cone", "gaussian", "planar", "fouri
                "pattern", "pattern3d", "focus", "lambert", "noreflect", "cyclic", "facedet", "roulette",
                "unitinmm", "gscatter", "outside_src_specular", "multisrc", "multisrc_id", "energy_out",
                "fluence_out", "invcdf", "angleinvcdf", "muafloat", "asf2h", "labelhalf", "asgnbyte", "asshort",
-               "pattern_share", "pattern3d_share"]
+               "pattern_share", "pattern3d_share", "rf_forward", "rf_roulette"]
 
 
 @pytest.mark.parametrize("name", EXACT_CASES)
@@ -94,6 +94,8 @@ def test_exact_kernel_matches_oracle_bits(gpu, O, name):
     else:
         raw = np.asarray(r["field_raw"]) * r["stat"]["normalizer"]
     flux = g["flux"] - g["dref"] if "dref" in g else g["flux"]
+    if np.iscomplexobj(flux):      # RF transport: real part, then imaginary part
+        flux = np.concatenate([flux.real.ravel(order="F"), flux.imag.ravel(order="F")])
     flux = flux.reshape(raw.shape, order="F")
     scale = max(np.abs(raw).max(), 1e-30)
     np.testing.assert_allclose(flux, raw, rtol=1e-4, atol=1e-6 * scale)

@@ -89,3 +89,43 @@ def test_head_fast_kernel_agrees_with_exact(gpu):
     assert abs(af - ae) < 0.005, (af, ae)
     df, de = f["stat"]["detected"], e["stat"]["detected"]
     assert abs(df - de) <= 4 * np.sqrt(de) + 0.01 * de, (df, de)
+
+
+def fddiffusion(mua, musp, n, omega, src, det):
+    """Frequency-domain form of the same dipole solution: the decay constant
+    sqrt(3 mua musp) becomes sqrt((mua + i omega n / c0) / D), the phase
+    convention of the RF transport's weight update exp(-(mua + i omega n /
+    c0) ds) (mcx_core.cl:2750-2760); zero internal reflection."""
+    D = 1.0 / (3.0 * (mua + musp))
+    zb = 2.0 * D
+    z0 = 1.0 / (musp + mua)
+    c0 = 299792458000.0                       # mm/s
+    k = np.sqrt((mua + 1j * omega * n / c0) / D)
+    src = np.asarray(src, float)
+    det = np.atleast_2d(np.asarray(det, float))
+    r1 = np.linalg.norm(det - (src + [0, 0, z0]), axis=1)
+    r2 = np.linalg.norm(det - (src + [0, 0, -z0 - 2 * zb]), axis=1)
+    return 1.0 / (4 * np.pi * D) * (np.exp(-k * r1) / r1 - np.exp(-k * r2) / r2)
+
+
+def test_homogeneous_cube_rf_follows_fd_diffusion(gpu):
+    """The RF transport (omega > 0, complex photon weights) on the homogeneous
+    cube at 500 MHz: the complex fluence agrees in amplitude and phase with
+    the frequency-domain diffusion solution, away from the entry point."""
+    import mcxcl_gb300
+    omega = 2 * np.pi * 5e8
+    cfg = workloads.config(1)
+    cfg.update(nphoton=20000000, outputtype="fluence", omega=omega)
+    r = mcxcl_gb300.run(cfg)
+    phi = r["flux"][..., 0]
+    assert phi.dtype == np.complex64
+    src = np.array([29.0, 29.0, 0.0])
+    pts = np.array([(29, 29, z) for z in range(12, 20)] + [(x, 29, 8) for x in range(31, 42)])
+    mc = np.array([phi[tuple(p)] + phi[28 - (p[0] - 29) if p[0] != 29 else 28, p[1], p[2]] for p in pts]) / 2
+    fd = fddiffusion(0.005, 0.99, 1.37, omega, src, pts + 0.5)
+    ratio = mc / fd
+    assert np.all(np.abs(np.abs(ratio) - 1) < 0.08), np.round(np.abs(ratio), 3)
+    assert np.all(np.abs(np.angle(ratio)) < 0.08), np.round(np.angle(ratio), 3)
+    # the phase lag grows with depth below the source
+    lag = -np.angle(mc[:8])
+    assert np.all(np.diff(lag) > 0) and lag[-1] > 1.0, np.round(lag, 3)

@@ -134,7 +134,7 @@ def test_host_replay_errors(oracle_mod):
 # ---------------------------------------------------------------- GPU
 
 REPLAY_GPU = [("jacobian", 0), ("jacobian", -1), ("jacobian", 1), ("nscat", 0), ("wm", -1), ("wltof", 0),
-              ("wptof", 0), ("flux", 0)]
+              ("wptof", 0), ("flux", 0), ("rf", 0), ("rf", -1), ("rfmus", 0)]
 
 
 @pytest.fixture(scope="module")
@@ -154,7 +154,11 @@ def test_exact_replay_matches_oracle(gpu, oracle_mod, ot, rd, nthread):
     O = oracle_mod
     base = cases.small_two_media(nphoton=6000)
     b = O.run(base, nthread=256, core=256, mathmode=O.MATH_PMATH)
-    cfg = cases.replay_cfg(base, b["detp"], b["seeds"], outputtype=ot, replaydet=rd)
+    # the rf outputs are phased at 100 MHz; the oracle's FP64 mode keeps their
+    # launch phase where the deposits read it (the reference's float path, pinned
+    # above, stores it elsewhere and comes out zero)
+    cfg = cases.replay_cfg(base, b["detp"], b["seeds"], outputtype=ot, replaydet=rd,
+                           omega=2 * np.pi * 1e8 if ot.startswith("rf") else 0.0)
     g = mcxcl_gb300.run(dict(cfg, autopilot=0, nthread=nthread, nblocksize=16, exactmath=1, savethreadenergy=1))
     r = O.run(cfg, nthread=nthread, core=gpu["core"], mathmode=O.MATH_PMATH, fieldmode=O.FIELD_DOUBLE)
     assert np.array_equal(g["threadenergy"].view(np.uint32), np.asarray(r["energy"], np.float32).view(np.uint32))
