@@ -249,7 +249,7 @@ struct mcxg_session* mcx_prepare_simulation(Config* cfg);
    addition, no counterpart in the reference (one simulation per
    mcx_run_simulation call).  Each simulation gets ceil(nphoton /
    photons_per_thread) reference threads (0: ceil(nphoton / 2^18) photons a
-   thread, clamped to 1..64) with seeds derived from its cfg.seed; flags: MCXG_GRAPH, MCXG_AGG.  Outputs go to each Config as
+   thread, clamped to 1..16) with seeds derived from its cfg.seed; flags: MCXG_GRAPH, MCXG_AGG.  Outputs go to each Config as
    mcx_run_simulation's do; an error is reported on cfgs[0].  Label volumes
    of at most 128 labels, one respin, no detectors, replay, extra sources,
    patterns or phase tables. */

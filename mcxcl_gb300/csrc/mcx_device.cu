@@ -1257,13 +1257,15 @@ int mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
         return MCXG_ERR_STATE;
     }
     MCXG_TRY(cudaSetDevice(s->device));
-    bool refl = false;
+    bool refl = false, common = true;
     for (const mcxg_simdesc& d : s->h_sims) {
         refl = refl || d.kp.dorefl_compiled;
+        common = common && !d.kp.is2d && d.kp.mediaformat <= 4 && d.kp.nphase <= 2;
     }
     const bool agg = (flags & MCXG_AGG) != 0;
     const int bpsm_req = s->bpsm_req ? s->bpsm_req : 3;
-    int lflags = (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) | (bpsm_req == 3 ? mcxg::LF_OCC3 : 0);
+    int lflags = (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) | (bpsm_req == 3 ? mcxg::LF_OCC3 : 0) |
+                 (common && !(flags & MCXG_GENERAL) ? mcxg::LF_COMMON : 0);
     int block = s->block_req ? s->block_req : 256;
     int occ = 0;
     MCXG_TRY(mcxg::batch_occupancy(lflags, block, (size_t)block * 32, &occ));

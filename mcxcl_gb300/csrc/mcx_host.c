@@ -1446,15 +1446,16 @@ void mcx_savedetphoton(float* ppath, void* seeds, int count, int doappend, Confi
 }
 
 /* Reference threads of one batch simulation: ceil(nphoton / ppt), and with
-   ppt 0 a photon count per thread of ceil(nphoton / 2^18) clamped to 1..64.
+   ppt 0 a photon count per thread of ceil(nphoton / 2^18) clamped to 1..16.
    The automatic count gives every simulation at least twice as many threads
    as a GB300 keeps resident (152 SMs x 3 x 256), so the resident threads work
    on one or two simulations at a time and a warp's lanes read one
-   descriptor, and it keeps the last threads of a wave short. */
+   descriptor, and the cap of 16 photons keeps the last threads of a wave
+   short (as the single-simulation autopilot does). */
 static size_t batch_threads(size_t nphoton, unsigned int ppt) {
     if (!ppt) {
         size_t p = (nphoton + (1u << 18) - 1) >> 18;
-        ppt = (unsigned int)(p < 1 ? 1 : (p > 64 ? 64 : p));
+        ppt = (unsigned int)(p < 1 ? 1 : (p > 16 ? 16 : p));
     }
     return (nphoton + ppt - 1) / ppt;
 }

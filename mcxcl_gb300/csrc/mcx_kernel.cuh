@@ -125,7 +125,7 @@ extern __shared__ float4 mcxg_smem[];
 /* --------------------------------------------------------- parameter source
  *
  * Where the kernel reads its parameters.  One simulation keeps them in
- * constant memory (ConstPS).  A batch of simulations (BatchPS) keeps one
+ * constant memory (ConstPS).  A batch of simulations (BatchPST) keeps one
  * descriptor per simulation in constant memory -- the parameter block, the
  * simulation's offsets into the batch's volume, field and reference-thread
  * numbering, its seed and property rows -- and each thread follows the
@@ -169,10 +169,11 @@ struct ConstPST {
 
 using ConstPS = ConstPST<false>;
 
-struct BatchPS {
+template <bool COMMON>
+struct BatchPST {
     static constexpr bool kBatch = true;
     static constexpr bool kXMedia = false;
-    static constexpr bool kCommon = false;
+    static constexpr bool kCommon = COMMON;   /* every simulation of the wave is 3-D */
     unsigned int sid;              /* the simulation of this wave the thread is running */
     unsigned int lo;               /* low-plane offset: the batch's total field length */
     __device__ __forceinline__ void init(const KArgs& a) {
@@ -1335,7 +1336,8 @@ __device__ __forceinline__ bool claim_vt(const KArgs& a, ConstPST<X, C>&, unsign
    left only once its counter has run out, so every reference thread is
    claimed; `open` (the shared counter word) is one past the highest
    simulation found exhausted. */
-__device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPS& ps, unsigned int& vt) {
+template <bool C>
+__device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPST<C>& ps, unsigned int& vt) {
     for (;;) {
         if (ps.sid < a.nsim) {
             const unsigned int v = atomicAdd(a.simctr + ps.sid, 1u);
@@ -1358,7 +1360,7 @@ template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool
           bool COMMON = false, bool RF = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
-    typedef typename std::conditional<BATCH, BatchPS, ConstPST<XMEDIA, COMMON>>::type PS;
+    typedef typename std::conditional<BATCH, BatchPST<COMMON>, ConstPST<XMEDIA, COMMON>>::type PS;
     PS ps;
     ps.init(a);
     Shared S;

@@ -21,18 +21,25 @@ cudaError_t batch_wave_upload(const mcxg_simdesc* d_descs, unsigned int n, cudaS
     return cudaMemcpyToSymbolAsync(c_sims, d_descs, sizeof(mcxg_simdesc) * n, 0, cudaMemcpyDeviceToDevice, st);
 }
 
-template <bool REFL, bool WAGG>
+/* COMMON: every simulation of the batch is 3-D (batches already take only
+   label volumes and the Henyey-Greenstein phase function) */
+template <bool REFL, bool WAGG, bool COMMON>
 static void* kbatch(bool occ3) {
-    return occ3 ? (void*)mcx_transport<false, false, REFL, WAGG, false, 3, true>
-           : (void*)mcx_transport<false, false, REFL, WAGG, false, 2, true>;
+    return occ3 ? (void*)mcx_transport<false, false, REFL, WAGG, false, 3, true, false, COMMON>
+           : (void*)mcx_transport<false, false, REFL, WAGG, false, 2, true, false, COMMON>;
+}
+
+template <bool COMMON>
+static void* kshape(bool refl, bool wagg, bool o3) {
+    if (wagg) {
+        return refl ? kbatch<true, true, COMMON>(o3) : kbatch<false, true, COMMON>(o3);
+    }
+    return refl ? kbatch<true, false, COMMON>(o3) : kbatch<false, false, COMMON>(o3);
 }
 
 static void* select(int flags) {
     const bool refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
-    if (wagg) {
-        return refl ? kbatch<true, true>(o3) : kbatch<false, true>(o3);
-    }
-    return refl ? kbatch<true, false>(o3) : kbatch<false, false>(o3);
+    return (flags & LF_COMMON) ? kshape<true>(refl, wagg, o3) : kshape<false>(refl, wagg, o3);
 }
 
 cudaError_t batch_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st) {

@@ -333,7 +333,7 @@ def run_batch(cfgs, photons_per_thread=0, graph=False, aggregate=False):
     cfgs: a list of run() dictionaries (label volumes, no detectors).  Returns
     the list of their output dictionaries, as run() would give one by one.
     photons_per_thread sets how many photons each reference thread (RNG
-    stream) runs (0: ceil(nphoton / 2**18), clamped to 1..64); graph=True captures the launch as a CUDA graph."""
+    stream) runs (0: ceil(nphoton / 2**18), clamped to 1..16); graph=True captures the launch as a CUDA graph."""
     L = _lib.load()
     Cs = [Config() for _ in cfgs]
     try:
