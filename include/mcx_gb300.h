@@ -76,6 +76,8 @@ enum TMCXParent {mpStandalone, mpMATLAB, mpPython};
 #define SAVE_PEXIT(a)  ((a) >> 4 & 0x1)
 #define SAVE_VEXIT(a)  ((a) >> 5 & 0x1)
 #define SAVE_W0(a)     ((a) >> 6 & 0x1)
+#define SAVE_IQUV(a)   ((a) >> 7 & 0x1)
+#define MCX_NANGLES    181              /* polar angles of the Mueller tables (src/mcx_const.h:67) */
 
 typedef struct { float x, y, z, w; } mcx_float4;
 typedef struct { unsigned int x, y, z, w; } mcx_uint4;
@@ -84,6 +86,15 @@ typedef struct { unsigned int x, y, z, w; } mcx_uint4;
 typedef struct MCXMedium {
     float mua, mus, g, n;
 } Medium;
+
+/* src/mcx_utils.h:88-94: the scatterers of one medium of a polarised run */
+typedef struct MCXPolarizeMedium {
+    float mua;                    /* background absorption, 1/mm */
+    float r;                      /* sphere radius, micron */
+    float rho;                    /* sphere number density, 1/micron^3 */
+    float nsph;                   /* sphere refractive index */
+    float nmed;                   /* background refractive index */
+} POLMedium;
 
 /* src/mcx_utils.h:100-105: one additional source */
 typedef struct MCXExtraSource {
@@ -196,6 +207,14 @@ typedef struct MCXConfig {
                                      (the reference reads the next photon's, mcx_core.cl:2571) */
     float omega;                  /* modulation angular frequency 2 pi f (rad/s), mcx_utils.h:231: > 0 runs the
                                      frequency-domain (RF) transport, or phases the rf/rfmus replay outputs */
+    /* polarised transport (mcx_utils.h:174-194, 232): one POLMedium per label 1..polmedianum (malloc'd,
+       freed by mcx_clearcfg), the wavelength in nm, the launch Stokes vector; mcx_validatecfg fills
+       smatrix (polmedianum x MCX_NANGLES {S11, S12, S33, S34}) and the labels' mus and g from Mie theory */
+    POLMedium* polprop;
+    unsigned int polmedianum;
+    float lambda;
+    mcx_float4 srciquv;
+    mcx_float4* smatrix;
     int errorcode;                /* last error in library mode */
     char errormsg[256];
 } Config;
@@ -236,6 +255,12 @@ int  mcx_last_error(const Config* cfg, const char** msg);
 /* Number of floats in one detected-photon record for this Config. */
 unsigned int mcx_detreclen(const Config* cfg);
 const char* mcx_version(void);
+/* Mie scattering of a sphere of size parameter x = 2 pi r n_med / lambda and
+   real relative index mrel = n_sph / n_med: the Mueller elements {S11, S12,
+   S33, S34} at the 181 polar angles pi i / 180 (181 x 4 floats), the
+   scattering efficiency and the anisotropy (the reference's Mie,
+   src/mcx_mie.cpp:91).  0 on success. */
+int mcx_mie(double x, double mrel, float* smatrix, double* qsca, double* g);
 /* The n words rand() returns after srand(seed) in glibc (the reference's
    per-thread seed words), without the C library's per-call lock. */
 void mcx_rand_words(unsigned int seed, uint32_t* out, size_t n);
@@ -363,6 +388,10 @@ int  mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, ui
 /* As mcxg_get_field with element i scaled by scales[i % nsrc]: the per-pattern
    normalisation of photon sharing, whose field interleaves the patterns. */
 int  mcxg_get_field_interleaved(mcxg_session* s, float* out, const double* scales, uint32_t nsrc);
+/* Polarised transport: nmedia x MCX_NANGLES Mueller rows {S11, S12, S33, S34}
+   for labels 1..nmedia and the launch Stokes vector s0[4]; nmedia 0 turns it
+   off.  Kept until the next call or mcxg_set_problem. */
+int  mcxg_set_polarization(mcxg_session* s, const float* smatrix, uint32_t nmedia, const float* s0);
 /* Adjoint Jacobians from the normalised float field of the last
    mcxg_get_field: fieldlen = nx ny nz maxgate (ns + nd), the first ns gate
    blocks the sources, the next nd the detectors run as sources.  kind 0:

@@ -89,7 +89,10 @@ class Config(ctypes.Structure):
         ("exportenergy", ctypes.POINTER(ctypes.c_float)), ("savethreadenergy", ctypes.c_int),
         ("autotune", ctypes.c_int), ("savedetweight", ctypes.c_int),
         ("exportdetweight", ctypes.POINTER(ctypes.c_float)), ("replaysiteown", ctypes.c_int),
-        ("omega", ctypes.c_float), ("errorcode", ctypes.c_int),
+        ("omega", ctypes.c_float),
+        ("polprop", ctypes.POINTER(ctypes.c_float)), ("polmedianum", ctypes.c_uint), ("lambda_", ctypes.c_float),
+        ("srciquv", Float4), ("smatrix", ctypes.POINTER(Float4)),
+        ("errorcode", ctypes.c_int),
         ("errormsg", ctypes.c_char * 256),
     ]
 
@@ -110,7 +113,7 @@ EXPORTS = [
     "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_launch", "mcxg_simulate",
     "mcxg_get_energy", "mcxg_get_thread_energy", "mcxg_get_field", "mcxg_get_field_f64", "mcxg_get_detected",
     "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc", "mcxg_autotune",
-    "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_field_interleaved", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",
+    "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_field_interleaved", "mcxg_set_polarization", "mcx_mie", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",
     "mcxg_batch_simulate", "mcxg_batch_get_energy", "mcxg_batch_get_field", "mcx_savedetphoton",
     "mcxg_adjoint",
 ]

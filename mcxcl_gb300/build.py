@@ -55,12 +55,13 @@ def build(force=False, verbose=False):
         objs.append(obj)
         if force or _stale(obj, [src] + hdeps):
             jobs.append([nvcc] + NVCC_COMMON + flags + ["-c", src, "-o", obj])
-    csrc = os.path.join(CSRC, "mcx_host.c")
-    cobj = os.path.join(BUILD, "mcx_host.o")
-    objs.append(cobj)
-    if force or _stale(cobj, [csrc] + hdeps):
-        jobs.append([os.environ.get("CC", "gcc"), "-std=gnu11", "-O2", "-fPIC", "-Wall", "-I" + CSRC,
-                     "-I" + INCLUDE, "-c", csrc, "-o", cobj])
+    for cunit in ("mcx_host.c", "mcx_mie.c"):
+        csrc = os.path.join(CSRC, cunit)
+        cobj = os.path.join(BUILD, cunit.replace(".c", ".o"))
+        objs.append(cobj)
+        if force or _stale(cobj, [csrc] + hdeps):
+            jobs.append([os.environ.get("CC", "gcc"), "-std=gnu11", "-O2", "-fPIC", "-Wall", "-I" + CSRC,
+                         "-I" + INCLUDE, "-c", csrc, "-o", cobj])
     procs = []
     for cmd in jobs:
         if verbose:

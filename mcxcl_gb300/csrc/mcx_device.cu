@@ -86,6 +86,10 @@ struct mcxg_session {
     unsigned long long* d_simvt = nullptr;
     size_t simvt_cap = 0;
     unsigned int* d_simctr = nullptr;   /* per-simulation reference-thread counters */
+    float4* d_smatrix = nullptr;        /* polarised transport: Mueller rows, 181 per medium */
+    size_t smatrix_cap = 0;
+    uint32_t npol = 0;
+    float4 pol_s0 = {1.f, 0.f, 0.f, 0.f};
     size_t simctr_cap = 0;
     uint8_t* d_bmedia = nullptr;
     size_t bmedia_cap = 0;
@@ -530,7 +534,7 @@ int mcxg_destroy(mcxg_session* s) {
     void* bufs[] = {s->d_media, s->d_prop, s->d_tables, s->d_pattern, s->d_seeds, s->d_field, s->d_energy,
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
                     s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw,
-                    s->d_sims, s->d_simvt, s->d_simctr, s->d_bmedia, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
+                    s->d_sims, s->d_simvt, s->d_simctr, s->d_smatrix, s->d_bmedia, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
                     s->d_adj};
     if (s->bgraph_exec) {
         cudaGraphExecDestroy(s->bgraph_exec);
@@ -626,6 +630,7 @@ int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, 
     s->h_srcx.assign(srcextra ? srcextra : prop, srcextra ? srcextra + 16 * kp.extrasrclen : prop);
     s->up_fast = s->up_exact = false;
     s->has_problem = true;
+    s->npol = 0;
     s->tuned = 0;
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
@@ -761,6 +766,9 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     a.srcpattern = s->d_pattern;
     a.seeds = s->d_seeds;
     a.field = s->d_field;
+    a.smatrix = s->d_smatrix;
+    a.s0 = s->pol_s0;
+    a.maxpol = s->npol;
     a.energy = s->d_energy;
     a.detp = s->d_detp;
     a.detseed = s->d_detseed;
@@ -781,20 +789,21 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
        the autotuner found it faster for this problem */
     const bool noagg = (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
     const bool rf = kp.omega > 0.f && !kp.replay;
+    const bool pol = s->npol > 0;
     const bool xmedia = !rf && kp.mediaformat > 4 && kp.mediaformat != 101;
     /* the instantiations that fix the common configuration's parameters */
-    const bool common = !rf && !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2 &&
+    const bool common = !rf && !pol && !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2 &&
                         kp.srcnum <= 1;
-    const int bpsm_sel = (xmedia || rf) ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
+    const int bpsm_sel = (xmedia || rf || pol) ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
                  (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
-                 (common ? mcxg::LF_COMMON : 0) | (rf ? mcxg::LF_RF : 0);
+                 (common ? mcxg::LF_COMMON : 0) | (rf ? mcxg::LF_RF : 0) | (pol ? mcxg::LF_POL : 0);
     int block = s->block_req ? s->block_req : 256;
     size_t smem = shared_bytes(kp, block);
     if (smem > s->info.sharedmem_per_block) {
         return MCXG_ERR_LIMIT;
     }
-    int bpsm = (s->bpsm_req && !xmedia && !rf) ? s->bpsm_req : (exact ? 2 : bpsm_sel);
+    int bpsm = (s->bpsm_req && !xmedia && !rf && !pol) ? s->bpsm_req : (exact ? 2 : bpsm_sel);
     if (!exact) {
         /* never more blocks than fit at once: a persistent grid must be resident */
         int occ = 0;
@@ -990,6 +999,25 @@ int mcxg_get_field_interleaved(mcxg_session* s, float* out, const double* scales
     s->out_valid = true;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_set_polarization(mcxg_session* s, const float* smatrix, uint32_t nmedia, const float* s0) {
+    if (!s || (nmedia && (!smatrix || !s0))) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    if (nmedia) {
+        int rc = ensure(&s->d_smatrix, &s->smatrix_cap, (size_t)nmedia * MCX_NANGLES);
+        if (rc) {
+            return rc;
+        }
+        MCXG_TRY(cudaMemcpyAsync(s->d_smatrix, smatrix, sizeof(float4) * nmedia * MCX_NANGLES, cudaMemcpyHostToDevice,
+                                 s->st));
+        MCXG_TRY(cudaStreamSynchronize(s->st));
+        s->pol_s0 = make_float4(s0[0], s0[1], s0[2], s0[3]);
+    }
+    s->npol = nmedia;
     return MCXG_OK;
 }
 

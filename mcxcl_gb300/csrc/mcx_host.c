@@ -123,6 +123,7 @@ void mcx_initcfg(Config* cfg) {
     cfg->his.respin = 1;
     cfg->parentid = mpStandalone;
     cfg->outputtype = otFlux;
+    cfg->srciquv.x = 1.f;          /* unpolarised launch (mcx_utils.c:338-339) */
 }
 
 void mcx_clearcfg(Config* cfg) {
@@ -148,6 +149,11 @@ void mcx_clearcfg(Config* cfg) {
     free(cfg->replay.tof);
     free(cfg->replay.detid);
     memset(&cfg->replay, 0, sizeof(cfg->replay));
+    free(cfg->polprop);
+    free(cfg->smatrix);
+    cfg->polprop = NULL;
+    cfg->smatrix = NULL;
+    cfg->polmedianum = 0;
     cfg->exportenergy = NULL;
     cfg->prop = NULL;
     cfg->detpos = NULL;
@@ -176,7 +182,7 @@ void mcx_normalize(float field[], float scale, int fieldlen, int option, int pid
 unsigned int mcx_detreclen(const Config* cfg) {
     unsigned int f = cfg->savedetflag;
     unsigned int partial = (cfg->medianum - 1) * (SAVE_NSCAT(f) + SAVE_PPATH(f) + SAVE_MOM(f));
-    return partial + SAVE_DETID(f) + 3 * (SAVE_PEXIT(f) + SAVE_VEXIT(f)) + SAVE_W0(f);
+    return partial + SAVE_DETID(f) + 3 * (SAVE_PEXIT(f) + SAVE_VEXIT(f)) + SAVE_W0(f) + 4 * SAVE_IQUV(f);
 }
 
 /* mcx_lookupindex (mcx_utils.c:5292-5305): face conditions "_ramc", detector flags "01" */
@@ -196,6 +202,40 @@ static int lookup_index(char* key, const char* table) {
 
 /* mcx_maskdet (mcx_utils.c:4085-4198): mark the boundary voxels within a
    detector's reach with the detector bit */
+/* mcx_prep_polarized (mcx_utils.c:1483-1519): the Mueller tables of each
+   label's scatterers from Mie theory, and the label's mua, n, mus and g from
+   them; a given mus (and g) sets the sphere density so that the label keeps
+   its mus (or its reduced mus), in the reference's float / double mix */
+static void prep_polarized(Config* cfg) {
+    free(cfg->smatrix);
+    cfg->smatrix = (mcx_float4*)malloc(sizeof(mcx_float4) * MCX_NANGLES * cfg->polmedianum);
+    if (!cfg->smatrix) {
+        MCX_ERROR(-2, "out of host memory");
+    }
+    for (unsigned int i = 0; i < cfg->polmedianum; i++) {
+        Medium* m = &cfg->prop[i + 1];
+        POLMedium* q = &cfg->polprop[i];
+        m->mua = q->mua;
+        m->n = q->nmed;
+        double qsca, g;
+        const double x = (double)(6.28318530717959f * q->r * q->nmed) / ((double)cfg->lambda * 1e-3);
+        const double A = (double)(3.1415926535897932f * q->r * q->r);
+        if (mcx_mie(x, (double)(q->nsph / q->nmed), (float*)(cfg->smatrix + i * MCX_NANGLES), &qsca, &g)) {
+            MCX_ERROR(-6, "invalid Mie scatterer (radius, indices and wavelength must be positive)");
+        }
+        if (m->mus > H_EPS) {
+            float target_mus = m->mus;
+            if (m->g < 1.f - H_EPS) {
+                const float target_musp = m->mus * (1.0f - m->g);
+                target_mus = (float)(target_musp / (1.0 - g));
+            }
+            q->rho = (float)(target_mus / qsca / A * 1e-3);
+        }
+        m->mus = (float)(qsca * A * q->rho * 1e3);
+        m->g = (float)g;
+    }
+}
+
 static void maskdet(Config* cfg) {
     unsigned int nx = cfg->dim.x, ny = cfg->dim.y, nz = cfg->dim.z;
     unsigned int dx = nx + 2, dy = ny + 2, dz = nz + 2;
@@ -341,6 +381,25 @@ static void preprocess(Config* cfg) {
     if ((cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D) && cfg->srcpattern == NULL) {
         MCX_ERROR(-4, "the 'srcpattern' field can not be empty when your 'srctype' is 'pattern'");
     }
+    if (cfg->polprop && cfg->polmedianum) {
+        /* mcx_preprocess (mcx_utils.c:1536-1549), before the unit scaling of the properties */
+        if (!(cfg->mediabyte <= 4)) {
+            MCX_ERROR(-1, "Unsupported media format for polarized simulation");
+        }
+        if (cfg->medianum != cfg->polmedianum + 1) {
+            MCX_ERROR(-6, "number of particle types does not match number of media");
+        }
+        if (cfg->lambda == 0.f) {
+            MCX_ERROR(-1, "you must specify light wavelength lambda to run polarized photon simulation");
+        }
+        if (cfg->omega > 0.f) {
+            MCX_ERROR(-6, "the polarised transport can not be combined with the frequency-domain transport");
+        }
+        if (cfg->dim.x == 1 || cfg->dim.y == 1 || cfg->dim.z == 1) {
+            MCX_ERROR(-6, "the polarised transport takes a 3-D domain in this build");
+        }
+        prep_polarized(cfg);
+    }
     if (cfg->steps.x != 1.f && cfg->unitinmm == 1.f) {
         cfg->unitinmm = cfg->steps.x;
     }
@@ -372,7 +431,7 @@ static void preprocess(Config* cfg) {
         MCX_ERROR(-1, "negative respin (photon divisions) is not supported by this build");
     }
     for (unsigned int i = 0; i < cfg->medianum; i++) {
-        if (cfg->prop[i].mus == 0.f) {
+        if (cfg->prop[i].mus == 0.f && !cfg->polmedianum) {
             cfg->prop[i].mus = H_EPS;
         }
     }
@@ -446,7 +505,13 @@ static void preprocess(Config* cfg) {
     if (cfg->issaveexit) {
         cfg->savedetflag |= 0x10 | 0x20;
     }
-    cfg->savedetflag &= ~0x80u;
+    if (cfg->polmedianum && cfg->polprop) {
+        /* a polarised run records partial paths, exit direction, initial weight
+           and the Stokes vector (mcx_utils.c:1777-1784) */
+        cfg->savedetflag |= 0x4 | 0x20 | 0x40 | 0x80;
+    } else {
+        cfg->savedetflag &= ~0x80u;
+    }
     if (cfg->issavedet && cfg->savedetflag == 0) {
         cfg->savedetflag = 0x5;
     }
@@ -1122,6 +1187,8 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     device_check(rc, "uploading the problem");
     device_check(mcxg_set_replay(s, cfg->replay.seed, cfg->replay.weight, cfg->replay.tof, cfg->replay.detid,
                                  replay ? (uint32_t)cfg->nphoton : 0u), "uploading the replay inputs");
+    device_check(mcxg_set_polarization(s, (const float*)cfg->smatrix, (cfg->polprop && cfg->smatrix) ? cfg->polmedianum : 0u,
+                                       &cfg->srciquv.x), "uploading the Mueller tables");
 
     /* seeds: srand(seed) then 4 rand() words per reference thread
        (mcx_host.cpp:696-700, 759-768); a replay launches every photon from its
@@ -1483,7 +1550,7 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
     for (int k = 0; k < n; k++) {
         Config* cfg = cfgs[k];
         if (!cfg || cfg->issavedet || cfg->seed == SEED_FROM_FILE || cfg->extrasrclen || cfg->nphase || cfg->nangle ||
-                cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D || cfg->mediabyte > 4 || cfg->omega > 0.f ||
+                cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D || cfg->mediabyte > 4 || cfg->omega > 0.f || cfg->polmedianum ||
                 cfg->medianum > MCXG_BATCH_MAXMEDIA || cfg->respin != 1 || cfg->issaveref || (cfg->debuglevel & 1)) {
             MCX_ERROR(-4, "a batch simulation takes label volumes of at most 4 property rows, one respin, and no "
                       "detectors, replay, extra sources, patterns, phase tables, saved reflectance or RF");
@@ -1655,7 +1722,8 @@ static const struct {
     MCX_FIELD(extrasrclen), MCX_FIELD(srcdata), MCX_FIELD(replay), MCX_FIELD(replaydet), MCX_FIELD(detdir), MCX_FIELD(exportjacob), MCX_FIELD(exactmath), MCX_FIELD(kernelms), MCX_FIELD(eventcount),
     MCX_FIELD(failedlaunch), MCX_FIELD(threadused), MCX_FIELD(exportenergy), MCX_FIELD(savethreadenergy),
     MCX_FIELD(autotune), MCX_FIELD(savedetweight), MCX_FIELD(exportdetweight), MCX_FIELD(replaysiteown), MCX_FIELD(omega),
-    MCX_FIELD(errorcode), MCX_FIELD(errormsg),
+    MCX_FIELD(polprop), MCX_FIELD(polmedianum), {"lambda_", offsetof(Config, lambda)}, MCX_FIELD(srciquv),
+    MCX_FIELD(smatrix), MCX_FIELD(errorcode), MCX_FIELD(errormsg),
 };
 
 size_t mcx_config_sizeof(void) {

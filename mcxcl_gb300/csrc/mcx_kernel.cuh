@@ -57,6 +57,8 @@ namespace {
 #define K_VERY_BIG       (1.f / K_EPS)
 #define K_ONE_PI         3.1415926535897932f
 #define K_TWO_PI         6.28318530717959f
+#define K_R_PI           0.318309886183791f
+#define K_NANGLES        181            /* polar angles of the Mueller tables */
 #define K_JUST_BELOW_ONE 0.9998f
 #define K_MAX_ACCUM      1000.f
 #define K_ROULETTE       10.f
@@ -81,6 +83,7 @@ enum { S_PENCIL, S_ISOTROPIC, S_CONE, S_GAUSSIAN, S_PLANAR, S_PATTERN, S_FOURIER
 #define SAVE_PEXIT(a) ((a) >> 4 & 0x1)
 #define SAVE_VEXIT(a) ((a) >> 5 & 0x1)
 #define SAVE_W0(a)    ((a) >> 6 & 0x1)
+#define SAVE_IQUV(a)  ((a) >> 7 & 0x1)
 
 /* status words written by the kernel */
 #define ST_FAILED_LAUNCH 0   /* reference threads whose launch failed (NO_LAUNCH) */
@@ -221,6 +224,8 @@ struct BatchPST {
    compiled with it; the rf / rfmus replay outputs in every one that replays */
 #define KP_RFFWD (RF && c_p.omega > 0.f && !c_p.replay)
 #define KP_RFREPLAY (c_p.replay && (c_p.outputtype == otRF || c_p.outputtype == otRFmus))
+/* polarised transport in the instantiations compiled with it */
+#define KP_POL (POL && a.maxpol > 0u)
 
 /* ------------------------------------------------------------------ math */
 
@@ -291,6 +296,7 @@ struct Photon {
     float w0, Lmove, pathlen, n1;
     Rng t;
     float wre, wim, w0re, w0im;    /* RF transport: complex weight now and at the last voxel change */
+    float4 st;                     /* polarised transport: Stokes vector {I, Q, U, V} */
 };
 
 template <class PS>
@@ -426,6 +432,66 @@ __device__ __forceinline__ void rotatevector(float4& v, float st, float ct, floa
         v.y *= r;
         v.z *= r;
     }
+}
+
+/* Polarised scattering angles (mcx_core.cl:2454-2469): theta uniform in cos,
+   phi uniform, accepted with the probability the Mueller matrix of the
+   medium gives the photon's Stokes vector at theta against the forward
+   direction; the draws are capped (a guard count records a cap hit) */
+template <bool EXACT>
+__device__ __forceinline__ void pol_angles(const KArgs& a, Photon& s, float& theta, float& phi) {
+    typedef Mth<EXACT> M;
+    const unsigned int ipol = K_NANGLES * (((s.mediaid & K_MED_MASK) - 1u) < a.maxpol ? (s.mediaid & K_MED_MASK) - 1u : 0u);
+    const float4 m0 = __ldg(a.smatrix + ipol);
+    unsigned int tries = 0;
+    for (;;) {
+        float sin2phi, cos2phi;
+        theta = M::acos(2.f * rnd(s.t) - 1.f);
+        phi = K_TWO_PI * rnd(s.t);
+        M::sincos(2.f * phi, &sin2phi, &cos2phi);
+        const float i0 = m0.x * s.st.x + m0.y * (s.st.y * cos2phi + s.st.z * sin2phi);
+        unsigned int ith = (unsigned int)(theta * K_NANGLES * (K_R_PI - K_EPS));
+        ith = ith < K_NANGLES ? ith : K_NANGLES - 1;
+        const float4 mt = __ldg(a.smatrix + ipol + ith);
+        const float i1 = mt.x * s.st.x + mt.y * (s.st.y * cos2phi + s.st.z * sin2phi);
+        if (!(rnd(s.t) * i0 >= i1)) {
+            return;
+        }
+        if (++tries >= K_CONE_CAP) {
+            atomicAdd(a.status + ST_GUARD, 1u);
+            return;
+        }
+    }
+}
+
+/* updatestokes (mcx_core.cl:792-835): rotate the Stokes vector into the
+   scattering plane, apply the Mueller matrix at theta, rotate back to the
+   new meridian plane and normalise to I = 1 */
+template <bool EXACT>
+__device__ __forceinline__ void update_stokes(const KArgs& a, Photon& s, float theta, float phi, const float3& u,
+                                              const float4& u2) {
+    typedef Mth<EXACT> M;
+    const float costheta = M::cos(theta);
+    float sin2phi, cos2phi;
+    M::sincos(2.f * phi, &sin2phi, &cos2phi);
+    float4 s2 = make_float4(s.st.x, s.st.y * cos2phi + s.st.z * sin2phi, -s.st.y * sin2phi + s.st.z * cos2phi, s.st.w);
+    const unsigned int imed = ((s.mediaid & K_MED_MASK) - 1u) < a.maxpol ? (s.mediaid & K_MED_MASK) - 1u : 0u;
+    unsigned int ith = (unsigned int)(theta * K_NANGLES * (K_R_PI - K_EPS));
+    ith = ith < K_NANGLES ? ith : K_NANGLES - 1;
+    const float4 m = __ldg(a.smatrix + K_NANGLES * imed + ith);
+    s.st.x = m.x * s2.x + m.y * s2.y;
+    s.st.y = m.y * s2.x + m.x * s2.y;
+    s.st.z = m.z * s2.z + m.w * s2.w;
+    s.st.w = -m.w * s2.z + m.z * s2.w;
+    float temp = (u2.z > -1.f && u2.z < 1.f) ? M::rsqrt((1.f - costheta * costheta) * (1.f - u2.z * u2.z)) : 0.f;
+    float cosi = (temp == 0.f) ? 0.f : (((phi > K_ONE_PI && phi < K_TWO_PI) ? 1.f : -1.f) * (u2.z * costheta - u.z) * temp);
+    cosi = fmaxf(-1.f, fminf(cosi, 1.f));
+    const float sini = M::sqrt(1.f - cosi * cosi);
+    const float cos22 = 2.f * cosi * cosi - 1.f;
+    const float sin22 = 2.f * sini * cosi;
+    s2 = make_float4(s.st.x, s.st.y * cos22 - s.st.z * sin22, s.st.y * sin22 + s.st.z * cos22, s.st.w);
+    temp = M::div(1.f, s2.x);
+    s.st = make_float4(1.f, s2.y * temp, s2.z * temp, s2.w * temp);
 }
 
 /* rotatevector2d, mcx_core.cl:1008-1023 */
@@ -585,7 +651,7 @@ __device__ __forceinline__ unsigned int finddetector(const PS& ps, const float4&
 }
 
 /* savedetphoton, mcx_core.cl:867-926 */
-template <class PS>
+template <bool POL, class PS>
 __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Photon& s, unsigned int isdet) {
     const mcxg_kparams& c_p = ps.p();
     int detid = (isdet == K_OUT_MIN) ? -1 : (int)finddetector(ps, s.p);
@@ -621,6 +687,12 @@ __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Pho
         }
         if (SAVE_W0(c_p.savedetflag)) {
             rec[k++] = ps.cold()->w0init;
+        }
+        if (POL && SAVE_IQUV(c_p.savedetflag)) {
+            rec[k++] = s.st.x;
+            rec[k++] = s.st.y;
+            rec[k++] = s.st.z;
+            rec[k++] = s.st.w;
         }
         if (a.detw) {
             a.detw[slot] = make_float2(s.p.w, s.f.y);
@@ -826,7 +898,7 @@ __device__ __forceinline__ void set_launch_voxel(const KArgs& a, const PS& ps, P
  * reference thread.  Returns 0 on launch, 1 when the thread's quota is done,
  * -1 when no launch position was found.
  */
-template <bool EXACT, bool DET, bool RF, class PS>
+template <bool EXACT, bool DET, bool RF, bool POL, class PS>
 __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Photon& s, unsigned int isdet,
                                unsigned int vt, unsigned long long* nfailed) {
     const mcxg_kparams& c_p = ps.p();
@@ -857,7 +929,7 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
             }
         }
         if (DET && c_p.savedet && (isdet & K_DET_MASK) == K_DET_MASK && s.mediaid == 0 && c_p.issaveref < 2) {
-            savedetphoton(a, ps, S, s, isdet);
+            savedetphoton<POL>(a, ps, S, s, isdet);
         }
     }
     if (DET) {
@@ -920,6 +992,9 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
         s.f.x = 0.f;
         s.f.y = 0.f;
         s.f.z = c_p.minaccumtime;
+        if (KP_POL) {
+            s.st = a.s0;      /* 1633-1638 */
+        }
         s.idx1d = __float_as_uint(lp2.z);
         s.mediaid = __float_as_uint(lp2.w);
         s.prop = make_float4(lpos.x, lpos.y, lpos.z, 0.f);
@@ -1357,7 +1432,7 @@ __device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPST<C>& ps, unsign
 }
 
 template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false,
-          bool COMMON = false, bool RF = false>
+          bool COMMON = false, bool RF = false, bool POL = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
     typedef typename std::conditional<BATCH, BatchPST<COMMON>, ConstPST<XMEDIA, COMMON>>::type PS;
@@ -1414,7 +1489,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             if (fresh && (unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
                 r = 1;
             } else {
-                r = launchnewphoton<EXACT, DET, RF>(a, ps, S, s, fresh ? 0u : relaunch_isdet, vt, &cnt_fail);
+                r = launchnewphoton<EXACT, DET, RF, POL>(a, ps, S, s, fresh ? 0u : relaunch_isdet, vt, &cnt_fail);
                 if (r && fresh) {
                     atomicAdd(a.status + ST_FAILED_LAUNCH, 1u);
                     r = 2;       /* NO_LAUNCH: the reference returns without writing energies */
@@ -1456,6 +1531,13 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 if (COUNT) {
                     cnt_scat++;
                 }
+                float polphi = 0.f;
+                if (KP_POL) {
+                    /* polarised: angles from the Mueller matrix (2454-2469) */
+                    pol_angles<EXACT>(a, s, theta, polphi);
+                    M::sincos(polphi, &sphi, &cphi);
+                    M::sincos(theta, &stheta, &ctheta);
+                } else {
                 if (!KP_IS2D) {
                     tmp0 = K_TWO_PI * rnd(s.t);
                     M::sincos(tmp0, &sphi, &cphi);
@@ -1504,6 +1586,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         }
                     }
                 }
+                }
                 if (DET && c_p.savedet && (s.mediaid & K_MED_MASK) - 1u < c_p.maxmedia) {
                     unsigned int med = (s.mediaid & K_MED_MASK) - 1;
                     if (SAVE_NSCAT(c_p.savedetflag)) {
@@ -1514,6 +1597,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         ps.pp(c_p.maxmedia * (SAVE_NSCAT(c_p.savedetflag) + SAVE_PPATH(c_p.savedetflag)) + med) += 1.f - ctheta;
                     }
                 }
+                const float3 olddir = make_float3(s.v.x, s.v.y, s.v.z);
                 if (KP_IS2D) {
                     rotatevector2d<EXACT>(s.v, (rnd(s.t) > 0.5f ? stheta : -stheta), ctheta, KP_IS2D);
                 } else {
@@ -1521,6 +1605,9 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 }
                 s.v.w += 1.f;
                 vdirty = true;
+                if (KP_POL) {
+                    update_stokes<EXACT>(a, s, theta, polphi, olddir, s.v);
+                }
                 if (c_p.replay && (c_p.outputtype == otWP || c_p.outputtype == otDCS || c_p.outputtype == otWPTOF ||
                                    c_p.outputtype == otRFmus)) {
                     replay_site_deposit(a, ps, S, s, vt, ctheta);
@@ -1848,5 +1935,6 @@ __global__ void mcx_rng_dump(const KArgs a) {
 #undef KP_SHARING
 #undef KP_RFFWD
 #undef KP_RFREPLAY
+#undef KP_POL
 
 #endif

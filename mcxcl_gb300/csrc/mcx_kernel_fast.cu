@@ -47,6 +47,13 @@ static void* krf() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, false, true>;
 }
 
+/* the polarised transport: Stokes vectors and Mueller tables, 3 blocks/SM,
+   direct deposits */
+template <bool DET, bool REFL>
+static void* kpol() {
+    return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, false, false, true>;
+}
+
 /* volumes in the less common encodings: 3 blocks/SM, direct deposits */
 template <bool DET, bool REFL>
 static void* kxmedia() {
@@ -55,6 +62,9 @@ static void* kxmedia() {
 
 static void* select(int flags) {
     const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    if (flags & LF_POL) {
+        return det ? (refl ? kpol<true, true>() : kpol<true, false>()) : (refl ? kpol<false, true>() : kpol<false, false>());
+    }
     if (flags & LF_RF) {
         return det ? (refl ? krf<true, true>() : krf<true, false>()) : (refl ? krf<false, true>() : krf<false, false>());
     }

@@ -40,10 +40,16 @@ struct KArgs {
     unsigned int* simctr;
     unsigned int nsim;
     unsigned int lo;
+    /* polarised transport: Mueller elements {S11, S12, S33, S34} at 181 polar
+       angles per scattering medium (maxpol media, labels 1..maxpol), and the
+       Stokes vector every photon starts with */
+    const float4* smatrix;
+    float4 s0;
+    unsigned int maxpol;
 };
 
 /* flag bits for the launch entries */
-enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128 };
+enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128, LF_POL = 256 };
 
 /* fast instantiation: hardware transcendental approximations */
 cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,

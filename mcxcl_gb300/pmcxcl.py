@@ -176,6 +176,23 @@ def parse_config(cfg, C):
         raise ValueError("the 'prop' field must have 4 columns (mua,mus,g,n)")
     C.medianum = p.shape[0]
     C.prop = _cbuf(p, Medium)
+    if "polprop" in cfg:
+        # scatterers of labels 1..N for the polarised transport: rows {mua, radius (um), number
+        # density (1/um^3), n_sphere, n_background} (src/pmcxcl.cpp:754-784)
+        pp = np.asarray(cfg["polprop"], np.float32)
+        if pp.ndim == 1:
+            pp = pp.reshape(1, -1)
+        if pp.ndim != 2 or pp.shape[1] != 5:
+            raise ValueError("the 'polprop' field must have 5 columns (mua, radius, rho, n_sph,n_bkg)")
+        C.polmedianum = pp.shape[0]
+        C.polprop = _cbuf(pp, ctypes.c_float)
+    if "lambda" in cfg:
+        C.lambda_ = float(cfg["lambda"])
+    if "srciquv" in cfg:
+        q = np.asarray(cfg["srciquv"], np.float32).ravel()
+        if q.size != 4:
+            raise ValueError("the 'srciquv' field must have 4 elements (I, Q, U, V)")
+        C.srciquv = Float4(*[float(v) for v in q])
     if "session" in cfg:
         C.session = str(cfg["session"]).encode()[:63]
     if "srctype" in cfg:
@@ -420,6 +437,17 @@ def _outputs(cfg, C):
         if C.exactmath:
             out["stat"]["eventcount"] = dict(zip(("step", "scatter", "launch", "reflect", "failed"),
                                                  [int(x) for x in C.eventcount]))
+    if C.polprop and C.polmedianum:
+        # the labels' properties after Mie theory set their mus and g, per mm (src/pmcxcl.cpp:1510-1521)
+        pr = np.ctypeslib.as_array(ctypes.cast(C.prop, ctypes.POINTER(ctypes.c_float)), shape=(C.medianum * 4,))
+        pr = pr.reshape(C.medianum, 4).copy()
+        pr[1:C.polmedianum + 1, :2] /= C.unitinmm
+        out["prop"] = pr.T
+        if C.smatrix:
+            # GB300 addition: the Mueller rows the run used, [polmedianum, 181, {S11, S12, S33, S34}]
+            sm = np.ctypeslib.as_array(ctypes.cast(C.smatrix, ctypes.POINTER(ctypes.c_float)),
+                                       shape=(C.polmedianum * 181 * 4,))
+            out["smatrix"] = sm.reshape(C.polmedianum, 181, 4).copy()
     if C.outputtype[0] >= 11 and C.exportjacob:
         # adjoint Jacobians by name, [Nx, Ny, Nz, sources x detectors] (src/pmcxcl.cpp:1413-1480)
         ot = C.outputtype[0]

@@ -61,6 +61,9 @@ enum { S_PENCIL, S_ISOTROPIC, S_CONE, S_GAUSSIAN, S_PLANAR, S_PATTERN, S_FOURIER
 #define SAVE_PEXIT(a) ((a) >> 4 & 0x1)
 #define SAVE_VEXIT(a) ((a) >> 5 & 0x1)
 #define SAVE_W0(a)    ((a) >> 6 & 0x1)
+#define SAVE_IQUV(a)  ((a) >> 7 & 0x1)
+#define K_NANGLES     181
+#define K_R_PI        0.318309886183791f
 
 typedef struct { float x, y, z, w; } f4;
 typedef struct { f4 pos, dir, p1, p2; } osrc;
@@ -90,6 +93,9 @@ typedef struct {
     int mathmode, variant, fieldmode;
     float omega;
     int rfmode;                   /* 0 real, 1 RF forward (complex weights), 2 RF replay output */
+    const f4* smatrix;            /* polarised transport: 181 Mueller rows per medium */
+    unsigned int maxpol;
+    f4 s0;
     unsigned int nthread;
     /* replay */
     int replay, replaydet, replaysiteown;
@@ -122,6 +128,7 @@ typedef struct {
     uint64_t photonseed[2];
     float* ppath;                 /* w0offset + srcnum (+ 2 for an RF replay) floats */
     float wre, wim, w0re, w0im;   /* RF forward: complex weight now and at the last voxel change */
+    f4 st;                        /* polarised transport: Stokes vector {I, Q, U, V} */
 } ostate;
 
 /* ---------------------------------------------------------------- helpers */
@@ -217,6 +224,41 @@ static inline void field_add_nospill(octx* X, size_t i, float w) {
     } else {
         X->fd[i >= c->dimlen[3] ? i - c->dimlen[3] : i] += (double)w;
     }
+}
+
+/* updatestokes (mcx_core.cl:792-835) with rotsphi (792-799) */
+static void update_stokes(const ocfg* c, ostate* s, float theta, float phi, const f4* u, const f4* u2) {
+    float costheta = m_cos(c, theta);
+    float sin2phi, cos2phi, temp, sini, cosi, sin22, cos22;
+    f4 s2, m;
+    uint32_t imedia, ithedeg;
+    m_sincos(c, 2.f * phi, &sin2phi, &cos2phi);
+    s2.x = s->st.x;
+    s2.y = s->st.y * cos2phi + s->st.z * sin2phi;
+    s2.z = -s->st.y * sin2phi + s->st.z * cos2phi;
+    s2.w = s->st.w;
+    imedia = K_NANGLES * ((s->mediaid & MED_MASK) - 1);
+    ithedeg = (uint32_t)(theta * K_NANGLES * (K_R_PI - K_EPS));
+    m = c->smatrix[imedia + ithedeg];
+    s->st.x = m.x * s2.x + m.y * s2.y;
+    s->st.y = m.y * s2.x + m.x * s2.y;
+    s->st.z = m.z * s2.z + m.w * s2.w;
+    s->st.w = -m.w * s2.z + m.z * s2.w;
+    temp = (u2->z > -1.f && u2->z < 1.f) ? m_rsqrt((1.f - costheta * costheta) * (1.f - u2->z * u2->z)) : 0.f;
+    cosi = (temp == 0.f) ? 0.f : (((phi > K_ONE_PI && phi < K_TWO_PI) ? 1.f : -1.f) * (u2->z * costheta - u->z) * temp);
+    cosi = fmaxf(-1.f, fminf(cosi, 1.f));
+    sini = sqrtf(1.f - cosi * cosi);
+    cos22 = 2.f * cosi * cosi - 1.f;
+    sin22 = 2.f * sini * cosi;
+    s2.x = s->st.x;
+    s2.y = s->st.y * cos22 - s->st.z * sin22;
+    s2.z = s->st.y * sin22 + s->st.z * cos22;
+    s2.w = s->st.w;
+    temp = 1.f / s2.x;
+    s->st.y = s2.y * temp;
+    s->st.z = s2.z * temp;
+    s->st.w = s2.w * temp;
+    s->st.x = 1.f;
 }
 
 /* a deposit with photon sharing (mcx_core.cl:1527-1538, 2902-2911, the
@@ -563,6 +605,12 @@ static void savedetphoton(octx* X, ostate* s, uint32_t isdet) {
             if (SAVE_W0(c->savedetflag)) {
                 X->detp[base++] = s->ppath[c->w0offset - 2];
             }
+            if (SAVE_IQUV(c->savedetflag)) {
+                X->detp[base++] = s->st.x;
+                X->detp[base++] = s->st.y;
+                X->detp[base++] = s->st.z;
+                X->detp[base++] = s->st.w;
+            }
         } else if (c->savedet == FILL_MAXDET) {
             X->detcount--;
         }
@@ -669,6 +717,9 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
         s->f.z = c->minaccumtime;
         s->idx1d = f2bits(ls->p2.z);
         s->mediaid = f2bits(ls->p2.w);
+        if (c->maxpol > 0) {
+            s->st = c->s0;    /* 1633-1638 */
+        }
         s->prop.x = ls->pos.x;
         s->prop.y = ls->pos.y;
         s->prop.z = ls->pos.z;
@@ -1106,6 +1157,22 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                 /* scattering, mcx_core.cl:2450-2560 */
                 float cphi = 1.f, sphi = 0.f, theta, stheta, ctheta, tmp0 = 0.f;
                 X->nscatter++;
+                if (c->maxpol > 0 && !c->is2d) {
+                    /* polarised angles by rejection against the Mueller matrix, 2454-2469 */
+                    const uint32_t ipol = K_NANGLES * ((s.mediaid & MED_MASK) - 1);
+                    float i0, i1, sin2phi, cos2phi;
+                    do {
+                        uint32_t ith;
+                        theta = m_acos(c, 2.f * rng_next(s.t) - 1.f);
+                        tmp0 = K_TWO_PI * rng_next(s.t);
+                        m_sincos(c, 2.f * tmp0, &sin2phi, &cos2phi);
+                        i0 = c->smatrix[ipol].x * s.st.x + c->smatrix[ipol].y * (s.st.y * cos2phi + s.st.z * sin2phi);
+                        ith = (uint32_t)(theta * K_NANGLES * (K_R_PI - K_EPS));
+                        i1 = c->smatrix[ipol + ith].x * s.st.x + c->smatrix[ipol + ith].y * (s.st.y * cos2phi + s.st.z * sin2phi);
+                    } while (rng_next(s.t) * i0 >= i1);
+                    m_sincos(c, tmp0, &sphi, &cphi);
+                    m_sincos(c, theta, &stheta, &ctheta);
+                } else {
                 if (!c->is2d) {
                     tmp0 = K_TWO_PI * rng_next(s.t);
                     m_sincos(c, tmp0, &sphi, &cphi);
@@ -1135,6 +1202,7 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                         m_sincos(c, theta, &stheta, &ctheta);
                     }
                 }
+                }
                 /* per-medium slots exist for labels 1..maxmedia; the reference indexes
                    outside them for label 0 and for label-half words */
                 if (SAVE_NSCAT(c->savedetflag) && (s.mediaid & MED_MASK) - 1u < c->maxmedia) {
@@ -1144,12 +1212,18 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                 if (SAVE_MOM(c->savedetflag) && (s.mediaid & MED_MASK) - 1u < c->maxmedia) {
                     s.ppath[c->maxmedia * (SAVE_NSCAT(c->savedetflag) + SAVE_PPATH(c->savedetflag)) + (s.mediaid & MED_MASK) - 1] += 1.f - ctheta;
                 }
-                if (c->is2d) {
-                    rotatevector2d(&s.v, (rng_next(s.t) > 0.5f ? stheta : -stheta), ctheta, c->is2d);
-                } else {
-                    rotatevector(c, &s.v, stheta, ctheta, sphi, cphi);
+                {
+                    const f4 olddir = s.v;
+                    if (c->is2d) {
+                        rotatevector2d(&s.v, (rng_next(s.t) > 0.5f ? stheta : -stheta), ctheta, c->is2d);
+                    } else {
+                        rotatevector(c, &s.v, stheta, ctheta, sphi, cphi);
+                    }
+                    s.v.w += 1.f;
+                    if (c->maxpol > 0) {
+                        update_stokes(c, &s, theta, tmp0, &olddir, &s.v);
+                    }
                 }
-                s.v.w += 1.f;
                 if (c->replay && (c->outputtype == otWP || c->outputtype == otDCS || c->outputtype == otWPTOF ||
                                   c->outputtype == otRFmus)) {
                     /* replay deposit at the scattering site, mcx_core.cl:2567-2604; the
@@ -1532,7 +1606,11 @@ static unsigned int savedetflag_eff(const mcxo_input* in) {
     if (in->issaveexit) {
         f |= 0x10 | 0x20;
     }
-    f &= ~0x80u;
+    if (in->polmedianum && in->smatrix) {
+        f |= 0x4 | 0x20 | 0x40 | 0x80;    /* mcx_utils.c:1777-1784 */
+    } else {
+        f &= ~0x80u;
+    }
     if (f == 0) {
         f = 0x5;
     }
@@ -1558,7 +1636,7 @@ static int savedet_eff(const mcxo_input* in) {
 unsigned int mcxo_reclen(const mcxo_input* in) {
     unsigned int f = savedetflag_eff(in);
     unsigned int partial = (in->medianum - 1) * (SAVE_NSCAT(f) + SAVE_PPATH(f) + SAVE_MOM(f));
-    return partial + SAVE_DETID(f) + 3 * (SAVE_PEXIT(f) + SAVE_VEXIT(f)) + SAVE_W0(f);
+    return partial + SAVE_DETID(f) + 3 * (SAVE_PEXIT(f) + SAVE_VEXIT(f)) + SAVE_W0(f) + 4 * SAVE_IQUV(f);
 }
 
 /* complex-weight transport (omega > 0, not a replay: mcx_host.cpp:473) or a
@@ -1794,6 +1872,9 @@ static int prepare(const mcxo_input* in, oprep* P) {
     c.nthread = in->nthread;
     c.omega = in->omega;
     c.rfmode = rf_mode(in);
+    c.smatrix = (const f4*)in->smatrix;
+    c.maxpol = in->smatrix ? in->polmedianum : 0u;
+    c.s0 = (f4){in->s0[0], in->s0[1], in->s0[2], in->s0[3]};
     if (is_replay(in)) {
         if (!in->replayseed || !in->replayweight || !in->replaytof || !in->replaydetid ||
                 (double)in->nreplay != in->nphoton) {
@@ -2315,6 +2396,11 @@ int mcxo_prepare_ref(const mcxo_input* in, mcxo_refprep* R) {
     R->fieldlen = P.fieldlen;
     R->omega = P.c.omega;
     R->rfmode = P.c.rfmode;
+    R->maxpolmedia = P.c.maxpol;
+    R->smatrix = in->smatrix;
+    for (i = 0; i < 4; i++) {
+        R->s0[i] = in->s0[i];
+    }
     return 0;
 }
 

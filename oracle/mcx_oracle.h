@@ -124,6 +124,13 @@ typedef struct mcxo_input {
        carries complex photon weights (RF forward), and the replay outputs
        'rf' and 'rfmus' are complex */
     float omega;
+
+    /* polarised transport: polmedianum x 181 Mueller rows {S11, S12, S33, S34}
+       (as mcx_prep_polarized leaves them in cfg->smatrix) and the launch
+       Stokes vector; prop must already hold the Mie-derived mus and g */
+    const float* smatrix;
+    unsigned int polmedianum;
+    float s0[4];
 } mcxo_input;
 
 typedef struct mcxo_stats {
@@ -194,6 +201,9 @@ typedef struct mcxo_refprep {
     unsigned int nvox, fieldlen;
     float omega;
     int rfmode;                 /* 0 real, 1 RF forward, 2 RF replay output */
+    unsigned int maxpolmedia;   /* polarised transport */
+    float s0[4];
+    const float* smatrix;
 } mcxo_refprep;
 
 int  mcxo_prepare_ref(const mcxo_input* in, mcxo_refprep* out);

@@ -60,6 +60,7 @@ class MCXOInput(ctypes.Structure):
         ("replayseed", ctypes.c_void_p), ("replayweight", ctypes.c_void_p), ("replaytof", ctypes.c_void_p),
         ("replaydetid", ctypes.c_void_p), ("nreplay", ctypes.c_uint), ("replaydet", ctypes.c_int),
         ("replaysiteown", ctypes.c_int), ("detweight_out", ctypes.c_void_p), ("omega", ctypes.c_float),
+        ("smatrix", ctypes.c_void_p), ("polmedianum", ctypes.c_uint), ("s0", ctypes.c_float * 4),
     ]
 
 
@@ -118,6 +119,17 @@ def reflib(pattern=False):
         _ref[path] = ctypes.CDLL(path)
         _ref[path].mcxref_run.restype = ctypes.c_int
     return _ref[path]
+
+
+def ref_mie(x, m):
+    """The reference's Mie routine (src/mcx_mie.cpp:91) from the harness:
+    (181 x 4 Mueller rows, qsca, g)."""
+    R = reflib()
+    sm = np.zeros((181, 4), np.float32)
+    q, g = ctypes.c_double(), ctypes.c_double()
+    R.mcxref_mie(ctypes.c_double(x), ctypes.c_double(m), sm.ctypes.data_as(ctypes.c_void_p), ctypes.byref(q),
+                 ctypes.byref(g))
+    return sm, q.value, g.value
 
 
 def _ptr(a):
@@ -197,6 +209,16 @@ def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT
         inp.srcpattern = _ptr(pat)
     inp.srcnum = int(cfg.get("srcnum", 1))
     inp.omega = float(cfg.get("omega", 0.0))
+    if cfg.get("smatrix") is not None:
+        # polarised transport: the Mueller rows of labels 1..N (N x 181 x 4) and the
+        # Mie-derived properties already in cfg["prop"]
+        sm = np.ascontiguousarray(np.asarray(cfg["smatrix"], np.float32).reshape(-1, 181, 4))
+        keep["smatrix"] = sm
+        inp.smatrix = _ptr(sm)
+        inp.polmedianum = sm.shape[0]
+    s0 = np.asarray(cfg.get("srciquv", [1, 0, 0, 0]), np.float32).ravel()
+    for i in range(4):
+        inp.s0[i] = float(s0[i])
 
     if "detpos" in cfg and np.asarray(cfg["detpos"]).size:
         det = np.ascontiguousarray(_rows(cfg["detpos"]))

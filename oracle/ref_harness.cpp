@@ -50,7 +50,7 @@ static void run_blocks(const mcxo_refprep& R, unsigned int nblock, unsigned int 
             mcx_main_loop<ispencil, isreflect, 1, 0, 0>(
                 media, field, genergy, seeds, detp, (const float4*)gprop, srcpattern, (const float4*)gdet,
                 &progress, detcount, rp.weight, rp.tof, rp.detid, gseed, nullptr, nullptr, (float*)invcdf, (float*)angleinvcdf,
-                (RandType*)sharedmem_raw, nullptr);
+                (RandType*)sharedmem_raw, (float4*)R.smatrix);
         }
     }
 }
@@ -115,6 +115,8 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     P.is2d = R.is2d;
     P.srcnum = R.srcnum;
     P.omega = R.omega;
+    P.maxpolmedia = R.maxpolmedia;
+    P.s0 = make_float4(R.s0[0], R.s0[1], R.s0[2], R.s0[3]);
     P.nphase = R.nphase;
     P.nphaselen = R.nphase + (R.nphase & 1);
     P.nangle = R.nangle;
@@ -208,4 +210,22 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     }
     mcxo_free_ref(&R);
     return 0;
+}
+
+/* The reference's Mie routine (src/mcx_mie.cpp:91), compiled from its own
+   source: Mueller rows {S11, S12, S33, S34} at the 181 angles the reference's
+   mcx_prep_polarized uses (mcx_utils.c:1484-1488), for pinning the polarised
+   transport and checking the library's own Mie series. */
+extern "C" void Mie(double x, double mx, const double* mu, float4* smatrix, double* qsca, double* g);
+
+extern "C" void mcx_error(const int id, const char* msg, const char* file, const int linenum) {
+    std::fprintf(stderr, "reference Mie error %d: %s\n", id, msg);
+}
+
+extern "C" void mcxref_mie(double x, double mrel, float* smatrix, double* qsca, double* g) {
+    std::vector<double> mu(181);
+    for (int i = 0; i < 181; i++) {
+        mu[i] = cos((double)(3.1415926535897932f * i / (181 - 1)));
+    }
+    Mie(x, mrel, mu.data(), (float4*)smatrix, qsca, g);
 }

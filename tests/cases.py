@@ -184,6 +184,51 @@ def pin_cases():
     return out
 
 
+def polarized(**kw):
+    """small_two_media with Mie scatterers in both labels (polystyrene spheres
+    of radius 0.5 and 0.3 um in water at 632.8 nm; prop's mus sets their
+    density), a linearly polarised launch and the Stokes vector recorded with
+    each detected photon."""
+    cfg = small_two_media(
+        prop=[[0, 0, 1, 1], [0.005, 1.0, 0.0, 1.33], [0.002, 2.0, 0.0, 1.33]],
+        polprop=[[0.005, 0.5, 0.0, 1.59, 1.33], [0.002, 0.3, 0.0, 1.59, 1.33]],
+        **{"lambda": 632.8}, srciquv=[1.0, 1.0, 0.0, 0.0], isreflect=0)
+    cfg.update(kw)
+    return cfg
+
+
+def pol_inputs(cfg, mie):
+    """The Mueller rows and the labels' properties mcx_prep_polarized derives
+    (mcx_utils.c:1483-1519), in its float / double arithmetic; mie(x, m) gives
+    (181 x 4 rows, qsca, g).  Returns a copy of cfg with 'smatrix' and the
+    derived 'prop' for the oracle, which takes them as inputs."""
+    f32 = np.float32
+    prop = np.array(cfg["prop"], np.float32)
+    pol = np.array(cfg["polprop"], np.float32).reshape(-1, 5)
+    lam = f32(cfg["lambda"])
+    rows = []
+    for i, (mua, r, rho, nsph, nmed) in enumerate(pol):
+        m = prop[i + 1]
+        m[0] = mua
+        m[3] = nmed
+        x = float(f32(f32(6.28318530717959) * r * nmed)) / (float(lam) * 1e-3)
+        A = float(f32(f32(3.1415926535897932) * r * r))
+        sm, qsca, g = mie(x, float(f32(nsph / nmed)))
+        if m[1] > f32(1e-10):
+            target = f32(m[1])
+            if m[2] < f32(1.0) - f32(1e-10):
+                musp = f32(m[1] * (f32(1.0) - m[2]))
+                target = f32(float(musp) / (1.0 - g))
+            rho = f32(float(target) / qsca / A * 1e-3)
+        m[1] = f32(qsca * A * float(rho) * 1e3)
+        m[2] = f32(g)
+        rows.append(np.asarray(sm, np.float32).reshape(181, 4))
+    out = dict(cfg)
+    out["prop"] = prop
+    out["smatrix"] = np.stack(rows)
+    return out
+
+
 def replay_cfg(base, detp, seeds, **kw):
     """A replay of base's detected photons: detp [reclen, N] records and
     seeds [N, 2] uint64 (or [16, N] uint8) from a baseline run."""

@@ -62,6 +62,13 @@ def main():
         r = oracle.run_reference(cfg, nthread=nthread, core=nthread)
         out[name] = dict(summarize(r), nthread=nthread)
         print(name, out[name]["ndet"], out[name]["energy_tot"])
+    # polarised transport: Mueller rows and properties from the reference's own Mie
+    # routine, stored with the pin (the oracle takes them as inputs)
+    pcfg = cases.pol_inputs(cases.polarized(), oracle.ref_mie)
+    r = oracle.run_reference(pcfg, nthread=128, core=128)
+    out["polarized"] = dict(summarize(r), nthread=128, smatrix=pcfg["smatrix"].ravel().tolist(),
+                            prop=np.asarray(pcfg["prop"], np.float32).ravel().tolist())
+    print("polarized", out["polarized"]["ndet"], out["polarized"]["energy_tot"])
     for name, bkw, rkw, nthread in cases.REPLAY_PINS:
         base = cases.small_two_media(**bkw)
         b = oracle.run_reference(base, nthread=128, core=128)

@@ -231,3 +231,45 @@ def test_common_and_general_fast_kernels_agree(gpu):
     for u, v in ((g0, g1), (d0, d1)):
         m = v > 0.01 * v.max()
         assert np.all(np.abs(u[m] - v[m]) <= 0.02 * v[m]), np.abs(u[m] / v[m] - 1).max()
+
+
+def test_exact_kernel_polarized_matches_oracle_bits(gpu, O):
+    """Polarised transport on the GPU (Stokes vectors, Mueller-matrix
+    rejection sampling and update, the Stokes vector in the detected
+    records): with the Mueller rows and properties the library derived by Mie
+    theory, the exact kernel reproduces the oracle's per-thread energies and
+    records bit for bit, and its field to the atomics' order."""
+    cfg = cases.polarized(nphoton=20000)
+    nthread = 256
+    g = _gpu_run(cfg, nthread, exactmath=1, savethreadenergy=1)
+    assert g["smatrix"].shape == (2, 181, 4)
+    ocfg = dict(cfg, smatrix=g["smatrix"], prop=np.asarray(g["prop"], np.float32).T)
+    r = O.run(ocfg, nthread=nthread, core=gpu["core"], mathmode=O.MATH_PMATH, variant=O.VARIANT_OPENCL,
+              fieldmode=O.FIELD_DOUBLE)
+    assert np.array_equal(g["threadenergy"].view(np.uint32), np.asarray(r["energy"], np.float32).view(np.uint32))
+    assert g["stat"]["detected"] == r["stat"]["detected"] > 0
+    rg, _ = _sorted_records(g["detp"], None)
+    rc, _ = _sorted_records(r["detp"], None)
+    assert np.array_equal(rg, rc)
+    raw = np.asarray(r["field_raw"]) * r["stat"]["normalizer"]
+    flux = g["flux"].reshape(raw.shape, order="F")
+    np.testing.assert_allclose(flux, raw, rtol=1e-4, atol=1e-6 * max(np.abs(raw).max(), 1e-30))
+
+
+def test_fast_kernel_polarized_agrees_with_exact(gpu):
+    """The fast polarised instantiation against the exact one on the same
+    problem: absorbed fraction, detected count and the mean Stokes vector of
+    the detected photons (a linearly polarised launch keeps part of its Q)."""
+    import mcxcl_gb300
+    cfg = cases.polarized(nphoton=400000)
+    f = mcxcl_gb300.run(dict(cfg))
+    e = mcxcl_gb300.run(dict(cfg, exactmath=1))
+    for k in (f, e):
+        assert k["detp"].shape[0] == 18
+    af, ae = _absorbed(f), _absorbed(e)
+    assert abs(af - ae) < 0.01, (af, ae)
+    nf, ne = f["detp"].shape[1], e["detp"].shape[1]
+    assert abs(nf - ne) < 5 * np.sqrt(ne) + 5, (nf, ne)
+    qf, qe = f["detp"][14:18].mean(axis=1), e["detp"][14:18].mean(axis=1)
+    assert np.allclose(qf[0], 1.0) and np.allclose(qe[0], 1.0)
+    assert np.all(np.abs(qf[1:] - qe[1:]) < 0.05), (qf, qe)

@@ -115,3 +115,23 @@ def test_oracle_double_field_close_to_float(oracle_mod):
     b = O.run(cfg, nthread=128, core=128, fieldmode=O.FIELD_DOUBLE)
     np.testing.assert_allclose(a["field_raw"], b["field_raw"], rtol=2e-5, atol=1e-4)
     np.testing.assert_array_equal(a["energy"], b["energy"])
+
+
+@pytest.mark.skipif(platform.machine() not in ("x86_64", "AMD64"),
+                    reason="libm-mode digests were recorded with x86-64 glibc")
+def test_oracle_polarized_matches_reference_bits(oracle_mod):
+    """Polarised transport (mcx_core.cl:792-835, 2454-2469, 2550-2565): with the
+    Mueller rows and properties the reference's own Mie routine gave (stored
+    with the pin), the oracle reproduces the reference kernel's energies,
+    field, and detected records with their Stokes vectors bit for bit."""
+    O = oracle_mod
+    pin = PINS["polarized"]
+    cfg = dict(cases.polarized(), smatrix=np.asarray(pin["smatrix"], np.float32).reshape(-1, 181, 4),
+               prop=np.asarray(pin["prop"], np.float32).reshape(-1, 4))
+    r = O.run(cfg, nthread=pin["nthread"], core=pin["nthread"], mathmode=O.MATH_LIBM, variant=O.VARIANT_NVCC,
+              fieldmode=O.FIELD_FLOAT_SPILL)
+    assert _sha(np.asarray(r["energy"], np.float32).view(np.uint32)) == pin["energy_sha"]
+    field = np.asarray(r["field_raw"], np.float32)
+    assert _sha(np.asfortranarray(field).ravel(order="F").view(np.uint32)) == pin["field_sha"]
+    assert r["detp"].shape[1] == pin["ndet"] and r["detp"].shape[0] == 1 + 3 * 2 + 3 + 3 + 1 + 4
+    assert _sha(np.asarray(r["detp"], np.float32).view(np.uint32)) == pin["detp_sha"]
