@@ -12,10 +12,12 @@ becomes one 32-bit word (x fastest) that the transport kernel decodes
 | float32 [3,Nx,Ny,Nz] | MEDIA_LABEL_HALF (99) | label \\| property index << 14 \\| half(value) << 16 |
 | uint8/int8 [4,Nx,Ny,Nz] | MEDIA_ASGN_BYTE (103) | four bytes: mua, mus, g, n between prop rows 1 and 2 |
 | int16 [2,Nx,Ny,Nz] | MEDIA_AS_SHORT (104) | two shorts: mua, mus between prop rows 1 and 2 |
+| uint8 [8,Nx,Ny,Nz] | MEDIA_2LABEL_SPLIT (97) | two planes: labels and plane point x y; point z and normal |
 """
 import numpy as np
 
 MEDIA_LABEL_HALF, MEDIA_AS_F2H, MEDIA_MUA_FLOAT, MEDIA_AS_HALF, MEDIA_ASGN_BYTE, MEDIA_AS_SHORT = 99, 100, 101, 102, 103, 104
+MEDIA_2LABEL_SPLIT = 97
 EPS = np.float32(1e-10)
 
 
@@ -83,7 +85,13 @@ def encode(vol, unitinmm=1.0, alloc=None):
         if vol.dtype in (np.int16, np.uint16) and lead == 3:
             raise ValueError("two-label mixture volumes (MEDIA_2LABEL_MIX) are not supported by this build")
         if vol.dtype in (np.uint8, np.int8) and lead == 8:
-            raise ValueError("split-voxel volumes (MEDIA_2LABEL_SPLIT) are not supported by this build")
+            # split voxels: bytes {lower label, upper label, reference point x y z, normal x y z}
+            # (0..255 each) -> two planes, the labels and point x y first, point z and the
+            # normal second (src/mcx_utils.c:1688-1711)
+            b = comps.astype(np.uint8).astype(np.uint32)
+            plane1 = b[3] | (b[2] << 8) | (b[1] << 16) | (b[0] << 24)
+            plane2 = b[7] | (b[6] << 8) | (b[5] << 16) | (b[4] << 24)
+            return np.concatenate([plane1, plane2]).astype(np.uint32), MEDIA_2LABEL_SPLIT, dims
         raise ValueError("unsupported 4-D volume: dtype %s with leading dimension %d" % (vol.dtype, lead))
     if vol.ndim == 2:
         vol = vol.reshape(vol.shape + (1,))

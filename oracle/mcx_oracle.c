@@ -45,6 +45,14 @@
 #define MED_MASK         0x7FFFFFFFu
 #define FILL_MAXDET      3
 #define MEDIA_MUA_FLOAT  101
+#define MEDIA_2LABEL_SPLIT 97
+/* split-voxel state (mcx_core.cl:577-587): lower and upper labels, whether the
+   voxel is split and which side the photon is on */
+#define SV_LOWER(sv)     ((sv) & 0xFFu)
+#define SV_UPPER(sv)     (((sv) >> 8) & 0xFFu)
+#define SV_ISSPLIT(sv)   (((sv) >> 16) & 1u)
+#define SV_ISUPPER(sv)   (((sv) >> 17) & 1u)
+#define SV_CURLABEL(sv)  (SV_ISUPPER(sv) ? SV_UPPER(sv) : SV_LOWER(sv))
 #define LAUNCH_ATTEMPT_CAP (1u << 16)  /* guard against a source that never yields weight */
 #define CONE_DRAW_CAP      (1u << 16)  /* guard against a cone of zero half-angle */
 
@@ -129,6 +137,8 @@ typedef struct {
     float* ppath;                 /* w0offset + srcnum (+ 2 for an RF replay) floats */
     float wre, wim, w0re, w0im;   /* RF forward: complex weight now and at the last voxel change */
     f4 st;                        /* polarised transport: Stokes vector {I, Q, U, V} */
+    float nv[3], pd;              /* split voxel: plane normal (pointing away from the photon's side), offset */
+    uint32_t sv;
 } ostate;
 
 /* ---------------------------------------------------------------- helpers */
@@ -259,6 +269,108 @@ static void update_stokes(const ocfg* c, ostate* s, float theta, float phi, cons
     s->st.z = s2.z * temp;
     s->st.w = s2.w * temp;
     s->st.x = 1.f;
+}
+
+/* updateproperty_svmc (mcx_core.cl:1231-1280): the properties of the side of
+   the voxel's plane the photon is on; the plane's reference point and normal
+   decode from the second volume plane */
+static void updateprop_svmc(const ocfg* c, f4* prop, uint32_t mediaid, uint32_t idx1d, const f4* p, ostate* s,
+                            const short fid[4]) {
+    uint32_t i0, i1, sv;
+    unsigned char b[8];
+    if (idx1d == OUT_MIN || idx1d == OUT_MAX) {
+        *prop = c->gprop[0];
+        return;
+    }
+    i0 = c->media[idx1d + c->dimlen[2]];
+    i1 = mediaid & MED_MASK;
+    b[0] = i0 & 0xFF, b[1] = (i0 >> 8) & 0xFF, b[2] = (i0 >> 16) & 0xFF, b[3] = (i0 >> 24) & 0xFF;
+    b[4] = i1 & 0xFF, b[5] = (i1 >> 8) & 0xFF, b[6] = (i1 >> 16) & 0xFF, b[7] = (i1 >> 24) & 0xFF;
+    sv = (uint32_t)b[7] | ((uint32_t)b[6] << 8);
+    if (b[6]) {
+        float rx = b[5] * (1.f / 255.f) + (float)fid[0];
+        float ry = b[4] * (1.f / 255.f) + (float)fid[1];
+        float rz = b[3] * (1.f / 255.f) + (float)fid[2];
+        float nx = b[2] * (2.f / 255.f) - 1.f, ny = b[1] * (2.f / 255.f) - 1.f, nz = b[0] * (2.f / 255.f) - 1.f;
+        float r = m_rsqrt(nx * nx + ny * ny + nz * nz);
+        nx = nx * r, ny = ny * r, nz = nz * r;
+        s->pd = rx * nx + ry * ny + rz * nz;
+        if (p->x * nx + p->y * ny + p->z * nz > s->pd) {
+            *prop = c->gprop[SV_UPPER(sv)];
+            sv |= 1u << 17;
+            nx = -nx, ny = -ny, nz = -nz;
+            s->pd = -s->pd;
+        } else {
+            *prop = c->gprop[SV_LOWER(sv)];
+            sv &= ~(1u << 17);
+        }
+        s->nv[0] = nx, s->nv[1] = ny, s->nv[2] = nz;
+        sv |= 1u << 16;
+    } else {
+        *prop = c->gprop[b[7]];
+        sv &= 0xFFFFu;
+    }
+    s->sv = sv;
+}
+
+/* ray_plane_intersect (1282-1303): clip the step at the voxel's plane when
+   the photon moves towards it and crosses it within the step */
+static int ray_plane_intersect(const ocfg* c, const ostate* s, float* len, float* slen) {
+    float vdotn = s->v.x * s->nv[0] + s->v.y * s->nv[1] + s->v.z * s->nv[2];
+    float d0, d1, len0;
+    if (vdotn <= 0.f) {
+        return 0;
+    }
+    d0 = s->p.x * s->nv[0] + s->p.y * s->nv[1] + s->p.z * s->nv[2] - s->pd;
+    d1 = d0 + (*len) * vdotn;
+    if (d0 * d1 > 0.f) {
+        return 0;
+    }
+    len0 = ((*len) * d0) / (d0 - d1);
+    *len = (len0 > 0.f) ? len0 : *len;
+    *slen = (*len) * s->prop.y * (s->v.w + 1.f > (float)c->gscatter ? (1.f - s->prop.z) : 1.f);
+    return 1;
+}
+
+/* reflectray_svmc (1305-1343): Fresnel reflection or refraction at the
+   voxel's plane; 1 when the photon refracts into a background half */
+static int reflectray_svmc(const ocfg* c, float n1, float* c0, ostate* s) {
+    float Icos, Re, Im, Rtotal, tmp0, tmp1, tmp2, n2;
+    Icos = fabsf(c0[0] * s->nv[0] + c0[1] * s->nv[1] + c0[2] * s->nv[2]);
+    n2 = SV_ISUPPER(s->sv) ? c->gprop[SV_UPPER(s->sv)].w : c->gprop[SV_LOWER(s->sv)].w;
+    tmp0 = n1 * n1;
+    tmp1 = n2 * n2;
+    tmp2 = 1.f - tmp0 / tmp1 * (1.f - Icos * Icos);
+    if (tmp2 > 0.f) {
+        Re = tmp0 * Icos * Icos + tmp1 * tmp2;
+        tmp2 = sqrtf(tmp2);
+        Im = 2.f * n1 * n2 * Icos * tmp2;
+        Rtotal = (Re - Im) / (Re + Im);
+        Re = tmp1 * Icos * Icos + tmp0 * tmp2 * tmp2;
+        Rtotal = (Rtotal + (Re - Im) / (Re + Im)) * 0.5f;
+        if (rng_next(s->t) <= Rtotal) {
+            c0[0] += (-2.f * Icos) * s->nv[0], c0[1] += (-2.f * Icos) * s->nv[1], c0[2] += (-2.f * Icos) * s->nv[2];
+            s->sv ^= 1u << 17;
+        } else {
+            int k;
+            c0[0] += (-Icos) * s->nv[0], c0[1] += (-Icos) * s->nv[1], c0[2] += (-Icos) * s->nv[2];
+            for (k = 0; k < 3; k++) {
+                c0[k] = tmp2 * s->nv[k] + (n1 / n2) * c0[k];
+            }
+            s->nv[0] = -s->nv[0], s->nv[1] = -s->nv[1], s->nv[2] = -s->nv[2];
+            s->pd = -s->pd;
+            if (SV_CURLABEL(s->sv) == 0) {
+                return 1;
+            }
+            s->prop = c->gprop[SV_CURLABEL(s->sv)];
+        }
+    } else {
+        c0[0] += (-2.f * Icos) * s->nv[0], c0[1] += (-2.f * Icos) * s->nv[1], c0[2] += (-2.f * Icos) * s->nv[2];
+        s->sv ^= 1u << 17;
+    }
+    tmp0 = m_rsqrt(c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2]);
+    c0[0] = c0[0] * tmp0, c0[1] = c0[1] * tmp0, c0[2] = c0[2] * tmp0;
+    return 0;
 }
 
 /* a deposit with photon sharing (mcx_core.cl:1527-1538, 2902-2911, the
@@ -522,7 +634,17 @@ static int skipvoid(const ocfg* c, f4* p, f4* v, f4* f, short fid[4]) {
                 f->y = (c->voidtime) ? f->y : 0.f;
                 {
                     f4 htime = {0.f, 0.f, 0.f, 0.f};
-                    updateprop(c, &htime, c->media[idx1d]);
+                    if (c->mediaformat == MEDIA_2LABEL_SPLIT) {
+                        /* the side of the entry voxel's plane (1404-1420); the launch then
+                           sets the photon's split state again, and the specular test uses
+                           that side's index where the reference reads the property table
+                           at the packed voxel word */
+                        ostate tmp;
+                        memset(&tmp, 0, sizeof(tmp));
+                        updateprop_svmc(c, &htime, c->media[idx1d], (uint32_t)idx1d, p, &tmp, fid);
+                    } else {
+                        updateprop(c, &htime, c->media[idx1d]);
+                    }
                     /* htime.w equals gproperty[label].w of mcx_core.cl:1425-1429 for labels;
                        for float-mua volumes the reference indexes past the table there */
                     if (c->isspecular && htime.w != c->gprop[0].w) {
@@ -660,7 +782,9 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
                 share_add(X, s, (size_t)s->idx1d + (size_t)tshift * c->dimlen[2], -s->p.w);
             }
         }
-        if ((isdet & DET_MASK) == DET_MASK && s->mediaid == 0 && c->issaveref < 2) {
+        if ((isdet & DET_MASK) == DET_MASK &&
+                (s->mediaid == 0 || (c->mediaformat == MEDIA_2LABEL_SPLIT && SV_CURLABEL(s->sv) == 0)) &&
+                c->issaveref < 2) {
             savedetphoton(X, s, isdet);
         }
     }
@@ -711,6 +835,9 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
             return -1;
         }
         s->p = ls->pos;
+        if (c->mediaformat == MEDIA_2LABEL_SPLIT) {
+            s->sv = 0;        /* 1640-1642 */
+        }
         s->v = ls->dir;
         s->f.x = 0.f;
         s->f.y = 0.f;
@@ -1084,7 +1211,11 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
 
     s->f.w += 1.f;
     s->prop = c->gprop[1];
-    updateprop(c, &s->prop, s->mediaid);
+    if (c->mediaformat == MEDIA_2LABEL_SPLIT) {
+        updateprop_svmc(c, &s->prop, s->mediaid, s->idx1d, &s->p, s, s->fid);
+    } else {
+        updateprop(c, &s->prop, s->mediaid);
+    }
     pp[1] += s->p.w;
     s->w0 = s->p.w;
     pp[2] = ((c->srcnum > 1) ? pp[2] : s->p.w);
@@ -1127,6 +1258,8 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
     ostate s;
     uint32_t idx1dold, mediaidold = 0;
     float ppbuf[4096];
+    const int svmc = (c->mediaformat == MEDIA_2LABEL_SPLIT);
+    int testint = 0, hitintf = 0;      /* split voxels: test the plane this step / the step ended on it */
     memset(&s, 0, sizeof(s));
     s.p.w = NAN;
     s.mediaid = f2bits(c->src.p2.w);
@@ -1205,12 +1338,16 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                 }
                 /* per-medium slots exist for labels 1..maxmedia; the reference indexes
                    outside them for label 0 and for label-half words */
-                if (SAVE_NSCAT(c->savedetflag) && (s.mediaid & MED_MASK) - 1u < c->maxmedia) {
-                    uint32_t n = f2bits(s.ppath[(s.mediaid & MED_MASK) - 1]) + 1u;
-                    s.ppath[(s.mediaid & MED_MASK) - 1] = bits2f(n);
-                }
-                if (SAVE_MOM(c->savedetflag) && (s.mediaid & MED_MASK) - 1u < c->maxmedia) {
-                    s.ppath[c->maxmedia * (SAVE_NSCAT(c->savedetflag) + SAVE_PPATH(c->savedetflag)) + (s.mediaid & MED_MASK) - 1] += 1.f - ctheta;
+                {
+                    /* split voxels record under the label of the photon's side (2507-2535) */
+                    const uint32_t lab = svmc ? SV_CURLABEL(s.sv) : (s.mediaid & MED_MASK);
+                    if (SAVE_NSCAT(c->savedetflag) && lab - 1u < c->maxmedia) {
+                        uint32_t n = f2bits(s.ppath[lab - 1]) + 1u;
+                        s.ppath[lab - 1] = bits2f(n);
+                    }
+                    if (SAVE_MOM(c->savedetflag) && lab - 1u < c->maxmedia) {
+                        s.ppath[c->maxmedia * (SAVE_NSCAT(c->savedetflag) + SAVE_PPATH(c->savedetflag)) + lab - 1] += 1.f - ctheta;
+                    }
                 }
                 {
                     const f4 olddir = s.v;
@@ -1256,10 +1393,17 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                 }
             }
             s.v.w = (float)(int)s.v.w;
+            if (svmc) {
+                testint = 1;      /* 2641-2647 */
+            }
         }
 
         s.n1 = s.prop.w;
-        updateprop(c, &s.prop, s.mediaid);
+        if (svmc) {
+            updateprop_svmc(c, &s.prop, s.mediaid, s.idx1d, &s.p, &s, s.fid);
+        } else {
+            updateprop(c, &s.prop, s.mediaid);
+        }
 
         /* advance to the next voxel face or the end of the free path, 2677-2765 */
         s.f.z = hitgrid(c, &s.p, &s.v, s.fid);
@@ -1267,19 +1411,26 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
             float slen = s.f.z * s.prop.y * (s.v.w + 1.f > (float)c->gscatter ? (1.f - s.prop.z) : 1.f);
             slen = fminf(slen, s.f.x);
             s.f.z = slen / (s.prop.y * (s.v.w + 1.f > (float)c->gscatter ? (1.f - s.prop.z) : 1.f));
+            hitintf = 0;
+            if (svmc && SV_ISSPLIT(s.sv) && testint) {
+                /* the voxel's plane cuts the step short (2687-2702) */
+                float tmplen = s.f.z;
+                hitintf = ray_plane_intersect(c, &s, &tmplen, &slen);
+                s.f.z = tmplen;
+            }
 
             s.pathlen += s.f.z;
             s.p.x = s.p.x + s.f.z * s.v.x;
             s.p.y = s.p.y + s.f.z * s.v.y;
             s.p.z = s.p.z + s.f.z * s.v.z;
             if (s.fid[3] == 0) {
-                s.fid[0] += (slen == s.f.x) ? 0 : (s.v.x > 0.f ? 1 : -1);
+                s.fid[0] += (slen == s.f.x || hitintf) ? 0 : (s.v.x > 0.f ? 1 : -1);
             }
             if (s.fid[3] == 1) {
-                s.fid[1] += (slen == s.f.x) ? 0 : (s.v.y > 0.f ? 1 : -1);
+                s.fid[1] += (slen == s.f.x || hitintf) ? 0 : (s.v.y > 0.f ? 1 : -1);
             }
             if (s.fid[3] == 2) {
-                s.fid[2] += (slen == s.f.x) ? 0 : (s.v.z > 0.f ? 1 : -1);
+                s.fid[2] += (slen == s.f.x || hitintf) ? 0 : (s.v.z > 0.f ? 1 : -1);
             }
             if (c->rfmode == 1) {
                 /* RF forward, 2750-2760: w <- w exp(-(mua + i omega n / c0) ds) */
@@ -1297,8 +1448,9 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
             s.f.x -= slen;
             s.f.y += s.f.z * s.prop.w * c->oneoverc0;
         }
-        if (c->savedet && SAVE_PPATH(c->savedetflag) && (s.mediaid & MED_MASK) - 1u < c->maxmedia) {
-            s.ppath[c->maxmedia * (SAVE_NSCAT(c->savedetflag)) + (s.mediaid & MED_MASK) - 1] += s.f.z;
+        if (c->savedet && SAVE_PPATH(c->savedetflag) &&
+                (svmc ? SV_CURLABEL(s.sv) : (s.mediaid & MED_MASK)) - 1u < c->maxmedia) {
+            s.ppath[c->maxmedia * (SAVE_NSCAT(c->savedetflag)) + (svmc ? SV_CURLABEL(s.sv) : (s.mediaid & MED_MASK)) - 1] += s.f.z;
         }
 
         /* new voxel, 2795-2811 */
@@ -1316,8 +1468,8 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
             s.mediaid &= MED_MASK;
         }
 
-        /* deposit on a voxel change, 2816-2929 */
-        if (s.idx1d != idx1dold && idx1dold < c->dimlen[2] && mediaidold) {
+        /* deposit on a voxel change (or at a split voxel's plane), 2816-2929 */
+        if ((s.idx1d != idx1dold || hitintf) && idx1dold < c->dimlen[2] && mediaidold) {
             if (c->save2pt && s.f.y >= c->twin0 && s.f.y < c->twin1) {
                 float weight = 0.f, weight_im = 0.f;
                 int tshift = (int)(floorf((s.f.y - c->twin0) * c->Rtstep));
@@ -1382,10 +1534,25 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
         } else {
             s.mediaid = mediaidold;
         }
+        if (svmc) {
+            /* the side of the plane after a voxel change or a plane crossing (2934-2950) */
+            if (s.idx1d != idx1dold) {
+                updateprop_svmc(c, &s.prop, s.mediaid, s.idx1d, &s.p, &s, s.fid);
+                testint = 1;
+            } else if (hitintf) {
+                s.nv[0] = -s.nv[0], s.nv[1] = -s.nv[1], s.nv[2] = -s.nv[2];
+                s.pd = -s.pd;
+                s.sv ^= 1u << 17;
+                testint = 0;
+            }
+        }
 
-        /* exit, time-out or cyclic boundary, 2958-3028 */
+        /* exit, time-out or cyclic boundary (and a background half of a split voxel), 2958-3028 */
         if ((s.mediaid == 0 && ((s.isdet & 0xF) == bcAbsorb || (s.isdet & 0xF) == bcCyclic ||
-                                ((s.isdet & 0xF) == bcReflect && s.n1 == c->gprop[0].w))) || s.f.y > c->twin1) {
+                                ((s.isdet & 0xF) == bcReflect && s.n1 == c->gprop[0].w))) ||
+                (svmc && ((s.idx1d != idx1dold || hitintf) && !SV_ISUPPER(s.sv) && !SV_LOWER(s.sv) &&
+                          (!c->doreflect || s.n1 == c->gprop[0].w))) ||
+                s.f.y > c->twin1) {
             if (s.isdet == bcCyclic) {
                 if (s.fid[3] == 0) {
                     s.p.x = nextafter_ref(rintf(((s.idx1d == OUT_MIN) ? c->maxidx.x : 0)), (s.v.x > 0.f) - (s.v.x < 0.f));
@@ -1412,6 +1579,9 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
             }
             s.isdet = s.mediaid & DET_MASK;
             s.mediaid &= MED_MASK;
+            if (svmc) {
+                testint = 1;      /* 3019-3023 */
+            }
             continue;
         }
 
@@ -1506,7 +1676,7 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
 
 /* mcx_maskdet, mcx_utils.c:4085-4198 */
 static void maskdet(uint32_t* vol, unsigned int nx, unsigned int ny, unsigned int nz, const float* detpos,
-                    unsigned int detnum) {
+                    unsigned int detnum, int svmc) {
     unsigned int dx = nx + 2, dy = ny + 2, dz = nz + 2;
     int isonecube = (nx == 1) && (ny == 1) && (nz == 1);
     static const float corners[8][3] = {{0.f, 0.f, 0.f}, {1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f},
@@ -1553,7 +1723,13 @@ static void maskdet(uint32_t* vol, unsigned int nx, unsigned int ny, unsigned in
                         continue;
                     }
                     idx1d = ((int)(iz + 1.f) * dy * dx + (int)(iy + 1.f) * dx + (int)(ix + 1.f));
-                    if (pad[idx1d]) {
+                    if (svmc) {
+                        /* split voxels with a background lower half (4155-4165) */
+                        uint32_t lower = (pad[idx1d] & 0xFF000000u) >> 24, upper = (pad[idx1d] & 0x00FF0000u) >> 16;
+                        if ((lower || upper) && !lower && upper) {
+                            vol[(int)iz * ny * nx + (int)iy * nx + (int)ix] |= DET_MASK;
+                        }
+                    } else if (pad[idx1d]) {
                         if (!(pad[idx1d + 1] && pad[idx1d - 1] && pad[idx1d + dx] && pad[idx1d - dx] &&
                                 pad[idx1d + dy * dx] && pad[idx1d - dy * dx] &&
                                 pad[idx1d + dx + 1] && pad[idx1d + dx - 1] && pad[idx1d - dx + 1] && pad[idx1d - dx - 1] &&
@@ -1639,6 +1815,17 @@ unsigned int mcxo_reclen(const mcxo_input* in) {
     return partial + SAVE_DETID(f) + 3 * (SAVE_PEXIT(f) + SAVE_VEXIT(f)) + SAVE_W0(f) + 4 * SAVE_IQUV(f);
 }
 
+/* a face condition that reflects ('r' or 'm') */
+static int bc_reflects(const mcxo_input* in) {
+    int i;
+    for (i = 0; i < 6; i++) {
+        if (in->bc[i] == 'r' || in->bc[i] == 'R' || in->bc[i] == 'm' || in->bc[i] == 'M') {
+            return 1;
+        }
+    }
+    return 0;
+}
+
 /* complex-weight transport (omega > 0, not a replay: mcx_host.cpp:473) or a
    complex replay output (rf, rfmus) */
 static int rf_mode(const mcxo_input* in) {
@@ -1721,10 +1908,12 @@ static int prepare(const mcxo_input* in, oprep* P) {
     if (in->dimx == 0 || in->dimy == 0 || in->dimz == 0 || in->medianum == 0 || in->nthread == 0) {
         return -1;
     }
-    if (in->mediabyte != 1 && in->mediabyte != 2 && in->mediabyte != 4 && !(in->mediabyte >= 99 && in->mediabyte <= 104)) {
+    if (in->mediabyte != 1 && in->mediabyte != 2 && in->mediabyte != 4 && in->mediabyte != MEDIA_2LABEL_SPLIT &&
+            !(in->mediabyte >= 99 && in->mediabyte <= 104)) {
         return -2;
     }
     if (in->issaveref > 1 || (in->srcnum > 1 && is_replay(in)) ||
+            (in->mediabyte == MEDIA_2LABEL_SPLIT && (in->isreflect || bc_reflects(in))) ||
             (rf_mode(in) && in->srcnum > 1 && (in->srctype == S_PATTERN || in->srctype == S_PATTERN3D))) {
         return -3;
     }
@@ -1753,8 +1942,9 @@ static int prepare(const mcxo_input* in, oprep* P) {
             gprop[i].y = H_EPS;
         }
     }
-    media = (uint32_t*)malloc((size_t)nvox * sizeof(uint32_t));
-    memcpy(media, in->vol, (size_t)nvox * sizeof(uint32_t));
+    /* split-voxel volumes carry a second plane: reference point and normal */
+    media = (uint32_t*)malloc((size_t)nvox * sizeof(uint32_t) * (in->mediabyte == MEDIA_2LABEL_SPLIT ? 2 : 1));
+    memcpy(media, in->vol, (size_t)nvox * sizeof(uint32_t) * (in->mediabyte == MEDIA_2LABEL_SPLIT ? 2 : 1));
 
     {
         float off = in->issrcfrom0 ? 0.f : 1.f;
@@ -1819,7 +2009,7 @@ static int prepare(const mcxo_input* in, oprep* P) {
             dp[i * 4 + 2] = gdet[i].z;
             dp[i * 4 + 3] = gdet[i].w;
         }
-        maskdet(media, in->dimx, in->dimy, in->dimz, dp, in->detnum);
+        maskdet(media, in->dimx, in->dimy, in->dimz, dp, in->detnum, in->mediabyte == MEDIA_2LABEL_SPLIT);
         free(dp);
     }
 

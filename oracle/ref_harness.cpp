@@ -24,7 +24,7 @@ struct ReplayBufs {
     int* detid = nullptr;
 };
 
-template <int ispencil, int isreflect>
+template <int ispencil, int isreflect, int issvmc>
 static void run_blocks(const mcxo_refprep& R, unsigned int nblock, unsigned int bsize, unsigned int* media,
                        float* field, float* genergy, unsigned int* seeds, float* detp, unsigned int* detcount,
                        float* gprop, float* gdet, RandType* gseed, float* srcpattern, const float* invcdf,
@@ -47,7 +47,7 @@ static void run_blocks(const mcxo_refprep& R, unsigned int nblock, unsigned int 
         }
         for (unsigned int t = 0; t < bsize; t++) {
             threadIdx = make_uint3(t, 0, 0);
-            mcx_main_loop<ispencil, isreflect, 1, 0, 0>(
+            mcx_main_loop<ispencil, isreflect, !issvmc, issvmc, 0>(
                 media, field, genergy, seeds, detp, (const float4*)gprop, srcpattern, (const float4*)gdet,
                 &progress, detcount, rp.weight, rp.tof, rp.detid, gseed, nullptr, nullptr, (float*)invcdf, (float*)angleinvcdf,
                 (RandType*)sharedmem_raw, (float4*)R.smatrix);
@@ -66,9 +66,11 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
         mcxo_free_ref(&R);
         return -10;
     }
-    if (in->mediabyte > 4) {
+    if (in->mediabyte > 4 && in->mediabyte != 97) {
+        /* the __NVCC__ launch path garbles prop.y/z for MEDIA_MUA_FLOAT (mcx_core.cl:2214-2231);
+           split voxels overwrite the whole property row there */
         mcxo_free_ref(&R);
-        return -11;      /* the __NVCC__ launch path garbles prop.y/z for MEDIA_MUA_FLOAT (mcx_core.cl:2214-2231) */
+        return -11;
     }
     MCXParam& P = gcfg_const[0];
     std::memset(&P, 0, sizeof(P));
@@ -127,7 +129,7 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     /* the __NVCC__ launch path reads media[idx + nvox] (updateproperty_asgn),
        so the volume is padded with a zero second half */
     std::vector<unsigned int> media(2 * (size_t)R.nvox, 0u);
-    std::memcpy(media.data(), R.media, sizeof(unsigned int) * R.nvox);
+    std::memcpy(media.data(), R.media, sizeof(unsigned int) * R.nvox * (R.mediaformat == 97 ? 2 : 1));
     /* RF: four quarters (re, re spill, im, im spill); the rfmus replay output
        writes the third quarter although the reference allocates two */
     std::vector<float> field((R.rfmode ? 4 : 2) * (size_t)R.fieldlen, 0.f);
@@ -167,17 +169,24 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
 
     int ispencil = (in->srctype == MCX_SRC_PENCIL);
     int isreflect = R.dorefl_compiled;
-#define RUN(a, b) run_blocks<a, b>(R, nblock, nblocksize, media.data(), field.data(), genergy.data(), seeds.data(), \
+#define RUN(a, b, sv) run_blocks<a, b, sv>(R, nblock, nblocksize, media.data(), field.data(), genergy.data(), seeds.data(), \
                                    detp.data(), &detcount, gprop.data(), gdet.data(), gseed.data(), (float*)in->srcpattern, \
                                    in->invcdf, in->nphase, in->angleinvcdf, in->nangle, nworkers, rp)
-    if (ispencil && isreflect) {
-        RUN(1, 1);
+    /* split-voxel volumes run the kernel built for them (issvmc), without reflection */
+    if (R.mediaformat == 97) {
+        if (ispencil) {
+            RUN(1, 0, 1);
+        } else {
+            RUN(0, 0, 1);
+        }
+    } else if (ispencil && isreflect) {
+        RUN(1, 1, 0);
     } else if (ispencil) {
-        RUN(1, 0);
+        RUN(1, 0, 0);
     } else if (isreflect) {
-        RUN(0, 1);
+        RUN(0, 1, 0);
     } else {
-        RUN(0, 0);
+        RUN(0, 0, 0);
     }
 #undef RUN
 

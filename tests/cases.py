@@ -69,6 +69,33 @@ def _voidtop():
     return vol
 
 
+def _svmc_vol():
+    """Split voxels (MEDIA_2LABEL_SPLIT): a radius-10 sphere of label 2 in
+    label 1 whose surface voxels carry the tangent plane (normal outward, so
+    the upper side is label 1), and a top layer split at z = 39.5 with
+    background above (normal down: the lower side is background)."""
+    n = 40
+    v = np.zeros((8, n, n, n), np.uint8)
+    x, y, z = np.meshgrid(np.arange(n) + 0.5, np.arange(n) + 0.5, np.arange(n) + 0.5, indexing="ij")
+    c = np.array([20.0, 20.0, 20.0])
+    r = np.sqrt((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2)
+    v[0] = np.where(r < 10, 2, 1)
+    split = np.abs(r - 10) < 0.8
+    nx, ny, nz = (x - c[0]) / r, (y - c[1]) / r, (z - c[2]) / r
+    px, py, pz = [np.clip(q + (10 - r) * d - np.floor(q), 0, 1) for q, d in ((x, nx), (y, ny), (z, nz))]
+    for k, a in enumerate((px, py, pz)):
+        v[2 + k] = np.where(split, np.round(a * 255), 0).astype(np.uint8)
+    for k, a in enumerate((nx, ny, nz)):
+        v[5 + k] = np.where(split, np.round((a + 1) * 127.5), 0).astype(np.uint8)
+    v[0] = np.where(split, 2, v[0])
+    v[1] = np.where(split, 1, 0)
+    top = (slice(None), slice(None), n - 1)
+    v[0][top], v[1][top] = 0, 1
+    v[2][top], v[3][top], v[4][top] = 128, 128, 128
+    v[5][top], v[6][top], v[7][top] = 128, 128, 0
+    return v
+
+
 def _pattern(n, seed):
     return np.random.RandomState(seed).rand(*n).astype(np.float32)
 
@@ -106,6 +133,8 @@ VARIANTS = {
     # RF forward: complex photon weights at 100 MHz (omega in rad/s), and with roulette
     "rf_forward": dict(omega=2 * np.pi * 1e8),
     "rf_roulette": dict(omega=2 * np.pi * 3e8, minenergy=0.01, outputtype="fluence"),
+    # split voxels: no Fresnel (this build, as the reference's host-compiled kernel, runs them without reflection)
+    "svmc": dict(vol=_svmc_vol(), isreflect=0),
     "focus": dict(srcdir=[0, 0, 1, 10]),
     "lambert": dict(srcdir=[0, 0, 1, -np.inf]),
     "noreflect": dict(isreflect=0),

@@ -190,8 +190,13 @@ def test_volume_encodings():
     v5[:, 0, 0, 0] = [7, 9]
     w, mb, _ = media.encode(v5)
     assert mb == 104 and w[0] == (9 << 16 | 7)
+    v8 = np.zeros((8, 2, 1, 1), np.uint8)
+    v8[:, 1, 0, 0] = [2, 1, 10, 20, 30, 40, 50, 60]     # lower, upper, point x y z, normal x y z
+    w, mb, dims = media.encode(v8)
+    assert mb == 97 and dims == (2, 1, 1) and w.size == 4
+    assert w[1] == (20 | 10 << 8 | 1 << 16 | 2 << 24) and w[3] == (60 | 50 << 8 | 40 << 16 | 30 << 24)
     with pytest.raises(ValueError):
-        media.encode(np.zeros((8, 2, 2, 2), np.uint8))
+        media.encode(np.zeros((3, 2, 2, 2), np.int16))
 
 
 def test_seed_words_match_the_c_library(lib):
