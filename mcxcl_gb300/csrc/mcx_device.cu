@@ -587,7 +587,8 @@ int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, 
     s->kp = kp;
     s->kp.mediaword = mediaword;
     s->kp.npattern = (uint32_t)(npattern ? npattern : 1);
-    size_t mbytes = (size_t)kp.nvox * mediaword;
+    /* split-voxel volumes carry a second plane (plane point and normal) */
+    size_t mbytes = (size_t)kp.nvox * mediaword * (kp.mediaformat == 97 ? 2 : 1);
     int rc = ensure((uint8_t**)&s->d_media, &s->media_cap, mbytes);
     if (!rc) {
         rc = ensure(&s->d_prop, &s->prop_cap, kp.medianum);
@@ -790,20 +791,22 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     const bool noagg = (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
     const bool rf = kp.omega > 0.f && !kp.replay;
     const bool pol = s->npol > 0;
-    const bool xmedia = !rf && kp.mediaformat > 4 && kp.mediaformat != 101;
+    const bool svmc = kp.mediaformat == 97;
+    const bool xmedia = !rf && !svmc && kp.mediaformat > 4 && kp.mediaformat != 101;
     /* the instantiations that fix the common configuration's parameters */
     const bool common = !rf && !pol && !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2 &&
                         kp.srcnum <= 1;
-    const int bpsm_sel = (xmedia || rf || pol) ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
+    const int bpsm_sel = (xmedia || rf || pol || svmc) ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
                  (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
-                 (common ? mcxg::LF_COMMON : 0) | (rf ? mcxg::LF_RF : 0) | (pol ? mcxg::LF_POL : 0);
+                 (common ? mcxg::LF_COMMON : 0) | (rf ? mcxg::LF_RF : 0) | (pol ? mcxg::LF_POL : 0) |
+                 (svmc ? mcxg::LF_SVMC : 0);
     int block = s->block_req ? s->block_req : 256;
     size_t smem = shared_bytes(kp, block);
     if (smem > s->info.sharedmem_per_block) {
         return MCXG_ERR_LIMIT;
     }
-    int bpsm = (s->bpsm_req && !xmedia && !rf && !pol) ? s->bpsm_req : (exact ? 2 : bpsm_sel);
+    int bpsm = (s->bpsm_req && !xmedia && !rf && !pol && !svmc) ? s->bpsm_req : (exact ? 2 : bpsm_sel);
     if (!exact) {
         /* never more blocks than fit at once: a persistent grid must be resident */
         int occ = 0;

@@ -287,7 +287,12 @@ static void maskdet(Config* cfg) {
                     }
                     size_t i = ((size_t)(int)(iz + 1.f) * dy * dx + (size_t)(int)(iy + 1.f) * dx + (size_t)(int)(ix + 1.f));
                     size_t dxy = (size_t)dy * dx;
-                    if (pad[i] &&
+                    if (cfg->mediabyte == 97) {
+                        /* split voxels: those with a background lower half (mcx_utils.c:4155-4165) */
+                        if (!(pad[i] & 0xFF000000u) && (pad[i] & 0x00FF0000u)) {
+                            cfg->vol[(int)iz * ny * nx + (int)iy * nx + (int)ix] |= DET_MASK;
+                        }
+                    } else if (pad[i] &&
                             !(pad[i + 1] && pad[i - 1] && pad[i + dx] && pad[i - dx] && pad[i + dxy] && pad[i - dxy] &&
                               pad[i + dx + 1] && pad[i + dx - 1] && pad[i - dx + 1] && pad[i - dx - 1] &&
                               pad[i + dxy + 1] && pad[i + dxy - 1] && pad[i - dxy + 1] && pad[i - dxy - 1] &&
@@ -474,6 +479,20 @@ static void preprocess(Config* cfg) {
             if ((cfg->vol[i] & 0x3FFFu) >= cfg->medianum) {
                 MCX_ERROR(-4, "input media optical properties are less than the labels in the volume");
             }
+        }
+    } else if (cfg->mediabyte == 97) {
+        /* split voxels: lower and upper labels in the top bytes of the first plane */
+        for (size_t i = 0; i < nvox; i++) {
+            if (((cfg->vol[i] >> 24) & 0x7Fu) >= cfg->medianum || ((cfg->vol[i] >> 16) & 0xFFu) >= cfg->medianum) {
+                MCX_ERROR(-4, "input media optical properties are less than the labels in the volume");
+            }
+        }
+        int reflects = cfg->isreflect;
+        for (int k = 0; k < 6; k++) {
+            reflects |= (cfg->bc[k] == 'r' || cfg->bc[k] == 'R' || cfg->bc[k] == 'm' || cfg->bc[k] == 'M');
+        }
+        if (reflects) {
+            MCX_ERROR(-4, "split-voxel volumes run without reflection in this build (set isreflect = 0)");
         }
     } else if (cfg->mediabyte < 100 || cfg->mediabyte > 104) {
         MCX_ERROR(-4, "this build supports label volumes (mediabyte 1/2/4), label + half property (99), half "

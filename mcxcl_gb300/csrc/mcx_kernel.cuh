@@ -226,6 +226,8 @@ struct BatchPST {
 #define KP_RFREPLAY (c_p.replay && (c_p.outputtype == otRF || c_p.outputtype == otRFmus))
 /* polarised transport in the instantiations compiled with it */
 #define KP_POL (POL && a.maxpol > 0u)
+/* split-voxel volumes (MEDIA_2LABEL_SPLIT) in the instantiations compiled with them */
+#define KP_SVMC (SVMC && c_p.mediaformat == 97u)
 
 /* ------------------------------------------------------------------ math */
 
@@ -297,7 +299,17 @@ struct Photon {
     Rng t;
     float wre, wim, w0re, w0im;    /* RF transport: complex weight now and at the last voxel change */
     float4 st;                     /* polarised transport: Stokes vector {I, Q, U, V} */
+    float3 nv;                     /* split voxel: plane normal, pointing away from the photon's side */
+    float pd;                      /* and the plane's offset along it */
+    unsigned int sv;               /* lower and upper label, split and side bits */
 };
+
+/* split-voxel state (mcx_core.cl:577-587) */
+#define SV_LOWER(sv)     ((sv) & 0xFFu)
+#define SV_UPPER(sv)     (((sv) >> 8) & 0xFFu)
+#define SV_ISSPLIT(sv)   (((sv) >> 16) & 1u)
+#define SV_ISUPPER(sv)   (((sv) >> 17) & 1u)
+#define SV_CURLABEL(sv)  (SV_ISUPPER(sv) ? SV_UPPER(sv) : SV_LOWER(sv))
 
 template <class PS>
 __device__ __forceinline__ unsigned int media_at(const KArgs& a, const PS& ps, unsigned int idx) {
@@ -434,6 +446,68 @@ __device__ __forceinline__ void rotatevector(float4& v, float st, float ct, floa
     }
 }
 
+/* updateproperty_svmc (mcx_core.cl:1231-1280): the properties of the side of
+   the voxel's plane the photon is on; the plane's reference point (in the
+   voxel) and normal decode from the second volume plane.  A voxel outside the
+   volume takes row 0 and leaves the split state as it was. */
+template <bool EXACT, class PS>
+__device__ __forceinline__ void updateprop_svmc(const KArgs& a, const PS& ps, const Shared& S, float4& prop,
+                                                unsigned int mediaid, unsigned int idx1d, const float4& p, int fx,
+                                                int fy, int fz, Photon& s) {
+    const mcxg_kparams& c_p = ps.p();
+    if (idx1d == K_OUT_MIN || idx1d == K_OUT_MAX) {
+        prop = ps.prop(S, 0);
+        return;
+    }
+    const unsigned int i0 = __ldg(a.media32 + ps.media_off() + c_p.nvox + idx1d);
+    const unsigned int i1 = mediaid & K_MED_MASK;
+    unsigned int sv = (i1 >> 24) | (((i1 >> 16) & 0xFFu) << 8);
+    if ((i1 >> 16) & 0xFFu) {
+        const float rx = (float)((i1 >> 8) & 0xFFu) * (1.f / 255.f) + (float)(short)fx;
+        const float ry = (float)(i1 & 0xFFu) * (1.f / 255.f) + (float)(short)fy;
+        const float rz = (float)(i0 >> 24) * (1.f / 255.f) + (float)(short)fz;
+        float nx = (float)((i0 >> 16) & 0xFFu) * (2.f / 255.f) - 1.f;
+        float ny = (float)((i0 >> 8) & 0xFFu) * (2.f / 255.f) - 1.f;
+        float nz = (float)(i0 & 0xFFu) * (2.f / 255.f) - 1.f;
+        const float r = Mth<EXACT>::rsqrt(nx * nx + ny * ny + nz * nz);
+        nx = nx * r, ny = ny * r, nz = nz * r;
+        float pd = rx * nx + ry * ny + rz * nz;
+        if (p.x * nx + p.y * ny + p.z * nz > pd) {
+            prop = ps.prop(S, SV_UPPER(sv));
+            sv |= 1u << 17;
+            nx = -nx, ny = -ny, nz = -nz;
+            pd = -pd;
+        } else {
+            prop = ps.prop(S, SV_LOWER(sv));
+        }
+        s.nv = make_float3(nx, ny, nz);
+        s.pd = pd;
+        sv |= 1u << 16;
+    } else {
+        prop = ps.prop(S, i1 >> 24);
+    }
+    s.sv = sv;
+}
+
+/* ray_plane_intersect (mcx_core.cl:1282-1303): clip the step at the voxel's
+   plane when the photon moves towards it and crosses it within the step */
+template <bool EXACT>
+__device__ __forceinline__ bool ray_plane_intersect(const Photon& s, float gscat, float& len, float& slen) {
+    const float vdotn = s.v.x * s.nv.x + s.v.y * s.nv.y + s.v.z * s.nv.z;
+    if (vdotn <= 0.f) {
+        return false;
+    }
+    const float d0 = s.p.x * s.nv.x + s.p.y * s.nv.y + s.p.z * s.nv.z - s.pd;
+    const float d1 = d0 + len * vdotn;
+    if (d0 * d1 > 0.f) {
+        return false;
+    }
+    const float len0 = Mth<EXACT>::div(len * d0, d0 - d1);
+    len = (len0 > 0.f) ? len0 : len;
+    slen = len * s.prop.y * (s.v.w + 1.f > gscat ? (1.f - s.prop.z) : 1.f);
+    return true;
+}
+
 /* Polarised scattering angles (mcx_core.cl:2454-2469): theta uniform in cos,
    phi uniform, accepted with the probability the Mueller matrix of the
    medium gives the photon's Stokes vector at theta against the forward
@@ -558,7 +632,7 @@ __device__ float reflectcoeff(const float4& v, float n1, float n2, int fw) {
 
 /* skipvoid, mcx_core.cl:1350-1455: march through background voxels to the
    first labelled voxel on the ray */
-template <bool EXACT, class PS>
+template <bool EXACT, bool SVMC, class PS>
 __device__ int skipvoid(const KArgs& a, const PS& ps, const Shared& S, float4& p, float4& v, float4& f, int& fx,
                         int& fy, int& fz, int& fw) {
     const mcxg_kparams& c_p = ps.p();
@@ -604,7 +678,15 @@ __device__ int skipvoid(const KArgs& a, const PS& ps, const Shared& S, float4& p
                 {
                     unsigned int m = media_at(a, ps, idx1d);
                     float4 ht = make_float4(0.f, 0.f, 0.f, 0.f);
-                    updateprop(ps, S, ht, m);
+                    if (KP_SVMC) {
+                        /* the side of the entry voxel's plane (1404-1420); the launch sets
+                           the photon's split state again, and the specular test uses that
+                           side's index where the reference reads the table at the voxel word */
+                        Photon tmp;
+                        updateprop_svmc<EXACT>(a, ps, S, ht, m, (unsigned int)idx1d, p, fx, fy, fz, tmp);
+                    } else {
+                        updateprop(ps, S, ht, m);
+                    }
                     /* ht.w is the entry voxel's index of refraction; the reference reads
                        gproperty[label].w, the same value for label volumes and an index past
                        the table for float-mua volumes */
@@ -898,7 +980,7 @@ __device__ __forceinline__ void set_launch_voxel(const KArgs& a, const PS& ps, P
  * reference thread.  Returns 0 on launch, 1 when the thread's quota is done,
  * -1 when no launch position was found.
  */
-template <bool EXACT, bool DET, bool RF, bool POL, class PS>
+template <bool EXACT, bool DET, bool RF, bool POL, bool SVMC, class PS>
 __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Photon& s, unsigned int isdet,
                                unsigned int vt, unsigned long long* nfailed) {
     const mcxg_kparams& c_p = ps.p();
@@ -928,7 +1010,8 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
                 field_add2(a.field, ps.lo_plane(), key, -s.p.w);
             }
         }
-        if (DET && c_p.savedet && (isdet & K_DET_MASK) == K_DET_MASK && s.mediaid == 0 && c_p.issaveref < 2) {
+        if (DET && c_p.savedet && (isdet & K_DET_MASK) == K_DET_MASK &&
+                (s.mediaid == 0 || (KP_SVMC && SV_CURLABEL(s.sv) == 0)) && c_p.issaveref < 2) {
             savedetphoton<POL>(a, ps, S, s, isdet);
         }
     }
@@ -989,6 +1072,9 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
         }
         s.p = lpos;
         s.v = ldir;
+        if (KP_SVMC) {
+            s.sv = 0u;        /* 1640-1642 */
+        }
         s.f.x = 0.f;
         s.f.y = 0.f;
         s.f.z = c_p.minaccumtime;
@@ -1298,7 +1384,7 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
         }
 
         if ((s.mediaid & K_MED_MASK) == 0) {
-            int idx = skipvoid<EXACT>(a, ps, S, s.p, s.v, s.f, s.fx, s.fy, s.fz, s.fw);
+            int idx = skipvoid<EXACT, SVMC>(a, ps, S, s.p, s.v, s.f, s.fx, s.fy, s.fz, s.fw);
             if (idx >= 0) {
                 s.idx1d = (unsigned int)idx;
                 s.mediaid = media_at(a, ps, s.idx1d);
@@ -1320,7 +1406,11 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
 
     s.f.w += 1.f;
     s.prop = ps.prop(S, 1);
-    updateprop(ps, S, s.prop, s.mediaid);
+    if (KP_SVMC) {
+        updateprop_svmc<EXACT>(a, ps, S, s.prop, s.mediaid, s.idx1d, s.p, s.fx, s.fy, s.fz, s);
+    } else {
+        updateprop(ps, S, s.prop, s.mediaid);
+    }
     ps.cold()->launched += s.p.w;
     s.w0 = s.p.w;
     if (!KP_SHARING) {
@@ -1432,7 +1522,7 @@ __device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPST<C>& ps, unsign
 }
 
 template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false,
-          bool COMMON = false, bool RF = false, bool POL = false>
+          bool COMMON = false, bool RF = false, bool POL = false, bool SVMC = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
     typedef typename std::conditional<BATCH, BatchPST<COMMON>, ConstPST<XMEDIA, COMMON>>::type PS;
@@ -1476,6 +1566,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     pd.old = pd.w = 0.f;
     float3 rv = make_float3(0.f, 0.f, 0.f);   /* fast kernel: rcp of the direction */
     bool vdirty = true;
+    bool testint = false, hitintf = false;    /* split voxels: test the plane this step / the step ended on it */
 
     while (claimed) {
         const mcxg_kparams& c_p = ps.p();
@@ -1489,7 +1580,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             if (fresh && (unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
                 r = 1;
             } else {
-                r = launchnewphoton<EXACT, DET, RF, POL>(a, ps, S, s, fresh ? 0u : relaunch_isdet, vt, &cnt_fail);
+                r = launchnewphoton<EXACT, DET, RF, POL, SVMC>(a, ps, S, s, fresh ? 0u : relaunch_isdet, vt, &cnt_fail);
                 if (r && fresh) {
                     atomicAdd(a.status + ST_FAILED_LAUNCH, 1u);
                     r = 2;       /* NO_LAUNCH: the reference returns without writing energies */
@@ -1587,8 +1678,10 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     }
                 }
                 }
-                if (DET && c_p.savedet && (s.mediaid & K_MED_MASK) - 1u < c_p.maxmedia) {
-                    unsigned int med = (s.mediaid & K_MED_MASK) - 1;
+                /* a split voxel records under the label of the photon's side (2507-2535) */
+                const unsigned int slab = KP_SVMC ? SV_CURLABEL(s.sv) : (s.mediaid & K_MED_MASK);
+                if (DET && c_p.savedet && slab - 1u < c_p.maxmedia) {
+                    unsigned int med = slab - 1;
                     if (SAVE_NSCAT(c_p.savedetflag)) {
                         float* q = &ps.pp(med);
                         *q = __uint_as_float(__float_as_uint(*q) + 1u);
@@ -1614,10 +1707,17 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 }
             }
             s.v.w = (float)(int)s.v.w;
+            if (KP_SVMC) {
+                testint = true;      /* 2641-2647 */
+            }
         }
 
         s.n1 = s.prop.w;
-        updateprop(ps, S, s.prop, s.mediaid);
+        if (KP_SVMC) {
+            updateprop_svmc<EXACT>(a, ps, S, s.prop, s.mediaid, s.idx1d, s.p, s.fx, s.fy, s.fz, s);
+        } else {
+            updateprop(ps, S, s.prop, s.mediaid);
+        }
 
         /* ---- move to the next voxel face or the end of the free path */
         if (EXACT) {
@@ -1639,11 +1739,16 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 const float4 rc = ps.recip(S, s.mediaid & K_MED_MASK);
                 s.f.z = slen * (reduced ? rc.y : rc.x);
             }
+            hitintf = false;
+            if (KP_SVMC && SV_ISSPLIT(s.sv) && testint) {
+                /* the voxel's plane cuts the step short (2687-2702) */
+                hitintf = ray_plane_intersect<EXACT>(s, gscat, s.f.z, slen);
+            }
             s.pathlen += s.f.z;
             s.p.x = s.p.x + s.f.z * s.v.x;
             s.p.y = s.p.y + s.f.z * s.v.y;
             s.p.z = s.p.z + s.f.z * s.v.z;
-            bool scat_here = (slen == s.f.x);
+            bool scat_here = (slen == s.f.x) || hitintf;
             if (s.fw == 0) {
                 s.fx += scat_here ? 0 : (s.v.x > 0.f ? 1 : -1);
             }
@@ -1671,8 +1776,11 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         }
         /* a photon in a label-0 voxel (entered from a medium of the same index)
            has no partial-path slot; the reference writes one slot early there */
-        if (DET && c_p.savedet && SAVE_PPATH(c_p.savedetflag) && (s.mediaid & K_MED_MASK) - 1u < c_p.maxmedia) {
-            ps.pp(c_p.maxmedia * SAVE_NSCAT(c_p.savedetflag) + (s.mediaid & K_MED_MASK) - 1) += s.f.z;
+        {
+            const unsigned int plab = KP_SVMC ? SV_CURLABEL(s.sv) : (s.mediaid & K_MED_MASK);
+            if (DET && c_p.savedet && SAVE_PPATH(c_p.savedetflag) && plab - 1u < c_p.maxmedia) {
+                ps.pp(c_p.maxmedia * SAVE_NSCAT(c_p.savedetflag) + plab - 1) += s.f.z;
+            }
         }
 
         /* ---- new voxel (mcx_core.cl:2795-2811) */
@@ -1695,7 +1803,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             bool dep = false, depim = false;
             unsigned int key = 0;
             float weight = 0.f, weight_im = 0.f;
-            if (s.idx1d != idx1dold && idx1dold < c_p.nvox && mediaidold) {
+            if ((s.idx1d != idx1dold || hitintf) && idx1dold < c_p.nvox && mediaidold) {
                 if (c_p.save2pt && s.f.y >= c_p.twin0 && s.f.y < c_p.twin1) {
                     int tshift = (int)(floorf((s.f.y - c_p.twin0) * c_p.Rtstep));
                     if (KP_RFFWD) {
@@ -1781,10 +1889,26 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 field_add2(a.field + 2 * (size_t)c_p.fieldlen, c_p.fieldlen, key, weight_im);
             }
         }
+        if (KP_SVMC) {
+            /* the side of the plane after a voxel change or a plane crossing (2934-2950) */
+            if (s.idx1d != idx1dold) {
+                updateprop_svmc<EXACT>(a, ps, S, s.prop, s.mediaid, s.idx1d, s.p, s.fx, s.fy, s.fz, s);
+                testint = true;
+            } else if (hitintf) {
+                s.nv = make_float3(-s.nv.x, -s.nv.y, -s.nv.z);
+                s.pd = -s.pd;
+                s.sv ^= 1u << 17;
+                testint = false;
+            }
+        }
 
-        /* ---- exit, time-out or cyclic boundary (mcx_core.cl:2958-3028) */
+        /* ---- exit, time-out or cyclic boundary, or a background half of a split
+           voxel (mcx_core.cl:2958-3028) */
         if ((s.mediaid == 0 && ((s.isdet & 0xF) == bcAbsorb || (s.isdet & 0xF) == bcCyclic ||
-                                ((s.isdet & 0xF) == bcReflect && s.n1 == ps.prop(S, 0).w))) || s.f.y > c_p.twin1) {
+                                ((s.isdet & 0xF) == bcReflect && s.n1 == ps.prop(S, 0).w))) ||
+                (KP_SVMC && (s.idx1d != idx1dold || hitintf) && !SV_ISUPPER(s.sv) && !SV_LOWER(s.sv) &&
+                 (!c_p.doreflect || s.n1 == ps.prop(S, 0).w)) ||
+                s.f.y > c_p.twin1) {
             if (s.isdet == bcCyclic) {
                 if (s.fw == 0) {
                     s.p.x = nextafter_ref(rintf(((s.idx1d == K_OUT_MIN) ? c_p.maxidx.x : 0)), (s.v.x > 0.f) - (s.v.x < 0.f));
@@ -1808,6 +1932,9 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             }
             relaunch = true;
             relaunch_isdet = exit_detflag(ps, s, mediaidold);
+            if (KP_SVMC) {
+                testint = true;      /* 3019-3023 */
+            }
             continue;
         }
 
@@ -1936,5 +2063,6 @@ __global__ void mcx_rng_dump(const KArgs a) {
 #undef KP_RFFWD
 #undef KP_RFREPLAY
 #undef KP_POL
+#undef KP_SVMC
 
 #endif

@@ -23,7 +23,7 @@ cudaError_t exact_upload(const mcxg_kparams* p, const float* det4, unsigned int 
 
 cudaError_t exact_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st) {
     (void)flags;
-    void* f = (void*)mcx_transport<true, true, true, false, true, 2, false, true, false, true, true>;
+    void* f = (void*)mcx_transport<true, true, true, false, true, 2, false, true, false, true, true, true>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) {

@@ -49,7 +49,7 @@ struct KArgs {
 };
 
 /* flag bits for the launch entries */
-enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128, LF_POL = 256 };
+enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128, LF_POL = 256, LF_SVMC = 512 };
 
 /* fast instantiation: hardware transcendental approximations */
 cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,

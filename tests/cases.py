@@ -135,6 +135,9 @@ VARIANTS = {
     "rf_roulette": dict(omega=2 * np.pi * 3e8, minenergy=0.01, outputtype="fluence"),
     # split voxels: no Fresnel (this build, as the reference's host-compiled kernel, runs them without reflection)
     "svmc": dict(vol=_svmc_vol(), isreflect=0),
+    # ... with a detector over the split top layer: detection in a background half follows the
+    # reference's OpenCL kernel (its host-compiled kernel detects only in fully void voxels)
+    "svmc_topdet": dict(vol=_svmc_vol(), isreflect=0, detpos=[[20, 20, 39, 6]], nphoton=20000),
     "focus": dict(srcdir=[0, 0, 1, 10]),
     "lambert": dict(srcdir=[0, 0, 1, -np.inf]),
     "noreflect": dict(isreflect=0),
@@ -186,7 +189,7 @@ VARIANTS.update({
     "asshort": dict(vol=np.random.RandomState(6).randint(1, 32767, (2, 40, 40, 40)).astype(np.int16),
                     savedetflag="dxvw"),
 })
-NOT_PINNED = {"muafloat", "asf2h", "labelhalf", "asgnbyte", "asshort"}
+NOT_PINNED = {"muafloat", "asf2h", "labelhalf", "asgnbyte", "asshort", "svmc_topdet"}
 
 
 def variant(name, **kw):

@@ -58,7 +58,7 @@ EXACT_CASES = ["pencil_gates", "isotropic", "cone", "gaussian", "planar", "fouri
                "pattern", "pattern3d", "focus", "lambert", "noreflect", "cyclic", "facedet", "roulette",
                "unitinmm", "gscatter", "outside_src_specular", "multisrc", "multisrc_id", "energy_out",
                "fluence_out", "invcdf", "angleinvcdf", "muafloat", "asf2h", "labelhalf", "asgnbyte", "asshort",
-               "pattern_share", "pattern3d_share", "rf_forward", "rf_roulette"]
+               "pattern_share", "pattern3d_share", "rf_forward", "rf_roulette", "svmc", "svmc_topdet"]
 
 
 @pytest.mark.parametrize("name", EXACT_CASES)
@@ -273,3 +273,16 @@ def test_fast_kernel_polarized_agrees_with_exact(gpu):
     qf, qe = f["detp"][14:18].mean(axis=1), e["detp"][14:18].mean(axis=1)
     assert np.allclose(qf[0], 1.0) and np.allclose(qe[0], 1.0)
     assert np.all(np.abs(qf[1:] - qe[1:]) < 0.05), (qf, qe)
+
+
+def test_fast_kernel_svmc_agrees_with_exact(gpu):
+    """The fast split-voxel instantiation against the exact one: absorbed
+    fraction and detections through the split top layer."""
+    import mcxcl_gb300
+    cfg = cases.variant("svmc_topdet", nphoton=400000)
+    f = mcxcl_gb300.run(dict(cfg))
+    e = mcxcl_gb300.run(dict(cfg, exactmath=1))
+    af, ae = _absorbed(f), _absorbed(e)
+    assert abs(af - ae) < 0.005, (af, ae)
+    nf, ne = f["detp"].shape[1], e["detp"].shape[1]
+    assert ne > 200 and abs(nf - ne) < 5 * np.sqrt(ne), (nf, ne)
