@@ -487,13 +487,6 @@ static void preprocess(Config* cfg) {
                 MCX_ERROR(-4, "input media optical properties are less than the labels in the volume");
             }
         }
-        int reflects = cfg->isreflect;
-        for (int k = 0; k < 6; k++) {
-            reflects |= (cfg->bc[k] == 'r' || cfg->bc[k] == 'R' || cfg->bc[k] == 'm' || cfg->bc[k] == 'M');
-        }
-        if (reflects) {
-            MCX_ERROR(-4, "split-voxel volumes run without reflection in this build (set isreflect = 0)");
-        }
     } else if (cfg->mediabyte < 100 || cfg->mediabyte > 104) {
         MCX_ERROR(-4, "this build supports label volumes (mediabyte 1/2/4), label + half property (99), half "
                   "mua/mus (100, 102), float mua (101), byte (103) and short (104) mixtures");

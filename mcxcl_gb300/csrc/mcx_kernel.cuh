@@ -508,6 +508,50 @@ __device__ __forceinline__ bool ray_plane_intersect(const Photon& s, float gscat
     return true;
 }
 
+/* reflectray_svmc (mcx_core.cl:1305-1343): Fresnel reflection or refraction
+   of direction c at a split voxel's plane (s.nv faces the side the photon
+   comes from); true when the photon refracts into a background half */
+template <bool EXACT, class PS>
+__device__ __forceinline__ bool reflectray_svmc(const PS& ps, const Shared& S, Photon& s, float n1, float3& c) {
+    typedef Mth<EXACT> M;
+    const float Icos = fabsf(c.x * s.nv.x + c.y * s.nv.y + c.z * s.nv.z);
+    const float n2 = ps.prop(S, SV_ISUPPER(s.sv) ? SV_UPPER(s.sv) : SV_LOWER(s.sv)).w;
+    const float tmp0 = n1 * n1, tmp1 = n2 * n2;
+    float tmp2 = 1.f - M::div(tmp0, tmp1) * (1.f - Icos * Icos);
+    if (tmp2 > 0.f) {
+        float Re = tmp0 * Icos * Icos + tmp1 * tmp2;
+        tmp2 = M::sqrt(tmp2);
+        const float Im = 2.f * n1 * n2 * Icos * tmp2;
+        float Rtotal = M::div(Re - Im, Re + Im);
+        Re = tmp1 * Icos * Icos + tmp0 * tmp2 * tmp2;
+        Rtotal = (Rtotal + M::div(Re - Im, Re + Im)) * 0.5f;
+        if (rnd(s.t) <= Rtotal) {
+            const float k = -2.f * Icos;
+            c.x += k * s.nv.x, c.y += k * s.nv.y, c.z += k * s.nv.z;
+            s.sv ^= 1u << 17;
+        } else {
+            const float k = -Icos, r = M::div(n1, n2);
+            c.x += k * s.nv.x, c.y += k * s.nv.y, c.z += k * s.nv.z;
+            c.x = tmp2 * s.nv.x + r * c.x;
+            c.y = tmp2 * s.nv.y + r * c.y;
+            c.z = tmp2 * s.nv.z + r * c.z;
+            s.nv = make_float3(-s.nv.x, -s.nv.y, -s.nv.z);
+            s.pd = -s.pd;
+            if (SV_CURLABEL(s.sv) == 0) {
+                return true;
+            }
+            s.prop = ps.prop(S, SV_CURLABEL(s.sv));
+        }
+    } else {
+        const float k = -2.f * Icos;
+        c.x += k * s.nv.x, c.y += k * s.nv.y, c.z += k * s.nv.z;
+        s.sv ^= 1u << 17;
+    }
+    const float r = M::rsqrt(c.x * c.x + c.y * c.y + c.z * c.z);
+    c.x = c.x * r, c.y = c.y * r, c.z = c.z * r;
+    return false;
+}
+
 /* Polarised scattering angles (mcx_core.cl:2454-2469): theta uniform in cos,
    phi uniform, accepted with the probability the Mueller matrix of the
    medium gives the photon's Stokes vector at theta against the forward
@@ -1575,6 +1619,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             int r;
             if (fresh) {
                 vt_begin(a, ps, S, s, vt);
+                testint = false;     /* each reference thread starts untested (2342) */
             }
             /* one call site for the first and every later launch keeps the hot loop small */
             if (fresh && (unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
@@ -1959,8 +2004,32 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         /* within the same voxel the medium and index are unchanged, so the test
            below cannot fire -- except for the encodings from 100 on, whose test
            compares with row 1's index rather than the voxel's */
-        if (REFL && c_p.dorefl_compiled && (s.idx1d != idx1dold || (PS::kXMedia && KP_MEDIAFORMAT >= 100))) {
-            updateprop(ps, S, s.prop, s.mediaid);
+        if (REFL && KP_SVMC && c_p.dorefl_compiled && hitintf) {
+            /* Fresnel at a split voxel's plane (mcx_core.cl:3065-3115) */
+            if (ps.prop(S, SV_LOWER(s.sv)).w != ps.prop(S, SV_UPPER(s.sv)).w) {
+                float3 c0 = make_float3(s.v.x, s.v.y, s.v.z);
+                s.nv = make_float3(-s.nv.x, -s.nv.y, -s.nv.z);
+                s.pd = -s.pd;
+                if (reflectray_svmc<EXACT>(ps, S, s, s.n1, c0)) {
+                    relaunch = true;
+                    relaunch_isdet = mediaidold & K_DET_MASK;
+                    testint = true;
+                    continue;
+                }
+                s.v.x = c0.x, s.v.y = c0.y, s.v.z = c0.z;
+                vdirty = true;
+            } else {
+                s.prop = ps.prop(S, SV_CURLABEL(s.sv));
+            }
+        } else if (REFL && c_p.dorefl_compiled &&
+                   (KP_SVMC || s.idx1d != idx1dold || (PS::kXMedia && KP_MEDIAFORMAT >= 100))) {
+            /* a split voxel's side already holds its properties (the OpenCL
+               kernel's update of the label is empty for that encoding); the side
+               is recomputed from the position every step, so the index can change
+               without a voxel change and the test runs every step there */
+            if (!KP_SVMC) {
+                updateprop(ps, S, s.prop, s.mediaid);
+            }
             if (((s.mediaid && c_p.doreflect) ||
                  (s.mediaid == 0 && (((s.isdet & 0xF) == bcUnknown && c_p.doreflect) ||
                                      ((s.isdet & 0xF) == bcReflect || (s.isdet & 0xF) == bcMirror)))) &&
@@ -2019,7 +2088,18 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                        reference keeps the face code here, which mcx_core.cl:2796 then
                        ORs into the medium index) */
                     s.isdet = m & K_DET_MASK;
-                    updateprop(ps, S, s.prop, s.mediaid);
+                    if (KP_SVMC) {
+                        /* back in the voxel it came from: its side of the plane
+                           (mcx_core.cl:3218-3236, the OpenCL kernel keeps testint) */
+                        updateprop_svmc<EXACT>(a, ps, S, s.prop, s.mediaid, s.idx1d, s.p, s.fx, s.fy, s.fz, s);
+                        if (SV_CURLABEL(s.sv) == 0) {
+                            relaunch = true;
+                            relaunch_isdet = mediaidold & K_DET_MASK;
+                            continue;
+                        }
+                    } else {
+                        updateprop(ps, S, s.prop, s.mediaid);
+                    }
                     s.n1 = s.prop.w;
                 }
             }

@@ -54,10 +54,10 @@ static void* kpol() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, false, false, true>;
 }
 
-/* split-voxel volumes (no Fresnel): 3 blocks/SM, direct deposits */
-template <bool DET>
+/* split-voxel volumes: 3 blocks/SM, direct deposits */
+template <bool DET, bool REFL>
 static void* ksvmc() {
-    return (void*)mcx_transport<false, DET, false, false, false, 3, false, false, false, false, false, true>;
+    return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, false, false, false, true>;
 }
 
 /* volumes in the less common encodings: 3 blocks/SM, direct deposits */
@@ -69,7 +69,8 @@ static void* kxmedia() {
 static void* select(int flags) {
     const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
     if (flags & LF_SVMC) {
-        return det ? ksvmc<true>() : ksvmc<false>();
+        return det ? (refl ? ksvmc<true, true>() : ksvmc<true, false>())
+                   : (refl ? ksvmc<false, true>() : ksvmc<false, false>());
     }
     if (flags & LF_POL) {
         return det ? (refl ? kpol<true, true>() : kpol<true, false>()) : (refl ? kpol<false, true>() : kpol<false, false>());

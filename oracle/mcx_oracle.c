@@ -1605,9 +1605,33 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
             }
         }
 
-        /* Fresnel reflection / refraction, 3126-3278 */
-        if (c->dorefl_compiled) {
-            updateprop(c, &s.prop, s.mediaid);
+        /* Fresnel at a split voxel's plane (3065-3115, the OpenCL kernel) */
+        if (c->dorefl_compiled && svmc && hitintf) {
+            if (c->gprop[SV_LOWER(s.sv)].w != c->gprop[SV_UPPER(s.sv)].w) {
+                float c0[3];
+                s.nv[0] = -s.nv[0], s.nv[1] = -s.nv[1], s.nv[2] = -s.nv[2];
+                s.pd = -s.pd;
+                c0[0] = s.v.x, c0[1] = s.v.y, c0[2] = s.v.z;
+                if (reflectray_svmc(c, s.n1, c0, &s)) {
+                    if (launchnewphoton(X, &s, (mediaidold & DET_MASK))) {
+                        break;
+                    }
+                    s.isdet = s.mediaid & DET_MASK;
+                    s.mediaid &= MED_MASK;
+                    testint = 1;
+                    continue;
+                }
+                s.v.x = c0[0], s.v.y = c0[1], s.v.z = c0[2];
+            } else {
+                s.prop = c->gprop[SV_CURLABEL(s.sv)];
+            }
+        } else if (c->dorefl_compiled) {
+            /* Fresnel reflection / refraction, 3126-3278; in a split-voxel volume the
+               photon's side already holds the properties (the OpenCL kernel's label
+               update is empty there) */
+            if (!svmc) {
+                updateprop(c, &s.prop, s.mediaid);
+            }
             if (((s.mediaid && c->doreflect) ||
                  (s.mediaid == 0 && (((s.isdet & 0xF) == bcUnknown && c->doreflect) || ((s.isdet & 0xF) == bcReflect ||
                                                                                          (s.isdet & 0xF) == bcMirror)))) &&
@@ -1616,7 +1640,9 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                 float Rtotal = 1.f;
                 float cphi, sphi, stheta, ctheta, tmp0, tmp1;
                 X->nreflect++;
-                updateprop(c, &s.prop, s.mediaid);
+                if (!svmc) {
+                    updateprop(c, &s.prop, s.mediaid);
+                }
                 tmp0 = s.n1 * s.n1;
                 tmp1 = s.prop.w * s.prop.w;
                 cphi = fabsf(vcomp(&s.v, s.fid[3]));
@@ -1661,7 +1687,24 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                        index (2796) and can turn label 2 into 3.  Both the oracle and
                        the product take the detector bit of the voxel it is back in. */
                     s.isdet = c->media[s.idx1d] & DET_MASK;
-                    updateprop(c, &s.prop, s.mediaid);
+                    if (svmc) {
+                        /* back in the voxel it came from: its side of the plane (3218-3236);
+                           only the CUDA branch tests the plane after the relaunch (3240-3243) */
+                        updateprop_svmc(c, &s.prop, s.mediaid, s.idx1d, &s.p, &s, s.fid);
+                        if (SV_CURLABEL(s.sv) == 0) {
+                            if (launchnewphoton(X, &s, (mediaidold & DET_MASK))) {
+                                break;
+                            }
+                            s.isdet = s.mediaid & DET_MASK;
+                            s.mediaid &= MED_MASK;
+                            if (c->variant == MCXO_VARIANT_NVCC) {
+                                testint = 1;
+                            }
+                            continue;
+                        }
+                    } else {
+                        updateprop(c, &s.prop, s.mediaid);
+                    }
                     s.n1 = s.prop.w;
                 }
             }
@@ -1815,17 +1858,6 @@ unsigned int mcxo_reclen(const mcxo_input* in) {
     return partial + SAVE_DETID(f) + 3 * (SAVE_PEXIT(f) + SAVE_VEXIT(f)) + SAVE_W0(f) + 4 * SAVE_IQUV(f);
 }
 
-/* a face condition that reflects ('r' or 'm') */
-static int bc_reflects(const mcxo_input* in) {
-    int i;
-    for (i = 0; i < 6; i++) {
-        if (in->bc[i] == 'r' || in->bc[i] == 'R' || in->bc[i] == 'm' || in->bc[i] == 'M') {
-            return 1;
-        }
-    }
-    return 0;
-}
-
 /* complex-weight transport (omega > 0, not a replay: mcx_host.cpp:473) or a
    complex replay output (rf, rfmus) */
 static int rf_mode(const mcxo_input* in) {
@@ -1913,7 +1945,6 @@ static int prepare(const mcxo_input* in, oprep* P) {
         return -2;
     }
     if (in->issaveref > 1 || (in->srcnum > 1 && is_replay(in)) ||
-            (in->mediabyte == MEDIA_2LABEL_SPLIT && (in->isreflect || bc_reflects(in))) ||
             (rf_mode(in) && in->srcnum > 1 && (in->srctype == S_PATTERN || in->srctype == S_PATTERN3D))) {
         return -3;
     }

@@ -172,10 +172,14 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
 #define RUN(a, b, sv) run_blocks<a, b, sv>(R, nblock, nblocksize, media.data(), field.data(), genergy.data(), seeds.data(), \
                                    detp.data(), &detcount, gprop.data(), gdet.data(), gseed.data(), (float*)in->srcpattern, \
                                    in->invcdf, in->nphase, in->angleinvcdf, in->nangle, nworkers, rp)
-    /* split-voxel volumes run the kernel built for them (issvmc), without reflection */
+    /* split-voxel volumes run the kernel built for them (issvmc) */
     if (R.mediaformat == 97) {
-        if (ispencil) {
+        if (ispencil && isreflect) {
+            RUN(1, 1, 1);
+        } else if (ispencil) {
             RUN(1, 0, 1);
+        } else if (isreflect) {
+            RUN(0, 1, 1);
         } else {
             RUN(0, 0, 1);
         }

@@ -133,8 +133,10 @@ VARIANTS = {
     # RF forward: complex photon weights at 100 MHz (omega in rad/s), and with roulette
     "rf_forward": dict(omega=2 * np.pi * 1e8),
     "rf_roulette": dict(omega=2 * np.pi * 3e8, minenergy=0.01, outputtype="fluence"),
-    # split voxels: no Fresnel (this build, as the reference's host-compiled kernel, runs them without reflection)
+    # split voxels: without Fresnel, and with Fresnel at the planes (indices 1.37 / 1.45) and
+    # at the voxel faces
     "svmc": dict(vol=_svmc_vol(), isreflect=0),
+    "svmc_refl": dict(vol=_svmc_vol(), isreflect=1),
     # ... with a detector over the split top layer: detection in a background half follows the
     # reference's OpenCL kernel (its host-compiled kernel detects only in fully void voxels)
     "svmc_topdet": dict(vol=_svmc_vol(), isreflect=0, detpos=[[20, 20, 39, 6]], nphoton=20000),
