@@ -390,7 +390,10 @@ def main():
     ndet = last["detp"].shape[1] if "detp" in last else 0
     reclen = last["detp"].shape[0] if "detp" in last else 0
     nseed = last["seeds"].shape[1] if last.get("seeds") is not None else 0
-    h2d = nvox * 1 + 16 * 3 + 16 * 4 + 16 * nthread
+    # the seed words are generated on the device from 31-word windows of <= 4096 blocks
+    nword = 4 * nthread
+    blocklen = max(-(-nword // 4096), 1024)
+    h2d = nvox * 1 + 16 * 3 + 16 * 4 + 4 * 31 * (-(-nword // blocklen))
     d2h = nvox * gates * 4 + ndet * reclen * 4 + nseed * 16 + 16 + 8 * 4 + 8 * 8
 
     out = None

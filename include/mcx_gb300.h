@@ -264,6 +264,11 @@ int mcx_mie(double x, double mrel, float* smatrix, double* qsca, double* g);
 /* The n words rand() returns after srand(seed) in glibc (the reference's
    per-thread seed words), without the C library's per-call lock. */
 void mcx_rand_words(unsigned int seed, uint32_t* out, size_t n);
+/* Jump-ahead into the same stream: the generator's 31-word windows (the
+   unshifted values of words k - 31 .. k - 1) at k = skip + j x blocklen for
+   j < nblock, into starts (31 x nblock words): each block of words can then
+   be generated on its own.  0 on success. */
+int mcx_rand_blocks(unsigned int seed, uint64_t skip, uint32_t nblock, uint32_t blocklen, uint32_t* starts);
 /* Everything mcx_run_simulation does before its first launch -- device
    selection, parameter block, volume packing, upload, seeds of the first
    repetition -- and nothing after: returns the ready device session so a
@@ -337,6 +342,12 @@ int  mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size,
 int  mcxg_set_params(mcxg_session* s, const void* kparams, size_t kparams_size);
 /* 4 seed words per reference thread, as the reference draws them with rand(). */
 int  mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread);
+/* The same words generated on the device: 4 x nthread words of the additive
+   generator, in nblock blocks of blocklen words ((nblock - 1) x blocklen <
+   4 x nthread <= nblock x blocklen), block j starting from the 31 words
+   starts[31 j ..] that mcx_rand_blocks returns. */
+int  mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock, uint32_t blocklen,
+                         uint32_t nthread);
 /* Launch shape of the persistent grid (0 = automatic).  blocks_per_sm = 3
    selects the instantiation whose registers are capped for three resident
    256-thread blocks per SM (also the automatic choice); 2 the uncapped one. */

@@ -107,10 +107,10 @@ class DevInfo(ctypes.Structure):
 # every symbol include/mcx_gb300.h declares
 EXPORTS = [
     "mcx_initcfg", "mcx_clearcfg", "mcx_validatecfg", "mcx_list_gpu", "mcx_cleargpuinfo", "mcx_run_simulation",
-    "mcx_normalize", "mcx_error", "mcx_last_error", "mcx_detreclen", "mcx_version", "mcx_rand_words", "mcx_config_sizeof",
+    "mcx_normalize", "mcx_error", "mcx_last_error", "mcx_detreclen", "mcx_version", "mcx_rand_words", "mcx_rand_blocks", "mcx_config_sizeof",
     "mcx_config_offsetof", "mcx_release_sessions", "mcx_prepare_simulation",
     "mcxg_device_count", "mcxg_device_info", "mcxg_error_string", "mcxg_create", "mcxg_destroy",
-    "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_launch", "mcxg_simulate",
+    "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_seeds_lfib", "mcxg_set_launch", "mcxg_simulate",
     "mcxg_get_energy", "mcxg_get_thread_energy", "mcxg_get_field", "mcxg_get_field_f64", "mcxg_get_detected",
     "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc", "mcxg_autotune",
     "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_field_interleaved", "mcxg_set_polarization", "mcx_mie", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",
@@ -144,6 +144,7 @@ def load():
     L.mcx_detreclen.restype = ctypes.c_uint
     L.mcx_version.restype = ctypes.c_char_p
     L.mcx_rand_words.argtypes = [ctypes.c_uint, vp, ctypes.c_size_t]
+    L.mcx_rand_blocks.argtypes = [ctypes.c_uint, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, vp]
     L.mcx_prepare_simulation.argtypes = [P(Config)]
     L.mcx_prepare_simulation.restype = vp
     L.mcx_config_sizeof.restype = ctypes.c_size_t

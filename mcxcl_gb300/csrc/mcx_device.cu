@@ -48,6 +48,8 @@ struct mcxg_session {
     size_t pattern_cap = 0;
     uint4* d_seeds = nullptr;
     size_t seeds_cap = 0;
+    uint32_t* d_lfib = nullptr;      /* 31-word generator windows, one per block of seed words */
+    size_t lfib_cap = 0;
     float* d_field = nullptr;        /* 2 x fieldlen */
     size_t field_cap = 0;
     float2* d_energy = nullptr;
@@ -535,7 +537,7 @@ int mcxg_destroy(mcxg_session* s) {
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
                     s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw,
                     s->d_sims, s->d_simvt, s->d_simctr, s->d_smatrix, s->d_bmedia, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
-                    s->d_adj};
+                    s->d_adj, s->d_lfib};
     if (s->bgraph_exec) {
         cudaGraphExecDestroy(s->bgraph_exec);
     }
@@ -672,6 +674,64 @@ int mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread) {
         return rc;
     }
     MCXG_TRY(cudaMemcpyAsync(s->d_seeds, seeds, sizeof(uint4) * nthread, cudaMemcpyHostToDevice, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    s->has_seeds = true;
+    return MCXG_OK;
+}
+
+/* Seed words of the additive lagged-Fibonacci generator o[k] = o[k-3] +
+   o[k-31] (mod 2^32), each word o[k] >> 1: block j (one thread) starts from
+   the window starts[31 j .. 31 j + 30] = o[j B - 31 .. j B - 1] and writes
+   words j B .. min((j + 1) B, nword) - 1.  The ring lives in registers: in
+   each unrolled group of 31, r[t] holds o[k - 31] before and o[k] after its
+   update, and r[(t + 28) % 31] holds o[k - 3] (this group's new value for
+   t >= 3, the previous group's, not yet overwritten, for t < 3). */
+__global__ void __launch_bounds__(128) lfib_words(const uint32_t* __restrict__ starts, uint32_t nblock,
+                                                  uint32_t blocklen, uint32_t nword, uint32_t* __restrict__ out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nblock) {
+        return;
+    }
+    uint32_t r[31];
+#pragma unroll
+    for (int t = 0; t < 31; t++) {
+        r[t] = starts[31 * (size_t)j + t];
+    }
+    const size_t begin = (size_t)j * blocklen;
+    const size_t end = begin + blocklen < nword ? begin + blocklen : nword;
+    for (size_t base = begin; base < end; base += 31) {
+#pragma unroll
+        for (int t = 0; t < 31; t++) {
+            r[t] += r[(t + 28) % 31];
+            if (base + t < end) {
+                out[base + t] = r[t] >> 1;
+            }
+        }
+    }
+}
+
+int mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock, uint32_t blocklen,
+                        uint32_t nthread) {
+    const uint64_t nword = 4ull * nthread;
+    if (!s || !starts || nthread == 0 || nblock == 0 || blocklen == 0 || nword > 0xFFFFFFFFull ||
+        (uint64_t)nblock * blocklen < nword || (uint64_t)(nblock - 1) * blocklen >= nword) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    int rc = ensure(&s->d_seeds, &s->seeds_cap, nthread);
+    if (!rc) {
+        rc = ensure(&s->d_energy, &s->energy_cap, nthread);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_lfib, &s->lfib_cap, 31 * (size_t)nblock);
+    }
+    if (rc) {
+        return rc;
+    }
+    MCXG_TRY(cudaMemcpyAsync(s->d_lfib, starts, sizeof(uint32_t) * 31 * (size_t)nblock, cudaMemcpyHostToDevice, s->st));
+    lfib_words<<<(nblock + 127) / 128, 128, 0, s->st>>>(s->d_lfib, nblock, blocklen, (uint32_t)nword,
+                                                         (uint32_t*)s->d_seeds);
+    MCXG_TRY(cudaGetLastError());
     MCXG_TRY(cudaStreamSynchronize(s->st));
     s->has_seeds = true;
     return MCXG_OK;

@@ -927,6 +927,111 @@ void mcx_rand_words(unsigned int seed, uint32_t* out, size_t n) {
     addrand_fill(&g, out, n);
 }
 
+/* Jump-ahead.  The generator is linear over the integers mod 2^32: with the
+   window W = (o[k-31], ..., o[k-1]) of its unshifted outputs, one step is
+   W' = M W with W'[t] = W[t+1] (t < 30) and W'[30] = W[0] + W[28] (o[k] =
+   o[k-31] + o[k-3]; the ring slot f holds o[k-31], b = f - 3 holds o[k-3]), so n steps
+   are M^n W, M^n by repeated squaring (31 x 31 matrices of words, products
+   wrapping mod 2^32 as the generator's sums do). */
+#define LF_N 31
+
+static void lf_matmul(const uint32_t* A, const uint32_t* B, uint32_t* C) {
+    uint32_t T[LF_N * LF_N];
+    for (int i = 0; i < LF_N; i++) {
+        uint32_t row[LF_N] = {0};
+        for (int k = 0; k < LF_N; k++) {
+            const uint32_t a = A[i * LF_N + k];
+            for (int j = 0; j < LF_N; j++) {
+                row[j] += a * B[k * LF_N + j];
+            }
+        }
+        memcpy(T + i * LF_N, row, sizeof(row));
+    }
+    memcpy(C, T, sizeof(T));
+}
+
+static void lf_matvec(const uint32_t* A, const uint32_t* w, uint32_t* out) {
+    uint32_t r[LF_N];
+    for (int i = 0; i < LF_N; i++) {
+        uint32_t acc = 0;
+        for (int k = 0; k < LF_N; k++) {
+            acc += A[i * LF_N + k] * w[k];
+        }
+        r[i] = acc;
+    }
+    memcpy(out, r, sizeof(r));
+}
+
+/* P = M^e */
+static void lf_pow(uint64_t e, uint32_t* P) {
+    uint32_t B[LF_N * LF_N] = {0};
+    memset(P, 0, sizeof(uint32_t) * LF_N * LF_N);
+    for (int i = 0; i < LF_N; i++) {
+        P[i * LF_N + i] = 1u;
+    }
+    for (int t = 0; t < LF_N - 1; t++) {
+        B[t * LF_N + t + 1] = 1u;
+    }
+    B[(LF_N - 1) * LF_N + 0] = 1u;
+    B[(LF_N - 1) * LF_N + 28] = 1u;
+    while (e) {
+        if (e & 1u) {
+            lf_matmul(P, B, P);
+        }
+        e >>= 1;
+        if (e) {
+            lf_matmul(B, B, B);
+        }
+    }
+}
+
+static void addrand_window(const AddRand* g, uint32_t* W) {
+    for (int t = 0; t < LF_N; t++) {
+        W[t] = g->x[(g->f + t) % LF_N];
+    }
+}
+
+static void addrand_set_window(AddRand* g, const uint32_t* W) {
+    memcpy(g->x, W, sizeof(uint32_t) * LF_N);
+    g->f = 0;
+    g->b = 28;
+}
+
+/* the windows at g's position + j x blocklen (j < nblock) into starts, and g
+   moved on by nword words */
+static void addrand_blocks(AddRand* g, uint64_t nword, uint32_t nblock, uint32_t blocklen, uint32_t* starts) {
+    uint32_t P[LF_N * LF_N], W[LF_N];
+    addrand_window(g, W);
+    lf_pow(blocklen, P);
+    for (uint32_t j = 0; j < nblock; j++) {
+        memcpy(starts + (size_t)LF_N * j, W, sizeof(W));
+        if (j + 1 < nblock) {
+            lf_matvec(P, W, W);
+        }
+    }
+    addrand_window(g, W);
+    lf_pow(nword, P);
+    lf_matvec(P, W, W);
+    addrand_set_window(g, W);
+}
+
+int mcx_rand_blocks(unsigned int seed, uint64_t skip, uint32_t nblock, uint32_t blocklen, uint32_t* starts) {
+    if (!starts || nblock == 0 || blocklen == 0) {
+        return -1;
+    }
+    AddRand g;
+    uint32_t P[LF_N * LF_N], W[LF_N];
+    addrand_seed(&g, seed);
+    if (skip) {
+        addrand_window(&g, W);
+        lf_pow(skip, P);
+        lf_matvec(P, W, W);
+        addrand_set_window(&g, W);
+    }
+    addrand_blocks(&g, 0, nblock, blocklen, starts);
+    return 0;
+}
+
 static void make_kparams(const Config* cfg, size_t nvox, size_t fieldlen, size_t autothread, unsigned int hostdetreclen,
                          unsigned int partialdata, unsigned int is2d, int replay, mcxg_kparams* kp) {
     memset(kp, 0, sizeof(*kp));
@@ -1207,7 +1312,7 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
        saved state, so its per-thread words are never drawn from */
     AddRand ar;
     addrand_seed(&ar, cfg->seed > 0 ? (unsigned int)cfg->seed : (replay ? 1u : (unsigned int)time(0)));
-    seeds = (uint32_t*)malloc(sizeof(uint32_t) * 4 * autothread);
+    seeds = (uint32_t*)malloc(sizeof(uint32_t) * 31 * 4096);    /* the generator windows of <= 4096 blocks */
     if (!seeds) {
         MCX_ERROR(-2, "out of host memory");
     }
@@ -1228,8 +1333,14 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
 
     float kms_total = 0.f;
     for (int iter = 0; iter < cfg->respin; iter++) {
-        addrand_fill(&ar, seeds, autothread * 4);
-        device_check(mcxg_set_seeds(s, seeds, (uint32_t)autothread), "uploading seeds");
+        /* the words are generated on the device from 31-word windows at block
+           starts (at most 4096 blocks: the host's jump-ahead costs 961
+           multiply-adds a block) */
+        const uint64_t nword = 4ull * autothread;
+        const uint32_t blocklen = (uint32_t)((nword + 4095) / 4096 > 1024 ? (nword + 4095) / 4096 : 1024);
+        const uint32_t nblock = (uint32_t)((nword + blocklen - 1) / blocklen);
+        addrand_blocks(&ar, nword, nblock, blocklen, seeds);
+        device_check(mcxg_set_seeds_lfib(s, seeds, nblock, blocklen, (uint32_t)autothread), "generating seeds");
         /* photon split in the reference's float arithmetic (mcx_host.cpp:1101-1102) */
         float tp = (float)cfg->nphoton * workload0 / (fullload * (float)autothread * (float)cfg->respin);
         kp.threadphoton = (uint32_t)(int)tp;

@@ -411,7 +411,7 @@ def _outputs(cfg, C):
         else:
             dims = (C.dim.x, C.dim.y, C.dim.z, gates)
         flux = f.reshape(dims, order="F")
-        if C.issaveref:
+        if C.issaveref != b"\0":
             vol = np.ctypeslib.as_array(C.vol, shape=(C.dim.x * C.dim.y * C.dim.z,))
             mask = (vol & 0x7FFFFFFF).reshape((1, C.dim.x, C.dim.y, C.dim.z), order="F") != 0
             fl = flux.reshape((nshare, C.dim.x, C.dim.y, C.dim.z, -1), order="F")

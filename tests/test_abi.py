@@ -217,6 +217,32 @@ def test_seed_words_match_the_c_library(lib):
         assert np.array_equal(got, want), seed
 
 
+def _expand_window(w, n):
+    """n words of the additive generator from a 31-word window of its
+    unshifted outputs: o[k] = o[k-3] + o[k-31] (mod 2^32), word = o >> 1."""
+    o = [int(v) for v in w]
+    for _ in range(n):
+        o.append((o[-3] + o[-31]) & 0xFFFFFFFF)
+    return np.array(o[31:], np.uint64).astype(np.uint32) >> 1
+
+
+def test_seed_jump_ahead_matches_the_stream(lib):
+    """The device seed path: 31-word windows from the host's jump-ahead
+    (matrix powers mod 2^32) expand to the same words as the serial
+    generator, at block starts and after long skips (a repetition's skip is
+    the previous repetitions' 4 x threads words)."""
+    for seed, skip, nblock, blocklen in ((1648335518, 0, 5, 300), (12345, 7, 3, 1024),
+                                         (29012392, 19922944, 2, 64), (1, 2**20 + 3, 4, 97)):
+        starts = np.zeros(31 * nblock, np.uint32)
+        assert lib.mcx_rand_blocks(seed, skip, nblock, blocklen, starts.ctypes.data) == 0
+        total = skip + nblock * blocklen
+        want = np.zeros(total, np.uint32)
+        lib.mcx_rand_words(seed, want.ctypes.data, total)
+        for j in range(nblock):
+            got = _expand_window(starts[31 * j:31 * j + 31], blocklen)
+            assert np.array_equal(got, want[skip + j * blocklen:skip + (j + 1) * blocklen]), (seed, skip, j)
+
+
 def _mie(lib, x, m):
     sm = np.zeros((181, 4), np.float32)
     q, g = ctypes.c_double(), ctypes.c_double()

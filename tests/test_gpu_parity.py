@@ -288,3 +288,16 @@ def test_fast_kernel_svmc_agrees_with_exact(gpu, isreflect):
     assert abs(af - ae) < 0.005, (af, ae)
     nf, ne = f["detp"].shape[1], e["detp"].shape[1]
     assert ne > 100 and abs(nf - ne) < 5 * np.sqrt(ne), (nf, ne)
+
+
+def test_dref_only_when_saved(gpu):
+    """The diffuse-reflectance output exists only when issaveref is set (the
+    reference's module, src/pmcxcl.cpp:1359-1380); without it the flux is
+    returned as simulated."""
+    import mcxcl_gb300
+    cfg = cases.variant("pattern_share", nphoton=20000)
+    on = mcxcl_gb300.run(dict(cfg))
+    off = mcxcl_gb300.run(dict(cfg, issaveref=0))
+    assert "dref" in on and "dref" not in off
+    assert on["dref"].shape == on["flux"].shape and np.all(on["dref"] >= 0)
+    assert np.any(on["dref"] > 0)
