@@ -686,6 +686,7 @@ int mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread) {
    each unrolled group of 31, r[t] holds o[k - 31] before and o[k] after its
    update, and r[(t + 28) % 31] holds o[k - 3] (this group's new value for
    t >= 3, the previous group's, not yet overwritten, for t < 3). */
+namespace {
 __global__ void __launch_bounds__(128) lfib_words(const uint32_t* __restrict__ starts, uint32_t nblock,
                                                   uint32_t blocklen, uint32_t nword, uint32_t* __restrict__ out) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -709,6 +710,7 @@ __global__ void __launch_bounds__(128) lfib_words(const uint32_t* __restrict__ s
         }
     }
 }
+}  // namespace
 
 int mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock, uint32_t blocklen,
                         uint32_t nthread) {

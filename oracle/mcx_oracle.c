@@ -2153,6 +2153,9 @@ static int prepare(const mcxo_input* in, oprep* P) {
     /* seeds, mcx_host.cpp:696-700, 759-768 */
     seedwords = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)in->nthread);
     srand(in->seed > 0 ? (unsigned int)in->seed : 0u);
+    for (i = 0; i < in->seedskip; i++) {
+        (void)rand();
+    }
     for (i = 0; i < in->nthread * 4; i++) {
         seedwords[i] = (uint32_t)rand();
     }

@@ -131,6 +131,11 @@ typedef struct mcxo_input {
     const float* smatrix;
     unsigned int polmedianum;
     float s0[4];
+
+    /* rand() words drawn and discarded before the per-thread seed words: a
+       later repetition of a respin run draws after the earlier ones'
+       4 x nthread words each (mcx_host.cpp:759-768 inside the respin loop) */
+    unsigned int seedskip;
 } mcxo_input;
 
 typedef struct mcxo_stats {

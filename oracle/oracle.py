@@ -61,6 +61,7 @@ class MCXOInput(ctypes.Structure):
         ("replaydetid", ctypes.c_void_p), ("nreplay", ctypes.c_uint), ("replaydet", ctypes.c_int),
         ("replaysiteown", ctypes.c_int), ("detweight_out", ctypes.c_void_p), ("omega", ctypes.c_float),
         ("smatrix", ctypes.c_void_p), ("polmedianum", ctypes.c_uint), ("s0", ctypes.c_float * 4),
+        ("seedskip", ctypes.c_uint),
     ]
 
 
@@ -156,7 +157,7 @@ def _flags(s, letters):
 
 
 def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL,
-               fieldmode=FIELD_DOUBLE, nworkers=0):
+               fieldmode=FIELD_DOUBLE, nworkers=0, seedskip=0):
     """Translate a pmcxcl-style dict into the oracle's input struct.
 
     Returns (struct, keepalive) -- keepalive holds the numpy buffers."""
@@ -270,6 +271,7 @@ def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT
         _replay_input(inp, keep, cfg, seed)
     else:
         inp.seed = int(seed)
+    inp.seedskip = int(seedskip)
     return inp, keep
 
 
@@ -318,11 +320,11 @@ def _replay_input(inp, keep, cfg, seed):
 
 
 def run(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL, fieldmode=FIELD_DOUBLE,
-        nworkers=0):
+        nworkers=0, seedskip=0):
     """Run the oracle.  Returns a dict with the merged raw field (float64,
     Fortran-ordered [x, y, z, gate]), the normalised field, per-thread energies,
     detected-photon records, seeds, stats and event counters."""
-    inp, keep = make_input(cfg, nthread, core, mathmode, variant, fieldmode, nworkers)
+    inp, keep = make_input(cfg, nthread, core, mathmode, variant, fieldmode, nworkers, seedskip)
     L = lib()
     fieldlen = L.mcxo_fieldlen(ctypes.byref(inp)) * L.mcxo_fieldcomp(ctypes.byref(inp))
     reclen = L.mcxo_reclen(ctypes.byref(inp))

@@ -301,3 +301,33 @@ def test_dref_only_when_saved(gpu):
     assert "dref" in on and "dref" not in off
     assert on["dref"].shape == on["flux"].shape and np.all(on["dref"] >= 0)
     assert np.any(on["dref"] > 0)
+
+
+def test_exact_kernel_respin_matches_oracle(gpu, O):
+    """respin = 2: each repetition runs nphoton / 2 photons (mcx_host.cpp:
+    1101-1102) from the next 4 x threads seed words (759-768, 1319-1330) and
+    the fields, energies and records add up: the exact kernel's records,
+    event counts and energies equal two oracle runs, the second drawing its
+    seed words after the first's."""
+    cfg = cases.small_two_media(nphoton=4000)
+    nthread = 256
+    g = _gpu_run(dict(cfg, respin=2), nthread, exactmath=1)
+    half = dict(cfg, nphoton=2000)
+    kw = dict(nthread=nthread, core=gpu["core"], mathmode=O.MATH_PMATH, variant=O.VARIANT_OPENCL,
+              fieldmode=O.FIELD_DOUBLE)
+    r0 = O.run(half, **kw)
+    r1 = O.run(half, seedskip=4 * nthread, **kw)
+    assert g["stat"]["nphoton"] == 8000          # the reference module's count (src/pmcxcl.cpp:1497)
+    assert g["stat"]["detected"] == r0["stat"]["detected"] + r1["stat"]["detected"]
+    ev = g["stat"]["eventcount"]
+    for k, o in (("step", "nstep"), ("scatter", "nscatter"), ("launch", "nlaunch"), ("reflect", "nreflect")):
+        assert ev[k] == r0["stat"][o] + r1["stat"][o], k
+    assert g["stat"]["energytot"] == pytest.approx(r0["stat"]["energytot"] + r1["stat"]["energytot"], rel=1e-12)
+    rg, sg = _sorted_records(g["detp"], g["seeds"].T)
+    both = [np.asarray(r["detp"]) for r in (r0, r1) if r["detp"].size]
+    sds = [np.ascontiguousarray(r["seeds"]).view(np.uint8).reshape(-1, 16) for r in (r0, r1) if r["detp"].size]
+    rc, sc = _sorted_records(np.concatenate(both, axis=1), np.concatenate(sds, axis=0))
+    assert np.array_equal(rg, rc) and np.array_equal(sg, sc)
+    raw = np.asarray(r0["field_raw"]) + np.asarray(r1["field_raw"])
+    flux = (g["flux"] / g["stat"]["normalizer"]).reshape(raw.shape, order="F")
+    np.testing.assert_allclose(flux, raw, rtol=1e-4, atol=1e-6 * raw.max())
