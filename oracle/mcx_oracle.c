@@ -112,6 +112,11 @@ typedef struct {
     const float* rweight;
     const float* rtof;
     const int* rdetid;
+    /* trajectory capture */
+    int debugmove;
+    unsigned int maxtraj;
+    float* traj;
+    unsigned int* ntraj;
 } ocfg;
 
 typedef struct {
@@ -755,6 +760,30 @@ static inline void set_launch_voxel(const ocfg* c, ostate* s) {
  * (escaped weight, saved reflectance, detection) and launch the next one.
  * Returns 0 on launch, 1 when this thread's quota is done, -1 on failure.
  */
+/* savedebugdata (mcx_core.cl:929-948): one trajectory record at a slot taken
+   from a shared counter; the photon id is the thread's launch counter plus
+   the thread's photon offset, which the close record (1501) computes with
+   min(tid, oddphoton) and the launch and scattering records (2247, 2630)
+   with min(tid, (tid < oddphoton) tid) */
+static void save_traj(octx* X, const ostate* s, int closing) {
+    const ocfg* c = X->c;
+    const int tid = (int)X->tid, odd = c->oddphoton;
+    const int off = closing ? (tid < odd ? tid : odd) : (tid < (tid < odd) * tid ? tid : (tid < odd) * tid);
+    const uint32_t id = (uint32_t)s->f.w + (uint32_t)(tid * (int)c->threadphoton) + (uint32_t)off;
+    unsigned int pos;
+#pragma omp atomic capture
+    pos = (*c->ntraj)++;
+    if (pos < c->maxtraj) {
+        float* r = c->traj + (size_t)pos * 6;
+        memcpy(r, &id, sizeof(id));
+        r[1] = s->p.x;
+        r[2] = s->p.y;
+        r[3] = s->p.z;
+        r[4] = s->p.w;
+        r[5] = (float)(int)s->ppath[c->w0offset - 1];
+    }
+}
+
 static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
     const ocfg* c = X->c;
     const osrc* ls = &c->src;
@@ -770,6 +799,9 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
 
     if (fabsf(s->p.w) >= 0.f) {
         s->ppath[c->partialdata] += s->p.w;
+        if (c->debugmove) {
+            save_traj(X, s, 1);
+        }
         if (s->mediaid == 0 && s->idx1d != OUT_MIN && s->idx1d != OUT_MAX && c->issaveref && s->p.w > 0.f) {
             if (c->issaveref == 1) {
                 int tshift = (int)floorf((s->f.y - c->twin0) * c->Rtstep);
@@ -1216,6 +1248,9 @@ static int launchnewphoton(octx* X, ostate* s, uint32_t isdet) {
     } else {
         updateprop(c, &s->prop, s->mediaid);
     }
+    if (c->debugmove) {
+        save_traj(X, s, 0);      /* 2243-2249: the source slot is the launched photon's */
+    }
     pp[1] += s->p.w;
     s->w0 = s->p.w;
     pp[2] = ((c->srcnum > 1) ? pp[2] : s->p.w);
@@ -1390,6 +1425,9 @@ static void run_thread(octx* X, const uint32_t* seedwords, float* energy, unsign
                             field_add_im(X, (size_t)s.idx1d + (size_t)(long long)tshift * c->dimlen[2], tim, 1);
                         }
                     }
+                }
+                if (c->debugmove) {
+                    save_traj(X, &s, 0);      /* 2625-2634: scattering sites, not the first draw */
                 }
             }
             s.v.w = (float)(int)s.v.w;
@@ -2089,6 +2127,13 @@ static int prepare(const mcxo_input* in, oprep* P) {
     c.media = media;
     c.mathmode = in->mathmode;
     c.variant = in->variant;
+    c.debugmove = in->debugmove;
+    c.maxtraj = in->maxtraj;
+    c.traj = in->traj_out;
+    c.ntraj = in->ntraj_out;
+    if (c.debugmove && (!c.traj || !c.ntraj)) {
+        return -3;
+    }
     c.fieldmode = in->fieldmode;
     c.nthread = in->nthread;
     c.omega = in->omega;

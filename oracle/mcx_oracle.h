@@ -136,6 +136,14 @@ typedef struct mcxo_input {
        later repetition of a respin run draws after the earlier ones'
        4 x nthread words each (mcx_host.cpp:759-768 inside the respin loop) */
     unsigned int seedskip;
+
+    /* trajectory capture (-D M, mcx_core.cl:929-948): records of 6 floats
+       {photon id (uint bits), x, y, z, w, source id} at every photon close,
+       launch and scattering site; at most maxtraj stored, *ntraj counts all */
+    int debugmove;
+    unsigned int maxtraj;
+    float* traj_out;
+    unsigned int* ntraj_out;
 } mcxo_input;
 
 typedef struct mcxo_stats {

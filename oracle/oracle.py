@@ -62,6 +62,8 @@ class MCXOInput(ctypes.Structure):
         ("replaysiteown", ctypes.c_int), ("detweight_out", ctypes.c_void_p), ("omega", ctypes.c_float),
         ("smatrix", ctypes.c_void_p), ("polmedianum", ctypes.c_uint), ("s0", ctypes.c_float * 4),
         ("seedskip", ctypes.c_uint),
+        ("debugmove", ctypes.c_int), ("maxtraj", ctypes.c_uint), ("traj_out", ctypes.c_void_p),
+        ("ntraj_out", ctypes.c_void_p),
     ]
 
 
@@ -262,6 +264,13 @@ def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT
     inp.nthread = int(nthread)
     inp.core = int(core if core is not None else nthread)
     inp.debugrng = int("R" in str(cfg.get("debuglevel", "")).upper())
+    inp.debugmove = int("M" in str(cfg.get("debuglevel", "")).upper())
+    if inp.debugmove:
+        inp.maxtraj = int(cfg.get("maxjumpdebug", 10000000))
+        keep["traj"] = np.zeros(max(1, inp.maxtraj) * 6, np.float32)
+        keep["ntraj"] = np.zeros(1, np.uint32)
+        inp.traj_out = _ptr(keep["traj"])
+        inp.ntraj_out = _ptr(keep["ntraj"])
     inp.mathmode = mathmode
     inp.variant = variant
     inp.fieldmode = fieldmode
@@ -356,6 +365,11 @@ def run(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT_OPENCL
         "stat": {k: getattr(st, k) for k, _ in MCXOStats._fields_},
         "gates": gates,
     }
+    if inp.debugmove:
+        # trajectory records [6, n] as the reference module returns them (src/pmcxcl.cpp:1266-1282)
+        n = min(int(keep["ntraj"][0]), inp.maxtraj)
+        out["traj"] = keep["traj"][:6 * n].reshape(n, 6).T.copy()
+        out["ntraj"] = int(keep["ntraj"][0])
     if inp.seed == SEED_FROM_FILE:
         n = inp.nreplay
         out["replay"] = {"weight": keep["rw"][:n].copy(), "tof": keep["rtof"][:n].copy(),
@@ -383,13 +397,18 @@ def run_reference(cfg, nthread=4096, core=None, nblocksize=64, nworkers=1):
         raise RuntimeError("reference harness failed with code %d" % rc)
     nsaved = min(cnt.value, maxdet)
     shape = (inp.dimx, inp.dimy, inp.dimz, -1)
-    return {
+    out = {
         "field_raw": field.reshape(shape, order="F"),
         "energy": energy.reshape(-1, 2),
         "detp": detp[:nsaved * reclen].reshape(nsaved, reclen).T if reclen else np.zeros((0, 0), np.float32),
         "seeds": seeds[:2 * nsaved].reshape(nsaved, 2) if inp.issaveseed else None,
         "detected": cnt.value,
     }
+    if inp.debugmove:
+        n = min(int(keep["ntraj"][0]), inp.maxtraj)
+        out["traj"] = keep["traj"][:6 * n].reshape(n, 6).T.copy()
+        out["ntraj"] = int(keep["ntraj"][0])
+    return out
 
 
 def cube60(**kw):

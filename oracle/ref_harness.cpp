@@ -22,6 +22,8 @@ struct ReplayBufs {
     float* weight = nullptr;
     float* tof = nullptr;
     int* detid = nullptr;
+    unsigned int* jump = nullptr;      /* trajectory capture (-D M): record counter and records */
+    float* debug = nullptr;
 };
 
 template <int ispencil, int isreflect, int issvmc>
@@ -49,7 +51,7 @@ static void run_blocks(const mcxo_refprep& R, unsigned int nblock, unsigned int 
             threadIdx = make_uint3(t, 0, 0);
             mcx_main_loop<ispencil, isreflect, !issvmc, issvmc, 0>(
                 media, field, genergy, seeds, detp, (const float4*)gprop, srcpattern, (const float4*)gdet,
-                &progress, detcount, rp.weight, rp.tof, rp.detid, gseed, nullptr, nullptr, (float*)invcdf, (float*)angleinvcdf,
+                &progress, detcount, rp.weight, rp.tof, rp.detid, gseed, rp.jump, rp.debug, (float*)invcdf, (float*)angleinvcdf,
                 (RandType*)sharedmem_raw, (float4*)R.smatrix);
         }
     }
@@ -119,6 +121,8 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     P.omega = R.omega;
     P.maxpolmedia = R.maxpolmedia;
     P.s0 = make_float4(R.s0[0], R.s0[1], R.s0[2], R.s0[3]);
+    P.debuglevel = in->debugmove ? 2u : 0u;    /* MCX_DEBUG_MOVE */
+    P.maxjumpdebug = in->maxtraj;
     P.nphase = R.nphase;
     P.nphaselen = R.nphase + (R.nphase & 1);
     P.nangle = R.nangle;
@@ -141,6 +145,16 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
        the reference's scattering-site deposits read one photon ahead */
     const bool replay = (in->seed == MCXO_SEED_FROM_FILE);
     ReplayBufs rp;
+    unsigned int jumpctr = 0;
+    std::vector<float> debugdata(in->debugmove ? 6 * (size_t)in->maxtraj + 6 : 0);
+    if (in->debugmove) {
+        if (!in->traj_out || !in->ntraj_out) {
+            mcxo_free_ref(&R);
+            return -3;
+        }
+        rp.jump = &jumpctr;
+        rp.debug = debugdata.data();
+    }
     std::vector<float> rweight, rtof;
     std::vector<int> rdetid;
     if (replay) {
@@ -220,6 +234,10 @@ extern "C" int mcxref_run(const mcxo_input* in, unsigned int nblocksize, int nwo
     }
     if (detcount_out) {
         *detcount_out = detcount;
+    }
+    if (in->debugmove) {
+        *in->ntraj_out = jumpctr;
+        std::memcpy(in->traj_out, debugdata.data(), sizeof(float) * 6 * (size_t)std::min(jumpctr, in->maxtraj));
     }
     mcxo_free_ref(&R);
     return 0;

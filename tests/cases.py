@@ -206,6 +206,20 @@ def twod(**kw):
     return cfg
 
 
+# trajectory capture (-D M): records at photon closes, launches and scattering sites
+TRAJ_PINS = [("traj", dict(nphoton=300, debuglevel="M", maxjumpdebug=100000)),
+             ("traj_multisrc", dict(VARIANTS["multisrc"], nphoton=300, debuglevel="M", maxjumpdebug=100000))]
+
+
+def traj_digest(traj):
+    """SHA-256 of trajectory records [6, n] in a canonical order (the record
+    slots come from an atomic counter)."""
+    import hashlib
+    t = np.ascontiguousarray(np.asarray(traj, np.float32).T).view(np.uint32)
+    t = t[np.lexsort(t.T[::-1])] if t.size else t
+    return hashlib.sha256(np.ascontiguousarray(t).tobytes()).hexdigest()
+
+
 def pin_cases():
     """(name, cfg, nthread) triples pinned against the reference kernel."""
     out = [("cube60", cube60(nphoton=3000), 256),

@@ -76,6 +76,10 @@ def main():
         r = oracle.run_reference(cfg, nthread=nthread, core=nthread, nblocksize=16)
         out[name] = dict(summarize(r), nthread=nthread)
         print(name, out[name]["ndet"], out[name]["field_sum"])
+    for name, kw in cases.TRAJ_PINS:
+        r = oracle.run_reference(cases.small_two_media(**kw), nthread=128, core=128)
+        out[name] = dict(summarize(r), nthread=128, ntraj=r["ntraj"], traj_sha=cases.traj_digest(r["traj"]))
+        print(name, r["ntraj"])
     with open(os.path.join(HERE, "ref_pins.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
 

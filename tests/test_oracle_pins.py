@@ -135,3 +135,19 @@ def test_oracle_polarized_matches_reference_bits(oracle_mod):
     assert _sha(np.asfortranarray(field).ravel(order="F").view(np.uint32)) == pin["field_sha"]
     assert r["detp"].shape[1] == pin["ndet"] and r["detp"].shape[0] == 1 + 3 * 2 + 3 + 3 + 1 + 4
     assert _sha(np.asarray(r["detp"], np.float32).view(np.uint32)) == pin["detp_sha"]
+
+
+@pytest.mark.skipif(platform.machine() not in ("x86_64", "AMD64"),
+                    reason="libm-mode digests were recorded with x86-64 glibc")
+@pytest.mark.parametrize("name,kw", cases.TRAJ_PINS)
+def test_oracle_trajectory_matches_reference_bits(oracle_mod, name, kw):
+    """Trajectory capture (-D M, mcx_core.cl:929-948, 1497-1503, 2243-2249,
+    2625-2634): the oracle's records at photon closes, launches and
+    scattering sites -- photon id, position, weight, source id -- equal the
+    reference kernel's, in a canonical order."""
+    O = oracle_mod
+    pin = PINS[name]
+    r = O.run(cases.small_two_media(**kw), nthread=pin["nthread"], core=pin["nthread"], mathmode=O.MATH_LIBM,
+              variant=O.VARIANT_NVCC, fieldmode=O.FIELD_FLOAT_SPILL)
+    assert r["ntraj"] == pin["ntraj"]
+    assert cases.traj_digest(r["traj"]) == pin["traj_sha"]
