@@ -215,6 +215,11 @@ typedef struct MCXConfig {
     float lambda;
     mcx_float4 srciquv;
     mcx_float4* smatrix;
+    /* trajectory capture (debuglevel M): records of 6 floats {photon id (uint
+       bits), x, y, z, w, source id}, at most maxjumpdebug per repetition */
+    unsigned int maxjumpdebug;
+    unsigned int debugdatalen;
+    float* exportdebugdata;
     int errorcode;                /* last error in library mode */
     char errormsg[256];
 } Config;
@@ -346,6 +351,11 @@ int  mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread);
    generator, in nblock blocks of blocklen words ((nblock - 1) x blocklen <
    4 x nthread <= nblock x blocklen), block j starting from the 31 words
    starts[31 j ..] that mcx_rand_blocks returns. */
+/* Trajectory capture (-D M): buffers for maxrec records (0: off); each
+   launch restarts the count.  get copies min(count, maxrec, capacity)
+   records and returns every record the launch made in *count. */
+int  mcxg_set_trajectory(mcxg_session* s, uint32_t maxrec);
+int  mcxg_get_trajectory(mcxg_session* s, float* out, uint32_t maxrec, uint32_t* count);
 int  mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock, uint32_t blocklen,
                          uint32_t nthread);
 /* Launch shape of the persistent grid (0 = automatic).  blocks_per_sm = 3

@@ -92,6 +92,8 @@ class Config(ctypes.Structure):
         ("omega", ctypes.c_float),
         ("polprop", ctypes.POINTER(ctypes.c_float)), ("polmedianum", ctypes.c_uint), ("lambda_", ctypes.c_float),
         ("srciquv", Float4), ("smatrix", ctypes.POINTER(Float4)),
+        ("maxjumpdebug", ctypes.c_uint), ("debugdatalen", ctypes.c_uint),
+        ("exportdebugdata", ctypes.POINTER(ctypes.c_float)),
         ("errorcode", ctypes.c_int),
         ("errormsg", ctypes.c_char * 256),
     ]
@@ -110,7 +112,7 @@ EXPORTS = [
     "mcx_normalize", "mcx_error", "mcx_last_error", "mcx_detreclen", "mcx_version", "mcx_rand_words", "mcx_rand_blocks", "mcx_config_sizeof",
     "mcx_config_offsetof", "mcx_release_sessions", "mcx_prepare_simulation",
     "mcxg_device_count", "mcxg_device_info", "mcxg_error_string", "mcxg_create", "mcxg_destroy",
-    "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_seeds_lfib", "mcxg_set_launch", "mcxg_simulate",
+    "mcxg_set_problem", "mcxg_set_params", "mcxg_set_seeds", "mcxg_set_seeds_lfib", "mcxg_set_trajectory", "mcxg_get_trajectory", "mcxg_set_launch", "mcxg_simulate",
     "mcxg_get_energy", "mcxg_get_thread_energy", "mcxg_get_field", "mcxg_get_field_f64", "mcxg_get_detected",
     "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc", "mcxg_autotune",
     "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_field_interleaved", "mcxg_set_polarization", "mcx_mie", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",

@@ -48,6 +48,10 @@ struct mcxg_session {
     size_t pattern_cap = 0;
     uint4* d_seeds = nullptr;
     size_t seeds_cap = 0;
+    unsigned int* d_jump = nullptr;  /* trajectory capture: record counter and records */
+    float* d_traj = nullptr;
+    size_t traj_cap = 0, jump_cap = 0;
+    uint32_t maxjump = 0;
     uint32_t* d_lfib = nullptr;      /* 31-word generator windows, one per block of seed words */
     size_t lfib_cap = 0;
     float* d_field = nullptr;        /* 2 x fieldlen */
@@ -537,7 +541,7 @@ int mcxg_destroy(mcxg_session* s) {
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
                     s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw,
                     s->d_sims, s->d_simvt, s->d_simctr, s->d_smatrix, s->d_bmedia, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
-                    s->d_adj, s->d_lfib};
+                    s->d_adj, s->d_lfib, s->d_jump, s->d_traj};
     if (s->bgraph_exec) {
         cudaGraphExecDestroy(s->bgraph_exec);
     }
@@ -739,6 +743,42 @@ int mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock
     return MCXG_OK;
 }
 
+int mcxg_set_trajectory(mcxg_session* s, uint32_t maxrec) {
+    if (!s) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    s->maxjump = 0;
+    if (maxrec) {
+        int rc = ensure(&s->d_jump, &s->jump_cap, 1);
+        if (!rc) {
+            rc = ensure(&s->d_traj, &s->traj_cap, 6 * (size_t)maxrec);
+        }
+        if (rc) {
+            return rc;
+        }
+        s->maxjump = maxrec;
+    }
+    return MCXG_OK;
+}
+
+int mcxg_get_trajectory(mcxg_session* s, float* out, uint32_t maxrec, uint32_t* count) {
+    if (!s || !count || (maxrec && !out) || !s->maxjump) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    unsigned int n = 0;
+    MCXG_TRY(cudaMemcpyAsync(&n, s->d_jump, sizeof(n), cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    *count = n;
+    const size_t take = (size_t)(n < s->maxjump ? n : s->maxjump) < maxrec ? (n < s->maxjump ? n : s->maxjump) : maxrec;
+    if (take) {
+        MCXG_TRY(cudaMemcpyAsync(out, s->d_traj, sizeof(float) * 6 * take, cudaMemcpyDeviceToHost, s->st));
+        MCXG_TRY(cudaStreamSynchronize(s->st));
+    }
+    return MCXG_OK;
+}
+
 int mcxg_set_replay(mcxg_session* s, const void* seeds16, const float* weight, const float* tof, const int* detid,
                     uint32_t n) {
     if (!s || (n && (!seeds16 || !weight || !tof || !detid))) {
@@ -832,6 +872,12 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     a.smatrix = s->d_smatrix;
     a.s0 = s->pol_s0;
     a.maxpol = s->npol;
+    a.jumpctr = s->d_jump;
+    a.traj = s->d_traj;
+    a.maxjump = s->maxjump;
+    if (s->maxjump) {
+        MCXG_TRY(cudaMemsetAsync(s->d_jump, 0, sizeof(unsigned int), s->st));
+    }
     a.energy = s->d_energy;
     a.detp = s->d_detp;
     a.detseed = s->d_detseed;
@@ -857,7 +903,7 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     const bool xmedia = !rf && !svmc && kp.mediaformat > 4 && kp.mediaformat != 101;
     /* the instantiations that fix the common configuration's parameters */
     const bool common = !rf && !pol && !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2 &&
-                        kp.srcnum <= 1;
+                        kp.srcnum <= 1 && !s->maxjump;
     const int bpsm_sel = (xmedia || rf || pol || svmc) ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
                  (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |

@@ -101,6 +101,7 @@ void mcx_initcfg(Config* cfg) {
     cfg->isnormalized = 1;
     cfg->issavedet = 1;
     cfg->respin = 1;
+    cfg->maxjumpdebug = 10000000;
     cfg->issave2pt = 1;
     cfg->unitinmm = 1.f;
     cfg->flog = stdout;
@@ -151,8 +152,11 @@ void mcx_clearcfg(Config* cfg) {
     memset(&cfg->replay, 0, sizeof(cfg->replay));
     free(cfg->polprop);
     free(cfg->smatrix);
+    free(cfg->exportdebugdata);
     cfg->polprop = NULL;
     cfg->smatrix = NULL;
+    cfg->exportdebugdata = NULL;
+    cfg->debugdatalen = 0;
     cfg->polmedianum = 0;
     cfg->exportenergy = NULL;
     cfg->prop = NULL;
@@ -1322,6 +1326,9 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     }
     cfg->detectedcount = 0;
     cfg->his.detected = 0;
+    free(cfg->exportdebugdata);
+    cfg->exportdebugdata = NULL;
+    cfg->debugdatalen = 0;
     cfg->his.respin = cfg->respin;
     cfg->his.colcount = hostdetreclen;
     cfg->energytot = 0.0;
@@ -1377,8 +1384,32 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
             flags |= tc->noagg ? MCXG_NOAGG : MCXG_AGG;
         }
         float kms = 0.f;
+        if (iter == 0) {
+            device_check(mcxg_set_trajectory(s, (cfg->debuglevel & 2) ? cfg->maxjumpdebug : 0u),
+                         "allocating the trajectory records");
+        }
         device_check(mcxg_simulate(s, flags, &kms), "running the transport kernel");
         kms_total += kms;
+        if ((cfg->debuglevel & 2) && cfg->maxjumpdebug) {
+            /* append this repetition's records (mcx_host.cpp:1175-1192) */
+            uint32_t made = 0;
+            device_check(mcxg_get_trajectory(s, NULL, 0, &made), "reading the trajectory count");
+            const uint32_t take = made < cfg->maxjumpdebug ? made : cfg->maxjumpdebug;
+            if (made > cfg->maxjumpdebug) {
+                fprintf(stderr, "WARNING: the saved trajectory positions (%u) are more than maxjumpdebug (%u)\n",
+                            made, cfg->maxjumpdebug);
+            }
+            float* grown = (float*)realloc(cfg->exportdebugdata, sizeof(float) * 6 * ((size_t)cfg->debugdatalen + take + 1));
+            if (!grown) {
+                MCX_ERROR(-2, "out of host memory");
+            }
+            cfg->exportdebugdata = grown;
+            if (take) {
+                device_check(mcxg_get_trajectory(s, grown + (size_t)6 * cfg->debugdatalen, take, &made),
+                             "reading the trajectory records");
+            }
+            cfg->debugdatalen += take;
+        }
 
         double esc = 0.0, tot = 0.0;
         device_check(mcxg_get_energy(s, &esc, &tot), "reducing energies");
@@ -1674,7 +1705,7 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
         Config* cfg = cfgs[k];
         if (!cfg || cfg->issavedet || cfg->seed == SEED_FROM_FILE || cfg->extrasrclen || cfg->nphase || cfg->nangle ||
                 cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D || cfg->mediabyte > 4 || cfg->omega > 0.f || cfg->polmedianum ||
-                cfg->medianum > MCXG_BATCH_MAXMEDIA || cfg->respin != 1 || cfg->issaveref || (cfg->debuglevel & 1)) {
+                cfg->medianum > MCXG_BATCH_MAXMEDIA || cfg->respin != 1 || cfg->issaveref || (cfg->debuglevel & 3)) {
             MCX_ERROR(-4, "a batch simulation takes label volumes of at most 4 property rows, one respin, and no "
                       "detectors, replay, extra sources, patterns, phase tables, saved reflectance or RF");
         }
@@ -1846,7 +1877,7 @@ static const struct {
     MCX_FIELD(failedlaunch), MCX_FIELD(threadused), MCX_FIELD(exportenergy), MCX_FIELD(savethreadenergy),
     MCX_FIELD(autotune), MCX_FIELD(savedetweight), MCX_FIELD(exportdetweight), MCX_FIELD(replaysiteown), MCX_FIELD(omega),
     MCX_FIELD(polprop), MCX_FIELD(polmedianum), {"lambda_", offsetof(Config, lambda)}, MCX_FIELD(srciquv),
-    MCX_FIELD(smatrix), MCX_FIELD(errorcode), MCX_FIELD(errormsg),
+    MCX_FIELD(smatrix), MCX_FIELD(maxjumpdebug), MCX_FIELD(debugdatalen), MCX_FIELD(exportdebugdata), MCX_FIELD(errorcode), MCX_FIELD(errormsg),
 };
 
 size_t mcx_config_sizeof(void) {

@@ -1018,6 +1018,28 @@ __device__ __forceinline__ void set_launch_voxel(const KArgs& a, const PS& ps, P
     }
 }
 
+/* savedebugdata (mcx_core.cl:929-948): one trajectory record {photon id
+   (uint bits), x, y, z, w, source id} at a slot from a global counter.  The
+   id is the reference thread's launch counter plus its photon offset, which
+   the close record computes with min(tid, oddphoton) (1501) and the launch
+   and scattering records with min(tid, (tid < oddphoton) tid) (2247, 2630). */
+__device__ __forceinline__ void save_traj(const KArgs& a, const mcxg_kparams& c_p, const Photon& s, float srcsel,
+                                          unsigned int vt, bool closing) {
+    const int tid = (int)vt, odd = c_p.oddphoton, x = (tid < odd) * tid;
+    const int off = closing ? min(tid, odd) : min(tid, x);
+    const unsigned int id = (unsigned int)s.f.w + (unsigned int)(tid * (int)c_p.threadphoton) + (unsigned int)off;
+    const unsigned int pos = atomicAdd(a.jumpctr, 1u);
+    if (pos < a.maxjump) {
+        float* r = a.traj + (size_t)pos * 6;
+        r[0] = __uint_as_float(id);
+        r[1] = s.p.x;
+        r[2] = s.p.y;
+        r[3] = s.p.z;
+        r[4] = s.p.w;
+        r[5] = (float)(int)srcsel;
+    }
+}
+
 /*
  * launchnewphoton (mcx_core.cl:1463-2275): close the current photon (escaped
  * weight, saved reflectance, detection) and launch the next one of this
@@ -1039,6 +1061,9 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
 
     if (fabsf(s.p.w) >= 0.f) {
         ps.cold()->esc += s.p.w;
+        if (!PS::kCommon && !PS::kBatch && a.maxjump) {
+            save_traj(a, ps.p(), s, ps.cold()->srcsel, vt, true);
+        }
         if (s.mediaid == 0 && s.idx1d != K_OUT_MIN && s.idx1d != K_OUT_MAX && c_p.issaveref && s.p.w > 0.f) {
             int tshift = (int)floorf((s.f.y - c_p.twin0) * c_p.Rtstep);
             if ((int)c_p.maxgate - 1 < tshift) {
@@ -1455,6 +1480,9 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
     } else {
         updateprop(ps, S, s.prop, s.mediaid);
     }
+    if (!PS::kCommon && !PS::kBatch && a.maxjump) {
+        save_traj(a, ps.p(), s, ps.cold()->srcsel, vt, false);      /* 2243-2249 */
+    }
     ps.cold()->launched += s.p.w;
     s.w0 = s.p.w;
     if (!KP_SHARING) {
@@ -1749,6 +1777,9 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 if (c_p.replay && (c_p.outputtype == otWP || c_p.outputtype == otDCS || c_p.outputtype == otWPTOF ||
                                    c_p.outputtype == otRFmus)) {
                     replay_site_deposit(a, ps, S, s, vt, ctheta);
+                }
+                if (!PS::kCommon && !PS::kBatch && a.maxjump) {
+                    save_traj(a, c_p, s, ps.cold()->srcsel, vt, false);      /* 2625-2634 */
                 }
             }
             s.v.w = (float)(int)s.v.w;

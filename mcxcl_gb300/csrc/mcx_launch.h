@@ -46,6 +46,11 @@ struct KArgs {
     const float4* smatrix;
     float4 s0;
     unsigned int maxpol;
+    /* trajectory capture (-D M): record counter, records of 6 floats, capacity
+       (0: off; only the general single-simulation instantiations record) */
+    unsigned int* jumpctr;
+    float* traj;
+    unsigned int maxjump;
 };
 
 /* flag bits for the launch entries */

@@ -28,7 +28,7 @@ OUTPUTTYPES = ["flux", "fluence", "energy", "jacobian", "nscat", "wl", "wp", "wm
 SAVEFLAGS = "DSPMXVWI"
 DEBUGFLAGS = "RMP"
 
-_SCALARS_INT = ["nphoton", "nblocksize", "nthread", "maxdetphoton", "maxgate", "respin", "isreflect", "isrefint",
+_SCALARS_INT = ["nphoton", "nblocksize", "nthread", "maxdetphoton", "maxgate", "maxjumpdebug", "respin", "isreflect", "isrefint",
                 "isnormalized", "isgpuinfo", "issrcfrom0", "autopilot", "voidtime", "issaveref", "maxvoidstep",
                 "gscatter", "srcnum", "srcid", "isatomic", "internalsrc", "issavedet", "exactmath",
                 "savethreadenergy", "autotune"]
@@ -458,6 +458,11 @@ def _outputs(cfg, C):
         j = np.ctypeslib.as_array(C.exportjacob, shape=(n * len(names),)).copy()
         for k, name in enumerate(names):
             out[name] = j[k * n:(k + 1) * n].reshape((C.dim.x, C.dim.y, C.dim.z, npair), order="F")
+    if (C.debuglevel & 2) and C.exportdebugdata:
+        # trajectory records [6, n] (src/pmcxcl.cpp:1266-1282): photon id as uint bits, x, y, z, w, source id
+        n = C.debugdatalen
+        tr = np.ctypeslib.as_array(C.exportdebugdata, shape=(max(n, 1) * 6,))[:n * 6].copy()
+        out["traj"] = tr.reshape(n, 6).T
     if C.savethreadenergy and C.exportenergy:
         e = np.ctypeslib.as_array(C.exportenergy, shape=(2 * C.threadused,)).copy()
         out["threadenergy"] = e.reshape(C.threadused, 2)

@@ -331,3 +331,22 @@ def test_exact_kernel_respin_matches_oracle(gpu, O):
     raw = np.asarray(r0["field_raw"]) + np.asarray(r1["field_raw"])
     flux = (g["flux"] / g["stat"]["normalizer"]).reshape(raw.shape, order="F")
     np.testing.assert_allclose(flux, raw, rtol=1e-4, atol=1e-6 * raw.max())
+
+
+@pytest.mark.parametrize("name,kw", cases.TRAJ_PINS)
+def test_exact_kernel_trajectory_matches_oracle(gpu, O, name, kw):
+    """Trajectory capture (debuglevel M): the exact kernel's records at photon
+    closes, launches and scattering sites equal the oracle's (ids, positions,
+    weights, source ids), in a canonical order; the fast kernel records the
+    same kinds of points."""
+    import mcxcl_gb300
+    cfg = cases.small_two_media(**kw)
+    nthread = 128
+    g = _gpu_run(cfg, nthread, exactmath=1)
+    r = O.run(cfg, nthread=nthread, core=gpu["core"], mathmode=O.MATH_PMATH, variant=O.VARIANT_OPENCL,
+              fieldmode=O.FIELD_DOUBLE)
+    assert g["traj"].shape == r["traj"].shape and g["traj"].shape[1] > 1000
+    assert cases.traj_digest(g["traj"]) == cases.traj_digest(r["traj"])
+    f = mcxcl_gb300.run(dict(cfg, nphoton=3000))
+    assert f["traj"].shape[0] == 6 and f["traj"].shape[1] > 3 * 3000
+    assert np.all((f["traj"][4] > 0) & (f["traj"][4] <= 1))
