@@ -1385,12 +1385,13 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
         }
         float kms = 0.f;
         if (iter == 0) {
-            device_check(mcxg_set_trajectory(s, (cfg->debuglevel & 2) ? cfg->maxjumpdebug : 0u),
+            /* MCX_DEBUG_MOVE (2) and MCX_DEBUG_MOVE_ONLY (8) both record (mcx_host.cpp:702, 1173) */
+            device_check(mcxg_set_trajectory(s, (cfg->debuglevel & 10) ? cfg->maxjumpdebug : 0u),
                          "allocating the trajectory records");
         }
         device_check(mcxg_simulate(s, flags, &kms), "running the transport kernel");
         kms_total += kms;
-        if ((cfg->debuglevel & 2) && cfg->maxjumpdebug) {
+        if ((cfg->debuglevel & 10) && cfg->maxjumpdebug) {
             /* append this repetition's records (mcx_host.cpp:1175-1192) */
             uint32_t made = 0;
             device_check(mcxg_get_trajectory(s, NULL, 0, &made), "reading the trajectory count");
@@ -1705,7 +1706,7 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
         Config* cfg = cfgs[k];
         if (!cfg || cfg->issavedet || cfg->seed == SEED_FROM_FILE || cfg->extrasrclen || cfg->nphase || cfg->nangle ||
                 cfg->srctype == MCX_SRC_PATTERN || cfg->srctype == MCX_SRC_PATTERN3D || cfg->mediabyte > 4 || cfg->omega > 0.f || cfg->polmedianum ||
-                cfg->medianum > MCXG_BATCH_MAXMEDIA || cfg->respin != 1 || cfg->issaveref || (cfg->debuglevel & 3)) {
+                cfg->medianum > MCXG_BATCH_MAXMEDIA || cfg->respin != 1 || cfg->issaveref || (cfg->debuglevel & 11)) {
             MCX_ERROR(-4, "a batch simulation takes label volumes of at most 4 property rows, one respin, and no "
                       "detectors, replay, extra sources, patterns, phase tables, saved reflectance or RF");
         }

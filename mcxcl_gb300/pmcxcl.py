@@ -26,7 +26,7 @@ OUTPUTTYPES = ["flux", "fluence", "energy", "jacobian", "nscat", "wl", "wp", "wm
                "wltof", "wptof", "adjoint", "adjoint_dcoeff", "adjoint_mus", "adjoint_musp", "adjoint_mua_d",
                "adjoint_mua_musp"]
 SAVEFLAGS = "DSPMXVWI"
-DEBUGFLAGS = "RMP"
+DEBUGFLAGS = "RMPT"        # R: RNG stream, M: trajectories, P: progress, T: trajectories only (mcx_utils.c:117)
 
 _SCALARS_INT = ["nphoton", "nblocksize", "nthread", "maxdetphoton", "maxgate", "maxjumpdebug", "respin", "isreflect", "isrefint",
                 "isnormalized", "isgpuinfo", "issrcfrom0", "autopilot", "voidtime", "issaveref", "maxvoidstep",
@@ -458,7 +458,7 @@ def _outputs(cfg, C):
         j = np.ctypeslib.as_array(C.exportjacob, shape=(n * len(names),)).copy()
         for k, name in enumerate(names):
             out[name] = j[k * n:(k + 1) * n].reshape((C.dim.x, C.dim.y, C.dim.z, npair), order="F")
-    if (C.debuglevel & 2) and C.exportdebugdata:
+    if (C.debuglevel & 10) and C.exportdebugdata:
         # trajectory records [6, n] (src/pmcxcl.cpp:1266-1282): photon id as uint bits, x, y, z, w, source id
         n = C.debugdatalen
         tr = np.ctypeslib.as_array(C.exportdebugdata, shape=(max(n, 1) * 6,))[:n * 6].copy()

@@ -264,7 +264,7 @@ def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT
     inp.nthread = int(nthread)
     inp.core = int(core if core is not None else nthread)
     inp.debugrng = int("R" in str(cfg.get("debuglevel", "")).upper())
-    inp.debugmove = int("M" in str(cfg.get("debuglevel", "")).upper())
+    inp.debugmove = int(any(k in str(cfg.get("debuglevel", "")).upper() for k in "MT"))
     if inp.debugmove:
         inp.maxtraj = int(cfg.get("maxjumpdebug", 10000000))
         keep["traj"] = np.zeros(max(1, inp.maxtraj) * 6, np.float32)
