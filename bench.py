@@ -27,6 +27,16 @@ persistent launch against one launch per simulation; "gradient" -- forward
 and replay-backward times of the differentiation workload and the backward
 pass's agreement with central differences.
 
+Also: "c1" and "c3" -- the homogeneous cube and the synthetic layered head
+(181 x 217 x 181, five labels, 16 detectors, roulette), each with its own
+photons/ms, FP32-issue roofline and DRAM traffic; "precision" (with
+--precision P) -- the error of the two-plane field, a plain float field and
+the reference's spill field against an FP64 accumulation of the same P
+photons on the cube and the cube + sphere workloads.
+
+--launches N --config K: profiling mode, N launches of workload K on
+resident data (one line per launch), for a profiler to capture.
+
 --impl reference times the reference's CPU path (the oracle, since the
 reference's OpenCL build does not run on this machine) on the host cores.
 Multi-GPU: replicas only (photons do not exchange anything); each rank runs
@@ -51,7 +61,10 @@ sys.path.insert(0, ROOT)
 OPS_PER_STEP, OPS_PER_SCATTER, OPS_PER_LAUNCH, OPS_PER_REFLECT = 48, 65, 20, 10
 MUFU_PER_STEP, MUFU_PER_SCATTER = 6, 11
 MUFU_PER_SM_CLK = 16          # special-function results per SM per clock
-TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_mcx_transport_config2.txt")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_mcx_transport_config%d.txt")
+# one name for the headline workload, printed by both arms
+WORKLOAD = ("60^3 cube + r15 sphere (label 2), Fresnel on, 50 gates x 0.1 ns, 4 r=1 detectors on z=0 saving "
+            "detid/nscat/ppath + seeds, pencil (29,29,0) +z, 1e8 photons per step")
 
 
 def parse_args():
@@ -65,6 +78,14 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-sims", type=int, default=512, help="simulations in the batched comparison (0: skip)")
     ap.add_argument("--no-gradient", action="store_true", help="skip the replay-gradient timing")
+    ap.add_argument("--no-configs", action="store_true", help="skip the cube and head sub-measurements")
+    ap.add_argument("--precision", type=float, default=0, help="photons of the FP64 precision check (0: skip)")
+    # profiling mode
+    ap.add_argument("--launches", type=int, default=0, help="profiling mode: launches of --config on resident data")
+    ap.add_argument("--config", type=int, default=2, help="profiling mode: 1 cube, 2 cube + sphere, 3 head")
+    ap.add_argument("--block", type=int, default=0, help="profiling mode: threads per block (0: automatic)")
+    ap.add_argument("--blocks-per-sm", type=int, default=0, help="profiling mode: resident blocks per SM")
+    ap.add_argument("--flags", type=int, default=0, help="profiling mode: mcxg_simulate flags")
     return ap.parse_args()
 
 
@@ -273,14 +294,169 @@ def run_reference_arm(args, rank, world):
         "impl": "reference", "metric": "photons/ms", "value": v, "unit": "photons/ms", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "60^3 cube + r15 sphere, Fresnel, 50x0.1ns gates, 4 detectors (dsp), "
-                               "%d photons per step" % int(cfg["nphoton"])},
+        "config": {"workload": WORKLOAD, "photons_per_step": int(cfg["nphoton"])},
         "cpu_baseline": dict(res, value=v),
         "e2e": {"value": v, "unit": "photons/ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's own CPU path is its OpenCL kernel, which needs an OpenCL CPU driver absent "
-                "from this box; the C restatement of that kernel (oracle/) is timed instead",
+                "from this box; the C restatement of that kernel (oracle/) is timed instead, on a bounded "
+                "sample of each step's photons (photons/ms is per-photon work, so the sample keeps the unit)",
     }
     print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- helpers
+
+def prepare(cfg):
+    """Validated Config and a device-resident session of one workload."""
+    import ctypes
+    from mcxcl_gb300 import _lib, pmcxcl
+    L = _lib.load()
+    C = _lib.Config()
+    pmcxcl.parse_config(cfg, C)
+    L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
+    pmcxcl._check(C)
+    sess = L.mcx_prepare_simulation(ctypes.byref(C))
+    pmcxcl._check(C)
+    return C, sess
+
+
+def simulate(sess, flags=0):
+    import ctypes
+    from mcxcl_gb300 import _lib
+    L = _lib.load()
+    ms = ctypes.c_float()
+    rc = L.mcxg_simulate(sess, flags, ctypes.byref(ms))
+    if rc:
+        raise RuntimeError(L.mcxg_error_string(rc).decode())
+    return ms.value
+
+
+def launch_shape(sess):
+    import ctypes
+    from mcxcl_gb300 import _lib
+    g, b, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _lib.load().mcxg_get_launch(sess, ctypes.byref(g), ctypes.byref(b), ctypes.byref(r))
+    return {"grid": g.value, "block": b.value, "regs": r.value}
+
+
+def event_model(cfg, sample):
+    """FP32 and MUFU operations per photon from the frozen model and the
+    exact kernel's event counts on a sample of the workload."""
+    import mcxcl_gb300
+    rx = mcxcl_gb300.run(dict(cfg, nphoton=int(sample), exactmath=1))
+    ev = rx["stat"]["eventcount"]
+    per = {k: ev[k] / float(sample) for k in ("step", "scatter", "launch", "reflect")}
+    ops = (OPS_PER_STEP * per["step"] + OPS_PER_SCATTER * per["scatter"] + OPS_PER_LAUNCH * per["launch"] +
+           OPS_PER_REFLECT * per["reflect"])
+    mufu = MUFU_PER_STEP * per["step"] + MUFU_PER_SCATTER * per["scatter"]
+    return per, ops, mufu
+
+
+def read_traffic(k):
+    path = TRAFFIC_FILE % k
+    if os.path.exists(path):
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_launch:"):
+                return float(ln.split(":")[1])
+    return None
+
+
+def roofline(per, ops, kms, nphoton, peak, k, sample):
+    achieved = ops * nphoton / (kms * 1e-3) / 1e9
+    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "Gop/s",
+            "frac": achieved / peak if peak else None, "traffic": read_traffic(k),
+            "peak_source": "measured in this run: 8-chain FMA kernel, one FMA = one op",
+            "ops_per_photon": ops, "events_per_photon": per,
+            "model": "48*step + 65*scatter + 20*launch + 10*Fresnel FP32 ops",
+            "events_from": "exact kernel (bit-identical to the oracle), %d-photon sample" % sample}
+
+
+def timed_launches(sess, steps, warmup, flush, flags=0):
+    """Kernel ms of `steps` launches after `warmup`, L2 flushed before each."""
+    import torch
+    for _ in range(max(3, warmup)):
+        simulate(sess, flags)
+    torch.cuda.synchronize()
+    kms = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        kms.append(simulate(sess, flags))
+    torch.cuda.synchronize()
+    return kms
+
+
+def config_measure(k, photons, steps, warmup, flush, peak):
+    """photons/ms, roofline and traffic of workload k (1 cube, 3 head) on resident data."""
+    from mcxcl_gb300 import _lib, workloads
+    import ctypes
+    cfg = workloads.config(k)
+    cfg["nphoton"] = int(photons)
+    C, sess = prepare(cfg)
+    try:
+        kms = timed_launches(sess, steps, warmup, flush)
+        shape = launch_shape(sess)
+    finally:
+        _lib.load().mcx_clearcfg(ctypes.byref(C))
+    ms = float(np.mean(kms))
+    sample = 2000000 if k == 3 else 5000000
+    per, ops, _ = event_model(cfg, sample)
+    return {"workload": workloads.describe(k), "photons_per_step": int(photons), "steps": steps,
+            "value": photons / ms, "unit": "photons/ms", "ms_per_step": ms, "launch": shape,
+            "roofline": roofline(per, ops, ms, photons, peak, k, sample)}
+
+
+def precision_measure(photons):
+    """Error of the two-plane field (the product), of a plain float field and
+    of the reference's +-1000 spill field against an FP64 accumulation of the
+    same deposits (one run, every deposit to all four), on the cube and the
+    cube + sphere workloads; relative error over every non-zero element."""
+    import ctypes
+    from mcxcl_gb300 import _lib, workloads
+    L = _lib.load()
+    out = {}
+    for k in (1, 2):
+        cfg = workloads.config(k)
+        cfg["nphoton"] = int(photons)
+        C, sess = prepare(cfg)
+        try:
+            simulate(sess, 128)                                   # MCXG_VERIFY
+            n = int(C.maxgate) * C.dim.x * C.dim.y * C.dim.z
+            two = np.zeros(n, np.float64)
+            f64 = np.zeros(n, np.float64)
+            plain = np.zeros(n, np.float32)
+            spill = np.zeros(n, np.float32)
+            L.mcxg_get_field_f64(sess, two.ctypes.data)
+            L.mcxg_get_verify(sess, f64.ctypes.data, plain.ctypes.data, spill.ctypes.data)
+        finally:
+            L.mcx_clearcfg(ctypes.byref(C))
+        nz = f64 > 0
+        res = {}
+        for name, x in (("two_plane", two), ("two_plane_float_output", two.astype(np.float32).astype(np.float64)),
+                        ("plain_float", plain.astype(np.float64)), ("reference_spill", spill.astype(np.float64))):
+            r = np.abs(x[nz] - f64[nz]) / f64[nz]
+            tot = abs(x.sum() - f64.sum()) / f64.sum()
+            res[name] = {"max": float(r.max()), "median": float(np.median(r)), "p99": float(np.quantile(r, 0.99)),
+                         "total": float(tot)}
+        out["config%d" % k] = dict(res, photons=int(photons), elements=int(nz.sum()))
+    return out
+
+
+def profile_mode(args):
+    """N launches of workload K on resident data, for a profiler to capture."""
+    import ctypes
+    from mcxcl_gb300 import _lib, workloads
+    L = _lib.load()
+    cfg = workloads.config(args.config)
+    if args.photons:
+        cfg["nphoton"] = int(args.photons)
+    C, sess = prepare(cfg)
+    if args.block or args.blocks_per_sm:
+        L.mcxg_set_launch(sess, args.block, args.blocks_per_sm)
+    for i in range(args.launches):
+        ms = simulate(sess, args.flags)
+        print("launch %d: %.3f ms, %.1f photons/ms" % (i, ms, cfg["nphoton"] / ms), flush=True)
+    L.mcx_clearcfg(ctypes.byref(C))
 
 
 def main():
@@ -292,22 +468,20 @@ def main():
     import ctypes
     import torch
     import mcxcl_gb300
-    from mcxcl_gb300 import _lib, pmcxcl
+    from mcxcl_gb300 import _lib
 
     torch.cuda.set_device(local)
     L = _lib.load()
+    if args.launches:
+        profile_mode(args)
+        return
     cfg = workload(args.photons)
     cfg["gpuid"] = local + 1
     cfg["seed"] = int(cfg["seed"]) + rank
     nphoton = int(cfg["nphoton"])
 
     # ---- device-resident session
-    C = _lib.Config()
-    pmcxcl.parse_config(cfg, C)
-    L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
-    pmcxcl._check(C)
-    sess = L.mcx_prepare_simulation(ctypes.byref(C))
-    pmcxcl._check(C)
+    C, sess = prepare(cfg)
     nthread = C.threadused
 
     # launch shape: the autotuner times the candidates on 2e6 photons of this workload
@@ -317,62 +491,41 @@ def main():
         raise RuntimeError(L.mcxg_error_string(rc).decode())
     tuned = {"block": tb.value, "blocks_per_sm": tp.value, "warp_aggregation": not tn.value}
 
-    def simulate(flags=0):
-        ms = ctypes.c_float()
-        rc = L.mcxg_simulate(sess, flags, ctypes.byref(ms))
-        if rc:
-            raise RuntimeError(L.mcxg_error_string(rc).decode())
-        return ms.value
-
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
     for _ in range(max(3, args.warmup)):
-        simulate()
+        simulate(sess)
     barrier(world)
     torch.cuda.synchronize()
     kms = []
     with ClockSampler(local) as clk:
-        t0 = time.perf_counter()
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            kms.append(simulate())
+            kms.append(simulate(sess))
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
     barrier(world)
     tot_ms = sum(kms)
     ms_per_step = allmax(tot_ms / args.steps, world)
     photons_all = allsum(nphoton * args.steps, world)
     value = photons_all / (ms_per_step * args.steps)
-    grid = ctypes.c_int()
-    block = ctypes.c_int()
-    regs = ctypes.c_int()
-    L.mcxg_get_launch(sess, ctypes.byref(grid), ctypes.byref(block), ctypes.byref(regs))
+    shape = launch_shape(sess)
 
     # ---- event counts from the exact kernel on a sample, and the FP32 peak
     sample = min(nphoton, 5000000)
-    cx = dict(cfg, nphoton=sample, exactmath=1)
-    rx = mcxcl_gb300.run(cx)
-    ev = rx["stat"]["eventcount"]
-    per_photon = {k: ev[k] / float(sample) for k in ("step", "scatter", "launch", "reflect")}
-    ops_per_photon = (OPS_PER_STEP * per_photon["step"] + OPS_PER_SCATTER * per_photon["scatter"] +
-                      OPS_PER_LAUNCH * per_photon["launch"] + OPS_PER_REFLECT * per_photon["reflect"])
+    per_photon, ops_per_photon, mufu_per_photon = event_model(cfg, sample)
     peak = ctypes.c_double()
-    sess2 = L.mcx_prepare_simulation(ctypes.byref(C))
-    L.mcxg_fp32_peak(sess2, ctypes.byref(peak))
-    achieved = ops_per_photon * nphoton / (tot_ms / args.steps * 1e-3) / 1e9
-    mufu_per_photon = MUFU_PER_STEP * per_photon["step"] + MUFU_PER_SCATTER * per_photon["scatter"]
-    mufu_achieved = mufu_per_photon * nphoton / (tot_ms / args.steps * 1e-3) / 1e9
+    L.mcxg_fp32_peak(sess, ctypes.byref(peak))
+    ms_avg = tot_ms / args.steps
     info = mcxcl_gb300.gpuinfo()[local]
     clock_summary = clk.summary()
     sm_mhz = clock_summary["sm_mhz"] or clock_summary["sm_max_mhz"] or 2070.0
+    mufu_achieved = mufu_per_photon * nphoton / (ms_avg * 1e-3) / 1e9
     mufu_peak = info["sm"] * MUFU_PER_SM_CLK * sm_mhz * 1e6 / 1e9
-    fp32_nominal = info["sm"] * 128 * sm_mhz * 1e6 / 1e9
-    traffic = None
-    if os.path.exists(TRAFFIC_FILE):
-        for ln in open(TRAFFIC_FILE):
-            if ln.startswith("dram_bytes_per_launch:"):
-                traffic = float(ln.split(":")[1])
+    roof = roofline(per_photon, ops_per_photon, ms_avg, nphoton, peak.value, 2, sample)
+    roof["fp32_nominal"] = info["sm"] * 128 * sm_mhz * 1e6 / 1e9
+    roof["mufu"] = {"achieved": mufu_achieved, "peak": mufu_peak, "unit": "Gop/s", "frac": mufu_achieved / mufu_peak,
+                    "model": "6*step + 11*scatter MUFU ops; peak 16/SM/clock at the sampled clock"}
 
     # ---- end to end through the public API, host buffers in and out
     e2e_steps = args.e2e_steps or max(2, min(args.steps, 3))
@@ -398,6 +551,11 @@ def main():
 
     out = None
     if rank == 0:
+        configs = None
+        if not args.no_configs:
+            configs = {"c1": config_measure(1, 1e8, 3, 2, flush, peak.value),
+                       "c3": config_measure(3, 1e8, 3, 1, flush, peak.value)}
+        precision = precision_measure(args.precision) if args.precision else None
         batched = batch_measure(args.batch_sims) if args.batch_sims > 0 else None
         gradient = None if args.no_gradient else gradient_measure()
         cpu = None if args.no_cpu_baseline else cpu_baseline(cfg)
@@ -406,33 +564,25 @@ def main():
             "metric": "photons/ms", "value": value, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "60^3 cube + r15 sphere (label 2), Fresnel on, 50 gates x 0.1 ns, 4 r=1 "
-                                   "detectors on z=0 saving detid/nscat/ppath, pencil (29,29,0) +z",
-                       "photons_per_step": nphoton, "reference_threads": nthread,
-                       "launch": {"grid": grid.value, "block": block.value, "regs": regs.value,
-                                  "autotuned": tuned},
+            "config": {"workload": WORKLOAD, "photons_per_step": nphoton, "reference_threads": nthread,
+                       "launch": dict(shape, autotuned=tuned),
                        "l2": "flushed between timed steps (256 MB write); working set < L2",
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "Gop/s",
-                         "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
-                         "peak_source": "measured in this run: 8-chain FMA kernel, one FMA = one op",
-                         "ops_per_photon": ops_per_photon, "events_per_photon": per_photon,
-                         "model": "48*step + 65*scatter + 20*launch + 10*Fresnel FP32 ops",
-                         "events_from": "exact kernel (bit-identical to the oracle), %d-photon sample" % sample,
-                         "fp32_nominal": fp32_nominal,
-                         "mufu": {"achieved": mufu_achieved, "peak": mufu_peak, "unit": "Gop/s",
-                                  "frac": mufu_achieved / mufu_peak,
-                                  "model": "6*step + 11*scatter MUFU ops; peak 16/SM/clock at the sampled clock"}},
+            "roofline": roof,
             "e2e": {"value": e2e_value, "unit": "photons/ms", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "cpu_baseline": cpu,
             "clocks": clock_summary,
             "gpu_launches": args.steps,
             "absorbed": absorbed,
-            "batched": batched,
-            "gradient": gradient,
             "detected_per_step": int(last["stat"]["detected"]),
         }
+        if configs:
+            out.update(configs)
+        if precision:
+            out["precision"] = precision
+        out["batched"] = batched
+        out["gradient"] = gradient
         print(json.dumps(out))
     L.mcx_clearcfg(ctypes.byref(C))
 

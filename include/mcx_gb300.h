@@ -315,6 +315,9 @@ void mcx_release_sessions(void);
 #define MCXG_GRAPH   32u   /* batch: capture the run as a CUDA graph once, replay it afterwards */
 #define MCXG_GENERAL 64u   /* fast kernel: the general instantiation even where the one specialised for the
                               common configuration (label volume, 3-D, Henyey-Greenstein) applies */
+#define MCXG_VERIFY 128u   /* precision check (fast kernel, common configuration, no replay, no KEEP): every
+                              deposit also goes to an FP64 field, a plain float field and a float field with
+                              the reference's +-1000 spill plane; read them with mcxg_get_verify */
 
 typedef struct mcxg_devinfo {
     char name[64];
@@ -423,6 +426,13 @@ int  mcxg_adjoint(mcxg_session* s, int kind, uint32_t ns, uint32_t nd, uint32_t 
                   uint32_t maxgate, float* out);
 /* Field: (hi + lo) in FP64, unscaled. */
 int  mcxg_get_field_f64(mcxg_session* s, double* out);
+/* The precision check's fields of the last MCXG_VERIFY launch, unscaled,
+   fieldlen values each (NULL skips one): the FP64 accumulation of the same
+   deposits, the plain float accumulation, and the spill accumulation with
+   its two planes added in float as the reference's host does
+   (src/mcx_core.cl:2880-2886, src/mcx_host.cpp:1252-1257).  No counterpart
+   in the reference: it exists to state the two-plane field's error. */
+int  mcxg_get_verify(mcxg_session* s, double* f64, float* plain, float* spill);
 /* Weight and time of flight (s) of each saved detected photon when it was
    detected, 2 floats per record, in record order. */
 int  mcxg_get_detweight(mcxg_session* s, float* out);
@@ -444,7 +454,8 @@ int  mcxg_fp32_peak(mcxg_session* s, double* gops);
  * mcxg_get_energy needs a session and a session allocates with cudaMalloc.
  * d_energy: device array of 2 x nthread floats {escaped, launched} per thread;
  * d_sums: device array receiving 2 doubles {escaped, launched}.  Runs on the
- * legacy default stream of `device` and returns after the sums are written.
+ * legacy default stream of `device` and returns after the sums are written;
+ * the calling thread's current device is the same on return as on entry.
  * Scratch: a static 64 KB device array, so nthread may not exceed 8,388,608
  * (MCXG_ERR_LIMIT beyond).  The first call on a device looks up that array's
  * device address (cudaGetSymbolAddress); make the first call before any

@@ -84,6 +84,12 @@ struct mcxg_session {
     bool out_valid = false;          /* d_out holds the last normalised float field */
     float* d_adj = nullptr;          /* adjoint Jacobians */
     size_t adj_cap = 0;
+    double* d_acc64 = nullptr;       /* precision check: FP64, plain float and spill fields */
+    size_t acc64_cap = 0;
+    float* d_accf = nullptr;
+    size_t accf_cap = 0;
+    float* d_accs = nullptr;         /* 2 x fieldlen */
+    size_t accs_cap = 0;
 
     /* batch of simulations in one persistent launch */
     std::vector<mcxg_simdesc> h_sims;
@@ -541,7 +547,7 @@ int mcxg_destroy(mcxg_session* s) {
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
                     s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw,
                     s->d_sims, s->d_simvt, s->d_simctr, s->d_smatrix, s->d_bmedia, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
-                    s->d_adj, s->d_lfib, s->d_jump, s->d_traj};
+                    s->d_adj, s->d_lfib, s->d_jump, s->d_traj, s->d_acc64, s->d_accf, s->d_accs};
     if (s->bgraph_exec) {
         cudaGraphExecDestroy(s->bgraph_exec);
     }
@@ -896,7 +902,8 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
 
     /* deposits go straight to the field unless aggregation is asked for or
        the autotuner found it faster for this problem */
-    const bool noagg = (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
+    const bool verify = (flags & MCXG_VERIFY) != 0;
+    const bool noagg = verify || (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
     const bool rf = kp.omega > 0.f && !kp.replay;
     const bool pol = s->npol > 0;
     const bool svmc = kp.mediaformat == 97;
@@ -908,7 +915,30 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
                  (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
                  (common ? mcxg::LF_COMMON : 0) | (rf ? mcxg::LF_RF : 0) | (pol ? mcxg::LF_POL : 0) |
-                 (svmc ? mcxg::LF_SVMC : 0);
+                 (svmc ? mcxg::LF_SVMC : 0) | (verify ? mcxg::LF_ACC64 : 0);
+    if (verify) {
+        /* the precision check runs the fast common-configuration instantiation */
+        if (exact || !common || kp.replay || (flags & MCXG_KEEP)) {
+            return MCXG_ERR_ARG;
+        }
+        const size_t n = kp.fieldlen;
+        int rc = ensure(&s->d_acc64, &s->acc64_cap, n);
+        if (!rc) {
+            rc = ensure(&s->d_accf, &s->accf_cap, n);
+        }
+        if (!rc) {
+            rc = ensure(&s->d_accs, &s->accs_cap, 2 * n);
+        }
+        if (rc) {
+            return rc;
+        }
+        MCXG_TRY(cudaMemsetAsync(s->d_acc64, 0, sizeof(double) * n, s->st));
+        MCXG_TRY(cudaMemsetAsync(s->d_accf, 0, sizeof(float) * n, s->st));
+        MCXG_TRY(cudaMemsetAsync(s->d_accs, 0, sizeof(float) * 2 * n, s->st));
+        a.acc64 = s->d_acc64;
+        a.accf = s->d_accf;
+        a.accs = s->d_accs;
+    }
     int block = s->block_req ? s->block_req : 256;
     size_t smem = shared_bytes(kp, block);
     if (smem > s->info.sharedmem_per_block) {
@@ -1171,6 +1201,34 @@ int mcxg_get_field_f64(mcxg_session* s, double* out) {
     s->out_valid = false;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(double) * total, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_get_verify(mcxg_session* s, double* f64, float* plain, float* spill) {
+    if (!s || !s->has_problem || !s->d_acc64 || s->acc64_cap < s->kp.fieldlen) {
+        return MCXG_ERR_STATE;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    const size_t n = s->kp.fieldlen;
+    if (f64) {
+        MCXG_TRY(cudaMemcpyAsync(f64, s->d_acc64, sizeof(double) * n, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (plain) {
+        MCXG_TRY(cudaMemcpyAsync(plain, s->d_accf, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+    }
+    std::vector<float> raw;
+    if (spill) {
+        raw.resize(2 * n);
+        MCXG_TRY(cudaMemcpyAsync(raw.data(), s->d_accs, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s->st));
+    }
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    if (spill) {
+        /* the reference's host merge of the two halves, in float
+           (mcx_host.cpp:1252-1257) */
+        for (size_t i = 0; i < n; i++) {
+            spill[i] = raw[i] + raw[i + n];
+        }
+    }
     return MCXG_OK;
 }
 
@@ -1506,15 +1564,8 @@ int mcxg_batch_get_field(mcxg_session* s, float* out, const double* scales) {
 static __device__ __align__(256) double g_noalloc_scratch[2 * MCXG_NOALLOC_MAX_BLOCKS + 2];
 static double* g_noalloc_scratch_addr[MCXG_NOALLOC_MAX_DEVICES];
 
-int mcxg_energy_sum_noalloc(int device, const float* d_energy, uint32_t nthread, double* d_sums) {
-    if (!d_energy || !d_sums || nthread == 0 || device < 0 || device >= MCXG_NOALLOC_MAX_DEVICES) {
-        return MCXG_ERR_ARG;
-    }
-    uint32_t nblocks = (nthread + MCXG_NOALLOC_CHUNK - 1) / MCXG_NOALLOC_CHUNK;
-    if (nblocks > MCXG_NOALLOC_MAX_BLOCKS) {
-        return MCXG_ERR_LIMIT;
-    }
-    MCXG_TRY(cudaSetDevice(device));
+static int energy_sum_noalloc_on(int device, const float* d_energy, uint32_t nthread, uint32_t nblocks,
+                                 double* d_sums) {
     if (!g_noalloc_scratch_addr[device]) {
         /* once per device, with that device current: the device address of the
            static array (its host-side name is not a device address) */
@@ -1532,6 +1583,23 @@ int mcxg_energy_sum_noalloc(int device, const float* d_energy, uint32_t nthread,
     MCXG_TRY(cudaMemcpyAsync(d_sums, scratch + 2 * nblocks, 2 * sizeof(double), cudaMemcpyDeviceToDevice, 0));
     MCXG_TRY(cudaStreamSynchronize(0));
     return MCXG_OK;
+}
+
+int mcxg_energy_sum_noalloc(int device, const float* d_energy, uint32_t nthread, double* d_sums) {
+    if (!d_energy || !d_sums || nthread == 0 || device < 0 || device >= MCXG_NOALLOC_MAX_DEVICES) {
+        return MCXG_ERR_ARG;
+    }
+    uint32_t nblocks = (nthread + MCXG_NOALLOC_CHUNK - 1) / MCXG_NOALLOC_CHUNK;
+    if (nblocks > MCXG_NOALLOC_MAX_BLOCKS) {
+        return MCXG_ERR_LIMIT;
+    }
+    /* run on `device`, then give the calling thread its current device back */
+    int prev = 0;
+    MCXG_TRY(cudaGetDevice(&prev));
+    MCXG_TRY(cudaSetDevice(device));
+    const int rc = energy_sum_noalloc_on(device, d_energy, nthread, nblocks, d_sums);
+    const cudaError_t e = cudaSetDevice(prev);
+    return rc != MCXG_OK ? rc : (e == cudaSuccess ? MCXG_OK : MCXG_ERR_CUDA);
 }
 
 int mcxg_get_launch(mcxg_session* s, int* grid, int* block, int* regs) {

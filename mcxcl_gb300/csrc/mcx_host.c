@@ -240,6 +240,21 @@ static void prep_polarized(Config* cfg) {
     }
 }
 
+/* A voxel of the padded volume lies on an interface when any of its 26
+   neighbours is void (label 0); the padding layer is void. */
+static int touches_void(const uint32_t* pad, size_t i, size_t dx, size_t dxy) {
+    for (int k = -1; k <= 1; k++) {
+        for (int j = -1; j <= 1; j++) {
+            for (int l = -1; l <= 1; l++) {
+                if ((k || j || l) && !pad[(ptrdiff_t)i + k * (ptrdiff_t)dxy + j * (ptrdiff_t)dx + l]) {
+                    return 1;
+                }
+            }
+        }
+    }
+    return 0;
+}
+
 static void maskdet(Config* cfg) {
     unsigned int nx = cfg->dim.x, ny = cfg->dim.y, nz = cfg->dim.z;
     unsigned int dx = nx + 2, dy = ny + 2, dz = nz + 2;
@@ -290,20 +305,13 @@ static void maskdet(Config* cfg) {
                         continue;
                     }
                     size_t i = ((size_t)(int)(iz + 1.f) * dy * dx + (size_t)(int)(iy + 1.f) * dx + (size_t)(int)(ix + 1.f));
-                    size_t dxy = (size_t)dy * dx;
                     if (cfg->mediabyte == 97) {
                         /* split voxels: those with a background lower half (mcx_utils.c:4155-4165) */
                         if (!(pad[i] & 0xFF000000u) && (pad[i] & 0x00FF0000u)) {
                             cfg->vol[(int)iz * ny * nx + (int)iy * nx + (int)ix] |= DET_MASK;
+                            count++;
                         }
-                    } else if (pad[i] &&
-                            !(pad[i + 1] && pad[i - 1] && pad[i + dx] && pad[i - dx] && pad[i + dxy] && pad[i - dxy] &&
-                              pad[i + dx + 1] && pad[i + dx - 1] && pad[i - dx + 1] && pad[i - dx - 1] &&
-                              pad[i + dxy + 1] && pad[i + dxy - 1] && pad[i - dxy + 1] && pad[i - dxy - 1] &&
-                              pad[i + dxy + dx] && pad[i + dxy - dx] && pad[i - dxy + dx] && pad[i - dxy - dx] &&
-                              pad[i + dxy + dx + 1] && pad[i + dxy + dx - 1] && pad[i + dxy - dx + 1] &&
-                              pad[i + dxy - dx - 1] && pad[i - dxy + dx + 1] && pad[i - dxy + dx - 1] &&
-                              pad[i - dxy - dx + 1] && pad[i - dxy - dx - 1])) {
+                    } else if (pad[i] && touches_void(pad, i, dx, (size_t)dy * dx)) {
                         cfg->vol[(int)iz * ny * nx + (int)iy * nx + (int)ix] |= DET_MASK;
                         count++;
                     }
@@ -422,6 +430,12 @@ static void preprocess(Config* cfg) {
     if (cfg->isrowmajor) {
         row2col(cfg);
         cfg->isrowmajor = 0;
+    }
+    if (cfg->debuglevel & 8) {
+        /* MCX_DEBUG_MOVE_ONLY: trajectories only, no field and no detected
+           photons (mcx_utils.c:1552-1555) */
+        cfg->issave2pt = 0;
+        cfg->issavedet = 0;
     }
     if (cfg->issavedet && cfg->detnum == 0 && isbcdet == 0) {
         cfg->issavedet = 0;
@@ -1364,8 +1378,14 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
                              ((cfg->debuglevel & 1) ? MCXG_RNGDUMP : 0u);
         if (iter == 0) {
             device_check(mcxg_set_launch(s, 0, 0), "resetting the launch shape");
+            /* MCX_DEBUG_MOVE (2) and MCX_DEBUG_MOVE_ONLY (8) both record (mcx_host.cpp:702, 1173);
+               set before any launch so a cached session never keeps the last run's setting */
+            device_check(mcxg_set_trajectory(s, (cfg->debuglevel & 10) ? cfg->maxjumpdebug : 0u),
+                         "allocating the trajectory records");
         }
-        if (cfg->autotune && !cfg->exactmath && !(cfg->debuglevel & 1)) {
+        /* trajectory runs take the general instantiation and record at every
+           launch: they are not tuned (the tuned shape is for the common one) */
+        if (cfg->autotune && !cfg->exactmath && !(cfg->debuglevel & 11)) {
             uint64_t sig = tune_signature(cfg, &kp);
             TuneCache* tc = &g_tune[device];
             if (!tc->valid || tc->sig != sig) {
@@ -1384,11 +1404,6 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
             flags |= tc->noagg ? MCXG_NOAGG : MCXG_AGG;
         }
         float kms = 0.f;
-        if (iter == 0) {
-            /* MCX_DEBUG_MOVE (2) and MCX_DEBUG_MOVE_ONLY (8) both record (mcx_host.cpp:702, 1173) */
-            device_check(mcxg_set_trajectory(s, (cfg->debuglevel & 10) ? cfg->maxjumpdebug : 0u),
-                         "allocating the trajectory records");
-        }
         device_check(mcxg_simulate(s, flags, &kms), "running the transport kernel");
         kms_total += kms;
         if ((cfg->debuglevel & 10) && cfg->maxjumpdebug) {

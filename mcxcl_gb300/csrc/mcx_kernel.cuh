@@ -30,7 +30,9 @@
  * -fmad=false -prec-div=true -prec-sqrt=true -ftz=false), DET (detector
  * bookkeeping compiled in), REFL (Fresnel / boundary-condition block
  * compiled in), WAGG (warp aggregation of deposits), COUNT (event counters),
- * MINB (resident 256-thread blocks per SM the register allocation targets).
+ * MINB (resident 256-thread blocks per SM the register allocation targets),
+ * ACC64 (every deposit also accumulated in FP64, plain float and the
+ * reference's spill form, to state the accumulation error).
  * DET and REFL are upper bounds: the runtime flags in the constant block
  * still decide, so the exact build runs every configuration.
  */
@@ -1593,8 +1595,22 @@ __device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPST<C>& ps, unsign
     }
 }
 
+/* Precision check: the same deposit into an FP64 field (the accumulation the
+   two-plane field is measured against), a plain float field, and a float
+   field with the reference's +-1000 spill into a shadow plane
+   (mcx_core.cl:2880-2886), so all three see exactly the photons of the run. */
+__device__ __forceinline__ void acc_verify(const KArgs& a, unsigned int fieldlen, unsigned int k, float w) {
+    atomicAdd(a.acc64 + k, (double)w);
+    atomicAdd(a.accf + k, w);
+    const float o = atomicAdd(a.accs + k, w);
+    if (fabsf(o) > K_MAX_ACCUM) {
+        atomicAdd(a.accs + k, o > 0.f ? -K_MAX_ACCUM : K_MAX_ACCUM);
+        atomicAdd(a.accs + fieldlen + k, o > 0.f ? K_MAX_ACCUM : -K_MAX_ACCUM);
+    }
+}
+
 template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false,
-          bool COMMON = false, bool RF = false, bool POL = false, bool SVMC = false>
+          bool COMMON = false, bool RF = false, bool POL = false, bool SVMC = false, bool ACC64 = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
     typedef typename std::conditional<BATCH, BatchPST<COMMON>, ConstPST<XMEDIA, COMMON>>::type PS;
@@ -1959,6 +1975,9 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 }
             } else {
                 deposit<WAGG>(a.field, ps.lo_plane(), dep, ps.field_off() + key, weight, pd);
+                if (ACC64 && dep) {
+                    acc_verify(a, c_p.fieldlen, key, weight);
+                }
             }
             if (RF && depim) {
                 /* the imaginary planes follow the real ones: [2F, 3F) and its low plane */

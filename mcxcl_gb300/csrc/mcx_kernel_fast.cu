@@ -66,8 +66,19 @@ static void* kxmedia() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, true>;
 }
 
+/* the common configuration with the FP64 / plain-float / spill accumulators
+   of the precision check: 3 blocks/SM, direct deposits */
+template <bool DET, bool REFL>
+static void* kacc64() {
+    return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, true, false, false, false, true>;
+}
+
 static void* select(int flags) {
     const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    if (flags & LF_ACC64) {
+        return det ? (refl ? kacc64<true, true>() : kacc64<true, false>())
+                   : (refl ? kacc64<false, true>() : kacc64<false, false>());
+    }
     if (flags & LF_SVMC) {
         return det ? (refl ? ksvmc<true, true>() : ksvmc<true, false>())
                    : (refl ? ksvmc<false, true>() : ksvmc<false, false>());

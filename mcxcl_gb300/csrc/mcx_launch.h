@@ -51,10 +51,17 @@ struct KArgs {
     unsigned int* jumpctr;
     float* traj;
     unsigned int maxjump;
+    /* precision check (instantiations with ACC64 only): every deposit also goes
+       to an FP64 field, a plain float field and a float field with the
+       reference's +-1000 spill into a second plane (2 x fieldlen) */
+    double* acc64;
+    float* accf;
+    float* accs;
 };
 
 /* flag bits for the launch entries */
-enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128, LF_POL = 256, LF_SVMC = 512 };
+enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128, LF_POL = 256, LF_SVMC = 512,
+       LF_ACC64 = 1024 };
 
 /* fast instantiation: hardware transcendental approximations */
 cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,

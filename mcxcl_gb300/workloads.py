@@ -105,6 +105,18 @@ def config(n):
     raise KeyError(n)
 
 
+def describe(n):
+    """One line naming benchmark configuration n and its sizes."""
+    return {
+        1: "60^3 homogeneous cube (mua 0.005, mus 1.0, g 0.01, n 1.37), pencil (29,29,0) +z, one 0-5 ns gate, "
+           "no reflection, no detectors",
+        2: "60^3 cube + r15 sphere (label 2), Fresnel on, 50 gates x 0.1 ns, 4 r=1 detectors on z=0 saving "
+           "detid/nscat/ppath + seeds, pencil (29,29,0) +z",
+        3: "181x217x181 synthetic layered head (5 ellipsoid shells), 10 gates over 0-5 ns, 16 r=2 detectors on a "
+           "30 mm ring, roulette at 1e-4, pencil on the top surface +z",
+    }[n]
+
+
 def gaussian_field(shape, corr, seed):
     """Unit-variance Gaussian random field: seeded white noise convolved
     (periodically, by FFT) with a Gaussian of standard deviation corr voxels."""

@@ -85,8 +85,8 @@ _ref = {}
 def build(ref=None):
     """Compile the oracle (and, when the reference sources exist, the reference harness)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    refdir = ref or os.environ.get("MCX_REFERENCE", "/root/reference")
-    if os.path.isfile(os.path.join(refdir, "src", "mcx_core.cl")):
+    refdir = ref or os.environ.get("MCX_REFERENCE", "")
+    if refdir and os.path.isfile(os.path.join(refdir, "src", "mcx_core.cl")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + refdir], check=True)
 
 

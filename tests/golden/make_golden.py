@@ -52,8 +52,11 @@ def summarize(res):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("MCX_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("MCX_REFERENCE"),
+                    help="the reference checkout (default: $MCX_REFERENCE)")
     args = ap.parse_args()
+    if not args.reference:
+        sys.exit("name the reference checkout with --reference or MCX_REFERENCE")
     oracle.build(args.reference)
     if not oracle.ref_available():
         sys.exit("reference harness could not be built from " + args.reference)
