@@ -30,7 +30,7 @@ pass's agreement with central differences.
 Also: "c1" and "c3" -- the homogeneous cube and the synthetic layered head
 (181 x 217 x 181, five labels, 16 detectors, roulette), each with its own
 photons/ms, FP32-issue roofline and DRAM traffic; "precision" (with
---precision P) -- the error of the two-plane field, a plain float field and
+--precision P) -- the error of the compensated field, a plain float field and
 the reference's spill field against an FP64 accumulation of the same P
 photons on the cube and the cube + sphere workloads.
 
@@ -407,10 +407,11 @@ def config_measure(k, photons, steps, warmup, flush, peak):
 
 
 def precision_measure(photons):
-    """Error of the two-plane field (the product), of a plain float field and
-    of the reference's +-1000 spill field against an FP64 accumulation of the
-    same deposits (one run, every deposit to all four), on the cube and the
-    cube + sphere workloads; relative error over every non-zero element."""
+    """Error of the compensated field (the product: float hi and lo planes
+    and an integer spill count), of a plain float field and of the
+    reference's +-1000 spill field against an FP64 accumulation of the same
+    deposits (one run, every deposit to all four), on the cube and the cube +
+    sphere workloads; relative error over every non-zero element."""
     import ctypes
     from mcxcl_gb300 import _lib, workloads
     L = _lib.load()
@@ -432,7 +433,7 @@ def precision_measure(photons):
             L.mcx_clearcfg(ctypes.byref(C))
         nz = f64 > 0
         res = {}
-        for name, x in (("two_plane", two), ("two_plane_float_output", two.astype(np.float32).astype(np.float64)),
+        for name, x in (("compensated", two), ("compensated_float_output", two.astype(np.float32).astype(np.float64)),
                         ("plain_float", plain.astype(np.float64)), ("reference_spill", spill.astype(np.float64))):
             r = np.abs(x[nz] - f64[nz]) / f64[nz]
             tot = abs(x.sum() - f64.sum()) / f64.sum()

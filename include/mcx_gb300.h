@@ -238,6 +238,22 @@ void mcx_clearcfg(Config* cfg);
    window are kept, with their detected weights (mcx_replayinit,
    src/mcx_utils.c:1355-1421). */
 void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte);
+/* Reads a JSON input file (src/mcx_utils.c:2011-2071 with mcx_loadjson
+   2401-3287): fname is a .json file, or the JSON text itself when it starts
+   with '{'.  Reads the sections the transport path uses -- Session (ID,
+   Photons, RNGSeed, MaxDetPhoton, BCFlags, Do* switches, DebugFlag,
+   SaveDataMask, OutputType, MinEnergy), Forward (T0, T1, Dt), Optode
+   (Source: Type, Pos, Dir, Param1, Param2, Weight, Frequency, WaveLength,
+   SrcNum, ID, Pattern, AngleInverseCDF, extra sources as arrays of vectors;
+   Detector: Pos, R, Dir), Domain (Media, MieScatter, Dim, Step, LengthUnit,
+   MediaFormat, OriginType, InverseCDF, VolumeFile of byte/short/integer
+   labels) and Shapes (Name, Origin, Grid, Sphere, Box, Subgrid, Cylinder,
+   UpperSpace, X/Y/ZSlabs, X/Y/ZLayers) -- then validates cfg as
+   mcx_validatecfg does: cfg is ready for mcx_run_simulation.  The legacy
+   .inp text format is not read.  Errors go through mcx_error. */
+void mcx_readconfig(char* fname, Config* cfg);
+/* The same from JSON text in memory (src/mcx_utils.c, mcx_parsejson). */
+void mcx_parsejson(char* jbuf, Config* cfg);
 /* Lists CUDA devices into *info (caller frees with mcx_cleargpuinfo); replaces
    mcx_list_gpu(Config*, unsigned*, cl_device_id*, GPUInfo**)
    (src/mcx_host.cpp:252).  Returns the number of active devices. */
@@ -384,7 +400,7 @@ int  mcxg_batch_set(mcxg_session* s, const void* sims, size_t desc_size, uint32_
 int  mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms);
 /* Per simulation: FP64 {escaped, launched} weight, 2 x nsim. */
 int  mcxg_batch_get_energy(mcxg_session* s, double* out);
-/* Every simulation's field, (hi + lo) x scales[i], at its field offset. */
+/* Every simulation's field, (hi + lo + 1024 x spill count) x scales[i], at its field offset. */
 int  mcxg_batch_get_field(mcxg_session* s, float* out, const double* scales);
 /* Replay inputs, one entry per replayed photon: the saved xorshift128+ state
    (16 bytes), detected weight, time of flight and detector id.  Used when
@@ -404,7 +420,8 @@ int  mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms);
 int  mcxg_get_energy(mcxg_session* s, double* escaped, double* launched);
 /* Per-thread {escaped, launched} floats, 2 x nthread. */
 int  mcxg_get_thread_energy(mcxg_session* s, float* out);
-/* Field: (hi + lo) in FP64, times scale, rounded to float; fieldlen values. */
+/* Field: the compensated accumulator (hi + lo + 1024 x spill count) in FP64, times scale,
+   rounded to float; fieldlen values. */
 int  mcxg_get_field(mcxg_session* s, float* out, double scale);
 /* Field split into nblocks equal blocks, block b scaled by scales[b]
    (a replay with one output per detector). */
@@ -424,14 +441,14 @@ int  mcxg_set_polarization(mcxg_session* s, const float* smatrix, uint32_t nmedi
    source-major over detector (src/mcx_core.cl:3320-3512). */
 int  mcxg_adjoint(mcxg_session* s, int kind, uint32_t ns, uint32_t nd, uint32_t nx, uint32_t ny, uint32_t nz,
                   uint32_t maxgate, float* out);
-/* Field: (hi + lo) in FP64, unscaled. */
+/* Field: the compensated accumulator in FP64, unscaled. */
 int  mcxg_get_field_f64(mcxg_session* s, double* out);
 /* The precision check's fields of the last MCXG_VERIFY launch, unscaled,
    fieldlen values each (NULL skips one): the FP64 accumulation of the same
    deposits, the plain float accumulation, and the spill accumulation with
    its two planes added in float as the reference's host does
    (src/mcx_core.cl:2880-2886, src/mcx_host.cpp:1252-1257).  No counterpart
-   in the reference: it exists to state the two-plane field's error. */
+   in the reference: it exists to state the compensated field's error. */
 int  mcxg_get_verify(mcxg_session* s, double* f64, float* plain, float* spill);
 /* Weight and time of flight (s) of each saved detected photon when it was
    detected, 2 floats per record, in record order. */

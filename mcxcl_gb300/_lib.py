@@ -117,7 +117,7 @@ EXPORTS = [
     "mcxg_get_counters", "mcxg_get_launch", "mcxg_fp32_peak", "mcxg_energy_sum_noalloc", "mcxg_autotune",
     "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_field_interleaved", "mcxg_set_polarization", "mcx_mie", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",
     "mcxg_batch_simulate", "mcxg_batch_get_energy", "mcxg_batch_get_field", "mcx_savedetphoton",
-    "mcxg_adjoint", "mcxg_get_verify",
+    "mcxg_adjoint", "mcxg_get_verify", "mcx_readconfig", "mcx_parsejson",
 ]
 
 _lib = None
@@ -139,6 +139,8 @@ def load():
     L.mcx_clearcfg.argtypes = [P(Config)]
     L.mcx_validatecfg.argtypes = [P(Config), vp, vp, ctypes.c_int]
     L.mcx_run_simulation.argtypes = [P(Config), vp, vp]
+    L.mcx_readconfig.argtypes = [ctypes.c_char_p, P(Config)]
+    L.mcx_parsejson.argtypes = [ctypes.c_char_p, P(Config)]
     L.mcx_list_gpu.argtypes = [P(Config), P(ctypes.c_uint), P(P(GPUInfo))]
     L.mcx_list_gpu.restype = ctypes.c_int
     L.mcx_cleargpuinfo.argtypes = [P(P(GPUInfo))]

@@ -55,11 +55,11 @@ def build(force=False, verbose=False):
         objs.append(obj)
         if force or _stale(obj, [src] + hdeps):
             jobs.append([nvcc] + NVCC_COMMON + flags + ["-c", src, "-o", obj])
-    for cunit in ("mcx_host.c", "mcx_mie.c"):
+    for cunit in ("mcx_host.c", "mcx_mie.c", "mcx_json.c"):
         csrc = os.path.join(CSRC, cunit)
         cobj = os.path.join(BUILD, cunit.replace(".c", ".o"))
         objs.append(cobj)
-        if force or _stale(cobj, [csrc] + hdeps):
+        if force or _stale(cobj, [csrc, os.path.join(CSRC, "mcx_json.h")] + hdeps):
             jobs.append([os.environ.get("CC", "gcc"), "-std=gnu11", "-O2", "-fPIC", "-Wall", "-I" + CSRC,
                          "-I" + INCLUDE, "-c", csrc, "-o", cobj])
     procs = []

@@ -54,7 +54,7 @@ struct mcxg_session {
     uint32_t maxjump = 0;
     uint32_t* d_lfib = nullptr;      /* 31-word generator windows, one per block of seed words */
     size_t lfib_cap = 0;
-    float* d_field = nullptr;        /* 2 x fieldlen */
+    float* d_field = nullptr;        /* per component: hi, lo, spill count planes (3 x fieldlen) */
     size_t field_cap = 0;
     float2* d_energy = nullptr;
     size_t energy_cap = 0;
@@ -106,7 +106,7 @@ struct mcxg_session {
     uint8_t* d_bmedia = nullptr;
     size_t bmedia_cap = 0;
     std::vector<unsigned long long> h_simvt;
-    float* d_bfield = nullptr;       /* 2 x totalfield */
+    float* d_bfield = nullptr;       /* hi, lo, spill count planes: 3 x totalfield */
     size_t bfield_cap = 0;
     float2* d_benergy = nullptr;     /* per reference thread of the batch */
     size_t benergy_cap = 0;
@@ -132,6 +132,10 @@ namespace {
 
 constexpr int kRedBlocks = 256;
 constexpr int kRedThreads = 256;
+/* the transport kernel's compensated field: hi, lo and spill-count planes per
+   component; a count stands for kSpill (the kernel's K_SPILL) */
+constexpr size_t kFieldPlanes = 3;
+constexpr double kSpill = 1024.0;
 
 int cuda_status(cudaError_t e) {
     if (e == cudaSuccess) {
@@ -213,11 +217,13 @@ __global__ void energy_final(double* part, int nblocks) {
 
 /* Output element i of a field of n elements per component: component
    c = i / n (1 real, or real then imaginary for RF), element j = i % n; each
-   component is a high plane followed by its low plane. */
+   component is a high plane, its low plane and its spill-count plane:
+   value = hi + lo + kSpill x count in FP64. */
 __device__ __forceinline__ double merged_at(const float* __restrict__ f, size_t n, size_t i, size_t& j) {
     const size_t c = i / n;
     j = i - c * n;
-    return (double)f[2 * c * n + j] + (double)f[2 * c * n + n + j];
+    const float* p = f + 3 * c * n;
+    return (double)p[j] + (double)p[n + j] + (double)kSpill * (double)((const int*)p)[2 * n + j];
 }
 
 __global__ void field_merge_f32(const float* __restrict__ f, size_t n, size_t total, double scale,
@@ -304,7 +310,8 @@ __global__ void batch_merge(const float* __restrict__ f, unsigned long long tota
     const unsigned int n = d.kp.fieldlen;
     const double sc = scales[blockIdx.y];
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        out[off + i] = (float)(((double)f[off + i] + (double)f[off + i + total]) * sc);
+        out[off + i] = (float)(((double)f[off + i] + (double)f[off + i + total] +
+                                (double)kSpill * (double)((const int*)f)[off + i + 2 * total]) * sc);
     }
 }
 
@@ -612,7 +619,7 @@ int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, 
         rc = ensure(&s->d_pattern, &s->pattern_cap, npattern);
     }
     if (!rc) {
-        rc = ensure(&s->d_field, &s->field_cap, 2 * (size_t)kp.fieldlen * field_comps(kp));
+        rc = ensure(&s->d_field, &s->field_cap, kFieldPlanes * (size_t)kp.fieldlen * field_comps(kp));
     }
     if (!rc && kp.savedet) {
         size_t recs = kp.maxdetphoton;
@@ -846,7 +853,7 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     }
     {
         /* a run that turns on the complex field after mcxg_set_problem */
-        const size_t need = 2 * (size_t)kp.fieldlen * field_comps(kp);
+        const size_t need = kFieldPlanes * (size_t)kp.fieldlen * field_comps(kp);
         if (need > s->field_cap) {
             if (flags & MCXG_KEEP) {
                 return MCXG_ERR_STATE;
@@ -858,7 +865,7 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
         }
     }
     if (!(flags & MCXG_KEEP)) {
-        MCXG_TRY(cudaMemsetAsync(s->d_field, 0, sizeof(float) * 2 * (size_t)kp.fieldlen * field_comps(kp), s->st));
+        MCXG_TRY(cudaMemsetAsync(s->d_field, 0, sizeof(float) * kFieldPlanes * (size_t)kp.fieldlen * field_comps(kp), s->st));
     }
     s->out_valid = false;
     MCXG_TRY(cudaMemsetAsync(s->d_energy, 0, sizeof(float2) * kp.nthread, s->st));
@@ -1352,7 +1359,7 @@ int batch_reset_graph(mcxg_session* s) {
    descriptors into constant memory and the transport launch; per-simulation
    sums */
 int batch_enqueue(mcxg_session* s, int lflags) {
-    MCXG_TRY(cudaMemsetAsync(s->d_bfield, 0, sizeof(float) * 2 * (size_t)s->totalfield, s->st));
+    MCXG_TRY(cudaMemsetAsync(s->d_bfield, 0, sizeof(float) * kFieldPlanes * (size_t)s->totalfield, s->st));
     MCXG_TRY(cudaMemsetAsync(s->d_benergy, 0, sizeof(float2) * (size_t)s->totalvt, s->st));
     MCXG_TRY(cudaMemsetAsync(s->d_words, 0, 8 * sizeof(unsigned int), s->st));
     KArgs a;
@@ -1419,7 +1426,7 @@ int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_
         rc = ensure(&s->d_bmedia, &s->bmedia_cap, (size_t)nmedia);
     }
     if (!rc) {
-        rc = ensure(&s->d_bfield, &s->bfield_cap, 2 * (size_t)field);
+        rc = ensure(&s->d_bfield, &s->bfield_cap, kFieldPlanes * (size_t)field);
     }
     if (!rc) {
         rc = ensure(&s->d_benergy, &s->benergy_cap, (size_t)vt);

@@ -26,6 +26,7 @@
 #include <time.h>
 
 #include "../../include/mcx_gb300.h"
+#include "mcx_json.h"
 #include "mcx_kparams.h"
 
 #define H_EPS        1e-10f        /* mcx_const.h:30 */
@@ -744,6 +745,71 @@ void mcx_validatecfg(Config* cfg, float* detps, int dimdetps[2], int seedbyte) {
     cfg->his.totalsource = ((cfg->srcid <= 0) ? cfg->extrasrclen + 1 : 1);
     replayinit(cfg, detps, dimdetps, seedbyte);
     MCX_LEAVE();
+}
+
+/* ------------------------------------------------------------- JSON input */
+
+/* mcx_parsejson (src/mcx_utils.c, called from mcx_readconfig 2041): the JSON
+   text into cfg, then what the reference's mcx_prepdomain does after
+   loading (0-based positions, volume preprocessing, detector mask) through
+   mcx_validatecfg: cfg is ready for mcx_run_simulation. */
+void mcx_parsejson(char* jbuf, Config* cfg) {
+    MCX_ENTER(cfg);
+    char err[256];
+    if (!jbuf) {
+        MCX_ERROR(-1, "no JSON input");
+    }
+    const int rc = mcxj_load(jbuf, cfg, err, sizeof(err));
+    if (rc) {
+        MCX_ERROR(rc, err);
+    }
+    MCX_LEAVE();
+    mcx_validatecfg(cfg, NULL, NULL, 0);
+}
+
+/* mcx_readconfig (src/mcx_utils.c:2011-2071): a .json input file, or the
+   JSON text itself when the name starts with '{'.  The reference's legacy
+   .inp text format is not read by this build. */
+void mcx_readconfig(char* fname, Config* cfg) {
+    MCX_ENTER(cfg);
+    char err[256];
+    if (!fname || !fname[0]) {
+        MCX_ERROR(-2, "reading the configuration from standard input is not supported by this build");
+    }
+    char* text = fname;
+    if (fname[0] != '{') {
+        if (!strstr(fname, ".json")) {
+            MCX_ERROR(-2, "this build reads JSON input files (.json) only");
+        }
+        FILE* fp = fopen(fname, "rb");
+        if (!fp) {
+            MCX_ERROR(-2, "can not load the specified config file");
+        }
+        long len = -1;
+        if (fseek(fp, 0, SEEK_END) == 0) {
+            len = ftell(fp);
+        }
+        text = (len >= 0) ? (char*)malloc((size_t)len + 1) : NULL;
+        if (!text || fseek(fp, 0, SEEK_SET) != 0 || fread(text, 1, (size_t)len, fp) != (size_t)len) {
+            fclose(fp);
+            free(text);
+            MCX_ERROR(-2, "reading input file is terminated");
+        }
+        fclose(fp);
+        text[len] = '\0';
+    }
+    const int rc = mcxj_load(text, cfg, err, sizeof(err));
+    if (text != fname) {
+        free(text);
+    }
+    if (rc) {
+        MCX_ERROR(rc, err);
+    }
+    if (cfg->session[0] == '\0') {
+        snprintf(cfg->session, sizeof(cfg->session), "%s", fname);
+    }
+    MCX_LEAVE();
+    mcx_validatecfg(cfg, NULL, NULL, 0);
 }
 
 /* ----------------------------------------------------------------- devices */

@@ -21,7 +21,8 @@
  *    the read-only path.
  *  - Fluence accumulated in two float planes with an error-free transform:
  *    the high plane takes the deposit with an atomic that returns the old
- *    value, the exact rounding error of that sum goes to the low plane.
+ *    value, the exact rounding error of that sum goes to the low plane, and
+ *    the high plane is held within +-1024 by spills into an integer count.
  *    Deposits to the same voxel and gate by several lanes of a warp are
  *    merged first (match, shuffle-sum, one leader atomic).
  *  - Detected-photon partial data in shared memory, strided per thread.
@@ -832,16 +833,46 @@ __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Pho
 
 /* ---------------------------------------------------------------- deposit */
 
-/* Two-plane compensated add: the high plane takes w, the exact rounding error
-   of that add (TwoSum on the value the atomic returned) goes to the low
-   plane.  hi + lo then carries the sum to ~2^-48 relative. */
-__device__ __forceinline__ void field_add2(float* field, unsigned int fieldlen, unsigned int i, float w) {
-    float old = atomicAdd(field + i, w);
-    float s = __fadd_rn(old, w);
-    float bp = __fsub_rn(s, old);
-    float e = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bp)), __fsub_rn(w, bp));
+/* Compensated accumulation in three planes per field component: a float
+   high plane, a float low plane, and an int32 spill count.  The high plane
+   takes each deposit with an atomic that returns the old value; the exact
+   rounding error of that add (TwoSum) goes to the low plane.  The high plane
+   is kept within +-K_SPILL by moving K_SPILL into the spill count whenever
+   an add carries it past that bound (that add's rounding error again to the
+   low plane): a high plane that grew without bound would make every later
+   deposit smaller than half its ulp, so all of it would pile up in the low
+   plane, which then saturates the same way (tens of percent lost in the
+   hottest voxels of a 1e9-photon run).  The value is
+   hi + lo + K_SPILL x count, summed in FP64: the bulk exact in the count,
+   the rest to ~2^-48 of the element.  Planes: hi at [i], lo at [lo + i],
+   count at [2 lo + i] (as int32), lo = the component's plane length. */
+#define K_SPILL 1024.f
+
+__device__ __forceinline__ float twosum_err(float old, float w, float s) {
+    const float bp = __fsub_rn(s, old);
+    return __fadd_rn(__fsub_rn(old, __fsub_rn(s, bp)), __fsub_rn(w, bp));
+}
+
+/* the add that produced s (s = old + w, |s| > K_SPILL) moves K_SPILL out */
+__device__ __noinline__ void field_spill(float* field, unsigned int lo, unsigned int i, float s) {
+    const float t = s > 0.f ? -K_SPILL : K_SPILL;
+    const float old = atomicAdd(field + i, t);
+    const float e = twosum_err(old, t, __fadd_rn(old, t));
     if (e != 0.f) {
-        atomicAdd(field + fieldlen + i, e);
+        atomicAdd(field + lo + i, e);
+    }
+    atomicAdd((int*)field + 2 * (size_t)lo + i, s > 0.f ? 1 : -1);
+}
+
+__device__ __forceinline__ void field_add2(float* field, unsigned int lo, unsigned int i, float w) {
+    const float old = atomicAdd(field + i, w);
+    const float s = __fadd_rn(old, w);
+    const float e = twosum_err(old, w, s);
+    if (e != 0.f) {
+        atomicAdd(field + lo + i, e);
+    }
+    if (fabsf(s) > K_SPILL) {
+        field_spill(field, lo, i, s);
     }
 }
 
@@ -854,13 +885,15 @@ struct Pending {
     bool on;
 };
 
-__device__ __forceinline__ void pend_complete(float* field, unsigned int fieldlen, Pending& pd) {
+__device__ __forceinline__ void pend_complete(float* field, unsigned int lo, Pending& pd) {
     if (pd.on) {
-        float s = __fadd_rn(pd.old, pd.w);
-        float bp = __fsub_rn(s, pd.old);
-        float e = __fadd_rn(__fsub_rn(pd.old, __fsub_rn(s, bp)), __fsub_rn(pd.w, bp));
+        const float s = __fadd_rn(pd.old, pd.w);
+        const float e = twosum_err(pd.old, pd.w, s);
         if (e != 0.f) {
-            atomicAdd(field + fieldlen + pd.idx, e);
+            atomicAdd(field + lo + pd.idx, e);
+        }
+        if (fabsf(s) > K_SPILL) {
+            field_spill(field, lo, pd.idx, s);
         }
         pd.on = false;
     }
@@ -926,7 +959,7 @@ __device__ __forceinline__ void rf_replay_deposit(const KArgs& a, const PS& ps, 
     }
     field_add2(a.field, ps.lo_plane(), key, wre);
     if (c_p.omega > 0.f) {
-        field_add2(a.field + 2 * (size_t)c_p.fieldlen, c_p.fieldlen, key, wim);
+        field_add2(a.field + 3 * (size_t)c_p.fieldlen, c_p.fieldlen, key, wim);
     }
 }
 
@@ -1001,7 +1034,7 @@ __device__ void replay_site_deposit(const KArgs& a, const PS& ps, const Shared& 
     }
     field_add2(a.field, ps.lo_plane(), ps.field_off() + (unsigned int)key, tmp0);
     if (c_p.outputtype == otRFmus) {
-        field_add2(a.field + 2 * (size_t)c_p.fieldlen, c_p.fieldlen, (unsigned int)key, tim);
+        field_add2(a.field + 3 * (size_t)c_p.fieldlen, c_p.fieldlen, (unsigned int)key, tim);
     }
 }
 
@@ -1980,8 +2013,8 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 }
             }
             if (RF && depim) {
-                /* the imaginary planes follow the real ones: [2F, 3F) and its low plane */
-                field_add2(a.field + 2 * (size_t)c_p.fieldlen, c_p.fieldlen, key, weight_im);
+                /* the imaginary component's planes follow the real one's: [3F, 6F) */
+                field_add2(a.field + 3 * (size_t)c_p.fieldlen, c_p.fieldlen, key, weight_im);
             }
         }
         if (KP_SVMC) {

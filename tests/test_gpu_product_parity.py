@@ -111,12 +111,13 @@ def test_fast_kernel_head_workload_parity():
 
 def test_fluence_accumulation_error_against_fp64():
     """The precision contract on the homogeneous cube at 1e8 photons: every
-    deposit of one run goes to the two-plane field (the product), to an FP64
-    field, to a plain float field and to a float field with the reference's
-    +-1000 spill (mcx_core.cl:2880-2886, merged in float as
-    mcx_host.cpp:1252-1257 does), so all four hold exactly the same photons.
-    The two-plane field's error against FP64 stays at or below 1e-6 (max and
-    median over every non-zero element); the plain float field's is worse."""
+    deposit of one run goes to the compensated field (the product: float high
+    and low planes with an integer spill count), to an FP64 field, to a plain
+    float field and to a float field with the reference's +-1000 spill
+    (mcx_core.cl:2880-2886, merged in float as mcx_host.cpp:1252-1257 does),
+    so all four hold exactly the same photons.  The compensated field's error
+    against FP64 stays at or below 1e-6 (max and median over every non-zero
+    element); the plain float field's is worse."""
     import ctypes
     from mcxcl_gb300 import _lib, pmcxcl, workloads
     L = _lib.load()
@@ -143,12 +144,12 @@ def test_fluence_accumulation_error_against_fp64():
     nz = f64 > 0
     assert nz.sum() > 100_000
     err = {}
-    for name, x in (("two-plane", two), ("plain float", plain.astype(np.float64)),
+    for name, x in (("compensated", two), ("plain float", plain.astype(np.float64)),
                     ("spill", spill.astype(np.float64))):
         r = np.abs(x[nz] - f64[nz]) / f64[nz]
         err[name] = (float(r.max()), float(np.median(r)))
     print("relative error against FP64 (max, median):", err)
-    assert err["two-plane"][0] <= 1e-6 and err["two-plane"][1] <= 1e-6, err
-    assert err["plain float"][0] > 10 * err["two-plane"][0], err
+    assert err["compensated"][0] <= 1e-6 and err["compensated"][1] <= 1e-6, err
+    assert err["plain float"][0] > 10 * err["compensated"][0], err
     # the same photons: the totals agree to the FP64 sum's own rounding
     assert abs(two.sum() - f64.sum()) <= 1e-9 * f64.sum()
