@@ -441,6 +441,12 @@ int  mcxg_set_polarization(mcxg_session* s, const float* smatrix, uint32_t nmedi
    source-major over detector (src/mcx_core.cl:3320-3512). */
 int  mcxg_adjoint(mcxg_session* s, int kind, uint32_t ns, uint32_t nd, uint32_t nx, uint32_t ny, uint32_t nz,
                   uint32_t maxgate, float* out);
+/* The same post-kernels on a caller's host field (nx ny nz maxgate (ns + nd)
+   floats, the layout above); the session needs no problem.  The reference's
+   mcx_adjoint_kernel / mcx_adjoint_dcoeff_kernel (src/mcx_core.cl:3393-3512)
+   with a real field. */
+int  mcxg_adjoint_field(mcxg_session* s, int kind, const float* field, uint32_t ns, uint32_t nd, uint32_t nx,
+                        uint32_t ny, uint32_t nz, uint32_t maxgate, float* out);
 /* Field: the compensated accumulator in FP64, unscaled. */
 int  mcxg_get_field_f64(mcxg_session* s, double* out);
 /* The precision check's fields of the last MCXG_VERIFY launch, unscaled,

@@ -1169,13 +1169,8 @@ int mcxg_set_polarization(mcxg_session* s, const float* smatrix, uint32_t nmedia
     return MCXG_OK;
 }
 
-int mcxg_adjoint(mcxg_session* s, int kind, uint32_t ns, uint32_t nd, uint32_t nx, uint32_t ny, uint32_t nz,
-                 uint32_t maxgate, float* out) {
-    if (!s || !out || !s->has_problem || !s->out_valid || ns == 0 || nd == 0 || nx == 0 || ny == 0 || nz == 0 ||
-            (unsigned long long)nx * ny * nz * maxgate * (ns + nd) != s->kp.fieldlen) {
-        return MCXG_ERR_ARG;
-    }
-    MCXG_TRY(cudaSetDevice(s->device));
+static int adjoint_run(mcxg_session* s, int kind, const float* dfield, uint32_t ns, uint32_t nd, uint32_t nx,
+                       uint32_t ny, uint32_t nz, uint32_t maxgate, float* out) {
     const unsigned int nvox = nx * ny * nz;
     const size_t len = (size_t)nvox * ns * nd;
     int rc = ensure(&s->d_adj, &s->adj_cap, len);
@@ -1184,14 +1179,41 @@ int mcxg_adjoint(mcxg_session* s, int kind, uint32_t ns, uint32_t nd, uint32_t n
     }
     const int grid = grid_for(s, nvox);
     if (kind == 0) {
-        adjoint_mua<<<grid, 256, 0, s->st>>>((const float*)s->d_out, s->d_adj, nvox, maxgate, ns, nd);
+        adjoint_mua<<<grid, 256, 0, s->st>>>(dfield, s->d_adj, nvox, maxgate, ns, nd);
     } else {
-        adjoint_dcoeff<<<grid, 256, 0, s->st>>>((const float*)s->d_out, s->d_adj, nvox, maxgate, ns, nd, nx, ny);
+        adjoint_dcoeff<<<grid, 256, 0, s->st>>>(dfield, s->d_adj, nvox, maxgate, ns, nd, nx, ny);
     }
     MCXG_TRY(cudaMemcpyAsync(out, s->d_adj, sizeof(float) * len, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
     MCXG_TRY(cudaGetLastError());
     return MCXG_OK;
+}
+
+int mcxg_adjoint(mcxg_session* s, int kind, uint32_t ns, uint32_t nd, uint32_t nx, uint32_t ny, uint32_t nz,
+                 uint32_t maxgate, float* out) {
+    if (!s || !out || !s->has_problem || !s->out_valid || ns == 0 || nd == 0 || nx == 0 || ny == 0 || nz == 0 ||
+            (unsigned long long)nx * ny * nz * maxgate * (ns + nd) != s->kp.fieldlen) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    return adjoint_run(s, kind, (const float*)s->d_out, ns, nd, nx, ny, nz, maxgate, out);
+}
+
+int mcxg_adjoint_field(mcxg_session* s, int kind, const float* field, uint32_t ns, uint32_t nd, uint32_t nx,
+                       uint32_t ny, uint32_t nz, uint32_t maxgate, float* out) {
+    if (!s || !field || !out || ns == 0 || nd == 0 || nx == 0 || ny == 0 || nz == 0 || maxgate == 0 ||
+            (unsigned long long)nx * ny * nz * maxgate * (ns + nd) > 0xFFFFFFFFull) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    const size_t n = (size_t)nx * ny * nz * maxgate * (ns + nd);
+    int rc = ensure((float**)&s->d_out, &s->out_cap, n);
+    if (rc) {
+        return rc;
+    }
+    s->out_valid = false;
+    MCXG_TRY(cudaMemcpyAsync(s->d_out, field, sizeof(float) * n, cudaMemcpyHostToDevice, s->st));
+    return adjoint_run(s, kind, (const float*)s->d_out, ns, nd, nx, ny, nz, maxgate, out);
 }
 
 int mcxg_get_field_f64(mcxg_session* s, double* out) {

@@ -106,16 +106,21 @@ def jdata_decode(obj):
 
 
 def save_jdet(path, detp, hdr, prop, seeds=None, zipped=True):
-    """Detected photons as JData JSON.  prop: medianum rows {mua, mus, g, n} per mm."""
+    """Detected photons as JData JSON.  prop: medianum rows {mua, mus, g, n}
+    in the run's length unit (mua and mus are divided by the header's
+    unitinmm, as the reference writes them per mm).  Header floats are the
+    float32 values the reference's header holds."""
     detp = np.asarray(detp, np.float32)
     h = dict(hdr)
+    f32 = np.float32
+    unit = f32(h["unitinmm"])
     info = {"Version": h["version"], "MediaNum": h["maxmedia"], "DetNum": h["detnum"], "ColumnNum": h["colcount"],
             "TotalPhoton": h["totalphoton"], "DetectedPhoton": int(detp.shape[1]), "SavedPhoton": h["savedphoton"],
-            "LengthUnit": h["unitinmm"], "SeedByte": h["seedbyte"], "Normalizer": h["normalizer"],
+            "LengthUnit": float(unit), "SeedByte": h["seedbyte"], "Normalizer": float(f32(h["normalizer"])),
             "Repeat": h["respin"], "SrcNum": h["srcnum"], "SaveDetFlag": h["savedetflag"],
             "TotalSource": h["totalsource"],
-            "Media": [{"mua": float(r[0]), "mus": float(r[1]), "g": float(r[2]), "n": float(r[3])}
-                      for r in np.asarray(prop, np.float64).reshape(-1, 4)]}
+            "Media": [{"mua": float(r[0] / unit), "mus": float(r[1] / unit), "g": float(r[2]), "n": float(r[3])}
+                      for r in np.asarray(prop, f32).reshape(-1, 4)]}
     data = {}
     col = 0
     n = detp.shape[1]
@@ -146,16 +151,27 @@ def load_jdet(path):
     return {k: jdata_decode(v) for k, v in d["PhotonData"].items()}, d["Info"]
 
 
-def save_jnii(path, vol, voxelsize=(1.0, 1.0, 1.0), name="", description="MCX volumetric output", zipped=True):
-    """A volume ([Nx, Ny, Nz(, gates, ...)], x fastest as run() returns it) as JNIfTI JSON."""
+# NIFTIHeader.Description by output type (src/mcx_utils.c:814-819)
+_JNII_DESCRIPTION = ["MCX volumetric output: Fluence rate (W/mm^2)", "MCX volumetric output: Fluence (J/mm^2)",
+                     "MCX volumetric output: Voxel-wise energy deposit (J)",
+                     "MCX volumetric output: Jacobian for mua (J/mm)", "MCX volumetric output: Scattering count",
+                     "MCX volumetric output: Partial momentum transfer"]
+
+
+def save_jnii(path, vol, voxelsize=(1.0, 1.0, 1.0), name="", outputtype=0, maxgate=1, zipped=True):
+    """A volume ([Nx, Ny, Nz(, gates, ...)], x fastest as run() returns it) as
+    JNIfTI JSON, with the header the reference writes (mcx_savejnii,
+    src/mcx_utils.c:761-884): Name the session, LastSliceID the gate count,
+    Description by output type (0 flux .. 5 momentum; -1 the generic one)."""
     v = np.asarray(vol, np.float32)
     dims = list(v.shape)
-    vs = list(voxelsize) + [1.0] * (len(dims) - len(voxelsize))
+    vs = [float(np.float32(x)) for x in list(voxelsize) + [1.0] * (len(dims) - len(voxelsize))]
+    desc = _JNII_DESCRIPTION[outputtype] if 0 <= outputtype < len(_JNII_DESCRIPTION) else "MCX volumetric output"
     hdr = {"NIIHeaderSize": 348, "Dim": dims, "Param1": 0, "Param2": 0, "Param3": 0, "Intent": 0,
            "DataType": "single", "BitDepth": 32, "FirstSliceID": 0, "VoxelSize": vs[:len(dims)],
            "Orientation": {"x": "r", "y": "a", "z": "s"}, "ScaleSlope": 1, "ScaleOffset": 0,
-           "LastSliceID": dims[3] if len(dims) > 3 else 1, "SliceType": 1, "Unit": {"L": "mm", "T": "s"},
-           "MaxIntensity": 1, "MinIntensity": 0, "SliceTime": 0, "TimeOffset": 0, "Description": description,
+           "LastSliceID": int(maxgate), "SliceType": 1, "Unit": {"L": "mm", "T": "s"},
+           "MaxIntensity": 1, "MinIntensity": 0, "SliceTime": 0, "TimeOffset": 0, "Description": desc,
            "AuxFile": "", "QForm": 0, "SForm": 1, "Quatern": {"b": 0, "c": 0, "d": 0},
            "QuaternOffset": {"x": 0, "y": 0, "z": 0}, "Affine": [[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0]],
            "Name": name, "NIIFormat": "jnifti"}
@@ -165,7 +181,11 @@ def save_jnii(path, vol, voxelsize=(1.0, 1.0, 1.0), name="", description="MCX vo
     with open(path, "w") as f:
         json.dump({"_DataInfo_": {"JNIFTIVersion": "0.5", "Comment": "Created by mcxcl_gb300",
                                   "AnnotationFormat": "https://neurojson.org/jnifti/draft1",
-                                  "SerialFormat": "https://json.org"},
+                                  "SerialFormat": "https://json.org",
+                                  "Parser": {"Python": ["https://neurojson.org/download/pyjdata",
+                                                        "https://neurojson.org/download/pybjdata"],
+                                             "MATLAB": ["https://neurojson.org/download/jnifty",
+                                                        "https://neurojson.org/download/jsonlab"]}},
                    "NIFTIHeader": hdr, "NIFTIData": data}, f, indent=1)
         f.write("\n")
 

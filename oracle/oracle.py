@@ -425,3 +425,97 @@ def cube60(**kw):
     }
     cfg.update(kw)
     return cfg
+
+
+# ---------------------------------------------------------------- host layer
+
+class RefCfgSummary(ctypes.Structure):
+    """oracle/ref_utils.c refcfg_summary"""
+    _fields_ = ([("dim", ctypes.c_uint * 3)] +
+                [(n, ctypes.c_uint) for n in ("medianum", "detnum", "maxgate", "srcnum", "extrasrclen", "savedetflag",
+                                               "debuglevel", "maxdetphoton")] +
+                [(n, ctypes.c_int) for n in ("srctype", "seed", "isreflect", "issavedet", "issave2pt", "isnormalized",
+                                              "outputtype", "mediabyte", "issrcfrom0", "issaveseed", "issaveexit",
+                                              "issaveref", "ismomentum", "isspecular", "autopilot", "srcid")] +
+                [("nphoton", ctypes.c_double)] +
+                [(n, ctypes.c_float) for n in ("tstart", "tstep", "tend", "unitinmm", "minenergy")] +
+                [("steps", ctypes.c_float * 3)] +
+                [(n, ctypes.c_float * 4) for n in ("srcpos", "srcdir", "srcparam1", "srcparam2")] +
+                [("bc", ctypes.c_char * 13), ("session", ctypes.c_char * 64)])
+
+
+CONFIG_SCALARS = ["medianum", "detnum", "maxgate", "srcnum", "extrasrclen", "savedetflag", "debuglevel", "maxdetphoton",
+                  "srctype", "seed", "isreflect", "issavedet", "issave2pt", "isnormalized", "outputtype", "mediabyte",
+                  "issrcfrom0", "issaveseed", "issaveexit", "issaveref", "ismomentum", "isspecular", "autopilot",
+                  "srcid", "nphoton", "tstart", "tstep", "tend", "unitinmm", "minenergy"]
+
+
+def refutils():
+    path = os.path.join(HERE, "_ref", "libmcxrefutils.so")
+    if path not in _ref:
+        _ref[path] = ctypes.CDLL(path)
+    return _ref[path]
+
+
+def refutils_available():
+    return os.path.exists(os.path.join(HERE, "_ref", "libmcxrefutils.so"))
+
+
+def ref_readconfig(path):
+    """The reference's mcx_readconfig on a JSON input (loading, shapes,
+    preprocessing, detector mask): scalars, media, detectors and volume words
+    of the loaded configuration."""
+    R = refutils()
+    s = RefCfgSummary()
+    R.mcxref_readconfig(path.encode(), ctypes.byref(s))
+    n = s.dim[0] * s.dim[1] * s.dim[2]
+    vol = np.zeros(n, np.uint32)
+    prop = np.zeros((s.medianum, 4), np.float32)
+    det = np.zeros((max(s.detnum, 1), 4), np.float32)
+    R.mcxref_copyconfig(_ptr(prop), _ptr(det), _ptr(vol))
+    R.mcxref_release()
+    out = {k: getattr(s, k) for k in CONFIG_SCALARS}
+    out.update(dim=list(s.dim), steps=list(s.steps), bc=s.bc.decode(errors="replace"), session=s.session.decode(),
+               prop=prop, detpos=det[:s.detnum], vol=vol,
+               **{k: np.asarray(list(getattr(s, k)), np.float32) for k in ("srcpos", "srcdir", "srcparam1", "srcparam2")})
+    return out
+
+
+def ref_savedet(session, hist, histf, prop, detp, seeds, issaveseed, jdat):
+    """The reference's detected-photon writer (mcx_savedetphoton / .jdat
+    mcx_savejdet) into the current directory: hist = {version, maxmedia,
+    detnum, colcount, totalphoton, detected, savedphoton, seedbyte, respin,
+    srcnum, savedetflag, totalsource}, histf = {unitinmm, normalizer}, prop
+    [maxmedia + 1, 4]; detp [count, colcount] float32, seeds [count, 16] uint8."""
+    R = refutils()
+    h = np.asarray(hist, np.uint32)
+    hf = np.asarray(histf, np.float32)
+    d = np.ascontiguousarray(detp, np.float32)
+    sd = np.ascontiguousarray(seeds, np.uint8) if seeds is not None else None
+    pr = np.ascontiguousarray(prop, np.float32)
+    R.mcxref_savedet(session.encode(), _ptr(h), _ptr(hf), _ptr(pr), _ptr(d), _ptr(sd), ctypes.c_int(d.shape[0]),
+                     ctypes.c_int(issaveseed), ctypes.c_int(jdat))
+
+
+def ref_savejnii(vol, voxelsize, name, session="", maxgate=1, outputtype=0):
+    """The reference's JNIfTI writer on a float32 volume (x fastest) into
+    <name>.jnii, with the header's Name, LastSliceID and Description from
+    session, maxgate and outputtype."""
+    R = refutils()
+    v = np.asfortranarray(np.asarray(vol, np.float32))
+    flat = np.ascontiguousarray(v.ravel(order="F"))
+    dims = np.asarray(v.shape, np.uint32)
+    vs = np.asarray(list(voxelsize) + [1.0] * (v.ndim - len(voxelsize)), np.float32)
+    R.mcxref_savejnii(_ptr(flat), ctypes.c_int(v.ndim), _ptr(dims), _ptr(vs), name.encode(), session.encode(),
+                      ctypes.c_uint(maxgate), ctypes.c_int(outputtype))
+
+
+def ref_adjoint(kind, field, ns, nd, nx, ny, nz, maxgate):
+    """The reference's adjoint post-kernels (mcx_core.cl:3393-3512) on a float32
+    field [nx ny nz maxgate (ns + nd)] (x fastest): [nx ny nz ns nd] floats."""
+    R = reflib()
+    f = np.ascontiguousarray(np.asarray(field, np.float32).ravel(order="F"))
+    out = np.zeros(nx * ny * nz * ns * nd, np.float32)
+    R.mcxref_adjoint(ctypes.c_int(kind), _ptr(f), _ptr(out), ctypes.c_uint(nx * ny * nz), ctypes.c_uint(maxgate),
+                     ctypes.c_uint(ns), ctypes.c_uint(nd), ctypes.c_uint(nx), ctypes.c_uint(ny))
+    return out

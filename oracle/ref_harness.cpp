@@ -11,6 +11,7 @@
  * order as the oracle's serial mode and the outputs compare bit for bit.
  */
 #include "ref_shim.hpp"
+#define MCX_ADJOINT_MODE       /* the adjoint post-kernels (mcx_core.cl:3313-3514) */
 #include "mcx_core.cl"
 
 #include "mcx_oracle.h"
@@ -259,4 +260,22 @@ extern "C" void mcxref_mie(double x, double mrel, float* smatrix, double* qsca, 
         mu[i] = cos((double)(3.1415926535897932f * i / (181 - 1)));
     }
     Mie(x, mrel, mu.data(), (float4*)smatrix, qsca, g);
+}
+
+/* The reference's adjoint post-kernels, one voxel per emulated thread:
+   kind 0 mcx_adjoint_kernel (phi_src x phi_det), 1 mcx_adjoint_dcoeff_kernel
+   (grad phi_src . grad phi_det), real fields (gfield_im NULL). */
+extern "C" void mcxref_adjoint(int kind, float* field, float* out, unsigned int dimxyz, unsigned int maxgate,
+                               unsigned int ns, unsigned int nd, unsigned int nx, unsigned int ny) {
+    blockDim = make_uint3(1, 1, 1);
+    gridDim = make_uint3(dimxyz, 1, 1);
+    threadIdx = make_uint3(0, 0, 0);
+    for (unsigned int v = 0; v < dimxyz; v++) {
+        blockIdx = make_uint3(v, 0, 0);
+        if (kind == 0) {
+            mcx_adjoint_kernel(field, nullptr, out, dimxyz, maxgate, ns, nd);
+        } else {
+            mcx_adjoint_dcoeff_kernel(field, nullptr, out, dimxyz, maxgate, ns, nd, nx, ny);
+        }
+    }
 }
