@@ -449,6 +449,10 @@ int  mcxg_adjoint_field(mcxg_session* s, int kind, const float* field, uint32_t 
                         uint32_t ny, uint32_t nz, uint32_t maxgate, float* out);
 /* Field: the compensated accumulator in FP64, unscaled. */
 int  mcxg_get_field_f64(mcxg_session* s, double* out);
+/* The compensated field's raw planes (fieldlen x components each, NULL
+   skips one): the float high plane, the float low plane and the int32 spill
+   count; an element's value is hi + lo + 1024 x count. */
+int  mcxg_get_field_planes(mcxg_session* s, float* hi, float* lo, int32_t* count);
 /* The precision check's fields of the last MCXG_VERIFY launch, unscaled,
    fieldlen values each (NULL skips one): the FP64 accumulation of the same
    deposits, the plain float accumulation, and the spill accumulation with

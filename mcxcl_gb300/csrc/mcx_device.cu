@@ -1233,6 +1233,30 @@ int mcxg_get_field_f64(mcxg_session* s, double* out) {
     return MCXG_OK;
 }
 
+int mcxg_get_field_planes(mcxg_session* s, float* hi, float* lo, int32_t* count) {
+    if (!s || !s->has_problem) {
+        return MCXG_ERR_STATE;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    /* component c's planes start at 3 c fieldlen: copy each plane of each component */
+    const size_t F = s->kp.fieldlen;
+    for (size_t c = 0; c < field_comps(s->kp); c++) {
+        const float* base = s->d_field + kFieldPlanes * c * F;
+        if (hi) {
+            MCXG_TRY(cudaMemcpyAsync(hi + c * F, base, sizeof(float) * F, cudaMemcpyDeviceToHost, s->st));
+        }
+        if (lo) {
+            MCXG_TRY(cudaMemcpyAsync(lo + c * F, base + F, sizeof(float) * F, cudaMemcpyDeviceToHost, s->st));
+        }
+        if (count) {
+            MCXG_TRY(cudaMemcpyAsync(count + c * F, base + 2 * F, sizeof(int32_t) * F, cudaMemcpyDeviceToHost,
+                                     s->st));
+        }
+    }
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
 int mcxg_get_verify(mcxg_session* s, double* f64, float* plain, float* spill) {
     if (!s || !s->has_problem || !s->d_acc64 || s->acc64_cap < s->kp.fieldlen) {
         return MCXG_ERR_STATE;

@@ -1,4 +1,5 @@
-"""Differentiable detector readings: d(readings)/d(mua, mus) by photon replay.
+"""Differentiable detector readings and fluence: d/d(mua, mus) per voxel or
+per label.
 
 The forward pass runs the transport kernel on a per-voxel float mua volume
 (the reference's MEDIA_MUA_FLOAT format, src/mcx_core.cl:1093-1096) and
@@ -30,6 +31,17 @@ the pmcxcl-compatible ``run()``; tensors cross as host arrays.
 import numpy as np
 
 from . import pmcxcl
+
+
+def _replay_threads(n):
+    """Thread layout of a replay: at least one reference thread per replayed
+    photon.  The reference's replay indexes photon seeds as
+    threadid * threadphoton + min(threadid, oddphoton - 1) + k
+    (mcx_core.cl:1591, 2847), which, whenever the thread count does not divide
+    the replayed photons, replays photon oddphoton * (threadphoton + 1) - 1
+    twice and the last photon never; with threadphoton 0 every thread that
+    runs a photon runs its own."""
+    return dict(autopilot=0, nthread=max(64, -(-int(n) // 64) * 64), nblocksize=64)
 
 
 class ReplayGradient:
@@ -79,7 +91,8 @@ class ReplayGradient:
         L = self.last
         cfg = dict(self.cfg, vol=L["mua"][None], prop=L["prop"], seed=L["seeds"],
                    replayweight=a.astype(np.float32), replaytof=L["tof"], replaydetid=L["detid"].astype(np.int32),
-                   outputtype=outputtype, isnormalized=0, issaveseed=0, savedetweight=0, replaysiteown=siteown)
+                   outputtype=outputtype, isnormalized=0, issaveseed=0, savedetweight=0, replaysiteown=siteown,
+                   **_replay_threads(a.size))
         res = self.run(cfg)
         return res["flux"][..., 0].astype(np.float64), res
 
@@ -103,6 +116,101 @@ class ReplayGradient:
         FN, _ = self._replay(a, "nscat", siteown=1)
         mus = float(L["prop"][1, 1]) * self.unitinmm
         return gmua, FN / mus - self.unitinmm * FJ
+
+
+class LabelReadings:
+    """Detector readings of a label volume as functions of every label's mua
+    and mus.  No replay is needed: a detected photon's partial path length
+    and scattering count in each label -- the per-medium columns of its
+    detected record (savedetflag 'dsp', mcx_core.cl:867-926, scatter counts
+    kept as integer bits as the reference keeps them) -- are exactly the
+    per-label sums of L_iv and n_iv:
+
+        dR_d/dmua_k = -(u/N) sum_{i in d} w_i P_ik
+        dR_d/dmus_k =  (1/N) sum_{i in d} w_i (n_ik / mus_k - u P_ik)
+
+    (P_ik in voxels, u the voxel size in mm, mua and mus per mm).  The
+    per-voxel replay Jacobian summed over a label's voxels gives the same
+    mua column; the seed is fixed, so repeated forwards share random
+    numbers.  cfg: a ``run()`` dictionary with a label ``vol`` and ``prop``."""
+
+    def __init__(self, cfg, run=None):
+        self.run = run or pmcxcl.run
+        self.cfg = dict(cfg)
+        self.cfg.update(issavedet=1, issaveseed=1, savedetweight=1, savedetflag="dsp")
+        self.nphoton = float(self.cfg["nphoton"])
+        self.ndet = int(np.asarray(self.cfg["detpos"]).reshape(-1, 4).shape[0])
+        self.unitinmm = float(self.cfg.get("unitinmm", 1.0))
+        self.prop0 = np.array(self.cfg["prop"], np.float32).reshape(-1, 4).copy()
+        self.nmed = self.prop0.shape[0] - 1
+        self.last = None
+
+    def forward(self, mua=None, mus=None):
+        """mua, mus: per label 1..nmed (None keeps the configuration's).
+        Returns the readings R [ndet] (float64)."""
+        prop = self.prop0.copy()
+        if mua is not None:
+            prop[1:, 0] = np.asarray(mua, np.float32)
+        if mus is not None:
+            prop[1:, 1] = np.asarray(mus, np.float32)
+        res = self.run(dict(self.cfg, prop=prop))
+        m = self.nmed
+        if "detp" in res:
+            d = np.asarray(res["detp"])
+            detid = d[0].astype(np.int64) & 0xFFFF
+            nscat = np.ascontiguousarray(d[1:1 + m]).view(np.uint32).astype(np.float64)
+            ppath = d[1 + m:1 + 2 * m].astype(np.float64)
+            w = res["detweight"][0].astype(np.float64)
+            tof = res["detweight"][1].astype(np.float32)
+            seeds = res["seeds"]
+        else:
+            detid = np.zeros(0, np.int64)
+            nscat = ppath = np.zeros((m, 0))
+            w = np.zeros(0)
+            tof = np.zeros(0, np.float32)
+            seeds = np.zeros((16, 0), np.uint8)
+        R = np.bincount(detid - 1, weights=w, minlength=self.ndet)[:self.ndet] / self.nphoton
+        self.last = dict(prop=prop, detid=detid, w=w, tof=tof, seeds=seeds, nscat=nscat, ppath=ppath,
+                         stat=res["stat"])
+        return R
+
+    def jacobian(self):
+        """(dR/dmua, dR/dmus), each [ndet, nmed], per mm, of the last forward."""
+        L = self.last
+        if L is None:
+            raise RuntimeError("jacobian() needs a forward() first")
+        u = self.unitinmm
+        mus = L["prop"][1:, 1].astype(np.float64)
+        Ja = np.zeros((self.ndet, self.nmed))
+        Js = np.zeros((self.ndet, self.nmed))
+        for k in range(self.nmed):
+            wa = -u * L["w"] * L["ppath"][k]
+            ws = L["w"] * ((L["nscat"][k] / mus[k] if mus[k] > 0 else 0.0) - u * L["ppath"][k])
+            Ja[:, k] = np.bincount(L["detid"] - 1, weights=wa, minlength=self.ndet)[:self.ndet]
+            Js[:, k] = np.bincount(L["detid"] - 1, weights=ws, minlength=self.ndet)[:self.ndet]
+        return Ja / self.nphoton, Js / self.nphoton
+
+    def backward(self, grad_R):
+        """dLoss/dR [ndet] -> (dLoss/dmua, dLoss/dmus), each [nmed]."""
+        Ja, Js = self.jacobian()
+        g = np.asarray(grad_R, np.float64).ravel()
+        return g @ Ja, g @ Js
+
+    def replay_mua_gradient(self, grad_R):
+        """dLoss/dmua per label from the replay Jacobian (mcx_core.cl:2845-2858):
+        the detected photons relaunched from their seeds, each with replay
+        weight dLoss/dR_d w_i / N, the per-voxel output summed over each
+        label's voxels."""
+        L = self.last
+        g = np.asarray(grad_R, np.float64).ravel()
+        a = g[L["detid"] - 1] * L["w"] / self.nphoton
+        cfg = dict(self.cfg, prop=L["prop"], seed=L["seeds"], replayweight=a.astype(np.float32),
+                   replaytof=L["tof"], replaydetid=L["detid"].astype(np.int32), outputtype="jacobian",
+                   isnormalized=0, issaveseed=0, savedetweight=0, **_replay_threads(a.size))
+        F = self.run(cfg)["flux"].astype(np.float64)
+        F = F.reshape(F.shape[:3] + (-1,)).sum(axis=3)      # every time gate of the detected photons
+        vol = np.asarray(self.cfg["vol"])
+        return np.array([-self.unitinmm * F[vol == k + 1].sum() for k in range(self.nmed)])
 
 
 def readings(sim, mua, mus=None):
@@ -130,3 +238,24 @@ def readings(sim, mua, mus=None):
             return torch.as_tensor(gmua, dtype=ctx.dtype, device=ctx.dev), gm
 
     return _Readings.apply(mua, mus)
+
+
+def label_readings(sim, mua, mus):
+    """Detector readings as a differentiable torch function of the per-label
+    mua and mus tensors ([nmed] each) of a LabelReadings setup."""
+    import torch
+
+    class _LabelReadings(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, mua_t, mus_t):
+            R = sim.forward(mua_t.detach().cpu().numpy(), mus_t.detach().cpu().numpy())
+            ctx.dev, ctx.dtype = mua_t.device, mua_t.dtype
+            return torch.as_tensor(R, dtype=torch.float64, device=mua_t.device)
+
+        @staticmethod
+        def backward(ctx, gR):
+            ga, gs = sim.backward(gR.detach().cpu().numpy())
+            return (torch.as_tensor(ga, dtype=ctx.dtype, device=ctx.dev),
+                    torch.as_tensor(gs, dtype=ctx.dtype, device=ctx.dev))
+
+    return _LabelReadings.apply(mua, mus)

@@ -21,7 +21,8 @@ from mcxcl_gb300 import diff, workloads
 
 def _oracle_engine(O):
     def run(cfg):
-        r = O.run(cfg, nthread=2048, core=2048, mathmode=O.MATH_LIBM, fieldmode=O.FIELD_DOUBLE)
+        nt = int(cfg["nthread"]) if cfg.get("autopilot", 1) == 0 and "nthread" in cfg else 2048
+        r = O.run(cfg, nthread=nt, core=nt, mathmode=O.MATH_LIBM, fieldmode=O.FIELD_DOUBLE)
         out = {"flux": r["flux"], "stat": {"detected": r["stat"]["detected"]}}
         if r["detp"].size:
             out["detp"] = r["detp"]
@@ -150,3 +151,76 @@ def test_torch_autograd_routes_through_replay(c4):
     loss.backward()
     ref = sim.backward(_dloss(R.detach().numpy(), Rt))
     np.testing.assert_allclose(m.grad.numpy(), ref.astype(np.float32), rtol=1e-6, atol=1e-12)
+
+
+# ------------------------------------------------------- per-label gradients
+
+def _label_cfg(nphoton):
+    import cases
+    cfg = cases.small_two_media(nphoton=nphoton, savedetflag="dsp", seed=31)
+    cfg["detpos"] = [[20, 10, 0, 2], [10, 20, 0, 2], [30, 20, 0, 2], [20, 30, 0, 2]]
+    return cfg
+
+
+def test_label_gradient_matches_fd_and_replay_on_oracle(oracle_mod):
+    """Per-label mua gradient from the detected records' partial paths:
+    central differences with common random numbers (the paths do not move),
+    and the replay Jacobian summed over each label's voxels (the replay
+    output pinned to the reference's, mcx_core.cl:2845-2858)."""
+    cfg = _label_cfg(100000)
+    sim = diff.LabelReadings(cfg, run=_oracle_engine(oracle_mod))
+    mua0 = sim.prop0[1:, 0].copy()
+    Rt = sim.forward(mua0 * 1.3)
+    R = sim.forward()
+    g = _dloss(R, Rt)
+    ga, gs = sim.backward(g)
+    assert np.all(np.isfinite(gs)) and len(sim.last["w"]) > 200
+    for k in range(sim.nmed):
+        h = 1e-3 * mua0[k]
+        mp, mm = mua0.copy(), mua0.copy()
+        mp[k] += h
+        mm[k] -= h
+        fd = (_loss(sim.forward(mp), Rt) - _loss(sim.forward(mm), Rt)) / float(np.float32(mp[k]) - np.float32(mm[k]))
+        assert abs(ga[k] / fd - 1) < 0.02, (k, ga[k], fd)
+    sim.forward()
+    rep = sim.replay_mua_gradient(g)
+    np.testing.assert_allclose(rep, ga, rtol=1e-5)
+
+
+@pytest.mark.gpu
+def test_label_gradients_on_gpu():
+    """The cube + sphere medium (labels 1 and 2), 4 detectors, 2e6 photons:
+    per-label mua gradients against central differences with common random
+    numbers (2 %) and against the replay Jacobian summed per label; per-label
+    mus gradients against central differences over +-5 % (mus moves the paths,
+    so those differences are statistical: 10 %); torch.autograd routes."""
+    import torch
+    cfg = dict(workloads.builtin("cubesph60b"), nphoton=2000000, seed=77)
+    sim = diff.LabelReadings(cfg)
+    mua0, mus0 = sim.prop0[1:, 0].copy(), sim.prop0[1:, 1].copy()
+    Rt = sim.forward(mua0 * np.float32(1.2), mus0 * np.float32(0.9))
+    R = sim.forward()
+    g = _dloss(R, Rt)
+    ga, gs = sim.backward(g)
+    for k in range(sim.nmed):
+        h = 1e-3 * mua0[k]
+        mp, mm = mua0.copy(), mua0.copy()
+        mp[k] += h
+        mm[k] -= h
+        fd = (_loss(sim.forward(mp), Rt) - _loss(sim.forward(mm), Rt)) / float(np.float32(mp[k]) - np.float32(mm[k]))
+        assert abs(ga[k] / fd - 1) < 0.02, ("mua", k, ga[k], fd)
+    sim.forward()
+    np.testing.assert_allclose(sim.replay_mua_gradient(g), ga, rtol=1e-3)
+    for k in range(sim.nmed):
+        h = 0.05 * mus0[k]
+        sp, sm = mus0.copy(), mus0.copy()
+        sp[k] += h
+        sm[k] -= h
+        fd = (_loss(sim.forward(None, sp), Rt) - _loss(sim.forward(None, sm), Rt)) / float(2 * h)
+        assert abs(gs[k] - fd) <= 0.1 * abs(fd), ("mus", k, gs[k], fd)
+    a = torch.tensor(mua0, requires_grad=True)
+    s = torch.tensor(mus0, requires_grad=True)
+    Rtt = diff.label_readings(sim, a, s)
+    ((torch.log(Rtt) - torch.log(torch.tensor(Rt))) ** 2).sum().backward()
+    np.testing.assert_allclose(a.grad.numpy(), ga.astype(np.float32), rtol=1e-5)
+    np.testing.assert_allclose(s.grad.numpy(), gs.astype(np.float32), rtol=1e-5)
