@@ -331,6 +331,9 @@ void mcx_release_sessions(void);
 #define MCXG_GRAPH   32u   /* batch: capture the run as a CUDA graph once, replay it afterwards */
 #define MCXG_GENERAL 64u   /* fast kernel: the general instantiation even where the one specialised for the
                               common configuration (label volume, 3-D, Henyey-Greenstein) applies */
+#define MCXG_ADJ1   256u   /* fluence gradient, pass 1: each photon's loss total (mcxg_set_adjoint first) */
+#define MCXG_ADJ2   512u   /* fluence gradient, pass 2: the gradients, same photons (read with
+                              mcxg_get_adjoint_grad) */
 #define MCXG_VERIFY 128u   /* precision check (fast kernel, common configuration, no replay, no KEEP): every
                               deposit also goes to an FP64 field, a plain float field and a float field with
                               the reference's +-1000 spill plane; read them with mcxg_get_verify */
@@ -389,7 +392,7 @@ int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
    into the concatenated volume (one byte per voxel, label | detector
    bit << 7) and field.  Reference threads are numbered contiguously across
    the batch (vt_off); seeds come from splitmix64 of the simulation's seed.
-   The simulations run in waves of 140, whose descriptors the kernel reads
+   The simulations run in waves of 136, whose descriptors the kernel reads
    from constant memory.  Not supported in a batch: detectors, replay, extra
    sources, patterns, phase tables, encodings other than labels. */
 int  mcxg_batch_set(mcxg_session* s, const void* sims, size_t desc_size, uint32_t nsim, const uint8_t* media,
@@ -400,7 +403,7 @@ int  mcxg_batch_set(mcxg_session* s, const void* sims, size_t desc_size, uint32_
 int  mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms);
 /* Per simulation: FP64 {escaped, launched} weight, 2 x nsim. */
 int  mcxg_batch_get_energy(mcxg_session* s, double* out);
-/* Every simulation's field, (hi + lo + 1024 x spill count) x scales[i], at its field offset. */
+/* Every simulation's field, the compensated accumulator in FP64 x scales[i], at its field offset. */
 int  mcxg_batch_get_field(mcxg_session* s, float* out, const double* scales);
 /* Replay inputs, one entry per replayed photon: the saved xorshift128+ state
    (16 bytes), detected weight, time of flight and detector id.  Used when
@@ -420,8 +423,8 @@ int  mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms);
 int  mcxg_get_energy(mcxg_session* s, double* escaped, double* launched);
 /* Per-thread {escaped, launched} floats, 2 x nthread. */
 int  mcxg_get_thread_energy(mcxg_session* s, float* out);
-/* Field: the compensated accumulator (hi + lo + 1024 x spill count) in FP64, times scale,
-   rounded to float; fieldlen values. */
+/* Field: the compensated accumulator (fixed-point count x unit + remainder) in FP64, times
+   scale, rounded to float; fieldlen values. */
 int  mcxg_get_field(mcxg_session* s, float* out, double scale);
 /* Field split into nblocks equal blocks, block b scaled by scales[b]
    (a replay with one output per detector). */
@@ -449,10 +452,20 @@ int  mcxg_adjoint_field(mcxg_session* s, int kind, const float* field, uint32_t 
                         uint32_t ny, uint32_t nz, uint32_t maxgate, float* out);
 /* Field: the compensated accumulator in FP64, unscaled. */
 int  mcxg_get_field_f64(mcxg_session* s, double* out);
+/* Fluence gradient (no counterpart in the reference, which differentiates
+   detector readings only, by replay): for a loss L of the raw flux or
+   fluence field, dloss = dL/dfield (fieldlen floats).  Then mcxg_simulate
+   with MCXG_ADJ1 and with MCXG_ADJ2 rerun the problem's photons (same seeds)
+   and mcxg_get_adjoint_grad returns dL/dmua and dL/dmus per voxel (nvox
+   floats each, per voxel-unit coefficient: multiply by unitinmm for per mm).
+   The paths must not depend on mua: no Russian roulette. */
+int  mcxg_set_adjoint(mcxg_session* s, const float* dloss, uint32_t n);
+int  mcxg_get_adjoint_grad(mcxg_session* s, float* gmua, float* gmus);
 /* The compensated field's raw planes (fieldlen x components each, NULL
-   skips one): the float high plane, the float low plane and the int32 spill
-   count; an element's value is hi + lo + 1024 x count. */
-int  mcxg_get_field_planes(mcxg_session* s, float* hi, float* lo, int32_t* count);
+   skips one): the int64 fixed-point counts and the float remainders; an
+   element's value is count x 2^-S + remainder, with 2^-S the unit the host
+   chose for the problem (field_scale in the host driver). */
+int  mcxg_get_field_planes(mcxg_session* s, int64_t* counts, float* rem);
 /* The precision check's fields of the last MCXG_VERIFY launch, unscaled,
    fieldlen values each (NULL skips one): the FP64 accumulation of the same
    deposits, the plain float accumulation, and the spill accumulation with

@@ -118,7 +118,7 @@ EXPORTS = [
     "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_field_interleaved", "mcxg_set_polarization", "mcx_mie", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",
     "mcxg_batch_simulate", "mcxg_batch_get_energy", "mcxg_batch_get_field", "mcx_savedetphoton",
     "mcxg_adjoint", "mcxg_get_verify", "mcx_readconfig", "mcx_parsejson", "mcxg_adjoint_field",
-    "mcxg_get_field_planes",
+    "mcxg_get_field_planes", "mcxg_set_adjoint", "mcxg_get_adjoint_grad",
 ]
 
 _lib = None
@@ -172,7 +172,9 @@ def load():
     L.mcxg_get_field.argtypes = [vp, vp, ctypes.c_double]
     L.mcxg_get_field_f64.argtypes = [vp, vp]
     L.mcxg_get_verify.argtypes = [vp, vp, vp, vp]
-    L.mcxg_get_field_planes.argtypes = [vp, vp, vp, vp]
+    L.mcxg_get_field_planes.argtypes = [vp, vp, vp]
+    L.mcxg_set_adjoint.argtypes = [vp, vp, ctypes.c_uint32]
+    L.mcxg_get_adjoint_grad.argtypes = [vp, vp, vp]
     u32 = ctypes.c_uint32
     L.mcxg_adjoint_field.argtypes = [vp, ctypes.c_int, vp, u32, u32, u32, u32, u32, u32, vp]
     L.mcxg_get_detected.argtypes = [vp, vp, vp, P(ctypes.c_uint32)]

@@ -84,6 +84,11 @@ struct mcxg_session {
     bool out_valid = false;          /* d_out holds the last normalised float field */
     float* d_adj = nullptr;          /* adjoint Jacobians */
     size_t adj_cap = 0;
+    float* d_adjc = nullptr;         /* fluence gradient: dLoss/d(raw field), fieldlen */
+    size_t adjc_cap = 0;
+    float* d_adjJ = nullptr;         /* per-photon loss totals, nthread x (threadphoton + 1) */
+    size_t adjJ_cap = 0;
+    bool adj_ready = false;
     double* d_acc64 = nullptr;       /* precision check: FP64, plain float and spill fields */
     size_t acc64_cap = 0;
     float* d_accf = nullptr;
@@ -132,10 +137,9 @@ namespace {
 
 constexpr int kRedBlocks = 256;
 constexpr int kRedThreads = 256;
-/* the transport kernel's compensated field: hi, lo and spill-count planes per
-   component; a count stands for kSpill (the kernel's K_SPILL) */
+/* the transport kernel's compensated field: an int64 fixed-point plane and a
+   float remainder plane per component, 3 floats of memory per element */
 constexpr size_t kFieldPlanes = 3;
-constexpr double kSpill = 1024.0;
 
 int cuda_status(cudaError_t e) {
     if (e == cudaSuccess) {
@@ -215,41 +219,42 @@ __global__ void energy_final(double* part, int nblocks) {
     }
 }
 
-/* Output element i of a field of n elements per component: component
-   c = i / n (1 real, or real then imaginary for RF), element j = i % n; each
-   component is a high plane, its low plane and its spill-count plane:
-   value = hi + lo + kSpill x count in FP64. */
-__device__ __forceinline__ double merged_at(const float* __restrict__ f, size_t n, size_t i, size_t& j) {
+/* Output element i of a field of n elements per component and total
+   elements over all components: component c = i / n (1 real, or real then
+   imaginary for RF), element j = i % n.  The buffer holds the fixed-point
+   planes of all components (int64 counts of unit), then their float
+   remainder planes: value = count x unit + remainder in FP64. */
+__device__ __forceinline__ double merged_at(const float* __restrict__ f, size_t n, size_t total, double unit, size_t i,
+                                            size_t& j) {
     const size_t c = i / n;
     j = i - c * n;
-    const float* p = f + 3 * c * n;
-    return (double)p[j] + (double)p[n + j] + (double)kSpill * (double)((const int*)p)[2 * n + j];
+    return (double)((const long long*)f)[i] * unit + (double)f[2 * total + i];
 }
 
-__global__ void field_merge_f32(const float* __restrict__ f, size_t n, size_t total, double scale,
+__global__ void field_merge_f32(const float* __restrict__ f, size_t n, size_t total, double unit, double scale,
                                 float* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         size_t j;
-        out[i] = (float)(merged_at(f, n, i, j) * scale);
+        out[i] = (float)(merged_at(f, n, total, unit, i, j) * scale);
     }
 }
 
 /* element j belongs to source j % nsrc (photon sharing interleaves the
    patterns innermost) */
-__global__ void field_merge_interleaved(const float* __restrict__ f, size_t n, size_t total, unsigned int nsrc,
-                                        const double* __restrict__ scales, float* __restrict__ out) {
+__global__ void field_merge_interleaved(const float* __restrict__ f, size_t n, size_t total, double unit,
+                                        unsigned int nsrc, const double* __restrict__ scales, float* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         size_t j;
-        const double v = merged_at(f, n, i, j);
+        const double v = merged_at(f, n, total, unit, i, j);
         out[i] = (float)(v * scales[j % nsrc]);
     }
 }
 
-__global__ void field_merge_blocks(const float* __restrict__ f, size_t n, size_t total, size_t blocklen,
+__global__ void field_merge_blocks(const float* __restrict__ f, size_t n, size_t total, double unit, size_t blocklen,
                                    const double* __restrict__ scales, float* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         size_t j;
-        const double v = merged_at(f, n, i, j);
+        const double v = merged_at(f, n, total, unit, i, j);
         out[i] = (float)(v * scales[j / blocklen]);
     }
 }
@@ -310,8 +315,8 @@ __global__ void batch_merge(const float* __restrict__ f, unsigned long long tota
     const unsigned int n = d.kp.fieldlen;
     const double sc = scales[blockIdx.y];
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        out[off + i] = (float)(((double)f[off + i] + (double)f[off + i + total] +
-                                (double)kSpill * (double)((const int*)f)[off + i + 2 * total]) * sc);
+        out[off + i] = (float)(((double)((const long long*)f)[off + i] * (double)d.kp.fxunit +
+                                (double)f[2 * total + off + i]) * sc);
     }
 }
 
@@ -390,10 +395,11 @@ __global__ void adjoint_dcoeff(const float* __restrict__ f, float* __restrict__ 
     }
 }
 
-__global__ void field_merge_f64(const float* __restrict__ f, size_t n, size_t total, double* __restrict__ out) {
+__global__ void field_merge_f64(const float* __restrict__ f, size_t n, size_t total, double unit,
+                                double* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         size_t j;
-        out[i] = merged_at(f, n, i, j);
+        out[i] = merged_at(f, n, total, unit, i, j);
     }
 }
 
@@ -554,7 +560,8 @@ int mcxg_destroy(mcxg_session* s) {
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
                     s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw,
                     s->d_sims, s->d_simvt, s->d_simctr, s->d_smatrix, s->d_bmedia, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
-                    s->d_adj, s->d_lfib, s->d_jump, s->d_traj, s->d_acc64, s->d_accf, s->d_accs};
+                    s->d_adj, s->d_lfib, s->d_jump, s->d_traj, s->d_acc64, s->d_accf, s->d_accs, s->d_adjc,
+                    s->d_adjJ};
     if (s->bgraph_exec) {
         cudaGraphExecDestroy(s->bgraph_exec);
     }
@@ -882,6 +889,8 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     a.srcpattern = s->d_pattern;
     a.seeds = s->d_seeds;
     a.field = s->d_field;
+    a.fhi = (unsigned long long*)s->d_field;
+    a.flo = s->d_field + 2 * (size_t)kp.fieldlen * field_comps(kp);
     a.smatrix = s->d_smatrix;
     a.s0 = s->pol_s0;
     a.maxpol = s->npol;
@@ -910,7 +919,21 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     /* deposits go straight to the field unless aggregation is asked for or
        the autotuner found it faster for this problem */
     const bool verify = (flags & MCXG_VERIFY) != 0;
-    const bool noagg = verify || (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
+    const unsigned int adjmode = (flags & MCXG_ADJ1) ? 1u : ((flags & MCXG_ADJ2) ? 2u : 0u);
+    if (adjmode) {
+        /* the two passes of the fluence gradient: flux or fluence output, fast
+           kernel, no replay, the loss gradient set for this problem */
+        if (exact || verify || kp.replay || (flags & MCXG_KEEP) || !s->adj_ready || kp.is2d ||
+                !(kp.outputtype == otFlux || kp.outputtype == otFluence) || kp.omega > 0.f || s->npol ||
+                kp.mediaformat == 97 || kp.srcnum > 1 || s->maxjump || kp.minenergy > 0.f ||
+                s->adjJ_cap < (size_t)kp.nthread * (kp.threadphoton + 1u)) {
+            return MCXG_ERR_ARG;
+        }
+        a.adjc = s->d_adjc;
+        a.adjJ = s->d_adjJ;
+        a.adjmode = adjmode;
+    }
+    const bool noagg = verify || adjmode || (flags & MCXG_NOAGG) || !((flags & MCXG_AGG) || (s->tuned && !s->tuned_noagg));
     const bool rf = kp.omega > 0.f && !kp.replay;
     const bool pol = s->npol > 0;
     const bool svmc = kp.mediaformat == 97;
@@ -922,7 +945,7 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
                  (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
                  (common ? mcxg::LF_COMMON : 0) | (rf ? mcxg::LF_RF : 0) | (pol ? mcxg::LF_POL : 0) |
-                 (svmc ? mcxg::LF_SVMC : 0) | (verify ? mcxg::LF_ACC64 : 0);
+                 (svmc ? mcxg::LF_SVMC : 0) | (verify ? mcxg::LF_ACC64 : 0) | (adjmode ? mcxg::LF_ADJ : 0);
     if (verify) {
         /* the precision check runs the fast common-configuration instantiation */
         if (exact || !common || kp.replay || (flags & MCXG_KEEP)) {
@@ -1099,7 +1122,8 @@ int mcxg_get_field(mcxg_session* s, float* out, double scale) {
     if (rc) {
         return rc;
     }
-    field_merge_f32<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, scale, (float*)s->d_out);
+    field_merge_f32<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, (double)s->kp.fxunit, scale,
+                                                           (float*)s->d_out);
     s->out_valid = true;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
@@ -1120,7 +1144,8 @@ int mcxg_get_field_blocks(mcxg_session* s, float* out, const double* scales, uin
         return rc;
     }
     MCXG_TRY(cudaMemcpyAsync(s->d_scales, scales, sizeof(double) * nblocks, cudaMemcpyHostToDevice, s->st));
-    field_merge_blocks<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, n / nblocks, s->d_scales,
+    field_merge_blocks<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, (double)s->kp.fxunit, n / nblocks,
+                                                              s->d_scales,
                                                               (float*)s->d_out);
     s->out_valid = true;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
@@ -1142,7 +1167,8 @@ int mcxg_get_field_interleaved(mcxg_session* s, float* out, const double* scales
         return rc;
     }
     MCXG_TRY(cudaMemcpyAsync(s->d_scales, scales, sizeof(double) * nsrc, cudaMemcpyHostToDevice, s->st));
-    field_merge_interleaved<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, nsrc, s->d_scales,
+    field_merge_interleaved<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, (double)s->kp.fxunit, nsrc,
+                                                                   s->d_scales,
                                                                    (float*)s->d_out);
     s->out_valid = true;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
@@ -1226,32 +1252,60 @@ int mcxg_get_field_f64(mcxg_session* s, double* out) {
     if (rc) {
         return rc;
     }
-    field_merge_f64<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, (double*)s->d_out);
+    field_merge_f64<<<grid_for(s, total), 256, 0, s->st>>>(s->d_field, n, total, (double)s->kp.fxunit,
+                                                           (double*)s->d_out);
     s->out_valid = false;
     MCXG_TRY(cudaMemcpyAsync(out, s->d_out, sizeof(double) * total, cudaMemcpyDeviceToHost, s->st));
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
 }
 
-int mcxg_get_field_planes(mcxg_session* s, float* hi, float* lo, int32_t* count) {
+int mcxg_set_adjoint(mcxg_session* s, const float* dloss, uint32_t n) {
+    if (!s || !s->has_problem || !dloss || n != s->kp.fieldlen) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    int rc = ensure(&s->d_adjc, &s->adjc_cap, (size_t)n);
+    if (!rc) {
+        rc = ensure(&s->d_adjJ, &s->adjJ_cap, (size_t)s->kp.nthread * (s->kp.threadphoton + 1u));
+    }
+    if (rc) {
+        return rc;
+    }
+    MCXG_TRY(cudaMemcpyAsync(s->d_adjc, dloss, sizeof(float) * n, cudaMemcpyHostToDevice, s->st));
+    MCXG_TRY(cudaMemsetAsync(s->d_adjJ, 0, sizeof(float) * s->adjJ_cap, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    s->adj_ready = true;
+    return MCXG_OK;
+}
+
+int mcxg_get_adjoint_grad(mcxg_session* s, float* gmua, float* gmus) {
+    if (!s || !s->has_problem || !s->adj_ready) {
+        return MCXG_ERR_STATE;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    const size_t nvox = s->kp.nvox, F = s->kp.fieldlen;
+    if (gmua) {
+        MCXG_TRY(cudaMemcpyAsync(gmua, s->d_field, sizeof(float) * nvox, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (gmus) {
+        MCXG_TRY(cudaMemcpyAsync(gmus, s->d_field + F, sizeof(float) * nvox, cudaMemcpyDeviceToHost, s->st));
+    }
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
+int mcxg_get_field_planes(mcxg_session* s, int64_t* counts, float* rem) {
     if (!s || !s->has_problem) {
         return MCXG_ERR_STATE;
     }
     MCXG_TRY(cudaSetDevice(s->device));
-    /* component c's planes start at 3 c fieldlen: copy each plane of each component */
-    const size_t F = s->kp.fieldlen;
-    for (size_t c = 0; c < field_comps(s->kp); c++) {
-        const float* base = s->d_field + kFieldPlanes * c * F;
-        if (hi) {
-            MCXG_TRY(cudaMemcpyAsync(hi + c * F, base, sizeof(float) * F, cudaMemcpyDeviceToHost, s->st));
-        }
-        if (lo) {
-            MCXG_TRY(cudaMemcpyAsync(lo + c * F, base + F, sizeof(float) * F, cudaMemcpyDeviceToHost, s->st));
-        }
-        if (count) {
-            MCXG_TRY(cudaMemcpyAsync(count + c * F, base + 2 * F, sizeof(int32_t) * F, cudaMemcpyDeviceToHost,
-                                     s->st));
-        }
+    const size_t total = (size_t)s->kp.fieldlen * field_comps(s->kp);
+    if (counts) {
+        MCXG_TRY(cudaMemcpyAsync(counts, s->d_field, sizeof(int64_t) * total, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (rem) {
+        MCXG_TRY(cudaMemcpyAsync(rem, s->d_field + 2 * total, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
     }
     MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
@@ -1413,6 +1467,8 @@ int batch_enqueue(mcxg_session* s, int lflags) {
     a.media8 = s->d_bmedia;
     a.media32 = (const uint32_t*)s->d_bmedia;
     a.field = s->d_bfield;
+    a.fhi = (unsigned long long*)s->d_bfield;
+    a.flo = s->d_bfield + 2 * (size_t)s->totalfield;
     a.energy = s->d_benergy;
     a.detcount = s->d_words + 0;
     a.vtcounter = s->d_words + 1;

@@ -1116,6 +1116,30 @@ int mcx_rand_blocks(unsigned int seed, uint64_t skip, uint32_t nblock, uint32_t 
     return 0;
 }
 
+/* The field accumulator's fixed-point unit 2^-S (the transport kernel's
+   deposits split into int64 counts of 2^-S and float remainders): the
+   largest S, at most 40, for which no element can reach 2^61 counts.  An
+   element gathers at most every photon's whole path -- the time window at
+   the speed of light, in voxels -- times its weight (a replay: the largest
+   replay weight), with a factor 4 to spare. */
+static void field_scale(const Config* cfg, int replay, float* sc, float* unit) {
+    const double twin1 = (double)cfg->tstart + (double)cfg->tstep * cfg->maxgate;
+    double path = twin1 * 2.99792458e11 / (cfg->unitinmm > 0.f ? cfg->unitinmm : 1.f);
+    path = path > 1.0 ? path : 1.0;
+    double wmax = 1.0;
+    if (replay && cfg->replay.weight) {
+        for (size_t i = 0; i < cfg->nphoton; i++) {
+            const double w = fabs((double)cfg->replay.weight[i]);
+            wmax = w > wmax ? w : wmax;
+        }
+    }
+    const double bound = 4.0 * (double)(cfg->nphoton ? cfg->nphoton : 1) * path * wmax;
+    int S = (int)floor(61.0 - log2(bound));
+    S = S < 0 ? 0 : (S > 40 ? 40 : S);
+    *sc = ldexpf(1.f, S);
+    *unit = ldexpf(1.f, -S);
+}
+
 static void make_kparams(const Config* cfg, size_t nvox, size_t fieldlen, size_t autothread, unsigned int hostdetreclen,
                          unsigned int partialdata, unsigned int is2d, int replay, mcxg_kparams* kp) {
     memset(kp, 0, sizeof(*kp));
@@ -1132,6 +1156,7 @@ static void make_kparams(const Config* cfg, size_t nvox, size_t fieldlen, size_t
     kp->fieldlen = (uint32_t)fieldlen;
     kp->twin0 = cfg->tstart;
     kp->twin1 = cfg->tstart + cfg->tstep * cfg->maxgate;
+    field_scale(cfg, replay, &kp->fxscale, &kp->fxunit);
     float minstep = fminf(fminf(cfg->steps.x, cfg->steps.y), cfg->steps.z);
     kp->oneoverc0 = R_C0 * cfg->unitinmm;
     kp->Rtstep = 1.f / cfg->tstep;

@@ -19,12 +19,10 @@
  *    staged in shared memory (label lookups diverge across a warp), the label
  *    volume as one byte per voxel (label | detector bit << 7) read through
  *    the read-only path.
- *  - Fluence accumulated in two float planes with an error-free transform:
- *    the high plane takes the deposit with an atomic that returns the old
- *    value, the exact rounding error of that sum goes to the low plane, and
- *    the high plane is held within +-1024 by spills into an integer count.
- *    Deposits to the same voxel and gate by several lanes of a warp are
- *    merged first (match, shuffle-sum, one leader atomic).
+ *  - Fluence accumulated exactly: each deposit splits into a 64-bit
+ *    fixed-point part (integer atomics, exact in any order) and a tiny float
+ *    remainder.  Deposits to the same voxel and gate by several lanes of a
+ *    warp can be merged first (match, shuffle-sum, one leader commit).
  *  - Detected-photon partial data in shared memory, strided per thread.
  *
  * Template flags: EXACT (IEEE-only math, no contraction: compile this TU with
@@ -33,7 +31,8 @@
  * compiled in), WAGG (warp aggregation of deposits), COUNT (event counters),
  * MINB (resident 256-thread blocks per SM the register allocation targets),
  * ACC64 (every deposit also accumulated in FP64, plain float and the
- * reference's spill form, to state the accumulation error).
+ * reference's spill form, to state the accumulation error), ADJ (the two
+ * passes of the fluence gradient instead of the deposits).
  * DET and REFL are upper bounds: the runtime flags in the constant block
  * still decide, so the exact build runs every configuration.
  */
@@ -96,7 +95,7 @@ __constant__ mcxg_kparams c_p;
 #ifdef MCXG_BATCH_TU
 /* the batch translation unit spends its constant bank on the descriptors of
    the simulations of one wave; batches have no detectors or extra sources */
-#define MCXG_BATCH_WAVE 140
+#define MCXG_BATCH_WAVE 136
 __constant__ float4 c_det[1];
 __constant__ float4 c_srcx[4];
 __constant__ mcxg_simdesc c_sims[MCXG_BATCH_WAVE];
@@ -833,88 +832,70 @@ __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Pho
 
 /* ---------------------------------------------------------------- deposit */
 
-/* Compensated accumulation in three planes per field component: a float
-   high plane, a float low plane, and an int32 spill count.  The high plane
-   takes each deposit with an atomic that returns the old value; the exact
-   rounding error of that add (TwoSum) goes to the low plane.  The high plane
-   is kept within +-K_SPILL by moving K_SPILL into the spill count whenever
-   an add carries it past that bound (that add's rounding error again to the
-   low plane): a high plane that grew without bound would make every later
-   deposit smaller than half its ulp, so all of it would pile up in the low
-   plane, which then saturates the same way (tens of percent lost in the
-   hottest voxels of a 1e9-photon run).  The value is
-   hi + lo + K_SPILL x count, summed in FP64: the bulk exact in the count,
-   the rest to ~2^-48 of the element.  Planes: hi at [i], lo at [lo + i],
-   count at [2 lo + i] (as int32), lo = the component's plane length. */
-#define K_SPILL 1024.f
-
-__device__ __forceinline__ float twosum_err(float old, float w, float s) {
-    const float bp = __fsub_rn(s, old);
-    return __fadd_rn(__fsub_rn(old, __fsub_rn(s, bp)), __fsub_rn(w, bp));
-}
-
-/* the add that produced s (s = old + w, |s| > K_SPILL) moves K_SPILL out */
-__device__ __noinline__ void field_spill(float* field, unsigned int lo, unsigned int i, float s) {
-    const float t = s > 0.f ? -K_SPILL : K_SPILL;
-    const float old = atomicAdd(field + i, t);
-    const float e = twosum_err(old, t, __fadd_rn(old, t));
-    if (e != 0.f) {
-        atomicAdd(field + lo + i, e);
-    }
-    atomicAdd((int*)field + 2 * (size_t)lo + i, s > 0.f ? 1 : -1);
-}
-
-__device__ __forceinline__ void field_add2(float* field, unsigned int lo, unsigned int i, float w) {
-    const float old = atomicAdd(field + i, w);
-    const float s = __fadd_rn(old, w);
-    const float e = twosum_err(old, w, s);
-    if (e != 0.f) {
-        atomicAdd(field + lo + i, e);
-    }
-    if (fabsf(s) > K_SPILL) {
-        field_spill(field, lo, i, s);
-    }
-}
-
-/* A high-plane atomic whose rounding error is still to be sent to the low
-   plane.  The old value returns from L2 while the photon takes its next step;
-   completing the add one deposit later keeps the warp from waiting on it. */
-struct Pending {
-    unsigned int idx;
-    float old, w;
-    bool on;
+/* Compensated accumulation: each field component is a plane of signed
+   64-bit fixed-point counts of 2^-S and a plane of float remainders.  A
+   deposit w is split exactly into k = round(w 2^S) and r = w - k 2^-S
+   (|r| <= 2^-(S+1)); k goes to the integer plane, r to the float plane, both
+   with fire-and-forget atomics.  Integer adds are exact in any order -- also
+   when the memory system merges the adds of several lanes to one address --
+   so the bulk of an element carries no rounding at all, and the remainders
+   are too small for the float plane's rounding to matter: an element is
+   count x 2^-S + remainder, summed in FP64.  The host picks S per problem so
+   that no element can reach 2^62 units (mcx_host.c, field_scale).  A float
+   running sum, or float high and low planes compensated by the value an
+   atomic returns (TwoSum), loses the low-order deposits of the hottest
+   voxels at 1e8-1e9 photons. */
+struct Field {
+    unsigned long long* hi;        /* fixed-point counts */
+    float* lo;                     /* remainders */
+    float sc, unit;                /* 2^S, 2^-S */
 };
 
-__device__ __forceinline__ void pend_complete(float* field, unsigned int lo, Pending& pd) {
-    if (pd.on) {
-        const float s = __fadd_rn(pd.old, pd.w);
-        const float e = twosum_err(pd.old, pd.w, s);
-        if (e != 0.f) {
-            atomicAdd(field + lo + pd.idx, e);
-        }
-        if (fabsf(s) > K_SPILL) {
-            field_spill(field, lo, pd.idx, s);
-        }
-        pd.on = false;
+/* component comp of the field (0 real, 1 imaginary); the planes of the
+   components follow one another, plane length ps.lo_plane() */
+template <class PS>
+__device__ __forceinline__ Field field_of(const KArgs& a, const PS& ps, unsigned int comp) {
+    const mcxg_kparams& c_p = ps.p();
+    const size_t F = ps.lo_plane();
+    Field f;
+    f.hi = a.fhi + comp * F;
+    f.lo = a.flo + comp * F;
+    f.sc = c_p.fxscale;
+    f.unit = c_p.fxunit;
+    return f;
+}
+
+/* w = k 2^-S + r exactly: k is w 2^S rounded to an integer (a float integer,
+   so exact in float), r the part below the grid */
+__device__ __forceinline__ void field_split(const Field& f, float w, long long& k, float& r) {
+    k = __float2ll_rn(__fmul_rn(w, f.sc));
+    r = __fsub_rn(w, __fmul_rn((float)k, f.unit));
+}
+
+__device__ __forceinline__ void field_commit(const Field& f, size_t i, long long k, float r) {
+    if (k) {
+        atomicAdd(f.hi + i, (unsigned long long)k);
+    }
+    if (r != 0.f) {
+        atomicAdd(f.lo + i, r);
     }
 }
 
-__device__ __forceinline__ void pend_issue(float* field, Pending& pd, unsigned int i, float w) {
-    pd.old = atomicAdd(field + i, w);
-    pd.idx = i;
-    pd.w = w;
-    pd.on = true;
+__device__ __forceinline__ void field_add(const Field& f, size_t i, float w) {
+    long long k;
+    float r;
+    field_split(f, w, k, r);
+    field_commit(f, i, k, r);
 }
 
-/* Deposit from every lane that has one; lanes of the warp hitting the same
-   field element are summed first and one leader commits. */
+/* Deposit from every lane that has one; with WAGG, lanes of the warp hitting
+   the same field element add their integer parts (exactly) and their
+   remainders first and one leader commits. */
 template <bool WAGG>
-__device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, bool doit, unsigned int key, float w,
-                                        Pending& pd) {
+__device__ __forceinline__ void deposit(const Field& f, bool doit, unsigned int key, float w) {
     if (!WAGG) {
         if (doit) {
-            pend_complete(field, fieldlen, pd);
-            pend_issue(field, pd, key, w);
+            field_add(f, key, w);
         }
         return;
     }
@@ -923,23 +904,26 @@ __device__ __forceinline__ void deposit(float* field, unsigned int fieldlen, boo
     if (!doit) {
         return;
     }
+    long long k;
+    float r;
+    field_split(f, w, k, r);
     unsigned int peers = __match_any_sync(m, key);
     unsigned int lane = threadIdx.x & 31u;
     if (peers == (1u << lane)) {
-        pend_complete(field, fieldlen, pd);
-        pend_issue(field, pd, key, w);
+        field_commit(f, key, k, r);
         return;
     }
-    float total = 0.f;
+    long long ksum = 0;
+    float rsum = 0.f;
     unsigned int rest = peers;
     while (rest) {
         int src = __ffs(rest) - 1;
         rest &= rest - 1;
-        total += __shfl_sync(peers, w, src);
+        ksum += __shfl_sync(peers, k, src);
+        rsum += __shfl_sync(peers, r, src);
     }
     if ((int)lane == __ffs(peers) - 1) {
-        pend_complete(field, fieldlen, pd);
-        pend_issue(field, pd, key, total);
+        field_commit(f, key, ksum, rsum);
     }
 }
 
@@ -957,9 +941,9 @@ __device__ __forceinline__ void rf_replay_deposit(const KArgs& a, const PS& ps, 
     if (key >= c_p.fieldlen) {
         key -= c_p.fieldlen;
     }
-    field_add2(a.field, ps.lo_plane(), key, wre);
+    field_add(field_of(a, ps, 0), key, wre);
     if (c_p.omega > 0.f) {
-        field_add2(a.field + 3 * (size_t)c_p.fieldlen, c_p.fieldlen, key, wim);
+        field_add(field_of(a, ps, 1), key, wim);
     }
 }
 
@@ -978,7 +962,7 @@ __device__ __forceinline__ void share_deposit(const KArgs& a, const PS& ps, unsi
             if (k >= c_p.fieldlen) {
                 k -= c_p.fieldlen;
             }
-            field_add2(a.field, ps.lo_plane(), k, w * pw);
+            field_add(field_of(a, ps, 0), k, w * pw);
         }
     }
 }
@@ -1032,9 +1016,9 @@ __device__ void replay_site_deposit(const KArgs& a, const PS& ps, const Shared& 
         atomicAdd(a.status + ST_GUARD, 1u);
         return;
     }
-    field_add2(a.field, ps.lo_plane(), ps.field_off() + (unsigned int)key, tmp0);
+    field_add(field_of(a, ps, 0), ps.field_off() + (unsigned int)key, tmp0);
     if (c_p.outputtype == otRFmus) {
-        field_add2(a.field + 3 * (size_t)c_p.fieldlen, c_p.fieldlen, (unsigned int)key, tim);
+        field_add(field_of(a, ps, 1), (unsigned int)key, tim);
     }
 }
 
@@ -1111,7 +1095,7 @@ __device__ int launchnewphoton(const KArgs& a, const PS& ps, const Shared& S, Ph
             if (KP_SHARING) {
                 share_deposit(a, ps, key, -s.p.w);
             } else {
-                field_add2(a.field, ps.lo_plane(), key, -s.p.w);
+                field_add(field_of(a, ps, 0), key, -s.p.w);
             }
         }
         if (DET && c_p.savedet && (isdet & K_DET_MASK) == K_DET_MASK &&
@@ -1642,8 +1626,33 @@ __device__ __forceinline__ void acc_verify(const KArgs& a, unsigned int fieldlen
     }
 }
 
+/* Fluence gradient.  For a loss L = sum_e c_e Phi_e of the raw field
+   (c_e = dL/dPhi_e, Phi_e = sum of the flux deposits D_k = w0_k (1 -
+   exp(-mua l_k)) / mua into element e), a photon's path does not depend on
+   mua, and the weight entering voxel visit k carries exp(-sum_{j<k} mua_j
+   l_j), so
+
+     dL/dmua_u = sum_{visits k in u} [ c_k dD_k/dmua  -  l_k (J - P_k) ]
+
+   with J = sum_k c_k D_k over the whole photon and P_k the same sum up to
+   and including visit k (dD/dmua = (w l - D) / mua, or -w0 l^2 / 2 when mua
+   is below EPS).  By the likelihood ratio of the free paths (density mus
+   exp(-mus l) per scattering), the later deposits of a scattering in u gain
+   1/mus_u and every path length in u costs -l:
+
+     dL/dmus_u = sum_{scatterings in u} (J - P_before) / mus_u
+                 - sum_{visits k in u} l_k (J - P_{k-1}).
+
+   J is known only when the photon ends, so the photons run twice with the
+   same random numbers: pass 1 stores each photon's J, pass 2 reads it at the
+   launch and accumulates the gradients. */
+__device__ __forceinline__ size_t adj_slot(const mcxg_kparams& c_p, unsigned int vt, float fw) {
+    return (size_t)vt * (c_p.threadphoton + 1u) + (unsigned int)((int)fw - 1);
+}
+
 template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false,
-          bool COMMON = false, bool RF = false, bool POL = false, bool SVMC = false, bool ACC64 = false>
+          bool COMMON = false, bool RF = false, bool POL = false, bool SVMC = false, bool ACC64 = false,
+          bool ADJ = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
     typedef typename std::conditional<BATCH, BatchPST<COMMON>, ConstPST<XMEDIA, COMMON>>::type PS;
@@ -1681,13 +1690,10 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     bool fresh = true;             /* vt just claimed: initial launch */
     unsigned int mediaidold = 0, idx1dold = 0;
     unsigned int nsteps = 0;       /* steps of the current photon, against K_STEP_CAP */
-    Pending pd;
-    pd.on = false;
-    pd.idx = 0;
-    pd.old = pd.w = 0.f;
     float3 rv = make_float3(0.f, 0.f, 0.f);   /* fast kernel: rcp of the direction */
     bool vdirty = true;
     bool testint = false, hitintf = false;    /* split voxels: test the plane this step / the step ended on it */
+    float adjJ = 0.f, adjP = 0.f;             /* fluence gradient: the photon's loss total and its running part */
 
     while (claimed) {
         const mcxg_kparams& c_p = ps.p();
@@ -1697,6 +1703,9 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             if (fresh) {
                 vt_begin(a, ps, S, s, vt);
                 testint = false;     /* each reference thread starts untested (2342) */
+            }
+            if (ADJ && !fresh && a.adjmode == 1u) {
+                a.adjJ[adj_slot(c_p, vt, s.f.w)] = adjJ;        /* the photon that just ended */
             }
             /* one call site for the first and every later launch keeps the hot loop small */
             if (fresh && (unsigned long long)vt >= (unsigned long long)c_p.threadphoton * c_p.nthread + (unsigned int)c_p.oddphoton) {
@@ -1720,6 +1729,10 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             }
             if (COUNT) {
                 cnt_launch++;
+            }
+            if (ADJ) {
+                adjP = 0.f;
+                adjJ = (a.adjmode == 2u) ? a.adjJ[adj_slot(c_p, vt, s.f.w)] : 0.f;
             }
             nsteps = 0;
             vdirty = true;
@@ -1820,6 +1833,10 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                 }
                 s.v.w += 1.f;
                 vdirty = true;
+                if (ADJ && a.adjmode == 2u && s.idx1d < c_p.nvox) {
+                    /* a scattering in this voxel: 1/mus on every later deposit */
+                    atomicAdd(a.field + c_p.fieldlen + s.idx1d, (adjJ - adjP) * __fdividef(1.f, s.prop.y));
+                }
                 if (KP_POL) {
                     update_stokes<EXACT>(a, s, theta, polphi, olddir, s.v);
                 }
@@ -1993,6 +2010,25 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                         key -= c_p.fieldlen;
                     }
                 }
+                if (ADJ) {
+                    /* the visit that just ended, in voxel idx1dold */
+                    const float c = dep ? __ldg(a.adjc + key) : 0.f;
+                    const float cD = c * weight;
+                    if (a.adjmode == 1u) {
+                        adjJ += cD;
+                    } else {
+                        const float l = s.pathlen, rest = adjJ - adjP;
+                        float own = 0.f;
+                        if (dep) {
+                            own = (s.prop.x < K_EPS) ? -0.5f * c * s.w0 * l * l
+                                                     : c * (s.p.w * l - weight) * __fdividef(1.f, s.prop.x);
+                        }
+                        atomicAdd(a.field + idx1dold, own - l * (rest - cD));
+                        atomicAdd(a.field + c_p.fieldlen + idx1dold, -l * rest);
+                        adjP += cD;
+                    }
+                    dep = false;
+                }
                 s.w0 = s.p.w;
                 if (KP_RFFWD) {
                     s.w0re = s.wre;
@@ -2007,14 +2043,14 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     share_deposit(a, ps, key, weight);
                 }
             } else {
-                deposit<WAGG>(a.field, ps.lo_plane(), dep, ps.field_off() + key, weight, pd);
+                deposit<WAGG>(field_of(a, ps, 0), dep, ps.field_off() + key, weight);
                 if (ACC64 && dep) {
                     acc_verify(a, c_p.fieldlen, key, weight);
                 }
             }
             if (RF && depim) {
                 /* the imaginary component's planes follow the real one's: [3F, 6F) */
-                field_add2(a.field + 3 * (size_t)c_p.fieldlen, c_p.fieldlen, key, weight_im);
+                field_add(field_of(a, ps, 1), key, weight_im);
             }
         }
         if (KP_SVMC) {
@@ -2189,7 +2225,6 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         }
     }
 
-    pend_complete(a.field, ps.lo_plane(), pd);
     if (COUNT) {
         atomicAdd(a.counters + 0, cnt_step);
         atomicAdd(a.counters + 1, cnt_scat);
@@ -2211,7 +2246,7 @@ __global__ void mcx_rng_dump(const KArgs a) {
         t.a = (unsigned long long)sd.x << 32 | sd.y;
         t.b = (unsigned long long)sd.z << 32 | sd.w;
         for (unsigned int j = vt; j < c_p.fieldlen; j += c_p.nthread) {
-            a.field[j] = rnd(t);
+            a.flo[j] = rnd(t);
         }
     }
 }

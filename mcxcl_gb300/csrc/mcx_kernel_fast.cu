@@ -73,8 +73,19 @@ static void* kacc64() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, true, false, false, false, true>;
 }
 
+/* the fluence-gradient passes: general media handling (labels or float mua),
+   no detectors, 3 blocks/SM */
+template <bool REFL>
+static void* kadj() {
+    return (void*)mcx_transport<false, false, REFL, false, false, 3, false, false, false, false, false, false, false,
+                                true>;
+}
+
 static void* select(int flags) {
     const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    if (flags & LF_ADJ) {
+        return refl ? kadj<true>() : kadj<false>();
+    }
     if (flags & LF_ACC64) {
         return det ? (refl ? kacc64<true, true>() : kacc64<true, false>())
                    : (refl ? kacc64<false, true>() : kacc64<false, false>());

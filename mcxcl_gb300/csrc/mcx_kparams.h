@@ -69,6 +69,7 @@ typedef struct mcxg_kparams {
     uint32_t dimy, dimz;           /* voxel counts along y and z */
     uint32_t srcnum;               /* patterns sharing each photon (pattern sources), else 1 */
     float omega;                   /* modulation angular frequency (rad/s); > 0 without replay: RF transport */
+    float fxscale, fxunit;         /* field accumulator: 2^S and 2^-S (the fixed-point plane counts units of 2^-S) */
 } mcxg_kparams;
 
 /* One simulation of a batch: its parameter block (nthread = its reference

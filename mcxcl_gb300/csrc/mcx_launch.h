@@ -21,7 +21,11 @@ struct KArgs {
     const float* angleinvcdf;
     const float* srcpattern;
     const uint4* seeds;            /* 4 x 32-bit seed words per reference thread */
-    float* field;                  /* [fieldlen] high plane, then [fieldlen] low plane */
+    float* field;                  /* the field buffer: fixed-point planes (comps x fieldlen int64), then
+                                      remainder planes (comps x fieldlen float); raw float scratch for
+                                      the fluence-gradient passes */
+    unsigned long long* fhi;       /* fixed-point counts of component c at fhi + c x plane length */
+    float* flo;                    /* float remainders of component c at flo + c x plane length */
     float2* energy;                /* per reference thread: escaped, launched weight */
     float* detp;                   /* maxdetphoton x reclen */
     unsigned long long* detseed;   /* maxdetphoton x 2 */
@@ -57,11 +61,18 @@ struct KArgs {
     double* acc64;
     float* accf;
     float* accs;
+    /* fluence gradient (instantiations with ADJ only): dLoss/d(raw field) per
+       field element, the per-photon loss totals J (nthread x (threadphoton +
+       1)), and the pass: 1 computes J, 2 accumulates d/dmua into field plane
+       0 and d/dmus into plane 1 (nvox each, voxel units) */
+    const float* adjc;
+    float* adjJ;
+    unsigned int adjmode;
 };
 
 /* flag bits for the launch entries */
 enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128, LF_POL = 256, LF_SVMC = 512,
-       LF_ACC64 = 1024 };
+       LF_ACC64 = 1024, LF_ADJ = 2048 };
 
 /* fast instantiation: hardware transcendental approximations */
 cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,
@@ -78,7 +89,7 @@ cudaError_t exact_rngdump(const KArgs& a, int grid, int block, cudaStream_t st);
 
 /* batch instantiations: simulation descriptors of one wave into constant
    memory (from device memory), then the launch */
-constexpr int kBatchWave = 140;
+constexpr int kBatchWave = 136;
 cudaError_t batch_wave_upload(const mcxg_simdesc* d_descs, unsigned int n, cudaStream_t st);
 cudaError_t batch_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st);
 cudaError_t batch_occupancy(int flags, int block, size_t smem, int* blocks_per_sm);

@@ -213,6 +213,97 @@ class LabelReadings:
         return np.array([-self.unitinmm * F[vol == k + 1].sum() for k in range(self.nmed)])
 
 
+class FluenceGradient:
+    """Gradient of a loss of the fluence (flux) field with respect to every
+    voxel's mua and mus, on the GPU.  A photon's path does not depend on
+    mua, so the transport kernel's fluence-gradient passes (MCXG_ADJ1 /
+    MCXG_ADJ2) rerun the forward photons with the same random numbers: the
+    first stores each photon's loss total, the second accumulates, per voxel
+    visit, the visit's own deposit derivative minus its path length times
+    the loss of the photon's later deposits, and per scattering the
+    likelihood-ratio term of mus.  Memory: one float per photon.  Label
+    volumes give per-label gradients by summing over each label's voxels.
+
+    cfg: a ``run()`` dictionary with ``vol`` (labels, or float mua as
+    [1, Nx, Ny, Nz]) and ``prop``; outputtype flux or fluence; no Russian
+    roulette (its survival draws depend on the weight)."""
+
+    def __init__(self, cfg):
+        import ctypes
+        from . import _lib
+        self._ct = ctypes
+        self._lib = _lib
+        self.L = _lib.load()
+        self.cfg = dict(cfg)
+        self.C = None
+        self.s = None
+        self.scale = None
+
+    def close(self):
+        if self.C is not None:
+            self.L.mcx_clearcfg(self._ct.byref(self.C))
+            self.C = None
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc:
+            raise RuntimeError("%s: %s" % (what, self.L.mcxg_error_string(rc).decode()))
+
+    def forward(self, **override):
+        """Runs the forward problem (cfg updated by ``override``, e.g. a new
+        ``vol`` or ``prop``); returns the normalised field [Nx, Ny, Nz, gates]
+        in FP64 (the compensated accumulator merged without rounding to
+        float)."""
+        ct = self._ct
+        self.close()
+        C = self._lib.Config()
+        pmcxcl.parse_config(dict(self.cfg, **override), C)
+        self.L.mcx_validatecfg(ct.byref(C), None, None, 0)
+        pmcxcl._check(C)
+        s = self.L.mcx_prepare_simulation(ct.byref(C))
+        pmcxcl._check(C)
+        self.C, self.s = C, s
+        ms = ct.c_float()
+        self._check(self.L.mcxg_simulate(s, 2, ct.byref(ms)), "forward")
+        self.forward_ms = ms.value
+        esc, tot = ct.c_double(), ct.c_double()
+        self._check(self.L.mcxg_get_energy(s, ct.byref(esc), ct.byref(tot)), "energies")
+        vvox = float(C.steps.x * C.steps.y * C.steps.z)
+        self.scale = float(C.unitinmm) / (tot.value * vvox * float(C.tstep))
+        if ord(C.outputtype) == 1:             # fluence: flux times the gate width
+            self.scale *= float(C.tstep)
+        self.shape = (C.dim.x, C.dim.y, C.dim.z, int(C.maxgate))
+        n = int(C.dim.x) * C.dim.y * C.dim.z * int(C.maxgate)
+        out = np.zeros(n, np.float64)
+        self._check(self.L.mcxg_get_field_f64(s, out.ctypes.data), "field")
+        return out.reshape(self.shape, order="F") * self.scale
+
+    def backward(self, dloss):
+        """dloss: dLoss/dfield [Nx, Ny, Nz, gates] of the last forward.
+        Returns (dLoss/dmua, dLoss/dmus), each [Nx, Ny, Nz], per mm."""
+        ct = self._ct
+        if self.s is None:
+            raise RuntimeError("backward() needs a forward() first")
+        c = (np.asarray(dloss, np.float64) * self.scale).astype(np.float32).ravel(order="F")
+        self._check(self.L.mcxg_set_adjoint(self.s, c.ctypes.data, c.size), "loss gradient")
+        ms1, ms2 = ct.c_float(), ct.c_float()
+        self._check(self.L.mcxg_simulate(self.s, 256, ct.byref(ms1)), "gradient pass 1")
+        self._check(self.L.mcxg_simulate(self.s, 512, ct.byref(ms2)), "gradient pass 2")
+        self.backward_ms = ms1.value + ms2.value
+        nvox = self.shape[0] * self.shape[1] * self.shape[2]
+        ga, gs = np.zeros(nvox, np.float32), np.zeros(nvox, np.float32)
+        self._check(self.L.mcxg_get_adjoint_grad(self.s, ga.ctypes.data, gs.ctypes.data), "gradients")
+        u = float(self.C.unitinmm)
+        f = self.shape[:3]
+        return (ga.astype(np.float64).reshape(f, order="F") * u, gs.astype(np.float64).reshape(f, order="F") * u)
+
+
 def readings(sim, mua, mus=None):
     """Detector readings as a differentiable torch function of mua (and of
     the scalar mus of label 1 when given as a tensor)."""

@@ -224,3 +224,83 @@ def test_label_gradients_on_gpu():
     ((torch.log(Rtt) - torch.log(torch.tensor(Rt))) ** 2).sum().backward()
     np.testing.assert_allclose(a.grad.numpy(), ga.astype(np.float32), rtol=1e-5)
     np.testing.assert_allclose(s.grad.numpy(), gs.astype(np.float32), rtol=1e-5)
+
+
+# ------------------------------------------------------- fluence gradients
+
+def _fluence_cfg(n=30, nphoton=2000000):
+    cfg, mua, target = workloads.diff_config(n=n, nphoton=nphoton)
+    cfg.pop("detpos")
+    cfg.update(issavedet=0, isreflect=0, outputtype="flux")
+    return cfg, mua, target
+
+
+@pytest.mark.gpu
+def test_fluence_gradient_per_voxel_mua_matches_central_differences():
+    """dLoss/dmua per voxel for L = sum (Phi - Phi_target)^2 over the fluence
+    field of a 30^3 float-mua volume: the two gradient passes against central
+    differences with common random numbers (relative step 1e-3) on the 16
+    voxels of largest gradient and 16 drawn at random among the rest of the
+    support: within 2 % in norm.  Also reports the backward/forward time."""
+    cfg, mua, target = _fluence_cfg()
+    sim = diff.FluenceGradient(cfg)
+    Ft = sim.forward(vol=target[None])
+    F = sim.forward(vol=mua[None])
+    ga, gs = sim.backward(2 * (F - Ft))
+    ratio = sim.backward_ms / sim.forward_ms
+    support = np.flatnonzero(np.abs(ga).ravel() > 1e-3 * np.abs(ga).max())
+    rng = np.random.default_rng(5)
+    top = np.argsort(-np.abs(ga).ravel())[:16]
+    picks = np.concatenate([top, rng.choice(np.setdiff1d(support, top), size=16, replace=False)])
+
+    def loss(m):
+        return float(np.sum((sim.forward(vol=m[None]) - Ft) ** 2))
+    bw, fd = [], []
+    for f in picks:
+        v = np.unravel_index(f, mua.shape)
+        h = np.float32(1e-3) * mua[v]
+        mp, mm = mua.copy(), mua.copy()
+        mp[v] += h
+        mm[v] -= h
+        fd.append((loss(mp) - loss(mm)) / float(mp[v] - mm[v]))
+        bw.append(ga[v])
+    bw, fd = np.array(bw), np.array(fd)
+    print("fluence gradient: backward/forward time %.2f, rel err %.4f" % (ratio, np.linalg.norm(bw - fd) / np.linalg.norm(fd)))
+    assert np.linalg.norm(bw - fd) <= 0.02 * np.linalg.norm(fd), np.c_[bw, fd]
+    assert np.all(np.isfinite(gs))
+    sim.close()
+
+
+@pytest.mark.gpu
+def test_fluence_gradient_per_label_matches_central_differences():
+    """A label volume (cube with a sphere): per-label dLoss/dmua (the
+    per-voxel gradient summed over each label) against central differences
+    with common random numbers (2 %), per-label dLoss/dmus against central
+    differences over +-5 % (mus moves the paths: 10 %)."""
+    from mcxcl_gb300 import workloads as W
+    cfg = dict(W.builtin("cubesph60b"), nphoton=2000000, seed=91, outputtype="flux", issavedet=0, isreflect=0,
+               tstep=1e-9)
+    cfg.pop("detpos")
+    vol = cfg["vol"]
+    prop0 = np.array(cfg["prop"], np.float32)
+    target = prop0.copy()
+    target[1:, 0] *= 1.2
+    target[1:, 1] *= 0.9
+    sim = diff.FluenceGradient(cfg)
+    Ft = sim.forward(prop=target)
+    F = sim.forward(prop=prop0)
+    ga, gs = sim.backward(2 * (F - Ft))
+    la = np.array([ga[vol == k].sum() for k in (1, 2)])
+    ls = np.array([gs[vol == k].sum() for k in (1, 2)])
+
+    def loss(p):
+        return float(np.sum((sim.forward(prop=p) - Ft) ** 2))
+    for k in (1, 2):
+        for col, g, rel, tol in ((0, la, 1e-3, 0.02), (1, ls, 0.05, 0.1)):
+            pp, pm = prop0.copy(), prop0.copy()
+            h = np.float32(rel) * prop0[k, col]
+            pp[k, col] += h
+            pm[k, col] -= h
+            fd = (loss(pp) - loss(pm)) / float(pp[k, col] - pm[k, col])
+            assert abs(g[k - 1] - fd) <= tol * abs(fd), ("mua" if col == 0 else "mus", k, g[k - 1], fd)
+    sim.close()
