@@ -234,11 +234,39 @@ def batch_measure(nsim):
     for c in sims:
         ks += mcxcl_gb300.run(c)["stat"]["kernelms"]
     ts = time.perf_counter() - t0
+    # precision: the batched launch with every deposit also accumulated in FP64
+    sub = sims[:64]
+    ver = mcxcl_gb300.run_batch(sub, verify=True)
+    prec = {"simulations": len(sub),
+            "relerr_max": max(r["stat"]["relerr_max"] for r in ver),
+            "relerr_median_max": max(r["stat"]["relerr_median"] for r in ver),
+            "relerr_total_max": max(r["stat"]["relerr_total"] for r in ver)}
+    # error of each arm: two independent runs (seed, seed + 1) of 8 of the
+    # simulations; per-voxel RSE = |a - b| / sqrt(2) / mean over voxels holding
+    # at least 1% of the simulation's peak fluence
+    rse = {"batched": [], "one_launch_per_sim": []}
+    pick = [sims[i] for i in range(0, nsim, max(1, nsim // 8))][:8]
+    alt = [dict(c, seed=int(c["seed"]) + 1) for c in pick]
+    pairs = {"batched": zip(mcxcl_gb300.run_batch(pick), mcxcl_gb300.run_batch(alt)),
+             "one_launch_per_sim": [(mcxcl_gb300.run(c), mcxcl_gb300.run(d)) for c, d in zip(pick, alt)]}
+    for arm, pr in pairs.items():
+        for ra, rb in pr:
+            fa, fb = ra["flux"].astype(np.float64), rb["flux"].astype(np.float64)
+            m = 0.5 * (fa + fb)
+            sel = m > 0.01 * m.max()
+            rse[arm].append(np.abs(fa - fb)[sel] / np.sqrt(2.0) / m[sel])
+    err = {}
+    for arm, lst in rse.items():
+        v = np.concatenate(lst)
+        # |a - b| / sqrt 2 is |N(0, sigma^2)|, whose median is 0.6745 sigma
+        err[arm] = {"rse": float(np.median(v) / 0.6745), "voxels": int(v.size),
+                    "estimator": "median over voxels >= 1% of peak of |a-b|/sqrt(2)/mean, / 0.6745"}
     return {"simulations": nsim, "photons": photons, "batched_sims_per_s": nsim / tb,
             "one_launch_per_sim_sims_per_s": nsim / ts, "ratio": ts / tb,
             "batched_wall_s": tb, "batched_kernel_ms": kb, "one_launch_per_sim_wall_s": ts,
             "one_launch_per_sim_kernel_ms": ks,
-            "equal_error": "same photons per simulation in both arms"}
+            "equal_error": "same photons per simulation in both arms; measured RSE below",
+            "rse": err, "precision_vs_fp64": prec}
 
 
 def gradient_measure():

@@ -305,6 +305,12 @@ struct mcxg_session* mcx_prepare_simulation(Config* cfg);
    of at most 128 labels, one respin, no detectors, replay, extra sources,
    patterns or phase tables. */
 void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsigned int flags);
+/* mcx_run_batch with every deposit also accumulated in FP64 (no
+   counterpart in the reference): the same outputs, and in relerr (3 x n
+   doubles) each simulation's max and median relative error of the
+   compensated field over its non-zero elements, and the relative error of
+   its total, against that FP64 accumulation of the same photons. */
+void mcx_run_batch_verify(Config** cfgs, int n, unsigned int photons_per_thread, double* relerr);
 /* sizeof(Config) and the byte offset of a named field ((size_t)-1 if
    unknown), for checking foreign-function mirrors of the struct. */
 size_t mcx_config_sizeof(void);
@@ -380,9 +386,11 @@ int  mcxg_set_trajectory(mcxg_session* s, uint32_t maxrec);
 int  mcxg_get_trajectory(mcxg_session* s, float* out, uint32_t maxrec, uint32_t* count);
 int  mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock, uint32_t blocklen,
                          uint32_t nthread);
-/* Launch shape of the persistent grid (0 = automatic).  blocks_per_sm = 3
-   selects the instantiation whose registers are capped for three resident
-   256-thread blocks per SM (also the automatic choice); 2 the uncapped one. */
+/* Launch shape of the persistent grid: block threads (32..256, a multiple of
+   32) and resident blocks per SM (0 = automatic: 256 threads x 3).  Shapes of
+   more than 512 threads per SM run the instantiation whose registers are
+   capped for 768 resident threads (80 a thread), the others the uncapped
+   one; blocks per SM are lowered to what fits at once. */
 int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
 /* ---- batches: many simulations in one persistent launch (no counterpart in
    the reference, which launches once per simulation).  sims points to nsim
@@ -398,9 +406,15 @@ int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
 int  mcxg_batch_set(mcxg_session* s, const void* sims, size_t desc_size, uint32_t nsim, const uint8_t* media,
                     uint64_t nmedia);
 /* Runs every simulation of the batch; MCXG_GRAPH replays a captured graph,
-   MCXG_AGG aggregates deposits.  *kernel_ms covers the clear, transport and
-   per-simulation sums. */
+   MCXG_AGG aggregates deposits, MCXG_VERIFY also accumulates every deposit
+   in FP64 (read with mcxg_batch_get_verify).  *kernel_ms covers the clear,
+   transport and per-simulation sums. */
 int  mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms);
+/* The precision check of the last MCXG_VERIFY batch run (no counterpart in
+   the reference): the FP64 accumulation of the same deposits and the
+   compensated field merged in FP64, both unscaled, for every simulation at
+   its field offset (NULL skips one). */
+int  mcxg_batch_get_verify(mcxg_session* s, double* f64, double* comp);
 /* Per simulation: FP64 {escaped, launched} weight, 2 x nsim. */
 int  mcxg_batch_get_energy(mcxg_session* s, double* out);
 /* Every simulation's field, the compensated accumulator in FP64 x scales[i], at its field offset. */
@@ -411,11 +425,12 @@ int  mcxg_batch_get_field(mcxg_session* s, float* out, const double* scales);
 int  mcxg_set_replay(mcxg_session* s, const void* seeds16, const float* weight, const float* tof, const int* detid,
                      uint32_t n);
 /* Pick the launch shape of the fast kernel for the current problem: time
-   each candidate (256 threads x 2 or 3 resident blocks per SM, warp
-   aggregation of deposits on or off) on the first sample_photons photons
-   and keep the fastest for later mcxg_simulate calls (unless a shape was
-   set with mcxg_set_launch).  Outputs may be NULL.  The trial runs
-   overwrite the field and energies. */
+   each candidate (blocks of 256, 128 and 64 threads at 768 resident threads
+   per SM with capped registers, 256 and 128 at 512 with uncapped ones; then
+   the fastest with warp-aggregated deposits) on the first sample_photons
+   photons and keep the fastest for later mcxg_simulate calls (unless a
+   shape was set with mcxg_set_launch).  Outputs may be NULL.  The trial
+   runs overwrite the field and energies. */
 int  mcxg_autotune(mcxg_session* s, uint32_t sample_photons, int* block, int* blocks_per_sm, int* noagg);
 /* Run all photons once; kernel time (CUDA events) into *kernel_ms. */
 int  mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms);

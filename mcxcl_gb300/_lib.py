@@ -118,7 +118,8 @@ EXPORTS = [
     "mcxg_set_replay", "mcxg_get_field_blocks", "mcxg_get_field_interleaved", "mcxg_set_polarization", "mcx_mie", "mcxg_get_detweight", "mcx_run_batch", "mcxg_batch_set",
     "mcxg_batch_simulate", "mcxg_batch_get_energy", "mcxg_batch_get_field", "mcx_savedetphoton",
     "mcxg_adjoint", "mcxg_get_verify", "mcx_readconfig", "mcx_parsejson", "mcxg_adjoint_field",
-    "mcxg_get_field_planes", "mcxg_set_adjoint", "mcxg_get_adjoint_grad",
+    "mcxg_get_field_planes", "mcxg_set_adjoint", "mcxg_get_adjoint_grad", "mcxg_batch_get_verify",
+    "mcx_run_batch_verify",
 ]
 
 _lib = None

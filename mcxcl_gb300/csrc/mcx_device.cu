@@ -320,6 +320,17 @@ __global__ void batch_merge(const float* __restrict__ f, unsigned long long tota
     }
 }
 
+/* every simulation's compensated field merged in FP64, unscaled */
+__global__ void batch_merge_f64(const float* __restrict__ f, unsigned long long total,
+                                const mcxg_simdesc* __restrict__ sims, double* __restrict__ out) {
+    const mcxg_simdesc& d = sims[blockIdx.y];
+    const unsigned long long off = d.field_off;
+    const unsigned int n = d.kp.fieldlen;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        out[off + i] = (double)((const long long*)f)[off + i] * (double)d.kp.fxunit + (double)f[2 * total + off + i];
+    }
+}
+
 /* Adjoint post-kernels (the reference's mcx_adjoint_kernel and
    mcx_adjoint_dcoeff_kernel, mcx_core.cl:3320-3512) on the normalised float
    field: per voxel, the time-integrated fluence of each source times that of
@@ -941,9 +952,16 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     /* the instantiations that fix the common configuration's parameters */
     const bool common = !rf && !pol && !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2 &&
                         kp.srcnum <= 1 && !s->maxjump;
-    const int bpsm_sel = (xmedia || rf || pol || svmc) ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
+    /* launch shape: block threads x blocks per SM; shapes of more than 512
+       threads per SM take the instantiation whose registers are capped for
+       768 resident threads (80 a thread), the others the uncapped one; the
+       specialised instantiations exist only capped */
+    const int block = s->block_req ? s->block_req : 256;
+    const bool special = xmedia || rf || pol || svmc || verify || adjmode;
+    const int bpsm_sel = special ? 768 / block : (s->bpsm_req ? s->bpsm_req : 768 / block);
+    const bool occ3 = special || block * bpsm_sel > 512;
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
-                 (noagg ? 0 : mcxg::LF_WAGG) | (bpsm_sel == 3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
+                 (noagg ? 0 : mcxg::LF_WAGG) | (occ3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
                  (common ? mcxg::LF_COMMON : 0) | (rf ? mcxg::LF_RF : 0) | (pol ? mcxg::LF_POL : 0) |
                  (svmc ? mcxg::LF_SVMC : 0) | (verify ? mcxg::LF_ACC64 : 0) | (adjmode ? mcxg::LF_ADJ : 0);
     if (verify) {
@@ -969,12 +987,11 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
         a.accf = s->d_accf;
         a.accs = s->d_accs;
     }
-    int block = s->block_req ? s->block_req : 256;
     size_t smem = shared_bytes(kp, block);
     if (smem > s->info.sharedmem_per_block) {
         return MCXG_ERR_LIMIT;
     }
-    int bpsm = (s->bpsm_req && !xmedia && !rf && !pol && !svmc) ? s->bpsm_req : (exact ? 2 : bpsm_sel);
+    int bpsm = exact ? 2 : bpsm_sel;
     if (!exact) {
         /* never more blocks than fit at once: a persistent grid must be resident */
         int occ = 0;
@@ -1033,14 +1050,23 @@ int mcxg_autotune(mcxg_session* s, uint32_t sample_photons, int* block, int* blo
     }
     s->kp = samp;
     s->up_fast = false;
+    /* the block sizes 64, 128 and 256 at 768 resident threads per SM (80
+       registers) and at 512 (uncapped registers), direct deposits; then the
+       fastest with warp-aggregated deposits */
     struct Cand {
         int block, bpsm, noagg;
-    } cands[] = {{256, 3, 1}, {256, 3, 0}, {256, 2, 1}, {256, 2, 0}};
+    } cands[] = {{256, 3, 1}, {128, 6, 1}, {64, 12, 1}, {256, 2, 1}, {128, 4, 1}, {0, 0, 0}};
+    const int ncand = (int)(sizeof(cands) / sizeof(cands[0]));
     float best = 1e30f;
     Cand pick = cands[0];
     int keep_block = s->block_req, keep_bpsm = s->bpsm_req;
     int rc = MCXG_OK;
-    for (const Cand& c : cands) {
+    for (int ci = 0; ci < ncand && !rc; ci++) {
+        Cand c = cands[ci];
+        if (!c.block) {
+            c = pick;            /* the last candidate: the best shape, aggregated */
+            c.noagg = 0;
+        }
         s->block_req = c.block;
         s->bpsm_req = c.bpsm;
         float ms = 0.f, t = 1e30f;
@@ -1050,10 +1076,7 @@ int mcxg_autotune(mcxg_session* s, uint32_t sample_photons, int* block, int* blo
                 t = ms;
             }
         }
-        if (rc) {
-            break;
-        }
-        if (t < best) {
+        if (!rc && t < best) {
             best = t;
             pick = c;
         }
@@ -1260,6 +1283,35 @@ int mcxg_get_field_f64(mcxg_session* s, double* out) {
     return MCXG_OK;
 }
 
+int mcxg_batch_get_verify(mcxg_session* s, double* f64, double* comp) {
+    if (!s || !s->has_batch || !s->d_acc64 || s->acc64_cap < s->totalfield) {
+        return MCXG_ERR_STATE;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    const size_t n = s->totalfield;
+    if (f64) {
+        MCXG_TRY(cudaMemcpyAsync(f64, s->d_acc64, sizeof(double) * n, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (comp) {
+        /* each simulation's elements merged with its own unit, unscaled */
+        std::vector<double> ones(s->nsim, 1.0);
+        int rc = ensure(&s->d_scales, &s->scales_cap, s->nsim);
+        if (!rc) {
+            rc = ensure((double**)&s->d_out, &s->out_cap, n);
+        }
+        if (rc) {
+            return rc;
+        }
+        MCXG_TRY(cudaMemcpyAsync(s->d_scales, ones.data(), sizeof(double) * s->nsim, cudaMemcpyHostToDevice, s->st));
+        batch_merge_f64<<<dim3(64, s->nsim), 256, 0, s->st>>>(s->d_bfield, s->totalfield, s->d_sims,
+                                                              (double*)s->d_out);
+        s->out_valid = false;
+        MCXG_TRY(cudaMemcpyAsync(comp, s->d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, s->st));
+    }
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    return MCXG_OK;
+}
+
 int mcxg_set_adjoint(mcxg_session* s, const float* dloss, uint32_t n) {
     if (!s || !s->has_problem || !dloss || n != s->kp.fieldlen) {
         return MCXG_ERR_ARG;
@@ -1460,6 +1512,12 @@ int batch_reset_graph(mcxg_session* s) {
    sums */
 int batch_enqueue(mcxg_session* s, int lflags) {
     MCXG_TRY(cudaMemsetAsync(s->d_bfield, 0, sizeof(float) * kFieldPlanes * (size_t)s->totalfield, s->st));
+    if (lflags & mcxg::LF_ACC64) {
+        const size_t n = s->totalfield;
+        MCXG_TRY(cudaMemsetAsync(s->d_acc64, 0, sizeof(double) * n, s->st));
+        MCXG_TRY(cudaMemsetAsync(s->d_accf, 0, sizeof(float) * n, s->st));
+        MCXG_TRY(cudaMemsetAsync(s->d_accs, 0, sizeof(float) * 2 * n, s->st));
+    }
     MCXG_TRY(cudaMemsetAsync(s->d_benergy, 0, sizeof(float2) * (size_t)s->totalvt, s->st));
     MCXG_TRY(cudaMemsetAsync(s->d_words, 0, 8 * sizeof(unsigned int), s->st));
     KArgs a;
@@ -1475,6 +1533,11 @@ int batch_enqueue(mcxg_session* s, int lflags) {
     a.status = s->d_words + 2;
     a.counters = s->d_events;
     a.lo = (unsigned int)s->totalfield;
+    if (lflags & mcxg::LF_ACC64) {
+        a.acc64 = s->d_acc64;
+        a.accf = s->d_accf;
+        a.accs = s->d_accs;
+    }
     MCXG_TRY(cudaMemsetAsync(s->d_simctr, 0, sizeof(unsigned int) * s->nsim, s->st));
     for (uint32_t w0 = 0; w0 < s->nsim; w0 += mcxg::kBatchWave) {
         const uint32_t n = std::min<uint32_t>(mcxg::kBatchWave, s->nsim - w0);
@@ -1568,10 +1631,29 @@ int mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
         refl = refl || d.kp.dorefl_compiled;
         common = common && !d.kp.is2d && d.kp.mediaformat <= 4 && d.kp.nphase <= 2;
     }
-    const bool agg = (flags & MCXG_AGG) != 0;
-    const int bpsm_req = s->bpsm_req ? s->bpsm_req : 3;
+    const bool verify = (flags & MCXG_VERIFY) != 0;
+    if (verify) {
+        /* the precision check: every deposit also to FP64, plain float and
+           spill fields of the whole batch (not captured in a graph) */
+        if (flags & MCXG_GRAPH) {
+            return MCXG_ERR_ARG;
+        }
+        const size_t n = s->totalfield;
+        int rc = ensure(&s->d_acc64, &s->acc64_cap, n);
+        if (!rc) {
+            rc = ensure(&s->d_accf, &s->accf_cap, n);
+        }
+        if (!rc) {
+            rc = ensure(&s->d_accs, &s->accs_cap, 2 * n);
+        }
+        if (rc) {
+            return rc;
+        }
+    }
+    const bool agg = (flags & MCXG_AGG) != 0 && !verify;
+    const int bpsm_req = verify ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
     int lflags = (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) | (bpsm_req == 3 ? mcxg::LF_OCC3 : 0) |
-                 (common && !(flags & MCXG_GENERAL) ? mcxg::LF_COMMON : 0);
+                 (common && !(flags & MCXG_GENERAL) ? mcxg::LF_COMMON : 0) | (verify ? mcxg::LF_ACC64 : 0);
     int block = s->block_req ? s->block_req : 256;
     int occ = 0;
     MCXG_TRY(mcxg::batch_occupancy(lflags, block, (size_t)block * 32, &occ));

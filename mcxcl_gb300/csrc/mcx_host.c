@@ -1791,9 +1791,17 @@ static size_t batch_threads(size_t nphoton, unsigned int ppt) {
 /* Runs n validated configurations in one persistent launch (a GB300
    addition: the reference runs one simulation per call).  Outputs go to each
    Config as mcx_run_simulation's do; errors are reported on cfgs[0]. */
-void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsigned int flags) {
-    static __thread void* btmp[5];
-    for (int i = 0; i < 5; i++) {
+static int cmp_double(const void* x, const void* y) {
+    const double a = *(const double*)x, b = *(const double*)y;
+    return (a > b) - (a < b);
+}
+
+/* relerr (3 per simulation): the compensated field's max and median
+   relative error over the simulation's non-zero elements and the error of
+   its total, against the FP64 accumulation of the same deposits */
+static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, unsigned int flags, double* relerr) {
+    static __thread void* btmp[7];
+    for (int i = 0; i < 7; i++) {
         free(btmp[i]);
         btmp[i] = NULL;
     }
@@ -1802,6 +1810,8 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
 #define bscale (*(double**)&btmp[2])
 #define bfield (*(float**)&btmp[3])
 #define bsums  (*(double**)&btmp[4])
+#define bf64   (*(double**)&btmp[5])
+#define bcomp  (*(double**)&btmp[6])
     if (n <= 0 || !cfgs || !cfgs[0]) {
         return;
     }
@@ -1879,10 +1889,38 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
     }
     device_check(mcxg_batch_set(s, bdesc, sizeof(mcxg_simdesc), (uint32_t)n, bmedia, nmedia), "uploading the batch");
     float kms = 0.f;
-    device_check(mcxg_batch_simulate(s, flags, &kms), "running the batch");
+    device_check(mcxg_batch_simulate(s, flags | (relerr ? MCXG_VERIFY : 0u), &kms), "running the batch");
     /* the volume copy is resident now (every slot is freed on both exit paths) */
     free(btmp[1]);
     btmp[1] = NULL;
+    if (relerr) {
+        bf64 = (double*)malloc(sizeof(double) * (nfield ? nfield : 1));
+        bcomp = (double*)malloc(sizeof(double) * (nfield ? nfield : 1));
+        if (!bf64 || !bcomp) {
+            MCX_ERROR(-2, "out of host memory");
+        }
+        device_check(mcxg_batch_get_verify(s, bf64, bcomp), "reading the precision check");
+        for (int k = 0; k < n; k++) {
+            const Config* cfg = cfgs[k];
+            const size_t off = bdesc[k].field_off, len = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z * cfg->maxgate;
+            double tf = 0.0, tc = 0.0, mx = 0.0;
+            size_t m = 0;
+            for (size_t i = 0; i < len; i++) {
+                const double f = bf64[off + i], c = bcomp[off + i];
+                tf += f;
+                tc += c;
+                if (f > 0.0) {
+                    const double r = fabs(c - f) / f;
+                    mx = r > mx ? r : mx;
+                    bf64[off + m++] = r;           /* reuse the slot for the sorted errors */
+                }
+            }
+            qsort(bf64 + off, m, sizeof(double), cmp_double);
+            relerr[3 * k] = mx;
+            relerr[3 * k + 1] = m ? bf64[off + m / 2] : 0.0;
+            relerr[3 * k + 2] = tf > 0.0 ? fabs(tc - tf) / tf : 0.0;
+        }
+    }
     bscale = (double*)malloc(sizeof(double) * (size_t)n);
     double* scales = bscale;
     bsums = (double*)malloc(sizeof(double) * 2 * (size_t)n);
@@ -1938,7 +1976,7 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
             cfg->exportfield[i] += src[i];
         }
     }
-    for (int i = 0; i < 5; i++) {
+    for (int i = 0; i < 7; i++) {
         free(btmp[i]);
         btmp[i] = NULL;
     }
@@ -1947,7 +1985,17 @@ void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsign
 #undef bscale
 #undef bfield
 #undef bsums
+#undef bf64
+#undef bcomp
     MCX_LEAVE();
+}
+
+void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsigned int flags) {
+    batch_run(cfgs, n, photons_per_thread, flags, NULL);
+}
+
+void mcx_run_batch_verify(Config** cfgs, int n, unsigned int photons_per_thread, double* relerr) {
+    batch_run(cfgs, n, photons_per_thread, 0u, relerr);
 }
 
 mcxg_session* mcx_prepare_simulation(Config* cfg) {

@@ -1616,13 +1616,13 @@ __device__ __forceinline__ bool claim_vt(const KArgs& a, BatchPST<C>& ps, unsign
    two-plane field is measured against), a plain float field, and a float
    field with the reference's +-1000 spill into a shadow plane
    (mcx_core.cl:2880-2886), so all three see exactly the photons of the run. */
-__device__ __forceinline__ void acc_verify(const KArgs& a, unsigned int fieldlen, unsigned int k, float w) {
+__device__ __forceinline__ void acc_verify(const KArgs& a, unsigned int planelen, unsigned int k, float w) {
     atomicAdd(a.acc64 + k, (double)w);
     atomicAdd(a.accf + k, w);
     const float o = atomicAdd(a.accs + k, w);
     if (fabsf(o) > K_MAX_ACCUM) {
         atomicAdd(a.accs + k, o > 0.f ? -K_MAX_ACCUM : K_MAX_ACCUM);
-        atomicAdd(a.accs + fieldlen + k, o > 0.f ? K_MAX_ACCUM : -K_MAX_ACCUM);
+        atomicAdd(a.accs + planelen + k, o > 0.f ? K_MAX_ACCUM : -K_MAX_ACCUM);
     }
 }
 
@@ -2045,7 +2045,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
             } else {
                 deposit<WAGG>(field_of(a, ps, 0), dep, ps.field_off() + key, weight);
                 if (ACC64 && dep) {
-                    acc_verify(a, c_p.fieldlen, key, weight);
+                    acc_verify(a, ps.lo_plane(), ps.field_off() + key, weight);
                 }
             }
             if (RF && depim) {

@@ -37,8 +37,19 @@ static void* kshape(bool refl, bool wagg, bool o3) {
     return refl ? kbatch<true, false, COMMON>(o3) : kbatch<false, false, COMMON>(o3);
 }
 
+/* the precision check of a batch: every deposit also to the FP64, plain
+   float and spill fields; 3 blocks/SM, direct deposits */
+template <bool REFL, bool COMMON>
+static void* kbatch_acc64() {
+    return (void*)mcx_transport<false, false, REFL, false, false, 3, true, false, COMMON, false, false, false, true>;
+}
+
 static void* select(int flags) {
     const bool refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    if (flags & LF_ACC64) {
+        return (flags & LF_COMMON) ? (refl ? kbatch_acc64<true, true>() : kbatch_acc64<false, true>())
+                                   : (refl ? kbatch_acc64<true, false>() : kbatch_acc64<false, false>());
+    }
     return (flags & LF_COMMON) ? kshape<true>(refl, wagg, o3) : kshape<false>(refl, wagg, o3);
 }
 

@@ -344,13 +344,17 @@ def run(cfg=None, **kwargs):
         L.mcx_clearcfg(ctypes.byref(C))
 
 
-def run_batch(cfgs, photons_per_thread=0, graph=False, aggregate=False):
+def run_batch(cfgs, photons_per_thread=0, graph=False, aggregate=False, verify=False):
     """Run many simulations in one persistent launch (a GB300 addition).
 
     cfgs: a list of run() dictionaries (label volumes, no detectors).  Returns
     the list of their output dictionaries, as run() would give one by one.
     photons_per_thread sets how many photons each reference thread (RNG
-    stream) runs (0: ceil(nphoton / 2**18), clamped to 1..16); graph=True captures the launch as a CUDA graph."""
+    stream) runs (0: ceil(nphoton / 2**18), clamped to 1..16); graph=True
+    captures the launch as a CUDA graph.  verify=True also accumulates every
+    deposit in FP64 and adds to each output's 'stat' the compensated field's
+    max and median relative error over its non-zero elements and the error
+    of its total against it ('relerr_max', 'relerr_median', 'relerr_total')."""
     L = _lib.load()
     Cs = [Config() for _ in cfgs]
     try:
@@ -359,10 +363,21 @@ def run_batch(cfgs, photons_per_thread=0, graph=False, aggregate=False):
             L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
             _check(C)
         arr = (ctypes.POINTER(Config) * len(Cs))(*[ctypes.pointer(C) for C in Cs])
-        flags = (32 if graph else 0) | (16 if aggregate else 0)
-        L.mcx_run_batch(arr, len(Cs), ctypes.c_uint(int(photons_per_thread)), ctypes.c_uint(flags))
+        rel = None
+        if verify:
+            rel = np.zeros(3 * len(Cs), np.float64)
+            L.mcx_run_batch_verify(arr, len(Cs), ctypes.c_uint(int(photons_per_thread)),
+                                   rel.ctypes.data_as(ctypes.c_void_p))
+        else:
+            flags = (32 if graph else 0) | (16 if aggregate else 0)
+            L.mcx_run_batch(arr, len(Cs), ctypes.c_uint(int(photons_per_thread)), ctypes.c_uint(flags))
         _check(Cs[0])
-        return [_outputs(cfg, C) for cfg, C in zip(cfgs, Cs)]
+        outs = [_outputs(cfg, C) for cfg, C in zip(cfgs, Cs)]
+        if rel is not None:
+            for k, o in enumerate(outs):
+                o["stat"].update(relerr_max=float(rel[3 * k]), relerr_median=float(rel[3 * k + 1]),
+                                 relerr_total=float(rel[3 * k + 2]))
+        return outs
     finally:
         for C in Cs:
             L.mcx_clearcfg(ctypes.byref(C))

@@ -193,7 +193,8 @@ def test_label_gradients_on_gpu():
     per-label mua gradients against central differences with common random
     numbers (2 %) and against the replay Jacobian summed per label; per-label
     mus gradients against central differences over +-5 % (mus moves the paths,
-    so those differences are statistical: 10 %); torch.autograd routes."""
+    so those differences are statistical: gradients and differences over 4
+    seeds agree within 3 standard errors); torch.autograd routes."""
     import torch
     cfg = dict(workloads.builtin("cubesph60b"), nphoton=2000000, seed=77)
     sim = diff.LabelReadings(cfg)
@@ -211,13 +212,27 @@ def test_label_gradients_on_gpu():
         assert abs(ga[k] / fd - 1) < 0.02, ("mua", k, ga[k], fd)
     sim.forward()
     np.testing.assert_allclose(sim.replay_mua_gradient(g), ga, rtol=1e-3)
-    for k in range(sim.nmed):
-        h = 0.05 * mus0[k]
-        sp, sm = mus0.copy(), mus0.copy()
-        sp[k] += h
-        sm[k] -= h
-        fd = (_loss(sim.forward(None, sp), Rt) - _loss(sim.forward(None, sm), Rt)) / float(2 * h)
-        assert abs(gs[k] - fd) <= 0.1 * abs(fd), ("mus", k, gs[k], fd)
+    # mus moves the paths: the likelihood-ratio gradient and the central
+    # differences are both statistical, so both are taken over 4 seeds and
+    # must agree within 3 combined standard errors
+    gl, fl = [], []
+    for sd in range(4):
+        sim.cfg["seed"] = 1000 + sd
+        Rs = sim.forward()
+        gl.append(sim.backward(_dloss(Rs, Rt))[1])
+        row = []
+        for k in range(sim.nmed):
+            h = 0.1 * mus0[k]
+            sp, sm = mus0.copy(), mus0.copy()
+            sp[k] += h
+            sm[k] -= h
+            row.append((_loss(sim.forward(None, sp), Rt) - _loss(sim.forward(None, sm), Rt)) / float(2 * h))
+        fl.append(row)
+    gl, fl = np.array(gl), np.array(fl)
+    se = np.sqrt(gl.var(0, ddof=1) / 4 + fl.var(0, ddof=1) / 4)
+    assert np.all(np.abs(gl.mean(0) - fl.mean(0)) <= 3 * se), (gl.mean(0), fl.mean(0), se)
+    sim.cfg["seed"] = 77
+    sim.forward()
     a = torch.tensor(mua0, requires_grad=True)
     s = torch.tensor(mus0, requires_grad=True)
     Rtt = diff.label_readings(sim, a, s)
@@ -276,7 +291,8 @@ def test_fluence_gradient_per_label_matches_central_differences():
     """A label volume (cube with a sphere): per-label dLoss/dmua (the
     per-voxel gradient summed over each label) against central differences
     with common random numbers (2 %), per-label dLoss/dmus against central
-    differences over +-5 % (mus moves the paths: 10 %)."""
+    differences over +-10 % (mus moves the paths: both over 4 seeds, within
+    3 combined standard errors)."""
     from mcxcl_gb300 import workloads as W
     cfg = dict(W.builtin("cubesph60b"), nphoton=2000000, seed=91, outputtype="flux", issavedet=0, isreflect=0,
                tstep=1e-9)
@@ -291,16 +307,29 @@ def test_fluence_gradient_per_label_matches_central_differences():
     F = sim.forward(prop=prop0)
     ga, gs = sim.backward(2 * (F - Ft))
     la = np.array([ga[vol == k].sum() for k in (1, 2)])
-    ls = np.array([gs[vol == k].sum() for k in (1, 2)])
 
     def loss(p):
         return float(np.sum((sim.forward(prop=p) - Ft) ** 2))
+
+    def central(k, col, rel):
+        pp, pm = prop0.copy(), prop0.copy()
+        h = np.float32(rel) * prop0[k, col]
+        pp[k, col] += h
+        pm[k, col] -= h
+        return (loss(pp) - loss(pm)) / float(pp[k, col] - pm[k, col])
     for k in (1, 2):
-        for col, g, rel, tol in ((0, la, 1e-3, 0.02), (1, ls, 0.05, 0.1)):
-            pp, pm = prop0.copy(), prop0.copy()
-            h = np.float32(rel) * prop0[k, col]
-            pp[k, col] += h
-            pm[k, col] -= h
-            fd = (loss(pp) - loss(pm)) / float(pp[k, col] - pm[k, col])
-            assert abs(g[k - 1] - fd) <= tol * abs(fd), ("mua" if col == 0 else "mus", k, g[k - 1], fd)
+        fd = central(k, 0, 1e-3)
+        assert abs(la[k - 1] - fd) <= 0.02 * abs(fd), ("mua", k, la[k - 1], fd)
+    # mus: likelihood-ratio gradients and central differences over +-10 %,
+    # both over 4 seeds, within 3 combined standard errors
+    gl, fl = [], []
+    for sd in range(4):
+        sim.cfg["seed"] = 500 + sd
+        Fs = sim.forward(prop=prop0)
+        _, gss = sim.backward(2 * (Fs - Ft))
+        gl.append([gss[vol == k].sum() for k in (1, 2)])
+        fl.append([central(k, 1, 0.1) for k in (1, 2)])
+    gl, fl = np.array(gl), np.array(fl)
+    se = np.sqrt(gl.var(0, ddof=1) / 4 + fl.var(0, ddof=1) / 4)
+    assert np.all(np.abs(gl.mean(0) - fl.mean(0)) <= 3 * se), (gl.mean(0), fl.mean(0), se)
     sim.close()

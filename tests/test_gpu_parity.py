@@ -357,3 +357,33 @@ def test_exact_kernel_trajectory_matches_oracle(gpu, O, name, kw):
     nodet = mcxcl_gb300.run(dict(cfg, nphoton=300, issavedet=0))
     assert cases.traj_digest(only["traj"]) == cases.traj_digest(nodet["traj"])
     assert "flux" not in only and "detp" not in only and "flux" in f and "detp" in f
+
+
+@pytest.mark.parametrize("shape", [(256, 3), (128, 6), (64, 12), (256, 2), (128, 4)])
+def test_every_autotuner_shape_keeps_the_answer(gpu, shape):
+    """Each launch shape the autotuner may pick (block threads x resident
+    blocks per SM, capped or uncapped registers) runs every photon and keeps
+    the cube60 known answer (mcx_gpu_benchmarks.m:46-69)."""
+    import ctypes
+    from mcxcl_gb300 import _lib, pmcxcl
+    L = _lib.load()
+    cfg = cases.cube60(nphoton=3000000, seed=29012392, issavedet=0)
+    C = _lib.Config()
+    try:
+        pmcxcl.parse_config(cfg, C)
+        L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
+        pmcxcl._check(C)
+        s = L.mcx_prepare_simulation(ctypes.byref(C))
+        pmcxcl._check(C)
+        assert L.mcxg_set_launch(s, shape[0], shape[1]) == 0
+        ms = ctypes.c_float()
+        assert L.mcxg_simulate(s, 2, ctypes.byref(ms)) == 0
+        grid, block, regs = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        L.mcxg_get_launch(s, ctypes.byref(grid), ctypes.byref(block), ctypes.byref(regs))
+        assert block.value == shape[0] and grid.value <= gpu["sm"] * shape[1]
+        esc, tot = ctypes.c_double(), ctypes.c_double()
+        assert L.mcxg_get_energy(s, ctypes.byref(esc), ctypes.byref(tot)) == 0
+        assert abs(tot.value - 3000000) <= 10
+        assert abs(1 - esc.value / tot.value - 0.1769) <= 0.005
+    finally:
+        L.mcx_clearcfg(ctypes.byref(C))
