@@ -435,11 +435,11 @@ def config_measure(k, photons, steps, warmup, flush, peak):
 
 
 def precision_measure(photons):
-    """Error of the compensated field (the product: float hi and lo planes
-    and an integer spill count), of a plain float field and of the
-    reference's +-1000 spill field against an FP64 accumulation of the same
-    deposits (one run, every deposit to all four), on the cube and the cube +
-    sphere workloads; relative error over every non-zero element."""
+    """Error of the compensated field (the product: int64 fixed-point counts
+    and a float remainder, merged in FP64), of a plain float field and of
+    the reference's +-1000 spill field against an FP64 accumulation of the
+    same deposits (one run, every deposit to all four), on the cube and the
+    cube + sphere workloads; relative error over every non-zero element."""
     import ctypes
     from mcxcl_gb300 import _lib, workloads
     L = _lib.load()

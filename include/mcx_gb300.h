@@ -317,6 +317,15 @@ size_t mcx_config_sizeof(void);
 size_t mcx_config_offsetof(const char* name);
 /* Releases the device sessions cached per GPU by mcx_run_simulation. */
 void mcx_release_sessions(void);
+/* keep = 1 (the default): mcx_run_simulation and mcx_run_batch keep one
+   device session per GPU between calls (device buffers, the uploaded volume
+   and the tuned launch shape are reused).  keep = 0: the cached sessions
+   are released now and at the end of every later call, so no device memory
+   outlives a call, as with the reference's mcx_run_simulation
+   (src/mcx_host.cpp, which frees every buffer before it returns).
+   A session returned by mcx_prepare_simulation stays usable until the next
+   mcx_run_simulation, mcx_run_batch or mcx_release_sessions. */
+void mcx_keep_sessions(int keep);
 
 /* ---- thin device layer ------------------------------------------------------ */
 

@@ -119,7 +119,7 @@ EXPORTS = [
     "mcxg_batch_simulate", "mcxg_batch_get_energy", "mcxg_batch_get_field", "mcx_savedetphoton",
     "mcxg_adjoint", "mcxg_get_verify", "mcx_readconfig", "mcx_parsejson", "mcxg_adjoint_field",
     "mcxg_get_field_planes", "mcxg_set_adjoint", "mcxg_get_adjoint_grad", "mcxg_batch_get_verify",
-    "mcx_run_batch_verify",
+    "mcx_run_batch_verify", "mcx_keep_sessions",
 ]
 
 _lib = None
@@ -152,6 +152,8 @@ def load():
     L.mcx_rand_words.argtypes = [ctypes.c_uint, vp, ctypes.c_size_t]
     L.mcx_rand_blocks.argtypes = [ctypes.c_uint, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, vp]
     L.mcx_prepare_simulation.argtypes = [P(Config)]
+    L.mcx_keep_sessions.argtypes = [ctypes.c_int]
+    L.mcx_keep_sessions.restype = None
     L.mcx_prepare_simulation.restype = vp
     L.mcx_config_sizeof.restype = ctypes.c_size_t
     L.mcx_config_offsetof.argtypes = [ctypes.c_char_p]

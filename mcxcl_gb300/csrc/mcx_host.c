@@ -1277,9 +1277,7 @@ static void adjoint_jacobians(Config* cfg, mcxg_session* s, size_t nvox) {
 static __thread int prepare_only = 0;
 static __thread mcxg_session* prepared_session = NULL;
 
-void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
-    (void)fluence;
-    (void)totalenergy;
+static void run_simulation(Config* cfg) {
     GPUInfo* gpu = NULL;
     /* temporaries live in thread-local slots so the library-mode error path
        (longjmp back to this frame) can free them */
@@ -1990,18 +1988,44 @@ static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, uns
     MCX_LEAVE();
 }
 
+/* 1: device sessions stay cached per GPU between calls (buffers, uploaded
+   volume and tuned launch shape are reused); 0: every call releases them */
+static int g_keep_sessions = 1;
+
+void mcx_keep_sessions(int keep) {
+    g_keep_sessions = keep != 0;
+    if (!g_keep_sessions) {
+        mcx_release_sessions();
+    }
+}
+
+void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
+    (void)fluence;
+    (void)totalenergy;
+    run_simulation(cfg);
+    if (!g_keep_sessions) {
+        mcx_release_sessions();
+    }
+}
+
 void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsigned int flags) {
     batch_run(cfgs, n, photons_per_thread, flags, NULL);
+    if (!g_keep_sessions) {
+        mcx_release_sessions();
+    }
 }
 
 void mcx_run_batch_verify(Config** cfgs, int n, unsigned int photons_per_thread, double* relerr) {
     batch_run(cfgs, n, photons_per_thread, 0u, relerr);
+    if (!g_keep_sessions) {
+        mcx_release_sessions();
+    }
 }
 
 mcxg_session* mcx_prepare_simulation(Config* cfg) {
     prepare_only = 1;
     prepared_session = NULL;
-    mcx_run_simulation(cfg, NULL, NULL);
+    run_simulation(cfg);
     prepare_only = 0;
     return cfg->errorcode ? NULL : prepared_session;
 }

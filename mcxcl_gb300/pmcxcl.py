@@ -323,7 +323,17 @@ def run(cfg=None, **kwargs):
     weight and time of flight when detected; a replay may give
     ``replayweight``/``replaytof``/``replaydetid`` (one entry per seed column)
     instead of ``detphotons``, and ``replaysiteown`` = 1 makes the
-    scattering-site outputs use each photon's own entries."""
+    scattering-site outputs use each photon's own entries.
+
+    Random numbers: with the default ``autopilot`` the fast kernel runs
+    about nphoton/16 threads, where the reference runs 64 x 64 x SM count,
+    so the same ``seed`` gives the same statistics but not the same photons
+    as the reference.  Give ``autopilot=0`` with the reference's ``nthread``
+    and ``nblocksize`` (and ``exactmath=1``) to follow its photons one for
+    one.
+
+    Device memory: one session per GPU stays cached between calls (see
+    ``keep_sessions``)."""
     cfg = dict(cfg or {}, **kwargs)
     L = _lib.load()
     C = Config()
@@ -342,6 +352,15 @@ def run(cfg=None, **kwargs):
         return _outputs(cfg, C)
     finally:
         L.mcx_clearcfg(ctypes.byref(C))
+
+
+def keep_sessions(keep=True):
+    """keep=True (the default): one device session per GPU stays cached
+    between ``run`` calls, reusing its buffers, uploaded volume and tuned
+    launch shape.  keep=False releases the cached sessions now and after
+    every later call, so no device memory outlives a call, as with the
+    reference's module."""
+    _lib.load().mcx_keep_sessions(1 if keep else 0)
 
 
 def run_batch(cfgs, photons_per_thread=0, graph=False, aggregate=False, verify=False):

@@ -387,3 +387,28 @@ def test_every_autotuner_shape_keeps_the_answer(gpu, shape):
         assert abs(1 - esc.value / tot.value - 0.1769) <= 0.005
     finally:
         L.mcx_clearcfg(ctypes.byref(C))
+
+
+def test_sessions_released_when_not_kept(gpu):
+    """keep_sessions(False) frees the cached device session after each call
+    (device memory returns to what it was before the call) and gives the
+    same answer as a cached session; keep_sessions(True) keeps it again."""
+    import torch
+
+    import mcxcl_gb300
+    cfg = cases.cube60(nphoton=200000, seed=7, tstep=1e-10)      # 50 gates: a 130 MB field
+    torch.cuda.init()
+    mcxcl_gb300._lib.load().mcx_release_sessions()
+    try:
+        mcxcl_gb300.keep_sessions(False)
+        free0 = torch.cuda.mem_get_info(0)[0]
+        a = mcxcl_gb300.run(cfg)
+        free1 = torch.cuda.mem_get_info(0)[0]
+        assert abs(free1 - free0) < (4 << 20), (free0, free1)
+        mcxcl_gb300.keep_sessions(True)
+        b = mcxcl_gb300.run(cfg)
+        free2 = torch.cuda.mem_get_info(0)[0]
+        assert free0 - free2 > (64 << 20), (free0, free2)
+        np.testing.assert_allclose(a["flux"], b["flux"], rtol=1e-6, atol=0)
+    finally:
+        mcxcl_gb300.keep_sessions(True)
