@@ -86,6 +86,8 @@ def parse_args():
     ap.add_argument("--block", type=int, default=0, help="profiling mode: threads per block (0: automatic)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="profiling mode: resident blocks per SM")
     ap.add_argument("--flags", type=int, default=0, help="profiling mode: mcxg_simulate flags")
+    ap.add_argument("--tile", type=int, default=-1,
+                    help="profiling mode: hot-voxel tile elements (0: off; default: the library's choice)")
     return ap.parse_args()
 
 
@@ -482,9 +484,13 @@ def profile_mode(args):
     C, sess = prepare(cfg)
     if args.block or args.blocks_per_sm:
         L.mcxg_set_launch(sess, args.block, args.blocks_per_sm)
+    if args.tile >= 0:
+        L.mcxg_set_tile(sess, args.tile)
+    box = np.zeros(8, np.uint32)
     for i in range(args.launches):
         ms = simulate(sess, args.flags)
-        print("launch %d: %.3f ms, %.1f photons/ms" % (i, ms, cfg["nphoton"] / ms), flush=True)
+        L.mcxg_get_tile(sess, box.ctypes.data)
+        print("launch %d: %.3f ms, %.1f photons/ms, tile %s" % (i, ms, cfg["nphoton"] / ms, box.tolist()), flush=True)
     L.mcx_clearcfg(ctypes.byref(C))
 
 

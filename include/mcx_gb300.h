@@ -401,6 +401,17 @@ int  mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nbloc
    capped for 768 resident threads (80 a thread), the others the uncapped
    one; blocks per SM are lowered to what fits at once. */
 int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
+/* Hot-voxel tile (no counterpart in the reference, which adds every deposit
+   to global memory, src/mcx_core.cl:2880-2886): with elements > 0, launches
+   of the fast kernel on a single simulation of the common configuration (no
+   replay, extra sources or precision check) accumulate the deposits of a box
+   of voxels next to the source, in the first gates, in each block's shared
+   memory -- at most `elements` field elements, fewer if shared memory is
+   short -- and add them to the field when the block ends.  Same fixed-point
+   split, same answer.  0 (the default) turns it off.  mcxg_get_tile gives
+   the last launch's box: x0 y0 z0 nx ny nz gates elements (all 0: none). */
+int  mcxg_set_tile(mcxg_session* s, uint32_t elements);
+int  mcxg_get_tile(mcxg_session* s, uint32_t* box);
 /* ---- batches: many simulations in one persistent launch (no counterpart in
    the reference, which launches once per simulation).  sims points to nsim
    mcxg_simdesc (csrc/mcx_kparams.h, desc_size bytes each): the parameter
@@ -488,7 +499,9 @@ int  mcxg_get_adjoint_grad(mcxg_session* s, float* gmua, float* gmus);
 /* The compensated field's raw planes (fieldlen x components each, NULL
    skips one): the int64 fixed-point counts and the float remainders; an
    element's value is count x 2^-S + remainder, with 2^-S the unit the host
-   chose for the problem (field_scale in the host driver). */
+   chose for the problem (field_scale in the host driver).  On the device
+   each element is an 8-byte cell {count bits 0-31, remainder} with the
+   count's bits 32-63 in a separate plane; this call assembles the counts. */
 int  mcxg_get_field_planes(mcxg_session* s, int64_t* counts, float* rem);
 /* The precision check's fields of the last MCXG_VERIFY launch, unscaled,
    fieldlen values each (NULL skips one): the FP64 accumulation of the same

@@ -119,7 +119,7 @@ EXPORTS = [
     "mcxg_batch_simulate", "mcxg_batch_get_energy", "mcxg_batch_get_field", "mcx_savedetphoton",
     "mcxg_adjoint", "mcxg_get_verify", "mcx_readconfig", "mcx_parsejson", "mcxg_adjoint_field",
     "mcxg_get_field_planes", "mcxg_set_adjoint", "mcxg_get_adjoint_grad", "mcxg_batch_get_verify",
-    "mcx_run_batch_verify", "mcx_keep_sessions",
+    "mcx_run_batch_verify", "mcx_keep_sessions", "mcxg_set_tile", "mcxg_get_tile",
 ]
 
 _lib = None
@@ -169,6 +169,8 @@ def load():
     L.mcxg_set_params.argtypes = [vp, vp, ctypes.c_size_t]
     L.mcxg_set_seeds.argtypes = [vp, vp, ctypes.c_uint32]
     L.mcxg_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.mcxg_set_tile.argtypes = [vp, ctypes.c_uint32]
+    L.mcxg_get_tile.argtypes = [vp, vp]
     L.mcxg_simulate.argtypes = [vp, ctypes.c_uint, P(ctypes.c_float)]
     L.mcxg_get_energy.argtypes = [vp, P(ctypes.c_double), P(ctypes.c_double)]
     L.mcxg_get_thread_energy.argtypes = [vp, vp]

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -111,7 +112,7 @@ struct mcxg_session {
     uint8_t* d_bmedia = nullptr;
     size_t bmedia_cap = 0;
     std::vector<unsigned long long> h_simvt;
-    float* d_bfield = nullptr;       /* hi, lo, spill count planes: 3 x totalfield */
+    float* d_bfield = nullptr;       /* int64 fixed-point counts (2 x totalfield floats), then float remainders */
     size_t bfield_cap = 0;
     float2* d_benergy = nullptr;     /* per reference thread of the batch */
     size_t benergy_cap = 0;
@@ -128,6 +129,8 @@ struct mcxg_session {
 
     std::vector<float> h_det, h_srcx;
     int block_req = 0, bpsm_req = 0;
+    uint32_t tile_req = 0;           /* hot-voxel tile: at most this many field elements (0: off) */
+    mcxg::KArgs::Tile tile_used{};   /* the last launch's tile (nx = 0: none) */
     int tuned = 0;                   /* 1 once mcxg_autotune picked a shape for this problem */
     int tuned_noagg = 0;
     int grid = 0, block = 0, regs = 0;
@@ -219,16 +222,24 @@ __global__ void energy_final(double* part, int nblocks) {
     }
 }
 
+/* Element i of a field buffer of total elements (all components): the
+   8-byte cells {count bits 0-31, float remainder} of every element, then the
+   counts' bits 32-63; value = count x unit + remainder in FP64. */
+__device__ __forceinline__ double cell_value(const float* __restrict__ f, size_t total, double unit, size_t i) {
+    const uint2 c = reinterpret_cast<const uint2*>(f)[i];
+    const unsigned int hi = reinterpret_cast<const unsigned int*>(f)[2 * total + i];
+    const long long count = (long long)(((unsigned long long)hi << 32) | c.x);
+    return (double)count * unit + (double)__uint_as_float(c.y);
+}
+
 /* Output element i of a field of n elements per component and total
    elements over all components: component c = i / n (1 real, or real then
-   imaginary for RF), element j = i % n.  The buffer holds the fixed-point
-   planes of all components (int64 counts of unit), then their float
-   remainder planes: value = count x unit + remainder in FP64. */
+   imaginary for RF), element j = i % n. */
 __device__ __forceinline__ double merged_at(const float* __restrict__ f, size_t n, size_t total, double unit, size_t i,
                                             size_t& j) {
     const size_t c = i / n;
     j = i - c * n;
-    return (double)((const long long*)f)[i] * unit + (double)f[2 * total + i];
+    return cell_value(f, total, unit, i);
 }
 
 __global__ void field_merge_f32(const float* __restrict__ f, size_t n, size_t total, double unit, double scale,
@@ -315,8 +326,7 @@ __global__ void batch_merge(const float* __restrict__ f, unsigned long long tota
     const unsigned int n = d.kp.fieldlen;
     const double sc = scales[blockIdx.y];
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        out[off + i] = (float)(((double)((const long long*)f)[off + i] * (double)d.kp.fxunit +
-                                (double)f[2 * total + off + i]) * sc);
+        out[off + i] = (float)(cell_value(f, total, (double)d.kp.fxunit, off + i) * sc);
     }
 }
 
@@ -327,7 +337,7 @@ __global__ void batch_merge_f64(const float* __restrict__ f, unsigned long long 
     const unsigned long long off = d.field_off;
     const unsigned int n = d.kp.fieldlen;
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        out[off + i] = (double)((const long long*)f)[off + i] * (double)d.kp.fxunit + (double)f[2 * total + off + i];
+        out[off + i] = cell_value(f, total, (double)d.kp.fxunit, off + i);
     }
 }
 
@@ -460,6 +470,79 @@ size_t shared_bytes(const mcxg_kparams& kp, int block) {
         det = (size_t)kp.partialdata + 2;    /* the launch phase's cos and sin follow the partial data */
     }
     return (size_t)kp.medianum * 32 + (size_t)block * 32 + (size_t)(kp.nphase + kp.nangle) * 4 + det * (size_t)block * 4;
+}
+
+/* q = umulhi(n, m) >> sh equals n / d for every n < bound: m = ceil(2^(32+sh) / d)
+   with the largest sh that keeps m below 2^32, exact when (bound - 1) e <
+   2^(32+sh), e = m d - 2^(32+sh) (the rounding error of m times d) */
+bool exact_divider(uint32_t d, uint32_t bound, uint32_t* m, uint32_t* sh) {
+    if (d < 2) {
+        return false;
+    }
+    for (int k = 31; k >= 0; k--) {
+        const unsigned long long p = 1ull << (32 + k);
+        const unsigned long long mm = (p + d - 1) / d;
+        if (mm >= (1ull << 32)) {
+            continue;
+        }
+        const unsigned long long e = mm * d - p;
+        if ((unsigned long long)(bound ? bound - 1 : 0) * e < p) {
+            *m = (uint32_t)mm;
+            *sh = (uint32_t)k;
+            return true;
+        }
+        return false;
+    }
+    return false;
+}
+
+/* The hot-voxel tile of a single simulation: a box of voxels next to the
+   source, along its direction, in the first gates.  Most deposits of a
+   pencil beam fall there (the oracle's deposit counts: 17 % of the cube +
+   sphere workload's in 11 x 11 x 11 voxels x 3 gates, 33 % of the head's in
+   16^3 voxels x 1 gate).  Gates: enough that they span about 64 voxels of
+   path at n = 1.4; the cube side is what the element budget then allows. */
+bool tile_geometry(const mcxg_kparams& kp, uint32_t maxelem, mcxg::KArgs::Tile& t) {
+    t = mcxg::KArgs::Tile{};
+    if (maxelem < 8 || kp.maxgate < 1 || kp.Rtstep <= 0.f || kp.oneoverc0 <= 0.f) {
+        return false;
+    }
+    const double pathvox = 1.0 / ((double)kp.Rtstep * kp.oneoverc0 * 1.4);
+    uint32_t ng = (uint32_t)std::ceil(64.0 / (pathvox > 1e-3 ? pathvox : 1e-3));
+    ng = std::max(1u, std::min(ng, std::min(8u, kp.maxgate)));
+    int side = (int)std::floor(std::cbrt((double)maxelem / ng));
+    while (side > 1 && (unsigned long long)side * side * side * ng > maxelem) {
+        side--;
+    }
+    if (side < 2) {
+        return false;
+    }
+    const int dims[3] = {(int)kp.dimx, (int)kp.dimy, (int)kp.dimz};
+    const float c[3] = {kp.srcpos.x + kp.srcdir.x * side * 0.5f, kp.srcpos.y + kp.srcdir.y * side * 0.5f,
+                        kp.srcpos.z + kp.srcdir.z * side * 0.5f};
+    int n[3], o[3];
+    for (int i = 0; i < 3; i++) {
+        n[i] = std::min(side, dims[i]);
+        float lo = std::floor(c[i] - n[i] * 0.5f);
+        if (!(lo >= 0.f)) {
+            lo = 0.f;
+        }
+        o[i] = std::min((int)lo, dims[i] - n[i]);
+    }
+    t.x0 = o[0];
+    t.y0 = o[1];
+    t.z0 = o[2];
+    t.nx = (uint32_t)n[0];
+    t.ny = (uint32_t)n[1];
+    t.nz = (uint32_t)n[2];
+    t.ng = ng;
+    t.lo = (uint32_t)o[2] * kp.dimxy;
+    t.span = (uint32_t)n[2] * kp.dimxy;
+    if (!exact_divider(kp.dimxy, kp.nvox, &t.mxy, &t.sxy) || !exact_divider(kp.dimx, kp.dimxy, &t.mx, &t.sx)) {
+        t = mcxg::KArgs::Tile{};
+        return false;
+    }
+    return true;
 }
 
 }  // namespace
@@ -841,6 +924,25 @@ int mcxg_set_replay(mcxg_session* s, const void* seeds16, const float* weight, c
     return MCXG_OK;
 }
 
+int mcxg_set_tile(mcxg_session* s, uint32_t elements) {
+    if (!s) {
+        return MCXG_ERR_ARG;
+    }
+    s->tile_req = elements;
+    return MCXG_OK;
+}
+
+int mcxg_get_tile(mcxg_session* s, uint32_t* box) {
+    if (!s || !box) {
+        return MCXG_ERR_ARG;
+    }
+    const KArgs::Tile& t = s->tile_used;
+    const uint32_t v[8] = {(uint32_t)t.x0, (uint32_t)t.y0, (uint32_t)t.z0, t.nx, t.ny, t.nz, t.ng,
+                           t.nx * t.ny * t.nz * t.ng};
+    memcpy(box, v, sizeof(v));
+    return MCXG_OK;
+}
+
 int mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm) {
     if (!s || block < 0 || block > 256 || (block % 32) || blocks_per_sm < 0) {
         return MCXG_ERR_ARG;
@@ -900,8 +1002,8 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     a.srcpattern = s->d_pattern;
     a.seeds = s->d_seeds;
     a.field = s->d_field;
-    a.fhi = (unsigned long long*)s->d_field;
-    a.flo = s->d_field + 2 * (size_t)kp.fieldlen * field_comps(kp);
+    a.fcell = reinterpret_cast<uint2*>(s->d_field);
+    a.fcarry = reinterpret_cast<unsigned int*>(s->d_field + 2 * (size_t)kp.fieldlen * field_comps(kp));
     a.smatrix = s->d_smatrix;
     a.s0 = s->pol_s0;
     a.maxpol = s->npol;
@@ -988,6 +1090,25 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
         a.accs = s->d_accs;
     }
     size_t smem = shared_bytes(kp, block);
+    s->tile_used = KArgs::Tile{};
+    if (s->tile_req && !exact && common && !verify && !adjmode && !kp.replay && !kp.extrasrclen && kp.srcnum <= 1 &&
+            kp.save2pt && !(flags & MCXG_RNGDUMP)) {
+        /* the hot-voxel tile: what shared memory is left at this shape's
+           blocks per SM (1 KB of each block's share is the system's) */
+        int smsm = 0;
+        MCXG_TRY(cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->device));
+        const size_t off = (smem + 7) & ~(size_t)7;
+        const long long avail = (long long)smsm / bpsm_sel - 1024 - (long long)off;
+        const uint32_t maxel = avail > 0 ? (uint32_t)std::min<long long>(avail / 12, (long long)s->tile_req) : 0u;
+        KArgs::Tile t;
+        if (tile_geometry(kp, maxel, t)) {
+            t.smemoff = (uint32_t)off;
+            a.tile = t;
+            smem = off + 12 * (size_t)t.nx * t.ny * t.nz * t.ng;
+            lflags |= mcxg::LF_TILE;
+            s->tile_used = t;
+        }
+    }
     if (smem > s->info.sharedmem_per_block) {
         return MCXG_ERR_LIMIT;
     }
@@ -1353,13 +1474,21 @@ int mcxg_get_field_planes(mcxg_session* s, int64_t* counts, float* rem) {
     }
     MCXG_TRY(cudaSetDevice(s->device));
     const size_t total = (size_t)s->kp.fieldlen * field_comps(s->kp);
+    std::vector<uint32_t> cells(2 * total), hi(counts ? total : 0);
+    MCXG_TRY(cudaMemcpyAsync(cells.data(), s->d_field, sizeof(uint32_t) * 2 * total, cudaMemcpyDeviceToHost, s->st));
     if (counts) {
-        MCXG_TRY(cudaMemcpyAsync(counts, s->d_field, sizeof(int64_t) * total, cudaMemcpyDeviceToHost, s->st));
-    }
-    if (rem) {
-        MCXG_TRY(cudaMemcpyAsync(rem, s->d_field + 2 * total, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
+        MCXG_TRY(cudaMemcpyAsync(hi.data(), s->d_field + 2 * total, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost,
+                                 s->st));
     }
     MCXG_TRY(cudaStreamSynchronize(s->st));
+    for (size_t i = 0; i < total; i++) {
+        if (counts) {
+            counts[i] = (int64_t)(((uint64_t)hi[i] << 32) | cells[2 * i]);
+        }
+        if (rem) {
+            memcpy(rem + i, &cells[2 * i + 1], sizeof(float));
+        }
+    }
     return MCXG_OK;
 }
 
@@ -1525,8 +1654,8 @@ int batch_enqueue(mcxg_session* s, int lflags) {
     a.media8 = s->d_bmedia;
     a.media32 = (const uint32_t*)s->d_bmedia;
     a.field = s->d_bfield;
-    a.fhi = (unsigned long long*)s->d_bfield;
-    a.flo = s->d_bfield + 2 * (size_t)s->totalfield;
+    a.fcell = reinterpret_cast<uint2*>(s->d_bfield);
+    a.fcarry = reinterpret_cast<unsigned int*>(s->d_bfield + 2 * (size_t)s->totalfield);
     a.energy = s->d_benergy;
     a.detcount = s->d_words + 0;
     a.vtcounter = s->d_words + 1;

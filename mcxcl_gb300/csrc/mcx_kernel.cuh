@@ -832,34 +832,40 @@ __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Pho
 
 /* ---------------------------------------------------------------- deposit */
 
-/* Compensated accumulation: each field component is a plane of signed
-   64-bit fixed-point counts of 2^-S and a plane of float remainders.  A
-   deposit w is split exactly into k = round(w 2^S) and r = w - k 2^-S
-   (|r| <= 2^-(S+1)); k goes to the integer plane, r to the float plane, both
-   with fire-and-forget atomics.  Integer adds are exact in any order -- also
-   when the memory system merges the adds of several lanes to one address --
-   so the bulk of an element carries no rounding at all, and the remainders
-   are too small for the float plane's rounding to matter: an element is
-   count x 2^-S + remainder, summed in FP64.  The host picks S per problem so
-   that no element can reach 2^62 units (mcx_host.c, field_scale).  A float
-   running sum, or float high and low planes compensated by the value an
-   atomic returns (TwoSum), loses the low-order deposits of the hottest
-   voxels at 1e8-1e9 photons. */
+/* Compensated accumulation: each field element holds a signed 64-bit
+   fixed-point count of 2^-S and a float remainder.  A deposit w is split
+   exactly into k = round(w 2^S) and r = w - k 2^-S (|r| <= 2^-(S+1)).
+   Integer adds are exact in any order -- also when the memory system merges
+   the adds of several lanes to one address -- so the bulk of an element
+   carries no rounding at all, and the remainders are too small for their
+   float rounding to matter: an element is count x 2^-S + remainder, summed
+   in FP64.  The host picks S per problem so that no element can reach 2^62
+   units (mcx_host.c, field_scale).  A float running sum, or float high and
+   low planes compensated by the value an atomic returns (TwoSum), loses the
+   low-order deposits of the hottest voxels at 1e8-1e9 photons.
+
+   Layout: per component, an 8-byte cell per element {low 32 bits of the
+   count, remainder} and a separate plane of the counts' high 32 bits.  A
+   deposit touches one cell -- one 32-byte sector for both adds -- and the
+   high word only when the low word wraps (the add's returned value says
+   when) or k itself reaches 2^32, so the working set the deposits keep in
+   L2 is 8 bytes an element. */
 struct Field {
-    unsigned long long* hi;        /* fixed-point counts */
-    float* lo;                     /* remainders */
+    uint2* cell;                   /* {count bits 0-31, remainder as float bits} */
+    unsigned int* carry;           /* count bits 32-63 */
     float sc, unit;                /* 2^S, 2^-S */
 };
 
-/* component comp of the field (0 real, 1 imaginary); the planes of the
-   components follow one another, plane length ps.lo_plane() */
+/* component comp of the field (0 real, 1 imaginary); the cells of the
+   components follow one another, then their high words, plane length
+   ps.lo_plane() */
 template <class PS>
 __device__ __forceinline__ Field field_of(const KArgs& a, const PS& ps, unsigned int comp) {
     const mcxg_kparams& c_p = ps.p();
     const size_t F = ps.lo_plane();
     Field f;
-    f.hi = a.fhi + comp * F;
-    f.lo = a.flo + comp * F;
+    f.cell = a.fcell + comp * F;
+    f.carry = a.fcarry + comp * F;
     f.sc = c_p.fxscale;
     f.unit = c_p.fxunit;
     return f;
@@ -872,12 +878,22 @@ __device__ __forceinline__ void field_split(const Field& f, float w, long long& 
     r = __fsub_rn(w, __fmul_rn((float)k, f.unit));
 }
 
+/* count += k as two 32-bit words: the low word's carry-out (the returned
+   old value plus the added word wraps) and k's own high word go to the high
+   word, modulo 2^32 -- the 64-bit two's-complement sum, exact for negative
+   k too */
 __device__ __forceinline__ void field_commit(const Field& f, size_t i, long long k, float r) {
-    if (k) {
-        atomicAdd(f.hi + i, (unsigned long long)k);
-    }
     if (r != 0.f) {
-        atomicAdd(f.lo + i, r);
+        atomicAdd((float*)&f.cell[i].y, r);
+    }
+    const unsigned int lo = (unsigned int)(unsigned long long)k;
+    unsigned int up = (unsigned int)((unsigned long long)k >> 32);
+    if (lo) {
+        const unsigned int old = atomicAdd(&f.cell[i].x, lo);
+        up += (old + lo < old) ? 1u : 0u;
+    }
+    if (up) {
+        atomicAdd(f.carry + i, up);
     }
 }
 
@@ -888,14 +904,62 @@ __device__ __forceinline__ void field_add(const Field& f, size_t i, float w) {
     field_commit(f, i, k, r);
 }
 
+/* The transport loop's own deposits defer the carry test of the low-word
+   add to the lane's next deposit (or the end of its work), so the add's
+   returned value is read about one step after it was issued and its latency
+   is hidden: old value, added word and element of the add in flight. */
+struct PendingCarry {
+    unsigned int old, lo, idx;
+};
+
+__device__ __forceinline__ void carry_settle(const Field& f, PendingCarry& p) {
+    if (p.lo && p.old + p.lo < p.old) {
+        atomicAdd(f.carry + p.idx, 1u);
+    }
+    p.lo = 0u;
+}
+
+__device__ __forceinline__ void field_commit_deferred(const Field& f, unsigned int i, long long k, float r,
+                                                      PendingCarry& p) {
+    if (r != 0.f) {
+        atomicAdd((float*)&f.cell[i].y, r);
+    }
+    const unsigned int lo = (unsigned int)(unsigned long long)k;
+    const unsigned int up = (unsigned int)((unsigned long long)k >> 32);
+    if (up) {
+        atomicAdd(f.carry + i, up);
+    }
+    if (lo) {
+        carry_settle(f, p);
+        p.old = atomicAdd(&f.cell[i].x, lo);
+        p.lo = lo;
+        p.idx = i;
+    }
+}
+
+/* either commit: deferred carry test (DEFER) or an immediate one */
+template <bool DEFER>
+__device__ __forceinline__ void field_commit_as(const Field& f, unsigned int i, long long k, float r, PendingCarry& p) {
+    if (DEFER) {
+        field_commit_deferred(f, i, k, r, p);
+    } else {
+        field_commit(f, i, k, r);
+    }
+}
+
 /* Deposit from every lane that has one; with WAGG, lanes of the warp hitting
    the same field element add their integer parts (exactly) and their
-   remainders first and one leader commits. */
-template <bool WAGG>
-__device__ __forceinline__ void deposit(const Field& f, bool doit, unsigned int key, float w) {
+   remainders first and one leader commits.  DEFER: the carry test waits for
+   the lane's next deposit (three registers the register-capped specialised
+   instantiations -- RF, polarised, split voxels -- do not have to spare). */
+template <bool WAGG, bool DEFER>
+__device__ __forceinline__ void deposit(const Field& f, bool doit, unsigned int key, float w, PendingCarry& p) {
     if (!WAGG) {
         if (doit) {
-            field_add(f, key, w);
+            long long k;
+            float r;
+            field_split(f, w, k, r);
+            field_commit_as<DEFER>(f, key, k, r, p);
         }
         return;
     }
@@ -910,7 +974,7 @@ __device__ __forceinline__ void deposit(const Field& f, bool doit, unsigned int 
     unsigned int peers = __match_any_sync(m, key);
     unsigned int lane = threadIdx.x & 31u;
     if (peers == (1u << lane)) {
-        field_commit(f, key, k, r);
+        field_commit_as<DEFER>(f, key, k, r, p);
         return;
     }
     long long ksum = 0;
@@ -923,7 +987,7 @@ __device__ __forceinline__ void deposit(const Field& f, bool doit, unsigned int 
         rsum += __shfl_sync(peers, r, src);
     }
     if ((int)lane == __ffs(peers) - 1) {
-        field_commit(f, key, ksum, rsum);
+        field_commit_as<DEFER>(f, key, ksum, rsum, p);
     }
 }
 
@@ -1646,13 +1710,41 @@ __device__ __forceinline__ void acc_verify(const KArgs& a, unsigned int planelen
    J is known only when the photon ends, so the photons run twice with the
    same random numbers: pass 1 stores each photon's J, pass 2 reads it at the
    launch and accumulates the gradients. */
+/* Hot-voxel tile: the element of the box that voxel idx of gate tshift falls
+   in, or 0xFFFFFFFF (the divisions are the host's exact multiply-shift pairs) */
+__device__ __forceinline__ unsigned int tile_element(const KArgs& a, const mcxg_kparams& c_p, unsigned int idx,
+                                                     int tshift) {
+    const KArgs::Tile& t = a.tile;
+    if (idx - t.lo >= t.span || (unsigned int)tshift >= t.ng) {
+        return 0xFFFFFFFFu;
+    }
+    const unsigned int z = __umulhi(idx, t.mxy) >> t.sxy;
+    const unsigned int r = idx - z * c_p.dimxy;
+    const unsigned int y = __umulhi(r, t.mx) >> t.sx;
+    const unsigned int x = r - y * c_p.dimx;
+    const unsigned int ty = y - (unsigned int)t.y0, tx = x - (unsigned int)t.x0;
+    if (ty >= t.ny || tx >= t.nx) {
+        return 0xFFFFFFFFu;
+    }
+    return (((unsigned int)tshift * t.nz + (z - (unsigned int)t.z0)) * t.ny + ty) * t.nx + tx;
+}
+
+/* the block's tile: fixed-point counts, then remainders, in shared memory */
+__device__ __forceinline__ unsigned long long* tile_counts(const KArgs& a) {
+    return (unsigned long long*)((char*)mcxg_smem + a.tile.smemoff);
+}
+
+__device__ __forceinline__ unsigned int tile_size(const KArgs& a) {
+    return a.tile.nx * a.tile.ny * a.tile.nz * a.tile.ng;
+}
+
 __device__ __forceinline__ size_t adj_slot(const mcxg_kparams& c_p, unsigned int vt, float fw) {
     return (size_t)vt * (c_p.threadphoton + 1u) + (unsigned int)((int)fw - 1);
 }
 
 template <bool EXACT, bool DET, bool REFL, bool WAGG, bool COUNT, int MINB, bool BATCH = false, bool XMEDIA = false,
           bool COMMON = false, bool RF = false, bool POL = false, bool SVMC = false, bool ACC64 = false,
-          bool ADJ = false>
+          bool ADJ = false, bool TILE = false>
 __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     typedef Mth<EXACT> M;
     typedef typename std::conditional<BATCH, BatchPST<COMMON>, ConstPST<XMEDIA, COMMON>>::type PS;
@@ -1694,6 +1786,17 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     bool vdirty = true;
     bool testint = false, hitintf = false;    /* split voxels: test the plane this step / the step ended on it */
     float adjJ = 0.f, adjP = 0.f;             /* fluence gradient: the photon's loss total and its running part */
+    PendingCarry pend = {0u, 0u, 0u};         /* the carry test of this lane's last deposit */
+    if (TILE) {
+        /* the hot-voxel tile starts empty in every block */
+        unsigned long long* tc = tile_counts(a);
+        float* tr = (float*)(tc + tile_size(a));
+        for (unsigned int i = threadIdx.x; i < tile_size(a); i += blockDim.x) {
+            tc[i] = 0ull;
+            tr[i] = 0.f;
+        }
+        __syncthreads();
+    }
 
     while (claimed) {
         const mcxg_kparams& c_p = ps.p();
@@ -2009,6 +2112,23 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     if (key >= c_p.fieldlen) {
                         key -= c_p.fieldlen;
                     }
+                    if (TILE && dep) {
+                        /* an element of the hot-voxel tile: the same split, into shared memory */
+                        const unsigned int te = tile_element(a, c_p, idx1dold, tshift);
+                        if (te != 0xFFFFFFFFu) {
+                            long long k;
+                            float r;
+                            field_split(field_of(a, ps, 0), weight, k, r);
+                            unsigned long long* tc = tile_counts(a);
+                            if (k) {
+                                atomicAdd(tc + te, (unsigned long long)k);
+                            }
+                            if (r != 0.f) {
+                                atomicAdd((float*)(tc + tile_size(a)) + te, r);
+                            }
+                            dep = false;
+                        }
+                    }
                 }
                 if (ADJ) {
                     /* the visit that just ended, in voxel idx1dold */
@@ -2043,7 +2163,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     share_deposit(a, ps, key, weight);
                 }
             } else {
-                deposit<WAGG>(field_of(a, ps, 0), dep, ps.field_off() + key, weight);
+                deposit<WAGG, !(RF || POL || SVMC)>(field_of(a, ps, 0), dep, ps.field_off() + key, weight, pend);
                 if (ACC64 && dep) {
                     acc_verify(a, ps.lo_plane(), ps.field_off() + key, weight);
                 }
@@ -2225,6 +2345,34 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         }
     }
 
+    carry_settle(field_of(a, ps, 0), pend);
+
+    if (TILE) {
+        /* the block's tile into the field: one pair of atomics per touched element */
+        __syncthreads();
+        const mcxg_kparams& kp = ps.p();
+        const Field f = field_of(a, ps, 0);
+        const unsigned long long* tc = tile_counts(a);
+        const float* tr = (const float*)(tc + tile_size(a));
+        const KArgs::Tile& t = a.tile;
+        for (unsigned int i = threadIdx.x; i < tile_size(a); i += blockDim.x) {
+            const unsigned long long c = tc[i];
+            const float r = tr[i];
+            if (c || r != 0.f) {
+                unsigned int j = i;
+                const unsigned int x = j % t.nx;
+                j /= t.nx;
+                const unsigned int y = j % t.ny;
+                j /= t.ny;
+                const unsigned int z = j % t.nz;
+                const unsigned int g = j / t.nz;
+                const size_t key = ps.field_off() + (size_t)((unsigned int)t.z0 + z) * kp.dimxy +
+                                   ((unsigned int)t.y0 + y) * kp.dimx + ((unsigned int)t.x0 + x) + (size_t)g * kp.nvox;
+                field_commit(f, key, (long long)c, r);
+            }
+        }
+    }
+
     if (COUNT) {
         atomicAdd(a.counters + 0, cnt_step);
         atomicAdd(a.counters + 1, cnt_scat);
@@ -2246,7 +2394,7 @@ __global__ void mcx_rng_dump(const KArgs a) {
         t.a = (unsigned long long)sd.x << 32 | sd.y;
         t.b = (unsigned long long)sd.z << 32 | sd.w;
         for (unsigned int j = vt; j < c_p.fieldlen; j += c_p.nthread) {
-            a.flo[j] = rnd(t);
+            reinterpret_cast<float*>(a.fcell)[2 * (size_t)j + 1] = rnd(t);   /* the remainder word */
         }
     }
 }

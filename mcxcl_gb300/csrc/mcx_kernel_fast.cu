@@ -81,8 +81,20 @@ static void* kadj() {
                                 true>;
 }
 
+/* the common configuration with the hot-voxel tile in shared memory:
+   3 blocks/SM, direct deposits */
+template <bool DET, bool REFL>
+static void* ktile() {
+    return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, true, false, false, false, false,
+                                false, true>;
+}
+
 static void* select(int flags) {
     const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    if (flags & LF_TILE) {
+        return det ? (refl ? ktile<true, true>() : ktile<true, false>())
+                   : (refl ? ktile<false, true>() : ktile<false, false>());
+    }
     if (flags & LF_ADJ) {
         return refl ? kadj<true>() : kadj<false>();
     }

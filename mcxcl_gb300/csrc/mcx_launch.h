@@ -21,11 +21,11 @@ struct KArgs {
     const float* angleinvcdf;
     const float* srcpattern;
     const uint4* seeds;            /* 4 x 32-bit seed words per reference thread */
-    float* field;                  /* the field buffer: fixed-point planes (comps x fieldlen int64), then
-                                      remainder planes (comps x fieldlen float); raw float scratch for
-                                      the fluence-gradient passes */
-    unsigned long long* fhi;       /* fixed-point counts of component c at fhi + c x plane length */
-    float* flo;                    /* float remainders of component c at flo + c x plane length */
+    float* field;                  /* the field buffer: 8-byte cells {count bits 0-31, float remainder}
+                                      (comps x fieldlen), then the counts' bits 32-63 (comps x fieldlen
+                                      uint32); raw float scratch for the fluence-gradient passes */
+    uint2* fcell;                  /* cells of component c at fcell + c x plane length */
+    unsigned int* fcarry;          /* high count words of component c at fcarry + c x plane length */
     float2* energy;                /* per reference thread: escaped, launched weight */
     float* detp;                   /* maxdetphoton x reclen */
     unsigned long long* detseed;   /* maxdetphoton x 2 */
@@ -68,11 +68,26 @@ struct KArgs {
     const float* adjc;
     float* adjJ;
     unsigned int adjmode;
+    /* hot-voxel tile (instantiations with TILE only): the field elements of
+       the box [x0, x0 + nx) x [y0, y0 + ny) x [z0, z0 + nz) in gates [0, ng)
+       accumulate in each block's shared memory, from byte smemoff of the
+       dynamic shared memory, and go to the field when the block ends.  A voxel
+       index i is tested as: (i - lo) < span (the box's z planes), then
+       z = umulhi(i, mxy) >> sxy, and y = umulhi(i - z dimxy, mx) >> sx --
+       divisions by dimxy and dimx that the host checked exact for every index
+       of the volume */
+    struct Tile {
+        int x0, y0, z0;
+        unsigned int nx, ny, nz, ng;
+        unsigned int lo, span;
+        unsigned int mx, mxy, sx, sxy;
+        unsigned int smemoff;
+    } tile;
 };
 
 /* flag bits for the launch entries */
 enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128, LF_POL = 256, LF_SVMC = 512,
-       LF_ACC64 = 1024, LF_ADJ = 2048 };
+       LF_ACC64 = 1024, LF_ADJ = 2048, LF_TILE = 4096 };
 
 /* fast instantiation: hardware transcendental approximations */
 cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int ndet, const float* srcx16,

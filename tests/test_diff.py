@@ -290,9 +290,16 @@ def test_fluence_gradient_per_voxel_mua_matches_central_differences():
 def test_fluence_gradient_per_label_matches_central_differences():
     """A label volume (cube with a sphere): per-label dLoss/dmua (the
     per-voxel gradient summed over each label) against central differences
-    with common random numbers (2 %), per-label dLoss/dmus against central
-    differences over +-10 % (mus moves the paths: both over 4 seeds, within
-    3 combined standard errors)."""
+    with common random numbers (2 %); per-label dLoss/dmus against central
+    differences over +-5 % (mus moves the paths: both over 4 seeds, within
+    3 combined standard errors).
+
+    The mus check differentiates the linear functional sum(c F) with c held
+    fixed (c = dLoss/dF of one earlier run): with c taken from the same
+    photons as the gradient, the likelihood-ratio estimate carries a
+    covariance term of order 1/N that the central difference of the noisy
+    loss does not have in the same form, so the two would differ by a bias
+    that is not an error of either."""
     from mcxcl_gb300 import workloads as W
     cfg = dict(W.builtin("cubesph60b"), nphoton=2000000, seed=91, outputtype="flux", issavedet=0, isreflect=0,
                tstep=1e-9)
@@ -320,15 +327,26 @@ def test_fluence_gradient_per_label_matches_central_differences():
     for k in (1, 2):
         fd = central(k, 0, 1e-3)
         assert abs(la[k - 1] - fd) <= 0.02 * abs(fd), ("mua", k, la[k - 1], fd)
-    # mus: likelihood-ratio gradients and central differences over +-10 %,
-    # both over 4 seeds, within 3 combined standard errors
+    # mus: likelihood-ratio gradients of sum(c F) and its central differences
+    # over +-5 %, both over 4 seeds, within 3 combined standard errors
+    c = 2 * (F - Ft)
+
+    def linear(p):
+        return float(np.sum(c * sim.forward(prop=p)))
+
+    def central_lin(k, rel):
+        pp, pm = prop0.copy(), prop0.copy()
+        h = np.float32(rel) * prop0[k, 1]
+        pp[k, 1] += h
+        pm[k, 1] -= h
+        return (linear(pp) - linear(pm)) / float(pp[k, 1] - pm[k, 1])
     gl, fl = [], []
     for sd in range(4):
         sim.cfg["seed"] = 500 + sd
-        Fs = sim.forward(prop=prop0)
-        _, gss = sim.backward(2 * (Fs - Ft))
+        sim.forward(prop=prop0)
+        _, gss = sim.backward(c)
         gl.append([gss[vol == k].sum() for k in (1, 2)])
-        fl.append([central(k, 1, 0.1) for k in (1, 2)])
+        fl.append([central_lin(k, 0.05) for k in (1, 2)])
     gl, fl = np.array(gl), np.array(fl)
     se = np.sqrt(gl.var(0, ddof=1) / 4 + fl.var(0, ddof=1) / 4)
     assert np.all(np.abs(gl.mean(0) - fl.mean(0)) <= 3 * se), (gl.mean(0), fl.mean(0), se)
