@@ -395,6 +395,8 @@ def roofline(per, ops, kms, nphoton, peak, k, sample):
     achieved = ops * nphoton / (kms * 1e-3) / 1e9
     return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "Gop/s",
             "frac": achieved / peak if peak else None, "traffic": read_traffic(k),
+            "traffic_from": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one full launch, "
+                            "profiles/traffic_mcx_transport_config%d.txt" % k,
             "peak_source": "measured in this run: 8-chain FMA kernel, one FMA = one op",
             "ops_per_photon": ops, "events_per_photon": per,
             "model": "48*step + 65*scatter + 20*launch + 10*Fresnel FP32 ops",

@@ -349,6 +349,8 @@ void mcx_keep_sessions(int keep);
 #define MCXG_ADJ1   256u   /* fluence gradient, pass 1: each photon's loss total (mcxg_set_adjoint first) */
 #define MCXG_ADJ2   512u   /* fluence gradient, pass 2: the gradients, same photons (read with
                               mcxg_get_adjoint_grad) */
+#define MCXG_NOL2WINDOW 1024u /* no persisting L2 window over the field's count plane (for measurement: the
+                                window keeps the counts in L2 and cuts the launch's DRAM write-backs) */
 #define MCXG_VERIFY 128u   /* precision check (fast kernel, common configuration, no replay, no KEEP): every
                               deposit also goes to an FP64 field, a plain float field and a float field with
                               the reference's +-1000 spill plane; read them with mcxg_get_verify */
@@ -499,9 +501,7 @@ int  mcxg_get_adjoint_grad(mcxg_session* s, float* gmua, float* gmus);
 /* The compensated field's raw planes (fieldlen x components each, NULL
    skips one): the int64 fixed-point counts and the float remainders; an
    element's value is count x 2^-S + remainder, with 2^-S the unit the host
-   chose for the problem (field_scale in the host driver).  On the device
-   each element is an 8-byte cell {count bits 0-31, remainder} with the
-   count's bits 32-63 in a separate plane; this call assembles the counts. */
+   chose for the problem (field_scale in the host driver). */
 int  mcxg_get_field_planes(mcxg_session* s, int64_t* counts, float* rem);
 /* The precision check's fields of the last MCXG_VERIFY launch, unscaled,
    fieldlen values each (NULL skips one): the FP64 accumulation of the same

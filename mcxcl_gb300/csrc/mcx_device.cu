@@ -130,6 +130,11 @@ struct mcxg_session {
     std::vector<float> h_det, h_srcx;
     int block_req = 0, bpsm_req = 0;
     uint32_t tile_req = 0;           /* hot-voxel tile: at most this many field elements (0: off) */
+    /* L2 persisting window over the field's count plane (l2_window) */
+    bool l2_set = false;             /* this session raised the context's persisting limit */
+    size_t l2_prev = 0;              /* the limit before */
+    const void* l2_base = nullptr;   /* the window set on the stream (nullptr: none) */
+    size_t l2_bytes = 0;
     mcxg::KArgs::Tile tile_used{};   /* the last launch's tile (nx = 0: none) */
     int tuned = 0;                   /* 1 once mcxg_autotune picked a shape for this problem */
     int tuned_noagg = 0;
@@ -223,13 +228,10 @@ __global__ void energy_final(double* part, int nblocks) {
 }
 
 /* Element i of a field buffer of total elements (all components): the
-   8-byte cells {count bits 0-31, float remainder} of every element, then the
-   counts' bits 32-63; value = count x unit + remainder in FP64. */
+   fixed-point planes of all components (int64 counts of unit), then their
+   float remainder planes; value = count x unit + remainder in FP64. */
 __device__ __forceinline__ double cell_value(const float* __restrict__ f, size_t total, double unit, size_t i) {
-    const uint2 c = reinterpret_cast<const uint2*>(f)[i];
-    const unsigned int hi = reinterpret_cast<const unsigned int*>(f)[2 * total + i];
-    const long long count = (long long)(((unsigned long long)hi << 32) | c.x);
-    return (double)count * unit + (double)__uint_as_float(c.y);
+    return (double)reinterpret_cast<const long long*>(f)[i] * unit + (double)f[2 * total + i];
 }
 
 /* Output element i of a field of n elements per component and total
@@ -545,6 +547,60 @@ bool tile_geometry(const mcxg_kparams& kp, uint32_t maxelem, mcxg::KArgs::Tile& 
     return true;
 }
 
+/* Keep the fixed-point count plane of the field in L2.  The deposits of a
+   single simulation hit the int64 counts and the float remainders of random
+   field elements with fire-and-forget reductions; when the planes together
+   approach L2's size (the cube + sphere workload's are 130 MB) the lines
+   thrash and the reductions write evicted lines back to DRAM (95 GB a
+   1e8-photon launch).  A persisting access-policy window on the session's
+   stream over the count plane (when it fits in the largest window the
+   device allows) keeps it in L2's persisting set-aside, which this
+   session raises to the device's maximum for its context; the remainders
+   and the streamed seeds and records share the rest.  Measured on the cube +
+   sphere workload: DRAM writes 95 GB -> 33 GB a launch, same kernel time. */
+void l2_window(mcxg_session* s, const mcxg_kparams& kp, bool on) {
+    int maxpersist = 0, maxwin = 0;
+    if (cudaDeviceGetAttribute(&maxpersist, cudaDevAttrMaxPersistingL2CacheSize, s->device) != cudaSuccess ||
+            cudaDeviceGetAttribute(&maxwin, cudaDevAttrMaxAccessPolicyWindowSize, s->device) != cudaSuccess) {
+        cudaGetLastError();
+        return;          /* no persisting L2 on this device: nothing to do */
+    }
+    /* only a count plane that fits in one window: a larger one (the head's 570 MB)
+       is mostly cold, and a window over its first gates took L2 from the hot
+       elements elsewhere (DRAM writes 0.6 GB -> 13 GB a launch) */
+    const size_t counts = sizeof(long long) * (size_t)kp.fieldlen * field_comps(kp);
+    const size_t nb = on && maxpersist > 0 && maxwin > 0 && counts <= (size_t)maxwin ? counts : 0;
+    const void* base = nb ? (const void*)s->d_field : nullptr;
+    if (base == s->l2_base && nb == s->l2_bytes) {
+        return;
+    }
+    if (nb && !s->l2_set) {
+        /* best effort: a context that refuses the set-aside runs without the window */
+        if (cudaDeviceGetLimit(&s->l2_prev, cudaLimitPersistingL2CacheSize) != cudaSuccess ||
+                cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)maxpersist) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        s->l2_set = true;
+    }
+    cudaStreamAttrValue v;
+    memset(&v, 0, sizeof(v));
+    if (nb) {
+        v.accessPolicyWindow.base_ptr = (void*)s->d_field;
+        v.accessPolicyWindow.num_bytes = nb;
+        v.accessPolicyWindow.hitRatio = std::min(1.f, (float)maxpersist / (float)nb);
+        v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    }
+    if (cudaStreamSetAttribute(s->st, cudaStreamAttributeAccessPolicyWindow, &v) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    s->l2_base = base;
+    s->l2_bytes = nb;
+    return;
+}
+
 }  // namespace
 
 extern "C" {
@@ -649,6 +705,13 @@ int mcxg_destroy(mcxg_session* s) {
     cudaSetDevice(s->device);
     if (s->st) {
         cudaStreamSynchronize(s->st);
+    }
+    if (s->l2_set) {
+        /* give the persisting set-aside back: no lines stay persisting, the
+           context's limit returns to what it was */
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, s->l2_prev);
+        cudaGetLastError();
     }
     void* bufs[] = {s->d_media, s->d_prop, s->d_tables, s->d_pattern, s->d_seeds, s->d_field, s->d_energy,
                     s->d_detp, s->d_detseed, s->d_words, s->d_events, s->d_red, s->d_out,
@@ -1002,8 +1065,8 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     a.srcpattern = s->d_pattern;
     a.seeds = s->d_seeds;
     a.field = s->d_field;
-    a.fcell = reinterpret_cast<uint2*>(s->d_field);
-    a.fcarry = reinterpret_cast<unsigned int*>(s->d_field + 2 * (size_t)kp.fieldlen * field_comps(kp));
+    a.fhi = reinterpret_cast<unsigned long long*>(s->d_field);
+    a.flo = s->d_field + 2 * (size_t)kp.fieldlen * field_comps(kp);
     a.smatrix = s->d_smatrix;
     a.s0 = s->pol_s0;
     a.maxpol = s->npol;
@@ -1134,6 +1197,7 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
         }
     }
 
+    l2_window(s, kp, !(flags & MCXG_NOL2WINDOW) && !adjmode);
     MCXG_TRY(cudaEventRecord(s->e0, s->st));
     if (flags & MCXG_RNGDUMP) {
         MCXG_TRY(mcxg::exact_rngdump(a, s->info.sm * 4, 256, s->st));
@@ -1474,21 +1538,13 @@ int mcxg_get_field_planes(mcxg_session* s, int64_t* counts, float* rem) {
     }
     MCXG_TRY(cudaSetDevice(s->device));
     const size_t total = (size_t)s->kp.fieldlen * field_comps(s->kp);
-    std::vector<uint32_t> cells(2 * total), hi(counts ? total : 0);
-    MCXG_TRY(cudaMemcpyAsync(cells.data(), s->d_field, sizeof(uint32_t) * 2 * total, cudaMemcpyDeviceToHost, s->st));
     if (counts) {
-        MCXG_TRY(cudaMemcpyAsync(hi.data(), s->d_field + 2 * total, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost,
-                                 s->st));
+        MCXG_TRY(cudaMemcpyAsync(counts, s->d_field, sizeof(int64_t) * total, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (rem) {
+        MCXG_TRY(cudaMemcpyAsync(rem, s->d_field + 2 * total, sizeof(float) * total, cudaMemcpyDeviceToHost, s->st));
     }
     MCXG_TRY(cudaStreamSynchronize(s->st));
-    for (size_t i = 0; i < total; i++) {
-        if (counts) {
-            counts[i] = (int64_t)(((uint64_t)hi[i] << 32) | cells[2 * i]);
-        }
-        if (rem) {
-            memcpy(rem + i, &cells[2 * i + 1], sizeof(float));
-        }
-    }
     return MCXG_OK;
 }
 
@@ -1654,8 +1710,8 @@ int batch_enqueue(mcxg_session* s, int lflags) {
     a.media8 = s->d_bmedia;
     a.media32 = (const uint32_t*)s->d_bmedia;
     a.field = s->d_bfield;
-    a.fcell = reinterpret_cast<uint2*>(s->d_bfield);
-    a.fcarry = reinterpret_cast<unsigned int*>(s->d_bfield + 2 * (size_t)s->totalfield);
+    a.fhi = reinterpret_cast<unsigned long long*>(s->d_bfield);
+    a.flo = s->d_bfield + 2 * (size_t)s->totalfield;
     a.energy = s->d_benergy;
     a.detcount = s->d_words + 0;
     a.vtcounter = s->d_words + 1;

@@ -832,40 +832,34 @@ __device__ void savedetphoton(const KArgs& a, const PS& ps, const Shared& S, Pho
 
 /* ---------------------------------------------------------------- deposit */
 
-/* Compensated accumulation: each field element holds a signed 64-bit
-   fixed-point count of 2^-S and a float remainder.  A deposit w is split
-   exactly into k = round(w 2^S) and r = w - k 2^-S (|r| <= 2^-(S+1)).
-   Integer adds are exact in any order -- also when the memory system merges
-   the adds of several lanes to one address -- so the bulk of an element
-   carries no rounding at all, and the remainders are too small for their
-   float rounding to matter: an element is count x 2^-S + remainder, summed
-   in FP64.  The host picks S per problem so that no element can reach 2^62
-   units (mcx_host.c, field_scale).  A float running sum, or float high and
-   low planes compensated by the value an atomic returns (TwoSum), loses the
-   low-order deposits of the hottest voxels at 1e8-1e9 photons.
-
-   Layout: per component, an 8-byte cell per element {low 32 bits of the
-   count, remainder} and a separate plane of the counts' high 32 bits.  A
-   deposit touches one cell -- one 32-byte sector for both adds -- and the
-   high word only when the low word wraps (the add's returned value says
-   when) or k itself reaches 2^32, so the working set the deposits keep in
-   L2 is 8 bytes an element. */
+/* Compensated accumulation: each field component is a plane of signed
+   64-bit fixed-point counts of 2^-S and a plane of float remainders.  A
+   deposit w is split exactly into k = round(w 2^S) and r = w - k 2^-S
+   (|r| <= 2^-(S+1)); k goes to the integer plane, r to the float plane, both
+   with fire-and-forget atomics.  Integer adds are exact in any order -- also
+   when the memory system merges the adds of several lanes to one address --
+   so the bulk of an element carries no rounding at all, and the remainders
+   are too small for the float plane's rounding to matter: an element is
+   count x 2^-S + remainder, summed in FP64.  The host picks S per problem so
+   that no element can reach 2^62 units (mcx_host.c, field_scale).  A float
+   running sum, or float high and low planes compensated by the value an
+   atomic returns (TwoSum), loses the low-order deposits of the hottest
+   voxels at 1e8-1e9 photons. */
 struct Field {
-    uint2* cell;                   /* {count bits 0-31, remainder as float bits} */
-    unsigned int* carry;           /* count bits 32-63 */
+    unsigned long long* hi;        /* fixed-point counts */
+    float* lo;                     /* remainders */
     float sc, unit;                /* 2^S, 2^-S */
 };
 
-/* component comp of the field (0 real, 1 imaginary); the cells of the
-   components follow one another, then their high words, plane length
-   ps.lo_plane() */
+/* component comp of the field (0 real, 1 imaginary); the planes of the
+   components follow one another, plane length ps.lo_plane() */
 template <class PS>
 __device__ __forceinline__ Field field_of(const KArgs& a, const PS& ps, unsigned int comp) {
     const mcxg_kparams& c_p = ps.p();
     const size_t F = ps.lo_plane();
     Field f;
-    f.cell = a.fcell + comp * F;
-    f.carry = a.fcarry + comp * F;
+    f.hi = a.fhi + comp * F;
+    f.lo = a.flo + comp * F;
     f.sc = c_p.fxscale;
     f.unit = c_p.fxunit;
     return f;
@@ -878,22 +872,12 @@ __device__ __forceinline__ void field_split(const Field& f, float w, long long& 
     r = __fsub_rn(w, __fmul_rn((float)k, f.unit));
 }
 
-/* count += k as two 32-bit words: the low word's carry-out (the returned
-   old value plus the added word wraps) and k's own high word go to the high
-   word, modulo 2^32 -- the 64-bit two's-complement sum, exact for negative
-   k too */
 __device__ __forceinline__ void field_commit(const Field& f, size_t i, long long k, float r) {
+    if (k) {
+        atomicAdd(f.hi + i, (unsigned long long)k);
+    }
     if (r != 0.f) {
-        atomicAdd((float*)&f.cell[i].y, r);
-    }
-    const unsigned int lo = (unsigned int)(unsigned long long)k;
-    unsigned int up = (unsigned int)((unsigned long long)k >> 32);
-    if (lo) {
-        const unsigned int old = atomicAdd(&f.cell[i].x, lo);
-        up += (old + lo < old) ? 1u : 0u;
-    }
-    if (up) {
-        atomicAdd(f.carry + i, up);
+        atomicAdd(f.lo + i, r);
     }
 }
 
@@ -904,62 +888,14 @@ __device__ __forceinline__ void field_add(const Field& f, size_t i, float w) {
     field_commit(f, i, k, r);
 }
 
-/* The transport loop's own deposits defer the carry test of the low-word
-   add to the lane's next deposit (or the end of its work), so the add's
-   returned value is read about one step after it was issued and its latency
-   is hidden: old value, added word and element of the add in flight. */
-struct PendingCarry {
-    unsigned int old, lo, idx;
-};
-
-__device__ __forceinline__ void carry_settle(const Field& f, PendingCarry& p) {
-    if (p.lo && p.old + p.lo < p.old) {
-        atomicAdd(f.carry + p.idx, 1u);
-    }
-    p.lo = 0u;
-}
-
-__device__ __forceinline__ void field_commit_deferred(const Field& f, unsigned int i, long long k, float r,
-                                                      PendingCarry& p) {
-    if (r != 0.f) {
-        atomicAdd((float*)&f.cell[i].y, r);
-    }
-    const unsigned int lo = (unsigned int)(unsigned long long)k;
-    const unsigned int up = (unsigned int)((unsigned long long)k >> 32);
-    if (up) {
-        atomicAdd(f.carry + i, up);
-    }
-    if (lo) {
-        carry_settle(f, p);
-        p.old = atomicAdd(&f.cell[i].x, lo);
-        p.lo = lo;
-        p.idx = i;
-    }
-}
-
-/* either commit: deferred carry test (DEFER) or an immediate one */
-template <bool DEFER>
-__device__ __forceinline__ void field_commit_as(const Field& f, unsigned int i, long long k, float r, PendingCarry& p) {
-    if (DEFER) {
-        field_commit_deferred(f, i, k, r, p);
-    } else {
-        field_commit(f, i, k, r);
-    }
-}
-
 /* Deposit from every lane that has one; with WAGG, lanes of the warp hitting
    the same field element add their integer parts (exactly) and their
-   remainders first and one leader commits.  DEFER: the carry test waits for
-   the lane's next deposit (three registers the register-capped specialised
-   instantiations -- RF, polarised, split voxels -- do not have to spare). */
-template <bool WAGG, bool DEFER>
-__device__ __forceinline__ void deposit(const Field& f, bool doit, unsigned int key, float w, PendingCarry& p) {
+   remainders first and one leader commits. */
+template <bool WAGG>
+__device__ __forceinline__ void deposit(const Field& f, bool doit, unsigned int key, float w) {
     if (!WAGG) {
         if (doit) {
-            long long k;
-            float r;
-            field_split(f, w, k, r);
-            field_commit_as<DEFER>(f, key, k, r, p);
+            field_add(f, key, w);
         }
         return;
     }
@@ -974,7 +910,7 @@ __device__ __forceinline__ void deposit(const Field& f, bool doit, unsigned int 
     unsigned int peers = __match_any_sync(m, key);
     unsigned int lane = threadIdx.x & 31u;
     if (peers == (1u << lane)) {
-        field_commit_as<DEFER>(f, key, k, r, p);
+        field_commit(f, key, k, r);
         return;
     }
     long long ksum = 0;
@@ -987,7 +923,7 @@ __device__ __forceinline__ void deposit(const Field& f, bool doit, unsigned int 
         rsum += __shfl_sync(peers, r, src);
     }
     if ((int)lane == __ffs(peers) - 1) {
-        field_commit_as<DEFER>(f, key, ksum, rsum, p);
+        field_commit(f, key, ksum, rsum);
     }
 }
 
@@ -1786,7 +1722,6 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
     bool vdirty = true;
     bool testint = false, hitintf = false;    /* split voxels: test the plane this step / the step ended on it */
     float adjJ = 0.f, adjP = 0.f;             /* fluence gradient: the photon's loss total and its running part */
-    PendingCarry pend = {0u, 0u, 0u};         /* the carry test of this lane's last deposit */
     if (TILE) {
         /* the hot-voxel tile starts empty in every block */
         unsigned long long* tc = tile_counts(a);
@@ -2163,7 +2098,7 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
                     share_deposit(a, ps, key, weight);
                 }
             } else {
-                deposit<WAGG, !(RF || POL || SVMC)>(field_of(a, ps, 0), dep, ps.field_off() + key, weight, pend);
+                deposit<WAGG>(field_of(a, ps, 0), dep, ps.field_off() + key, weight);
                 if (ACC64 && dep) {
                     acc_verify(a, ps.lo_plane(), ps.field_off() + key, weight);
                 }
@@ -2345,8 +2280,6 @@ __global__ void __launch_bounds__(256, MINB) mcx_transport(const KArgs a) {
         }
     }
 
-    carry_settle(field_of(a, ps, 0), pend);
-
     if (TILE) {
         /* the block's tile into the field: one pair of atomics per touched element */
         __syncthreads();
@@ -2394,7 +2327,7 @@ __global__ void mcx_rng_dump(const KArgs a) {
         t.a = (unsigned long long)sd.x << 32 | sd.y;
         t.b = (unsigned long long)sd.z << 32 | sd.w;
         for (unsigned int j = vt; j < c_p.fieldlen; j += c_p.nthread) {
-            reinterpret_cast<float*>(a.fcell)[2 * (size_t)j + 1] = rnd(t);   /* the remainder word */
+            a.flo[j] = rnd(t);
         }
     }
 }

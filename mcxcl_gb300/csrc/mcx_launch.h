@@ -21,11 +21,11 @@ struct KArgs {
     const float* angleinvcdf;
     const float* srcpattern;
     const uint4* seeds;            /* 4 x 32-bit seed words per reference thread */
-    float* field;                  /* the field buffer: 8-byte cells {count bits 0-31, float remainder}
-                                      (comps x fieldlen), then the counts' bits 32-63 (comps x fieldlen
-                                      uint32); raw float scratch for the fluence-gradient passes */
-    uint2* fcell;                  /* cells of component c at fcell + c x plane length */
-    unsigned int* fcarry;          /* high count words of component c at fcarry + c x plane length */
+    float* field;                  /* the field buffer: fixed-point planes (comps x fieldlen int64), then
+                                      remainder planes (comps x fieldlen float); raw float scratch for
+                                      the fluence-gradient passes */
+    unsigned long long* fhi;       /* fixed-point counts of component c at fhi + c x plane length */
+    float* flo;                    /* float remainders of component c at flo + c x plane length */
     float2* energy;                /* per reference thread: escaped, launched weight */
     float* detp;                   /* maxdetphoton x reclen */
     unsigned long long* detseed;   /* maxdetphoton x 2 */
