@@ -1360,7 +1360,9 @@ static void run_simulation(Config* cfg) {
         MCX_ERROR(-6, "replay inputs are missing: call mcx_validatecfg with the baseline records first");
     }
     size_t fieldlen = nvox * cfg->maxgate * mult;
-    if (fieldlen > 0xFFFFFFFFull || nvox > 0x7FFFFFFFull) {
+    /* the kernel forms index + gate x nvox in 32 bits, one gate past the end
+       included (a time of flight a rounding below the window's end) */
+    if (fieldlen + nvox > 0xFFFFFFFFull || nvox > 0x7FFFFFFFull) {
         MCX_ERROR(-1, "volume x gates too large for 32-bit field indices");
     }
 

@@ -146,6 +146,12 @@ VARIANTS = {
     "cyclic": dict(bc="ccrrcc", isreflect=0),
     "facedet": dict(bc="aaaaaa001000", isreflect=0),
     "roulette": dict(minenergy=0.01),
+    # edge cases: fewer photons than reference threads (every thread but the
+    # first `oddphoton` runs none), and a one-voxel domain with a detector over
+    # its face (the detector mask's single-voxel radius rule, mcx_utils.c:4141)
+    "fewphotons": dict(nphoton=100),
+    "onevoxel": dict(vol=np.ones((1, 1, 1), np.uint8), srcpos=[0.5, 0.5, 0], detpos=[[0.5, 0.5, 0, 1]],
+                     nphoton=500),
     "unitinmm": dict(unitinmm=0.5),
     "gscatter": dict(gscatter=3),
     "outside_src_specular": dict(srcpos=[20, 20, -5], isspecular=1),
@@ -192,6 +198,13 @@ VARIANTS.update({
                     savedetflag="dxvw"),
 })
 NOT_PINNED = {"muafloat", "asf2h", "labelhalf", "asgnbyte", "asshort", "svmc_topdet"}
+# Cases where a photon can leave the domain on the step right after a Fresnel
+# reflection at the domain boundary: the reference then has lost the voxel's
+# detector bit (its isdet still holds the face's boundary code, mcx_core.cl:2796,
+# 3212) and does not record the photon; the oracle and the product do.  The
+# pins hold the reference's records there, which must be a subset of the
+# oracle's; energies and field are bit-identical.
+DETECT_AFTER_REFLECT = {"onevoxel"}
 
 
 def variant(name, **kw):

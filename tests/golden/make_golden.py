@@ -64,6 +64,9 @@ def main():
     for name, cfg, nthread in cases.pin_cases():
         r = oracle.run_reference(cfg, nthread=nthread, core=nthread)
         out[name] = dict(summarize(r), nthread=nthread)
+        if name in cases.DETECT_AFTER_REFLECT:
+            # the records themselves (float bits), for the subset check
+            out[name]["detp_bits"] = np.asarray(r["detp"], np.float32).T.view(np.uint32).tolist()
         print(name, out[name]["ndet"], out[name]["energy_tot"])
     # polarised transport: Mueller rows and properties from the reference's own Mie
     # routine, stored with the pin (the oracle takes them as inputs)

@@ -58,7 +58,8 @@ EXACT_CASES = ["pencil_gates", "isotropic", "cone", "gaussian", "planar", "fouri
                "pattern", "pattern3d", "focus", "lambert", "noreflect", "cyclic", "facedet", "roulette",
                "unitinmm", "gscatter", "outside_src_specular", "multisrc", "multisrc_id", "energy_out",
                "fluence_out", "invcdf", "angleinvcdf", "muafloat", "asf2h", "labelhalf", "asgnbyte", "asshort",
-               "pattern_share", "pattern3d_share", "rf_forward", "rf_roulette", "svmc", "svmc_topdet", "svmc_refl"]
+               "pattern_share", "pattern3d_share", "rf_forward", "rf_roulette", "svmc", "svmc_topdet", "svmc_refl",
+               "fewphotons", "onevoxel"]
 
 
 @pytest.mark.parametrize("name", EXACT_CASES)
