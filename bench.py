@@ -391,10 +391,25 @@ def read_traffic(k):
     return None
 
 
+def hbm_peak():
+    """The measured copy bandwidth of the GB300s (GB/s) and its source."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback (6.8 TB/s, one earlier GB300 measurement)"
+
+
 def roofline(per, ops, kms, nphoton, peak, k, sample):
     achieved = ops * nphoton / (kms * 1e-3) / 1e9
+    traffic = read_traffic(k)
+    hbm, hbm_src = hbm_peak()
+    dram = traffic / (kms * 1e-3) / 1e9 if traffic else None
     return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "Gop/s",
-            "frac": achieved / peak if peak else None, "traffic": read_traffic(k),
+            "frac": achieved / peak if peak else None, "traffic": traffic,
+            "dram": {"achieved": dram, "peak": hbm, "unit": "GB/s", "frac": dram / hbm if dram else None,
+                     "peak_source": hbm_src,
+                     "note": "DRAM bytes of one full launch (traffic) over this run's kernel time: not the bound"},
             "traffic_from": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one full launch, "
                             "profiles/traffic_mcx_transport_config%d.txt" % k,
             "peak_source": "measured in this run: 8-chain FMA kernel, one FMA = one op",
