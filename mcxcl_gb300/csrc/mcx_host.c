@@ -1965,15 +1965,18 @@ static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, uns
     for (int k = 0; k < n; k++) {
         Config* cfg = cfgs[k];
         size_t len = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z * cfg->maxgate;
+        const float* src = bfield + bdesc[k].field_off;
         if (!cfg->exportfield) {
-            cfg->exportfield = (float*)calloc(len, sizeof(float));
+            cfg->exportfield = (float*)malloc(len * sizeof(float));
             if (!cfg->exportfield) {
                 MCX_ERROR(-2, "out of host memory");
             }
-        }
-        const float* src = bfield + bdesc[k].field_off;
-        for (size_t i = 0; i < len; i++) {
-            cfg->exportfield[i] += src[i];
+            memcpy(cfg->exportfield, src, len * sizeof(float));
+        } else {
+            /* a caller's buffer accumulates, as a respin of mcx_run_simulation does */
+            for (size_t i = 0; i < len; i++) {
+                cfg->exportfield[i] += src[i];
+            }
         }
     }
     for (int i = 0; i < 7; i++) {
