@@ -639,7 +639,7 @@ int mcxg_device_info(int device, mcxg_devinfo* info) {
     cudaDeviceProp p;
     MCXG_TRY(cudaGetDeviceProperties(&p, device));
     memset(info, 0, sizeof(*info));
-    strncpy(info->name, p.name, sizeof(info->name) - 1);
+    snprintf(info->name, sizeof(info->name), "%s", p.name);
     info->major = p.major;
     info->minor = p.minor;
     info->sm = p.multiProcessorCount;

@@ -620,7 +620,7 @@ static void replayinit(Config* cfg, const float* detps, const int dimdetps[2], i
         if (!(cfg->replaydet <= 0 || cfg->replaydet == (did & 0xFFFF))) {
             continue;
         }
-        if (!(cfg->srcid <= 0 || ((did & 0xFFFF0000) && cfg->srcid == ((did & 0xFFFF0000) >> 16)))) {
+        if (!(cfg->srcid <= 0 || ((did & 0xFFFF0000) && cfg->srcid == (int)(((unsigned int)did & 0xFFFF0000u) >> 16)))) {
             continue;
         }
         if (i != kept) {
@@ -853,7 +853,7 @@ int mcx_list_gpu(Config* cfg, unsigned int* activedev, GPUInfo** info) {
         }
         GPUInfo* g = (*info) + act;
         memset(g, 0, sizeof(*g));
-        strncpy(g->name, d.name, MAX_SESSION_LENGTH - 1);
+        snprintf(g->name, sizeof(g->name), "%s", d.name);
         g->id = i + 1;
         g->devcount = n;
         g->major = d.major;

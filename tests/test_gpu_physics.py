@@ -12,7 +12,6 @@
 import numpy as np
 import pytest
 
-import cases
 from mcxcl_gb300 import workloads
 
 pytestmark = pytest.mark.gpu

@@ -6,7 +6,6 @@ import os
 import struct
 
 import numpy as np
-import pytest
 
 import cases
 from mcxcl_gb300 import io
