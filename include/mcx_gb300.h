@@ -324,7 +324,11 @@ void mcx_release_sessions(void);
    outlives a call, as with the reference's mcx_run_simulation
    (src/mcx_host.cpp, which frees every buffer before it returns).
    A session returned by mcx_prepare_simulation stays usable until the next
-   mcx_run_simulation, mcx_run_batch or mcx_release_sessions. */
+   mcx_run_simulation, mcx_run_batch or mcx_release_sessions.  These calls
+   share the cached sessions across host threads and hold one process-wide
+   lock while they run, so calls from several threads run one at a time; the
+   device-layer mcxg_* calls on a session take no lock (one thread a
+   session). */
 void mcx_keep_sessions(int keep);
 
 /* ---- thin device layer ------------------------------------------------------ */

@@ -17,6 +17,7 @@
  */
 #define _GNU_SOURCE
 #include <math.h>
+#include <pthread.h>
 #include <setjmp.h>
 #include <stdarg.h>
 #include <stdint.h>
@@ -944,13 +945,24 @@ static uint64_t tune_signature(const Config* cfg, const mcxg_kparams* kp) {
     return h;
 }
 
-void mcx_release_sessions(void) {
+/* The cached sessions are shared by every host thread of the process: the
+   public entry points that use or release them hold this lock, so calls from
+   several threads run one after another instead of sharing device buffers. */
+static pthread_mutex_t g_run_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static void release_sessions(void) {
     for (int i = 0; i < MAX_DEVICE; i++) {
         if (g_sessions[i]) {
             mcxg_destroy(g_sessions[i]);
             g_sessions[i] = NULL;
         }
     }
+}
+
+void mcx_release_sessions(void) {
+    pthread_mutex_lock(&g_run_lock);
+    release_sessions();
+    pthread_mutex_unlock(&g_run_lock);
 }
 
 static void device_check(int rc, const char* what) {
@@ -1998,41 +2010,52 @@ static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, uns
 static int g_keep_sessions = 1;
 
 void mcx_keep_sessions(int keep) {
+    pthread_mutex_lock(&g_run_lock);
     g_keep_sessions = keep != 0;
     if (!g_keep_sessions) {
-        mcx_release_sessions();
+        release_sessions();
     }
+    pthread_mutex_unlock(&g_run_lock);
 }
 
 void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     (void)fluence;
     (void)totalenergy;
-    run_simulation(cfg);
+    pthread_mutex_lock(&g_run_lock);
+    run_simulation(cfg);         /* library-mode errors return here through its own setjmp */
     if (!g_keep_sessions) {
-        mcx_release_sessions();
+        release_sessions();
     }
+    pthread_mutex_unlock(&g_run_lock);
 }
 
 void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsigned int flags) {
+    pthread_mutex_lock(&g_run_lock);
     batch_run(cfgs, n, photons_per_thread, flags, NULL);
     if (!g_keep_sessions) {
-        mcx_release_sessions();
+        release_sessions();
     }
+    pthread_mutex_unlock(&g_run_lock);
 }
 
 void mcx_run_batch_verify(Config** cfgs, int n, unsigned int photons_per_thread, double* relerr) {
+    pthread_mutex_lock(&g_run_lock);
     batch_run(cfgs, n, photons_per_thread, 0u, relerr);
     if (!g_keep_sessions) {
-        mcx_release_sessions();
+        release_sessions();
     }
+    pthread_mutex_unlock(&g_run_lock);
 }
 
 mcxg_session* mcx_prepare_simulation(Config* cfg) {
+    pthread_mutex_lock(&g_run_lock);
     prepare_only = 1;
     prepared_session = NULL;
     run_simulation(cfg);
     prepare_only = 0;
-    return cfg->errorcode ? NULL : prepared_session;
+    mcxg_session* s = cfg->errorcode ? NULL : prepared_session;
+    pthread_mutex_unlock(&g_run_lock);
+    return s;
 }
 
 /* ---- layout introspection, so foreign-function mirrors of Config can be checked */

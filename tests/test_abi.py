@@ -282,3 +282,30 @@ def test_mie_matches_the_reference_routine(lib, oracle_mod):
         b, qb, gb = _mie(lib, x, m)
         assert abs(qa / qb - 1) < 1e-6 and abs(ga - gb) < 1e-6
         assert np.all(np.abs(a - b) <= 5e-6 * np.abs(a[:, :1]) + 1e-30), (x, m)
+
+
+@pytest.mark.timeout(120)
+def test_run_lock_released_on_error_paths(lib):
+    """Without a usable device, run() fails in library mode; the lock that
+    serialises runs across host threads is released on that path (a second
+    call, and one from another thread, fail the same way instead of
+    waiting)."""
+    import threading
+
+    import mcxcl_gb300
+    if mcxcl_gb300.gpuinfo():
+        pytest.skip("a device is visible: the error path is not taken")
+    cfg = dict(nphoton=1000, vol=np.ones((4, 4, 4), np.uint8), prop=[[0, 0, 1, 1], [0.01, 1, 0.5, 1.37]],
+               srcpos=[2, 2, 0], srcdir=[0, 0, 1], tstart=0, tend=5e-9, tstep=5e-9)
+    errors = []
+
+    def call():
+        try:
+            mcxcl_gb300.run(cfg)
+        except mcxcl_gb300.MCXError as e:
+            errors.append(str(e))
+    call()
+    t = threading.Thread(target=call)
+    t.start()
+    t.join(60)
+    assert not t.is_alive() and len(errors) == 2

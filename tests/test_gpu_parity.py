@@ -413,3 +413,27 @@ def test_sessions_released_when_not_kept(gpu):
         np.testing.assert_allclose(a["flux"], b["flux"], rtol=1e-6, atol=0)
     finally:
         mcxcl_gb300.keep_sessions(True)
+
+
+def test_concurrent_runs_from_two_threads(gpu):
+    """run() from two host threads at once (ctypes releases the interpreter
+    lock during the call): the library serialises the calls on its shared
+    device session, so each thread gets what it gets alone."""
+    import threading
+
+    import mcxcl_gb300
+    cfgs = [cases.cube60(nphoton=300000, seed=11, tstep=5e-10), cases.cube60(nphoton=300000, seed=12, isreflect=1)]
+    alone = [mcxcl_gb300.run(c) for c in cfgs]
+    out = [None, None]
+
+    def work(i):
+        out[i] = mcxcl_gb300.run(cfgs[i])
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for a, b in zip(alone, out):
+        assert b is not None
+        assert a["stat"]["energyabs"] == b["stat"]["energyabs"]
+        np.testing.assert_allclose(a["flux"], b["flux"], rtol=1e-6, atol=0)
