@@ -261,7 +261,9 @@ int  mcx_list_gpu(Config* cfg, unsigned int* activedev, GPUInfo** info);
 void mcx_cleargpuinfo(GPUInfo** info);
 /* Runs the simulation (src/mcx_host.h:168); fluence and totalenergy are unused,
    as in the reference.  Outputs go to cfg: exportfield, exportdetected,
-   seeddata, detectedcount, energytot/energyesc/energyabs, normalizer, runtime. */
+   seeddata, detectedcount, energytot/energyesc/energyabs, normalizer, runtime.
+   The calling thread's current CUDA device is the same on return as before
+   (the run itself uses the device cfg selects). */
 void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy);
 /* Writes detected photons as <session>.mch: the History header, count records
    of his.colcount floats, then the seeds (src/mcx_utils.c:963-998). */

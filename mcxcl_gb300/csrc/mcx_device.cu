@@ -618,6 +618,24 @@ const char* mcxg_error_string(int code) {
     }
 }
 
+/* the calling thread's current device, and setting it back: the host
+   driver restores the caller's device when a public call returns
+   (internal to the library, not in the public header) */
+int mcxg_internal_current_device(void) {
+    int d = -1;
+    if (cudaGetDevice(&d) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return d;
+}
+
+void mcxg_internal_restore_device(int d) {
+    if (d >= 0 && cudaSetDevice(d) != cudaSuccess) {
+        cudaGetLastError();
+    }
+}
+
 int mcxg_device_count(int* n) {
     if (!n) {
         return MCXG_ERR_ARG;

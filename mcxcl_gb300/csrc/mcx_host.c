@@ -950,6 +950,11 @@ static uint64_t tune_signature(const Config* cfg, const mcxg_kparams* kp) {
    several threads run one after another instead of sharing device buffers. */
 static pthread_mutex_t g_run_lock = PTHREAD_MUTEX_INITIALIZER;
 
+/* the device layer switches the thread's current CUDA device to the one it
+   runs on; the public calls put the caller's back (mcx_device.cu) */
+int mcxg_internal_current_device(void);
+void mcxg_internal_restore_device(int d);
+
 static void release_sessions(void) {
     for (int i = 0; i < MAX_DEVICE; i++) {
         if (g_sessions[i]) {
@@ -2022,28 +2027,34 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy) {
     (void)fluence;
     (void)totalenergy;
     pthread_mutex_lock(&g_run_lock);
+    const int dev = mcxg_internal_current_device();
     run_simulation(cfg);         /* library-mode errors return here through its own setjmp */
     if (!g_keep_sessions) {
         release_sessions();
     }
+    mcxg_internal_restore_device(dev);
     pthread_mutex_unlock(&g_run_lock);
 }
 
 void mcx_run_batch(Config** cfgs, int n, unsigned int photons_per_thread, unsigned int flags) {
     pthread_mutex_lock(&g_run_lock);
+    const int dev = mcxg_internal_current_device();
     batch_run(cfgs, n, photons_per_thread, flags, NULL);
     if (!g_keep_sessions) {
         release_sessions();
     }
+    mcxg_internal_restore_device(dev);
     pthread_mutex_unlock(&g_run_lock);
 }
 
 void mcx_run_batch_verify(Config** cfgs, int n, unsigned int photons_per_thread, double* relerr) {
     pthread_mutex_lock(&g_run_lock);
+    const int dev = mcxg_internal_current_device();
     batch_run(cfgs, n, photons_per_thread, 0u, relerr);
     if (!g_keep_sessions) {
         release_sessions();
     }
+    mcxg_internal_restore_device(dev);
     pthread_mutex_unlock(&g_run_lock);
 }
 

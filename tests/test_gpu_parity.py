@@ -437,3 +437,15 @@ def test_concurrent_runs_from_two_threads(gpu):
         assert b is not None
         assert a["stat"]["energyabs"] == b["stat"]["energyabs"]
         np.testing.assert_allclose(a["flux"], b["flux"], rtol=1e-6, atol=0)
+
+
+def test_run_keeps_the_callers_current_device(gpu):
+    """mcx_run_simulation switches to the device it runs on and puts the
+    caller's current device back (checked through torch, which reads the
+    same runtime state)."""
+    import torch
+
+    import mcxcl_gb300
+    before = torch.cuda.current_device()
+    mcxcl_gb300.run(cases.cube60(nphoton=20000))
+    assert torch.cuda.current_device() == before
