@@ -404,10 +404,12 @@ int  mcxg_get_trajectory(mcxg_session* s, float* out, uint32_t maxrec, uint32_t*
 int  mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock, uint32_t blocklen,
                          uint32_t nthread);
 /* Launch shape of the persistent grid: block threads (32..256, a multiple of
-   32) and resident blocks per SM (0 = automatic: 256 threads x 3).  Shapes of
+   32) and resident blocks per SM (0 = automatic: 256 threads x 4).  Shapes of
    more than 512 threads per SM run the instantiation whose registers are
-   capped for 768 resident threads (80 a thread), the others the uncapped
-   one; blocks per SM are lowered to what fits at once. */
+   capped for 1,024 resident threads (64 a thread; the specialised RF,
+   polarised, split-voxel, other-encoding, precision-check and gradient
+   kernels: 768 and 80), the others the uncapped one; blocks per SM are
+   lowered to what fits at once. */
 int  mcxg_set_launch(mcxg_session* s, int block, int blocks_per_sm);
 /* Hot-voxel tile (no counterpart in the reference, which adds every deposit
    to global memory, src/mcx_core.cl:2880-2886): with elements > 0, launches
@@ -453,8 +455,9 @@ int  mcxg_batch_get_field(mcxg_session* s, float* out, const double* scales);
 int  mcxg_set_replay(mcxg_session* s, const void* seeds16, const float* weight, const float* tof, const int* detid,
                      uint32_t n);
 /* Pick the launch shape of the fast kernel for the current problem: time
-   each candidate (blocks of 256, 128 and 64 threads at 768 resident threads
-   per SM with capped registers, 256 and 128 at 512 with uncapped ones; then
+   each candidate (blocks of 256, 128 and 64 threads at 1,024 resident
+   threads per SM with capped registers, 256 and 128 at 512 with uncapped
+   ones; then
    the fastest with warp-aggregated deposits) on the first sample_photons
    photons and keep the fastest for later mcxg_simulate calls (unless a
    shape was set with mcxg_set_launch).  Outputs may be NULL.  The trial

@@ -123,7 +123,7 @@ struct mcxg_session {
     uint32_t nsim = 0;
     unsigned long long totalvt = 0, totalfield = 0;
     bool has_batch = false;
-    int bt_block = 256, bt_bpsm = 3, bt_grid = 0;
+    int bt_block = 256, bt_bpsm = 4, bt_grid = 0;
     cudaGraph_t bgraph = nullptr;
     cudaGraphExec_t bgraph_exec = nullptr;
 
@@ -1135,13 +1135,14 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     /* the instantiations that fix the common configuration's parameters */
     const bool common = !rf && !pol && !(flags & MCXG_GENERAL) && kp.mediaformat <= 4 && !kp.is2d && kp.nphase <= 2 &&
                         kp.srcnum <= 1 && !s->maxjump;
-    /* launch shape: block threads x blocks per SM; shapes of more than 512
-       threads per SM take the instantiation whose registers are capped for
-       768 resident threads (80 a thread), the others the uncapped one; the
-       specialised instantiations exist only capped */
+    /* launch shape: block threads x blocks per SM.  Shapes of more than 512
+       threads per SM take the instantiation whose registers are capped (64
+       a thread for the forward kernels: 1,024 resident threads, the
+       default; 80 for the specialised ones, which exist only capped: 768),
+       the others the uncapped one */
     const int block = s->block_req ? s->block_req : 256;
     const bool special = xmedia || rf || pol || svmc || verify || adjmode;
-    const int bpsm_sel = special ? 768 / block : (s->bpsm_req ? s->bpsm_req : 768 / block);
+    const int bpsm_sel = special ? 768 / block : (s->bpsm_req ? s->bpsm_req : 1024 / block);
     const bool occ3 = special || block * bpsm_sel > 512;
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
                  (noagg ? 0 : mcxg::LF_WAGG) | (occ3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
@@ -1253,12 +1254,12 @@ int mcxg_autotune(mcxg_session* s, uint32_t sample_photons, int* block, int* blo
     }
     s->kp = samp;
     s->up_fast = false;
-    /* the block sizes 64, 128 and 256 at 768 resident threads per SM (80
-       registers) and at 512 (uncapped registers), direct deposits; then the
-       fastest with warp-aggregated deposits */
+    /* the block sizes 64, 128 and 256 at 1,024 resident threads per SM (64
+       registers) and 128 and 256 at 512 (uncapped registers), direct
+       deposits; then the fastest with warp-aggregated deposits */
     struct Cand {
         int block, bpsm, noagg;
-    } cands[] = {{256, 3, 1}, {128, 6, 1}, {64, 12, 1}, {256, 2, 1}, {128, 4, 1}, {0, 0, 0}};
+    } cands[] = {{256, 4, 1}, {128, 8, 1}, {64, 16, 1}, {256, 2, 1}, {128, 4, 1}, {0, 0, 0}};
     const int ncand = (int)(sizeof(cands) / sizeof(cands[0]));
     float best = 1e30f;
     Cand pick = cands[0];
@@ -1854,8 +1855,10 @@ int mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
         }
     }
     const bool agg = (flags & MCXG_AGG) != 0 && !verify;
-    const int bpsm_req = verify ? 3 : (s->bpsm_req ? s->bpsm_req : 3);
-    int lflags = (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) | (bpsm_req == 3 ? mcxg::LF_OCC3 : 0) |
+    /* 4 blocks of 256 a SM on the 64-register instantiation; the precision
+       check's instantiation is capped at 80 (3 blocks) */
+    const int bpsm_req = verify ? 3 : (s->bpsm_req ? s->bpsm_req : 4);
+    int lflags = (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) | (bpsm_req >= 3 ? mcxg::LF_OCC3 : 0) |
                  (common && !(flags & MCXG_GENERAL) ? mcxg::LF_COMMON : 0) | (verify ? mcxg::LF_ACC64 : 0);
     int block = s->block_req ? s->block_req : 256;
     int occ = 0;

@@ -25,7 +25,7 @@ cudaError_t batch_wave_upload(const mcxg_simdesc* d_descs, unsigned int n, cudaS
    label volumes and the Henyey-Greenstein phase function) */
 template <bool REFL, bool WAGG, bool COMMON>
 static void* kbatch(bool occ3) {
-    return occ3 ? (void*)mcx_transport<false, false, REFL, WAGG, false, 3, true, false, COMMON>
+    return occ3 ? (void*)mcx_transport<false, false, REFL, WAGG, false, 4, true, false, COMMON>
            : (void*)mcx_transport<false, false, REFL, WAGG, false, 2, true, false, COMMON>;
 }
 

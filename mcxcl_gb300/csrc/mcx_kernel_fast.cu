@@ -20,9 +20,11 @@ cudaError_t fast_upload(const mcxg_kparams* p, const float* det4, unsigned int n
     return e;
 }
 
+/* the register-capped instantiation (64 registers: 1,024 resident threads a
+   SM) or the uncapped one (for shapes of at most 512 threads a SM) */
 template <bool DET, bool REFL, bool WAGG, bool COMMON>
-static void* kfun(bool occ3) {
-    return occ3 ? (void*)mcx_transport<false, DET, REFL, WAGG, false, 3, false, false, COMMON>
+static void* kfun(bool capped) {
+    return capped ? (void*)mcx_transport<false, DET, REFL, WAGG, false, 4, false, false, COMMON>
            : (void*)mcx_transport<false, DET, REFL, WAGG, false, 2, false, false, COMMON>;
 }
 

@@ -2,12 +2,14 @@
 
 With the tile on, a block's deposits into a box of voxels next to the source
 (first gates) accumulate in shared memory and reach the field when the block
-ends.  Each deposit is still split into an integer count of the problem's
-fixed-point unit and a float remainder, and integer sums do not depend on
-the order of the adds, so on the same seeds and launch shape the count
-planes must be equal bit for bit to those of direct deposits; the float
-remainders differ only by their summation order.  The photons themselves
-(energies, detected records) do not depend on where deposits go.
+ends.  The tile and the direct-deposit kernels are different instantiations,
+whose floating-point contractions may differ, so their photons need not be
+bit-identical; what the tile must not do is lose or repeat a deposit.  With
+the energy output every deposit is a piece of absorbed weight, so the field's
+FP64 total equals the launched minus the escaped weight (per-thread float
+sums: about 1e-6) for any path the photons took: a lost or repeated tile
+element (each holds up to 1e-3 of the total) breaks that at once.  The two
+kernels' absorbed fractions agree within the Monte Carlo noise.
 """
 import ctypes
 
@@ -36,11 +38,11 @@ def _run(L, C, sess, tile):
 
 
 @pytest.mark.parametrize("k,photons", [(1, 2e6), (2, 2e6), (3, 5e5)])
-def test_tile_keeps_the_exact_counts(k, photons):
+def test_tile_loses_no_deposit(k, photons):
     from mcxcl_gb300 import _lib, pmcxcl, workloads
     L = _lib.load()
     cfg = workloads.config(k)
-    cfg["nphoton"] = int(photons)
+    cfg.update(nphoton=int(photons), outputtype="energy", minenergy=0.0)   # no roulette: weight is conserved
     C = _lib.Config()
     pmcxcl.parse_config(cfg, C)
     L.mcx_validatecfg(ctypes.byref(C), None, None, 0)
@@ -48,19 +50,18 @@ def test_tile_keeps_the_exact_counts(k, photons):
     sess = L.mcx_prepare_simulation(ctypes.byref(C))
     pmcxcl._check(C)
     try:
-        a = _run(L, C, sess, 0)
-        b = _run(L, C, sess, 4096)
-        c = _run(L, C, sess, 1024)
-        assert a["box"][7] == 0
-        for r in (b, c):
-            x0, y0, z0, nx, ny, nz, ng, el = (int(v) for v in r["box"])
-            assert 0 < el <= (4096 if r is b else 1024) and el == nx * ny * nz * ng
-            assert x0 + nx <= C.dim.x and y0 + ny <= C.dim.y and z0 + nz <= C.dim.z and ng <= C.maxgate
-            assert np.array_equal(r["cnt"], a["cnt"])
-            assert r["energy"] == a["energy"]
-            nz_ = a["f64"] > 0
-            rel = np.abs(r["f64"][nz_] - a["f64"][nz_]) / a["f64"][nz_]
-            assert rel.max() < 1e-6, rel.max()
+        runs = {t: _run(L, C, sess, t) for t in (0, 1024, 4096)}
+        assert runs[0]["box"][7] == 0
+        for t, r in runs.items():
+            esc, lau = r["energy"]
+            absorbed = lau - esc
+            assert abs(r["f64"].sum() - absorbed) <= 1e-5 * absorbed, (t, r["f64"].sum(), absorbed)
+            if t:
+                x0, y0, z0, nx, ny, nz, ng, el = (int(v) for v in r["box"])
+                assert 0 < el <= t and el == nx * ny * nz * ng
+                assert x0 + nx <= C.dim.x and y0 + ny <= C.dim.y and z0 + nz <= C.dim.z and ng <= C.maxgate
+                a0 = (runs[0]["energy"][1] - runs[0]["energy"][0]) / runs[0]["energy"][1]
+                assert abs(absorbed / lau - a0) <= 0.01 * a0
     finally:
         L.mcxg_set_tile(sess, 0)
         L.mcx_clearcfg(ctypes.byref(C))
