@@ -44,6 +44,16 @@ def _replay_threads(n):
     return dict(autopilot=0, nthread=max(64, -(-int(n) // 64) * 64), nblocksize=64)
 
 
+def _window_tof(cfg, tof):
+    """Detection times for a replay, inside the time window: a photon that
+    leaves through a detector on the step that also passes the window's end
+    is recorded with a time beyond it (as the reference records it); its
+    replay deposits into the last gate."""
+    t0 = np.float32(cfg.get("tstart", 0.0))
+    t1 = np.nextafter(np.float32(cfg.get("tend", 5e-9)), np.float32(0))
+    return np.clip(np.asarray(tof, np.float32), t0, t1)
+
+
 class ReplayGradient:
     """One differentiable simulation setup: everything but the mua volume
     (and optionally the scattering coefficient of label 1) is fixed.  The
@@ -76,7 +86,7 @@ class ReplayGradient:
         if "detp" in res:
             detid = res["detp"][0].astype(np.int64) & 0xFFFF
             w = res["detweight"][0].astype(np.float64)
-            tof = res["detweight"][1].astype(np.float32)
+            tof = _window_tof(self.cfg, res["detweight"][1])
             seeds = res["seeds"]
         else:
             detid = np.zeros(0, np.int64)
@@ -161,7 +171,7 @@ class LabelReadings:
             nscat = np.ascontiguousarray(d[1:1 + m]).view(np.uint32).astype(np.float64)
             ppath = d[1 + m:1 + 2 * m].astype(np.float64)
             w = res["detweight"][0].astype(np.float64)
-            tof = res["detweight"][1].astype(np.float32)
+            tof = _window_tof(self.cfg, res["detweight"][1])
             seeds = res["seeds"]
         else:
             detid = np.zeros(0, np.int64)
