@@ -301,8 +301,8 @@ struct mcxg_session* mcx_prepare_simulation(Config* cfg);
 /* Runs n validated configurations in one persistent launch: a GB300
    addition, no counterpart in the reference (one simulation per
    mcx_run_simulation call).  Each simulation gets ceil(nphoton /
-   photons_per_thread) reference threads (0: ceil(nphoton / 2^18) photons a
-   thread, clamped to 1..16) with seeds derived from its cfg.seed; flags: MCXG_GRAPH, MCXG_AGG.  Outputs go to each Config as
+   photons_per_thread) reference threads (0: 1 photon a thread up to 2^18
+   photons, 2 above) with seeds derived from its cfg.seed; flags: MCXG_GRAPH, MCXG_AGG.  Outputs go to each Config as
    mcx_run_simulation's do; an error is reported on cfgs[0].  Label volumes
    of at most 128 labels, one respin, no detectors, replay, extra sources,
    patterns or phase tables. */

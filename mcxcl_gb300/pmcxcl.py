@@ -370,7 +370,7 @@ def run_batch(cfgs, photons_per_thread=0, graph=False, aggregate=False, verify=F
     cfgs: a list of run() dictionaries (label volumes, no detectors).  Returns
     the list of their output dictionaries, as run() would give one by one.
     photons_per_thread sets how many photons each reference thread (RNG
-    stream) runs (0: ceil(nphoton / 2**18), clamped to 1..16); graph=True
+    stream) runs (0: 1 up to 2**18 photons, 2 above); graph=True
     captures the launch as a CUDA graph.  verify=True also accumulates every
     deposit in FP64 and adds to each output's 'stat' the compensated field's
     max and median relative error over its non-zero elements and the error
