@@ -1334,16 +1334,16 @@ static void run_simulation(Config* cfg) {
     if (cfg->autopilot) {
         /* the reference's NVIDIA compute >= 6 choice (mcx_host.cpp:617-620),
            which the exact kernel keeps.  The fast kernel's persistent grid
-           ends when its slowest reference thread does, so it takes up to 8
+           ends when its slowest reference thread does, so it takes up to 32
            times as many threads, down to 2 photons each: shorter threads
-           shorten the end of the launch (cube + sphere: +10 % at 1e8 photons
-           with 8 times the threads; at 1e7 photons, 2 photons a thread
-           instead of 16: +17 %) */
+           shorten the end of the launch (cube + sphere at 1e8 photons: +10 %
+           with 8 times the threads, +1.3 % more with 32; at 1e7 photons, 2
+           photons a thread instead of 16: +17 %) */
         autoblock = 64;
         autothread = autoblock * 64 * (size_t)g.sm;
         if (!cfg->exactmath && !(cfg->debuglevel & 1)) {
             const size_t per = (size_t)(cfg->nphoton / (cfg->respin > 0 ? cfg->respin : 1)) / 2;
-            const size_t cap = 8 * autothread;
+            const size_t cap = 32 * autothread;
             autothread = per > cap ? cap : (per > autothread ? per : autothread);
         }
     } else {

@@ -326,7 +326,7 @@ def run(cfg=None, **kwargs):
     scattering-site outputs use each photon's own entries.
 
     Random numbers: with the default ``autopilot`` the fast kernel runs
-    nphoton/2 threads (at least 64 x 64 x SM count, at most 8 times that),
+    nphoton/2 threads (at least 64 x 64 x SM count, at most 32 times that),
     where the reference runs 64 x 64 x SM count,
     so the same ``seed`` gives the same statistics but not the same photons
     as the reference.  Give ``autopilot=0`` with the reference's ``nthread``
