@@ -1137,12 +1137,13 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
                         kp.srcnum <= 1 && !s->maxjump;
     /* launch shape: block threads x blocks per SM.  Shapes of more than 512
        threads per SM take the instantiation whose registers are capped (64
-       a thread for the forward kernels: 1,024 resident threads, the
-       default; 80 for the specialised ones, which exist only capped: 768),
-       the others the uncapped one */
+       a thread: 1,024 resident threads, the default), the others the
+       uncapped one.  The specialised instantiations exist only capped: the
+       fluence-gradient passes at 64 registers, the others at 80 (768
+       threads) */
     const int block = s->block_req ? s->block_req : 256;
     const bool special = xmedia || rf || pol || svmc || verify || adjmode;
-    const int bpsm_sel = special ? 768 / block : (s->bpsm_req ? s->bpsm_req : 1024 / block);
+    const int bpsm_sel = special ? (adjmode ? 1024 : 768) / block : (s->bpsm_req ? s->bpsm_req : 1024 / block);
     const bool occ3 = special || block * bpsm_sel > 512;
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
                  (noagg ? 0 : mcxg::LF_WAGG) | (occ3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |

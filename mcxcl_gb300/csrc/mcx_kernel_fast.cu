@@ -42,49 +42,51 @@ static void* kshape(bool det, bool refl, bool wagg, bool o3) {
     return refl ? kfun<false, true, false, COMMON>(o3) : kfun<false, false, false, COMMON>(o3);
 }
 
-/* the RF (frequency-domain) transport: complex photon weights, 3 blocks/SM,
-   direct deposits */
+/* the RF (frequency-domain) transport: complex photon weights, 80-register
+   cap (3 blocks of 256 a SM; at 64 it ran 1 % slower), direct deposits */
 template <bool DET, bool REFL>
 static void* krf() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, false, true>;
 }
 
-/* the polarised transport: Stokes vectors and Mueller tables, 3 blocks/SM,
-   direct deposits */
+/* the polarised transport: Stokes vectors and Mueller tables, 80-register
+   cap, direct deposits */
 template <bool DET, bool REFL>
 static void* kpol() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, false, false, true>;
 }
 
-/* split-voxel volumes: 3 blocks/SM, direct deposits */
+/* split-voxel volumes: 80-register cap (3 blocks of 256 a SM: at 64 they
+   spill), direct deposits */
 template <bool DET, bool REFL>
 static void* ksvmc() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, false, false, false, true>;
 }
 
-/* volumes in the less common encodings: 3 blocks/SM, direct deposits */
+/* volumes in the less common encodings: 80-register cap, direct deposits */
 template <bool DET, bool REFL>
 static void* kxmedia() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, true>;
 }
 
 /* the common configuration with the FP64 / plain-float / spill accumulators
-   of the precision check: 3 blocks/SM, direct deposits */
+   of the precision check: 80-register cap, direct deposits */
 template <bool DET, bool REFL>
 static void* kacc64() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, true, false, false, false, true>;
 }
 
 /* the fluence-gradient passes: general media handling (labels or float mua),
-   no detectors, 3 blocks/SM */
+   no detectors, 64-register cap (4 blocks of 256 a SM: the two passes ran
+   5 % faster than at 80) */
 template <bool REFL>
 static void* kadj() {
-    return (void*)mcx_transport<false, false, REFL, false, false, 3, false, false, false, false, false, false, false,
+    return (void*)mcx_transport<false, false, REFL, false, false, 4, false, false, false, false, false, false, false,
                                 true>;
 }
 
 /* the common configuration with the hot-voxel tile in shared memory:
-   3 blocks/SM, direct deposits */
+   80-register cap, direct deposits */
 template <bool DET, bool REFL>
 static void* ktile() {
     return (void*)mcx_transport<false, DET, REFL, false, false, 3, false, false, true, false, false, false, false,
