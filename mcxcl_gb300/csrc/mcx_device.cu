@@ -1144,9 +1144,9 @@ int mcxg_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     const int block = s->block_req ? s->block_req : 256;
     const bool special = xmedia || rf || pol || svmc || verify || adjmode;
     const int bpsm_sel = special ? (adjmode ? 1024 : 768) / block : (s->bpsm_req ? s->bpsm_req : 1024 / block);
-    const bool occ3 = special || block * bpsm_sel > 512;
+    const bool capped = special || block * bpsm_sel > 512;
     int lflags = (kp.savedet ? mcxg::LF_DET : 0) | (kp.dorefl_compiled ? mcxg::LF_REFL : 0) |
-                 (noagg ? 0 : mcxg::LF_WAGG) | (occ3 ? mcxg::LF_OCC3 : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
+                 (noagg ? 0 : mcxg::LF_WAGG) | (capped ? mcxg::LF_CAPPED : 0) | (xmedia ? mcxg::LF_XMEDIA : 0) |
                  (common ? mcxg::LF_COMMON : 0) | (rf ? mcxg::LF_RF : 0) | (pol ? mcxg::LF_POL : 0) |
                  (svmc ? mcxg::LF_SVMC : 0) | (verify ? mcxg::LF_ACC64 : 0) | (adjmode ? mcxg::LF_ADJ : 0);
     if (verify) {
@@ -1859,7 +1859,7 @@ int mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {
     /* 4 blocks of 256 a SM on the 64-register instantiation; the precision
        check's instantiation is capped at 80 (3 blocks) */
     const int bpsm_req = verify ? 3 : (s->bpsm_req ? s->bpsm_req : 4);
-    int lflags = (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) | (bpsm_req >= 3 ? mcxg::LF_OCC3 : 0) |
+    int lflags = (refl ? mcxg::LF_REFL : 0) | (agg ? mcxg::LF_WAGG : 0) | (bpsm_req >= 3 ? mcxg::LF_CAPPED : 0) |
                  (common && !(flags & MCXG_GENERAL) ? mcxg::LF_COMMON : 0) | (verify ? mcxg::LF_ACC64 : 0);
     int block = s->block_req ? s->block_req : 256;
     int occ = 0;

@@ -1792,17 +1792,11 @@ void mcx_savedetphoton(float* ppath, void* seeds, int count, int doappend, Confi
 }
 
 /* Reference threads of one batch simulation: ceil(nphoton / ppt), and with
-   ppt 0 a photon count per thread of ceil(nphoton / 2^18) clamped to 1..16.
-   The automatic count gives every simulation at least twice as many threads
-   as a GB300 keeps resident (152 SMs x 3 x 256), so the resident threads work
-   on one or two simulations at a time and a warp's lanes read one
-   descriptor, and the cap of 16 photons keeps the last threads of a wave
-   short (as the single-simulation autopilot does). */
-/* reference threads of a batch simulation: ppt photons each, or by default
-   1 photon a thread up to 2^18 photons and 2 above (a thread of a simulation
-   keeps claiming that simulation's threads, so short ones end the waves with
-   a short tail: 2 photons a thread ran the 512-simulation batch in 7.32 s,
-   16 in 7.86 s) */
+   ppt 0 one photon a thread up to 2^18 photons and two above.  A simulation
+   of more than 2^18 photons then has at least 2^17 threads, so the resident
+   threads work on one or two simulations at a time and a warp's lanes read
+   one descriptor; short threads end each wave with a short tail (2 photons
+   a thread ran the 512-simulation batch in 7.32 s, up to 16 in 7.86 s). */
 static size_t batch_threads(size_t nphoton, unsigned int ppt) {
     if (!ppt) {
         size_t p = (nphoton + (1u << 18) - 1) >> 18;

@@ -24,17 +24,17 @@ cudaError_t batch_wave_upload(const mcxg_simdesc* d_descs, unsigned int n, cudaS
 /* COMMON: every simulation of the batch is 3-D (batches already take only
    label volumes and the Henyey-Greenstein phase function) */
 template <bool REFL, bool WAGG, bool COMMON>
-static void* kbatch(bool occ3) {
-    return occ3 ? (void*)mcx_transport<false, false, REFL, WAGG, false, 4, true, false, COMMON>
+static void* kbatch(bool capped) {
+    return capped ? (void*)mcx_transport<false, false, REFL, WAGG, false, 4, true, false, COMMON>
            : (void*)mcx_transport<false, false, REFL, WAGG, false, 2, true, false, COMMON>;
 }
 
 template <bool COMMON>
-static void* kshape(bool refl, bool wagg, bool o3) {
+static void* kshape(bool refl, bool wagg, bool cap) {
     if (wagg) {
-        return refl ? kbatch<true, true, COMMON>(o3) : kbatch<false, true, COMMON>(o3);
+        return refl ? kbatch<true, true, COMMON>(cap) : kbatch<false, true, COMMON>(cap);
     }
-    return refl ? kbatch<true, false, COMMON>(o3) : kbatch<false, false, COMMON>(o3);
+    return refl ? kbatch<true, false, COMMON>(cap) : kbatch<false, false, COMMON>(cap);
 }
 
 /* the precision check of a batch: every deposit also to the FP64, plain
@@ -45,12 +45,12 @@ static void* kbatch_acc64() {
 }
 
 static void* select(int flags) {
-    const bool refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    const bool refl = flags & LF_REFL, wagg = flags & LF_WAGG, cap = flags & LF_CAPPED;
     if (flags & LF_ACC64) {
         return (flags & LF_COMMON) ? (refl ? kbatch_acc64<true, true>() : kbatch_acc64<false, true>())
                                    : (refl ? kbatch_acc64<true, false>() : kbatch_acc64<false, false>());
     }
-    return (flags & LF_COMMON) ? kshape<true>(refl, wagg, o3) : kshape<false>(refl, wagg, o3);
+    return (flags & LF_COMMON) ? kshape<true>(refl, wagg, cap) : kshape<false>(refl, wagg, cap);
 }
 
 cudaError_t batch_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st) {

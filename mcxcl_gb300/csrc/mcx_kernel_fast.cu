@@ -29,17 +29,17 @@ static void* kfun(bool capped) {
 }
 
 template <bool COMMON>
-static void* kshape(bool det, bool refl, bool wagg, bool o3) {
+static void* kshape(bool det, bool refl, bool wagg, bool cap) {
     if (wagg) {
         if (det) {
-            return refl ? kfun<true, true, true, COMMON>(o3) : kfun<true, false, true, COMMON>(o3);
+            return refl ? kfun<true, true, true, COMMON>(cap) : kfun<true, false, true, COMMON>(cap);
         }
-        return refl ? kfun<false, true, true, COMMON>(o3) : kfun<false, false, true, COMMON>(o3);
+        return refl ? kfun<false, true, true, COMMON>(cap) : kfun<false, false, true, COMMON>(cap);
     }
     if (det) {
-        return refl ? kfun<true, true, false, COMMON>(o3) : kfun<true, false, false, COMMON>(o3);
+        return refl ? kfun<true, true, false, COMMON>(cap) : kfun<true, false, false, COMMON>(cap);
     }
-    return refl ? kfun<false, true, false, COMMON>(o3) : kfun<false, false, false, COMMON>(o3);
+    return refl ? kfun<false, true, false, COMMON>(cap) : kfun<false, false, false, COMMON>(cap);
 }
 
 /* the RF (frequency-domain) transport: complex photon weights, 80-register
@@ -94,7 +94,7 @@ static void* ktile() {
 }
 
 static void* select(int flags) {
-    const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, o3 = flags & LF_OCC3;
+    const bool det = flags & LF_DET, refl = flags & LF_REFL, wagg = flags & LF_WAGG, cap = flags & LF_CAPPED;
     if (flags & LF_TILE) {
         return det ? (refl ? ktile<true, true>() : ktile<true, false>())
                    : (refl ? ktile<false, true>() : ktile<false, false>());
@@ -120,7 +120,7 @@ static void* select(int flags) {
         return det ? (refl ? kxmedia<true, true>() : kxmedia<true, false>())
                    : (refl ? kxmedia<false, true>() : kxmedia<false, false>());
     }
-    return (flags & LF_COMMON) ? kshape<true>(det, refl, wagg, o3) : kshape<false>(det, refl, wagg, o3);
+    return (flags & LF_COMMON) ? kshape<true>(det, refl, wagg, cap) : kshape<false>(det, refl, wagg, cap);
 }
 
 cudaError_t fast_launch(const KArgs& a, int flags, int grid, int block, size_t smem, cudaStream_t st) {

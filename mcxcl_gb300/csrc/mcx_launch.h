@@ -86,7 +86,7 @@ struct KArgs {
 };
 
 /* flag bits for the launch entries */
-enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_OCC3 = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128, LF_POL = 256, LF_SVMC = 512,
+enum { LF_DET = 1, LF_REFL = 2, LF_WAGG = 4, LF_CAPPED = 8, LF_XMEDIA = 32, LF_COMMON = 64, LF_RF = 128, LF_POL = 256, LF_SVMC = 512,
        LF_ACC64 = 1024, LF_ADJ = 2048, LF_TILE = 4096 };
 
 /* fast instantiation: hardware transcendental approximations */
