@@ -265,6 +265,11 @@ void mcx_cleargpuinfo(GPUInfo** info);
    The calling thread's current CUDA device is the same on return as before
    (the run itself uses the device cfg selects). */
 void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy);
+/* Frees one output buffer that a caller took over from cfg (exportfield,
+   exportdetected, seeddata, ...: set the Config's pointer to NULL first so
+   mcx_clearcfg leaves it alone).  A GB300 addition: the Python module hands
+   the buffers to numpy arrays without copying them. */
+void mcx_free_buffer(void* p);
 /* Writes detected photons as <session>.mch: the History header, count records
    of his.colcount floats, then the seeds (src/mcx_utils.c:963-998). */
 void mcx_savedetphoton(float* ppath, void* seeds, int count, int doappend, Config* cfg);
@@ -396,13 +401,21 @@ int  mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread);
    generator, in nblock blocks of blocklen words ((nblock - 1) x blocklen <
    4 x nthread <= nblock x blocklen), block j starting from the 31 words
    starts[31 j ..] that mcx_rand_blocks returns. */
+int  mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock, uint32_t blocklen,
+                         uint32_t nthread);
+/* The same words with the jump-ahead also on the device: window holds the
+   generator's 31 unshifted outputs before the first word (what
+   mcx_rand_blocks returns for block 0); the device raises the one-step matrix
+   to the block length and its powers of two and starts each block of words
+   from its own window.  mcx_run_simulation seeds this way. */
+int  mcxg_set_seeds_window(mcxg_session* s, const uint32_t* window, uint32_t nthread);
+/* The session's 4 x nthread seed words, back to the host (out: 4 x nthread words). */
+int  mcxg_get_seeds(mcxg_session* s, uint32_t* out, uint32_t nthread);
 /* Trajectory capture (-D M): buffers for maxrec records (0: off); each
    launch restarts the count.  get copies min(count, maxrec, capacity)
    records and returns every record the launch made in *count. */
 int  mcxg_set_trajectory(mcxg_session* s, uint32_t maxrec);
 int  mcxg_get_trajectory(mcxg_session* s, float* out, uint32_t maxrec, uint32_t* count);
-int  mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock, uint32_t blocklen,
-                         uint32_t nthread);
 /* Launch shape of the persistent grid: block threads (32..256, a multiple of
    32) and resident blocks per SM (0 = automatic: 256 threads x 4).  Shapes of
    more than 512 threads per SM run the instantiation whose registers are

@@ -119,7 +119,8 @@ EXPORTS = [
     "mcxg_batch_simulate", "mcxg_batch_get_energy", "mcxg_batch_get_field", "mcx_savedetphoton",
     "mcxg_adjoint", "mcxg_get_verify", "mcx_readconfig", "mcx_parsejson", "mcxg_adjoint_field",
     "mcxg_get_field_planes", "mcxg_set_adjoint", "mcxg_get_adjoint_grad", "mcxg_batch_get_verify",
-    "mcx_run_batch_verify", "mcx_keep_sessions", "mcxg_set_tile", "mcxg_get_tile",
+    "mcx_run_batch_verify", "mcx_keep_sessions", "mcxg_set_tile", "mcxg_get_tile", "mcx_free_buffer",
+    "mcxg_set_seeds_window", "mcxg_get_seeds",
 ]
 
 _lib = None
@@ -146,6 +147,8 @@ def load():
     L.mcx_list_gpu.argtypes = [P(Config), P(ctypes.c_uint), P(P(GPUInfo))]
     L.mcx_list_gpu.restype = ctypes.c_int
     L.mcx_cleargpuinfo.argtypes = [P(P(GPUInfo))]
+    L.mcx_free_buffer.argtypes = [ctypes.c_void_p]
+    L.mcx_free_buffer.restype = None
     L.mcx_detreclen.argtypes = [P(Config)]
     L.mcx_detreclen.restype = ctypes.c_uint
     L.mcx_version.restype = ctypes.c_char_p
@@ -168,6 +171,8 @@ def load():
                                    ctypes.c_size_t]
     L.mcxg_set_params.argtypes = [vp, vp, ctypes.c_size_t]
     L.mcxg_set_seeds.argtypes = [vp, vp, ctypes.c_uint32]
+    L.mcxg_set_seeds_window.argtypes = [vp, vp, ctypes.c_uint32]
+    L.mcxg_get_seeds.argtypes = [vp, vp, ctypes.c_uint32]
     L.mcxg_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.mcxg_set_tile.argtypes = [vp, ctypes.c_uint32]
     L.mcxg_get_tile.argtypes = [vp, vp]

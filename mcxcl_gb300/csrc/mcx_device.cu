@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -654,6 +655,17 @@ int mcxg_device_info(int device, mcxg_devinfo* info) {
     if (!info) {
         return MCXG_ERR_ARG;
     }
+    /* cudaGetDeviceProperties takes about 9 ms on a GB300 and every
+       mcx_run_simulation lists the devices: the properties do not change
+       while the process runs, so each device is queried once */
+    static std::mutex lock;
+    static mcxg_devinfo cache[64];
+    static bool cached[64] = {};
+    std::lock_guard<std::mutex> guard(lock);
+    if (device >= 0 && device < 64 && cached[device]) {
+        *info = cache[device];
+        return MCXG_OK;
+    }
     cudaDeviceProp p;
     MCXG_TRY(cudaGetDeviceProperties(&p, device));
     memset(info, 0, sizeof(*info));
@@ -669,6 +681,10 @@ int mcxg_device_info(int device, mcxg_devinfo* info) {
     info->constmem = p.totalConstMem;
     info->regs_per_block = p.regsPerBlock;
     info->max_threads_per_sm = p.maxThreadsPerMultiProcessor;
+    if (device >= 0 && device < 64) {
+        cache[device] = *info;
+        cached[device] = true;
+    }
     return MCXG_OK;
 }
 
@@ -886,6 +902,18 @@ int mcxg_set_seeds(mcxg_session* s, const uint32_t* seeds, uint32_t nthread) {
    update, and r[(t + 28) % 31] holds o[k - 3] (this group's new value for
    t >= 3, the previous group's, not yet overwritten, for t < 3). */
 namespace {
+__device__ __forceinline__ void lfib_expand(uint32_t (&r)[31], size_t begin, size_t end, uint32_t* __restrict__ out) {
+    for (size_t base = begin; base < end; base += 31) {
+#pragma unroll
+        for (int t = 0; t < 31; t++) {
+            r[t] += r[(t + 28) % 31];
+            if (base + t < end) {
+                out[base + t] = r[t] >> 1;
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) lfib_words(const uint32_t* __restrict__ starts, uint32_t nblock,
                                                   uint32_t blocklen, uint32_t nword, uint32_t* __restrict__ out) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -898,16 +926,93 @@ __global__ void __launch_bounds__(128) lfib_words(const uint32_t* __restrict__ s
         r[t] = starts[31 * (size_t)j + t];
     }
     const size_t begin = (size_t)j * blocklen;
-    const size_t end = begin + blocklen < nword ? begin + blocklen : nword;
-    for (size_t base = begin; base < end; base += 31) {
+    lfib_expand(r, begin, begin + blocklen < nword ? begin + blocklen : nword, out);
+}
+
+/* The jump-ahead on the device.  One step of the generator is the window
+   map W' = M W (W = o[k-31 .. k-1]; W'[t] = W[t+1] for t < 30, W'[30] =
+   W[0] + W[28]), so block j's window is (M^B)^j W0.  lf_powers (one CTA, a
+   thread per matrix element, products mod 2^32 in shared memory) makes Q_0 =
+   M^B by square-and-multiply and Q_b = Q_{b-1}^2; lfib_jump_words then
+   applies Q_b to W0 for each set bit b of its block index and expands the
+   block as lfib_words does. */
+__device__ __forceinline__ void lf_mul_shared(const uint32_t* X, const uint32_t* Y, uint32_t* Z, int t) {
+    uint32_t acc = 0;
+    if (t < 31 * 31) {
+        const int i = t / 31, k = t - 31 * (t / 31);
 #pragma unroll
-        for (int t = 0; t < 31; t++) {
-            r[t] += r[(t + 28) % 31];
-            if (base + t < end) {
-                out[base + t] = r[t] >> 1;
+        for (int m = 0; m < 31; m++) {
+            acc += X[31 * i + m] * Y[31 * m + k];
+        }
+    }
+    __syncthreads();
+    if (t < 31 * 31) {
+        Z[t] = acc;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) lf_powers(uint32_t blocklen, uint32_t npow, uint32_t* __restrict__ pows) {
+    __shared__ uint32_t P[31 * 31], B[31 * 31];
+    const int t = threadIdx.x;
+    if (t < 31 * 31) {
+        const int i = t / 31, k = t - 31 * (t / 31);
+        P[t] = (i == k) ? 1u : 0u;
+        B[t] = (i < 30 && k == i + 1) || (i == 30 && (k == 0 || k == 28)) ? 1u : 0u;
+    }
+    __syncthreads();
+    for (uint32_t e = blocklen; e;) {
+        if (e & 1u) {
+            lf_mul_shared(P, B, P, t);
+        }
+        e >>= 1;
+        if (e) {
+            lf_mul_shared(B, B, B, t);
+        }
+    }
+    for (uint32_t b = 0; b < npow; b++) {
+        if (t < 31 * 31) {
+            pows[31 * 31 * (size_t)b + t] = P[t];
+        }
+        if (b + 1 < npow) {
+            lf_mul_shared(P, P, P, t);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) lfib_jump_words(const uint32_t* __restrict__ w0, const uint32_t* __restrict__ pows,
+                                                       uint32_t npow, uint32_t nblock, uint32_t blocklen, uint32_t nword,
+                                                       uint32_t* __restrict__ out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nblock) {
+        return;
+    }
+    uint32_t r[31];
+#pragma unroll
+    for (int t = 0; t < 31; t++) {
+        r[t] = w0[t];
+    }
+    for (uint32_t b = 0; b < npow; b++) {
+        if ((j >> b) & 1u) {
+            const uint32_t* Q = pows + 31 * 31 * (size_t)b;
+            uint32_t w[31];
+#pragma unroll
+            for (int i = 0; i < 31; i++) {
+                uint32_t acc = 0;
+#pragma unroll
+                for (int m = 0; m < 31; m++) {
+                    acc += __ldg(Q + 31 * i + m) * r[m];
+                }
+                w[i] = acc;
+            }
+#pragma unroll
+            for (int i = 0; i < 31; i++) {
+                r[i] = w[i];
             }
         }
     }
+    const size_t begin = (size_t)j * blocklen;
+    lfib_expand(r, begin, begin + blocklen < nword ? begin + blocklen : nword, out);
 }
 }  // namespace
 
@@ -935,6 +1040,52 @@ int mcxg_set_seeds_lfib(mcxg_session* s, const uint32_t* starts, uint32_t nblock
     MCXG_TRY(cudaGetLastError());
     MCXG_TRY(cudaStreamSynchronize(s->st));
     s->has_seeds = true;
+    return MCXG_OK;
+}
+
+int mcxg_set_seeds_window(mcxg_session* s, const uint32_t* window, uint32_t nthread) {
+    const uint64_t nword = 4ull * nthread;
+    if (!s || !window || nthread == 0 || nword > 0xFFFFFFFFull) {
+        return MCXG_ERR_ARG;
+    }
+    /* blocks of at least 1,024 words, at most 65,536 blocks: a 1e8-photon
+       launch's 80 M words in 65,536 blocks of 1,216 */
+    const uint32_t blocklen = (uint32_t)std::max<uint64_t>(1024, (nword + 65535) / 65536);
+    const uint32_t nblock = (uint32_t)((nword + blocklen - 1) / blocklen);
+    uint32_t npow = 0;
+    while (npow < 32 && ((uint64_t)1 << npow) < nblock) {
+        npow++;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    int rc = ensure(&s->d_seeds, &s->seeds_cap, nthread);
+    if (!rc) {
+        rc = ensure(&s->d_energy, &s->energy_cap, nthread);
+    }
+    if (!rc) {
+        rc = ensure(&s->d_lfib, &s->lfib_cap, 31 + 31 * 31 * (size_t)std::max<uint32_t>(npow, 1));
+    }
+    if (rc) {
+        return rc;
+    }
+    MCXG_TRY(cudaMemcpyAsync(s->d_lfib, window, sizeof(uint32_t) * 31, cudaMemcpyHostToDevice, s->st));
+    if (npow) {
+        lf_powers<<<1, 1024, 0, s->st>>>(blocklen, npow, s->d_lfib + 31);
+    }
+    lfib_jump_words<<<(nblock + 127) / 128, 128, 0, s->st>>>(s->d_lfib, s->d_lfib + 31, npow, nblock, blocklen,
+                                                              (uint32_t)nword, (uint32_t*)s->d_seeds);
+    MCXG_TRY(cudaGetLastError());
+    MCXG_TRY(cudaStreamSynchronize(s->st));
+    s->has_seeds = true;
+    return MCXG_OK;
+}
+
+int mcxg_get_seeds(mcxg_session* s, uint32_t* out, uint32_t nthread) {
+    if (!s || !out || !s->has_seeds || nthread > s->seeds_cap) {
+        return MCXG_ERR_ARG;
+    }
+    MCXG_TRY(cudaSetDevice(s->device));
+    MCXG_TRY(cudaMemcpyAsync(out, s->d_seeds, sizeof(uint4) * nthread, cudaMemcpyDeviceToHost, s->st));
+    MCXG_TRY(cudaStreamSynchronize(s->st));
     return MCXG_OK;
 }
 

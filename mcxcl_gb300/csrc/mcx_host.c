@@ -889,6 +889,10 @@ int mcx_list_gpu(Config* cfg, unsigned int* activedev, GPUInfo** info) {
     return (int)act;
 }
 
+void mcx_free_buffer(void* p) {
+    free(p);
+}
+
 void mcx_cleargpuinfo(GPUInfo** info) {
     if (info && *info) {
         free(*info);
@@ -1098,6 +1102,15 @@ static void addrand_set_window(AddRand* g, const uint32_t* W) {
     g->b = 28;
 }
 
+/* g moved on by nword words */
+static void addrand_skip(AddRand* g, uint64_t nword) {
+    uint32_t P[LF_N * LF_N], W[LF_N];
+    addrand_window(g, W);
+    lf_pow(nword, P);
+    lf_matvec(P, W, W);
+    addrand_set_window(g, W);
+}
+
 /* the windows at g's position + j x blocklen (j < nblock) into starts, and g
    moved on by nword words */
 static void addrand_blocks(AddRand* g, uint64_t nword, uint32_t nblock, uint32_t blocklen, uint32_t* starts) {
@@ -1110,10 +1123,7 @@ static void addrand_blocks(AddRand* g, uint64_t nword, uint32_t nblock, uint32_t
             lf_matvec(P, W, W);
         }
     }
-    addrand_window(g, W);
-    lf_pow(nword, P);
-    lf_matvec(P, W, W);
-    addrand_set_window(g, W);
+    addrand_skip(g, nword);
 }
 
 int mcx_rand_blocks(unsigned int seed, uint64_t skip, uint32_t nblock, uint32_t blocklen, uint32_t* starts) {
@@ -1121,13 +1131,9 @@ int mcx_rand_blocks(unsigned int seed, uint64_t skip, uint32_t nblock, uint32_t 
         return -1;
     }
     AddRand g;
-    uint32_t P[LF_N * LF_N], W[LF_N];
     addrand_seed(&g, seed);
     if (skip) {
-        addrand_window(&g, W);
-        lf_pow(skip, P);
-        lf_matvec(P, W, W);
-        addrand_set_window(&g, W);
+        addrand_skip(&g, skip);
     }
     addrand_blocks(&g, 0, nblock, blocklen, starts);
     return 0;
@@ -1304,9 +1310,6 @@ static void run_simulation(Config* cfg) {
         tmp[i] = NULL;
     }
 #define packed   (*(uint8_t**)&tmp[0])
-#define seeds    (*(uint32_t**)&tmp[1])
-#define detbuf   (*(float**)&tmp[2])
-#define seedbuf  (*(uint64_t**)&tmp[3])
 #define fieldtmp (*(float**)&tmp[4])
 #define blockscale (*(double**)&tmp[5])
     MCX_ENTER(cfg);
@@ -1439,14 +1442,6 @@ static void run_simulation(Config* cfg) {
        saved state, so its per-thread words are never drawn from */
     AddRand ar;
     addrand_seed(&ar, cfg->seed > 0 ? (unsigned int)cfg->seed : (replay ? 1u : (unsigned int)time(0)));
-    seeds = (uint32_t*)malloc(sizeof(uint32_t) * 31 * 4096);    /* the generator windows of <= 4096 blocks */
-    if (!seeds) {
-        MCX_ERROR(-2, "out of host memory");
-    }
-    if (cfg->issavedet) {
-        detbuf = (float*)malloc(sizeof(float) * (size_t)cfg->maxdetphoton * (hostdetreclen ? hostdetreclen : 1));
-        seedbuf = cfg->issaveseed ? (uint64_t*)malloc(sizeof(uint64_t) * 2 * (size_t)cfg->maxdetphoton) : NULL;
-    }
     cfg->detectedcount = 0;
     cfg->his.detected = 0;
     free(cfg->exportdebugdata);
@@ -1463,14 +1458,16 @@ static void run_simulation(Config* cfg) {
 
     float kms_total = 0.f;
     for (int iter = 0; iter < cfg->respin; iter++) {
-        /* the words are generated on the device from 31-word windows at block
-           starts (at most 4096 blocks: the host's jump-ahead costs 961
-           multiply-adds a block) */
+        /* the words are generated on the device from the generator's window
+           at this repetition's first word: the device jumps each block of
+           words ahead from it; the host moves on only for a next repetition */
         const uint64_t nword = 4ull * autothread;
-        const uint32_t blocklen = (uint32_t)((nword + 4095) / 4096 > 1024 ? (nword + 4095) / 4096 : 1024);
-        const uint32_t nblock = (uint32_t)((nword + blocklen - 1) / blocklen);
-        addrand_blocks(&ar, nword, nblock, blocklen, seeds);
-        device_check(mcxg_set_seeds_lfib(s, seeds, nblock, blocklen, (uint32_t)autothread), "generating seeds");
+        uint32_t window[LF_N];
+        addrand_window(&ar, window);
+        device_check(mcxg_set_seeds_window(s, window, (uint32_t)autothread), "generating seeds");
+        if (iter + 1 < cfg->respin) {
+            addrand_skip(&ar, nword);
+        }
         /* photon split in the reference's float arithmetic (mcx_host.cpp:1101-1102) */
         float tp = (float)cfg->nphoton * workload0 / (fullload * (float)autothread * (float)cfg->respin);
         kp.threadphoton = (uint32_t)(int)tp;
@@ -1557,8 +1554,10 @@ static void run_simulation(Config* cfg) {
         cfg->failedlaunch += stw[0];
 
         if (cfg->issavedet) {
+            /* the count first, then this repetition's records straight into the
+               grown export buffers */
             uint32_t detected = 0;
-            device_check(mcxg_get_detected(s, detbuf, seedbuf, &detected), "reading detected photons");
+            device_check(mcxg_get_detected(s, NULL, NULL, &detected), "reading the detected photon count");
             if (detected > cfg->maxdetphoton && cfg->flog) {
                 fprintf(cfg->flog, "WARNING: the detected photon number is more than what your have specified (%u > %u), "
                         "please use the -H option to specify a greater number\t", detected, cfg->maxdetphoton);
@@ -1572,8 +1571,17 @@ static void run_simulation(Config* cfg) {
                     MCX_ERROR(-2, "out of host memory");
                 }
                 cfg->exportdetected = nd;
-                memcpy(cfg->exportdetected + (size_t)cfg->detectedcount * hostdetreclen, detbuf,
-                       sizeof(float) * saved * hostdetreclen);
+                uint64_t* sd = NULL;
+                if (cfg->issaveseed) {
+                    void* ns = realloc(cfg->seeddata, sizeof(uint64_t) * 2 * ((size_t)cfg->detectedcount + saved));
+                    if (!ns) {
+                        MCX_ERROR(-2, "out of host memory");
+                    }
+                    cfg->seeddata = ns;
+                    sd = (uint64_t*)cfg->seeddata + (size_t)cfg->detectedcount * 2;
+                }
+                device_check(mcxg_get_detected(s, cfg->exportdetected + (size_t)cfg->detectedcount * hostdetreclen, sd,
+                                               &detected), "reading detected photons");
                 if (cfg->savedetweight) {
                     float* nw = (float*)realloc(cfg->exportdetweight, sizeof(float) * 2 * ((size_t)cfg->detectedcount + saved));
                     if (!nw) {
@@ -1582,14 +1590,6 @@ static void run_simulation(Config* cfg) {
                     cfg->exportdetweight = nw;
                     device_check(mcxg_get_detweight(s, cfg->exportdetweight + (size_t)cfg->detectedcount * 2),
                                  "reading detected weights");
-                }
-                if (cfg->issaveseed) {
-                    void* ns = realloc(cfg->seeddata, sizeof(uint64_t) * 2 * ((size_t)cfg->detectedcount + saved));
-                    if (!ns) {
-                        MCX_ERROR(-2, "out of host memory");
-                    }
-                    cfg->seeddata = ns;
-                    memcpy((uint64_t*)cfg->seeddata + (size_t)cfg->detectedcount * 2, seedbuf, sizeof(uint64_t) * 2 * saved);
                 }
                 cfg->detectedcount += saved;
             }
@@ -1757,9 +1757,6 @@ static void run_simulation(Config* cfg) {
         tmp[i] = NULL;
     }
 #undef packed
-#undef seeds
-#undef detbuf
-#undef seedbuf
 #undef fieldtmp
 #undef blockscale
     MCX_LEAVE();

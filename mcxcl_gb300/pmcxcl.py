@@ -11,6 +11,7 @@ Fortran-ordered (x fastest), ``flux`` is ``[Nx, Ny, Nz, gates]``, ``detp`` is
 ``[reclen, ndetected]`` and ``seeds`` is ``uint8 [16, ndetected]``.
 """
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -403,21 +404,32 @@ def run_batch(cfgs, photons_per_thread=0, graph=False, aggregate=False, verify=F
             L.mcx_clearcfg(ctypes.byref(C))
 
 
+def _take(C, name, ctype, n):
+    """A 1-D array of n ctype items over the library's output buffer C.<name>,
+    without a copy: the Config lets go of the buffer (mcx_clearcfg skips a
+    NULL pointer) and the array frees it with mcx_free_buffer when the last
+    view of it is collected."""
+    addr = ctypes.cast(getattr(C, name), ctypes.c_void_p).value
+    arr = np.ctypeslib.as_array(ctypes.cast(addr, ctypes.POINTER(ctype)), shape=(n,))
+    setattr(C, name, None)
+    weakref.finalize(arr, _lib.load().mcx_free_buffer, addr)
+    return arr
+
+
 def _outputs(cfg, C):
-    """Assemble the output dictionary (src/pmcxcl.cpp:1263-1521)."""
+    """Assemble the output dictionary (src/pmcxcl.cpp:1263-1521).  The field
+    and the detected-photon records are the library's buffers, taken over
+    without a copy."""
     L = _lib.load()
     out = {}
     reclen = L.mcx_detreclen(ctypes.byref(C))
     ndet = C.detectedcount
     if C.issaveseed != b"\0" and ndet:
-        seeds = np.ctypeslib.as_array(ctypes.cast(C.seeddata, ctypes.POINTER(ctypes.c_uint8)), shape=(ndet * 16,))
-        out["seeds"] = seeds.copy().reshape(ndet, 16).T
+        out["seeds"] = _take(C, "seeddata", ctypes.c_uint8, ndet * 16).reshape(ndet, 16).T
     if C.issavedet != b"\0" and ndet:
-        d = np.ctypeslib.as_array(C.exportdetected, shape=(ndet * reclen,))
-        out["detp"] = d.copy().reshape(ndet, reclen).T
+        out["detp"] = _take(C, "exportdetected", ctypes.c_float, ndet * reclen).reshape(ndet, reclen).T
         if C.savedetweight and C.exportdetweight:
-            w = np.ctypeslib.as_array(C.exportdetweight, shape=(ndet * 2,))
-            out["detweight"] = w.copy().reshape(ndet, 2).T
+            out["detweight"] = _take(C, "exportdetweight", ctypes.c_float, ndet * 2).reshape(ndet, 2).T
     if C.issave2pt != b"\0":
         gates = int((C.tend - C.tstart) / C.tstep + 0.5)
         nsrc = C.extrasrclen + 1 if (C.extrasrclen and C.srcid < 0) else 1
@@ -431,7 +443,7 @@ def _outputs(cfg, C):
         rfrep = replay and ord(C.outputtype) in (OUTPUTTYPES.index("rf") - 2, OUTPUTTYPES.index("rfmus") - 2)
         comps = 2 if (rffwd or rfrep) else 1
         n = C.dim.x * C.dim.y * C.dim.z * gates * nsrc * ndetblk * nshare
-        f = np.ctypeslib.as_array(C.exportfield, shape=(n * comps,)).copy()
+        f = _take(C, "exportfield", ctypes.c_float, n * comps)
         if rffwd:
             f = f[:n] + 1j * f[n:]
             f = f.astype(np.complex64)
