@@ -267,8 +267,11 @@ void mcx_cleargpuinfo(GPUInfo** info);
 void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy);
 /* Frees one output buffer that a caller took over from cfg (exportfield,
    exportdetected, seeddata, ...: set the Config's pointer to NULL first so
-   mcx_clearcfg leaves it alone).  A GB300 addition: the Python module hands
-   the buffers to numpy arrays without copying them. */
+   mcx_clearcfg leaves it alone).  Buffers of 1 MB and more are kept (up to 8
+   and 1 GB) for the next run's field and detected records, whose readbacks
+   then land in resident pages; mcx_release_sessions frees them.  A GB300
+   addition: the Python module hands the buffers to numpy arrays without
+   copying them. */
 void mcx_free_buffer(void* p);
 /* Writes detected photons as <session>.mch: the History header, count records
    of his.colcount floats, then the seeds (src/mcx_utils.c:963-998). */

@@ -3,14 +3,16 @@
 pmcxcl._take hands a buffer the library allocated (the field, the detected
 records, the seeds) to a numpy array: the Config's pointer becomes NULL, so
 mcx_clearcfg leaves the buffer alone, and the array frees it through
-mcx_free_buffer once its last view is gone.  Checked here on the label volume
+mcx_free_buffer once its last view is gone.  Checked on the label volume
 of a validated Config, a buffer of the same kind (malloc'd, freed by
-mcx_clearcfg), with no GPU.
+mcx_clearcfg), with no GPU; on the GPU, a run whose outputs reuse the
+buffers an earlier run gave back must hold only its own values.
 """
 import ctypes
 import gc
 
 import numpy as np
+import pytest
 
 
 def test_take_moves_ownership_and_frees_once(monkeypatch):
@@ -47,3 +49,27 @@ def test_take_moves_ownership_and_frees_once(monkeypatch):
     del view
     gc.collect()
     assert len(freed) == 1                            # freed once, by the array
+
+
+@pytest.mark.gpu
+def test_reused_output_buffers_hold_only_the_new_run():
+    """A run's field and records may land in buffers an earlier run's arrays
+    gave back (mcx_free_buffer keeps them): every element must be the new
+    run's.  The second run's source sits in the opposite corner of a strongly
+    absorbing cube, so the first run's hot voxels are nearly empty in it."""
+    import mcxcl_gb300
+    vol = np.ones((40, 40, 40), np.uint8)
+    base = {"nphoton": 200000, "vol": vol, "tstart": 0, "tend": 5e-9, "tstep": 5e-10, "srcdir": [0, 0, 1],
+            "prop": [[0, 0, 1, 1], [0.5, 2.0, 0.0, 1.0]], "issrcfrom0": 1, "seed": 7,
+            "detpos": [[2, 2, 0, 2], [37, 37, 39, 2]], "savedetflag": "dp"}
+    a = mcxcl_gb300.run(dict(base, srcpos=[2, 2, 0]))
+    hot = a["flux"][:4, :4, :4].copy()
+    na = a["detp"].shape[1]
+    del a
+    gc.collect()
+    b = mcxcl_gb300.run(dict(base, srcpos=[37, 37, 39], srcdir=[0, 0, -1]))
+    assert hot.sum() > 0
+    assert b["flux"][:4, :4, :4].sum() < 1e-3 * hot.sum()
+    assert np.isfinite(b["flux"]).all()
+    assert b["detp"].shape[1] > 0 and na > 0
+    assert (b["detp"][0] >= 1).all() and (b["detp"][0] <= 2).all()    # detector ids, not stale bytes
