@@ -896,6 +896,10 @@ int mcx_list_gpu(Config* cfg, unsigned int* activedev, GPUInfo** info) {
    new pages, 0.3 ms into resident ones).  Buffers of 1 MB and more, at most
    8 of them and 1 GB; released with the device sessions. */
 #define OUTCACHE_N 8
+/* 1: device sessions stay cached per GPU between calls (buffers, uploaded
+   volume and tuned launch shape are reused), and so do given-back output
+   buffers; 0: every call releases them */
+static int g_keep_sessions = 1;
 static pthread_mutex_t g_outcache_lock = PTHREAD_MUTEX_INITIALIZER;
 static void* g_outcache[OUTCACHE_N];
 static size_t g_outcache_size[OUTCACHE_N];
@@ -936,7 +940,7 @@ void mcx_free_buffer(void* p) {
         return;
     }
     const size_t n = malloc_usable_size(p);
-    if (n >= ((size_t)1 << 20)) {
+    if (g_keep_sessions && n >= ((size_t)1 << 20)) {
         pthread_mutex_lock(&g_outcache_lock);
         size_t held = 0;
         int slot = -1;
@@ -2073,9 +2077,6 @@ static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, uns
     MCX_LEAVE();
 }
 
-/* 1: device sessions stay cached per GPU between calls (buffers, uploaded
-   volume and tuned launch shape are reused); 0: every call releases them */
-static int g_keep_sessions = 1;
 
 void mcx_keep_sessions(int keep) {
     pthread_mutex_lock(&g_run_lock);
