@@ -983,9 +983,16 @@ __global__ void __launch_bounds__(1024) lf_powers(uint32_t blocklen, uint32_t np
 __global__ void __launch_bounds__(128) lfib_jump_words(const uint32_t* __restrict__ w0, const uint32_t* __restrict__ pows,
                                                        uint32_t npow, uint32_t nblock, uint32_t blocklen, uint32_t nword,
                                                        uint32_t* __restrict__ out) {
+    /* one 31-word group of each lane at a time, through a per-warp tile: the
+       warp then writes lane L's 31 consecutive words with 31 lanes (one
+       coalesced run) instead of 32 words 4 x blocklen bytes apart */
+    __shared__ uint32_t tile[4][32 * 33];
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nblock) {
-        return;
+    const unsigned int lane = threadIdx.x & 31u;
+    uint32_t* my = tile[threadIdx.x >> 5];
+    const uint32_t j0 = j - lane;             /* the warp's first block */
+    if (j0 >= nblock) {
+        return;                               /* the whole warp is past the last block */
     }
     uint32_t r[31];
 #pragma unroll
@@ -993,7 +1000,7 @@ __global__ void __launch_bounds__(128) lfib_jump_words(const uint32_t* __restric
         r[t] = w0[t];
     }
     for (uint32_t b = 0; b < npow; b++) {
-        if ((j >> b) & 1u) {
+        if (j < nblock && ((j >> b) & 1u)) {
             const uint32_t* Q = pows + 31 * 31 * (size_t)b;
             uint32_t w[31];
 #pragma unroll
@@ -1011,8 +1018,24 @@ __global__ void __launch_bounds__(128) lfib_jump_words(const uint32_t* __restric
             }
         }
     }
-    const size_t begin = (size_t)j * blocklen;
-    lfib_expand(r, begin, begin + blocklen < nword ? begin + blocklen : nword, out);
+    for (uint32_t off = 0; off < blocklen; off += 31) {
+#pragma unroll
+        for (int t = 0; t < 31; t++) {
+            r[t] += r[(t + 28) % 31];
+            my[lane * 33 + t] = r[t] >> 1;
+        }
+        __syncwarp();
+        /* lanes past the last block hold no words: their runs start at or past nword */
+        for (unsigned int L = 0; L < 32; L++) {
+            const size_t bL = (size_t)(j0 + L) * blocklen;
+            const size_t eL = bL + blocklen < nword ? bL + blocklen : nword;
+            const size_t k = bL + off + lane;
+            if (lane < 31 && k < eL) {
+                out[k] = my[L * 33 + lane];
+            }
+        }
+        __syncwarp();
+    }
 }
 }  // namespace
 
