@@ -301,6 +301,11 @@ void mcx_rand_words(unsigned int seed, uint32_t* out, size_t n);
    j < nblock, into starts (31 x nblock words): each block of words can then
    be generated on its own.  0 on success. */
 int mcx_rand_blocks(unsigned int seed, uint64_t skip, uint32_t nblock, uint32_t blocklen, uint32_t* starts);
+/* A label volume of nx x ny x nz bytes to the Config's uint32 words, x
+   fastest (out: nx ny nz words).  c_order = 1 when vol is laid out [x][y][z]
+   with z fastest (numpy's default order), 0 when x is already fastest.  A GB300
+   addition: the Python module's volume conversion for uint8 labels. */
+void mcx_labels_u8(const uint8_t* vol, uint32_t nx, uint32_t ny, uint32_t nz, int c_order, uint32_t* out);
 /* Everything mcx_run_simulation does before its first launch -- device
    selection, parameter block, volume packing, upload, seeds of the first
    repetition -- and nothing after: returns the ready device session so a

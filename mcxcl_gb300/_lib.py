@@ -120,7 +120,7 @@ EXPORTS = [
     "mcxg_adjoint", "mcxg_get_verify", "mcx_readconfig", "mcx_parsejson", "mcxg_adjoint_field",
     "mcxg_get_field_planes", "mcxg_set_adjoint", "mcxg_get_adjoint_grad", "mcxg_batch_get_verify",
     "mcx_run_batch_verify", "mcx_keep_sessions", "mcxg_set_tile", "mcxg_get_tile", "mcx_free_buffer",
-    "mcxg_set_seeds_window", "mcxg_get_seeds",
+    "mcxg_set_seeds_window", "mcxg_get_seeds", "mcx_labels_u8",
 ]
 
 _lib = None
@@ -154,6 +154,8 @@ def load():
     L.mcx_version.restype = ctypes.c_char_p
     L.mcx_rand_words.argtypes = [ctypes.c_uint, vp, ctypes.c_size_t]
     L.mcx_rand_blocks.argtypes = [ctypes.c_uint, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, vp]
+    L.mcx_labels_u8.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, vp]
+    L.mcx_labels_u8.restype = None
     L.mcx_prepare_simulation.argtypes = [P(Config)]
     L.mcx_keep_sessions.argtypes = [ctypes.c_int]
     L.mcx_keep_sessions.restype = None

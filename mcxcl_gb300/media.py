@@ -99,8 +99,16 @@ def encode(vol, unitinmm=1.0, alloc=None):
         raise ValueError("the 'vol' field must be a 2-D or 3-D array of labels or a 4-D array of properties")
     if vol.dtype.kind not in "uifb":
         raise TypeError("unsupported volume dtype %s" % vol.dtype)
-    # x fastest: one strided pass that transposes and widens
     words = alloc(vol.size) if alloc else np.empty(vol.size, np.uint32)
-    words.reshape(vol.shape[::-1])[...] = vol.T
+    if vol.dtype.itemsize == 1 and vol.dtype.kind in "ub" and (vol.flags.c_contiguous or vol.flags.f_contiguous) \
+            and vol.size:
+        # byte labels: the library's tiled transpose-and-widen, x fastest
+        from . import _lib
+        nx, ny, nz = (int(d) for d in vol.shape)
+        _lib.load().mcx_labels_u8(vol.ctypes.data, nx, ny, nz, 0 if vol.flags.f_contiguous else 1,
+                                  words.ctypes.data)
+    else:
+        # x fastest: one strided pass that transposes and widens
+        words.reshape(vol.shape[::-1])[...] = vol.T
     mb = {1: 1, 2: 2}.get(vol.dtype.itemsize, 4) if vol.dtype.kind in "uib" else 4
     return words, mb, vol.shape

@@ -309,3 +309,23 @@ def test_run_lock_released_on_error_paths(lib):
     t.start()
     t.join(60)
     assert not t.is_alive() and len(errors) == 2
+
+
+def test_label_bytes_to_words_x_fastest(lib):
+    """mcx_labels_u8 (the Python module's uint8 volume conversion) gives the
+    Config's x-fastest uint32 words from a C- or Fortran-ordered byte volume,
+    for shapes that are not multiples of its 32 x 32 tiles, and media.encode
+    agrees with numpy's own transpose-and-widen."""
+    from mcxcl_gb300 import media
+    rng = np.random.default_rng(11)
+    for shape in [(1, 1, 1), (33, 1, 65), (7, 40, 3), (64, 31, 33), (60, 60, 60)]:
+        vol = (rng.random(shape) * 255).astype(np.uint8)
+        want = np.empty(vol.size, np.uint32)
+        want.reshape(vol.shape[::-1])[...] = vol.T
+        for order, c in (("C", 1), ("F", 0)):
+            v = np.asarray(vol, order=order)
+            got = np.zeros(vol.size, np.uint32)
+            lib.mcx_labels_u8(v.ctypes.data, shape[0], shape[1], shape[2], c, got.ctypes.data)
+            assert np.array_equal(got, want), (shape, order)
+            w, mb, dims = media.encode(v)
+            assert np.array_equal(w, want) and mb == 1 and tuple(dims) == shape
