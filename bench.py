@@ -29,7 +29,8 @@ pass's agreement with central differences.
 
 Also: "c1" and "c3" -- the homogeneous cube and the synthetic layered head
 (181 x 217 x 181, five labels, 16 detectors, roulette), each with its own
-photons/ms, FP32-issue roofline and DRAM traffic; "precision" (with
+photons/ms, end-to-end photons/ms through mcxcl_gb300.run, FP32-issue
+roofline and DRAM traffic; "precision" (with
 --precision P) -- the error of the compensated field, a plain float field and
 the reference's spill field against an FP64 accumulation of the same P
 photons on the cube and the cube + sphere workloads.
@@ -435,8 +436,26 @@ def timed_launches(sess, steps, warmup, flush, flags=0):
     return kms
 
 
+def e2e_bytes(cfg, out):
+    """Host-device bytes of one run() call: the packed labels, property rows,
+    detector positions and the 31-word seed window in; the field, detected
+    records, seeds, energy sums and counters out."""
+    nvox = int(np.asarray(cfg["vol"]).size)
+    nprop = len(cfg["prop"])
+    ndetpos = len(cfg.get("detpos", []))
+    gates = out["flux"].shape[3]
+    ndet = out["detp"].shape[1] if "detp" in out else 0
+    reclen = out["detp"].shape[0] if "detp" in out else 0
+    nseed = out["seeds"].shape[1] if out.get("seeds") is not None else 0
+    h2d = nvox * 1 + 16 * nprop + 16 * ndetpos + 4 * 31
+    d2h = nvox * gates * 4 + ndet * reclen * 4 + nseed * 16 + 16 + 8 * 4 + 8 * 8
+    return h2d, d2h
+
+
 def config_measure(k, photons, steps, warmup, flush, peak):
-    """photons/ms, roofline and traffic of workload k (1 cube, 3 head) on resident data."""
+    """photons/ms, roofline and traffic of workload k (1 cube, 3 head) on
+    resident data, and end to end through mcxcl_gb300.run with host buffers."""
+    import mcxcl_gb300
     from mcxcl_gb300 import _lib, workloads
     import ctypes
     cfg = workloads.config(k)
@@ -450,8 +469,17 @@ def config_measure(k, photons, steps, warmup, flush, peak):
     ms = float(np.mean(kms))
     sample = 2000000 if k == 3 else 5000000
     per, ops, _ = event_model(cfg, sample)
+    mcxcl_gb300.run(dict(cfg))           # warm the path
+    n_e2e = 2
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        last = mcxcl_gb300.run(dict(cfg))
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / n_e2e
+    h2d, d2h = e2e_bytes(cfg, last)
     return {"workload": workloads.describe(k), "photons_per_step": int(photons), "steps": steps,
             "value": photons / ms, "unit": "photons/ms", "ms_per_step": ms, "launch": shape,
+            "e2e": {"value": photons / e2e_ms, "unit": "photons/ms", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": n_e2e},
             "roofline": roofline(per, ops, ms, photons, peak, k, sample)}
 
 
@@ -592,16 +620,7 @@ def main():
     torch.cuda.synchronize()
     e2e_wall = allmax(time.perf_counter() - t0, world)
     e2e_value = allsum(nphoton * e2e_steps, world) / (e2e_wall * 1e3)
-    nvox = 60 ** 3
-    gates = last["flux"].shape[3]
-    ndet = last["detp"].shape[1] if "detp" in last else 0
-    reclen = last["detp"].shape[0] if "detp" in last else 0
-    nseed = last["seeds"].shape[1] if last.get("seeds") is not None else 0
-    # the seed words are generated on the device from 31-word windows of <= 4096 blocks
-    nword = 4 * nthread
-    blocklen = max(-(-nword // 4096), 1024)
-    h2d = nvox * 1 + 16 * 3 + 16 * 4 + 4 * 31 * (-(-nword // blocklen))
-    d2h = nvox * gates * 4 + ndet * reclen * 4 + nseed * 16 + 16 + 8 * 4 + 8 * 8
+    h2d, d2h = e2e_bytes(cfg, last)
 
     out = None
     if rank == 0:

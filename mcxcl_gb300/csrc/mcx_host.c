@@ -243,13 +243,23 @@ static void prep_polarized(Config* cfg) {
     }
 }
 
-/* A voxel of the padded volume lies on an interface when any of its 26
-   neighbours is void (label 0); the padding layer is void. */
-static int touches_void(const uint32_t* pad, size_t i, size_t dx, size_t dxy) {
+/* The reference masks detectors on a copy of the volume padded by one void
+   voxel on every side (mcx_utils.c:4085-4198); the same lookups are made here
+   on the volume itself, at padded coordinates (1..n inside, 0 and n + 1 the
+   void padding), so no padded copy is built (the head volume: 29 MB). */
+static inline uint32_t pad_at(const uint32_t* vol, unsigned int nx, unsigned int ny, unsigned int nz, int x, int y, int z) {
+    if (x < 1 || y < 1 || z < 1 || x > (int)nx || y > (int)ny || z > (int)nz) {
+        return 0u;
+    }
+    return vol[((size_t)(z - 1) * ny + (size_t)(y - 1)) * nx + (size_t)(x - 1)];
+}
+
+/* a voxel lies on an interface when any of its 26 neighbours is void (label 0) */
+static int touches_void(const uint32_t* vol, unsigned int nx, unsigned int ny, unsigned int nz, int x, int y, int z) {
     for (int k = -1; k <= 1; k++) {
         for (int j = -1; j <= 1; j++) {
             for (int l = -1; l <= 1; l++) {
-                if ((k || j || l) && !pad[(ptrdiff_t)i + k * (ptrdiff_t)dxy + j * (ptrdiff_t)dx + l]) {
+                if ((k || j || l) && !pad_at(vol, nx, ny, nz, x + l, y + j, z + k)) {
                     return 1;
                 }
             }
@@ -258,23 +268,17 @@ static int touches_void(const uint32_t* pad, size_t i, size_t dx, size_t dxy) {
     return 0;
 }
 
+/* Two passes, so every test reads the volume as it was before masking (as
+   the reference's padded copy does): the voxels to mark first, then the
+   marks. */
 static void maskdet(Config* cfg) {
     unsigned int nx = cfg->dim.x, ny = cfg->dim.y, nz = cfg->dim.z;
-    unsigned int dx = nx + 2, dy = ny + 2, dz = nz + 2;
     int isonecube = (nx == 1) && (ny == 1) && (nz == 1);
     static const float corners[8][3] = {{0.f, 0.f, 0.f}, {1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f},
         {1.f, 1.f, 0.f}, {1.f, 0.f, 1.f}, {0.f, 1.f, 1.f}, {1.f, 1.f, 1.f}
     };
-    uint32_t* pad = (uint32_t*)calloc((size_t)dx * dy * dz, sizeof(uint32_t));
-    if (!pad) {
-        MCX_ERROR(-2, "out of host memory while masking detectors");
-    }
-    for (unsigned int zi = 1; zi <= nz; zi++) {
-        for (unsigned int yi = 1; yi <= ny; yi++) {
-            memcpy(pad + (size_t)zi * dy * dx + yi * dx + 1, cfg->vol + (size_t)(zi - 1) * ny * nx + (yi - 1) * nx,
-                   nx * sizeof(uint32_t));
-        }
-    }
+    size_t nmark = 0, capmark = 0;
+    size_t* mark = NULL;
     for (unsigned int d = 0; d < cfg->detnum; d++) {
         const mcx_float4 dp = cfg->detpos[d];
         float d2max = (dp.w + 1.7321f) * (dp.w + 1.7321f);
@@ -307,15 +311,26 @@ static void maskdet(Config* cfg) {
                             mind2 >= (dp.w + 0.5f * (1.f + isonecube)) * (dp.w + 0.5f * (1.f + isonecube))) {
                         continue;
                     }
-                    size_t i = ((size_t)(int)(iz + 1.f) * dy * dx + (size_t)(int)(iy + 1.f) * dx + (size_t)(int)(ix + 1.f));
+                    const int px = (int)(ix + 1.f), py = (int)(iy + 1.f), pz = (int)(iz + 1.f);
+                    const uint32_t v = pad_at(cfg->vol, nx, ny, nz, px, py, pz);
+                    int hit;
                     if (cfg->mediabyte == 97) {
                         /* split voxels: those with a background lower half (mcx_utils.c:4155-4165) */
-                        if (!(pad[i] & 0xFF000000u) && (pad[i] & 0x00FF0000u)) {
-                            cfg->vol[(int)iz * ny * nx + (int)iy * nx + (int)ix] |= DET_MASK;
-                            count++;
+                        hit = !(v & 0xFF000000u) && (v & 0x00FF0000u);
+                    } else {
+                        hit = v && touches_void(cfg->vol, nx, ny, nz, px, py, pz);
+                    }
+                    if (hit) {
+                        if (nmark == capmark) {
+                            capmark = capmark ? 2 * capmark : 4096;
+                            size_t* grown = (size_t*)realloc(mark, capmark * sizeof(size_t));
+                            if (!grown) {
+                                free(mark);
+                                MCX_ERROR(-2, "out of host memory while masking detectors");
+                            }
+                            mark = grown;
                         }
-                    } else if (pad[i] && touches_void(pad, i, dx, (size_t)dy * dx)) {
-                        cfg->vol[(int)iz * ny * nx + (int)iy * nx + (int)ix] |= DET_MASK;
+                        mark[nmark++] = (size_t)(int)iz * ny * nx + (size_t)(int)iy * nx + (size_t)(int)ix;
                         count++;
                     }
                 }
@@ -326,7 +341,10 @@ static void maskdet(Config* cfg) {
                     d + 1);
         }
     }
-    free(pad);
+    for (size_t i = 0; i < nmark; i++) {
+        cfg->vol[mark[i]] |= DET_MASK;
+    }
+    free(mark);
 }
 
 /* row-major (C) to column-major volume, mcx_convertrow2col */
