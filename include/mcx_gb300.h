@@ -349,6 +349,9 @@ void mcx_keep_sessions(int keep);
 
 /* ---- thin device layer ------------------------------------------------------ */
 
+/* mcxg_set_problem: 32-bit label words in, packed to bytes on the device */
+#define MCXG_MEDIA_PACK 0x101u
+
 #define MCXG_OK              0
 #define MCXG_ERR_CUDA        1
 #define MCXG_ERR_ARG         2
@@ -395,7 +398,9 @@ int  mcxg_destroy(mcxg_session* s);
  * Upload one problem.  kparams points to an mcxg_kparams (csrc/mcx_kparams.h),
  * passed opaquely with its size for ABI checking.  media holds nvox voxels of
  * mediaword bytes each (1: label | detector bit << 7; 4: the reference's
- * 32-bit word).  prop: medianum x 4 floats; detpos: detnum x 4; srcextra:
+ * 32-bit word), or with mediaword MCXG_MEDIA_PACK the reference's 32-bit
+ * words (label | detector bit 31, labels below 128, medianum <= 128), which
+ * the device packs to the one-byte form.  prop: medianum x 4 floats; detpos: detnum x 4; srcextra:
  * extrasrclen x 16; tables may be NULL when their length is 0.
  */
 int  mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, const void* media,

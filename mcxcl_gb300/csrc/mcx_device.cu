@@ -50,6 +50,8 @@ struct mcxg_session {
     size_t pattern_cap = 0;
     uint4* d_seeds = nullptr;
     size_t seeds_cap = 0;
+    uint32_t* d_words32 = nullptr;   /* 32-bit label words before packing (MCXG_MEDIA_PACK) */
+    size_t words32_cap = 0;
     unsigned int* d_jump = nullptr;  /* trajectory capture: record counter and records */
     float* d_traj = nullptr;
     size_t traj_cap = 0, jump_cap = 0;
@@ -752,7 +754,7 @@ int mcxg_destroy(mcxg_session* s) {
                     s->d_rseed, s->d_rweight, s->d_rtof, s->d_rdetid, s->d_scales, s->d_detw,
                     s->d_sims, s->d_simvt, s->d_simctr, s->d_smatrix, s->d_bmedia, s->d_bfield, s->d_benergy, s->d_bsum, s->d_bout,
                     s->d_adj, s->d_lfib, s->d_jump, s->d_traj, s->d_acc64, s->d_accf, s->d_accs, s->d_adjc,
-                    s->d_adjJ};
+                    s->d_adjJ, s->d_words32};
     if (s->bgraph_exec) {
         cudaGraphExecDestroy(s->bgraph_exec);
     }
@@ -777,6 +779,17 @@ int mcxg_destroy(mcxg_session* s) {
     return MCXG_OK;
 }
 
+namespace {
+/* 32-bit label words (label | detector bit 31) to the kernel's bytes (label |
+   detector bit 7), labels below 128 */
+__global__ void pack_labels(const uint32_t* __restrict__ words, size_t n, uint8_t* __restrict__ bytes) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t w = words[i];
+        bytes[i] = (uint8_t)((w & 0x7Fu) | ((w >> 24) & 0x80u));
+    }
+}
+}  // namespace
+
 int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, const void* media,
                      uint32_t mediaword, const float* prop, const float* detpos, const float* srcextra,
                      const float* invcdf, const float* angleinvcdf, const float* srcpattern, size_t npattern) {
@@ -784,6 +797,14 @@ int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, 
         return MCXG_ERR_ARG;
     }
     const mcxg_kparams& kp = *(const mcxg_kparams*)kparams;
+    /* MCXG_MEDIA_PACK: 32-bit words in, bytes on the device */
+    const bool pack = mediaword == MCXG_MEDIA_PACK;
+    if (pack) {
+        if (kp.mediaformat > 4 || kp.medianum > 128) {
+            return MCXG_ERR_ARG;
+        }
+        mediaword = 1;
+    }
     if (mediaword != 1 && mediaword != 4) {
         return MCXG_ERR_ARG;
     }
@@ -829,10 +850,19 @@ int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, 
             rc = ensure(&s->d_detw, &s->detw_cap, recs + 1);
         }
     }
+    if (!rc && pack) {
+        rc = ensure(&s->d_words32, &s->words32_cap, (size_t)kp.nvox);
+    }
     if (rc) {
         return rc;
     }
-    MCXG_TRY(cudaMemcpyAsync(s->d_media, media, mbytes, cudaMemcpyHostToDevice, s->st));
+    if (pack) {
+        MCXG_TRY(cudaMemcpyAsync(s->d_words32, media, sizeof(uint32_t) * (size_t)kp.nvox, cudaMemcpyHostToDevice, s->st));
+        pack_labels<<<grid_for(s, kp.nvox), 256, 0, s->st>>>(s->d_words32, kp.nvox, (uint8_t*)s->d_media);
+        MCXG_TRY(cudaGetLastError());
+    } else {
+        MCXG_TRY(cudaMemcpyAsync(s->d_media, media, mbytes, cudaMemcpyHostToDevice, s->st));
+    }
     MCXG_TRY(cudaMemcpyAsync(s->d_prop, prop, sizeof(float) * 4 * kp.medianum, cudaMemcpyHostToDevice, s->st));
     if (kp.nphase) {
         MCXG_TRY(cudaMemcpyAsync(s->d_tables, invcdf, sizeof(float) * kp.nphase, cudaMemcpyHostToDevice, s->st));

@@ -11,9 +11,9 @@
  * normalisation factors -- and calls CUDA only through the mcxg_* layer.
  *
  * What is new: a persistent device session cached per GPU (buffers are reused
- * across calls), the label volume packed to one byte per voxel when every
- * label fits in seven bits, and the FP64 energy sums and field normalisation
- * done on the GPU.
+ * across calls), the label volume packed on the device to one byte per voxel
+ * when every label fits in seven bits, and the FP64 energy sums and field
+ * normalisation done on the GPU.
  */
 #define _GNU_SOURCE
 #include <malloc.h>
@@ -1427,7 +1427,6 @@ static void run_simulation(Config* cfg) {
         free(tmp[i]);
         tmp[i] = NULL;
     }
-#define packed   (*(uint8_t**)&tmp[0])
 #define fieldtmp (*(float**)&tmp[4])
 #define blockscale (*(double**)&tmp[5])
     MCX_ENTER(cfg);
@@ -1519,36 +1518,20 @@ static void run_simulation(Config* cfg) {
     make_kparams(cfg, nvox, fieldlen, autothread, hostdetreclen, partialdata, is2d, replay, &kp);
 
     /* the label volume: one byte per voxel (label | detector bit << 7) when
-       every label fits in seven bits, else the reference's 32-bit words */
-    uint32_t mediaword = 4;
-    if (cfg->mediabyte <= 4) {
-        int fits = cfg->medianum <= 128;
-        if (fits) {
-            packed = (uint8_t*)malloc(nvox);
-            if (!packed) {
-                MCX_ERROR(-2, "out of host memory");
-            }
-            for (size_t i = 0; i < nvox; i++) {
-                uint32_t v = cfg->vol[i];
-                packed[i] = (uint8_t)((v & 0x7Fu) | ((v & DET_MASK) ? 0x80u : 0u));
-            }
-            mediaword = 1;
-        }
-    }
+       every label fits in seven bits -- the 32-bit words go up and the device
+       packs them -- else the reference's 32-bit words */
+    const uint32_t mediaword = (cfg->mediabyte <= 4 && cfg->medianum <= 128) ? MCXG_MEDIA_PACK : 4u;
 
     mcxg_session* s = session_for(device);
     if (!s) {
-        free(packed);
         MCX_ERROR(-99, "failed to open a CUDA session on the selected GPU");
     }
-    int rc = mcxg_set_problem(s, &kp, sizeof(kp), mediaword == 1 ? (const void*)packed : (const void*)cfg->vol, mediaword,
+    int rc = mcxg_set_problem(s, &kp, sizeof(kp), (const void*)cfg->vol, mediaword,
                               (const float*)cfg->prop, (const float*)cfg->detpos, (const float*)cfg->srcdata,
                               cfg->invcdf, cfg->angleinvcdf, cfg->srcpattern,
                               cfg->srctype == MCX_SRC_PATTERN ? (size_t)((int)(cfg->srcparam1.w * cfg->srcparam2.w) * cfg->srcnum)
                               : (cfg->srctype == MCX_SRC_PATTERN3D ?
                                  (size_t)((int)(cfg->srcparam1.x * cfg->srcparam1.y * cfg->srcparam1.z) * cfg->srcnum) : 0));
-    free(packed);
-    packed = NULL;
     device_check(rc, "uploading the problem");
     device_check(mcxg_set_replay(s, cfg->replay.seed, cfg->replay.weight, cfg->replay.tof, cfg->replay.detid,
                                  replay ? (uint32_t)cfg->nphoton : 0u), "uploading the replay inputs");
@@ -1876,7 +1859,6 @@ static void run_simulation(Config* cfg) {
         free(tmp[i]);
         tmp[i] = NULL;
     }
-#undef packed
 #undef fieldtmp
 #undef blockscale
     MCX_LEAVE();
