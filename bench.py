@@ -469,7 +469,10 @@ def config_measure(k, photons, steps, warmup, flush, peak):
     ms = float(np.mean(kms))
     sample = 2000000 if k == 3 else 5000000
     per, ops, _ = event_model(cfg, sample)
-    mcxcl_gb300.run(dict(cfg))           # warm the path
+    # warm the path: a loop that keeps each result while the next call runs
+    # reaches its steady state (output buffers reused) on its third call
+    for _ in range(2):
+        last = mcxcl_gb300.run(dict(cfg))
     n_e2e = 2
     t0 = time.perf_counter()
     for _ in range(n_e2e):
@@ -611,10 +614,14 @@ def main():
 
     # ---- end to end through the public API, host buffers in and out
     e2e_steps = args.e2e_steps or max(2, min(args.steps, 3))
-    mcxcl_gb300.run(dict(cfg))           # warm the path (session cache, page-ins)
+    # warm the path (session cache, page-ins): a loop that keeps each result
+    # while the next call runs reaches its steady state (output buffers
+    # reused) on its third call
+    last = None
+    for _ in range(2):
+        last = mcxcl_gb300.run(dict(cfg))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    last = None
     for _ in range(e2e_steps):
         last = mcxcl_gb300.run(dict(cfg))
     torch.cuda.synchronize()

@@ -462,6 +462,12 @@ int  mcxg_get_tile(mcxg_session* s, uint32_t* box);
    sources, patterns, phase tables, encodings other than labels. */
 int  mcxg_batch_set(mcxg_session* s, const void* sims, size_t desc_size, uint32_t nsim, const uint8_t* media,
                     uint64_t nmedia);
+/* The same with each simulation's volume as the Config's 32-bit label words
+   (words[i]: sims[i].kp.nvox of them, labels below 128): they are uploaded
+   to media_off of an nmedia-word staging buffer and packed to the label bytes
+   on the device (detector bits dropped: a batch saves no detected photons). */
+int  mcxg_batch_set_words(mcxg_session* s, const void* sims, size_t desc_size, uint32_t nsim,
+                          const uint32_t* const* words, uint64_t nmedia);
 /* Runs every simulation of the batch; MCXG_GRAPH replays a captured graph,
    MCXG_AGG aggregates deposits, MCXG_VERIFY also accumulates every deposit
    in FP64 (read with mcxg_batch_get_verify).  *kernel_ms covers the clear,

@@ -121,6 +121,7 @@ EXPORTS = [
     "mcxg_get_field_planes", "mcxg_set_adjoint", "mcxg_get_adjoint_grad", "mcxg_batch_get_verify",
     "mcx_run_batch_verify", "mcx_keep_sessions", "mcxg_set_tile", "mcxg_get_tile", "mcx_free_buffer",
     "mcxg_set_seeds_window", "mcxg_get_seeds", "mcx_labels_u8",
+    "mcxg_batch_set_words",
 ]
 
 _lib = None

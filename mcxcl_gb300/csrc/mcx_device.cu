@@ -781,11 +781,11 @@ int mcxg_destroy(mcxg_session* s) {
 
 namespace {
 /* 32-bit label words (label | detector bit 31) to the kernel's bytes (label |
-   detector bit 7), labels below 128 */
-__global__ void pack_labels(const uint32_t* __restrict__ words, size_t n, uint8_t* __restrict__ bytes) {
+   detector bit 7, the bits of keep), labels below 128 */
+__global__ void pack_labels(const uint32_t* __restrict__ words, size_t n, uint32_t keep, uint8_t* __restrict__ bytes) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const uint32_t w = words[i];
-        bytes[i] = (uint8_t)((w & 0x7Fu) | ((w >> 24) & 0x80u));
+        bytes[i] = (uint8_t)(((w & 0x7Fu) | ((w >> 24) & 0x80u)) & keep);
     }
 }
 }  // namespace
@@ -858,7 +858,7 @@ int mcxg_set_problem(mcxg_session* s, const void* kparams, size_t kparams_size, 
     }
     if (pack) {
         MCXG_TRY(cudaMemcpyAsync(s->d_words32, media, sizeof(uint32_t) * (size_t)kp.nvox, cudaMemcpyHostToDevice, s->st));
-        pack_labels<<<grid_for(s, kp.nvox), 256, 0, s->st>>>(s->d_words32, kp.nvox, (uint8_t*)s->d_media);
+        pack_labels<<<grid_for(s, kp.nvox), 256, 0, s->st>>>(s->d_words32, kp.nvox, 0xFFu, (uint8_t*)s->d_media);
         MCXG_TRY(cudaGetLastError());
     } else {
         MCXG_TRY(cudaMemcpyAsync(s->d_media, media, mbytes, cudaMemcpyHostToDevice, s->st));
@@ -1962,14 +1962,13 @@ int batch_enqueue(mcxg_session* s, int lflags) {
 
 }  // namespace
 
-int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_t nsim, const uint8_t* media,
-                   uint64_t nmedia) {
-    const mcxg_simdesc* sims = (const mcxg_simdesc*)sims_;
-    if (!s || !sims || desc_size != sizeof(mcxg_simdesc) || nsim == 0 || !media) {
-        return MCXG_ERR_ARG;
-    }
-    /* the simulations' reference threads must number 0.. contiguously, and
-       every offset must stay inside the buffers given */
+namespace {
+/* The checks and buffers of a batch (the simulations' reference threads must
+   number 0.. contiguously, and every offset must stay inside the buffers
+   given), then its upload: the volume as bytes, or as each simulation's
+   32-bit label words packed on the device. */
+int batch_upload(mcxg_session* s, const mcxg_simdesc* sims, uint32_t nsim, const uint8_t* media,
+                 const uint32_t* const* words, uint64_t nmedia) {
     std::vector<unsigned long long> simvt(nsim + 1);
     unsigned long long vt = 0, field = 0;
     for (uint32_t i = 0; i < nsim; i++) {
@@ -1977,7 +1976,8 @@ int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_
         if (d.vt_off != vt || d.kp.nthread == 0 || d.kp.mediaword != 1 || d.kp.savedet || d.kp.replay ||
                 d.kp.extrasrclen || d.kp.nphase || d.kp.nangle || d.kp.npattern || d.kp.mediaformat > 4 ||
                 d.kp.medianum > MCXG_BATCH_MAXMEDIA || d.media_off + d.kp.nvox > nmedia ||
-                (unsigned long long)d.kp.threadphoton * d.kp.nthread + (unsigned int)d.kp.oddphoton == 0) {
+                (unsigned long long)d.kp.threadphoton * d.kp.nthread + (unsigned int)d.kp.oddphoton == 0 ||
+                (words && !words[i])) {
             return MCXG_ERR_ARG;
         }
         simvt[i] = vt;
@@ -1999,6 +1999,9 @@ int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_
     if (!rc) {
         rc = ensure(&s->d_bmedia, &s->bmedia_cap, (size_t)nmedia);
     }
+    if (!rc && words) {
+        rc = ensure(&s->d_words32, &s->words32_cap, (size_t)nmedia);
+    }
     if (!rc) {
         rc = ensure(&s->d_bfield, &s->bfield_cap, kFieldPlanes * (size_t)field);
     }
@@ -2014,7 +2017,18 @@ int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_
     MCXG_TRY(cudaMemcpyAsync(s->d_sims, sims, sizeof(mcxg_simdesc) * nsim, cudaMemcpyHostToDevice, s->st));
     MCXG_TRY(cudaMemcpyAsync(s->d_simvt, simvt.data(), sizeof(unsigned long long) * (nsim + 1), cudaMemcpyHostToDevice,
                              s->st));
-    MCXG_TRY(cudaMemcpyAsync(s->d_bmedia, media, (size_t)nmedia, cudaMemcpyHostToDevice, s->st));
+    if (words) {
+        for (uint32_t i = 0; i < nsim; i++) {
+            MCXG_TRY(cudaMemcpyAsync(s->d_words32 + sims[i].media_off, words[i], sizeof(uint32_t) * (size_t)sims[i].kp.nvox,
+                                     cudaMemcpyHostToDevice, s->st));
+        }
+        /* a batch saves no detected photons: the label alone, as the byte upload takes it */
+        pack_labels<<<grid_for(s, (size_t)nmedia), 256, 0, s->st>>>(s->d_words32, (size_t)nmedia, 0x7Fu,
+                                                                     (uint8_t*)s->d_bmedia);
+        MCXG_TRY(cudaGetLastError());
+    } else {
+        MCXG_TRY(cudaMemcpyAsync(s->d_bmedia, media, (size_t)nmedia, cudaMemcpyHostToDevice, s->st));
+    }
     batch_recip<<<grid_for(s, (size_t)nsim * MCXG_BATCH_MAXMEDIA), 256, 0, s->st>>>(s->d_sims, nsim);
     MCXG_TRY(cudaStreamSynchronize(s->st));
     MCXG_TRY(cudaGetLastError());
@@ -2025,6 +2039,23 @@ int mcxg_batch_set(mcxg_session* s, const void* sims_, size_t desc_size, uint32_
     s->totalfield = field;
     s->has_batch = true;
     return batch_reset_graph(s);
+}
+}  // namespace
+
+int mcxg_batch_set(mcxg_session* s, const void* sims, size_t desc_size, uint32_t nsim, const uint8_t* media,
+                   uint64_t nmedia) {
+    if (!s || !sims || desc_size != sizeof(mcxg_simdesc) || nsim == 0 || !media) {
+        return MCXG_ERR_ARG;
+    }
+    return batch_upload(s, (const mcxg_simdesc*)sims, nsim, media, nullptr, nmedia);
+}
+
+int mcxg_batch_set_words(mcxg_session* s, const void* sims, size_t desc_size, uint32_t nsim,
+                         const uint32_t* const* words, uint64_t nmedia) {
+    if (!s || !sims || desc_size != sizeof(mcxg_simdesc) || nsim == 0 || !words) {
+        return MCXG_ERR_ARG;
+    }
+    return batch_upload(s, (const mcxg_simdesc*)sims, nsim, nullptr, words, nmedia);
 }
 
 int mcxg_batch_simulate(mcxg_session* s, unsigned int flags, float* kernel_ms) {

@@ -1922,7 +1922,7 @@ static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, uns
         btmp[i] = NULL;
     }
 #define bdesc  (*(mcxg_simdesc**)&btmp[0])
-#define bmedia (*(uint8_t**)&btmp[1])
+#define bwords (*(const uint32_t***)&btmp[1])
 #define bscale (*(double**)&btmp[2])
 #define bfield (*(float**)&btmp[3])
 #define bsums  (*(double**)&btmp[4])
@@ -1965,8 +1965,8 @@ static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, uns
     free(gpu);
 
     bdesc = (mcxg_simdesc*)calloc((size_t)n, sizeof(mcxg_simdesc));
-    bmedia = (uint8_t*)malloc(nmedia ? nmedia : 1);
-    if (!bdesc || !bmedia) {
+    bwords = (const uint32_t**)malloc(sizeof(uint32_t*) * (size_t)n);
+    if (!bdesc || !bwords) {
         MCX_ERROR(-2, "out of host memory");
     }
     uint64_t moff = 0, foff = 0, voff = 0;
@@ -1989,9 +1989,7 @@ static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, uns
         d->field_off = foff;
         d->vt_off = voff;
         d->seed = (uint64_t)(uint32_t)(cfg->seed > 0 ? cfg->seed : (int)time(0) + k) * 0x100000001B3ull;
-        for (size_t i = 0; i < nvox; i++) {
-            bmedia[moff + i] = (uint8_t)(cfg->vol[i] & 0x7Fu);
-        }
+        bwords[k] = cfg->vol;        /* packed to label bytes on the device */
         memcpy(d->prop, cfg->prop, sizeof(float) * 4 * cfg->medianum);
         moff += nvox;
         foff += fieldlen;
@@ -2003,7 +2001,7 @@ static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, uns
     if (!s) {
         MCX_ERROR(-99, "failed to open a CUDA session on the selected GPU");
     }
-    device_check(mcxg_batch_set(s, bdesc, sizeof(mcxg_simdesc), (uint32_t)n, bmedia, nmedia), "uploading the batch");
+    device_check(mcxg_batch_set_words(s, bdesc, sizeof(mcxg_simdesc), (uint32_t)n, bwords, nmedia), "uploading the batch");
     float kms = 0.f;
     device_check(mcxg_batch_simulate(s, flags | (relerr ? MCXG_VERIFY : 0u), &kms), "running the batch");
     /* the volume copy is resident now (every slot is freed on both exit paths) */
@@ -2100,7 +2098,7 @@ static void batch_run(Config** cfgs, int n, unsigned int photons_per_thread, uns
         btmp[i] = NULL;
     }
 #undef bdesc
-#undef bmedia
+#undef bwords
 #undef bscale
 #undef bfield
 #undef bsums
