@@ -268,8 +268,8 @@ void mcx_run_simulation(Config* cfg, float* fluence, float* totalenergy);
 /* Frees one output buffer that a caller took over from cfg (exportfield,
    exportdetected, seeddata, ...: set the Config's pointer to NULL first so
    mcx_clearcfg leaves it alone).  While sessions are kept (mcx_keep_sessions,
-   on by default), buffers of 1 MB and more are kept too (up to 8 and 1 GB,
-   the oldest given up first) for the next run's field and detected records, whose readbacks then land
+   on by default), buffers of 1 MB and more are kept too (up to 8 and 1 GB)
+   for the next run's field and detected records, whose readbacks then land
    in resident pages; mcx_release_sessions frees them.  A GB300
    addition: the Python module hands the buffers to numpy arrays without
    copying them. */

@@ -577,6 +577,15 @@ void l2_window(mcxg_session* s, const mcxg_kparams& kp, bool on) {
     if (base == s->l2_base && nb == s->l2_bytes) {
         return;
     }
+    if (!nb && s->l2_set) {
+        /* no window for this problem: the lines an earlier problem marked
+           persisting would keep their share of L2 from it, so they go back
+           to normal and the set-aside to what it was */
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, s->l2_prev);
+        cudaGetLastError();
+        s->l2_set = false;
+    }
     if (nb && !s->l2_set) {
         /* best effort: a context that refuses the set-aside runs without the window */
         if (cudaDeviceGetLimit(&s->l2_prev, cudaLimitPersistingL2CacheSize) != cudaSuccess ||

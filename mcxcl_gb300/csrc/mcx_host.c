@@ -911,9 +911,8 @@ int mcx_list_gpu(Config* cfg, unsigned int* activedev, GPUInfo** info) {
 /* Output buffers handed back with mcx_free_buffer, kept for the next run's
    field and detected records: their pages are resident, so the copies from
    the device skip the first-touch page faults (a 43 MB field: 1.7 ms into
-   new pages, 0.3 ms into resident ones; the head's 284 MB field: 24 ms and
-   1.5 ms).  Buffers of 1 MB and more, at most 8 of them and 1 GB, the oldest
-   given up first to make room; released with the device sessions. */
+   new pages, 0.3 ms into resident ones).  Buffers of 1 MB and more, at most
+   8 of them and 1 GB; released with the device sessions. */
 #define OUTCACHE_N 8
 /* 1: device sessions stay cached per GPU between calls (buffers, uploaded
    volume and tuned launch shape are reused), and so do given-back output
@@ -922,8 +921,6 @@ static int g_keep_sessions = 1;
 static pthread_mutex_t g_outcache_lock = PTHREAD_MUTEX_INITIALIZER;
 static void* g_outcache[OUTCACHE_N];
 static size_t g_outcache_size[OUTCACHE_N];
-static uint64_t g_outcache_age[OUTCACHE_N];    /* when each was given back */
-static uint64_t g_outcache_clock;
 
 /* n bytes for an output the run writes in full: the smallest cached buffer
    that holds n and wastes at most n + 1 MB, else a new one */
@@ -961,38 +958,22 @@ void mcx_free_buffer(void* p) {
         return;
     }
     const size_t n = malloc_usable_size(p);
-    const size_t limit = (size_t)1 << 30;
-    void* evicted[OUTCACHE_N];
-    int nevict = 0;
-    if (g_keep_sessions && n >= ((size_t)1 << 20) && n <= limit) {
+    if (g_keep_sessions && n >= ((size_t)1 << 20)) {
         pthread_mutex_lock(&g_outcache_lock);
-        for (;;) {
-            size_t held = 0;
-            int slot = -1, oldest = -1;
-            for (int i = 0; i < OUTCACHE_N; i++) {
-                held += g_outcache_size[i];
-                if (!g_outcache[i]) {
-                    slot = slot < 0 ? i : slot;
-                } else if (oldest < 0 || g_outcache_age[i] < g_outcache_age[oldest]) {
-                    oldest = i;
-                }
+        size_t held = 0;
+        int slot = -1;
+        for (int i = 0; i < OUTCACHE_N; i++) {
+            held += g_outcache_size[i];
+            if (!g_outcache[i] && slot < 0) {
+                slot = i;
             }
-            if (slot >= 0 && held + n <= limit) {
-                g_outcache[slot] = p;
-                g_outcache_size[slot] = n;
-                g_outcache_age[slot] = ++g_outcache_clock;
-                p = NULL;
-                break;
-            }
-            /* no room: give up the oldest buffer (there is one, since n <= limit) */
-            evicted[nevict++] = g_outcache[oldest];
-            g_outcache[oldest] = NULL;
-            g_outcache_size[oldest] = 0;
+        }
+        if (slot >= 0 && held + n <= ((size_t)1 << 30)) {
+            g_outcache[slot] = p;
+            g_outcache_size[slot] = n;
+            p = NULL;
         }
         pthread_mutex_unlock(&g_outcache_lock);
-    }
-    for (int i = 0; i < nevict; i++) {
-        free(evicted[i]);
     }
     free(p);
 }
