@@ -505,10 +505,22 @@ static void preprocess(Config* cfg) {
     }
     size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
     if (cfg->mediabyte <= 4) {
+        /* eight running maxima, so the compiler can keep them in one vector */
+        unsigned int m8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        size_t i = 0;
+        for (; i + 8 <= nvox; i += 8) {
+            for (int k = 0; k < 8; k++) {
+                const unsigned int l = cfg->vol[i + k] & MED_MASK;
+                m8[k] = l > m8[k] ? l : m8[k];
+            }
+        }
         unsigned int maxlabel = 0;
-        for (size_t i = 0; i < nvox; i++) {
-            unsigned int l = cfg->vol[i] & MED_MASK;
+        for (; i < nvox; i++) {
+            const unsigned int l = cfg->vol[i] & MED_MASK;
             maxlabel = l > maxlabel ? l : maxlabel;
+        }
+        for (int k = 0; k < 8; k++) {
+            maxlabel = m8[k] > maxlabel ? m8[k] : maxlabel;
         }
         if (cfg->medianum <= maxlabel) {
             MCX_ERROR(-4, "input media optical properties are less than the labels in the volume");

@@ -329,3 +329,26 @@ def test_label_bytes_to_words_x_fastest(lib):
             assert np.array_equal(got, want), (shape, order)
             w, mb, dims = media.encode(v)
             assert np.array_equal(w, want) and mb == 1 and tuple(dims) == shape
+
+
+def test_label_scan_finds_an_out_of_range_label_anywhere(lib):
+    """The label check scans eight voxels at a time plus a remainder: a label
+    past the property table is found in the first voxel, inside a group of
+    eight and in the remainder, and a volume of valid labels passes."""
+    from mcxcl_gb300 import _lib, pmcxcl
+    prop = [[0, 0, 1, 1], [0.1, 1, 0, 1], [0.2, 1, 0, 1]]
+    for n, bad in ((13, 0), (13, 5), (13, 12), (16, 15), (3, 2)):
+        vol = np.ones((n, 1, 1), np.uint8)
+        vol[bad, 0, 0] = 3
+        C = _lib.Config()
+        pmcxcl.parse_config({"nphoton": 10, "vol": vol, "prop": prop, "srcpos": [0, 0, 0], "srcdir": [1, 0, 0],
+                             "issrcfrom0": 1}, C)
+        lib.mcx_validatecfg(ctypes.byref(C), None, None, 0)
+        assert C.errorcode != 0 and b"less than the labels" in C.errormsg, (n, bad)
+        lib.mcx_clearcfg(ctypes.byref(C))
+    C = _lib.Config()
+    pmcxcl.parse_config({"nphoton": 10, "vol": np.full((13, 1, 1), 2, np.uint8), "prop": prop, "srcpos": [0, 0, 0],
+                         "srcdir": [1, 0, 0], "issrcfrom0": 1}, C)
+    lib.mcx_validatecfg(ctypes.byref(C), None, None, 0)
+    assert C.errorcode == 0, C.errormsg
+    lib.mcx_clearcfg(ctypes.byref(C))
