@@ -335,8 +335,8 @@ def run(cfg=None, **kwargs):
     one.
 
     Device memory: one session per GPU stays cached between calls (see
-    ``keep_sessions``).  Output arrays: ``flux``, ``detp``, ``seeds`` and
-    ``detweight`` are views of the library's own output buffers, handed over
+    ``keep_sessions``).  Output arrays: ``flux`` (a real field without saved
+    reflectance), ``detp``, ``seeds`` and ``detweight`` are views of the library's own output buffers, handed over
     without a copy (writable, ``base`` not None); a buffer goes back to the
     library when its last view is collected, and while sessions are kept the
     next call reads its outputs into it."""
