@@ -42,9 +42,11 @@ def float_to_half_bits(x):
     return (np.where(den, h_den, h_norm) & 0xFFFF).astype(np.uint16)
 
 
-def encode(vol, unitinmm=1.0, alloc=None):
+def encode(vol, unitinmm=1.0, alloc=None, native=True):
     """Returns (words uint32 [Nx*Ny*Nz], mediabyte, (Nx, Ny, Nz)).  alloc(n),
-    when given, supplies the uint32 array a label volume is written into."""
+    when given, supplies the uint32 array a label volume is written into.
+    native=False converts byte labels with numpy instead of the library's
+    tiled transpose (same words)."""
     vol = np.asarray(vol)
     u = np.float32(unitinmm)
     if vol.ndim == 4:
@@ -100,8 +102,8 @@ def encode(vol, unitinmm=1.0, alloc=None):
     if vol.dtype.kind not in "uifb":
         raise TypeError("unsupported volume dtype %s" % vol.dtype)
     words = alloc(vol.size) if alloc else np.empty(vol.size, np.uint32)
-    if vol.dtype.itemsize == 1 and vol.dtype.kind in "ub" and (vol.flags.c_contiguous or vol.flags.f_contiguous) \
-            and vol.size:
+    if native and vol.dtype.itemsize == 1 and vol.dtype.kind in "ub" and \
+            (vol.flags.c_contiguous or vol.flags.f_contiguous) and vol.size:
         # byte labels: the library's tiled transpose-and-widen, x fastest
         from . import _lib
         nx, ny, nz = (int(d) for d in vol.shape)

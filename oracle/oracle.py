@@ -166,12 +166,12 @@ def make_input(cfg, nthread=4096, core=None, mathmode=MATH_LIBM, variant=VARIANT
     keep = {}
     inp = MCXOInput()
     # the pmcxcl volume encoding (src/pmcxcl.cpp:93-426): the oracle decodes the
-    # same words the kernel gets
+    # same words the kernel gets, converted by numpy alone (no product code)
     import sys
     if os.path.dirname(HERE) not in sys.path:
         sys.path.insert(0, os.path.dirname(HERE))
     from mcxcl_gb300 import media
-    words, inp.mediabyte, dims = media.encode(cfg["vol"], float(cfg.get("unitinmm", 1.0)))
+    words, inp.mediabyte, dims = media.encode(cfg["vol"], float(cfg.get("unitinmm", 1.0)), native=False)
     words = np.ascontiguousarray(words)
     keep["vol"] = words
     inp.dimx, inp.dimy, inp.dimz = [int(d) for d in dims]
